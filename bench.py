@@ -1,0 +1,342 @@
+"""Benchmark: BVH ray casting (Accel::Intersect) on the synthetic ray-cast scene.
+
+Workload (one "step"): closest-hit queries of 16,777,216 rays (origins uniform
+in [-0.1,1.1]^3, directions uniform on the sphere, tmin 1e-4) against
+1,524,288 triangles (1,000,000 seeded random triangles with lognormal edge
+lengths in the unit cube plus a 512x512-quad sinusoid heightfield), on a BVH
+built once on the GPU.  Metric: Mrays/s.
+
+  value  rays already resident in HBM, K back-to-back traversal launches timed
+         with CUDA events on the launching stream;
+  e2e    the same query through the host-pointer C-ABI call (lmgpu_trace) with
+         pinned host buffers: host->device rays, traversal, device->host hits
+         inside the timed region.
+
+`--impl reference` times the CPU oracle of the reference's accel on the host
+cores (the reference's own sources when their x86-64 harness exists here,
+else the C restatement of accel::bvh_sahbin) on a bounded sample of the rays.
+
+Under torchrun each rank traces its own 16.8M rays against a replicated BVH
+(weak scaling); rank 0 prints the JSON line with the max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "lightmetrica-v2_gb300"))
+
+METRIC = "Mrays/s (BVH)"
+UNIT = "Mrays/s"
+N_RANDOM, HF_RES, N_RAYS = 1_000_000, 512, 1 << 24
+NODE_BYTES, TRI_BYTES, RAY_BYTES, HIT_BYTES = 80, 48, 32, 16
+
+
+def workload_config(extra: dict | None = None) -> dict:
+    c = {"workload": "bvh_raycast_closest_hit", "triangles": N_RANDOM + 2 * HF_RES * HF_RES, "rays_per_step": N_RAYS,
+         "scene": "1M random tris (lognormal edges, mu=ln 0.005, sigma=0.5) + 512x512 heightfield, seed 0x5EED",
+         "tmin": 1e-4, "query": "closest-hit", "l2": "inputs larger than L2 (512 MiB of rays per step), no flush"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        time.sleep(0.2)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peak() -> tuple[float, str]:
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, burst)"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch() -> float | None:
+    """DRAM bytes per full launch from the committed ncu summary, if any."""
+    p = os.path.join(REPO, "profiles", "trace_closest_traffic.json")
+    if os.path.exists(p):
+        try:
+            return float(json.load(open(p))["dram_bytes_per_full_launch"])
+        except Exception:
+            return None
+    return None
+
+
+class CpuReference:
+    """The CPU oracle of the reference's accel on the host cores.
+
+    kind "port": the C restatement of accel::bvh_sahbin (oracle/), the only
+    form that runs on an aarch64 host; kind "reference": the reference's own
+    accel::qbvh compiled from its sources by oracle/build_ref.sh (x86-64
+    only), used when --use-ref-binary is given and the binary exists.
+    """
+
+    def __init__(self, tris: np.ndarray, threads: int, use_ref_binary: bool = False):
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import lmoracle
+
+        self.lo = lmoracle
+        self.tris = tris
+        self.threads = threads
+        self.kind = "port"
+        if use_ref_binary and os.path.exists(lmoracle.REF_ACCEL) and os.access(lmoracle.REF_ACCEL, os.X_OK):
+            self.kind = "reference"
+            self.acc = None
+        else:
+            self.acc = lmoracle.OracleAccel(lmoracle.BVH_SAHBIN, tris)
+
+    def time_sample(self, rays: np.ndarray, budget_s: float) -> dict:
+        """Traces a prefix of `rays` sized to about budget_s seconds."""
+        if self.kind == "reference":
+            n = min(len(rays), 1 << 18)
+            with tempfile.TemporaryDirectory() as tmp:
+                ps, pr, po = (os.path.join(tmp, x) for x in ("s.bin", "r.bin", "o.bin"))
+                self.lo.write_ref_inputs(ps, pr, [self.tris], rays[:n])
+                out = subprocess.run([self.lo.REF_ACCEL, "accel::qbvh", ps, pr, po, str(self.threads)],
+                                     capture_output=True, text=True, check=True).stdout
+            rec = json.loads(out.strip().splitlines()[-1])
+            return {"rays_per_s": n / rec["trace_s"], "n": n, "s": rec["trace_s"],
+                    "sample": f"{n} rays of the step, reference accel::qbvh compiled from its sources, "
+                              f"{self.threads} threads, build excluded"}
+        n = min(len(rays), 1 << 13)
+        t0 = time.perf_counter()
+        self.acc.trace(rays[:n], threads=self.threads)
+        est = n / max(time.perf_counter() - t0, 1e-9)
+        m = int(min(len(rays), max(n, est * budget_s)))
+        t0 = time.perf_counter()
+        self.acc.trace(rays[:m], threads=self.threads)
+        dt = time.perf_counter() - t0
+        return {"rays_per_s": m / dt, "n": m, "s": dt,
+                "sample": f"{m} rays of the step, oracle restatement of accel::bvh_sahbin "
+                          f"(accel_bvh_sahbin.cpp), {self.threads} threads, {dt:.1f} s, build excluded"}
+
+
+def run_reference(args) -> None:
+    ws, rank, _ = dist_env()
+    if ws > 1 and rank != 0:
+        return
+    from lmgpu import scenes
+
+    tris = scenes.raycast_scene(N_RANDOM, HF_RES)
+    rays = scenes.raycast_rays(N_RAYS)
+    threads = os.cpu_count() or 1
+    ref = CpuReference(tris, threads, use_ref_binary=args.use_ref_binary)
+    budget = max(0.5, 60.0 / max(1, args.steps + args.warmup))
+    vals = []
+    res = None
+    for k in range(args.warmup + args.steps):
+        off = (k * 1_000_003) % (N_RAYS // 2)
+        res = ref.time_sample(rays[off:], budget)
+        if k >= args.warmup:
+            vals.append(res["rays_per_s"] / 1e6)
+    v = statistics.median(vals)
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": N_RAYS / (v * 1e6) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": workload_config(), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": ref.kind,
+                             "sample": "per step: " + res["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args) -> None:
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import lmgpu
+    from lmgpu import scenes
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    tris = scenes.raycast_scene(N_RANDOM, HF_RES)
+    rays = scenes.raycast_rays(N_RAYS, stream=3 + rank)
+    stream = torch.cuda.Stream()
+    s = stream.cuda_stream
+    acc = lmgpu.Accel()
+    with torch.cuda.stream(stream):
+        d_tris = torch.from_numpy(tris).cuda()
+        acc.build_device(d_tris.data_ptr(), tris.shape[0], s)
+        d_rays = torch.from_numpy(rays).cuda()
+        d_hits = torch.empty((N_RAYS, 4), dtype=torch.float32, device="cuda")
+    info = acc.info()
+
+    # fetch counts of the same query (instrumented kernel, outside the timed region)
+    st = acc.trace_stats_device(d_rays.data_ptr(), d_hits.data_ptr(), N_RAYS, False, s)
+    bytes_per_ray = RAY_BYTES + HIT_BYTES + (st["node_fetches"] * NODE_BYTES + st["triangle_fetches"] * TRI_BYTES) / N_RAYS
+
+    for _ in range(args.warmup):
+        acc.trace_device(d_rays.data_ptr(), d_hits.data_ptr(), N_RAYS, False, s)
+    acc.check(s)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        acc.trace_device(d_rays.data_ptr(), d_hits.data_ptr(), N_RAYS, False, s)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    acc.check(s)
+    ms = ev0.elapsed_time(ev1)
+
+    # e2e: host buffers through the C ABI, copies inside the timed region
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_hits = torch.empty((N_RAYS, 4), dtype=torch.float32).pin_memory()
+    e2e_steps = max(3, min(args.steps, 20))
+    for _ in range(2):
+        acc.trace_ptr(h_rays.data_ptr(), h_hits.data_ptr(), N_RAYS)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        acc.trace_ptr(h_rays.data_ptr(), h_hits.data_ptr(), N_RAYS)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    barrier()
+
+    if ws > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms, e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, e2e_s = float(t[0]), float(t[1])
+
+    if rank == 0:
+        per_launch_s = ms / 1e3 / args.steps
+        value = ws * N_RAYS / per_launch_s / 1e6
+        e2e_value = ws * N_RAYS * e2e_steps / e2e_s / 1e6
+        peak, peak_src = measured_peak()
+        achieved = N_RAYS * bytes_per_ray / per_launch_s / 1e9
+        traffic = traffic_per_launch()
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": workload_config({"parallelism": f"replicated BVH, rays sharded x{ws}" if ws > 1 else "1 GPU"}),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N_RAYS * RAY_BYTES,
+                        "d2h_bytes_per_step": N_RAYS * HIT_BYTES, "steps": e2e_steps,
+                        "api": "lmgpu_trace (host pointers, pinned)"},
+                "gpu_launches": args.steps,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                             "kernel": "k_trace<closest>",
+                             "bytes_per_ray": bytes_per_ray,
+                             "nodes_per_ray": st["node_fetches"] / N_RAYS,
+                             "tris_per_ray": st["triangle_fetches"] / N_RAYS,
+                             "note": "algorithmic bytes = 32 B ray + 16 B hit + 80 B per node fetch + 48 B per "
+                                     "triangle test; node/triangle fetches are mostly L2 hits"},
+                "clocks": clk,
+                "accel": {"build_ms": info["build_ms"], "wide_nodes": info["num_wide_nodes"],
+                          "binary_depth": info["binary_depth"], "wide_depth": info["wide_depth"],
+                          "hit_fraction": st["hits"] / N_RAYS}}
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            cb = CpuReference(tris, threads).time_sample(rays, 15.0)
+            line["cpu_baseline"] = {"value": cb["rays_per_s"] / 1e6, "unit": UNIT, "cores": threads,
+                                    "kind": "port", "sample": cb["sample"]}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--use-ref-binary", action="store_true",
+                    help="reference arm: time the reference's own qbvh (x86-64 harness) if built")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,120 @@
+/*
+ * lmgpu: C ABI of the GB300 (sm_103a) ray-intersection and path-sampling
+ * library.  Plain C types only; every entry point returns an int status
+ * (LMGPU_OK == 0) and never throws.  On failure lmgpu_last_error() returns a
+ * message for the calling thread.
+ *
+ * Each entry point names the reference interface it stands in for
+ * (Lightmetrica v2, file:line within that project).
+ *
+ * Buffer conventions
+ *   triangles : float[ntri * 9], vertices p1, p2, p3 of each triangle after the
+ *               primitive transform, in global triangle order (primitives in
+ *               scene order, faces in mesh order: accel_naive.cpp:62-87).
+ *   rays      : float[n * 8] = (ox, oy, oz, tmin, dx, dy, dz, tmax).
+ *   hits      : lmgpu_hit[n]; prim == -1 (0xFFFFFFFF) means no hit in
+ *               [tmin, tmax].  b1, b2 weight vertices p2 and p3, the (u, v)
+ *               IntersectionUtils::CreateTriangleIntersection takes
+ *               (intersectionutils.h:59, :115-124).
+ *   "_device" entry points take device pointers and a cudaStream_t passed
+ *   as void* (NULL = legacy default stream); the others take host pointers
+ *   and include the host<->device copies.
+ */
+#ifndef LMGPU_H
+#define LMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LMGPU_OK 0
+#define LMGPU_ERR_INVALID 1     /* bad argument */
+#define LMGPU_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define LMGPU_ERR_NOT_BUILT 3   /* accel used before a successful build */
+#define LMGPU_ERR_OVERFLOW 4    /* a device-side bound (traversal stack) was exceeded */
+#define LMGPU_ERR_NO_DEVICE 5   /* no CUDA device visible */
+
+typedef struct {
+    float t;
+    int32_t prim;   /* global triangle id, -1 = miss */
+    float b1, b2;
+} lmgpu_hit;
+
+typedef struct lmgpu_accel lmgpu_accel;
+
+/* Properties of a built accel. */
+typedef struct {
+    uint64_t num_triangles;
+    uint64_t num_binary_nodes;  /* nodes of the binned-SAH binary tree */
+    uint64_t num_wide_nodes;    /* 8-wide compressed nodes (80 bytes each) */
+    uint64_t node_bytes;
+    uint64_t triangle_bytes;
+    int32_t binary_depth;
+    int32_t wide_depth;
+    double build_ms;            /* device time of the last build */
+} lmgpu_accel_info;
+
+/* Traversal counters of one instrumented launch (sums over all rays). */
+typedef struct {
+    uint64_t rays;
+    uint64_t node_fetches;      /* wide nodes loaded (80 bytes each) */
+    uint64_t triangle_fetches;  /* triangles tested (48 bytes each) */
+    uint64_t hits;
+} lmgpu_trace_stats;
+
+/* Version string of the library. */
+const char* lmgpu_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* lmgpu_last_error(void);
+
+/* Creates an empty accel on the current device.
+ * Stands in for Accel::Initialize (include/lightmetrica/accel.h:67);
+ * the reference accels take no parameters (accel_naive.cpp:53-57). */
+int lmgpu_accel_create(lmgpu_accel** out);
+
+/* Frees an accel and its device buffers (accel_embree.cpp:68-78 frees its
+ * device scene in the destructor the same way).  NULL is ignored. */
+void lmgpu_accel_destroy(lmgpu_accel* accel);
+
+/* Builds a binned-SAH BVH on the GPU and collapses it into 8-wide
+ * compressed nodes.  Host triangle buffer.
+ * Stands in for Accel::Build (include/lightmetrica/accel.h:79). */
+int lmgpu_accel_build(lmgpu_accel* accel, const float* triangles, uint64_t ntri);
+
+/* As lmgpu_accel_build, with the triangle buffer already on the device. */
+int lmgpu_accel_build_device(lmgpu_accel* accel, const float* d_triangles, uint64_t ntri, void* stream);
+
+/* Fills *info for a built accel. */
+int lmgpu_accel_get_info(const lmgpu_accel* accel, lmgpu_accel_info* info);
+
+/* Closest hit (anyhit = 0) or any hit (anyhit = 1) for n rays, host buffers,
+ * copies included.  Closest hit stands in for Accel3::Intersect
+ * (include/lightmetrica/accel3.h:68); any hit for Scene3::Visible
+ * (include/lightmetrica/scene3.h:107-116), which the reference answers with a
+ * full closest-hit query.  Ties at equal t resolve to the higher global
+ * triangle id, the order accel::naive keeps (accel_naive.cpp:99-110). */
+int lmgpu_trace(const lmgpu_accel* accel, const float* rays, lmgpu_hit* hits, uint64_t n, int anyhit);
+
+/* As lmgpu_trace on device buffers (rays 16-byte aligned), asynchronous on
+ * `stream`; the status of device-side bounds is checked by the next
+ * lmgpu_accel_check or synchronous call. */
+int lmgpu_trace_device(const lmgpu_accel* accel, const float* d_rays, lmgpu_hit* d_hits, uint64_t n,
+                       int anyhit, void* stream);
+
+/* Runs the instrumented traversal once (device buffers) and returns its
+ * counters; used to state the algorithmic bytes per ray. */
+int lmgpu_trace_stats_device(const lmgpu_accel* accel, const float* d_rays, lmgpu_hit* d_hits, uint64_t n,
+                             int anyhit, void* stream, lmgpu_trace_stats* stats);
+
+/* Synchronises `stream` and reports device-side errors (stack overflow)
+ * raised by earlier asynchronous launches. */
+int lmgpu_accel_check(const lmgpu_accel* accel, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,49 @@
+// Device-side state of one accel (the object behind lmgpu_accel*).
+#pragma once
+
+#include "common.cuh"
+#include "../../include/lmgpu.h"
+
+#include <mutex>
+
+struct lmgpu_accel {
+    int device = 0;
+    uint64_t ntri = 0;
+    bool built = false;
+
+    // Output of the build: 8-wide compressed nodes and the triangles they
+    // reference, both in HBM for the lifetime of the accel.
+    lmgpu::WNode* nodes = nullptr;
+    lmgpu::WTri* tris = nullptr;
+    uint64_t num_wide = 0;
+    uint64_t cap_wide = 0;
+    uint64_t cap_tris = 0;
+
+    // Device status word raised by traversal kernels (stack overflow).
+    uint32_t* status = nullptr;
+    // Traversal counters of the instrumented kernel (4 x u64).
+    unsigned long long* counters = nullptr;
+
+    lmgpu_accel_info info{};
+
+    // Staging buffers of the host-pointer trace entry point, reused across
+    // calls; host_mu serialises callers (Accel3::Intersect may be called from
+    // several threads at once, scheduler.cpp:146-183).
+    std::mutex host_mu;
+    float* stage_rays = nullptr;
+    lmgpu_hit* stage_hits = nullptr;
+    uint64_t stage_cap = 0;
+    cudaStream_t stage_stream[2] = {nullptr, nullptr};
+};
+
+namespace lmgpu {
+
+// Builds the binned-SAH binary tree on the device and collapses it into the
+// accel's wide nodes.  d_tris: float[ntri*9] on the device.
+int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t stream);
+
+// Launches the traversal kernel over n rays.
+int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, uint64_t n, bool anyhit,
+                 bool stats, cudaStream_t stream);
+
+}  // namespace lmgpu

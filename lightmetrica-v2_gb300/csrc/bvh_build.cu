@@ -1,0 +1,1176 @@
+// GPU binned-SAH BVH construction and collapse into 8-wide compressed nodes.
+//
+// Reference behaviour this replaces: Accel_BVHSAHBin::Build
+// (src/liblightmetrica/accel/accel_bvh_sahbin.cpp:70-232), a single-threaded
+// recursive binned SAH over triangle AABBs (100 bins on the node's longest
+// axis, object partition by centroid bin).  Here the same kind of tree is
+// built top-down on the GPU:
+//
+//   1. large phase, one level per iteration: every task (node) with more than
+//      kSmallTask primitives is binned by all blocks covering its range
+//      (32 centroid bins on each of the three axes, shared-memory atomics,
+//      then one global flush per block), the best SAH split over all axes is
+//      chosen by one warp per task, and the range is partitioned stably
+//      (chunk counts -> per-task scan -> scatter);
+//   2. small phase: one block per remaining task builds its whole subtree in
+//      shared memory (16 bins per axis, stable block partition);
+//   3. collapse: a top-down pass turns the binary tree into 8-wide nodes,
+//      expanding the child of largest surface area until 8 children exist,
+//      ordering children by ray octant, quantising child boxes to 8 bits
+//      against a padded frame, and writing each node's leaf triangles
+//      contiguously.
+//
+// Leaves hold at most kMaxLeaf = 3 triangles (a wide-node leaf slot encodes
+// its count in 3 unary bits).  The tree topology is deterministic; node
+// storage order depends on atomic allocation order, which changes no query
+// result.
+#include "accel.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace lmgpu {
+namespace {
+
+constexpr int kBinsLarge = 32;
+constexpr int kBinsSmall = 16;
+constexpr int kBinWords = 13;  // count, aabb lo[3], aabb hi[3], centroid lo[3], centroid hi[3]
+constexpr int kChunk = 2048;   // primitives per block in the large phase
+constexpr int kLargeThreads = 256;
+constexpr int kSmallTask = 1024;
+constexpr int kSmallThreads = 128;
+constexpr int kMaxLeaf = 3;
+constexpr int kSmallStack = 48;
+
+struct Task {
+    int32_t node;
+    int32_t begin;
+    int32_t count;
+    int32_t depth;
+    float cmin[3];
+    float cmax[3];
+};
+
+struct Decision {
+    int32_t axis;   // -1: median split by position
+    int32_t split;  // last bin of the left side
+    int32_t nleft;
+    int32_t pad;
+    float cscale;   // bin scale on `axis`
+    float cmin;
+    float pad2[2];
+};
+
+__device__ __forceinline__ float area_of(const float lo[3], const float hi[3])
+{
+    const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+__device__ __forceinline__ float bin_scale(float cmin, float cmax, int nbins)
+{
+    const float ext = cmax - cmin;
+    if (!(ext > 0.0f)) return 0.0f;
+    const float s = (float)nbins / ext;
+    return isfinite(s) ? s : 0.0f;
+}
+
+__device__ __forceinline__ int bin_of(float c, float cmin, float scale, int nbins)
+{
+    int b = (int)((c - cmin) * scale);
+    b = b < 0 ? 0 : b;
+    return b > nbins - 1 ? nbins - 1 : b;
+}
+
+// ---------------------------------------------------------------------------
+// Per-triangle AABBs, identity index array and root bounds.
+__global__ void k_prep(const float* __restrict__ tris, uint64_t n, float4* __restrict__ aabb,
+                       int32_t* __restrict__ idx, uint32_t* __restrict__ root /* 12 ordered words */)
+{
+    __shared__ uint32_t s[12];
+    if (threadIdx.x < 12) s[threadIdx.x] = (threadIdx.x % 6) < 3 ? ordered_pos_max() : ordered_neg_max();
+    __syncthreads();
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float* p = tris + 9 * i;
+        float lo[3], hi[3];
+        for (int k = 0; k < 3; k++) {
+            lo[k] = fminf(fminf(p[k], p[3 + k]), p[6 + k]);
+            hi[k] = fmaxf(fmaxf(p[k], p[3 + k]), p[6 + k]);
+        }
+        aabb[2 * i] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+        aabb[2 * i + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+        idx[i] = (int32_t)i;
+        for (int k = 0; k < 3; k++) {
+            const float c = (lo[k] + hi[k]) * 0.5f;
+            atomicMin(&s[k], float_to_ordered(lo[k]));
+            atomicMax(&s[3 + k], float_to_ordered(hi[k]));
+            atomicMin(&s[6 + k], float_to_ordered(c));
+            atomicMax(&s[9 + k], float_to_ordered(c));
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        if ((threadIdx.x % 6) < 3) atomicMin(&root[threadIdx.x], s[threadIdx.x]);
+        else atomicMax(&root[threadIdx.x], s[threadIdx.x]);
+    }
+}
+
+__global__ void k_init_root(const uint32_t* __restrict__ root, uint64_t n, BNode* __restrict__ nodes,
+                            Task* __restrict__ tasks, Task* __restrict__ small_tasks, int32_t* __restrict__ counters)
+{
+    // counters: [0] node count, [1] next large task count, [2] small task count, [3] max depth
+    BNode b;
+    for (int k = 0; k < 3; k++) {
+        b.lo[k] = ordered_to_float(root[k]);
+        b.hi[k] = ordered_to_float(root[3 + k]);
+    }
+    b.left = -1;
+    b.begin = 0;
+    b.count = (int32_t)n;
+    b.depth = 0;
+    b.pad[0] = b.pad[1] = 0;
+    nodes[0] = b;
+    Task t;
+    t.node = 0;
+    t.begin = 0;
+    t.count = (int32_t)n;
+    t.depth = 0;
+    for (int k = 0; k < 3; k++) {
+        t.cmin[k] = ordered_to_float(root[6 + k]);
+        t.cmax[k] = ordered_to_float(root[9 + k]);
+    }
+    counters[0] = 1;
+    counters[1] = 0;
+    counters[3] = 0;
+    if (n > (uint64_t)kSmallTask) {
+        tasks[0] = t;
+        counters[2] = 0;
+    } else {
+        small_tasks[0] = t;
+        counters[2] = 1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Large phase.
+
+__global__ void k_init_bins(uint32_t* __restrict__ bins, int ntasks)
+{
+    const int total = ntasks * 3 * kBinsLarge * kBinWords;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int w = i % kBinWords;
+        bins[i] = w == 0 ? 0u : ((w - 1) % 6 < 3 ? ordered_pos_max() : ordered_neg_max());
+    }
+}
+
+// Exclusive scan of per-task chunk counts (single block).
+__global__ void k_chunk_offsets(const Task* __restrict__ tasks, int ntasks, int32_t* __restrict__ chunk_off)
+{
+    __shared__ int32_t carry;
+    __shared__ int32_t warp_sums[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < ntasks; base += blockDim.x) {
+        const int t = base + threadIdx.x;
+        int32_t v = t < ntasks ? (tasks[t].count + kChunk - 1) / kChunk : 0;
+        // inclusive warp scan
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        int32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int32_t w = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            warp_sums[lane] = w;
+        }
+        __syncthreads();
+        const int32_t before = (warp > 0 ? warp_sums[warp - 1] : 0) + x - v;
+        if (t < ntasks) chunk_off[t] = carry + before;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += before + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) chunk_off[ntasks] = carry;
+}
+
+// Finds the task owning chunk `c` (largest t with chunk_off[t] <= c).
+__device__ __forceinline__ int find_task(const int32_t* __restrict__ chunk_off, int ntasks, int c)
+{
+    int lo = 0, hi = ntasks - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (chunk_off[mid] <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(kLargeThreads) k_bin_large(const Task* __restrict__ tasks, int ntasks,
+                                                             const int32_t* __restrict__ chunk_off,
+                                                             const int32_t* __restrict__ idx,
+                                                             const float4* __restrict__ aabb,
+                                                             uint32_t* __restrict__ bins)
+{
+    __shared__ uint32_t s[3 * kBinsLarge * kBinWords];
+    const int c = blockIdx.x;
+    if (c >= chunk_off[ntasks]) return;
+    const int t = find_task(chunk_off, ntasks, c);
+    const Task task = tasks[t];
+    const int chunk = c - chunk_off[t];
+    const int begin = task.begin + chunk * kChunk;
+    const int end = min(begin + kChunk, task.begin + task.count);
+    for (int i = threadIdx.x; i < 3 * kBinsLarge * kBinWords; i += blockDim.x) {
+        const int w = i % kBinWords;
+        s[i] = w == 0 ? 0u : ((w - 1) % 6 < 3 ? ordered_pos_max() : ordered_neg_max());
+    }
+    float scale[3];
+    for (int k = 0; k < 3; k++) scale[k] = bin_scale(task.cmin[k], task.cmax[k], kBinsLarge);
+    __syncthreads();
+    for (int p = begin + threadIdx.x; p < end; p += blockDim.x) {
+        const int prim = idx[p];
+        const float4 lo = aabb[2 * prim], hi = aabb[2 * prim + 1];
+        const float l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z};
+        for (int a = 0; a < 3; a++) {
+            const float cc = (l[a] + h[a]) * 0.5f;
+            const int b = bin_of(cc, task.cmin[a], scale[a], kBinsLarge);
+            uint32_t* w = s + (a * kBinsLarge + b) * kBinWords;
+            atomicAdd(&w[0], 1u);
+            for (int k = 0; k < 3; k++) {
+                const float ck = (l[k] + h[k]) * 0.5f;
+                atomicMin(&w[1 + k], float_to_ordered(l[k]));
+                atomicMax(&w[4 + k], float_to_ordered(h[k]));
+                atomicMin(&w[7 + k], float_to_ordered(ck));
+                atomicMax(&w[10 + k], float_to_ordered(ck));
+            }
+        }
+    }
+    __syncthreads();
+    uint32_t* g = bins + (size_t)t * 3 * kBinsLarge * kBinWords;
+    for (int i = threadIdx.x; i < 3 * kBinsLarge * kBinWords; i += blockDim.x) {
+        const int bin = i / kBinWords, w = i % kBinWords;
+        if (s[bin * kBinWords] == 0) continue;
+        if (w == 0) atomicAdd(&g[i], s[i]);
+        else if ((w - 1) % 6 < 3) atomicMin(&g[i], s[i]);
+        else atomicMax(&g[i], s[i]);
+    }
+}
+
+// Reads one bin (decoded) from a bin array.
+struct BinVal {
+    int count;
+    float lo[3], hi[3], clo[3], chi[3];
+};
+
+__device__ __forceinline__ BinVal read_bin(const uint32_t* w)
+{
+    BinVal v;
+    v.count = (int)w[0];
+    for (int k = 0; k < 3; k++) {
+        v.lo[k] = ordered_to_float(w[1 + k]);
+        v.hi[k] = ordered_to_float(w[4 + k]);
+        v.clo[k] = ordered_to_float(w[7 + k]);
+        v.chi[k] = ordered_to_float(w[10 + k]);
+    }
+    return v;
+}
+
+__device__ __forceinline__ void grow(float lo[3], float hi[3], const float l[3], const float h[3])
+{
+    for (int k = 0; k < 3; k++) {
+        lo[k] = fminf(lo[k], l[k]);
+        hi[k] = fmaxf(hi[k], h[k]);
+    }
+}
+
+// Best SAH split of one axis over `nbins` bins; returns cost (inf if none).
+__device__ float best_split_axis(const uint32_t* axis_bins, int nbins, int* out_split)
+{
+    float rarea[kBinsLarge];
+    int rcount[kBinsLarge];
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    int n = 0;
+    for (int b = nbins - 1; b >= 1; b--) {
+        const BinVal v = read_bin(axis_bins + b * kBinWords);
+        if (v.count > 0) grow(lo, hi, v.lo, v.hi);
+        n += v.count;
+        rarea[b] = n > 0 ? area_of(lo, hi) : 0.0f;
+        rcount[b] = n;
+    }
+    float best = INFINITY;
+    int best_s = -1;
+    float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    int nl = 0;
+    for (int s = 0; s < nbins - 1; s++) {
+        const BinVal v = read_bin(axis_bins + s * kBinWords);
+        if (v.count > 0) grow(llo, lhi, v.lo, v.hi);
+        nl += v.count;
+        const int nr = rcount[s + 1];
+        if (nl == 0 || nr == 0) continue;
+        const float cost = area_of(llo, lhi) * (float)nl + rarea[s + 1] * (float)nr;
+        if (cost < best) {
+            best = cost;
+            best_s = s;
+        }
+    }
+    *out_split = best_s;
+    return best;
+}
+
+// One warp per task: choose the split, create both children, route them to
+// the next large level or to the small list.
+__global__ void k_split_large(const Task* __restrict__ tasks, int ntasks, const uint32_t* __restrict__ bins,
+                              BNode* __restrict__ nodes, Decision* __restrict__ dec,
+                              Task* __restrict__ next_tasks, Task* __restrict__ small_tasks,
+                              int32_t* __restrict__ counters, int max_nodes, uint32_t* __restrict__ status)
+{
+    const int t = blockIdx.x;
+    if (t >= ntasks) return;
+    const int lane = threadIdx.x;
+    const Task task = tasks[t];
+    const uint32_t* tb = bins + (size_t)t * 3 * kBinsLarge * kBinWords;
+    float cost = INFINITY;
+    int split = -1;
+    if (lane < 3 && task.cmax[lane] > task.cmin[lane] && bin_scale(task.cmin[lane], task.cmax[lane], kBinsLarge) > 0.0f)
+        cost = best_split_axis(tb + lane * kBinsLarge * kBinWords, kBinsLarge, &split);
+    // pick the minimum cost, ties to the lower axis
+    float c0 = __shfl_sync(0xffffffffu, cost, 0), c1 = __shfl_sync(0xffffffffu, cost, 1),
+          c2 = __shfl_sync(0xffffffffu, cost, 2);
+    int s0 = __shfl_sync(0xffffffffu, split, 0), s1 = __shfl_sync(0xffffffffu, split, 1),
+        s2 = __shfl_sync(0xffffffffu, split, 2);
+    if (lane != 0) return;
+    int axis = -1, s = -1;
+    float best = INFINITY;
+    if (s0 >= 0 && c0 < best) { best = c0; axis = 0; s = s0; }
+    if (s1 >= 0 && c1 < best) { best = c1; axis = 1; s = s1; }
+    if (s2 >= 0 && c2 < best) { best = c2; axis = 2; s = s2; }
+
+    float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float rlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float lclo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lchi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float rclo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rchi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    int nl = 0;
+    Decision d;
+    d.pad = 0;
+    d.pad2[0] = d.pad2[1] = 0.0f;
+    if (axis >= 0) {
+        const uint32_t* ab = tb + axis * kBinsLarge * kBinWords;
+        for (int b = 0; b < kBinsLarge; b++) {
+            const BinVal v = read_bin(ab + b * kBinWords);
+            if (v.count == 0) continue;
+            if (b <= s) {
+                grow(llo, lhi, v.lo, v.hi);
+                grow(lclo, lchi, v.clo, v.chi);
+                nl += v.count;
+            } else {
+                grow(rlo, rhi, v.lo, v.hi);
+                grow(rclo, rchi, v.clo, v.chi);
+            }
+        }
+        d.axis = axis;
+        d.split = s;
+        d.cscale = bin_scale(task.cmin[axis], task.cmax[axis], kBinsLarge);
+        d.cmin = task.cmin[axis];
+    } else {
+        // All centroids coincide: split by position.  Child boxes are the
+        // parent's (a conservative bound), centroid bounds unchanged.
+        nl = task.count / 2;
+        const BNode& pn = nodes[task.node];
+        for (int k = 0; k < 3; k++) {
+            llo[k] = rlo[k] = pn.lo[k];
+            lhi[k] = rhi[k] = pn.hi[k];
+            lclo[k] = rclo[k] = task.cmin[k];
+            lchi[k] = rchi[k] = task.cmax[k];
+        }
+        d.axis = -1;
+        d.split = 0;
+        d.cscale = 0.0f;
+        d.cmin = 0.0f;
+    }
+    d.nleft = nl;
+    dec[t] = d;
+
+    const int child = atomicAdd(&counters[0], 2);
+    if (child + 2 > max_nodes) {
+        atomicOr(status, kStatusBuildOverflow);
+        return;
+    }
+    nodes[task.node].left = child;
+    const int depth = task.depth + 1;
+    atomicMax(&counters[3], depth);
+    for (int side = 0; side < 2; side++) {
+        BNode b;
+        const float* lo = side ? rlo : llo;
+        const float* hi = side ? rhi : lhi;
+        for (int k = 0; k < 3; k++) {
+            b.lo[k] = lo[k];
+            b.hi[k] = hi[k];
+        }
+        b.left = -1;
+        b.begin = side ? task.begin + nl : task.begin;
+        b.count = side ? task.count - nl : nl;
+        b.depth = depth;
+        b.pad[0] = b.pad[1] = 0;
+        nodes[child + side] = b;
+        Task ct;
+        ct.node = child + side;
+        ct.begin = b.begin;
+        ct.count = b.count;
+        ct.depth = depth;
+        for (int k = 0; k < 3; k++) {
+            ct.cmin[k] = side ? rclo[k] : lclo[k];
+            ct.cmax[k] = side ? rchi[k] : lchi[k];
+        }
+        if (ct.count > kSmallTask) next_tasks[atomicAdd(&counters[1], 1)] = ct;
+        else small_tasks[atomicAdd(&counters[2], 1)] = ct;
+    }
+}
+
+__device__ __forceinline__ bool goes_left(const Decision& d, const Task& task, int pos, int prim,
+                                          const float4* __restrict__ aabb)
+{
+    if (d.axis < 0) return (pos - task.begin) < d.nleft;
+    const float4 lo = aabb[2 * prim], hi = aabb[2 * prim + 1];
+    const float l = d.axis == 0 ? lo.x : (d.axis == 1 ? lo.y : lo.z);
+    const float h = d.axis == 0 ? hi.x : (d.axis == 1 ? hi.y : hi.z);
+    return bin_of((l + h) * 0.5f, d.cmin, d.cscale, kBinsLarge) <= d.split;
+}
+
+// Per-chunk count of left-going primitives.
+__global__ void __launch_bounds__(kLargeThreads) k_part_count(const Task* __restrict__ tasks, int ntasks,
+                                                              const int32_t* __restrict__ chunk_off,
+                                                              const Decision* __restrict__ dec,
+                                                              const int32_t* __restrict__ idx,
+                                                              const float4* __restrict__ aabb,
+                                                              int32_t* __restrict__ chunk_left)
+{
+    __shared__ int32_t sum;
+    const int c = blockIdx.x;
+    if (c >= chunk_off[ntasks]) return;
+    if (threadIdx.x == 0) sum = 0;
+    __syncthreads();
+    const int t = find_task(chunk_off, ntasks, c);
+    const Task task = tasks[t];
+    const Decision d = dec[t];
+    const int begin = task.begin + (c - chunk_off[t]) * kChunk;
+    const int end = min(begin + kChunk, task.begin + task.count);
+    int n = 0;
+    for (int p = begin + threadIdx.x; p < end; p += blockDim.x) n += goes_left(d, task, p, idx[p], aabb) ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xffffffffu, n, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&sum, n);
+    __syncthreads();
+    if (threadIdx.x == 0) chunk_left[c] = sum;
+}
+
+// Exclusive scan of chunk_left within each task (one thread per task).
+__global__ void k_part_scan(const Task* __restrict__ tasks, int ntasks, const int32_t* __restrict__ chunk_off,
+                            const int32_t* __restrict__ chunk_left, int32_t* __restrict__ chunk_left_off)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntasks) return;
+    int run = 0;
+    for (int c = chunk_off[t]; c < chunk_off[t + 1]; c++) {
+        chunk_left_off[c] = run;
+        run += chunk_left[c];
+    }
+}
+
+// Block-wide exclusive scan of one int per thread (blockDim.x == kLargeThreads).
+template <int THREADS>
+__device__ __forceinline__ int block_exclusive_scan(int v, int* total)
+{
+    __shared__ int warp_sums[THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < THREADS / 32 ? warp_sums[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < THREADS / 32) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const int before = (warp > 0 ? warp_sums[warp - 1] : 0) + x - v;
+    *total = warp_sums[THREADS / 32 - 1];
+    __syncthreads();
+    return before;
+}
+
+// Stable scatter of each chunk into idx_out.
+__global__ void __launch_bounds__(kLargeThreads) k_part_scatter(const Task* __restrict__ tasks, int ntasks,
+                                                                const int32_t* __restrict__ chunk_off,
+                                                                const Decision* __restrict__ dec,
+                                                                const int32_t* __restrict__ chunk_left_off,
+                                                                const int32_t* __restrict__ idx,
+                                                                const float4* __restrict__ aabb,
+                                                                int32_t* __restrict__ idx_out,
+                                                                uint32_t* __restrict__ status)
+{
+    constexpr int kPer = kChunk / kLargeThreads;
+    const int c = blockIdx.x;
+    if (c >= chunk_off[ntasks]) return;
+    const int t = find_task(chunk_off, ntasks, c);
+    const Task task = tasks[t];
+    const Decision d = dec[t];
+    const int chunk = c - chunk_off[t];
+    const int begin = task.begin + chunk * kChunk;
+    const int end = min(begin + kChunk, task.begin + task.count);
+    const int p0 = begin + threadIdx.x * kPer;
+    int prim[kPer];
+    bool left[kPer];
+    int nleft = 0;
+    for (int j = 0; j < kPer; j++) {
+        const int p = p0 + j;
+        if (p < end) {
+            prim[j] = idx[p];
+            left[j] = goes_left(d, task, p, prim[j], aabb);
+            nleft += left[j] ? 1 : 0;
+        }
+    }
+    int total;
+    int lrank = block_exclusive_scan<kLargeThreads>(nleft, &total);
+    const int before_left = chunk_left_off[c];
+    const int before_right = chunk * kChunk - before_left;
+    int rrank = (p0 - begin < end - begin ? p0 - begin : end - begin) - lrank;
+    const int task_end = task.begin + task.count;
+    for (int j = 0; j < kPer; j++) {
+        const int p = p0 + j;
+        if (p >= end) break;
+        // destinations stay inside the task's range when the flags agree
+        // with the bin counts; a disagreement is flagged, never written
+        const int dst = left[j] ? task.begin + before_left + lrank++ : task.begin + d.nleft + before_right + rrank++;
+        if (dst < task.begin || dst >= task_end || (left[j] && dst >= task.begin + d.nleft)) {
+            atomicOr(status, kStatusBuildOverflow);
+            continue;
+        }
+        idx_out[dst] = prim[j];
+    }
+}
+
+__global__ void __launch_bounds__(kLargeThreads) k_copy_back(const Task* __restrict__ tasks, int ntasks,
+                                                             const int32_t* __restrict__ chunk_off,
+                                                             const int32_t* __restrict__ src,
+                                                             int32_t* __restrict__ dst)
+{
+    const int c = blockIdx.x;
+    if (c >= chunk_off[ntasks]) return;
+    const int t = find_task(chunk_off, ntasks, c);
+    const Task task = tasks[t];
+    const int begin = task.begin + (c - chunk_off[t]) * kChunk;
+    const int end = min(begin + kChunk, task.begin + task.count);
+    for (int p = begin + threadIdx.x; p < end; p += blockDim.x) dst[p] = src[p];
+}
+
+// ---------------------------------------------------------------------------
+// Small phase: one block builds the subtree of one task in shared memory.
+
+struct SmallSub {
+    int32_t node, b, n, depth;
+    float cmin[3], cmax[3];
+};
+
+__global__ void __launch_bounds__(kSmallThreads) k_build_small(const Task* __restrict__ small_tasks,
+                                                               const float4* __restrict__ aabb,
+                                                               int32_t* __restrict__ idx,
+                                                               BNode* __restrict__ nodes,
+                                                               int32_t* __restrict__ counters, int max_nodes,
+                                                               uint32_t* __restrict__ status)
+{
+    __shared__ float s_lo[3][kSmallTask];
+    __shared__ float s_hi[3][kSmallTask];
+    __shared__ int32_t s_gid[kSmallTask];
+    __shared__ int16_t s_idx[kSmallTask];
+    __shared__ int16_t s_tmp[kSmallTask];
+    __shared__ uint32_t s_bins[3 * kBinsSmall * kBinWords];
+    __shared__ SmallSub s_stack[kSmallStack];
+    __shared__ int s_sp;
+    __shared__ SmallSub s_cur;
+    __shared__ int s_axis, s_split, s_nleft, s_child, s_abort;
+    __shared__ float s_cost[3];
+    __shared__ int s_splits[3];
+
+    const Task task = small_tasks[blockIdx.x];
+    for (int i = threadIdx.x; i < task.count; i += blockDim.x) {
+        const int g = idx[task.begin + i];
+        s_gid[i] = g;
+        s_idx[i] = (int16_t)i;
+        const float4 lo = aabb[2 * g], hi = aabb[2 * g + 1];
+        s_lo[0][i] = lo.x; s_lo[1][i] = lo.y; s_lo[2][i] = lo.z;
+        s_hi[0][i] = hi.x; s_hi[1][i] = hi.y; s_hi[2][i] = hi.z;
+    }
+    if (threadIdx.x == 0) {
+        SmallSub r;
+        r.node = task.node;
+        r.b = 0;
+        r.n = task.count;
+        r.depth = task.depth;
+        for (int k = 0; k < 3; k++) { r.cmin[k] = task.cmin[k]; r.cmax[k] = task.cmax[k]; }
+        s_stack[0] = r;
+        s_sp = 1;
+        s_abort = 0;
+    }
+    __syncthreads();
+
+    while (true) {
+        if (threadIdx.x == 0) {
+            if (s_sp > 0 && !s_abort) s_cur = s_stack[--s_sp];
+            else s_cur.n = -1;
+        }
+        __syncthreads();
+        const SmallSub cur = s_cur;
+        if (cur.n < 0) break;
+        if (cur.n <= kMaxLeaf) {
+            // leaf: node already carries begin/count/bounds; left stays -1
+            __syncthreads();
+            continue;
+        }
+        float scale[3];
+        for (int k = 0; k < 3; k++) scale[k] = bin_scale(cur.cmin[k], cur.cmax[k], kBinsSmall);
+        for (int i = threadIdx.x; i < 3 * kBinsSmall * kBinWords; i += blockDim.x) {
+            const int w = i % kBinWords;
+            s_bins[i] = w == 0 ? 0u : ((w - 1) % 6 < 3 ? ordered_pos_max() : ordered_neg_max());
+        }
+        __syncthreads();
+        for (int i = cur.b + threadIdx.x; i < cur.b + cur.n; i += blockDim.x) {
+            const int li = s_idx[i];
+            float l[3], h[3];
+            for (int k = 0; k < 3; k++) { l[k] = s_lo[k][li]; h[k] = s_hi[k][li]; }
+            for (int a = 0; a < 3; a++) {
+                if (scale[a] == 0.0f) continue;
+                const int b = bin_of((l[a] + h[a]) * 0.5f, cur.cmin[a], scale[a], kBinsSmall);
+                uint32_t* w = s_bins + (a * kBinsSmall + b) * kBinWords;
+                atomicAdd(&w[0], 1u);
+                for (int k = 0; k < 3; k++) {
+                    const float ck = (l[k] + h[k]) * 0.5f;
+                    atomicMin(&w[1 + k], float_to_ordered(l[k]));
+                    atomicMax(&w[4 + k], float_to_ordered(h[k]));
+                    atomicMin(&w[7 + k], float_to_ordered(ck));
+                    atomicMax(&w[10 + k], float_to_ordered(ck));
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            int sp = -1;
+            float c = INFINITY;
+            if (scale[threadIdx.x] > 0.0f) c = best_split_axis(s_bins + threadIdx.x * kBinsSmall * kBinWords, kBinsSmall, &sp);
+            s_cost[threadIdx.x] = c;
+            s_splits[threadIdx.x] = sp;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int axis = -1, sp = -1;
+            float best = INFINITY;
+            for (int a = 0; a < 3; a++)
+                if (s_splits[a] >= 0 && s_cost[a] < best) { best = s_cost[a]; axis = a; sp = s_splits[a]; }
+            s_axis = axis;
+            s_split = sp;
+        }
+        __syncthreads();
+        const int axis = s_axis, split = s_split;
+        // stable partition of [cur.b, cur.b + cur.n) into s_tmp
+        constexpr int kPer = kSmallTask / kSmallThreads;
+        const int p0 = cur.b + threadIdx.x * kPer;
+        const int end = cur.b + cur.n;
+        bool left[kPer];
+        int nl = 0;
+        for (int j = 0; j < kPer; j++) {
+            const int p = p0 + j;
+            left[j] = false;
+            if (p < end) {
+                if (axis < 0) {
+                    left[j] = (p - cur.b) < cur.n / 2;
+                } else {
+                    const int li = s_idx[p];
+                    const float c = (s_lo[axis][li] + s_hi[axis][li]) * 0.5f;
+                    left[j] = bin_of(c, cur.cmin[axis], scale[axis], kBinsSmall) <= split;
+                }
+                nl += left[j] ? 1 : 0;
+            }
+        }
+        int total;
+        int lrank = block_exclusive_scan<kSmallThreads>(nl, &total);
+        int rrank = max(0, min(p0, end) - cur.b) - lrank;
+        for (int j = 0; j < kPer; j++) {
+            const int p = p0 + j;
+            if (p >= end) break;
+            if (left[j]) s_tmp[cur.b + lrank++] = s_idx[p];
+            else s_tmp[cur.b + total + rrank++] = s_idx[p];
+        }
+        if (threadIdx.x == 0) {
+            s_nleft = total;
+            const int child = atomicAdd(&counters[0], 2);
+            if (child + 2 > max_nodes) {
+                atomicOr(status, kStatusBuildOverflow);
+                s_abort = 1;
+                s_child = -1;
+            } else {
+                s_child = child;
+            }
+        }
+        __syncthreads();
+        for (int p = cur.b + threadIdx.x; p < end; p += blockDim.x) s_idx[p] = s_tmp[p];
+        if (threadIdx.x == 0 && s_child >= 0) {
+            const int nleft = s_nleft;
+            // child bounds and centroid bounds from the bins of the split axis
+            float lo[2][3], hi[2][3], clo[2][3], chi[2][3];
+            for (int sd = 0; sd < 2; sd++)
+                for (int k = 0; k < 3; k++) {
+                    lo[sd][k] = clo[sd][k] = FLT_MAX;
+                    hi[sd][k] = chi[sd][k] = -FLT_MAX;
+                }
+            if (axis >= 0) {
+                for (int b = 0; b < kBinsSmall; b++) {
+                    const BinVal v = read_bin(s_bins + (axis * kBinsSmall + b) * kBinWords);
+                    if (v.count == 0) continue;
+                    const int sd = b <= split ? 0 : 1;
+                    grow(lo[sd], hi[sd], v.lo, v.hi);
+                    grow(clo[sd], chi[sd], v.clo, v.chi);
+                }
+            } else {
+                const BNode& pn = nodes[cur.node];
+                for (int sd = 0; sd < 2; sd++)
+                    for (int k = 0; k < 3; k++) {
+                        lo[sd][k] = pn.lo[k]; hi[sd][k] = pn.hi[k];
+                        clo[sd][k] = cur.cmin[k]; chi[sd][k] = cur.cmax[k];
+                    }
+            }
+            const int child = s_child;
+            nodes[cur.node].left = child;
+            const int depth = cur.depth + 1;
+            atomicMax(&counters[3], depth);
+            SmallSub subs[2];
+            for (int sd = 0; sd < 2; sd++) {
+                BNode bn;
+                for (int k = 0; k < 3; k++) { bn.lo[k] = lo[sd][k]; bn.hi[k] = hi[sd][k]; }
+                bn.left = -1;
+                bn.begin = task.begin + (sd ? cur.b + nleft : cur.b);
+                bn.count = sd ? cur.n - nleft : nleft;
+                bn.depth = depth;
+                bn.pad[0] = bn.pad[1] = 0;
+                nodes[child + sd] = bn;
+                subs[sd].node = child + sd;
+                subs[sd].b = sd ? cur.b + nleft : cur.b;
+                subs[sd].n = bn.count;
+                subs[sd].depth = depth;
+                for (int k = 0; k < 3; k++) { subs[sd].cmin[k] = clo[sd][k]; subs[sd].cmax[k] = chi[sd][k]; }
+            }
+            // push the larger first so the smaller is processed next (bounded stack)
+            const int big = subs[0].n >= subs[1].n ? 0 : 1;
+            for (int q = 0; q < 2; q++) {
+                const SmallSub& sb = subs[q == 0 ? big : 1 - big];
+                if (sb.n <= kMaxLeaf) continue;  // leaves need no processing
+                if (s_sp < kSmallStack) s_stack[s_sp++] = sb;
+                else { atomicOr(status, kStatusBuildOverflow); s_abort = 1; }
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < task.count; i += blockDim.x) idx[task.begin + i] = s_gid[s_idx[i]];
+}
+
+// ---------------------------------------------------------------------------
+// Collapse into 8-wide compressed nodes.
+
+struct CollapseItem {
+    int32_t bnode;
+    int32_t wnode;
+};
+
+__device__ __forceinline__ float node_area(const BNode& b) { return area_of(b.lo, b.hi); }
+
+__device__ __forceinline__ bool is_leafish(const BNode& b) { return b.left < 0 || b.count <= kMaxLeaf; }
+
+// Smallest e with 253 * 2^e >= ext, and no lower than the floors.
+__device__ int frame_exponent(float ext, float max_ext, float mag)
+{
+    int e = -126;
+    if (ext > 0.0f) {
+        int k;
+        const float m = frexpf(ext / 253.0f, &k);  // ext/253 = m * 2^k, m in [0.5, 1)
+        e = (m == 0.5f) ? k - 1 : k;
+        while (253.0f * ldexpf(1.0f, e) < ext) e++;
+    }
+    if (max_ext > 0.0f) {
+        int k;
+        frexpf(max_ext, &k);
+        e = max(e, k - 17);  // flat axes still get a pad of ~max_ext * 2^-17
+    }
+    if (mag > 0.0f) {
+        int k;
+        frexpf(mag, &k);
+        e = max(e, k - 21);  // at least 8 ulps of the node's coordinates
+    }
+    return min(max(e, -126), 127);
+}
+
+__global__ void k_collapse(const CollapseItem* __restrict__ in, int nin, CollapseItem* __restrict__ out,
+                           const BNode* __restrict__ bnodes, const int32_t* __restrict__ idx,
+                           const float* __restrict__ tris, WNode* __restrict__ wnodes, WTri* __restrict__ wtris,
+                           int32_t* __restrict__ counters /* [0] wide count, [1] tri count, [2] out count */,
+                           int max_wide, uint32_t* __restrict__ status)
+{
+    const int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nin) return;
+    const CollapseItem item = in[it];
+    const BNode parent = bnodes[item.bnode];
+
+    int ch[8];
+    int n = 0;
+    if (parent.left < 0) {
+        ch[n++] = item.bnode;
+    } else {
+        ch[n++] = parent.left;
+        ch[n++] = parent.left + 1;
+    }
+    while (n < 8) {
+        int best = -1;
+        float best_a = -1.0f;
+        for (int i = 0; i < n; i++) {
+            const BNode b = bnodes[ch[i]];
+            if (is_leafish(b)) continue;
+            const float a = node_area(b);
+            if (a > best_a) { best_a = a; best = i; }
+        }
+        if (best < 0) break;
+        const int l = bnodes[ch[best]].left;
+        ch[best] = l;
+        ch[n++] = l + 1;
+    }
+
+    // Octant ordering: slot s holds the child met first by rays whose
+    // direction signs are given by s (bit set = negative component).
+    float pc[3];
+    for (int k = 0; k < 3; k++) pc[k] = (parent.lo[k] + parent.hi[k]) * 0.5f;
+    int slot_of[8];
+    bool used_slot[8];
+    bool assigned[8];
+    float cost[8][8];
+    for (int i = 0; i < 8; i++) { used_slot[i] = false; assigned[i] = false; slot_of[i] = -1; }
+    for (int i = 0; i < n; i++) {
+        const BNode b = bnodes[ch[i]];
+        float c[3];
+        for (int k = 0; k < 3; k++) c[k] = (b.lo[k] + b.hi[k]) * 0.5f - pc[k];
+        for (int s = 0; s < 8; s++) {
+            const float dx = (s & 1) ? -1.0f : 1.0f, dy = (s & 2) ? -1.0f : 1.0f, dz = (s & 4) ? -1.0f : 1.0f;
+            cost[i][s] = c[0] * dx + c[1] * dy + c[2] * dz;
+        }
+    }
+    for (int r = 0; r < n; r++) {
+        int bi = -1, bs = -1;
+        float bc = INFINITY;
+        for (int i = 0; i < n; i++) {
+            if (assigned[i]) continue;
+            for (int s = 0; s < 8; s++) {
+                if (used_slot[s]) continue;
+                if (cost[i][s] < bc || bi < 0) { bc = cost[i][s]; bi = i; bs = s; }
+            }
+        }
+        assigned[bi] = true;
+        used_slot[bs] = true;
+        slot_of[bi] = bs;
+    }
+    int child_at[8];
+    for (int s = 0; s < 8; s++) child_at[s] = -1;
+    for (int i = 0; i < n; i++) child_at[slot_of[i]] = ch[i];
+
+    // Quantisation frame: p = lo - 2^e per axis.
+    float ext[3], max_ext = 0.0f, mag = 0.0f;
+    for (int k = 0; k < 3; k++) {
+        ext[k] = parent.hi[k] - parent.lo[k];
+        max_ext = fmaxf(max_ext, ext[k]);
+        mag = fmaxf(mag, fmaxf(fabsf(parent.lo[k]), fabsf(parent.hi[k])));
+    }
+    int e[3];
+    float p[3];
+    double sc[3];
+    for (int k = 0; k < 3; k++) {
+        e[k] = frame_exponent(ext[k], max_ext, mag);
+        sc[k] = ldexp(1.0, e[k]);
+        p[k] = parent.lo[k] - (float)sc[k];
+    }
+
+    int ninner = 0, ntris = 0;
+    for (int s = 0; s < 8; s++) {
+        if (child_at[s] < 0) continue;
+        const BNode b = bnodes[child_at[s]];
+        if (is_leafish(b)) ntris += b.count;
+        else ninner++;
+    }
+    const int child_base = ninner ? atomicAdd(&counters[0], ninner) : 0;
+    const int tri_base = ntris ? atomicAdd(&counters[1], ntris) : 0;
+    if (child_base + ninner > max_wide) {
+        atomicOr(status, kStatusBuildOverflow);
+        return;
+    }
+
+    uint8_t meta[8], qlo[3][8], qhi[3][8];
+    uint32_t imask = 0;
+    int inner_rank = 0, tri_off = 0;
+    for (int s = 0; s < 8; s++) {
+        meta[s] = 0;
+        for (int k = 0; k < 3; k++) { qlo[k][s] = 0; qhi[k][s] = 0; }
+        if (child_at[s] < 0) continue;
+        const BNode b = bnodes[child_at[s]];
+        for (int k = 0; k < 3; k++) {
+            double lo = floor(((double)b.lo[k] - (double)p[k]) / sc[k]) - 1.0;
+            double hi = ceil(((double)b.hi[k] - (double)p[k]) / sc[k]) + 1.0;
+            lo = lo < 0.0 ? 0.0 : (lo > 255.0 ? 255.0 : lo);
+            hi = hi < 0.0 ? 0.0 : (hi > 255.0 ? 255.0 : hi);
+            qlo[k][s] = (uint8_t)lo;
+            qhi[k][s] = (uint8_t)hi;
+        }
+        if (is_leafish(b)) {
+            const int cnt = b.count;  // 1..3
+            if (cnt < 1 || cnt > kMaxLeaf || tri_off + cnt > 24) {
+                atomicOr(status, kStatusBuildOverflow);
+                return;
+            }
+            meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | (uint32_t)tri_off);
+            for (int j = 0; j < cnt; j++) {
+                const int g = idx[b.begin + j];
+                const float* v = tris + 9 * (size_t)g;
+                WTri w;
+                w.v0 = make_float4(v[0], v[1], v[2], __int_as_float(g));
+                w.v1 = make_float4(v[3], v[4], v[5], 0.0f);
+                w.v2 = make_float4(v[6], v[7], v[8], 0.0f);
+                wtris[tri_base + tri_off + j] = w;
+            }
+            tri_off += cnt;
+        } else {
+            meta[s] = (uint8_t)((1u << 5) | (24u + (uint32_t)s));
+            imask |= 1u << s;
+            const int wn = child_base + inner_rank++;
+            const int o = atomicAdd(&counters[2], 1);
+            out[o] = CollapseItem{child_at[s], wn};
+        }
+    }
+
+    auto pack4 = [](const uint8_t* b) -> uint32_t {
+        return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+    };
+    WNode w;
+    w.w[0] = make_uint4(__float_as_uint(p[0]), __float_as_uint(p[1]), __float_as_uint(p[2]),
+                        (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) |
+                            (imask << 24));
+    w.w[1] = make_uint4((uint32_t)child_base, (uint32_t)tri_base, pack4(meta), pack4(meta + 4));
+    w.w[2] = make_uint4(pack4(qlo[0]), pack4(qlo[0] + 4), pack4(qlo[1]), pack4(qlo[1] + 4));
+    w.w[3] = make_uint4(pack4(qlo[2]), pack4(qlo[2] + 4), pack4(qhi[0]), pack4(qhi[0] + 4));
+    w.w[4] = make_uint4(pack4(qhi[1]), pack4(qhi[1] + 4), pack4(qhi[2]), pack4(qhi[2] + 4));
+    wnodes[item.wnode] = w;
+}
+
+template <typename T>
+int dalloc(T** p, size_t count)
+{
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        *p = nullptr;
+        return LMGPU_ERR_CUDA;
+    }
+    return LMGPU_OK;
+}
+
+struct Scratch {
+    std::vector<void*> ptrs;
+    ~Scratch()
+    {
+        for (void* p : ptrs) cudaFree(p);
+    }
+    template <typename T>
+    int get(T** p, size_t count)
+    {
+        int rc = dalloc(p, count);
+        if (rc == LMGPU_OK) ptrs.push_back((void*)*p);
+        return rc;
+    }
+};
+
+}  // namespace
+
+int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t stream)
+{
+    a->built = false;
+    a->ntri = ntri;
+    a->num_wide = 0;
+    a->info = lmgpu_accel_info{};
+    a->info.num_triangles = ntri;
+    if (ntri == 0) {
+        a->built = true;
+        return LMGPU_OK;
+    }
+    if (ntri > (uint64_t)(1u << 30)) {
+        set_error("lmgpu_accel_build: more than 2^30 triangles");
+        return LMGPU_ERR_INVALID;
+    }
+    const int n = (int)ntri;
+    const int max_nodes = 2 * n + 1;
+
+    cudaEvent_t ev0, ev1;
+    LMGPU_CUDA_TRY(cudaEventCreate(&ev0));
+    LMGPU_CUDA_TRY(cudaEventCreate(&ev1));
+    LMGPU_CUDA_TRY(cudaEventRecord(ev0, stream));
+
+    Scratch S;
+    float4* aabb;
+    int32_t *idx, *idx_alt, *counters, *chunk_off, *chunk_left, *chunk_left_off;
+    uint32_t* root;
+    BNode* bnodes;
+    Task *tasks_a, *tasks_b, *small_tasks;
+    Decision* dec;
+    uint32_t* bins;
+    const int max_large = n / kSmallTask * 2 + 2;  // live large tasks at one level
+    const int max_chunks = n / kChunk + max_large + 1;
+    int rc = LMGPU_OK;
+    if ((rc = S.get(&aabb, 2 * (size_t)n)) || (rc = S.get(&idx, n)) || (rc = S.get(&idx_alt, n)) ||
+        (rc = S.get(&counters, 8)) || (rc = S.get(&root, 12)) || (rc = S.get(&bnodes, max_nodes)) ||
+        (rc = S.get(&tasks_a, max_large)) || (rc = S.get(&tasks_b, max_large)) || (rc = S.get(&small_tasks, n)) ||
+        (rc = S.get(&dec, max_large)) || (rc = S.get(&bins, (size_t)max_large * 3 * kBinsLarge * kBinWords)) ||
+        (rc = S.get(&chunk_off, max_large + 1)) || (rc = S.get(&chunk_left, max_chunks)) ||
+        (rc = S.get(&chunk_left_off, max_chunks)))
+        return rc;
+
+    uint32_t root_init[12];
+    for (int i = 0; i < 12; i++) root_init[i] = (i % 6) < 3 ? ordered_pos_max() : ordered_neg_max();
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(root, root_init, sizeof(root_init), cudaMemcpyHostToDevice, stream));
+    LMGPU_CUDA_TRY(cudaMemsetAsync(a->status, 0, sizeof(uint32_t), stream));
+    k_prep<<<(n + 255) / 256, 256, 0, stream>>>(d_tris, ntri, aabb, idx, root);
+    k_init_root<<<1, 1, 0, stream>>>(root, ntri, bnodes, tasks_a, small_tasks, counters);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+
+    int ntasks = n > kSmallTask ? 1 : 0;
+    Task* cur = tasks_a;
+    Task* nxt = tasks_b;
+    while (ntasks > 0) {
+        if (ntasks > max_large) {
+            set_error("bvh build: large-task list overflow");
+            return LMGPU_ERR_OVERFLOW;
+        }
+        const int grid = std::min(max_chunks, n / kChunk + ntasks + 1);
+        k_init_bins<<<std::min(1024, (ntasks * 3 * kBinsLarge * kBinWords + 255) / 256), 256, 0, stream>>>(bins, ntasks);
+        k_chunk_offsets<<<1, 1024, 0, stream>>>(cur, ntasks, chunk_off);
+        k_bin_large<<<grid, kLargeThreads, 0, stream>>>(cur, ntasks, chunk_off, idx, aabb, bins);
+        LMGPU_CUDA_TRY(cudaMemsetAsync(counters + 1, 0, sizeof(int32_t), stream));
+        k_split_large<<<ntasks, 32, 0, stream>>>(cur, ntasks, bins, bnodes, dec, nxt, small_tasks, counters,
+                                                 max_nodes, a->status);
+        k_part_count<<<grid, kLargeThreads, 0, stream>>>(cur, ntasks, chunk_off, dec, idx, aabb, chunk_left);
+        k_part_scan<<<(ntasks + 127) / 128, 128, 0, stream>>>(cur, ntasks, chunk_off, chunk_left, chunk_left_off);
+        k_part_scatter<<<grid, kLargeThreads, 0, stream>>>(cur, ntasks, chunk_off, dec, chunk_left_off, idx, aabb,
+                                                           idx_alt, a->status);
+        k_copy_back<<<grid, kLargeThreads, 0, stream>>>(cur, ntasks, chunk_off, idx_alt, idx);
+        LMGPU_CUDA_TRY(cudaGetLastError());
+        int32_t next = 0;
+        uint32_t lst = 0;
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(&next, counters + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(&lst, a->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+        if (lst & kStatusBuildOverflow) {
+            set_error("bvh build: partition or node bound exceeded in the large phase");
+            return LMGPU_ERR_OVERFLOW;
+        }
+        ntasks = next;
+        std::swap(cur, nxt);
+    }
+    int32_t hc[4];
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, stream));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    const int nsmall = hc[2];
+    if (nsmall > 0) {
+        k_build_small<<<nsmall, kSmallThreads, 0, stream>>>(small_tasks, aabb, idx, bnodes, counters, max_nodes,
+                                                            a->status);
+        LMGPU_CUDA_TRY(cudaGetLastError());
+    }
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, stream));
+    uint32_t st = 0;
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(&st, a->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (st & kStatusBuildOverflow) {
+        set_error("bvh build: device-side node or stack bound exceeded");
+        return LMGPU_ERR_OVERFLOW;
+    }
+    const int nbin = hc[0];
+    a->info.num_binary_nodes = (uint64_t)nbin;
+    a->info.binary_depth = hc[3];
+
+    // Collapse.  Wide nodes <= binary internal nodes + 1.
+    const int max_wide = n + 1;
+    if ((uint64_t)max_wide > a->cap_wide) {
+        if (a->nodes) cudaFree(a->nodes);
+        a->nodes = nullptr;
+        a->cap_wide = 0;
+        if ((rc = dalloc(&a->nodes, max_wide))) return rc;
+        a->cap_wide = (uint64_t)max_wide;
+    }
+    if (ntri > a->cap_tris) {
+        if (a->tris) cudaFree(a->tris);
+        a->tris = nullptr;
+        a->cap_tris = 0;
+        if ((rc = dalloc(&a->tris, ntri))) return rc;
+        a->cap_tris = ntri;
+    }
+    CollapseItem *qa, *qb;
+    int32_t* ccount;
+    if ((rc = S.get(&qa, max_wide)) || (rc = S.get(&qb, max_wide)) || (rc = S.get(&ccount, 4))) return rc;
+    const CollapseItem root_item{0, 0};
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(qa, &root_item, sizeof(root_item), cudaMemcpyHostToDevice, stream));
+    int32_t cinit[4] = {1, 0, 0, 0};
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(ccount, cinit, sizeof(cinit), cudaMemcpyHostToDevice, stream));
+    int nin = 1, wdepth = 0;
+    while (nin > 0) {
+        LMGPU_CUDA_TRY(cudaMemsetAsync(ccount + 2, 0, sizeof(int32_t), stream));
+        k_collapse<<<(nin + 127) / 128, 128, 0, stream>>>(qa, nin, qb, bnodes, idx, d_tris, a->nodes, a->tris, ccount,
+                                                         max_wide, a->status);
+        LMGPU_CUDA_TRY(cudaGetLastError());
+        int32_t next = 0;
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(&next, ccount + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+        LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+        nin = next;
+        wdepth++;
+        std::swap(qa, qb);
+    }
+    int32_t cc[4];
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(cc, ccount, sizeof(cc), cudaMemcpyDeviceToHost, stream));
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(&st, a->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    LMGPU_CUDA_TRY(cudaEventRecord(ev1, stream));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (st & kStatusBuildOverflow) {
+        set_error("bvh collapse: wide node bound exceeded");
+        return LMGPU_ERR_OVERFLOW;
+    }
+    if ((uint64_t)cc[1] != ntri) {
+        set_error("bvh collapse: triangle count mismatch (" + std::to_string(cc[1]) + " of " + std::to_string(ntri) + ")");
+        return LMGPU_ERR_OVERFLOW;
+    }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    a->num_wide = (uint64_t)cc[0];
+    a->info.num_wide_nodes = a->num_wide;
+    a->info.wide_depth = wdepth;
+    a->info.node_bytes = a->num_wide * sizeof(WNode);
+    a->info.triangle_bytes = ntri * sizeof(WTri);
+    a->info.build_ms = ms;
+    a->built = true;
+    return LMGPU_OK;
+}
+
+}  // namespace lmgpu

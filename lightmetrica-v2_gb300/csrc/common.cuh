@@ -1,0 +1,97 @@
+// Shared device/host helpers of the lmgpu library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <float.h>
+#include <string>
+
+namespace lmgpu {
+
+// ---------------------------------------------------------------------------
+// Error reporting: one message per host thread, read by lmgpu_last_error().
+void set_error(const std::string& msg);
+void clear_error();
+
+#define LMGPU_CUDA_TRY(expr)                                                        \
+    do {                                                                            \
+        cudaError_t e_ = (expr);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            ::lmgpu::set_error(std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+            return LMGPU_ERR_CUDA;                                                  \
+        }                                                                           \
+    } while (0)
+
+// Status bits raised by kernels into a device word.
+enum : uint32_t {
+    kStatusStackOverflow = 1u << 0,
+    kStatusBuildOverflow = 1u << 1,
+    kStatusBadTree = 1u << 2,  // traversal met an out-of-range index or too many nodes
+};
+
+// ---------------------------------------------------------------------------
+// Ordered-uint encoding of floats, so that atomicMin/atomicMax on uint32
+// order like the floats they encode (NaN-free inputs).
+__host__ __device__ __forceinline__ uint32_t float_to_ordered(float f)
+{
+#ifdef __CUDA_ARCH__
+    uint32_t u = __float_as_uint(f);
+#else
+    uint32_t u;
+    memcpy(&u, &f, 4);
+#endif
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__host__ __device__ __forceinline__ float ordered_to_float(uint32_t u)
+{
+    uint32_t v = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(v);
+#else
+    float f;
+    memcpy(&f, &v, 4);
+    return f;
+#endif
+}
+
+// Encoded +FLT_MAX / -FLT_MAX, the initial values of min / max reductions.
+__host__ __device__ __forceinline__ uint32_t ordered_pos_max() { return 0x80000000u | 0x7f7fffffu; }
+__host__ __device__ __forceinline__ uint32_t ordered_neg_max() { return ~(0x80000000u | 0x7f7fffffu); }
+
+// ---------------------------------------------------------------------------
+// Device data layouts.
+
+// Binary node of the binned-SAH tree (48 bytes).  Every subtree covers the
+// contiguous primitive range [begin, begin + count) of the final index array.
+struct BNode {
+    float lo[3];
+    int32_t left;   // left child (right = left + 1), -1 for a leaf
+    float hi[3];
+    int32_t begin;
+    int32_t count;
+    int32_t depth;
+    int32_t pad[2];
+};
+static_assert(sizeof(BNode) == 48, "BNode layout");
+
+// 8-wide compressed node (80 bytes, five 16-byte words).
+//   w0: origin p (3 floats), byte exponents ex, ey, ez, inner mask imask
+//   w1: child_base, tri_base, meta[0..3], meta[4..7]
+//   w2: qlo_x[0..7], qlo_y[0..7]
+//   w3: qlo_z[0..7], qhi_x[0..7]
+//   w4: qhi_y[0..7], qhi_z[0..7]
+// Child box of slot i on axis a: [p_a + qlo_a[i] * 2^e_a, p_a + qhi_a[i] * 2^e_a].
+// meta[i]: 0 = empty slot; inner child = 0b001_11sss (24 + slot);
+// leaf = unary triangle count (001, 011, 111) << 5 | offset from tri_base.
+struct __align__(16) WNode {
+    uint4 w[5];
+};
+static_assert(sizeof(WNode) == 80, "WNode layout");
+
+// Triangle record (48 bytes): three float4 with the global id in v0.w.
+struct __align__(16) WTri {
+    float4 v0, v1, v2;
+};
+
+}  // namespace lmgpu

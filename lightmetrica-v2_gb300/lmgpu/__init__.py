@@ -1,0 +1,162 @@
+"""Python view of the lmgpu C ABI (include/lmgpu.h), via ctypes.
+
+Used by the tests and the benchmark; the product boundary is the C ABI
+itself.  Loading fails loudly when liblmgpu.so has not been built: there is
+no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .build import LIB_PATH
+
+LMGPU_OK = 0
+ERROR_NAMES = {1: "INVALID", 2: "CUDA", 3: "NOT_BUILT", 4: "OVERFLOW", 5: "NO_DEVICE"}
+
+
+class LmgpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"lmgpu error {code} ({ERROR_NAMES.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Hit(ctypes.Structure):
+    _fields_ = [("t", ctypes.c_float), ("prim", ctypes.c_int32), ("b1", ctypes.c_float), ("b2", ctypes.c_float)]
+
+
+HIT_DTYPE = np.dtype([("t", "<f4"), ("prim", "<i4"), ("b1", "<f4"), ("b2", "<f4")])
+
+
+class AccelInfo(ctypes.Structure):
+    _fields_ = [
+        ("num_triangles", ctypes.c_uint64),
+        ("num_binary_nodes", ctypes.c_uint64),
+        ("num_wide_nodes", ctypes.c_uint64),
+        ("node_bytes", ctypes.c_uint64),
+        ("triangle_bytes", ctypes.c_uint64),
+        ("binary_depth", ctypes.c_int32),
+        ("wide_depth", ctypes.c_int32),
+        ("build_ms", ctypes.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class TraceStats(ctypes.Structure):
+    _fields_ = [
+        ("rays", ctypes.c_uint64),
+        ("node_fetches", ctypes.c_uint64),
+        ("triangle_fetches", ctypes.c_uint64),
+        ("hits", ctypes.c_uint64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Loads liblmgpu.so (built in-tree by lmgpu.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()')")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, u64, i32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int
+    L.lmgpu_version.restype = ctypes.c_char_p
+    L.lmgpu_last_error.restype = ctypes.c_char_p
+    L.lmgpu_accel_create.argtypes = [ctypes.POINTER(vp)]
+    L.lmgpu_accel_destroy.argtypes = [vp]
+    L.lmgpu_accel_destroy.restype = None
+    L.lmgpu_accel_build.argtypes = [vp, vp, u64]
+    L.lmgpu_accel_build_device.argtypes = [vp, vp, u64, vp]
+    L.lmgpu_accel_get_info.argtypes = [vp, ctypes.POINTER(AccelInfo)]
+    L.lmgpu_trace.argtypes = [vp, vp, vp, u64, i32]
+    L.lmgpu_trace_device.argtypes = [vp, vp, vp, u64, i32, vp]
+    L.lmgpu_trace_stats_device.argtypes = [vp, vp, vp, u64, i32, vp, ctypes.POINTER(TraceStats)]
+    L.lmgpu_accel_check.argtypes = [vp, vp]
+    for name in ("lmgpu_accel_create", "lmgpu_accel_build", "lmgpu_accel_build_device", "lmgpu_accel_get_info",
+                 "lmgpu_trace", "lmgpu_trace_device", "lmgpu_trace_stats_device", "lmgpu_accel_check"):
+        getattr(L, name).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def _check(rc: int) -> None:
+    if rc != LMGPU_OK:
+        raise LmgpuError(rc, lib().lmgpu_last_error().decode())
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class Accel:
+    """An accel::cuda instance: GPU-built binned-SAH BVH8 with watertight traversal."""
+
+    def __init__(self) -> None:
+        h = ctypes.c_void_p()
+        _check(lib().lmgpu_accel_create(ctypes.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().lmgpu_accel_destroy(self._h)
+            self._h = None
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def build(self, tris: np.ndarray) -> None:
+        t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+        _check(lib().lmgpu_accel_build(self._h, _ptr(t), t.shape[0]))
+
+    def build_device(self, d_tris_ptr: int, ntri: int, stream: int = 0) -> None:
+        _check(lib().lmgpu_accel_build_device(self._h, d_tris_ptr, ntri, stream))
+
+    def info(self) -> dict:
+        i = AccelInfo()
+        _check(lib().lmgpu_accel_get_info(self._h, ctypes.byref(i)))
+        return i.as_dict()
+
+    def trace(self, rays: np.ndarray, anyhit: bool = False, out: np.ndarray | None = None) -> np.ndarray:
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        if out is None:
+            out = np.empty(r.shape[0], dtype=HIT_DTYPE)
+        _check(lib().lmgpu_trace(self._h, _ptr(r), _ptr(out), r.shape[0], int(anyhit)))
+        return out
+
+    def trace_ptr(self, rays_ptr: int, hits_ptr: int, n: int, anyhit: bool = False) -> None:
+        """Host-pointer trace (pinned buffers from torch, for instance)."""
+        _check(lib().lmgpu_trace(self._h, rays_ptr, hits_ptr, n, int(anyhit)))
+
+    def trace_device(self, d_rays_ptr: int, d_hits_ptr: int, n: int, anyhit: bool = False, stream: int = 0) -> None:
+        _check(lib().lmgpu_trace_device(self._h, d_rays_ptr, d_hits_ptr, n, int(anyhit), stream))
+
+    def trace_stats_device(self, d_rays_ptr: int, d_hits_ptr: int, n: int, anyhit: bool = False,
+                           stream: int = 0) -> dict:
+        s = TraceStats()
+        _check(lib().lmgpu_trace_stats_device(self._h, d_rays_ptr, d_hits_ptr, n, int(anyhit), stream,
+                                              ctypes.byref(s)))
+        return s.as_dict()
+
+    def check(self, stream: int = 0) -> None:
+        _check(lib().lmgpu_accel_check(self._h, stream))
+
+
+def version() -> str:
+    return lib().lmgpu_version().decode()

@@ -1,0 +1,121 @@
+"""Seeded synthetic inputs for the ray-intersection workloads.
+
+All randomness comes from numpy's Philox counter-based generator, so a seed
+fixes the triangle soup and the ray set on one machine (transcendental
+functions may differ in the last bit between CPU architectures; tests always
+compare the GPU path and the oracle on inputs generated in the same process).
+
+Triangle arrays are float32 (N, 9): vertices p1, p2, p3 in global triangle
+order.  Ray arrays are float32 (N, 8): ox, oy, oz, tmin, dx, dy, dz, tmax.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+FLT_MAX = np.float32(np.finfo(np.float32).max)
+EPS_ISECT = np.float32(1e-4)  # Math::EpsIsect (math.h:1668), the camera/bounce ray tmin
+
+
+def rng(seed: int, stream: int = 0) -> np.random.Generator:
+    return np.random.Generator(np.random.Philox(key=[seed & 0xFFFFFFFFFFFFFFFF, stream]))
+
+
+def unit_vectors(g: np.random.Generator, n: int) -> np.ndarray:
+    """Directions uniform on the sphere (z = 1 - 2u, phi = 2 pi v)."""
+    u = g.random(n)
+    v = g.random(n)
+    z = 1.0 - 2.0 * u
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    phi = 2.0 * np.pi * v
+    return np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1)
+
+
+def random_soup(n: int, seed: int = 0x5EED, mu: float = np.log(0.005), sigma: float = 0.5) -> np.ndarray:
+    """n triangles with centroids uniform in [0,1]^3.
+
+    Each vertex sits at the centroid plus a random unit vector times a
+    lognormal(mu, sigma) length; the three offsets are re-centred so the
+    centroid is exact.  Edge lengths are then of order exp(mu).
+    """
+    g = rng(seed, 1)
+    c = g.random((n, 3))
+    off = np.empty((n, 3, 3))
+    for k in range(3):
+        L = np.exp(mu + sigma * g.standard_normal(n))
+        off[:, k, :] = unit_vectors(g, n) * L[:, None]
+    off -= off.mean(axis=1, keepdims=True)
+    tris = (c[:, None, :] + off).reshape(n, 9)
+    return tris.astype(np.float32)
+
+
+def heightfield(res: int = 512, seed: int = 0x5EED, amplitude: float = 0.05, base: float = 0.0) -> np.ndarray:
+    """res x res quads (2 * res^2 triangles) over [0,1]^2 in xz at height
+    y = base + sum of 4 seeded sinusoids whose amplitudes sum to `amplitude`."""
+    g = rng(seed, 2)
+    freqs = g.uniform(1.0, 6.0, size=(4, 2))
+    phases = g.uniform(0.0, 2.0 * np.pi, size=4)
+    amps = np.full(4, amplitude / 4.0)
+    xs = np.linspace(0.0, 1.0, res + 1)
+    X, Z = np.meshgrid(xs, xs, indexing="ij")
+    Y = np.full_like(X, base)
+    for i in range(4):
+        Y += amps[i] * np.sin(2.0 * np.pi * (freqs[i, 0] * X + freqs[i, 1] * Z) + phases[i])
+    P = np.stack([X, Y, Z], axis=-1)  # (res+1, res+1, 3)
+    p00 = P[:-1, :-1].reshape(-1, 3)
+    p10 = P[1:, :-1].reshape(-1, 3)
+    p11 = P[1:, 1:].reshape(-1, 3)
+    p01 = P[:-1, 1:].reshape(-1, 3)
+    t1 = np.concatenate([p00, p01, p11], axis=1)
+    t2 = np.concatenate([p00, p11, p10], axis=1)
+    tris = np.stack([t1, t2], axis=1).reshape(-1, 9)
+    return tris.astype(np.float32)
+
+
+def raycast_scene(n_random: int = 1_000_000, hf_res: int = 512, seed: int = 0x5EED) -> np.ndarray:
+    """BVH ray-cast benchmark scene: random soup then heightfield (global order)."""
+    return np.concatenate([random_soup(n_random, seed), heightfield(hf_res, seed)], axis=0)
+
+
+def raycast_rays(n: int, seed: int = 0x5EED, lo: float = -0.1, hi: float = 1.1,
+                 tmin: float = 1e-4, tmax: float = float(FLT_MAX), stream: int = 3) -> np.ndarray:
+    """n rays: origins uniform in [lo,hi]^3, directions uniform on the sphere."""
+    g = rng(seed, stream)
+    o = g.uniform(lo, hi, size=(n, 3))
+    d = unit_vectors(g, n)
+    r = np.empty((n, 8), dtype=np.float32)
+    r[:, 0:3] = o
+    r[:, 3] = np.float32(tmin)
+    r[:, 4:7] = d
+    r[:, 7] = np.float32(tmax)
+    return r
+
+
+def closed_icosphere(level: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Closed, consistently wound icosphere (20 * 4^level triangles)."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    V = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    F = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+         (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(v, dtype=np.float64) / np.linalg.norm(v) for v in V]
+    faces = list(F)
+    for _ in range(level):
+        cache: dict = {}
+
+        def mid(a: int, b: int) -> int:
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    Vn = np.array(verts) * radius + np.asarray(center, dtype=np.float64)
+    Fn = np.array(faces)
+    return Vn[Fn].reshape(-1, 9).astype(np.float32)

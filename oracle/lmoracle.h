@@ -1,0 +1,70 @@
+/*
+ * CPU oracle for the ray-intersection and path-sampling hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the
+ * reference's CPU algorithms, used by tests/ as the checker and by bench.py
+ * as the timed CPU baseline.  The product (the CUDA library behind
+ * include/lmgpu.h) never links, loads or calls it.
+ *
+ * Every function names the reference file:line it restates.  Floating-point
+ * expressions keep the reference's operation order and are compiled with
+ * -ffp-contract=off, so that results are bit-identical to the reference
+ * compiled from its own sources (checked against fixtures in tests/golden/).
+ */
+#ifndef LMORACLE_H
+#define LMORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* TriAccelTriangle (include/lightmetrica/triaccel.h:35-48). */
+typedef struct {
+    uint32_t k;
+    float n_u, n_v, n_d;
+    float a_u, a_v;
+    float b_nu, b_nv;
+    float c_nu, c_nv;
+    uint32_t face_index;
+    uint32_t prim_index;
+} lmo_triaccel;
+
+/* One hit record, shared by every trace routine of the oracle.
+ * id = global triangle id or -1; b = barycentrics weighting vertices 2, 3;
+ * p = ray.o + ray.d * t, the point the reference stores (accel_naive.cpp:118). */
+typedef struct {
+    int32_t id;
+    float t;
+    float b0, b1;
+    float p[3];
+} lmo_hit;
+
+/* Ray layout of the C-ABI: ox, oy, oz, tmin, dx, dy, dz, tmax (32 bytes). */
+
+int  lmo_triaccel_load(lmo_triaccel* tri, const float A[3], const float B[3], const float C[3]);
+int  lmo_triaccel_intersect(const lmo_triaccel* tri, const float o[3], const float d[3],
+                            float mint, float maxt, float* u, float* v, float* t);
+
+/* Opaque accel built over `ntri` triangles given as 9 floats each
+ * (v1, v2, v3 in global triangle order). */
+typedef struct lmo_accel lmo_accel;
+
+/* kind: 0 = accel::naive (accel_naive.cpp), 1 = accel::bvh_sahbin (accel_bvh_sahbin.cpp) */
+lmo_accel* lmo_accel_build(int kind, const float* tris, size_t ntri);
+void       lmo_accel_free(lmo_accel* a);
+/* Closest hit for n rays using `threads` POSIX threads. */
+void       lmo_accel_trace(const lmo_accel* a, const float* rays, size_t n, lmo_hit* out, int threads);
+/* Counts of the binary BVH (bvh_sahbin only): nodes, leaves, max depth. */
+void       lmo_accel_stats(const lmo_accel* a, size_t* nodes, size_t* leaves, int* depth);
+
+/* FP64 recomputation of the ray parameter t at which the ray meets the plane
+ * of triangle `tri` (9 floats), and of its barycentrics (b1, b2). */
+double     lmo_plane_t_fp64(const float* tri, const float* ray, double* b1, double* b2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

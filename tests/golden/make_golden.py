@@ -1,0 +1,172 @@
+"""Generates the golden fixtures of tests/golden/ from the reference itself.
+
+Run in a checkout that has the reference tree (default /root/reference) and
+the reference harness built by oracle/build_ref.sh (oracle/_ref/ref_accel):
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+
+Fixtures written:
+  accel3_simple.npz, accel3_simple2.npz
+      The two meshes of the reference's accel test (read from
+      src/lightmetrica-test/test_accel3.cpp), its 9x9 ray grids with
+      directions normalised by the reference's own Math::Normalize, the
+      expected values that test asserts (p, gn, sn, uv), and the hits of the
+      reference accels naive / bvh_sahbin / qbvh on those rays.
+  soup_small.npz
+      A seeded three-primitive scene (random triangle soup, heightfield,
+      duplicated triangles for exact-t ties, zero-area triangles) and rays
+      (random, axis-aligned, and finite segments), with the hits of the
+      reference accels.
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+sys.path.insert(0, os.path.join(REPO, "lightmetrica-v2_gb300"))
+
+import lmoracle as lo  # noqa: E402
+from lmgpu import scenes  # noqa: E402
+
+FLT_MAX = np.float32(np.finfo(np.float32).max)
+ACCELS = ["accel::naive", "accel::bvh_sahbin", "accel::qbvh"]
+
+
+def parse_mesh(src: str, cls: str) -> dict:
+    """Reads the ps/ns/ts/fs initialisers of one stub mesh class."""
+    start = src.index(f"class {cls} ")
+    body = src[start:src.index("};\n\nclass", start) if "};\n\nclass" in src[start:] else len(src)]
+    out = {}
+    for name in ("ps", "ns", "ts", "fs"):
+        m = re.search(r"std::vector<(?:Float|unsigned int)> " + name + r"\{([^}]*)\}", body)
+        vals = [v.strip().replace("_f", "") for v in m.group(1).replace("\n", " ").split(",") if v.strip()]
+        out[name] = np.array([float(v) for v in vals], dtype=np.float32 if name != "fs" else np.float64)
+    out["fs"] = out["fs"].astype(np.uint32)
+    return out
+
+
+def ref_normalize(vs: np.ndarray, tmp: str) -> np.ndarray:
+    vs = np.ascontiguousarray(vs, dtype=np.float32).reshape(-1, 3)
+    pin, pout = os.path.join(tmp, "nin.bin"), os.path.join(tmp, "nout.bin")
+    with open(pin, "wb") as f:
+        f.write(np.uint32(vs.shape[0]).tobytes())
+        f.write(vs.tobytes())
+    subprocess.run([lo.REF_ACCEL, "--normalize", pin, pout], check=True)
+    return np.fromfile(pout, dtype=np.float32).reshape(-1, 3)
+
+
+def run_ref(meshes: list, rays: np.ndarray, tmp: str) -> dict:
+    ps, pr = os.path.join(tmp, "scene.bin"), os.path.join(tmp, "rays.bin")
+    lo.write_ref_inputs(ps, pr, meshes, rays)
+    res = {}
+    for key in ACCELS:
+        po = os.path.join(tmp, "out.bin")
+        subprocess.run([lo.REF_ACCEL, key, ps, pr, po, "8"], check=True, capture_output=True)
+        o = lo.read_ref_output(po)
+        tag = key.split("::")[1]
+        res[f"{tag}_id"] = o["id"]
+        res[f"{tag}_p"] = o["p"]
+        res[f"{tag}_b"] = o["b"]
+    return res
+
+
+def accel3_case(src: str, cls: str, simple2: bool, tmp: str) -> dict:
+    mesh = parse_mesh(src, cls)
+    tris = mesh["ps"].reshape(-1, 3)[mesh["fs"].reshape(-1, 3)].reshape(-1, 9)
+    steps = 10
+    delta = np.float32(1.0) / np.float32(steps)
+    rays, exp_p, exp_gn, exp_uv = [], [], [], []
+    raw_dirs = []
+    for i in range(1, steps):
+        y = np.float32(delta * np.float32(i))
+        for j in range(1, steps):
+            x = np.float32(delta * np.float32(j))
+            if simple2:
+                o = np.array([x, y, 1], dtype=np.float32)
+                raw_dirs.append(None)
+                rays.append(np.array([o[0], o[1], o[2], 0, 0, 0, -1, FLT_MAX], dtype=np.float32))
+                exp_p.append([x, y, -x])
+            else:
+                o = np.array([0, 0, 1], dtype=np.float32)
+                raw_dirs.append(np.array([x, y, 0], dtype=np.float32) - o)
+                rays.append(np.array([0, 0, 1, 0, 0, 0, 0, FLT_MAX], dtype=np.float32))
+                exp_p.append([x, y, 0])
+            exp_uv.append([x, y])
+    rays = np.array(rays, dtype=np.float32)
+    if not simple2:
+        d = ref_normalize(np.array(raw_dirs), tmp)
+        rays[:, 4:7] = d
+        n = np.array([0, 0, 1], dtype=np.float32)
+    else:
+        n = ref_normalize(np.array([[1, 0, 1]], dtype=np.float32), tmp)[0]
+    exp_gn = np.tile(n, (rays.shape[0], 1))
+    out = dict(positions=mesh["ps"], normals=mesh["ns"], texcoords=mesh["ts"], faces=mesh["fs"], tris=tris,
+               rays=rays, expected_p=np.array(exp_p, dtype=np.float32), expected_gn=exp_gn,
+               expected_sn=exp_gn.copy(), expected_uv=np.array(exp_uv, dtype=np.float32),
+               tolerance=np.float32(1e-3))
+    out.update(run_ref([tris], rays, tmp))
+    return out
+
+
+def soup_case(tmp: str) -> dict:
+    g = scenes.rng(0xC0FFEE, 7)
+    soup = scenes.random_soup(3000, seed=0xC0FFEE, mu=np.log(0.03))
+    hf = scenes.heightfield(24, seed=0xC0FFEE, amplitude=0.1, base=0.3)
+    dup_src = soup[g.choice(soup.shape[0], 16, replace=False)]
+    degenerate = np.array([
+        [0.2, 0.2, 0.2, 0.2, 0.2, 0.2, 0.2, 0.2, 0.2],      # a point
+        [0.1, 0.5, 0.5, 0.3, 0.5, 0.5, 0.6, 0.5, 0.5],      # collinear
+        [0.5, 0.1, 0.5, 0.5, 0.4, 0.5, 0.5, 0.9, 0.5],      # collinear
+        [0.7, 0.7, 0.1, 0.7, 0.7, 0.1, 0.7, 0.7, 0.9],      # two equal vertices
+    ], dtype=np.float32)
+    extra = np.concatenate([dup_src, degenerate], axis=0)
+    meshes = [soup, hf, extra]
+    r_rand = scenes.raycast_rays(3072, seed=0xC0FFEE, stream=9)
+    # axis-aligned rays (zero direction components)
+    o = g.uniform(-0.1, 1.1, size=(512, 3)).astype(np.float32)
+    axis = g.integers(0, 3, size=512)
+    sign = np.where(g.random(512) < 0.5, -1.0, 1.0)
+    d = np.zeros((512, 3), dtype=np.float32)
+    d[np.arange(512), axis] = sign
+    r_axis = np.concatenate([o, np.full((512, 1), 1e-4, np.float32), d, np.full((512, 1), FLT_MAX, np.float32)], 1)
+    # finite segments (shadow-ray style [1e-4, L(1 - 1e-4)])
+    a = g.uniform(0.0, 1.0, size=(512, 3))
+    b = g.uniform(0.0, 1.0, size=(512, 3))
+    L = np.linalg.norm(b - a, axis=1)
+    dd = (b - a) / L[:, None]
+    r_seg = np.concatenate([a, np.full((512, 1), 1e-4), dd, (L * (1 - 1e-4))[:, None]], 1).astype(np.float32)
+    # rays aimed exactly at the duplicated triangles' centroids (exact ties)
+    cen = dup_src.reshape(-1, 3, 3).mean(axis=1)
+    src = cen + np.array([0.0, 0.0, 0.5])
+    dt = (cen - src) / np.linalg.norm(cen - src, axis=1, keepdims=True)
+    r_tie = np.concatenate([src, np.full((16, 1), 1e-4), dt, np.full((16, 1), FLT_MAX)], 1).astype(np.float32)
+    rays = np.concatenate([r_rand, r_axis, r_seg, r_tie], axis=0).astype(np.float32)
+    out = dict(mesh_sizes=np.array([m.shape[0] for m in meshes], dtype=np.int64),
+               tris=np.concatenate(meshes, axis=0), rays=rays,
+               groups=np.array([3072, 512, 512, 16], dtype=np.int64))
+    out.update(run_ref(meshes, rays, tmp))
+    return out
+
+
+def main() -> None:
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if not os.path.exists(lo.REF_ACCEL):
+        subprocess.run([os.path.join(REPO, "oracle", "build_ref.sh"), ref], check=True)
+    src = open(os.path.join(ref, "src", "lightmetrica-test", "test_accel3.cpp")).read()
+    with tempfile.TemporaryDirectory() as tmp:
+        np.savez_compressed(os.path.join(HERE, "accel3_simple.npz"), **accel3_case(src, "StubTriangleMesh_Simple", False, tmp))
+        np.savez_compressed(os.path.join(HERE, "accel3_simple2.npz"), **accel3_case(src, "StubTriangleMesh_Simple2", True, tmp))
+        np.savez_compressed(os.path.join(HERE, "soup_small.npz"), **soup_case(tmp))
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,223 @@
+"""Parity of accel::cuda (the GPU BVH build + traversal behind the C ABI)
+with the reference's accels, on the GPU.
+
+Levels checked:
+  * the reference's own accel test (Accel3Test.Simple / Simple2,
+    src/lightmetrica-test/test_accel3.cpp:272-345): p, gn, sn, uv within 1e-3;
+  * fixtures of the compiled reference accels: the same global triangle id
+    on every ray outside the documented disagreement classes (tests/hitcheck.py),
+    t within 1e-5 relative of an FP64 recomputation;
+  * seeded scenes against the oracle at sizes it finishes in seconds;
+  * size-independent properties at the benchmark size (1.52M triangles,
+    16.8M rays): any-hit flags equal closest-hit flags, a seeded subsample
+    agrees with the oracle, hit t >= tmin.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import hitcheck
+
+pytestmark = pytest.mark.gpu
+
+T_REL_TOL = 1e-5  # hit t vs FP64 recomputation, relative
+
+
+def load(golden_dir, name):
+    return dict(np.load(os.path.join(golden_dir, name + ".npz")))
+
+
+def gpu_trace(gpu_lib, tris, rays, anyhit=False):
+    acc = gpu_lib.Accel()
+    acc.build(tris)
+    h = acc.trace(rays, anyhit=anyhit)
+    info = acc.info()
+    acc.close()
+    return h, info
+
+
+def check_t(tris, rays, h):
+    import lmoracle as lo
+
+    hit = np.nonzero(h["prim"] >= 0)[0]
+    if len(hit) == 0:
+        return
+    t64 = lo.t_fp64(tris, rays[hit], h["prim"][hit])
+    rel = np.abs(h["t"][hit].astype(np.float64) - t64) / np.maximum(np.abs(t64), 1e-30)
+    # grazing hits make the plane parameter ill-conditioned; exclude them
+    N = hitcheck.tri_normals(tris)[h["prim"][hit]]
+    D = rays[hit][:, 4:7].astype(np.float64)
+    cosang = np.abs(np.einsum("ij,ij->i", N, D)) / (np.linalg.norm(N, axis=1) * np.linalg.norm(D, axis=1))
+    ok = cosang > 1e-3
+    assert rel[ok].max() <= T_REL_TOL, rel[ok].max()
+
+
+@pytest.mark.parametrize("case", ["accel3_simple", "accel3_simple2"])
+def test_accel3_reference_test(gpu_lib, golden_dir, case):
+    z = load(golden_dir, case)
+    h, _ = gpu_trace(gpu_lib, z["tris"], z["rays"])
+    tol = float(z["tolerance"])
+    assert (h["prim"] >= 0).all()
+    for i in range(len(h)):
+        r = z["rays"][i]
+        p, gn, sn, uv = hitcheck.hit_geometry(z["positions"], z["normals"], z["texcoords"], z["faces"],
+                                              int(h["prim"][i]), float(h["b1"][i]), float(h["b2"][i]),
+                                              r[0:3], r[4:7], float(h["t"][i]))
+        assert np.allclose(p, z["expected_p"][i], atol=tol), (i, p)
+        assert np.allclose(gn, z["expected_gn"][i], atol=tol)
+        assert np.allclose(sn, z["expected_sn"][i], atol=tol)
+        assert np.allclose(uv, z["expected_uv"][i], atol=tol)
+
+
+def test_soup_fixture_vs_reference_naive(gpu_lib, golden_dir):
+    z = load(golden_dir, "soup_small")
+    h, info = gpu_trace(gpu_lib, z["tris"], z["rays"])
+    c = hitcheck.classify(z["tris"], z["rays"], h["prim"], z["naive_id"])
+    print("classes", {k: v for k, v in c.items() if k != "unexplained"}, info)
+    assert c["unexplained"] == [], c
+    check_t(z["tris"], z["rays"], h)
+    # exact-t ties (duplicated triangles) resolve to the higher id, as naive does
+    ntie = int(z["groups"][-1])
+    tie_rays = slice(len(z["rays"]) - ntie, None)
+    same = h["prim"][tie_rays] == z["naive_id"][tie_rays]
+    assert same.all()
+
+
+def test_soup_fixture_barycentrics(gpu_lib, golden_dir):
+    z = load(golden_dir, "soup_small")
+    h, _ = gpu_trace(gpu_lib, z["tris"], z["rays"])
+    agree = (h["prim"] == z["naive_id"]) & (h["prim"] >= 0)
+    assert np.allclose(h["b1"][agree], z["naive_b"][agree, 0], atol=1e-4)
+    assert np.allclose(h["b2"][agree], z["naive_b"][agree, 1], atol=1e-4)
+    p = z["rays"][agree][:, 0:3] + z["rays"][agree][:, 4:7] * h["t"][agree][:, None]
+    assert np.allclose(p, z["naive_p"][agree], atol=1e-5)
+
+
+@pytest.mark.parametrize("ntri", [0, 1, 2, 3, 4, 17, 1025, 5000])
+def test_small_and_edge_sizes(gpu_lib, oracle_lib, ntri):
+    from lmgpu import scenes
+
+    tris = scenes.random_soup(max(ntri, 1), seed=1234 + ntri, mu=np.log(0.2))[:ntri]
+    rays = scenes.raycast_rays(4096, seed=99 + ntri)
+    h, _ = gpu_trace(gpu_lib, tris, rays)
+    ref = oracle_lib.OracleAccel(0, tris).trace(rays, threads=8)
+    c = hitcheck.classify(tris, rays, h["prim"], ref["id"])
+    assert c["unexplained"] == [], c
+
+
+def test_medium_scene_vs_oracle(gpu_lib, oracle_lib):
+    from lmgpu import scenes
+
+    tris = scenes.raycast_scene(200_000, 128, seed=77)
+    rays = scenes.raycast_rays(1 << 16, seed=78)
+    h, info = gpu_trace(gpu_lib, tris, rays)
+    ref = oracle_lib.OracleAccel(1, tris).trace(rays, threads=16)
+    c = hitcheck.classify(tris, rays, h["prim"], ref["id"])
+    print("classes", {k: v for k, v in c.items() if k != "unexplained"}, info)
+    assert len(c["unexplained"]) <= 1e-5 * len(rays), c
+    check_t(tris, rays, h)
+
+
+def test_watertight_closed_mesh(gpu_lib):
+    """Rays from inside a closed icosphere always hit it (no leaks through
+    shared edges or vertices), including rays aimed exactly at vertices."""
+    from lmgpu import scenes
+
+    tris = scenes.closed_icosphere(4, radius=0.5, center=(0.5, 0.5, 0.5))
+    g = scenes.rng(5, 5)
+    n = 1 << 16
+    o = 0.5 + g.uniform(-0.2, 0.2, size=(n, 3))
+    d = scenes.unit_vectors(g, n)
+    # aim a quarter of the rays exactly at mesh vertices
+    V = tris.reshape(-1, 3).astype(np.float64)
+    k = n // 4
+    tgt = V[g.integers(0, V.shape[0], size=k)]
+    d[:k] = (tgt - o[:k]) / np.linalg.norm(tgt - o[:k], axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = o
+    rays[:, 3] = 0.0
+    rays[:, 4:7] = d
+    rays[:, 7] = np.finfo(np.float32).max
+    h, _ = gpu_trace(gpu_lib, tris, rays)
+    assert (h["prim"] >= 0).all(), int((h["prim"] < 0).sum())
+
+
+def test_anyhit_matches_closest_flags(gpu_lib, golden_dir):
+    z = load(golden_dir, "soup_small")
+    acc = gpu_lib.Accel()
+    acc.build(z["tris"])
+    hc = acc.trace(z["rays"])
+    ha = acc.trace(z["rays"], anyhit=True)
+    assert np.array_equal(hc["prim"] >= 0, ha["prim"] >= 0)
+    # the any-hit triangle is a genuine hit within the ray's range
+    hit = ha["prim"] >= 0
+    assert (ha["t"][hit] >= z["rays"][hit, 3]).all() and (ha["t"][hit] <= z["rays"][hit, 7]).all()
+
+
+def test_device_entry_matches_host_entry(gpu_lib):
+    import torch
+    from lmgpu import scenes
+
+    tris = scenes.raycast_scene(50_000, 64, seed=3)
+    rays = scenes.raycast_rays(100_000, seed=4)
+    acc = gpu_lib.Accel()
+    dt = torch.from_numpy(tris).cuda()
+    acc.build_device(dt.data_ptr(), tris.shape[0], torch.cuda.current_stream().cuda_stream)
+    h_host = acc.trace(rays)
+    dr = torch.from_numpy(rays).cuda()
+    dh = torch.empty((rays.shape[0], 4), dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    acc.trace_device(dr.data_ptr(), dh.data_ptr(), rays.shape[0], False, s)
+    acc.check(s)
+    hd = dh.cpu().numpy().view(gpu_lib.HIT_DTYPE).reshape(-1)
+    assert np.array_equal(hd["prim"], h_host["prim"])
+    assert np.array_equal(hd["t"], h_host["t"])
+    st = acc.trace_stats_device(dr.data_ptr(), dh.data_ptr(), rays.shape[0], False, s)
+    assert st["rays"] == rays.shape[0]
+    assert st["hits"] == int((h_host["prim"] >= 0).sum())
+    assert st["node_fetches"] > 0
+
+
+def test_deterministic_across_builds(gpu_lib):
+    from lmgpu import scenes
+
+    tris = scenes.raycast_scene(100_000, 64, seed=11)
+    rays = scenes.raycast_rays(200_000, seed=12)
+    h1, _ = gpu_trace(gpu_lib, tris, rays)
+    h2, _ = gpu_trace(gpu_lib, tris, rays)
+    assert np.array_equal(h1["prim"], h2["prim"])
+    assert np.array_equal(h1["t"], h2["t"])
+
+
+def test_benchmark_size_properties(gpu_lib, oracle_lib):
+    """The BVH ray-cast workload at full size: 1,524,288 triangles, 16,777,216 rays."""
+    import torch
+    from lmgpu import scenes
+
+    tris = scenes.raycast_scene()
+    n = 1 << 24
+    rays = scenes.raycast_rays(n)
+    acc = gpu_lib.Accel()
+    acc.build(tris)
+    info = acc.info()
+    assert info["num_triangles"] == tris.shape[0] == 1_524_288
+    s = torch.cuda.current_stream().cuda_stream
+    dr = torch.from_numpy(rays).cuda()
+    dh = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    da = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    acc.trace_device(dr.data_ptr(), dh.data_ptr(), n, False, s)
+    acc.trace_device(dr.data_ptr(), da.data_ptr(), n, True, s)
+    acc.check(s)
+    hc = dh.cpu().numpy().view(gpu_lib.HIT_DTYPE).reshape(-1)
+    ha = da.cpu().numpy().view(gpu_lib.HIT_DTYPE).reshape(-1)
+    assert np.array_equal(hc["prim"] >= 0, ha["prim"] >= 0)
+    hit = hc["prim"] >= 0
+    assert (hc["t"][hit] >= rays[hit, 3]).all()
+    # a seeded subsample against the oracle's binned-SAH BVH
+    sub = scenes.rng(2024, 1).choice(n, 1 << 15, replace=False)
+    ref = oracle_lib.OracleAccel(1, tris).trace(rays[sub], threads=16)
+    c = hitcheck.classify(tris, rays[sub], hc["prim"][sub], ref["id"])
+    print("classes", {k: v for k, v in c.items() if k != "unexplained"}, info)
+    assert len(c["unexplained"]) <= 1e-5 * len(sub) + 1, c
+    check_t(tris, rays[sub], hc[sub])
