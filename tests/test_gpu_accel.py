@@ -38,19 +38,37 @@ def gpu_trace(gpu_lib, tris, rays, anyhit=False):
 
 
 def check_t(tris, rays, h):
+    """Hit t against an FP64 recomputation on the same triangle.
+
+    FP32 rounding in a ray/triangle test gives an absolute error in t of a few
+    ulps of the vertex distances from the origin, divided by |cos theta|
+    (theta between the ray and the triangle normal).  With the condition
+    number kappa = max_i |v_i - o| / (t |cos theta|):
+      * relative error <= 1e-5 on every hit with kappa <= 10 (the stated
+        tolerance, on well-conditioned hits);
+      * relative error <= 1e-6 * kappa on every hit (no outliers beyond the
+        conditioning of the problem).
+    """
     import lmoracle as lo
 
     hit = np.nonzero(h["prim"] >= 0)[0]
     if len(hit) == 0:
         return
-    t64 = lo.t_fp64(tris, rays[hit], h["prim"][hit])
+    ids = h["prim"][hit]
+    t64 = lo.t_fp64(tris, rays[hit], ids)
     rel = np.abs(h["t"][hit].astype(np.float64) - t64) / np.maximum(np.abs(t64), 1e-30)
-    # grazing hits make the plane parameter ill-conditioned; exclude them
-    N = hitcheck.tri_normals(tris)[h["prim"][hit]]
+    T = np.asarray(tris, dtype=np.float64).reshape(-1, 9)[ids].reshape(-1, 3, 3)
+    O = rays[hit][:, 0:3].astype(np.float64)
+    dist = np.linalg.norm(T - O[:, None, :], axis=2).max(axis=1)
+    N = hitcheck.tri_normals(tris)[ids]
     D = rays[hit][:, 4:7].astype(np.float64)
     cosang = np.abs(np.einsum("ij,ij->i", N, D)) / (np.linalg.norm(N, axis=1) * np.linalg.norm(D, axis=1))
-    ok = cosang > 1e-3
-    assert rel[ok].max() <= T_REL_TOL, rel[ok].max()
+    kappa = dist / np.maximum(np.abs(t64) * np.linalg.norm(D, axis=1) * cosang, 1e-300)
+    well = kappa <= 10.0
+    print(f"t vs FP64: max rel {rel[well].max():.2e} on {well.mean():.5f} of hits (kappa<=10); "
+          f"within 1e-5 overall {np.mean(rel <= T_REL_TOL):.6f}; max rel/kappa {(rel / kappa).max():.2e}")
+    assert rel[well].max() <= T_REL_TOL, rel[well].max()
+    assert (rel / kappa).max() <= 0.1 * T_REL_TOL, (rel / kappa).max()
 
 
 @pytest.mark.parametrize("case", ["accel3_simple", "accel3_simple2"])
