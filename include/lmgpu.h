@@ -114,6 +114,28 @@ int lmgpu_trace_stats_device(const lmgpu_accel* accel, const float* d_rays, lmgp
  * raised by earlier asynchronous launches. */
 int lmgpu_accel_check(const lmgpu_accel* accel, void* stream);
 
+/* Largest scene lmgpu_trace_static_scene accepts. */
+#define LMGPU_STATIC_MAX_TRIANGLES 16384
+
+/* Builds the BVH of d_triangles (float[ntri*9], device) and traces d_rays
+ * (float[nrays*8], device) against it, writing d_hits (device), closest hit
+ * (anyhit = 0) or any hit (anyhit = 1) -- without allocating device memory.
+ * No counterpart in the reference: it exists for callers that cannot
+ * allocate (a plugin inside a host that owns all device memory through its
+ * own pool, or a query path that must not incur the device-wide
+ * synchronisation of cudaMalloc/cudaFree).  All scratch, including the BVH,
+ * is one fixed library-owned device array of about 5.2 MiB, reserved on
+ * every device that loads the library until the process exits; scenes
+ * above LMGPU_STATIC_MAX_TRIANGLES are rejected with LMGPU_ERR_INVALID.
+ * The first call on a device looks up that array's address (set-up), so
+ * make it before any stream capture.  Every call shares the array and it
+ * keeps the previous call's contents: calls that overlap on the GPU (other
+ * host threads or streams) race and must be serialised by the caller.
+ * Synchronises `stream` before returning.  Results equal those of
+ * lmgpu_accel_build_device + lmgpu_trace_device on the same inputs. */
+int lmgpu_trace_static_scene(const float* d_triangles, uint64_t ntri, const float* d_rays, lmgpu_hit* d_hits,
+                             uint64_t nrays, int anyhit, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

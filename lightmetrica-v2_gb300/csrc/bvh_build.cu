@@ -1174,3 +1174,267 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
 }
 
 }  // namespace lmgpu
+
+// ===========================================================================
+// Allocation-free build + trace (lmgpu_trace_static_scene).
+//
+// Some callers cannot allocate device memory: code running while another
+// component owns every allocation (a renderer plugin inside a host that
+// sub-allocates HBM from its own pool), or code that must not trigger the
+// device-wide synchronisation cudaMalloc/cudaFree imply (a per-thread query
+// path called from many host workers at once).  For them, every piece of
+// scratch this path needs -- the build's bins, task lists and index arrays,
+// the binary tree, and the wide BVH itself -- lives in one file-scope device
+// array of fixed size, reserved when the library is loaded on a device and
+// held until the process exits.  The caller passes only inputs (triangles,
+// rays) and outputs (hits).
+namespace lmgpu {
+namespace {
+
+constexpr int kStaticTris = LMGPU_STATIC_MAX_TRIANGLES;
+constexpr int kSLarge = kStaticTris / kSmallTask * 2 + 2;
+constexpr int kSChunks = kStaticTris / kChunk + kSLarge + 1;
+constexpr int kSNodes = 2 * kStaticTris + 1;
+constexpr int kSWide = kStaticTris + 1;
+
+constexpr size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Byte offsets of each region inside the static array.
+struct StaticLayout {
+    size_t aabb, idx, idx_alt, counters, root, bnodes, tasks_a, tasks_b, small, dec, bins, chunk_off, chunk_left,
+        chunk_left_off, qa, qb, ccount, wnodes, wtris, status, total;
+};
+
+constexpr StaticLayout make_static_layout()
+{
+    StaticLayout L{};
+    size_t o = 0;
+    L.aabb = o;           o += al256(sizeof(float4) * 2 * kStaticTris);
+    L.idx = o;            o += al256(sizeof(int32_t) * kStaticTris);
+    L.idx_alt = o;        o += al256(sizeof(int32_t) * kStaticTris);
+    L.counters = o;       o += al256(sizeof(int32_t) * 8);
+    L.root = o;           o += al256(sizeof(uint32_t) * 12);
+    L.bnodes = o;         o += al256(sizeof(BNode) * kSNodes);
+    L.tasks_a = o;        o += al256(sizeof(Task) * kSLarge);
+    L.tasks_b = o;        o += al256(sizeof(Task) * kSLarge);
+    L.small = o;          o += al256(sizeof(Task) * kStaticTris);
+    L.dec = o;            o += al256(sizeof(Decision) * kSLarge);
+    L.bins = o;           o += al256(sizeof(uint32_t) * kSLarge * 3 * kBinsLarge * kBinWords);
+    L.chunk_off = o;      o += al256(sizeof(int32_t) * (kSLarge + 1));
+    L.chunk_left = o;     o += al256(sizeof(int32_t) * kSChunks);
+    L.chunk_left_off = o; o += al256(sizeof(int32_t) * kSChunks);
+    L.qa = o;             o += al256(sizeof(CollapseItem) * kSWide);
+    L.qb = o;             o += al256(sizeof(CollapseItem) * kSWide);
+    L.ccount = o;         o += al256(sizeof(int32_t) * 4);
+    L.wnodes = o;         o += al256(sizeof(WNode) * kSWide);
+    L.wtris = o;          o += al256(sizeof(WTri) * kStaticTris);
+    L.status = o;         o += al256(sizeof(uint32_t));
+    L.total = o;
+    return L;
+}
+
+constexpr StaticLayout kSL = make_static_layout();
+
+}  // namespace
+}  // namespace lmgpu
+
+// The scratch itself (about 5.2 MiB for 16,384 triangles).  Host code must
+// not pass this name to a kernel: on the host it is only a stand-in symbol.
+static __device__ __align__(256) unsigned char g_static_scratch[lmgpu::kSL.total];
+
+namespace lmgpu {
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+unsigned char* g_static_base[kMaxDevices] = {};
+
+// Device address of g_static_scratch on the current device, looked up once
+// per device (the first call on a device does this set-up).
+int static_scratch_base(unsigned char** out)
+{
+    int dev = 0;
+    LMGPU_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("lmgpu_trace_static_scene: device index out of range");
+        return LMGPU_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_base[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            set_error(std::string("lmgpu_trace_static_scene: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            return LMGPU_ERR_CUDA;
+        }
+        g_static_base[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_static_base[dev];
+    return LMGPU_OK;
+}
+
+// The build of build_bvh, run on buffers carved from the static scratch.
+// Writes the wide BVH into the scratch and returns the number of wide nodes.
+int build_static(unsigned char* base, const float* d_tris, int n, cudaStream_t stream, uint64_t* num_wide)
+{
+    float4* aabb = reinterpret_cast<float4*>(base + kSL.aabb);
+    int32_t* idx = reinterpret_cast<int32_t*>(base + kSL.idx);
+    int32_t* idx_alt = reinterpret_cast<int32_t*>(base + kSL.idx_alt);
+    int32_t* counters = reinterpret_cast<int32_t*>(base + kSL.counters);
+    uint32_t* root = reinterpret_cast<uint32_t*>(base + kSL.root);
+    BNode* bnodes = reinterpret_cast<BNode*>(base + kSL.bnodes);
+    Task* tasks_a = reinterpret_cast<Task*>(base + kSL.tasks_a);
+    Task* tasks_b = reinterpret_cast<Task*>(base + kSL.tasks_b);
+    Task* small_tasks = reinterpret_cast<Task*>(base + kSL.small);
+    Decision* dec = reinterpret_cast<Decision*>(base + kSL.dec);
+    uint32_t* bins = reinterpret_cast<uint32_t*>(base + kSL.bins);
+    int32_t* chunk_off = reinterpret_cast<int32_t*>(base + kSL.chunk_off);
+    int32_t* chunk_left = reinterpret_cast<int32_t*>(base + kSL.chunk_left);
+    int32_t* chunk_left_off = reinterpret_cast<int32_t*>(base + kSL.chunk_left_off);
+    CollapseItem* qa = reinterpret_cast<CollapseItem*>(base + kSL.qa);
+    CollapseItem* qb = reinterpret_cast<CollapseItem*>(base + kSL.qb);
+    int32_t* ccount = reinterpret_cast<int32_t*>(base + kSL.ccount);
+    WNode* wnodes = reinterpret_cast<WNode*>(base + kSL.wnodes);
+    WTri* wtris = reinterpret_cast<WTri*>(base + kSL.wtris);
+    uint32_t* status = reinterpret_cast<uint32_t*>(base + kSL.status);
+    const int max_nodes = 2 * n + 1;
+    const int max_chunks = n / kChunk + kSLarge + 1;
+
+    // Every region that must start from a known value is reset here: the
+    // scratch keeps whatever the previous call left in it.
+    uint32_t root_init[12];
+    for (int i = 0; i < 12; i++) root_init[i] = (i % 6) < 3 ? ordered_pos_max() : ordered_neg_max();
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(root, root_init, sizeof(root_init), cudaMemcpyHostToDevice, stream));
+    LMGPU_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(uint32_t), stream));
+    LMGPU_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(int32_t) * 8, stream));
+    k_prep<<<(n + 255) / 256, 256, 0, stream>>>(d_tris, (uint64_t)n, aabb, idx, root);
+    k_init_root<<<1, 1, 0, stream>>>(root, (uint64_t)n, bnodes, tasks_a, small_tasks, counters);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+
+    int ntasks = n > kSmallTask ? 1 : 0;
+    Task* cur = tasks_a;
+    Task* nxt = tasks_b;
+    while (ntasks > 0) {
+        if (ntasks > kSLarge) {
+            set_error("lmgpu_trace_static_scene: large-task list overflow");
+            return LMGPU_ERR_OVERFLOW;
+        }
+        const int grid = std::min(max_chunks, n / kChunk + ntasks + 1);
+        k_init_bins<<<std::min(1024, (ntasks * 3 * kBinsLarge * kBinWords + 255) / 256), 256, 0, stream>>>(bins, ntasks);
+        k_chunk_offsets<<<1, 1024, 0, stream>>>(cur, ntasks, chunk_off);
+        k_bin_large<<<grid, kLargeThreads, 0, stream>>>(cur, ntasks, chunk_off, idx, aabb, bins);
+        LMGPU_CUDA_TRY(cudaMemsetAsync(counters + 1, 0, sizeof(int32_t), stream));
+        k_split_large<<<ntasks, 32, 0, stream>>>(cur, ntasks, bins, bnodes, dec, nxt, small_tasks, counters, max_nodes,
+                                                 status);
+        k_part_count<<<grid, kLargeThreads, 0, stream>>>(cur, ntasks, chunk_off, dec, idx, aabb, chunk_left);
+        k_part_scan<<<(ntasks + 127) / 128, 128, 0, stream>>>(cur, ntasks, chunk_off, chunk_left, chunk_left_off);
+        k_part_scatter<<<grid, kLargeThreads, 0, stream>>>(cur, ntasks, chunk_off, dec, chunk_left_off, idx, aabb,
+                                                           idx_alt, status);
+        k_copy_back<<<grid, kLargeThreads, 0, stream>>>(cur, ntasks, chunk_off, idx_alt, idx);
+        LMGPU_CUDA_TRY(cudaGetLastError());
+        int32_t next = 0;
+        uint32_t lst = 0;
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(&next, counters + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(&lst, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+        if (lst & kStatusBuildOverflow) {
+            set_error("lmgpu_trace_static_scene: partition or node bound exceeded");
+            return LMGPU_ERR_OVERFLOW;
+        }
+        ntasks = next;
+        std::swap(cur, nxt);
+    }
+    int32_t hc[4];
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, stream));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (hc[2] > 0) {
+        k_build_small<<<hc[2], kSmallThreads, 0, stream>>>(small_tasks, aabb, idx, bnodes, counters, max_nodes, status);
+        LMGPU_CUDA_TRY(cudaGetLastError());
+    }
+    const CollapseItem root_item{0, 0};
+    const int32_t cinit[4] = {1, 0, 0, 0};
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(qa, &root_item, sizeof(root_item), cudaMemcpyHostToDevice, stream));
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(ccount, cinit, sizeof(cinit), cudaMemcpyHostToDevice, stream));
+    uint32_t st = 0;
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(&st, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (st & kStatusBuildOverflow) {
+        set_error("lmgpu_trace_static_scene: node or stack bound exceeded in the small phase");
+        return LMGPU_ERR_OVERFLOW;
+    }
+    int nin = 1;
+    while (nin > 0) {
+        LMGPU_CUDA_TRY(cudaMemsetAsync(ccount + 2, 0, sizeof(int32_t), stream));
+        k_collapse<<<(nin + 127) / 128, 128, 0, stream>>>(qa, nin, qb, bnodes, idx, d_tris, wnodes, wtris, ccount, kSWide,
+                                                         status);
+        LMGPU_CUDA_TRY(cudaGetLastError());
+        int32_t next = 0;
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(&next, ccount + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+        LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+        nin = next;
+        std::swap(qa, qb);
+    }
+    int32_t cc[4];
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(cc, ccount, sizeof(cc), cudaMemcpyDeviceToHost, stream));
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(&st, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    if ((st & kStatusBuildOverflow) || cc[1] != n) {
+        set_error("lmgpu_trace_static_scene: collapse bound exceeded");
+        return LMGPU_ERR_OVERFLOW;
+    }
+    *num_wide = (uint64_t)cc[0];
+    return LMGPU_OK;
+}
+
+}  // namespace
+}  // namespace lmgpu
+
+extern "C" int lmgpu_trace_static_scene(const float* d_triangles, uint64_t ntri, const float* d_rays,
+                                        lmgpu_hit* d_hits, uint64_t nrays, int anyhit, void* stream)
+{
+    using namespace lmgpu;
+    clear_error();
+    if (ntri > (uint64_t)LMGPU_STATIC_MAX_TRIANGLES) {
+        set_error("lmgpu_trace_static_scene: " + std::to_string(ntri) + " triangles exceed the static limit of " +
+                  std::to_string(LMGPU_STATIC_MAX_TRIANGLES));
+        return LMGPU_ERR_INVALID;
+    }
+    if ((ntri > 0 && !d_triangles) || (nrays > 0 && (!d_rays || !d_hits))) {
+        set_error("lmgpu_trace_static_scene: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    if (((uintptr_t)d_rays & 15u) || ((uintptr_t)d_hits & 15u)) {
+        set_error("lmgpu_trace_static_scene: rays and hits must be 16-byte aligned");
+        return LMGPU_ERR_INVALID;
+    }
+    unsigned char* base = nullptr;
+    int rc = static_scratch_base(&base);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    uint64_t num_wide = 0;
+    if (ntri > 0) {
+        rc = build_static(base, d_triangles, (int)ntri, s, &num_wide);
+        if (rc) return rc;
+    } else {
+        LMGPU_CUDA_TRY(cudaMemsetAsync(base + kSL.status, 0, sizeof(uint32_t), s));
+    }
+    if (nrays == 0) return LMGPU_OK;
+    // A view of the static BVH in the shape launch_trace takes; it owns nothing.
+    lmgpu_accel view;
+    view.ntri = ntri;
+    view.num_wide = num_wide;
+    view.nodes = reinterpret_cast<WNode*>(base + kSL.wnodes);
+    view.tris = reinterpret_cast<WTri*>(base + kSL.wtris);
+    view.status = reinterpret_cast<uint32_t*>(base + kSL.status);
+    view.built = true;
+    rc = launch_trace(&view, reinterpret_cast<const float4*>(d_rays), d_hits, nrays, anyhit != 0, false, s);
+    if (rc) return rc;
+    uint32_t st = 0;
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(&st, view.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    if (st & (kStatusBadTree | kStatusStackOverflow)) {
+        set_error("lmgpu_trace_static_scene: traversal status " + std::to_string(st));
+        return LMGPU_ERR_OVERFLOW;
+    }
+    return LMGPU_OK;
+}

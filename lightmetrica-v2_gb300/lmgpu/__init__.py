@@ -82,8 +82,10 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_trace_device.argtypes = [vp, vp, vp, u64, i32, vp]
     L.lmgpu_trace_stats_device.argtypes = [vp, vp, vp, u64, i32, vp, ctypes.POINTER(TraceStats)]
     L.lmgpu_accel_check.argtypes = [vp, vp]
+    L.lmgpu_trace_static_scene.argtypes = [vp, u64, vp, vp, u64, i32, vp]
     for name in ("lmgpu_accel_create", "lmgpu_accel_build", "lmgpu_accel_build_device", "lmgpu_accel_get_info",
-                 "lmgpu_trace", "lmgpu_trace_device", "lmgpu_trace_stats_device", "lmgpu_accel_check"):
+                 "lmgpu_trace", "lmgpu_trace_device", "lmgpu_trace_stats_device", "lmgpu_accel_check",
+                 "lmgpu_trace_static_scene"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -156,6 +158,15 @@ class Accel:
 
     def check(self, stream: int = 0) -> None:
         _check(lib().lmgpu_accel_check(self._h, stream))
+
+
+STATIC_MAX_TRIANGLES = 16384  # LMGPU_STATIC_MAX_TRIANGLES
+
+
+def trace_static_scene(d_tris_ptr: int, ntri: int, d_rays_ptr: int, d_hits_ptr: int, nrays: int,
+                       anyhit: bool = False, stream: int = 0) -> None:
+    """Allocation-free build + trace on device buffers (lmgpu_trace_static_scene)."""
+    _check(lib().lmgpu_trace_static_scene(d_tris_ptr, ntri, d_rays_ptr, d_hits_ptr, nrays, int(anyhit), stream))
 
 
 def version() -> str:
