@@ -223,7 +223,8 @@ def run_gpu(args) -> None:
             dist.barrier()
 
     tris = scenes.raycast_scene(N_RANDOM, HF_RES)
-    rays = scenes.raycast_rays(N_RAYS, stream=3 + rank)
+    nr = args.rays
+    rays = scenes.raycast_rays(nr, stream=3 + rank)
     stream = torch.cuda.Stream()
     s = stream.cuda_stream
     acc = lmgpu.Accel()
@@ -231,15 +232,16 @@ def run_gpu(args) -> None:
         d_tris = torch.from_numpy(tris).cuda()
         acc.build_device(d_tris.data_ptr(), tris.shape[0], s)
         d_rays = torch.from_numpy(rays).cuda()
-        d_hits = torch.empty((N_RAYS, 4), dtype=torch.float32, device="cuda")
+        d_hits = torch.empty((nr, 4), dtype=torch.float32, device="cuda")
     info = acc.info()
+    ah = bool(args.anyhit)
 
     # fetch counts of the same query (instrumented kernel, outside the timed region)
-    st = acc.trace_stats_device(d_rays.data_ptr(), d_hits.data_ptr(), N_RAYS, False, s)
-    bytes_per_ray = RAY_BYTES + HIT_BYTES + (st["node_fetches"] * NODE_BYTES + st["triangle_fetches"] * TRI_BYTES) / N_RAYS
+    st = acc.trace_stats_device(d_rays.data_ptr(), d_hits.data_ptr(), nr, ah, s)
+    bytes_per_ray = RAY_BYTES + HIT_BYTES + (st["node_fetches"] * NODE_BYTES + st["triangle_fetches"] * TRI_BYTES) / nr
 
     for _ in range(args.warmup):
-        acc.trace_device(d_rays.data_ptr(), d_hits.data_ptr(), N_RAYS, False, s)
+        acc.trace_device(d_rays.data_ptr(), d_hits.data_ptr(), nr, ah, s)
     acc.check(s)
     torch.cuda.synchronize()
     barrier()
@@ -251,7 +253,7 @@ def run_gpu(args) -> None:
     barrier()
     ev0.record(stream)
     for _ in range(args.steps):
-        acc.trace_device(d_rays.data_ptr(), d_hits.data_ptr(), N_RAYS, False, s)
+        acc.trace_device(d_rays.data_ptr(), d_hits.data_ptr(), nr, ah, s)
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -261,15 +263,15 @@ def run_gpu(args) -> None:
 
     # e2e: host buffers through the C ABI, copies inside the timed region
     h_rays = torch.from_numpy(rays).pin_memory()
-    h_hits = torch.empty((N_RAYS, 4), dtype=torch.float32).pin_memory()
+    h_hits = torch.empty((nr, 4), dtype=torch.float32).pin_memory()
     e2e_steps = max(3, min(args.steps, 20))
     for _ in range(2):
-        acc.trace_ptr(h_rays.data_ptr(), h_hits.data_ptr(), N_RAYS)
+        acc.trace_ptr(h_rays.data_ptr(), h_hits.data_ptr(), nr, ah)
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        acc.trace_ptr(h_rays.data_ptr(), h_hits.data_ptr(), N_RAYS)
+        acc.trace_ptr(h_rays.data_ptr(), h_hits.data_ptr(), nr, ah)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     barrier()
@@ -283,31 +285,32 @@ def run_gpu(args) -> None:
 
     if rank == 0:
         per_launch_s = ms / 1e3 / args.steps
-        value = ws * N_RAYS / per_launch_s / 1e6
-        e2e_value = ws * N_RAYS * e2e_steps / e2e_s / 1e6
+        value = ws * nr / per_launch_s / 1e6
+        e2e_value = ws * nr * e2e_steps / e2e_s / 1e6
         peak, peak_src = measured_peak()
-        achieved = N_RAYS * bytes_per_ray / per_launch_s / 1e9
+        achieved = nr * bytes_per_ray / per_launch_s / 1e9
         traffic = traffic_per_launch()
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-                "config": workload_config({"parallelism": f"replicated BVH, rays sharded x{ws}" if ws > 1 else "1 GPU"}),
-                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N_RAYS * RAY_BYTES,
-                        "d2h_bytes_per_step": N_RAYS * HIT_BYTES, "steps": e2e_steps,
+                "config": workload_config({"parallelism": f"replicated BVH, rays sharded x{ws}" if ws > 1 else "1 GPU",
+                                           "rays_per_step": nr, "query": "any-hit" if ah else "closest-hit"}),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nr * RAY_BYTES,
+                        "d2h_bytes_per_step": nr * HIT_BYTES, "steps": e2e_steps,
                         "api": "lmgpu_trace (host pointers, pinned)"},
                 "gpu_launches": args.steps,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
-                             "kernel": "k_trace<closest>",
+                             "kernel": "k_trace<anyhit>" if ah else "k_trace<closest>",
                              "bytes_per_ray": bytes_per_ray,
-                             "nodes_per_ray": st["node_fetches"] / N_RAYS,
-                             "tris_per_ray": st["triangle_fetches"] / N_RAYS,
+                             "nodes_per_ray": st["node_fetches"] / nr,
+                             "tris_per_ray": st["triangle_fetches"] / nr,
                              "note": "algorithmic bytes = 32 B ray + 16 B hit + 80 B per node fetch + 48 B per "
                                      "triangle test; node/triangle fetches are mostly L2 hits"},
                 "clocks": clk,
                 "accel": {"build_ms": info["build_ms"], "wide_nodes": info["num_wide_nodes"],
                           "binary_depth": info["binary_depth"], "wide_depth": info["wide_depth"],
-                          "hit_fraction": st["hits"] / N_RAYS}}
+                          "hit_fraction": st["hits"] / nr}}
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
             cb = CpuReference(tris, threads).time_sample(rays, 15.0)
@@ -327,6 +330,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling of smaller cases)")
+    ap.add_argument("--anyhit", action="store_true", help="time any-hit queries instead of closest hit")
     ap.add_argument("--use-ref-binary", action="store_true",
                     help="reference arm: time the reference's own qbvh (x86-64 harness) if built")
     args = ap.parse_args()
