@@ -110,6 +110,13 @@ int lmgpu_trace_device(const lmgpu_accel* accel, const float* d_rays, lmgpu_hit*
 int lmgpu_trace_stats_device(const lmgpu_accel* accel, const float* d_rays, lmgpu_hit* d_hits, uint64_t n,
                              int anyhit, void* stream, lmgpu_trace_stats* stats);
 
+/* Sets the traversal kernel's scheduling knobs for this accel: a warp takes
+ * new rays once `refill` of its 32 lanes are idle (1..32), and postpones
+ * triangle tests while fewer than `postpone` lanes have triangle work
+ * (0..32, 0 = never postpone).  Results do not depend on them; speed does.
+ * No counterpart in the reference (its accels trace one ray per call). */
+int lmgpu_accel_set_tuning(lmgpu_accel* accel, int refill, int postpone);
+
 /* Synchronises `stream` and reports device-side errors (stack overflow)
  * raised by earlier asynchronous launches. */
 int lmgpu_accel_check(const lmgpu_accel* accel, void* stream);

@@ -6,6 +6,16 @@
 
 #include <mutex>
 
+namespace lmgpu {
+// Tuning knobs of the traversal kernel (see trace.cu): lanes idle before a
+// warp refills, and lanes with triangle work below which triangles are
+// postponed.
+struct TraceConfig {
+    int refill = 4;
+    int postpone = 12;
+};
+}  // namespace lmgpu
+
 struct lmgpu_accel {
     int device = 0;
     uint64_t ntri = 0;
@@ -25,6 +35,7 @@ struct lmgpu_accel {
     unsigned long long* counters = nullptr;
 
     lmgpu_accel_info info{};
+    lmgpu::TraceConfig tune;
 
     // Staging buffers of the host-pointer trace entry point, reused across
     // calls; host_mu serialises callers (Accel3::Intersect may be called from

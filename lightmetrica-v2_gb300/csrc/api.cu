@@ -255,6 +255,18 @@ int lmgpu_trace(const lmgpu_accel* ca, const float* rays, lmgpu_hit* hits, uint6
     return read_status(a, a->stage_stream[0]);
 }
 
+int lmgpu_accel_set_tuning(lmgpu_accel* a, int refill, int postpone)
+{
+    clear_error();
+    if (!a || refill < 1 || refill > 32 || postpone < 0 || postpone > 32) {
+        set_error("lmgpu_accel_set_tuning: refill must be in [1, 32] and postpone in [0, 32]");
+        return LMGPU_ERR_INVALID;
+    }
+    a->tune.refill = refill;
+    a->tune.postpone = postpone;
+    return LMGPU_OK;
+}
+
 int lmgpu_accel_check(const lmgpu_accel* a, void* stream)
 {
     clear_error();

@@ -63,7 +63,13 @@ __device__ __forceinline__ void setup_ray(const float4 r0, const float4 r1, RayS
     R.Sz = 1.0f / dkz;
 }
 
-__device__ __forceinline__ float qbyte(uint32_t w, int k) { return (float)((w >> (8 * k)) & 0xffu); }
+// Byte k of w as a float: the byte becomes the low mantissa bits of 2^23,
+// and subtracting 2^23 leaves it exactly (PRMT + FADD instead of a
+// shift/mask and an int-to-float conversion).
+__device__ __forceinline__ float qbyte(uint32_t w, int k)
+{
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)k)) - 8388608.0f;
+}
 
 // Tests the eight child boxes of one node; returns the hit mask
 // (bits 24..31 inner children in permuted slot order, bits 0..23 triangles).
@@ -161,95 +167,161 @@ __device__ __forceinline__ bool intersect_tri(const WTri* __restrict__ tris, uin
     return true;
 }
 
+// Persistent traversal.  Each block owns the contiguous ray range
+// [blockIdx * n / grid, (blockIdx + 1) * n / grid) and its warps take rays
+// from it through a shared-memory counter, so no global state outlives a
+// launch and concurrent launches on other streams are independent.
+//
+// Per warp, every iteration of the main loop:
+//   1. refill: when at least `refill` lanes are idle, they take new rays
+//      together (one shared atomic per warp);
+//   2. node step: a lane with no pending triangles visits one node (or pops
+//      a group from its stack, or finishes its ray);
+//   3. triangle steps: lanes with pending triangles test them one at a time
+//      while at least `postpone` lanes of the warp have triangle work; when
+//      fewer do, lanes that also have node work push their triangles back on
+//      the stack and go on traversing (after Aila & Laine 2009 and Ylitie,
+//      Karras & Laine 2017), so the warp keeps doing one kind of work at once.
 template <bool ANYHIT, bool STATS>
 __global__ void __launch_bounds__(kTraceThreads) k_trace(const WNode* __restrict__ nodes, const WTri* __restrict__ tris,
                                                          const float4* __restrict__ rays, lmgpu_hit* __restrict__ hits,
                                                          uint64_t n, uint32_t num_nodes, uint32_t num_tris,
-                                                         uint32_t* __restrict__ status,
+                                                         int refill, int postpone, uint32_t* __restrict__ status,
                                                          unsigned long long* __restrict__ counters)
 {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (!STATS && i >= n) return;
-    const bool active = i < n;
-    const float4 r0 = active ? __ldg(rays + 2 * i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    const float4 r1 = active ? __ldg(rays + 2 * i + 1) : make_float4(1.0f, 0.0f, 0.0f, -1.0f);
-    RayState R;
-    setup_ray(r0, r1, R);
-    float best_t = r1.w;
-    int best_id = -1;
-    float best_b1 = 0.0f, best_b2 = 0.0f;
-    uint32_t node_fetch = 0, tri_fetch = 0;
+    __shared__ unsigned long long s_next;
+    const uint64_t begin = (uint64_t)blockIdx.x * n / gridDim.x;
+    const uint64_t end = (uint64_t)(blockIdx.x + 1) * n / gridDim.x;
+    if (threadIdx.x == 0) s_next = begin;
+    __syncthreads();
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt_mask = (1u << lane) - 1u;
 
+    bool active = false, exhausted = false;
+    uint64_t rid = 0;
+    RayState R;
+    float best_t = 0.0f, best_b1 = 0.0f, best_b2 = 0.0f;
+    int best_id = -1;
+    uint2 ng = make_uint2(0u, 0u), tg = make_uint2(0u, 0u);
     uint2 stack[kStack];
     int sp = 0;
-    // Root group: one inner child at bit 31, base 0, inner mask 0.
-    uint2 ng = make_uint2(0u, (num_nodes > 0 && active) ? 0x80000000u : 0u);
-    bool done = false;
-    // A tree visits each node at most once per ray; more iterations than
-    // nodes means a malformed tree: flag it and stop instead of looping.
-    uint32_t budget = num_nodes + 1;
-    while (!done) {
-        if (ng.y & 0xff000000u) {
-            const uint32_t bit = 31u - __clz(ng.y & 0xff000000u);
-            ng.y &= ~(1u << bit);
-            const uint32_t slot = (bit - 24u) ^ R.oct_inv;
-            const uint32_t rel = __popc(ng.y & 0xffu & ((1u << slot) - 1u));
-            const uint32_t ni = ng.x + rel;
-            if (ni >= num_nodes || budget-- == 0) {
-                atomicOr(status, kStatusBadTree);
-                break;
+    uint32_t budget = 0;
+    uint32_t node_fetch = 0, tri_fetch = 0, nrays = 0, nhits = 0;
+
+    while (true) {
+        // 1. refill idle lanes
+        const unsigned idle = __ballot_sync(FULL, !active);
+        if (!exhausted && __popc(idle) >= refill) {
+            const unsigned leader = __ffs(idle) - 1u;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(&s_next, (unsigned long long)__popc(idle));
+            base = __shfl_sync(FULL, base, leader);
+            if (base + __popc(idle) >= end) exhausted = true;
+            if (!active) {
+                const uint64_t id = base + __popc(idle & lt_mask);
+                if (id < end) {
+                    rid = id;
+                    const float4 r0 = __ldg(rays + 2 * id);
+                    const float4 r1 = __ldg(rays + 2 * id + 1);
+                    setup_ray(r0, r1, R);
+                    best_t = r1.w;
+                    best_id = -1;
+                    best_b1 = best_b2 = 0.0f;
+                    ng = make_uint2(0u, num_nodes > 0 ? 0x80000000u : 0u);
+                    tg = make_uint2(0u, 0u);
+                    sp = 0;
+                    budget = num_nodes + 1;
+                    active = true;
+                    if (STATS) nrays++;
+                }
             }
+        }
+        if (!__any_sync(FULL, active)) break;
+
+        // 2. node step
+        if (active && tg.y == 0u) {
             if (ng.y & 0xff000000u) {
-                if (sp < kStack) stack[sp++] = ng;
-                else atomicOr(status, kStatusStackOverflow);
-            }
-            uint32_t child_base, tri_base, imask;
-            const uint32_t hm = intersect_node(nodes, ni, R, best_t, child_base, tri_base, imask);
-            if (STATS) node_fetch++;
-            ng = make_uint2(child_base, (hm & 0xff000000u) | imask);
-            uint32_t tmask = hm & 0x00ffffffu;
-            while (tmask) {
-                const uint32_t k = __ffs(tmask) - 1;
-                tmask &= tmask - 1;
-                if (tri_base + k >= num_tris) {
+                const uint32_t bit = 31u - __clz(ng.y & 0xff000000u);
+                ng.y &= ~(1u << bit);
+                const uint32_t slot = (bit - 24u) ^ R.oct_inv;
+                const uint32_t rel = __popc(ng.y & 0xffu & ((1u << slot) - 1u));
+                const uint32_t ni = ng.x + rel;
+                if (ni >= num_nodes || budget-- == 0u) {
                     atomicOr(status, kStatusBadTree);
-                    break;
-                }
-                float t, b1, b2;
-                int id;
-                if (STATS) tri_fetch++;
-                if (intersect_tri(tris, tri_base + k, R, best_t, t, b1, b2, id)) {
-                    if (t < best_t || id > best_id) {
-                        best_t = t;
-                        best_id = id;
-                        best_b1 = b1;
-                        best_b2 = b2;
+                    ng.y = 0u;
+                    sp = 0;
+                } else {
+                    if (ng.y & 0xff000000u) {
+                        if (sp < kStack) stack[sp++] = ng;
+                        else atomicOr(status, kStatusStackOverflow);
                     }
-                    if (ANYHIT) {
-                        done = true;
-                        break;
+                    uint32_t child_base, tri_base, imask;
+                    const uint32_t hm = intersect_node(nodes, ni, R, best_t, child_base, tri_base, imask);
+                    if (STATS) node_fetch++;
+                    ng = make_uint2(child_base, (hm & 0xff000000u) | imask);
+                    tg = make_uint2(tri_base, hm & 0x00ffffffu);
+                }
+            } else if (sp > 0) {
+                const uint2 g = stack[--sp];
+                if (g.y & 0xff000000u) ng = g;
+                else tg = g;
+            } else {
+                lmgpu_hit h;
+                h.t = best_id >= 0 ? best_t : 0.0f;
+                h.prim = best_id;
+                h.b1 = best_b1;
+                h.b2 = best_b2;
+                reinterpret_cast<float4*>(hits)[rid] = *reinterpret_cast<const float4*>(&h);
+                if (STATS && best_id >= 0) nhits++;
+                active = false;
+            }
+        }
+
+        // 3. triangle steps
+        while (true) {
+            const bool has = active && tg.y != 0u;
+            const unsigned m = __ballot_sync(FULL, has);
+            if (m == 0u) break;
+            const bool few = __popc(m) < postpone;
+            if (few && has && (ng.y & 0xff000000u) && sp < kStack) {
+                stack[sp++] = tg;
+                tg.y = 0u;
+            }
+            if (active && tg.y != 0u) {
+                const uint32_t k = __ffs(tg.y) - 1u;
+                tg.y &= tg.y - 1u;
+                if (tg.x + k >= num_tris) {
+                    atomicOr(status, kStatusBadTree);
+                    tg.y = 0u;
+                } else {
+                    float t, b1, b2;
+                    int id;
+                    if (STATS) tri_fetch++;
+                    if (intersect_tri(tris, tg.x + k, R, best_t, t, b1, b2, id)) {
+                        if (t < best_t || id > best_id) {
+                            best_t = t;
+                            best_id = id;
+                            best_b1 = b1;
+                            best_b2 = b2;
+                        }
+                        if (ANYHIT) {
+                            tg.y = 0u;
+                            ng.y = 0u;
+                            sp = 0;
+                        }
                     }
                 }
             }
-        } else if (sp > 0) {
-            ng = stack[--sp];
-        } else {
-            done = true;
+            if (few) break;
         }
     }
-    lmgpu_hit h;
-    h.t = best_id >= 0 ? best_t : 0.0f;
-    h.prim = best_id;
-    h.b1 = best_b1;
-    h.b2 = best_b2;
-    if (active) reinterpret_cast<float4*>(hits)[i] = *reinterpret_cast<const float4*>(&h);
     if (STATS) {
-        // every lane of the warp reaches this point (no early return with STATS)
-        unsigned long long v[4] = {active ? 1ull : 0ull, node_fetch, tri_fetch, best_id >= 0 ? 1ull : 0ull};
+        unsigned long long v[4] = {nrays, node_fetch, tri_fetch, nhits};
         for (int q = 0; q < 4; q++) {
             unsigned long long x = v[q];
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-            if ((threadIdx.x & 31) == 0) atomicAdd(&counters[q], x);
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(FULL, x, o);
+            if (lane == 0) atomicAdd(&counters[q], x);
         }
     }
 }
@@ -260,19 +332,27 @@ int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, 
                  cudaStream_t stream)
 {
     if (n == 0) return LMGPU_OK;
-    const uint64_t blocks = (n + kTraceThreads - 1) / kTraceThreads;
-    if (blocks > 0x7fffffffull) {
-        set_error("lmgpu_trace: too many rays for one launch");
-        return LMGPU_ERR_INVALID;
+    static int grid_cap = 0;
+    if (grid_cap == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        LMGPU_CUDA_TRY(cudaGetDevice(&dev));
+        LMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        LMGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false, false>, kTraceThreads, 0));
+        grid_cap = sms * (per_sm > 0 ? per_sm : 1);
     }
+    const TraceConfig cfg = a->tune;
+    // at least ~4 warps' worth of rays per block
+    const uint64_t by_rays = (n + 4 * kTraceThreads - 1) / (4 * kTraceThreads);
+    const unsigned grid = (unsigned)(by_rays < (uint64_t)grid_cap ? by_rays : (uint64_t)grid_cap);
     const uint32_t nn = a->ntri > 0 ? (uint32_t)a->num_wide : 0u;
     const uint32_t nt = (uint32_t)a->ntri;
+    auto* cnt = a->counters;
     if (anyhit) {
-        if (stats) k_trace<true, true><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, a->status, a->counters);
-        else k_trace<true, false><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, a->status, a->counters);
+        if (stats) k_trace<true, true><<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, cfg.refill, cfg.postpone, a->status, cnt);
+        else k_trace<true, false><<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, cfg.refill, cfg.postpone, a->status, cnt);
     } else {
-        if (stats) k_trace<false, true><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, a->status, a->counters);
-        else k_trace<false, false><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, a->status, a->counters);
+        if (stats) k_trace<false, true><<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, cfg.refill, cfg.postpone, a->status, cnt);
+        else k_trace<false, false><<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, cfg.refill, cfg.postpone, a->status, cnt);
     }
     LMGPU_CUDA_TRY(cudaGetLastError());
     return LMGPU_OK;

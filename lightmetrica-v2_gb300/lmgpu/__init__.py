@@ -83,9 +83,10 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_trace_stats_device.argtypes = [vp, vp, vp, u64, i32, vp, ctypes.POINTER(TraceStats)]
     L.lmgpu_accel_check.argtypes = [vp, vp]
     L.lmgpu_trace_static_scene.argtypes = [vp, u64, vp, vp, u64, i32, vp]
+    L.lmgpu_accel_set_tuning.argtypes = [vp, i32, i32]
     for name in ("lmgpu_accel_create", "lmgpu_accel_build", "lmgpu_accel_build_device", "lmgpu_accel_get_info",
                  "lmgpu_trace", "lmgpu_trace_device", "lmgpu_trace_stats_device", "lmgpu_accel_check",
-                 "lmgpu_trace_static_scene"):
+                 "lmgpu_trace_static_scene", "lmgpu_accel_set_tuning"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -155,6 +156,9 @@ class Accel:
         _check(lib().lmgpu_trace_stats_device(self._h, d_rays_ptr, d_hits_ptr, n, int(anyhit), stream,
                                               ctypes.byref(s)))
         return s.as_dict()
+
+    def set_tuning(self, refill: int, postpone: int) -> None:
+        _check(lib().lmgpu_accel_set_tuning(self._h, refill, postpone))
 
     def check(self, stream: int = 0) -> None:
         _check(lib().lmgpu_accel_check(self._h, stream))
