@@ -121,6 +121,64 @@ int lmgpu_accel_set_tuning(lmgpu_accel* accel, int refill, int postpone);
  * raised by earlier asynchronous launches. */
 int lmgpu_accel_check(const lmgpu_accel* accel, void* stream);
 
+/* ---- Path tracing (renderer::pt) -------------------------------------- */
+
+#define LMGPU_BSDF_NULL 0     /* bsdf::null: paths end here (bsdf_null.cpp) */
+#define LMGPU_BSDF_DIFFUSE 1  /* bsdf::diffuse, reflectance R (bsdf_diffuse.cpp) */
+
+/* One scene primitive (Primitive, include/lightmetrica/primitive.h:56-80):
+ * its BSDF and, if is_light, an area light (light::area, light_area.cpp)
+ * with radiance Le over its triangles, emitting on the front side. */
+typedef struct {
+    int32_t bsdf;
+    int32_t is_light;
+    float R[3];
+    float Le[3];
+} lmgpu_prim;
+
+/* Pinhole sensor at a lookat node (scene3.cpp:213-221, sensor_pinhole.cpp):
+ * vertical fov in degrees, film width x height. */
+typedef struct {
+    float eye[3], center[3], up[3];
+    float fov_deg;
+    int32_t width, height;
+} lmgpu_camera;
+
+/* renderer::pt parameters (renderer_pt.cpp:56-62): samples per pixel
+ * (the reference's num_samples = width * height * spp), max_num_vertices
+ * (-1 = unbounded), and the seed of the counter-based random numbers. */
+typedef struct {
+    uint64_t spp;
+    int32_t max_num_vertices;
+    uint32_t seed;
+} lmgpu_pt_params;
+
+typedef struct lmgpu_scene lmgpu_scene;
+
+/* Uploads a scene (triangles in global order, the primitive of each, the
+ * primitives, the camera) and builds its BVH on the GPU.  Stands in for
+ * Scene::Initialize (include/lightmetrica/scene.h:59) with Accel::Build. */
+int lmgpu_scene_create(const float* triangles, const int32_t* tri_prim, uint64_t ntri, const lmgpu_prim* prims,
+                       uint32_t nprims, const lmgpu_camera* camera, lmgpu_scene** out);
+
+/* Frees a scene and everything it owns.  NULL is ignored. */
+void lmgpu_scene_destroy(lmgpu_scene* scene);
+
+/* The scene's accel (owned by the scene), for ray queries on its triangles. */
+int lmgpu_scene_accel(const lmgpu_scene* scene, const lmgpu_accel** accel);
+
+/* Renders the scene with the wavefront path tracer and writes the film
+ * (height x width x 3 floats, row = raster y from the bottom, as
+ * film_hdr.cpp:218-223 indexes it) and, if variance is not NULL, the
+ * per-pixel variance of that estimate.  Host buffers.  Stands in for
+ * Renderer::Render of renderer::pt (include/lightmetrica/renderer.h:81). */
+int lmgpu_render_pt(lmgpu_scene* scene, const lmgpu_pt_params* params, float* image, float* variance);
+
+/* As lmgpu_render_pt into device buffers on `stream` (NULL: the scene's
+ * stream); returns after the render has finished. */
+int lmgpu_render_pt_device(lmgpu_scene* scene, const lmgpu_pt_params* params, float* d_image, float* d_variance,
+                           void* stream);
+
 /* Largest scene lmgpu_trace_static_scene accepts. */
 #define LMGPU_STATIC_MAX_TRIANGLES 16384
 

@@ -1,0 +1,212 @@
+// Scene object of the path tracers and its C ABI (include/lmgpu.h).
+#include "scene.cuh"
+
+#include <cmath>
+#include <cstring>
+
+namespace lmgpu {
+
+namespace {
+
+template <typename T>
+int grow(T** p, uint64_t count)
+{
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        return LMGPU_ERR_CUDA;
+    }
+    return LMGPU_OK;
+}
+
+float3 make3(const float* v) { return make_float3(v[0], v[1], v[2]); }
+float3 sub3(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+float3 cross(float3 a, float3 b)
+{
+    return make_float3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+float3 normalize(float3 a)
+{
+    const float l = std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    return make_float3(a.x / l, a.y / l, a.z / l);
+}
+
+}  // namespace
+
+int ensure_film(lmgpu_scene* sc, uint64_t npix)
+{
+    if (sc->film_cap >= npix) return LMGPU_OK;
+    int rc;
+    if ((rc = grow(&sc->film, 3 * npix)) || (rc = grow(&sc->film_sq, 3 * npix)) ||
+        (rc = grow(&sc->d_image, 3 * npix)) || (rc = grow(&sc->d_variance, 3 * npix)))
+        return rc;
+    sc->film_cap = npix;
+    return LMGPU_OK;
+}
+
+int ensure_queues(lmgpu_scene* sc, uint64_t n)
+{
+    if (sc->q_cap >= n) return LMGPU_OK;
+    int rc;
+    for (int i = 0; i < 2; i++)
+        if ((rc = grow(&sc->q_ray[i], 2 * n)) || (rc = grow(&sc->q_state[i], n))) return rc;
+    if ((rc = grow(&sc->q_hit, n))) return rc;
+    sc->q_cap = n;
+    return LMGPU_OK;
+}
+
+SceneGPU scene_view(const lmgpu_scene* sc)
+{
+    SceneGPU g;
+    g.tris = sc->tris;
+    g.tri_prim = sc->tri_prim;
+    g.prims = sc->prims;
+    return g;
+}
+
+}  // namespace lmgpu
+
+using namespace lmgpu;
+
+extern "C" {
+
+int lmgpu_scene_create(const float* tris, const int32_t* tri_prim, uint64_t ntri, const lmgpu_prim* prims,
+                       uint32_t nprims, const lmgpu_camera* cam, lmgpu_scene** out)
+{
+    clear_error();
+    if (!out || !cam || (ntri > 0 && (!tris || !tri_prim)) || (nprims > 0 && !prims)) {
+        set_error("lmgpu_scene_create: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    *out = nullptr;
+    if (cam->width <= 0 || cam->height <= 0 || !(cam->fov_deg > 0.0f && cam->fov_deg < 180.0f)) {
+        set_error("lmgpu_scene_create: bad camera (width, height > 0, 0 < fov < 180)");
+        return LMGPU_ERR_INVALID;
+    }
+    for (uint64_t i = 0; i < ntri; i++) {
+        if (tri_prim[i] < 0 || (uint32_t)tri_prim[i] >= nprims) {
+            set_error("lmgpu_scene_create: triangle " + std::to_string(i) + " names primitive " +
+                      std::to_string(tri_prim[i]) + " of " + std::to_string(nprims));
+            return LMGPU_ERR_INVALID;
+        }
+    }
+    for (uint32_t i = 0; i < nprims; i++) {
+        if (prims[i].bsdf != LMGPU_BSDF_NULL && prims[i].bsdf != LMGPU_BSDF_DIFFUSE) {
+            set_error("lmgpu_scene_create: unsupported bsdf kind " + std::to_string(prims[i].bsdf));
+            return LMGPU_ERR_INVALID;
+        }
+    }
+    lmgpu_scene* sc = new lmgpu_scene();
+    auto fail = [&](int rc) {
+        lmgpu_scene_destroy(sc);
+        return rc;
+    };
+    int rc = lmgpu_accel_create(&sc->accel);
+    if (rc) return fail(rc);
+    if (cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost((void**)&sc->h_count, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc((void**)&sc->q_count, sizeof(uint32_t)) != cudaSuccess) {
+        set_error("lmgpu_scene_create: stream or buffer allocation failed");
+        return fail(LMGPU_ERR_CUDA);
+    }
+    sc->ntri = ntri;
+    sc->nprims = nprims;
+    if ((rc = grow(&sc->tris, 9 * ntri)) || (rc = grow(&sc->tri_prim, ntri)) || (rc = grow(&sc->prims, nprims)))
+        return fail(rc);
+    static_assert(sizeof(PrimGPU) == sizeof(lmgpu_prim), "primitive layout");
+    if (cudaMemcpy(sc->tris, tris, sizeof(float) * 9 * ntri, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(sc->tri_prim, tri_prim, sizeof(int32_t) * ntri, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(sc->prims, prims, sizeof(PrimGPU) * nprims, cudaMemcpyHostToDevice) != cudaSuccess) {
+        set_error("lmgpu_scene_create: upload failed");
+        return fail(LMGPU_ERR_CUDA);
+    }
+    rc = build_bvh(sc->accel, sc->tris, ntri, sc->stream);
+    if (rc) return fail(rc);
+    // lookat basis (scene3.cpp:213-221) and pinhole parameters (sensor_pinhole.cpp:46-62)
+    const float3 eye = make3(cam->eye), center = make3(cam->center), up = make3(cam->up);
+    CameraGPU& c = sc->cam;
+    c.eye = eye;
+    c.vz = normalize(sub3(eye, center));
+    c.vx = normalize(cross(up, c.vz));
+    c.vy = cross(c.vz, c.vx);
+    c.tan_fov = std::tan(cam->fov_deg * 3.14159265358979323846f / 180.0f * 0.5f);
+    c.aspect = (float)cam->width / (float)cam->height;
+    c.width = cam->width;
+    c.height = cam->height;
+    *out = sc;
+    return LMGPU_OK;
+}
+
+void lmgpu_scene_destroy(lmgpu_scene* sc)
+{
+    if (!sc) return;
+    if (sc->stream) cudaStreamSynchronize(sc->stream);
+    lmgpu_accel_destroy(sc->accel);
+    void* ptrs[] = {sc->tris, sc->tri_prim, sc->prims, sc->film, sc->film_sq, sc->d_image, sc->d_variance,
+                    sc->q_ray[0], sc->q_ray[1], sc->q_state[0], sc->q_state[1], sc->q_hit, sc->q_count};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (sc->h_count) cudaFreeHost(sc->h_count);
+    if (sc->stream) cudaStreamDestroy(sc->stream);
+    delete sc;
+}
+
+int lmgpu_scene_accel(const lmgpu_scene* sc, const lmgpu_accel** accel)
+{
+    clear_error();
+    if (!sc || !accel) {
+        set_error("lmgpu_scene_accel: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    *accel = sc->accel;
+    return LMGPU_OK;
+}
+
+int lmgpu_render_pt_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance,
+                           void* stream)
+{
+    clear_error();
+    if (!sc || !prm || !d_image) {
+        set_error("lmgpu_render_pt_device: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    if (prm->spp == 0 || (uint64_t)sc->cam.width * sc->cam.height * prm->spp > (1ull << 40)) {
+        set_error("lmgpu_render_pt_device: spp must be in [1, 2^40 / pixels]");
+        return LMGPU_ERR_INVALID;
+    }
+    cudaStream_t s = stream ? (cudaStream_t)stream : sc->stream;
+    int rc = render_pt(sc, prm, d_image, d_variance, s);
+    if (rc) return rc;
+    uint32_t st = 0;
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(&st, sc->accel->status, sizeof(st), cudaMemcpyDeviceToHost, s));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    if (st & (kStatusBadTree | kStatusStackOverflow)) {
+        set_error("lmgpu_render_pt: traversal status " + std::to_string(st));
+        return LMGPU_ERR_OVERFLOW;
+    }
+    return LMGPU_OK;
+}
+
+int lmgpu_render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image, float* variance)
+{
+    clear_error();
+    if (!sc || !prm || !image) {
+        set_error("lmgpu_render_pt: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    const uint64_t npix = (uint64_t)sc->cam.width * sc->cam.height;
+    int rc = ensure_film(sc, npix);
+    if (rc) return rc;
+    rc = lmgpu_render_pt_device(sc, prm, sc->d_image, variance ? sc->d_variance : nullptr, sc->stream);
+    if (rc) return rc;
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(image, sc->d_image, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost, sc->stream));
+    if (variance)
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(variance, sc->d_variance, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost,
+                                       sc->stream));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(sc->stream));
+    return LMGPU_OK;
+}
+
+}  // extern "C"

@@ -84,9 +84,16 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_accel_check.argtypes = [vp, vp]
     L.lmgpu_trace_static_scene.argtypes = [vp, u64, vp, vp, u64, i32, vp]
     L.lmgpu_accel_set_tuning.argtypes = [vp, i32, i32]
+    L.lmgpu_scene_create.argtypes = [vp, vp, u64, vp, ctypes.c_uint32, vp, ctypes.POINTER(vp)]
+    L.lmgpu_scene_destroy.argtypes = [vp]
+    L.lmgpu_scene_destroy.restype = None
+    L.lmgpu_scene_accel.argtypes = [vp, ctypes.POINTER(vp)]
+    L.lmgpu_render_pt.argtypes = [vp, vp, vp, vp]
+    L.lmgpu_render_pt_device.argtypes = [vp, vp, vp, vp, vp]
     for name in ("lmgpu_accel_create", "lmgpu_accel_build", "lmgpu_accel_build_device", "lmgpu_accel_get_info",
                  "lmgpu_trace", "lmgpu_trace_device", "lmgpu_trace_stats_device", "lmgpu_accel_check",
-                 "lmgpu_trace_static_scene", "lmgpu_accel_set_tuning"):
+                 "lmgpu_trace_static_scene", "lmgpu_accel_set_tuning", "lmgpu_scene_create", "lmgpu_scene_accel",
+                 "lmgpu_render_pt", "lmgpu_render_pt_device"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -171,6 +178,79 @@ def trace_static_scene(d_tris_ptr: int, ntri: int, d_rays_ptr: int, d_hits_ptr: 
                        anyhit: bool = False, stream: int = 0) -> None:
     """Allocation-free build + trace on device buffers (lmgpu_trace_static_scene)."""
     _check(lib().lmgpu_trace_static_scene(d_tris_ptr, ntri, d_rays_ptr, d_hits_ptr, nrays, int(anyhit), stream))
+
+
+class Prim(ctypes.Structure):
+    _fields_ = [("bsdf", ctypes.c_int32), ("is_light", ctypes.c_int32), ("R", ctypes.c_float * 3),
+                ("Le", ctypes.c_float * 3)]
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("eye", ctypes.c_float * 3), ("center", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("fov_deg", ctypes.c_float), ("width", ctypes.c_int32), ("height", ctypes.c_int32)]
+
+
+class PtParams(ctypes.Structure):
+    _fields_ = [("spp", ctypes.c_uint64), ("max_num_vertices", ctypes.c_int32), ("seed", ctypes.c_uint32)]
+
+
+BSDF_NULL, BSDF_DIFFUSE = 0, 1
+
+
+class Scene:
+    """A device-resident scene (lmgpu_scene): triangles, primitives, camera, BVH.
+
+    `scene` is the dict of lmgpu.scenes (prims with kind 0 = diffuse,
+    1 = area light without a BSDF; camera)."""
+
+    def __init__(self, scene: dict) -> None:
+        from .scenes import scene_triangles
+
+        tris, tri_prim = scene_triangles(scene)
+        self.tris = np.ascontiguousarray(tris, dtype=np.float32)
+        self.tri_prim = np.ascontiguousarray(tri_prim, dtype=np.int32)
+        prims = (Prim * len(scene["prims"]))()
+        for i, p in enumerate(scene["prims"]):
+            prims[i].bsdf = BSDF_DIFFUSE if p["kind"] == 0 else BSDF_NULL
+            prims[i].is_light = 1 if p["kind"] == 1 else 0
+            for k in range(3):
+                prims[i].R[k] = p["R"][k]
+                prims[i].Le[k] = p["Le"][k]
+        c = scene["camera"]
+        cam = Camera()
+        for k in range(3):
+            cam.eye[k], cam.center[k], cam.up[k] = c["eye"][k], c["center"][k], c["up"][k]
+        cam.fov_deg, cam.width, cam.height = c["fov"], c["width"], c["height"]
+        self.width, self.height = c["width"], c["height"]
+        h = ctypes.c_void_p()
+        _check(lib().lmgpu_scene_create(self.tris.ctypes.data, self.tri_prim.ctypes.data, self.tris.shape[0],
+                                        ctypes.addressof(prims), len(scene["prims"]), ctypes.addressof(cam),
+                                        ctypes.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().lmgpu_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render_pt(self, spp: int, max_num_vertices: int = -1, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        """renderer::pt: film (H, W, 3) and per-pixel variance of the estimate."""
+        img = np.empty((self.height, self.width, 3), np.float32)
+        var = np.empty((self.height, self.width, 3), np.float32)
+        prm = PtParams(spp, max_num_vertices, seed)
+        _check(lib().lmgpu_render_pt(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
+        return img, var
+
+    def render_pt_device(self, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,
+                         seed: int = 0, stream: int = 0) -> None:
+        prm = PtParams(spp, max_num_vertices, seed)
+        _check(lib().lmgpu_render_pt_device(self._h, ctypes.byref(prm), d_image, d_variance, stream))
 
 
 def version() -> str:

@@ -119,3 +119,71 @@ def closed_icosphere(level: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)) ->
     Vn = np.array(verts) * radius + np.asarray(center, dtype=np.float64)
     Fn = np.array(faces)
     return Vn[Fn].reshape(-1, 9).astype(np.float32)
+
+
+# ---------------------------------------------------------------------------
+# Scenes for the path tracers.  A scene is a dict:
+#   prims  : list of {"kind": 0 diffuse | 1 area light (no BSDF),
+#                     "R": (r,g,b), "Le": (r,g,b), "tris": float32 (n, 9)}
+#            in scene order (global triangle ids follow it);
+#   camera : {"eye", "center", "up", "fov" (vertical, degrees), "width", "height"}.
+DIFFUSE, AREA_LIGHT = 0, 1
+
+
+def _quad(p0, p1, p2, p3) -> np.ndarray:
+    """Two triangles (p0,p1,p2), (p0,p2,p3); normal = (p1-p0) x (p2-p0)."""
+    return np.array([list(p0) + list(p1) + list(p2), list(p0) + list(p2) + list(p3)], dtype=np.float64)
+
+
+def _box(size, angle_deg, base_xz) -> np.ndarray:
+    """Axis-aligned box of `size` (sx, sy, sz) standing on y = 0, rotated by
+    `angle_deg` about +y around its centre, centre at base_xz; 12 outward
+    facing triangles."""
+    sx, sy, sz = size
+    x0, x1, y0, y1, z0, z1 = -sx / 2, sx / 2, 0.0, sy, -sz / 2, sz / 2
+    faces = [
+        _quad((x0, y1, z0), (x0, y1, z1), (x1, y1, z1), (x1, y1, z0)),  # top (+y)
+        _quad((x0, y0, z0), (x1, y0, z0), (x1, y0, z1), (x0, y0, z1)),  # bottom (-y)
+        _quad((x0, y0, z0), (x0, y1, z0), (x1, y1, z0), (x1, y0, z0)),  # front (-z)
+        _quad((x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1)),  # back (+z)
+        _quad((x0, y0, z0), (x0, y0, z1), (x0, y1, z1), (x0, y1, z0)),  # left (-x)
+        _quad((x1, y0, z0), (x1, y1, z0), (x1, y1, z1), (x1, y0, z1)),  # right (+x)
+    ]
+    t = np.concatenate(faces, axis=0).reshape(-1, 3)
+    a = np.radians(angle_deg)
+    R = np.array([[np.cos(a), 0, np.sin(a)], [0, 1, 0], [-np.sin(a), 0, np.cos(a)]])
+    t = t @ R.T + np.array([base_xz[0], 0.0, base_xz[1]])
+    return t.reshape(-1, 9)
+
+
+def cornell_box(width: int = 256, height: int = 256) -> dict:
+    """Procedural Cornell-style box: walls of [0,1]^3 without the z = 0 side
+    (10 triangles, normals facing in), two rotated boxes (12 + 12), and a
+    0.25 x 0.2 area light at y = 0.999 facing down (2); camera at
+    (0.5, 0.5, -1.4) looking +z, vertical fov 40 degrees."""
+    grey, red, green = (0.75, 0.75, 0.75), (0.63, 0.065, 0.05), (0.14, 0.45, 0.09)
+    walls = [
+        (grey, _quad((0, 0, 0), (0, 0, 1), (1, 0, 1), (1, 0, 0))),   # floor, +y
+        (grey, _quad((0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1))),   # ceiling, -y
+        (grey, _quad((0, 0, 1), (0, 1, 1), (1, 1, 1), (1, 0, 1))),   # back wall, -z
+        (red, _quad((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1))),    # left wall x = 0, +x
+        (green, _quad((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0))),  # right wall x = 1, -x
+    ]
+    prims = [{"kind": DIFFUSE, "R": c, "Le": (0.0, 0.0, 0.0), "tris": t.astype(np.float32)} for c, t in walls]
+    prims.append({"kind": DIFFUSE, "R": grey, "Le": (0.0, 0.0, 0.0),
+                  "tris": _box((0.3, 0.3, 0.3), -17.0, (0.68, 0.35)).astype(np.float32)})
+    prims.append({"kind": DIFFUSE, "R": grey, "Le": (0.0, 0.0, 0.0),
+                  "tris": _box((0.3, 0.6, 0.3), 17.0, (0.32, 0.65)).astype(np.float32)})
+    lx0, lx1, lz0, lz1, ly = 0.5 - 0.125, 0.5 + 0.125, 0.5 - 0.1, 0.5 + 0.1, 0.999
+    prims.append({"kind": AREA_LIGHT, "R": (0.0, 0.0, 0.0), "Le": (17.0, 12.0, 4.0),
+                  "tris": _quad((lx0, ly, lz0), (lx1, ly, lz0), (lx1, ly, lz1), (lx0, ly, lz1)).astype(np.float32)})
+    camera = {"eye": (0.5, 0.5, -1.4), "center": (0.5, 0.5, 0.0), "up": (0.0, 1.0, 0.0), "fov": 40.0,
+              "width": width, "height": height}
+    return {"prims": prims, "camera": camera}
+
+
+def scene_triangles(scene: dict) -> tuple[np.ndarray, np.ndarray]:
+    """All triangles in global order and the primitive index of each."""
+    tris = np.concatenate([p["tris"] for p in scene["prims"]], axis=0).astype(np.float32)
+    prim = np.concatenate([np.full(p["tris"].shape[0], i, np.int32) for i, p in enumerate(scene["prims"])])
+    return tris, prim

@@ -1,7 +1,12 @@
 #!/usr/bin/env bash
-# Compiles the reference's own accel sources, in place under the reference
-# tree, into a CPU oracle binary oracle/_ref/ref_accel.  Test infrastructure
-# only: nothing in the product links or runs it.
+# Compiles the reference's own accel and renderer sources, in place under the
+# reference tree, into CPU oracle binaries in oracle/_ref/:
+#   ref_accel     accel::naive / bvh_sahbin / qbvh driver (single precision)
+#   ref_render    renderer::pt with bsdf::diffuse, bsdf::null, light::area,
+#                 sensor::pinhole, Random (dSFMT) and accel::qbvh (single)
+#   ref_render64  the same in double precision (LM_USE_DOUBLE_PRECISION,
+#                 cmake/LMBuildOptions.cmake:32-43) with accel::bvh_sahbin
+# Test infrastructure only: nothing in the product links or runs them.
 #
 # The reference library cannot be built as shipped (boost, TBB, FreeImage,
 # yaml-cpp and Embree are absent), so:
@@ -9,8 +14,8 @@
 #   * each source is preprocessed and its `#pragma region` lines are dropped,
 #     because GCC 13 rejects them inside the default-member-initialiser lambdas
 #     that LM_IMPL_F creates;
-#   * oracle/refharness/ref_runtime.cpp stands in for the component factory and
-#     logger exports of liblightmetrica.
+#   * oracle/refharness/*.cpp stand in for the component factory, logger,
+#     property tree, assets, film, scheduler and scene of liblightmetrica.
 # x86-64 only: the reference forces SSE intrinsics (math.h:69, accel_qbvh.cpp:34).
 #
 # Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
@@ -28,31 +33,42 @@ case "$(uname -m)" in
 esac
 mkdir -p "$OUT"
 CXX="${CXX:-g++}"
-DEFS="-DLM_EXPORTS -DLM_USE_SINGLE_PRECISION -DNDEBUG"
-INC="-I$HERE/refharness/shim -I$REF/include"
+CC="${CC:-gcc}"
+INC="-I$HERE/refharness/shim -I$REF/include -I$REF/external-src/dSFMT-src-2.2.3"
 FLAGS="-std=c++14 -O3 -msse4.2 -ffp-contract=off -w"
+L="$REF/src/liblightmetrica"
 
-SRCS=(
-  "$REF/src/liblightmetrica/accel/accel_naive.cpp"
-  "$REF/src/liblightmetrica/accel/accel_bvh_sahbin.cpp"
-  "$REF/src/liblightmetrica/accel/accel_qbvh.cpp"
-  "$HERE/refharness/ref_runtime.cpp"
-  "$HERE/refharness/ref_accel_cli.cpp"
-)
-OBJS=()
-pids=()
-for src in "${SRCS[@]}"; do
-  base="$(basename "$src" .cpp)"
-  (
-    $CXX $FLAGS $DEFS $INC -E "$src" -o "$OUT/$base.ii"
-    sed -i -E '/^[[:space:]]*#[[:space:]]*pragma[[:space:]]+(end)?region/d' "$OUT/$base.ii"
-    $CXX $FLAGS -c -x c++ "$OUT/$base.ii" -o "$OUT/$base.o"
-    rm -f "$OUT/$base.ii"
-  ) &
-  pids+=($!)
-  OBJS+=("$OUT/$base.o")
-done
-for p in "${pids[@]}"; do wait "$p"; done
-$CXX -O3 -o "$OUT/ref_accel" "${OBJS[@]}" -lpthread
-rm -f "${OBJS[@]}"
-echo "built $OUT/ref_accel"
+ACCEL_SRCS=("$L/accel/accel_naive.cpp" "$L/accel/accel_bvh_sahbin.cpp" "$L/accel/accel_qbvh.cpp" "$HERE/refharness/ref_runtime.cpp")
+RENDER_SRCS=("$L/renderer/renderer_pt.cpp" "$L/asset/bsdf/bsdf_diffuse.cpp" "$L/asset/bsdf/bsdf_null.cpp"
+             "$L/asset/light/light_area.cpp" "$L/asset/sensor/sensor_pinhole.cpp" "$L/random.cpp"
+             "$HERE/refharness/ref_render_cli.cpp")
+
+# compile_set <tag> <defs> <sources...>: objects into $OUT/<tag>_*.o
+compile_set() {
+  local tag="$1" defs="$2"; shift 2
+  local pids=()
+  for src in "$@"; do
+    local base; base="$(basename "$src" .cpp)"
+    (
+      $CXX $FLAGS $defs $INC -E "$src" -o "$OUT/${tag}_$base.ii"
+      sed -i -E '/^[[:space:]]*#[[:space:]]*pragma[[:space:]]+(end)?region/d' "$OUT/${tag}_$base.ii"
+      $CXX $FLAGS -c -x c++ "$OUT/${tag}_$base.ii" -o "$OUT/${tag}_$base.o"
+      rm -f "$OUT/${tag}_$base.ii"
+    ) &
+    pids+=($!)
+  done
+  for p in "${pids[@]}"; do wait "$p"; done
+}
+
+S="-DLM_EXPORTS -DLM_USE_SINGLE_PRECISION -DNDEBUG"
+D="-DLM_EXPORTS -DLM_USE_DOUBLE_PRECISION -DNDEBUG"
+compile_set f "$S" "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}" "$HERE/refharness/ref_accel_cli.cpp"
+compile_set d "$D" "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}"
+$CC -O3 -msse2 -DDSFMT_MEXP=19937 -DNDEBUG -w -c "$REF/external-src/dSFMT-src-2.2.3/dSFMT.c" -o "$OUT/dsfmt.o"
+
+obj() { local tag="$1"; shift; for s in "$@"; do echo "$OUT/${tag}_$(basename "$s" .cpp).o"; done; }
+$CXX -O3 -o "$OUT/ref_accel" $(obj f "${ACCEL_SRCS[@]}" "$HERE/refharness/ref_accel_cli.cpp") -lpthread
+$CXX -O3 -o "$OUT/ref_render" $(obj f "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}") "$OUT/dsfmt.o" -lpthread
+$CXX -O3 -o "$OUT/ref_render64" $(obj d "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}") "$OUT/dsfmt.o" -lpthread
+rm -f "$OUT"/*.o
+echo "built $OUT/ref_accel $OUT/ref_render $OUT/ref_render64"

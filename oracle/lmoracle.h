@@ -64,6 +64,32 @@ void       lmo_accel_stats(const lmo_accel* a, size_t* nodes, size_t* leaves, in
  * of triangle `tri` (9 floats), and of its barycentrics (b1, b2). */
 double     lmo_plane_t_fp64(const float* tri, const float* ray, double* b1, double* b2);
 
+/* ---- renderer::pt (lmoracle_pt.c) ---- */
+
+#define LMO_BSDF_NULL 0
+#define LMO_BSDF_DIFFUSE 1
+
+/* One scene primitive: its BSDF and, when is_light, an area light on it. */
+typedef struct {
+    int32_t bsdf;      /* LMO_BSDF_NULL or LMO_BSDF_DIFFUSE */
+    int32_t is_light;
+    float R[3];
+    float Le[3];
+} lmo_pt_prim;
+
+/* Pinhole camera from a lookat node; fov is vertical, in degrees. */
+typedef struct {
+    float eye[3], center[3], up[3];
+    float fov_deg;
+    int32_t width, height;
+} lmo_pt_camera;
+
+/* Renders num_samples paths with `threads` threads; fills per-pixel sums of
+ * splatted values and of their squares (H*W*3 doubles each, row = raster y). */
+uint64_t lmo_render_pt(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
+                       const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices, uint64_t seed,
+                       int threads, double* sum, double* sumsq);
+
 #ifdef __cplusplus
 }
 #endif

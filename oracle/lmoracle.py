@@ -49,6 +49,9 @@ def lib() -> ctypes.CDLL:
         L.lmo_accel_stats.restype = None
         L.lmo_plane_t_fp64.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         L.lmo_plane_t_fp64.restype = ctypes.c_double
+        L.lmo_render_pt.argtypes = [vp, vp, sz, vp, vp, ctypes.c_uint64, ctypes.c_int, ctypes.c_uint64,
+                                    ctypes.c_int, vp, vp]
+        L.lmo_render_pt.restype = ctypes.c_uint64
         _lib = L
     return _lib
 
@@ -126,3 +129,109 @@ REF_OUT_DTYPE = np.dtype([("id", "<i4"), ("p", "<f4", (3,)), ("b", "<f4", (2,))]
 
 def read_ref_output(path: str) -> np.ndarray:
     return np.fromfile(path, dtype=REF_OUT_DTYPE)
+
+
+REF_RENDER = os.path.join(HERE, "_ref", "ref_render")
+REF_RENDER64 = os.path.join(HERE, "_ref", "ref_render64")
+
+
+def write_render_scene(path: str, scene: dict, num_samples: int, max_num_vertices: int, seed: int,
+                       threads: int) -> None:
+    """Writes the input file of oracle/_ref/ref_render (refharness/ref_render_cli.cpp)."""
+    cam = scene["camera"]
+    with open(path, "wb") as f:
+        f.write(np.array([0x53524D4C, 1, cam["width"], cam["height"]], dtype=np.uint32).tobytes())
+        f.write(np.array(list(cam["eye"]) + list(cam["center"]) + list(cam["up"]) + [cam["fov"]],
+                         dtype=np.float32).tobytes())
+        f.write(np.uint32(len(scene["prims"])).tobytes())
+        for p in scene["prims"]:
+            f.write(np.int32(p["kind"]).tobytes())
+            f.write(np.array(list(p["R"]) + list(p["Le"]), dtype=np.float32).tobytes())
+            t = np.ascontiguousarray(p["tris"], dtype=np.float32).reshape(-1, 9)
+            f.write(np.uint32(t.shape[0]).tobytes())
+            f.write(t.tobytes())
+        f.write(np.uint64(num_samples).tobytes())
+        f.write(np.int32(max_num_vertices).tobytes())
+        f.write(np.uint32(seed).tobytes())
+        f.write(np.uint32(threads).tobytes())
+
+
+def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,
+                   double: bool = False) -> dict:
+    """Runs the reference renderer::pt (compiled from its sources) and returns
+    the film (H, W, 3), the per-pixel variance of that estimate and timing."""
+    import json
+    import tempfile
+
+    cam = scene["camera"]
+    W, H = cam["width"], cam["height"]
+    with tempfile.TemporaryDirectory() as tmp:
+        ps, po = os.path.join(tmp, "scene.bin"), os.path.join(tmp, "out.bin")
+        write_render_scene(ps, scene, num_samples, max_num_vertices, seed, threads)
+        exe = REF_RENDER64 if double else REF_RENDER
+        out = subprocess.run([exe, ps, po], capture_output=True, text=True, check=True).stdout
+        raw = open(po, "rb").read()
+    n = W * H * 3
+    img = np.frombuffer(raw[:4 * n], dtype=np.float32).reshape(H, W, 3)
+    sumsq = np.frombuffer(raw[4 * n:12 * n], dtype=np.float64).reshape(H, W, 3)
+    N = int(np.frombuffer(raw[12 * n:12 * n + 8], dtype=np.uint64)[0])
+    return {"image": img, "variance": pixel_variance(img.astype(np.float64), sumsq, N, W * H), "samples": N,
+            "info": json.loads(out.strip().splitlines()[-1])}
+
+
+def pixel_variance(image: np.ndarray, sumsq: np.ndarray, num_samples: int, num_pixels: int) -> np.ndarray:
+    """Variance of the film estimate I_p = (W H / N) sum_i C_i [i in p] with
+    raster positions uniform over the film (renderer_pt.cpp:84-91,
+    film_hdr.cpp:218-223, scheduler.cpp:281-288): with X_i = C_i [i in p],
+    Var(I_p) = (W H)^2 Var(X) / N, Var(X) = E[X^2] - E[X]^2."""
+    scale = num_pixels / num_samples
+    ex = image / scale / num_samples          # E[X] = (sum_i X_i) / N
+    ex2 = sumsq / num_samples                 # E[X^2]
+    return (num_pixels ** 2) * np.maximum(ex2 - ex * ex, 0.0) / num_samples
+
+
+class PtPrim(ctypes.Structure):
+    _fields_ = [("bsdf", ctypes.c_int32), ("is_light", ctypes.c_int32), ("R", ctypes.c_float * 3),
+                ("Le", ctypes.c_float * 3)]
+
+
+class PtCamera(ctypes.Structure):
+    _fields_ = [("eye", ctypes.c_float * 3), ("center", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("fov_deg", ctypes.c_float), ("width", ctypes.c_int32), ("height", ctypes.c_int32)]
+
+
+def scene_prims(scene: dict) -> "ctypes.Array":
+    """Scene primitives in the oracle's layout (kind 0 = diffuse, 1 = light without BSDF)."""
+    arr = (PtPrim * len(scene["prims"]))()
+    for i, p in enumerate(scene["prims"]):
+        arr[i].bsdf = 1 if p["kind"] == 0 else 0
+        arr[i].is_light = 1 if p["kind"] == 1 else 0
+        for k in range(3):
+            arr[i].R[k] = p["R"][k]
+            arr[i].Le[k] = p["Le"][k]
+    return arr
+
+
+def scene_camera(scene: dict) -> PtCamera:
+    c = scene["camera"]
+    cam = PtCamera()
+    for k in range(3):
+        cam.eye[k], cam.center[k], cam.up[k] = c["eye"][k], c["center"][k], c["up"][k]
+    cam.fov_deg, cam.width, cam.height = c["fov"], c["width"], c["height"]
+    return cam
+
+
+def render_pt(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int) -> dict:
+    """The oracle's renderer::pt: film (H, W, 3) and per-pixel variance."""
+    tris = np.ascontiguousarray(np.concatenate([p["tris"] for p in scene["prims"]]), dtype=np.float32)
+    tri_prim = np.concatenate([np.full(p["tris"].shape[0], i, np.int32) for i, p in enumerate(scene["prims"])])
+    W, H = scene["camera"]["width"], scene["camera"]["height"]
+    s = np.zeros((H, W, 3), np.float64)
+    q = np.zeros((H, W, 3), np.float64)
+    prims = scene_prims(scene)
+    cam = scene_camera(scene)
+    lib().lmo_render_pt(tris.ctypes.data, tri_prim.ctypes.data, tris.shape[0], ctypes.addressof(prims),
+                        ctypes.addressof(cam), num_samples, max_num_vertices, seed, threads, s.ctypes.data,
+                        q.ctypes.data)
+    img = s * (W * H / num_samples)
+    return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}

@@ -12,6 +12,11 @@ Fixtures written:
       directions normalised by the reference's own Math::Normalize, the
       expected values that test asserts (p, gn, sn, uv), and the hits of the
       reference accels naive / bvh_sahbin / qbvh on those rays.
+  cornell_pt.npz
+      The Cornell-style box of the path-tracing configuration at 64x64: the
+      scene, and the film and per-pixel variance of the reference's own
+      renderer::pt (compiled from its sources) at 16,384 samples per pixel,
+      in single precision and in double precision (LM_USE_DOUBLE_PRECISION).
   soup_small.npz
       A seeded three-primitive scene (random triangle soup, heightfield,
       duplicated triangles for exact-t ties, zero-area triangles) and rays
@@ -156,15 +161,37 @@ def soup_case(tmp: str) -> dict:
     return out
 
 
+def cornell_case() -> dict:
+    sc = scenes.cornell_box(64, 64)
+    W, H = 64, 64
+    N = W * H * 16384
+    f = lo.run_ref_render(sc, N, 9, 20240601, os.cpu_count() or 8)
+    d = lo.run_ref_render(sc, N, 9, 20240602, os.cpu_count() or 8, double=True)
+    out = {"width": np.int32(W), "height": np.int32(H), "num_samples": np.int64(N), "max_num_vertices": np.int32(9),
+           "ref_image": f["image"].astype(np.float32), "ref_variance": f["variance"].astype(np.float32),
+           "ref64_image": d["image"].astype(np.float64), "ref64_variance": d["variance"].astype(np.float64)}
+    for i, p in enumerate(sc["prims"]):
+        out[f"prim{i}_tris"] = p["tris"]
+        out[f"prim{i}_kind"] = np.int32(p["kind"])
+        out[f"prim{i}_R"] = np.array(p["R"], np.float32)
+        out[f"prim{i}_Le"] = np.array(p["Le"], np.float32)
+    out["nprims"] = np.int32(len(sc["prims"]))
+    c = sc["camera"]
+    out["cam_eye"], out["cam_center"], out["cam_up"] = (np.array(c[k], np.float32) for k in ("eye", "center", "up"))
+    out["cam_fov"] = np.float32(c["fov"])
+    return out
+
+
 def main() -> None:
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if not os.path.exists(lo.REF_ACCEL):
+    if not (os.path.exists(lo.REF_ACCEL) and os.path.exists(lo.REF_RENDER) and os.path.exists(lo.REF_RENDER64)):
         subprocess.run([os.path.join(REPO, "oracle", "build_ref.sh"), ref], check=True)
     src = open(os.path.join(ref, "src", "lightmetrica-test", "test_accel3.cpp")).read()
     with tempfile.TemporaryDirectory() as tmp:
         np.savez_compressed(os.path.join(HERE, "accel3_simple.npz"), **accel3_case(src, "StubTriangleMesh_Simple", False, tmp))
         np.savez_compressed(os.path.join(HERE, "accel3_simple2.npz"), **accel3_case(src, "StubTriangleMesh_Simple2", True, tmp))
         np.savez_compressed(os.path.join(HERE, "soup_small.npz"), **soup_case(tmp))
+    np.savez_compressed(os.path.join(HERE, "cornell_pt.npz"), **cornell_case())
     print("fixtures written to", HERE)
 
 

@@ -1,0 +1,91 @@
+"""renderer::pt on the GPU (lmgpu_render_pt) against the reference's own
+renderer::pt and the oracle, per pixel within the statistical bar of
+tests/imgcheck.py."""
+import os
+
+import numpy as np
+import pytest
+
+import imgcheck
+import ptscene
+
+pytestmark = pytest.mark.gpu
+
+
+def render(gpu_lib, scene, spp, max_nv, seed):
+    sc = gpu_lib.Scene(scene)
+    img, var = sc.render_pt(spp, max_nv, seed)
+    sc.close()
+    return img, var
+
+
+def test_pt_matches_reference_film(gpu_lib, golden_dir):
+    """Per pixel against the reference film (16,384 spp, single and double precision)."""
+    scene, z = ptscene.load_cornell(golden_dir)
+    img, var = render(gpu_lib, scene, 16384, int(z["max_num_vertices"]), 7)
+    s32 = imgcheck.assert_same_image(img, var, z["ref_image"], z["ref_variance"], "gpu vs ref f32")
+    s64 = imgcheck.assert_same_image(img, var, z["ref64_image"], z["ref64_variance"], "gpu vs ref f64")
+    print("vs f32", s32, "\nvs f64", s64)
+    rel = imgcheck.relmse(img, z["ref64_image"])
+    print("relMSE vs FP64 reference", rel)
+
+
+def test_pt_matches_oracle_on_variant_scene(gpu_lib, oracle_lib, golden_dir):
+    """A non-square film, other fov and light, shorter paths: GPU vs oracle."""
+    scene, _ = ptscene.load_cornell(golden_dir)
+    scene["camera"].update(width=48, height=32, fov=55.0)
+    scene["prims"][-1]["Le"] = (4.0, 9.0, 20.0)
+    img, var = render(gpu_lib, scene, 16384, 6, 11)
+    r = oracle_lib.render_pt(scene, 48 * 32 * 4096, 6, 99, os.cpu_count() or 4)
+    a, va = ptscene.downsample(img.astype(np.float64), var.astype(np.float64), 2)
+    b, vb = ptscene.downsample(r["image"], r["variance"], 2)
+    print(imgcheck.assert_same_image(a, va, b, vb, "gpu vs oracle"))
+
+
+def test_pt_deterministic_and_seeded(gpu_lib, golden_dir):
+    scene, _ = ptscene.load_cornell(golden_dir)
+    sc = gpu_lib.Scene(scene)
+    a, _ = sc.render_pt(256, 9, 3)
+    b, _ = sc.render_pt(256, 9, 3)
+    c, _ = sc.render_pt(256, 9, 4)
+    sc.close()
+    # film sums are float atomics: equal up to summation order
+    assert np.allclose(a, b, rtol=1e-5, atol=1e-6)
+    assert not np.allclose(a, c)
+
+
+def test_pt_two_vertices_only_lights(gpu_lib, golden_dir):
+    scene, _ = ptscene.load_cornell(golden_dir)
+    img, _ = render(gpu_lib, scene, 64, 2, 1)
+    lit = img.sum(axis=2) > 0
+    assert 0 < lit.sum() < 0.05 * lit.size
+    # directly seen light: exactly Le (throughput 1)
+    le = np.array(scene["prims"][-1]["Le"], np.float32)
+    full = np.all(np.isclose(img, le, rtol=1e-5), axis=2)
+    assert full.sum() > 0
+
+
+def test_pt_device_entry_matches_host_entry(gpu_lib, golden_dir):
+    import torch
+
+    scene, _ = ptscene.load_cornell(golden_dir)
+    sc = gpu_lib.Scene(scene)
+    a, va = sc.render_pt(128, 9, 21)
+    di = torch.empty((64, 64, 3), dtype=torch.float32, device="cuda")
+    dv = torch.empty((64, 64, 3), dtype=torch.float32, device="cuda")
+    sc.render_pt_device(di.data_ptr(), dv.data_ptr(), 128, 9, 21, torch.cuda.current_stream().cuda_stream)
+    sc.close()
+    assert np.allclose(di.cpu().numpy(), a, rtol=1e-5, atol=1e-6)
+    assert np.allclose(dv.cpu().numpy(), va, rtol=1e-4, atol=1e-6)
+
+
+def test_pt_full_configuration_256_64spp(gpu_lib, golden_dir):
+    """The path-tracing configuration at full size (256 x 256, 64 spp, 8
+    segments): 8 x 8 block means against 2 x 2 block means of the 64 x 64
+    reference film (the same 32 x 32 raster cells)."""
+    scene, z = ptscene.load_cornell(golden_dir)
+    scene["camera"].update(width=256, height=256)
+    img, var = render(gpu_lib, scene, 64, 9, 2024)
+    a, va = ptscene.downsample(img.astype(np.float64), var.astype(np.float64), 8)
+    b, vb = ptscene.downsample(z["ref_image"].astype(np.float64), z["ref_variance"].astype(np.float64), 2)
+    print(imgcheck.assert_same_image(a, va, b, vb, "gpu 256x256x64 vs ref"))
