@@ -323,6 +323,65 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
+def run_pt(args) -> None:
+    """Path-tracing configuration: renderer::pt on the Cornell-style box,
+    256 x 256, 64 samples per pixel, max_num_vertices 9 (8 segments).
+    Metric Msamples/s; value = device-resident film, e2e = the host-pointer
+    lmgpu_render_pt (film copied back every step)."""
+    import torch
+
+    import lmgpu
+    from lmgpu import scenes
+
+    W = H = 256
+    spp, max_nv = 64, 9
+    scene = scenes.cornell_box(W, H)
+    stream = torch.cuda.Stream()
+    sc = lmgpu.Scene(scene)
+    di = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    dv = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    samples = W * H * spp
+    for k in range(args.warmup):
+        sc.render_pt_device(di.data_ptr(), dv.data_ptr(), spp, max_nv, k, stream.cuda_stream)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for k in range(args.steps):
+        sc.render_pt_device(di.data_ptr(), dv.data_ptr(), spp, max_nv, 1000 + k, stream.cuda_stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        sc.render_pt(spp, max_nv, 2000 + k)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import lmoracle
+
+    threads = os.cpu_count() or 1
+    n_cpu = W * H * 8
+    t0 = time.perf_counter()
+    lmoracle.render_pt(scene, n_cpu, max_nv, 5, threads)
+    cpu_s = time.perf_counter() - t0
+    line = {"metric": "Msamples/s (renderer::pt)", "value": samples / ms / 1e3, "unit": "Msamples/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural Cornell box)",
+            "config": {"workload": "pt_cornell_256x256_64spp", "width": W, "height": H, "spp": spp,
+                       "max_num_vertices": max_nv, "triangles": 36},
+            "e2e": {"value": samples / e2e_s / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": W * H * 3 * 4 * 2, "api": "lmgpu_render_pt (host film)"},
+            "clocks": clk,
+            "cpu_baseline": {"value": n_cpu / cpu_s / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+                             "sample": f"{n_cpu} samples (8 spp) of the same scene, oracle restatement of "
+                                       f"renderer::pt (renderer_pt.cpp), {threads} threads"}}
+    print(json.dumps(line), flush=True)
+    sc.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -332,6 +391,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling of smaller cases)")
     ap.add_argument("--anyhit", action="store_true", help="time any-hit queries instead of closest hit")
+    ap.add_argument("--workload", choices=["raycast", "pt"], default="raycast",
+                    help="raycast: the BVH ray-cast configuration (default); pt: renderer::pt on the Cornell box")
     ap.add_argument("--use-ref-binary", action="store_true",
                     help="reference arm: time the reference's own qbvh (x86-64 harness) if built")
     args = ap.parse_args()
@@ -339,6 +400,8 @@ def main() -> None:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "pt":
+        run_pt(args)
     else:
         run_gpu(args)
 

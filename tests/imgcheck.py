@@ -57,6 +57,16 @@ def assert_same_image(a, va, b, vb, label=""):
     return s
 
 
+def assert_same_aggregates(a, va, b, vb, label=""):
+    """Bias check for low-sample renders, whose per-pixel statistics are not
+    yet normal: image totals within 4 sigma and 8 x 8 block means within 4.5
+    sigma, per channel."""
+    s = compare(a, va, b, vb)
+    assert max(abs(x) for x in s["total_z"]) < 4.0, (label, s)
+    assert s["block_max_abs_z"] < 4.5, (label, s)
+    return s
+
+
 def relmse(img, ref, eps=1e-2):
     """Relative MSE of img against ref: mean((img - ref)^2 / (ref^2 + eps))."""
     img = np.asarray(img, np.float64)

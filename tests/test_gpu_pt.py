@@ -36,7 +36,7 @@ def test_pt_matches_oracle_on_variant_scene(gpu_lib, oracle_lib, golden_dir):
     scene["camera"].update(width=48, height=32, fov=55.0)
     scene["prims"][-1]["Le"] = (4.0, 9.0, 20.0)
     img, var = render(gpu_lib, scene, 16384, 6, 11)
-    r = oracle_lib.render_pt(scene, 48 * 32 * 4096, 6, 99, os.cpu_count() or 4)
+    r = oracle_lib.render_pt(scene, 48 * 32 * 16384, 6, 99, os.cpu_count() or 4)
     a, va = ptscene.downsample(img.astype(np.float64), var.astype(np.float64), 2)
     b, vb = ptscene.downsample(r["image"], r["variance"], 2)
     print(imgcheck.assert_same_image(a, va, b, vb, "gpu vs oracle"))
@@ -81,11 +81,18 @@ def test_pt_device_entry_matches_host_entry(gpu_lib, golden_dir):
 
 def test_pt_full_configuration_256_64spp(gpu_lib, golden_dir):
     """The path-tracing configuration at full size (256 x 256, 64 spp, 8
-    segments): 8 x 8 block means against 2 x 2 block means of the 64 x 64
-    reference film (the same 32 x 32 raster cells)."""
+    segments).  At 64 spp per-pixel statistics are far from normal, so the
+    checks are the aggregates: 4 x 4 block means against 1 x 1 pixels of the
+    64 x 64 reference film (the same raster cells) via totals and 8 x 8
+    blocks, and the measured relMSE against the FP64 reference film must
+    match what the render's own variance predicts."""
     scene, z = ptscene.load_cornell(golden_dir)
     scene["camera"].update(width=256, height=256)
     img, var = render(gpu_lib, scene, 64, 9, 2024)
-    a, va = ptscene.downsample(img.astype(np.float64), var.astype(np.float64), 8)
-    b, vb = ptscene.downsample(z["ref_image"].astype(np.float64), z["ref_variance"].astype(np.float64), 2)
-    print(imgcheck.assert_same_image(a, va, b, vb, "gpu 256x256x64 vs ref"))
+    a, va = ptscene.downsample(img.astype(np.float64), var.astype(np.float64), 4)
+    print(imgcheck.assert_same_aggregates(a, va, z["ref_image"], z["ref_variance"], "gpu 256x256x64 vs ref"))
+    ref = z["ref64_image"].astype(np.float64)
+    measured = imgcheck.relmse(a, ref)
+    predicted = float(np.mean((va + z["ref64_variance"]) / (ref * ref + 1e-2)))
+    print("relMSE at 64 spp (4x4 blocks) vs FP64 reference", measured, "predicted", predicted)
+    assert measured < 3.0 * predicted
