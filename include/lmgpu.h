@@ -123,17 +123,25 @@ int lmgpu_accel_check(const lmgpu_accel* accel, void* stream);
 
 /* ---- Path tracing (renderer::pt) -------------------------------------- */
 
-#define LMGPU_BSDF_NULL 0     /* bsdf::null: paths end here (bsdf_null.cpp) */
-#define LMGPU_BSDF_DIFFUSE 1  /* bsdf::diffuse, reflectance R (bsdf_diffuse.cpp) */
+#define LMGPU_BSDF_NULL 0           /* bsdf::null: paths end here (bsdf_null.cpp) */
+#define LMGPU_BSDF_DIFFUSE 1        /* bsdf::diffuse, reflectance R (bsdf_diffuse.cpp) */
+#define LMGPU_BSDF_DIELECTRIC 2     /* bsdf::flesnel, R, eta1 (outside), eta2 (inside) */
+#define LMGPU_BSDF_COOK_TORRANCE 3  /* bsdf::cook_torrance: GGX, R, conductor eta/k, roughness */
 
 /* One scene primitive (Primitive, include/lightmetrica/primitive.h:56-80):
  * its BSDF and, if is_light, an area light (light::area, light_area.cpp)
- * with radiance Le over its triangles, emitting on the front side. */
+ * with radiance Le over its triangles, emitting on the front side.
+ * Parameter defaults of the reference: eta1 1, eta2 2 (bsdf_flesnel.cpp:49-50);
+ * ct_eta (0.14, 0.129, 0.1585), ct_k (4.58625, 3.348125, 2.329375),
+ * roughness 0.1 (bsdf_cooktorrance.cpp:58-63). */
 typedef struct {
     int32_t bsdf;
     int32_t is_light;
     float R[3];
     float Le[3];
+    float eta1, eta2;
+    float ct_eta[3], ct_k[3];
+    float roughness;
 } lmgpu_prim;
 
 /* Pinhole sensor at a lookat node (scene3.cpp:213-221, sensor_pinhole.cpp):
@@ -163,6 +171,12 @@ int lmgpu_scene_create(const float* triangles, const int32_t* tri_prim, uint64_t
 
 /* Frees a scene and everything it owns.  NULL is ignored. */
 void lmgpu_scene_destroy(lmgpu_scene* scene);
+
+/* Adds (Le != NULL) or removes a constant environment light (light::env
+ * without an envmap, light_env.cpp): radiance Le arrives from every
+ * direction on the scene's bounding sphere (scene3.cpp:52-78), which rays
+ * meet when they leave the geometry (scene3.cpp:464-475). */
+int lmgpu_scene_set_environment(lmgpu_scene* scene, const float* Le);
 
 /* The scene's accel (owned by the scene), for ray queries on its triangles. */
 int lmgpu_scene_accel(const lmgpu_scene* scene, const lmgpu_accel** accel);

@@ -7,6 +7,10 @@
 // Russian roulette with probability 0.5 after every hit, and stops after
 // max_num_vertices vertices or at a surface whose BSDF is null.
 //
+// BSDFs: bsdf::null, bsdf::diffuse, bsdf::flesnel (dielectric) and
+// bsdf::cook_torrance (GGX conductor); lights: light::area on primitives and a
+// constant light::env reached by rays that leave the geometry.
+//
 // GPU structure, one wave of up to kWave paths at a time:
 //   k_pt_generate   camera rays for paths [p0, p0 + n) (sensor_pinhole.cpp:79-90)
 //   k_trace         closest hit for the queue (trace.cu)
@@ -99,6 +103,124 @@ __global__ void k_pt_generate(CameraGPU cam, uint64_t p0, uint32_t n, uint32_t s
     state[i] = s;
 }
 
+// BSDF_Flesnel::EvaluateFresnelTerm (bsdf_flesnel.cpp:243-257).
+__device__ __forceinline__ float fresnel_dielectric(float wiDotN, float etaI, float etaT)
+{
+    const float eta = etaI / etaT;
+    const float cosThetaTSq = 1.0f - eta * eta * (1.0f - wiDotN * wiDotN);
+    if (cosThetaTSq <= 0.0f) return 1.0f;
+    const float ci = fabsf(wiDotN), ct = sqrtf(cosThetaTSq);
+    const float rs = (etaI * ci - etaT * ct) / (etaI * ci + etaT * ct);
+    const float rt = (etaI * ct - etaT * ci) / (etaI * ct + etaT * ci);
+    return (rs * rs + rt * rt) * 0.5f;
+}
+
+// BSDF_CookTorrance::EvaluateGGX (bsdf_cooktorrance.cpp:187-198).
+__device__ __forceinline__ float ggx_d(float3 H, float a)
+{
+    const float c = H.z;
+    if (c <= 0.0f) return 0.0f;
+    const float t = 1.0f - c * c;
+    const float tanH = t <= 0.0f ? 0.0f : sqrtf(t) / c;
+    const float q = a * a + tanH * tanH;
+    return (a * a) / (3.14159265358979f * c * c * c * c * q * q);
+}
+
+// BSDF_CookTorrance::SampleGGX (bsdf_cooktorrance.cpp:200-225); Math::Eps<float> = 1e-4.
+__device__ __forceinline__ float3 ggx_sample(float ua, float ub, float a)
+{
+    const float eps = 1e-4f;
+    const float u0 = (1.0f - eps) * ua + eps;
+    const float u1 = (1.0f - 2.0f * eps) * ub + eps;
+    const float den = sqrtf(1.0f - (1.0f - a * a) * u0);
+    const float cosT = sqrtf(1.0f - u0) / den;
+    const float sinT = a * (sqrtf(u0) / den);
+    float sp, cp;
+    sincosf(3.14159265358979f * (2.0f * u1 - 1.0f), &sp, &cp);
+    return f3(sinT * cp, sinT * sp, cosT);
+}
+
+// BSDF_CookTorrance::EvaluateFrConductor (bsdf_cooktorrance.cpp:283-291), one channel.
+__device__ __forceinline__ float fresnel_conductor(float c, float eta, float k)
+{
+    const float tmp = (eta * eta + k * k) * (c * c);
+    const float rParl2 = (tmp - eta * (2.0f * c) + 1.0f) / (tmp + eta * (2.0f * c) + 1.0f);
+    const float tmpF = eta * eta + k * k;
+    const float rPerp2 = (tmpF - eta * (2.0f * c) + c * c) / (tmpF + eta * (2.0f * c) + c * c);
+    return (rParl2 + rPerp2) * 0.5f;
+}
+
+// Samples the BSDF of P at a surface with normal n (shading normal = geometric
+// normal: meshes here carry no vertex normals) for the eye-to-light transport
+// direction.  Returns false when the path ends; otherwise the world-space
+// direction wo and the weight f = fs / pdf (projected solid angle).
+__device__ __forceinline__ bool sample_bsdf(const PrimGPU& P, float3 n, float3 wi, float u0, float u1, float u2,
+                                            float3& wo, float f[3])
+{
+    float3 bx, by;
+    basis(n, bx, by);
+    const float3 lwi = f3(dot3(wi, bx), dot3(wi, by), dot3(wi, n));
+    float3 lwo;
+    if (P.bsdf == LMGPU_BSDF_DIFFUSE) {
+        // bsdf_diffuse.cpp:69-104: one-sided, fs / pdf = R
+        if (lwi.z <= 0.0f) return false;
+        lwo = cosine_hemisphere(u0, u1);
+        if (lwo.z <= 0.0f) return false;
+        for (int k = 0; k < 3; k++) f[k] = P.R[k];
+    } else if (P.bsdf == LMGPU_BSDF_DIELECTRIC) {
+        // bsdf_flesnel.cpp:59-164: reflect with probability Fr, else refract;
+        // fs / pdf = R, or R (etaI / etaT)^2 for refraction (EL direction)
+        float etaI = P.eta1, etaT = P.eta2;
+        if (lwi.z < 0.0f) { const float t = etaI; etaI = etaT; etaT = t; }
+        const float Fr = fresnel_dielectric(lwi.z, etaI, etaT);
+        float scale = 1.0f;
+        if (u2 <= Fr) {
+            lwo = f3(-lwi.x, -lwi.y, lwi.z);
+        } else {
+            const float eta = etaI / etaT;
+            const float cosTSq = 1.0f - eta * eta * (1.0f - lwi.z * lwi.z);
+            const float cosT = sqrtf(fmaxf(cosTSq, 0.0f)) * (lwi.z > 0.0f ? -1.0f : 1.0f);
+            lwo = f3(-eta * lwi.x, -eta * lwi.y, cosT);
+            scale = eta * eta;
+        }
+        for (int k = 0; k < 3; k++) f[k] = P.R[k] * scale;
+    } else if (P.bsdf == LMGPU_BSDF_COOK_TORRANCE) {
+        // bsdf_cooktorrance.cpp:73-120, GGX; G uses |wo.H| in both terms
+        if (lwi.z <= 0.0f) return false;
+        const float3 H = ggx_sample(u0, u1, P.roughness);
+        const float dih = -dot3(lwi, H);
+        lwo = (lwi * -1.0f) - H * (2.0f * dih);
+        if (lwo.z <= 0.0f) return false;
+        const float3 Hn = normalize3(lwi + lwo);
+        const float D = ggx_d(Hn, P.roughness);
+        const float woH = fabsf(dot3(lwo, Hn));
+        const float G = fminf(1.0f, fminf(2.0f * Hn.z * lwo.z / woH, 2.0f * Hn.z * lwi.z / woH));
+        const float pdf = D * Hn.z / (4.0f * dot3(lwo, Hn)) / lwo.z;
+        if (!(pdf > 0.0f)) return false;
+        const float cih = dot3(lwi, Hn);
+        for (int k = 0; k < 3; k++) {
+            const float F = fresnel_conductor(cih, P.ct_eta[k], P.ct_k[k]);
+            f[k] = (P.R[k] * D * G * F / (4.0f * lwi.z) / lwo.z) / pdf;
+        }
+    } else {
+        return false;  // bsdf::null
+    }
+    if (f[0] == 0.0f && f[1] == 0.0f && f[2] == 0.0f) return false;
+    wo = bx * lwo.x + by * lwo.y + n * lwo.z;
+    return true;
+}
+
+__device__ __forceinline__ void splat(float* __restrict__ film, double* __restrict__ film_sq, uint32_t pixel,
+                                      const float c[3])
+{
+    for (int k = 0; k < 3; k++) {
+        if (c[k] != 0.0f) {
+            atomicAdd(&film[3 * (size_t)pixel + k], c[k]);
+            atomicAdd(&film_sq[3 * (size_t)pixel + k], (double)c[k] * (double)c[k]);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(const float4* __restrict__ rays,
                                                             const PathState* __restrict__ state,
                                                             const lmgpu_hit* __restrict__ hits, uint32_t n,
@@ -114,46 +236,43 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(const float4* __rest
     PathState ns;
     if (i < n) {
         const lmgpu_hit h = hits[i];
-        if (h.prim >= 0) {
+        const PathState s = state[i];
+        const uint32_t pixel = __float_as_uint(s.thr.w);
+        if (h.prim < 0) {
+            // miss: the environment light, if any (scene3.cpp:464-475); the
+            // path ends there (renderer_pt.cpp:200-203)
+            if (sc.has_env) {
+                const float c[3] = {s.thr.x * sc.env_Le[0], s.thr.y * sc.env_Le[1], s.thr.z * sc.env_Le[2]};
+                splat(film, film_sq, pixel, c);
+            }
+        } else {
             const float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
-            PathState s = state[i];
             const float3 o = f3(r0.x, r0.y, r0.z), d = f3(r1.x, r1.y, r1.z);
             const float* T = sc.tris + 9 * (size_t)h.prim;
             const float3 p1 = f3(T[0], T[1], T[2]), p2 = f3(T[3], T[4], T[5]), p3 = f3(T[6], T[7], T[8]);
             const float3 gn = normalize3(cross3(p2 - p1, p3 - p1));
             const PrimGPU P = sc.prims[sc.tri_prim[h.prim]];
             const float3 pos = o + d * h.t;
-            const uint32_t pixel = __float_as_uint(s.thr.w);
             uint32_t nv = s.id.z;
             if (P.is_light && -dot3(d, gn) > 0.0f) {
                 // throughput * Le(-d) * EvaluatePosition (= 1), renderer_pt.cpp:183-194
                 const float c[3] = {s.thr.x * P.Le[0], s.thr.y * P.Le[1], s.thr.z * P.Le[2]};
-                for (int k = 0; k < 3; k++) {
-                    if (c[k] != 0.0f) {
-                        atomicAdd(&film[3 * (size_t)pixel + k], c[k]);
-                        atomicAdd(&film_sq[3 * (size_t)pixel + k], (double)c[k] * (double)c[k]);
-                    }
-                }
+                splat(film, film_sq, pixel, c);
             }
             const Philox4x32 r = philox4x32_10(s.id.x, s.id.y, nv, 0u, seed, kKeyBounce);
             // Russian roulette, probability 0.5 (renderer_pt.cpp:207-216)
-            if (u01(r.v[2]) <= 0.5f) {
+            if (u01(r.v[3]) <= 0.5f) {
                 nv++;
                 const bool more = max_nv < 0 || (int)nv < max_nv;
-                const float3 wi = d * -1.0f;
-                if (more && P.bsdf == LMGPU_BSDF_DIFFUSE && dot3(wi, gn) > 0.0f) {
-                    float3 bx, by;
-                    basis(gn, bx, by);
-                    const float3 lw = cosine_hemisphere(u01(r.v[0]), u01(r.v[1]));
-                    const float3 wo = bx * lw.x + by * lw.y + gn * lw.z;
-                    if (lw.z > 0.0f && dot3(wo, gn) > 0.0f) {
-                        keep = true;
-                        nr0 = make_float4(pos.x, pos.y, pos.z, 1e-4f);
-                        nr1 = make_float4(wo.x, wo.y, wo.z, FLT_MAX);
-                        ns.thr = make_float4(2.0f * s.thr.x * P.R[0], 2.0f * s.thr.y * P.R[1],
-                                             2.0f * s.thr.z * P.R[2], s.thr.w);
-                        ns.id = make_uint4(s.id.x, s.id.y, nv, 0u);
-                    }
+                float3 wo;
+                float f[3];
+                if (more && sample_bsdf(P, gn, d * -1.0f, u01(r.v[0]), u01(r.v[1]), u01(r.v[2]), wo, f)) {
+                    keep = true;
+                    nr0 = make_float4(pos.x, pos.y, pos.z, 1e-4f);
+                    nr1 = make_float4(wo.x, wo.y, wo.z, FLT_MAX);
+                    ns.thr = make_float4(2.0f * s.thr.x * f[0], 2.0f * s.thr.y * f[1], 2.0f * s.thr.z * f[2],
+                                         s.thr.w);
+                    ns.id = make_uint4(s.id.x, s.id.y, nv, 0u);
                 }
             }
         }

@@ -63,6 +63,8 @@ SceneGPU scene_view(const lmgpu_scene* sc)
     g.tris = sc->tris;
     g.tri_prim = sc->tri_prim;
     g.prims = sc->prims;
+    g.has_env = sc->has_env;
+    for (int k = 0; k < 3; k++) g.env_Le[k] = sc->env_Le[k];
     return g;
 }
 
@@ -93,7 +95,7 @@ int lmgpu_scene_create(const float* tris, const int32_t* tri_prim, uint64_t ntri
         }
     }
     for (uint32_t i = 0; i < nprims; i++) {
-        if (prims[i].bsdf != LMGPU_BSDF_NULL && prims[i].bsdf != LMGPU_BSDF_DIFFUSE) {
+        if (prims[i].bsdf < LMGPU_BSDF_NULL || prims[i].bsdf > LMGPU_BSDF_COOK_TORRANCE) {
             set_error("lmgpu_scene_create: unsupported bsdf kind " + std::to_string(prims[i].bsdf));
             return LMGPU_ERR_INVALID;
         }
@@ -135,7 +137,33 @@ int lmgpu_scene_create(const float* tris, const int32_t* tri_prim, uint64_t ntri
     c.aspect = (float)cam->width / (float)cam->height;
     c.width = cam->width;
     c.height = cam->height;
+    // bounding sphere of the mesh vertices and the sensor position
+    // (scene3.cpp:52-78, sensor_pinhole.cpp:158-161), radius grown by 1%
+    float lo[3] = {eye.x, eye.y, eye.z}, hi[3] = {eye.x, eye.y, eye.z};
+    for (uint64_t i = 0; i < 3 * ntri; i++)
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::fmin(lo[k], tris[3 * i + k]);
+            hi[k] = std::fmax(hi[k], tris[3 * i + k]);
+        }
+    float r2 = 0.0f;
+    for (int k = 0; k < 3; k++) {
+        sc->sphere_center[k] = (hi[k] + lo[k]) * 0.5f;
+        r2 += (sc->sphere_center[k] - hi[k]) * (sc->sphere_center[k] - hi[k]);
+    }
+    sc->sphere_radius = std::sqrt(r2) * 1.01f;
     *out = sc;
+    return LMGPU_OK;
+}
+
+int lmgpu_scene_set_environment(lmgpu_scene* sc, const float* Le)
+{
+    clear_error();
+    if (!sc) {
+        set_error("lmgpu_scene_set_environment: NULL scene");
+        return LMGPU_ERR_INVALID;
+    }
+    sc->has_env = Le ? 1 : 0;
+    for (int k = 0; k < 3; k++) sc->env_Le[k] = Le ? Le[k] : 0.0f;
     return LMGPU_OK;
 }
 

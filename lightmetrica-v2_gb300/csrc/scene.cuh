@@ -17,6 +17,9 @@ struct PrimGPU {
     int32_t is_light;
     float R[3];
     float Le[3];
+    float eta1, eta2;
+    float ct_eta[3], ct_k[3];
+    float roughness;
 };
 
 // Pinhole camera: lookat basis (scene3.cpp:213-221) and projection
@@ -39,6 +42,8 @@ struct SceneGPU {
     const float* tris;
     const int32_t* tri_prim;
     const PrimGPU* prims;
+    int32_t has_env;
+    float env_Le[3];
 };
 
 }  // namespace lmgpu
@@ -51,6 +56,10 @@ struct lmgpu_scene {
     lmgpu::PrimGPU* prims = nullptr;
     uint32_t nprims = 0;
     lmgpu::CameraGPU cam{};
+    int32_t has_env = 0;
+    float env_Le[3] = {0.0f, 0.0f, 0.0f};
+    float sphere_center[3] = {0.0f, 0.0f, 0.0f};  // bounding sphere (scene3.cpp:74-78)
+    float sphere_radius = 0.0f;
 
     // film: per-pixel sums of splats (FP32) and of their squares (FP64)
     float* film = nullptr;

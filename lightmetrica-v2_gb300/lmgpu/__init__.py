@@ -87,13 +87,14 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_scene_create.argtypes = [vp, vp, u64, vp, ctypes.c_uint32, vp, ctypes.POINTER(vp)]
     L.lmgpu_scene_destroy.argtypes = [vp]
     L.lmgpu_scene_destroy.restype = None
+    L.lmgpu_scene_set_environment.argtypes = [vp, vp]
     L.lmgpu_scene_accel.argtypes = [vp, ctypes.POINTER(vp)]
     L.lmgpu_render_pt.argtypes = [vp, vp, vp, vp]
     L.lmgpu_render_pt_device.argtypes = [vp, vp, vp, vp, vp]
     for name in ("lmgpu_accel_create", "lmgpu_accel_build", "lmgpu_accel_build_device", "lmgpu_accel_get_info",
                  "lmgpu_trace", "lmgpu_trace_device", "lmgpu_trace_stats_device", "lmgpu_accel_check",
                  "lmgpu_trace_static_scene", "lmgpu_accel_set_tuning", "lmgpu_scene_create", "lmgpu_scene_accel",
-                 "lmgpu_render_pt", "lmgpu_render_pt_device"):
+                 "lmgpu_render_pt", "lmgpu_render_pt_device", "lmgpu_scene_set_environment"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -182,7 +183,8 @@ def trace_static_scene(d_tris_ptr: int, ntri: int, d_rays_ptr: int, d_hits_ptr: 
 
 class Prim(ctypes.Structure):
     _fields_ = [("bsdf", ctypes.c_int32), ("is_light", ctypes.c_int32), ("R", ctypes.c_float * 3),
-                ("Le", ctypes.c_float * 3)]
+                ("Le", ctypes.c_float * 3), ("eta1", ctypes.c_float), ("eta2", ctypes.c_float),
+                ("ct_eta", ctypes.c_float * 3), ("ct_k", ctypes.c_float * 3), ("roughness", ctypes.c_float)]
 
 
 class Camera(ctypes.Structure):
@@ -194,7 +196,7 @@ class PtParams(ctypes.Structure):
     _fields_ = [("spp", ctypes.c_uint64), ("max_num_vertices", ctypes.c_int32), ("seed", ctypes.c_uint32)]
 
 
-BSDF_NULL, BSDF_DIFFUSE = 0, 1
+BSDF_NULL, BSDF_DIFFUSE, BSDF_DIELECTRIC, BSDF_COOK_TORRANCE = 0, 1, 2, 3
 
 
 class Scene:
@@ -204,18 +206,22 @@ class Scene:
     1 = area light without a BSDF; camera)."""
 
     def __init__(self, scene: dict) -> None:
-        from .scenes import scene_triangles
+        from .scenes import prim_params, scene_triangles
 
         tris, tri_prim = scene_triangles(scene)
         self.tris = np.ascontiguousarray(tris, dtype=np.float32)
         self.tri_prim = np.ascontiguousarray(tri_prim, dtype=np.int32)
         prims = (Prim * len(scene["prims"]))()
-        for i, p in enumerate(scene["prims"]):
-            prims[i].bsdf = BSDF_DIFFUSE if p["kind"] == 0 else BSDF_NULL
-            prims[i].is_light = 1 if p["kind"] == 1 else 0
+        for i, p0 in enumerate(scene["prims"]):
+            p = prim_params(p0)
+            prims[i].bsdf = p["bsdf"]
+            prims[i].is_light = 1 if p["light"] else 0
             for k in range(3):
                 prims[i].R[k] = p["R"][k]
                 prims[i].Le[k] = p["Le"][k]
+                prims[i].ct_eta[k] = p["ct_eta"][k]
+                prims[i].ct_k[k] = p["ct_k"][k]
+            prims[i].eta1, prims[i].eta2, prims[i].roughness = p["eta1"], p["eta2"], p["roughness"]
         c = scene["camera"]
         cam = Camera()
         for k in range(3):
@@ -227,6 +233,9 @@ class Scene:
                                         ctypes.addressof(prims), len(scene["prims"]), ctypes.addressof(cam),
                                         ctypes.byref(h)))
         self._h = h
+        if scene.get("env") is not None:
+            le = (ctypes.c_float * 3)(*scene["env"])
+            _check(lib().lmgpu_scene_set_environment(self._h, le))
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -187,3 +187,46 @@ def scene_triangles(scene: dict) -> tuple[np.ndarray, np.ndarray]:
     tris = np.concatenate([p["tris"] for p in scene["prims"]], axis=0).astype(np.float32)
     prim = np.concatenate([np.full(p["tris"].shape[0], i, np.int32) for i, p in enumerate(scene["prims"])])
     return tris, prim
+
+
+# BSDF kinds of a primitive (the reference's bsdf::null, bsdf::diffuse,
+# bsdf::flesnel, bsdf::cook_torrance) and their parameter defaults
+# (bsdf_flesnel.cpp:47-50, bsdf_cooktorrance.cpp:58-63).
+BSDF_NULL, BSDF_DIFFUSE, BSDF_DIELECTRIC, BSDF_COOK_TORRANCE = 0, 1, 2, 3
+PRIM_DEFAULTS = {"bsdf": BSDF_NULL, "light": False, "R": (0.0, 0.0, 0.0), "Le": (0.0, 0.0, 0.0), "eta1": 1.0,
+                 "eta2": 2.0, "ct_eta": (0.14, 0.129, 0.1585), "ct_k": (4.58625, 3.348125, 2.329375),
+                 "roughness": 0.1}
+
+
+def prim_params(p: dict) -> dict:
+    """Full parameter set of a primitive; the short form {"kind": 0|1} means
+    a diffuse surface (0) or an area light without a BSDF (1)."""
+    q = dict(PRIM_DEFAULTS)
+    if "kind" in p and "bsdf" not in p:
+        q["bsdf"] = BSDF_DIFFUSE if p["kind"] == DIFFUSE else BSDF_NULL
+        q["light"] = p["kind"] == AREA_LIGHT
+    for k, v in p.items():
+        if k in q:
+            q[k] = v
+    q["tris"] = p["tris"]
+    return q
+
+
+def cornell_materials(width: int = 64, height: int = 64) -> dict:
+    """The Cornell-style box with the short box in glass (bsdf::flesnel,
+    eta 1 -> 1.5), the tall box a GGX conductor (bsdf::cook_torrance,
+    roughness 0.2, the reference's default eta/k), and a constant blue-white
+    environment light reached through the open front."""
+    s = cornell_box(width, height)
+    # the boxes stand 1e-3 above the floor: a glass box whose bottom face is
+    # coplanar with the floor makes every ray reaching y = 0 an exact tie
+    # between two surfaces, an ill-posed case whose outcome depends on the
+    # accel's traversal order
+    lift = np.array([0.0, 1e-3, 0.0] * 3, np.float32)
+    short_box, tall_box = s["prims"][5], s["prims"][6]
+    s["prims"][5] = {"bsdf": BSDF_DIELECTRIC, "light": False, "R": (1.0, 1.0, 1.0), "eta1": 1.0, "eta2": 1.5,
+                     "tris": short_box["tris"] + lift}
+    s["prims"][6] = {"bsdf": BSDF_COOK_TORRANCE, "light": False, "R": (0.9, 0.9, 0.9), "roughness": 0.2,
+                     "tris": tall_box["tris"] + lift}
+    s["env"] = (0.2, 0.3, 0.5)
+    return s

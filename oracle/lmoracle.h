@@ -68,14 +68,25 @@ double     lmo_plane_t_fp64(const float* tri, const float* ray, double* b1, doub
 
 #define LMO_BSDF_NULL 0
 #define LMO_BSDF_DIFFUSE 1
+#define LMO_BSDF_DIELECTRIC 2     /* bsdf::flesnel */
+#define LMO_BSDF_COOK_TORRANCE 3  /* bsdf::cook_torrance (GGX) */
 
 /* One scene primitive: its BSDF and, when is_light, an area light on it. */
 typedef struct {
-    int32_t bsdf;      /* LMO_BSDF_NULL or LMO_BSDF_DIFFUSE */
+    int32_t bsdf;
     int32_t is_light;
     float R[3];
     float Le[3];
+    float eta1, eta2;          /* flesnel: outside / inside index */
+    float ct_eta[3], ct_k[3];  /* cook_torrance: conductor eta, k */
+    float roughness;           /* cook_torrance: GGX alpha */
 } lmo_pt_prim;
+
+/* Constant environment light (light::env without an envmap). */
+typedef struct {
+    int32_t enabled;
+    float Le[3];
+} lmo_pt_env;
 
 /* Pinhole camera from a lookat node; fov is vertical, in degrees. */
 typedef struct {
@@ -87,8 +98,8 @@ typedef struct {
 /* Renders num_samples paths with `threads` threads; fills per-pixel sums of
  * splatted values and of their squares (H*W*3 doubles each, row = raster y). */
 uint64_t lmo_render_pt(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
-                       const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices, uint64_t seed,
-                       int threads, double* sum, double* sumsq);
+                       const lmo_pt_env* env, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
+                       uint64_t seed, int threads, double* sum, double* sumsq);
 
 #ifdef __cplusplus
 }

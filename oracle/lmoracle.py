@@ -49,7 +49,7 @@ def lib() -> ctypes.CDLL:
         L.lmo_accel_stats.restype = None
         L.lmo_plane_t_fp64.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         L.lmo_plane_t_fp64.restype = ctypes.c_double
-        L.lmo_render_pt.argtypes = [vp, vp, sz, vp, vp, ctypes.c_uint64, ctypes.c_int, ctypes.c_uint64,
+        L.lmo_render_pt.argtypes = [vp, vp, sz, vp, vp, vp, ctypes.c_uint64, ctypes.c_int, ctypes.c_uint64,
                                     ctypes.c_int, vp, vp]
         L.lmo_render_pt.restype = ctypes.c_uint64
         _lib = L
@@ -135,21 +135,35 @@ REF_RENDER = os.path.join(HERE, "_ref", "ref_render")
 REF_RENDER64 = os.path.join(HERE, "_ref", "ref_render64")
 
 
+def _prim_full(p: dict) -> dict:
+    import sys as _s
+
+    _s.path.insert(0, os.path.join(os.path.dirname(HERE), "lightmetrica-v2_gb300"))
+    from lmgpu.scenes import prim_params
+
+    return prim_params(p)
+
+
 def write_render_scene(path: str, scene: dict, num_samples: int, max_num_vertices: int, seed: int,
                        threads: int) -> None:
-    """Writes the input file of oracle/_ref/ref_render (refharness/ref_render_cli.cpp)."""
+    """Writes the input file of oracle/_ref/ref_render (refharness/ref_render_cli.cpp), version 2."""
     cam = scene["camera"]
     with open(path, "wb") as f:
-        f.write(np.array([0x53524D4C, 1, cam["width"], cam["height"]], dtype=np.uint32).tobytes())
+        f.write(np.array([0x53524D4C, 2, cam["width"], cam["height"]], dtype=np.uint32).tobytes())
         f.write(np.array(list(cam["eye"]) + list(cam["center"]) + list(cam["up"]) + [cam["fov"]],
                          dtype=np.float32).tobytes())
         f.write(np.uint32(len(scene["prims"])).tobytes())
-        for p in scene["prims"]:
-            f.write(np.int32(p["kind"]).tobytes())
-            f.write(np.array(list(p["R"]) + list(p["Le"]), dtype=np.float32).tobytes())
+        for p0 in scene["prims"]:
+            p = _prim_full(p0)
+            f.write(np.array([p["bsdf"], 1 if p["light"] else 0], dtype=np.int32).tobytes())
+            f.write(np.array(list(p["R"]) + list(p["Le"]) + [p["eta1"], p["eta2"]] + list(p["ct_eta"]) +
+                             list(p["ct_k"]) + [p["roughness"]], dtype=np.float32).tobytes())
             t = np.ascontiguousarray(p["tris"], dtype=np.float32).reshape(-1, 9)
             f.write(np.uint32(t.shape[0]).tobytes())
             f.write(t.tobytes())
+        env = scene.get("env")
+        f.write(np.int32(1 if env is not None else 0).tobytes())
+        f.write(np.array(env if env is not None else (0.0, 0.0, 0.0), dtype=np.float32).tobytes())
         f.write(np.uint64(num_samples).tobytes())
         f.write(np.int32(max_num_vertices).tobytes())
         f.write(np.uint32(seed).tobytes())
@@ -192,7 +206,12 @@ def pixel_variance(image: np.ndarray, sumsq: np.ndarray, num_samples: int, num_p
 
 class PtPrim(ctypes.Structure):
     _fields_ = [("bsdf", ctypes.c_int32), ("is_light", ctypes.c_int32), ("R", ctypes.c_float * 3),
-                ("Le", ctypes.c_float * 3)]
+                ("Le", ctypes.c_float * 3), ("eta1", ctypes.c_float), ("eta2", ctypes.c_float),
+                ("ct_eta", ctypes.c_float * 3), ("ct_k", ctypes.c_float * 3), ("roughness", ctypes.c_float)]
+
+
+class PtEnv(ctypes.Structure):
+    _fields_ = [("enabled", ctypes.c_int32), ("Le", ctypes.c_float * 3)]
 
 
 class PtCamera(ctypes.Structure):
@@ -203,12 +222,16 @@ class PtCamera(ctypes.Structure):
 def scene_prims(scene: dict) -> "ctypes.Array":
     """Scene primitives in the oracle's layout (kind 0 = diffuse, 1 = light without BSDF)."""
     arr = (PtPrim * len(scene["prims"]))()
-    for i, p in enumerate(scene["prims"]):
-        arr[i].bsdf = 1 if p["kind"] == 0 else 0
-        arr[i].is_light = 1 if p["kind"] == 1 else 0
+    for i, p0 in enumerate(scene["prims"]):
+        p = _prim_full(p0)
+        arr[i].bsdf = p["bsdf"]
+        arr[i].is_light = 1 if p["light"] else 0
         for k in range(3):
             arr[i].R[k] = p["R"][k]
             arr[i].Le[k] = p["Le"][k]
+            arr[i].ct_eta[k] = p["ct_eta"][k]
+            arr[i].ct_k[k] = p["ct_k"][k]
+        arr[i].eta1, arr[i].eta2, arr[i].roughness = p["eta1"], p["eta2"], p["roughness"]
     return arr
 
 
@@ -230,8 +253,13 @@ def render_pt(scene: dict, num_samples: int, max_num_vertices: int, seed: int, t
     q = np.zeros((H, W, 3), np.float64)
     prims = scene_prims(scene)
     cam = scene_camera(scene)
+    env = PtEnv()
+    if scene.get("env") is not None:
+        env.enabled = 1
+        for k in range(3):
+            env.Le[k] = scene["env"][k]
     lib().lmo_render_pt(tris.ctypes.data, tri_prim.ctypes.data, tris.shape[0], ctypes.addressof(prims),
-                        ctypes.addressof(cam), num_samples, max_num_vertices, seed, threads, s.ctypes.data,
-                        q.ctypes.data)
+                        ctypes.addressof(env), ctypes.addressof(cam), num_samples, max_num_vertices, seed, threads,
+                        s.ctypes.data, q.ctypes.data)
     img = s * (W * H / num_samples)
     return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}

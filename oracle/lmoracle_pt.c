@@ -7,7 +7,11 @@
  *   lookat camera basis              src/liblightmetrica/scene3.cpp:213-221
  *   BSDF_Diffuse sample/evaluate     src/liblightmetrica/asset/bsdf/bsdf_diffuse.cpp:69-104
  *   concentric-disk cosine sampling  include/lightmetrica/sampler.h:44-67
+ *   BSDF_Flesnel sample/evaluate     src/liblightmetrica/asset/bsdf/bsdf_flesnel.cpp:59-164, 225-241
+ *   BSDF_CookTorrance (GGX)          src/liblightmetrica/asset/bsdf/bsdf_cooktorrance.cpp:73-292
  *   Light_Area emission (front face) src/liblightmetrica/asset/light/light_area.cpp:108-113
+ *   Light_EnvLight (constant Le) on the scene's bounding sphere, hit when
+ *   the accel misses            light_env.cpp:42-230, scene3.cpp:52-78, 464-475
  *   hit frame (gn, OrthonormalBasis) include/lightmetrica/intersectionutils.h:78-131, math.h:2355-2359
  *   Film_HDR::Splat pixel index      src/liblightmetrica/asset/film/film_hdr.cpp:218-223
  * Intersections use the oracle's accel::bvh_sahbin (lmoracle_accel.c) with
@@ -52,6 +56,7 @@ typedef struct {
     const float* tris;
     const int32_t* tri_prim;
     const lmo_pt_prim* prims;
+    lmo_pt_env env;
     lmo_pt_camera cam;
     v3 vx, vy, vz, eye;
     float tan_fov, aspect;
@@ -97,6 +102,52 @@ static void basis(v3 a, v3* b, v3* c)
     *b = cross(*c, a);
 }
 
+/* BSDF_Flesnel::EvaluateFresnelTerm (bsdf_flesnel.cpp:243-257) */
+static float fresnel_dielectric(float wiDotN, float etaI, float etaT)
+{
+    const float eta = etaI / etaT;
+    const float cosThetaTSq = 1.0f - eta * eta * (1.0f - wiDotN * wiDotN);
+    if (cosThetaTSq <= 0.0f) return 1.0f;
+    const float ci = fabsf(wiDotN), ct = sqrtf(cosThetaTSq);
+    const float rs = (etaI * ci - etaT * ct) / (etaI * ci + etaT * ct);
+    const float rt = (etaI * ct - etaT * ci) / (etaI * ct + etaT * ci);
+    return (rs * rs + rt * rt) * 0.5f;
+}
+
+/* BSDF_CookTorrance::EvaluateGGX (bsdf_cooktorrance.cpp:187-198) */
+static float ggx_d(v3 H, float a)
+{
+    const float c = H.z;
+    if (c <= 0.0f) return 0.0f;
+    const float t = 1.0f - c * c;
+    const float tanH = t <= 0.0f ? 0.0f : sqrtf(t) / c;
+    const float q = a * a + tanH * tanH;
+    return (a * a) / (PI_F * c * c * c * c * q * q);
+}
+
+/* BSDF_CookTorrance::SampleGGX (bsdf_cooktorrance.cpp:200-225), Eps = 1e-4 */
+static v3 ggx_sample(float ua, float ub, float a)
+{
+    const float eps = 1e-4f;
+    const float u0 = (1.0f - eps) * ua + eps;
+    const float u1 = (1.0f - 2.0f * eps) * ub + eps;
+    const float den = sqrtf(1.0f - (1.0f - a * a) * u0);
+    const float cosT = sqrtf(1.0f - u0) / den;
+    const float sinT = a * (sqrtf(u0) / den);
+    const float phi = PI_F * (2.0f * u1 - 1.0f);
+    return V(sinT * cosf(phi), sinT * sinf(phi), cosT);
+}
+
+/* BSDF_CookTorrance::EvaluateFrConductor (bsdf_cooktorrance.cpp:283-291), one channel */
+static float fresnel_conductor(float c, float eta, float k)
+{
+    const float tmp = (eta * eta + k * k) * (c * c);
+    const float rParl2 = (tmp - (eta * (2.0f * c)) + 1.0f) / (tmp + (eta * (2.0f * c)) + 1.0f);
+    const float tmpF = eta * eta + k * k;
+    const float rPerp2 = (tmpF - (eta * (2.0f * c)) + c * c) / (tmpF + (eta * (2.0f * c)) + c * c);
+    return (rParl2 + rPerp2) * 0.5f;
+}
+
 static void* pt_worker_fn(void* arg)
 {
     pt_worker* w = (pt_worker*)arg;
@@ -135,7 +186,18 @@ static void* pt_worker_fn(void* arg)
             float ray[8] = {o.x, o.y, o.z, 1e-4f, d.x, d.y, d.z, FLT_MAX};
             lmo_hit h;
             lmo_accel_trace(J->accel, ray, 1, &h, 1);
-            if (h.id < 0) break;
+            if (h.id < 0) {
+                /* the environment's bounding sphere contains every vertex and
+                 * the sensor, so a ray leaving the geometry always meets it */
+                if (J->env.enabled) {
+                    const float c[3] = {thr.x * J->env.Le[0], thr.y * J->env.Le[1], thr.z * J->env.Le[2]};
+                    for (int k = 0; k < 3; k++) {
+                        sum[3 * pix + k] += c[k];
+                        sumsq[3 * pix + k] += (double)c[k] * (double)c[k];
+                    }
+                }
+                break;
+            }
             const float* T = J->tris + 9 * (size_t)h.id;
             const v3 p1 = V(T[0], T[1], T[2]), p2 = V(T[3], T[4], T[5]), p3 = V(T[6], T[7], T[8]);
             const v3 gn = normalize(cross(sub(p2, p1), sub(p3, p1)));
@@ -156,18 +218,62 @@ static void* pt_worker_fn(void* arg)
             thr = mul(thr, 2.0f);
             nv++;
             if (J->max_num_vertices != -1 && nv >= J->max_num_vertices) break;
-            if (P->bsdf != LMO_BSDF_DIFFUSE) break; /* bsdf::null: black, path ends */
-            /* bsdf::diffuse (bsdf_diffuse.cpp:69-104), sn = gn (no vertex normals) */
+            if (P->bsdf == LMO_BSDF_NULL) break; /* bsdf::null: black, path ends */
+            /* shading frame: sn = gn (no vertex normals), OrthonormalBasis */
             const v3 wi = mul(d, -1.0f);
-            if (dot(wi, gn) <= 0.0f) break;
             v3 bx, by;
             basis(gn, &bx, &by);
-            const float a0 = rnd(&rng), a1 = rnd(&rng);
-            const v3 lw = cosine_hemisphere(a0, a1);
-            if (lw.z <= 0.0f) break;
-            const v3 wo = add(add(mul(bx, lw.x), mul(by, lw.y)), mul(gn, lw.z));
-            if (dot(wo, gn) <= 0.0f) break;
-            thr = V(thr.x * P->R[0], thr.y * P->R[1], thr.z * P->R[2]);
+            const v3 lwi = V(dot(wi, bx), dot(wi, by), dot(wi, gn));
+            const float a0 = rnd(&rng), a1 = rnd(&rng), a2 = rnd(&rng);
+            v3 lwo;
+            float f[3];
+            if (P->bsdf == LMO_BSDF_DIFFUSE) {
+                /* bsdf_diffuse.cpp:69-104: fs / pdf = R */
+                if (lwi.z <= 0.0f) break;
+                lwo = cosine_hemisphere(a0, a1);
+                if (lwo.z <= 0.0f) break;
+                for (int k = 0; k < 3; k++) f[k] = P->R[k];
+            } else if (P->bsdf == LMO_BSDF_DIELECTRIC) {
+                /* bsdf_flesnel.cpp:59-164: reflect w.p. Fr, else refract;
+                 * fs / pdf = R, or R * (etaI / etaT)^2 for refraction (EL) */
+                float etaI = P->eta1, etaT = P->eta2;
+                if (lwi.z < 0.0f) { const float t = etaI; etaI = etaT; etaT = t; }
+                const float Fr = fresnel_dielectric(lwi.z, etaI, etaT);
+                float scale = 1.0f;
+                if (a2 <= Fr) {
+                    lwo = V(-lwi.x, -lwi.y, lwi.z);
+                } else {
+                    const float eta = etaI / etaT;
+                    const float cosTSq = 1.0f - eta * eta * (1.0f - lwi.z * lwi.z);
+                    const float cosT = sqrtf(cosTSq > 0.0f ? cosTSq : 0.0f) * (lwi.z > 0.0f ? -1.0f : 1.0f);
+                    lwo = V(-eta * lwi.x, -eta * lwi.y, cosT);
+                    scale = eta * eta;
+                }
+                for (int k = 0; k < 3; k++) f[k] = P->R[k] * scale;
+            } else {
+                /* bsdf_cooktorrance.cpp:73-120 (GGX):
+                 * fs / pdf = R D G F / (4 cos_i cos_o) / (D cos_H / (4 (wo.H)) / cos_o) */
+                if (lwi.z <= 0.0f) break;
+                const v3 H = ggx_sample(a0, a1, P->roughness);
+                const float dih = dot(mul(lwi, -1.0f), H);
+                lwo = sub(mul(lwi, -1.0f), mul(H, 2.0f * dih));
+                if (lwo.z <= 0.0f) break;
+                const v3 Hn = normalize(add(lwi, lwo));
+                const float D = ggx_d(Hn, P->roughness);
+                const float woH = fabsf(dot(lwo, Hn));
+                const float G1 = 2.0f * Hn.z * lwo.z / woH, G2 = 2.0f * Hn.z * lwi.z / woH;
+                const float G = fminf(1.0f, fminf(G1, G2));
+                const float pdf = D * Hn.z / (4.0f * dot(lwo, Hn)) / lwo.z;
+                if (!(pdf > 0.0f)) break;
+                for (int k = 0; k < 3; k++) {
+                    const float F = fresnel_conductor(dot(lwi, Hn), P->ct_eta[k], P->ct_k[k]);
+                    const float fs = P->R[k] * D * G * F / (4.0f * lwi.z) / lwo.z;
+                    f[k] = fs / pdf;
+                }
+            }
+            if (f[0] == 0.0f && f[1] == 0.0f && f[2] == 0.0f) break;
+            const v3 wo = add(add(mul(bx, lwo.x), mul(by, lwo.y)), mul(gn, lwo.z));
+            thr = V(thr.x * f[0], thr.y * f[1], thr.z * f[2]);
             o = p;
             d = wo;
         }
@@ -181,11 +287,12 @@ static void* pt_worker_fn(void* arg)
 }
 
 uint64_t lmo_render_pt(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
-                       const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices, uint64_t seed,
-                       int threads, double* sum, double* sumsq)
+                       const lmo_pt_env* env, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
+                       uint64_t seed, int threads, double* sum, double* sumsq)
 {
     pt_job J;
     memset(&J, 0, sizeof(J));
+    if (env) J.env = *env;
     J.accel = lmo_accel_build(1, tris, ntri);
     J.tris = tris;
     J.tri_prim = tri_prim;

@@ -18,14 +18,24 @@
 //                     own film, then films are accumulated and rescaled by
 //                     W*H / processed samples
 //   HarnessScene      Scene3 queries (scene3.cpp:458-539): Intersect with
-//                     [EpsIsect, Inf], uniform light-primitive selection, the
-//                     sensor, lookat camera basis (scene3.cpp:213-221)
+//                     [EpsIsect, Inf] then the emitter shapes (environment),
+//                     uniform light-primitive selection, the sensor, lookat
+//                     camera basis (scene3.cpp:213-221), scene bound and
+//                     bounding sphere (scene3.cpp:52-78).  One deliberate
+//                     difference: EmitterShape_EnvLight::Intersect leaves
+//                     isect.primitive unset (light_env.cpp:52-75), which makes
+//                     renderer::pt dereference a null primitive on an
+//                     environment hit; the harness sets it to the environment
+//                     light's primitive, as a fixed scene would.
 //
 // Usage: ref_render <scene.bin> <out.bin>
-//   scene.bin: u32 magic 'LMRS', u32 version 1, u32 W, H,
+//   scene.bin: u32 magic 'LMRS', u32 version 2, u32 W, H,
 //              f32 eye[3], center[3], up[3], fov_deg,
-//              u32 nprims, per primitive: i32 kind (0 diffuse, 1 area light
-//              with no BSDF), f32 R[3], f32 Le[3], u32 nfaces, f32 pos[nfaces*9],
+//              u32 nprims, per primitive: i32 bsdf (0 null, 1 diffuse,
+//              2 flesnel, 3 cook_torrance), i32 is_light, f32 R[3], Le[3],
+//              eta1, eta2, ct_eta[3], ct_k[3], roughness, u32 nfaces,
+//              f32 pos[nfaces*9],
+//              i32 has_env, f32 env_Le[3],
 //              u64 num_samples, i32 max_num_vertices, u32 seed, u32 threads
 //   out.bin:   f32 image[W*H*3] (the reference film after Rescale),
 //              f64 sumsq[W*H*3] (sum of squared splats per pixel),
@@ -48,6 +58,7 @@
 #include <lightmetrica/sensor.h>
 #include <lightmetrica/spectrum.h>
 #include <lightmetrica/ray.h>
+#include <lightmetrica/emitter.h>
 
 #include <cstdint>
 #include <map>
@@ -198,7 +209,21 @@ public:
     LM_IMPL_F(GetAccel) = [this]() -> const Accel* { return accel; };
     LM_IMPL_F(Intersect) = [this](const Ray& ray, Intersection& isect) -> bool
     {
-        return accel->Intersect(this, ray, isect, Math::EpsIsect(), Math::Inf());
+        bool hit = accel->Intersect(this, ray, isect, Math::EpsIsect(), Math::Inf());
+        if (!hit)
+        {
+            Float maxT = Math::Inf();
+            for (size_t i = 0; i < emitterShapes.size(); i++)
+            {
+                if (emitterShapes[i]->Intersect(ray, Math::EpsIsect(), maxT, isect))
+                {
+                    maxT = Math::Length(isect.geom.p - ray.o);
+                    isect.primitive = emitterShapePrims[i];
+                    hit = true;
+                }
+            }
+        }
+        return hit;
     };
     LM_IMPL_F(IntersectWithRange) = [this](const Ray& ray, Intersection& isect, Float minT, Float maxT) -> bool
     {
@@ -237,6 +262,8 @@ public:
     const Accel3* accel = nullptr;
     Bound bound;
     SphereBound sphereBound;
+    std::vector<const EmitterShape*> emitterShapes;
+    std::vector<const Primitive*> emitterShapePrims;
 };
 
 LM_COMPONENT_REGISTER_IMPL(HarnessScheduler, "Scheduler_");
@@ -268,7 +295,7 @@ int main(int argc, char** argv)
         std::fclose(f);
     }
     const char* p = buf.data();
-    if (Rd<uint32_t>(p) != 0x53524D4Cu || Rd<uint32_t>(p) != 1u) { std::fprintf(stderr, "bad scene file\n"); return 2; }
+    if (Rd<uint32_t>(p) != 0x53524D4Cu || Rd<uint32_t>(p) != 2u) { std::fprintf(stderr, "bad scene file\n"); return 2; }
     const int W = (int)Rd<uint32_t>(p), H = (int)Rd<uint32_t>(p);
     float eye[3], center[3], up[3];
     for (auto* v : { eye, center, up }) for (int k = 0; k < 3; k++) v[k] = Rd<float>(p);
@@ -287,10 +314,15 @@ int main(int argc, char** argv)
 
     for (uint32_t i = 0; i < nprims; i++)
     {
-        const int kind = Rd<int32_t>(p);
-        float R[3], Le[3];
+        const int bsdfKind = Rd<int32_t>(p);
+        const int isLight = Rd<int32_t>(p);
+        float R[3], Le[3], ctEta[3], ctK[3];
         for (int k = 0; k < 3; k++) R[k] = Rd<float>(p);
         for (int k = 0; k < 3; k++) Le[k] = Rd<float>(p);
+        const float eta1 = Rd<float>(p), eta2 = Rd<float>(p);
+        for (int k = 0; k < 3; k++) ctEta[k] = Rd<float>(p);
+        for (int k = 0; k < 3; k++) ctK[k] = Rd<float>(p);
+        const float roughness = Rd<float>(p);
         const uint32_t nf = Rd<uint32_t>(p);
         std::unique_ptr<HarnessMesh> m(new HarnessMesh);
         m->ps.resize((size_t)nf * 9);
@@ -302,18 +334,34 @@ int main(int argc, char** argv)
         prim->transform = Mat4::Identity();
         prim->normalTransform = Mat3::Identity();
         prim->mesh = m.get();
-        if (kind == 0)
+        char fb[64];
+        if (bsdfKind == 0)
         {
-            auto b = ComponentFactory::Create<BSDF>("bsdf::diffuse");
+            prim->bsdf = nullBSDF.get();
+        }
+        else
+        {
+            static const char* keys[] = { "", "bsdf::diffuse", "bsdf::flesnel", "bsdf::cook_torrance" };
+            if (bsdfKind < 1 || bsdfKind > 3) return 3;
+            auto b = ComponentFactory::Create<BSDF>(keys[bsdfKind]);
             props.emplace_back(new HarnessProp);
             props.back()->Set("R", Vec3Str(R));
+            if (bsdfKind == 2)
+            {
+                std::snprintf(fb, sizeof(fb), "%.9g", eta1); props.back()->Set("eta1", fb);
+                std::snprintf(fb, sizeof(fb), "%.9g", eta2); props.back()->Set("eta2", fb);
+            }
+            if (bsdfKind == 3)
+            {
+                props.back()->Set("eta", Vec3Str(ctEta)).Set("k", Vec3Str(ctK));
+                std::snprintf(fb, sizeof(fb), "%.9g", roughness); props.back()->Set("roughness", fb);
+            }
             if (!b->Load(props.back().get(), &assets, prim.get())) return 3;
             prim->bsdf = b.get();
             keep.emplace_back(b.release(), b.get_deleter());
         }
-        else
+        if (isLight)
         {
-            prim->bsdf = nullBSDF.get();
             auto l = ComponentFactory::Create<Light>("light::area");
             props.emplace_back(new HarnessProp);
             props.back()->Set("Le", Vec3Str(Le));
@@ -327,6 +375,9 @@ int main(int argc, char** argv)
         meshes.push_back(std::move(m));
         scene.prims.push_back(std::move(prim));
     }
+    const int hasEnv = Rd<int32_t>(p);
+    float envLe[3];
+    for (int k = 0; k < 3; k++) envLe[k] = Rd<float>(p);
     const uint64_t numSamples = Rd<uint64_t>(p);
     const int maxNumVertices = Rd<int32_t>(p);
     const uint32_t seed = Rd<uint32_t>(p);
@@ -357,11 +408,48 @@ int main(int argc, char** argv)
         scene.prims.push_back(std::move(prim));
     }
 
+    // scene bound and bounding sphere (scene3.cpp:52-78): mesh vertices and
+    // the sensor position
+    for (const auto& prim : scene.prims)
+    {
+        if (prim->mesh)
+        {
+            const auto* ps = prim->mesh->Positions();
+            for (int i = 0; i < prim->mesh->NumVertices(); i++)
+                scene.bound = Math::Union(scene.bound, Vec3(prim->transform * Vec4(ps[3 * i], ps[3 * i + 1], ps[3 * i + 2], 1_f)));
+        }
+        if (prim->emitter && prim->emitter->GetBound.Implemented()) scene.bound = Math::Union(scene.bound, prim->emitter->GetBound());
+    }
+    scene.sphereBound.center = (scene.bound.max + scene.bound.min) * .5_f;
+    scene.sphereBound.radius = Math::Length(scene.sphereBound.center - scene.bound.max) * 1.01_f;
+    if (hasEnv)
+    {
+        std::unique_ptr<Primitive> prim(new Primitive);
+        prim->index = (int)scene.prims.size();
+        prim->transform = Mat4::Identity();
+        prim->normalTransform = Mat3::Identity();
+        prim->bsdf = nullBSDF.get();
+        auto l = ComponentFactory::Create<Light>("light::env");
+        props.emplace_back(new HarnessProp);
+        props.back()->Set("Le", Vec3Str(envLe));
+        if (!l->Load(props.back().get(), &assets, prim.get())) return 3;
+        if (!l->PostLoad(&scene)) return 3;
+        prim->light = l.get();
+        prim->emitter = l.get();
+        prim->lightIndex = scene.lightIndices.size();
+        scene.lightIndices.push_back((int)scene.prims.size());
+        scene.emitterShapes.push_back(l->GetEmitterShape());
+        scene.emitterShapePrims.push_back(prim.get());
+        keep.emplace_back(l.release(), l.get_deleter());
+        scene.prims.push_back(std::move(prim));
+    }
+
 #if LM_SINGLE_PRECISION && LM_SSE
     const char* accelKey = "accel::qbvh";
 #else
     const char* accelKey = "accel::bvh_sahbin";
 #endif
+    if (const char* k = std::getenv("LM_REF_ACCEL")) accelKey = k;  // e.g. accel::bvh_sahbin
     auto accel = ComponentFactory::Create<Accel3>(accelKey);
     if (!accel || !accel->Initialize(nullptr) || !accel->Build(&scene)) return 4;
     scene.accel = accel.get();

@@ -17,6 +17,10 @@ Fixtures written:
       scene, and the film and per-pixel variance of the reference's own
       renderer::pt (compiled from its sources) at 16,384 samples per pixel,
       in single precision and in double precision (LM_USE_DOUBLE_PRECISION).
+  materials_pt.npz
+      The same box with a glass box (bsdf::flesnel), a GGX conductor box
+      (bsdf::cook_torrance) and a constant environment light (light::env),
+      reference films likewise.
   soup_small.npz
       A seeded three-primitive scene (random triangle soup, heightfield,
       duplicated triangles for exact-t ties, zero-area triangles) and rays
@@ -161,24 +165,36 @@ def soup_case(tmp: str) -> dict:
     return out
 
 
-def cornell_case() -> dict:
-    sc = scenes.cornell_box(64, 64)
-    W, H = 64, 64
-    N = W * H * 16384
-    f = lo.run_ref_render(sc, N, 9, 20240601, os.cpu_count() or 8)
-    d = lo.run_ref_render(sc, N, 9, 20240602, os.cpu_count() or 8, double=True)
-    out = {"width": np.int32(W), "height": np.int32(H), "num_samples": np.int64(N), "max_num_vertices": np.int32(9),
-           "ref_image": f["image"].astype(np.float32), "ref_variance": f["variance"].astype(np.float32),
-           "ref64_image": d["image"].astype(np.float64), "ref64_variance": d["variance"].astype(np.float64)}
-    for i, p in enumerate(sc["prims"]):
-        out[f"prim{i}_tris"] = p["tris"]
-        out[f"prim{i}_kind"] = np.int32(p["kind"])
-        out[f"prim{i}_R"] = np.array(p["R"], np.float32)
-        out[f"prim{i}_Le"] = np.array(p["Le"], np.float32)
-    out["nprims"] = np.int32(len(sc["prims"]))
+def scene_arrays(sc: dict) -> dict:
+    """A path-tracing scene as flat arrays (read back by tests/ptscene.py)."""
+    out = {"nprims": np.int32(len(sc["prims"]))}
+    for i, p0 in enumerate(sc["prims"]):
+        p = scenes.prim_params(p0)
+        out[f"prim{i}_tris"] = np.asarray(p["tris"], np.float32)
+        out[f"prim{i}_bsdf"] = np.int32(p["bsdf"])
+        out[f"prim{i}_light"] = np.int32(1 if p["light"] else 0)
+        for k in ("R", "Le", "ct_eta", "ct_k"):
+            out[f"prim{i}_{k}"] = np.array(p[k], np.float32)
+        for k in ("eta1", "eta2", "roughness"):
+            out[f"prim{i}_{k}"] = np.float32(p[k])
     c = sc["camera"]
     out["cam_eye"], out["cam_center"], out["cam_up"] = (np.array(c[k], np.float32) for k in ("eye", "center", "up"))
     out["cam_fov"] = np.float32(c["fov"])
+    out["width"], out["height"] = np.int32(c["width"]), np.int32(c["height"])
+    out["has_env"] = np.int32(1 if sc.get("env") is not None else 0)
+    out["env_Le"] = np.array(sc.get("env") or (0.0, 0.0, 0.0), np.float32)
+    return out
+
+
+def pt_case(sc: dict, spp: int, seed: int) -> dict:
+    W, H = sc["camera"]["width"], sc["camera"]["height"]
+    N = W * H * spp
+    f = lo.run_ref_render(sc, N, 9, seed, os.cpu_count() or 8)
+    d = lo.run_ref_render(sc, N, 9, seed + 1, os.cpu_count() or 8, double=True)
+    out = scene_arrays(sc)
+    out.update({"num_samples": np.int64(N), "max_num_vertices": np.int32(9),
+                "ref_image": f["image"].astype(np.float32), "ref_variance": f["variance"].astype(np.float32),
+                "ref64_image": d["image"].astype(np.float64), "ref64_variance": d["variance"].astype(np.float64)})
     return out
 
 
@@ -191,7 +207,9 @@ def main() -> None:
         np.savez_compressed(os.path.join(HERE, "accel3_simple.npz"), **accel3_case(src, "StubTriangleMesh_Simple", False, tmp))
         np.savez_compressed(os.path.join(HERE, "accel3_simple2.npz"), **accel3_case(src, "StubTriangleMesh_Simple2", True, tmp))
         np.savez_compressed(os.path.join(HERE, "soup_small.npz"), **soup_case(tmp))
-    np.savez_compressed(os.path.join(HERE, "cornell_pt.npz"), **cornell_case())
+    np.savez_compressed(os.path.join(HERE, "cornell_pt.npz"), **pt_case(scenes.cornell_box(64, 64), 16384, 20240601))
+    np.savez_compressed(os.path.join(HERE, "materials_pt.npz"),
+                        **pt_case(scenes.cornell_materials(64, 64), 16384, 20240701))
     print("fixtures written to", HERE)
 
 

@@ -36,3 +36,15 @@ def test_oracle_pt_max_vertices_two_sees_only_lights(oracle_lib, golden_dir):
     r = oracle_lib.render_pt(scene, W * H * 64, 2, 5, 4)
     lit = r["image"].sum(axis=2) > 0
     assert 0 < lit.sum() < 0.05 * W * H
+
+
+def test_oracle_pt_materials_match_reference(oracle_lib, golden_dir):
+    """Glass (bsdf::flesnel), GGX conductor (bsdf::cook_torrance) and a
+    constant environment light, against the reference's film."""
+    scene, z = ptscene.load_scene(golden_dir, "materials_pt")
+    W, H = scene["camera"]["width"], scene["camera"]["height"]
+    imgcheck.assert_same_image(z["ref_image"], z["ref_variance"], z["ref64_image"], z["ref64_variance"], "ref f32/f64")
+    r = oracle_lib.render_pt(scene, W * H * 4096, int(z["max_num_vertices"]), 4321, os.cpu_count() or 4)
+    a, va = ptscene.downsample(r["image"], r["variance"], 2)
+    b, vb = ptscene.downsample(z["ref_image"].astype(np.float64), z["ref_variance"].astype(np.float64), 2)
+    print(imgcheck.assert_same_image(a, va, b, vb, "oracle vs ref (materials)"))
