@@ -323,61 +323,82 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
-def run_pt(args) -> None:
-    """Path-tracing configuration: renderer::pt on the Cornell-style box,
-    256 x 256, 64 samples per pixel, max_num_vertices 9 (8 segments).
-    Metric Msamples/s; value = device-resident film, e2e = the host-pointer
-    lmgpu_render_pt (film copied back every step)."""
+RENDER_WORKLOADS = {
+    # renderer::pt on the Cornell-style box: 256 x 256, 64 spp, max_num_vertices 9 (8 segments)
+    "pt": {"renderer": "pt", "workload": "pt_cornell_256x256_64spp", "width": 256, "height": 256, "spp": 64,
+           "max_num_vertices": 9, "data": "synthetic (procedural Cornell box)", "cpu_spp": 8},
+    # renderer::bdpt on the caustic room: 1280 x 720, 32 spp, path length 10, all (s, t) strategies
+    "bdpt": {"renderer": "bdpt", "workload": "bdpt_caustic_room_1280x720_32spp", "width": 1280, "height": 720,
+             "spp": 32, "max_num_vertices": 10,
+             "data": "synthetic (procedural room, level-5 glass icosphere, sphere light behind a panel)",
+             "cpu_spp": 1},
+}
+
+
+def run_render(args) -> None:
+    """Rendering configurations (renderer::pt, renderer::bdpt).  Metric
+    Msamples/s; value = film left on the device (lmgpu_render_*_device),
+    e2e = the host-pointer lmgpu_render_* (film and variance copied back
+    every step)."""
     import torch
 
     import lmgpu
     from lmgpu import scenes
 
-    W = H = 256
-    spp, max_nv = 64, 9
-    scene = scenes.cornell_box(W, H)
+    cfg = RENDER_WORKLOADS[args.workload]
+    W, H, spp, max_nv = cfg["width"], cfg["height"], cfg["spp"], cfg["max_num_vertices"]
+    scene = scenes.cornell_box(W, H) if cfg["renderer"] == "pt" else scenes.caustic_room(W, H)
     stream = torch.cuda.Stream()
     sc = lmgpu.Scene(scene)
+    render_dev = sc.render_pt_device if cfg["renderer"] == "pt" else sc.render_bdpt_device
+    render_host = sc.render_pt if cfg["renderer"] == "pt" else sc.render_bdpt
     di = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
     dv = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
     samples = W * H * spp
     for k in range(args.warmup):
-        sc.render_pt_device(di.data_ptr(), dv.data_ptr(), spp, max_nv, k, stream.cuda_stream)
+        render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, k, stream.cuda_stream)
     torch.cuda.synchronize()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
+    l0 = sc.launch_count()
     ev0.record(stream)
     for k in range(args.steps):
-        sc.render_pt_device(di.data_ptr(), dv.data_ptr(), spp, max_nv, 1000 + k, stream.cuda_stream)
+        render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, 1000 + k, stream.cuda_stream)
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
+    launches = sc.launch_count() - l0
     ms = ev0.elapsed_time(ev1) / args.steps
     t0 = time.perf_counter()
     for k in range(args.steps):
-        sc.render_pt(spp, max_nv, 2000 + k)
+        render_host(spp, max_nv, 2000 + k)
     e2e_s = (time.perf_counter() - t0) / args.steps
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import lmoracle
-
-    threads = os.cpu_count() or 1
-    n_cpu = W * H * 8
-    t0 = time.perf_counter()
-    lmoracle.render_pt(scene, n_cpu, max_nv, 5, threads)
-    cpu_s = time.perf_counter() - t0
-    line = {"metric": "Msamples/s (renderer::pt)", "value": samples / ms / 1e3, "unit": "Msamples/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural Cornell box)",
-            "config": {"workload": "pt_cornell_256x256_64spp", "width": W, "height": H, "spp": spp,
-                       "max_num_vertices": max_nv, "triangles": 36},
+    ntri = int(sum(p["tris"].shape[0] for p in scene["prims"]))
+    line = {"metric": f"Msamples/s (renderer::{cfg['renderer']})", "value": samples / ms / 1e3,
+            "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": cfg["data"],
+            "config": {"workload": cfg["workload"], "width": W, "height": H, "spp": spp,
+                       "max_num_vertices": max_nv, "triangles": ntri,
+                       "l2": "film and scene stay resident (the workload's working set)"},
             "e2e": {"value": samples / e2e_s / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": W * H * 3 * 4 * 2, "api": "lmgpu_render_pt (host film)"},
-            "clocks": clk,
-            "cpu_baseline": {"value": n_cpu / cpu_s / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
-                             "sample": f"{n_cpu} samples (8 spp) of the same scene, oracle restatement of "
-                                       f"renderer::pt (renderer_pt.cpp), {threads} threads"}}
+                    "d2h_bytes_per_step": W * H * 3 * 4 * 2, "api": f"lmgpu_render_{cfg['renderer']} (host film)"},
+            "gpu_launches": launches, "clocks": clk}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import lmoracle
+
+        threads = os.cpu_count() or 1
+        n_cpu = W * H * cfg["cpu_spp"]
+        fn = lmoracle.render_pt if cfg["renderer"] == "pt" else lmoracle.render_bdpt
+        t0 = time.perf_counter()
+        fn(scene, n_cpu, max_nv, 5, threads)
+        cpu_s = time.perf_counter() - t0
+        line["cpu_baseline"] = {
+            "value": n_cpu / cpu_s / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"{n_cpu} samples ({cfg['cpu_spp']} spp) of the same scene, oracle restatement of "
+                      f"renderer::{cfg['renderer']} (renderer_{cfg['renderer']}.cpp), {threads} threads"}
     print(json.dumps(line), flush=True)
     sc.close()
 
@@ -391,8 +412,9 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling of smaller cases)")
     ap.add_argument("--anyhit", action="store_true", help="time any-hit queries instead of closest hit")
-    ap.add_argument("--workload", choices=["raycast", "pt"], default="raycast",
-                    help="raycast: the BVH ray-cast configuration (default); pt: renderer::pt on the Cornell box")
+    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt"], default="raycast",
+                    help="raycast: the BVH ray-cast configuration (default); pt: renderer::pt on the Cornell "
+                         "box; bdpt: renderer::bdpt on the caustic room")
     ap.add_argument("--use-ref-binary", action="store_true",
                     help="reference arm: time the reference's own qbvh (x86-64 harness) if built")
     args = ap.parse_args()
@@ -400,8 +422,8 @@ def main() -> None:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "pt":
-        run_pt(args)
+    elif args.workload in RENDER_WORKLOADS:
+        run_render(args)
     else:
         run_gpu(args)
 

@@ -178,6 +178,10 @@ void lmgpu_scene_destroy(lmgpu_scene* scene);
  * meet when they leave the geometry (scene3.cpp:464-475). */
 int lmgpu_scene_set_environment(lmgpu_scene* scene, const float* Le);
 
+/* Number of kernels the renderers have launched for this scene since it was
+ * created (a diagnostic; no counterpart in the reference). */
+int lmgpu_scene_launch_count(const lmgpu_scene* scene, uint64_t* count);
+
 /* The scene's accel (owned by the scene), for ray queries on its triangles. */
 int lmgpu_scene_accel(const lmgpu_scene* scene, const lmgpu_accel** accel);
 
@@ -192,6 +196,22 @@ int lmgpu_render_pt(lmgpu_scene* scene, const lmgpu_pt_params* params, float* im
  * stream); returns after the render has finished. */
 int lmgpu_render_pt_device(lmgpu_scene* scene, const lmgpu_pt_params* params, float* d_image, float* d_variance,
                            void* stream);
+
+/* Renders the scene with bidirectional path tracing (all (s, t) strategies,
+ * power-heuristic MIS) and writes the film as lmgpu_render_pt does.  Stands
+ * in for Renderer::Render of renderer::bdpt
+ * (src/liblightmetrica/renderer/renderer_bdpt.cpp:841-998).  The scene needs
+ * at least one area light (LMGPU_ERR_INVALID otherwise); the environment
+ * light is not part of this estimator, as in the reference.  Light and eye
+ * subpaths are capped at 16 vertices each (max_num_vertices = -1 included);
+ * with roulette 0.5 per step a subpath reaches that cap with probability
+ * 2^-14. */
+int lmgpu_render_bdpt(lmgpu_scene* scene, const lmgpu_pt_params* params, float* image, float* variance);
+
+/* As lmgpu_render_bdpt into device buffers on `stream` (NULL: the scene's
+ * stream); returns after the render has finished. */
+int lmgpu_render_bdpt_device(lmgpu_scene* scene, const lmgpu_pt_params* params, float* d_image, float* d_variance,
+                             void* stream);
 
 /* Largest scene lmgpu_trace_static_scene accepts. */
 #define LMGPU_STATIC_MAX_TRIANGLES 16384

@@ -18,7 +18,7 @@
 //                   (bsdf_diffuse.cpp:69-104, sampler.h:44-67); surviving
 //                   paths are appended to the next queue (warp-aggregated
 //                   atomics, so queues stay compact)
-//   k_pt_finalize   per-pixel mean and FP64 variance of the mean
+//   k_film_finalize per-pixel mean and FP64 variance of the mean (scene.cu)
 // Sampling differs from the reference only in ways that keep the estimator's
 // expectation: raster positions are stratified per pixel (spp jittered
 // samples in each pixel instead of W*H*spp uniform positions over the film),
@@ -26,61 +26,12 @@
 #include "accel.cuh"
 #include "rng.cuh"
 #include "scene.cuh"
+#include "bsdf.cuh"
 
 namespace lmgpu {
 namespace {
 
 constexpr int kShadeThreads = 256;
-
-__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
-__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ float3 cross3(float3 a, float3 b)
-{
-    return f3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
-}
-__device__ __forceinline__ float3 normalize3(float3 a) { return a * rsqrtf(dot3(a, a)); }
-
-// Sampler::UniformConcentricDiskSample + CosineSampleHemisphere (sampler.h:44-67).
-__device__ __forceinline__ float3 cosine_hemisphere(float u0, float u1)
-{
-    const float vx = 2.0f * u0 - 1.0f, vy = 2.0f * u1 - 1.0f;
-    float sx = 0.0f, sy = 0.0f;
-    if (!(vx == 0.0f && vy == 0.0f)) {
-        const float qp = 0.78539816339744831f;  // pi / 4
-        float r, theta;
-        if (vx > -vy) {
-            if (vx > vy) { r = vx; theta = qp * __fdividef(vy, vx); }
-            else { r = vy; theta = qp * (2.0f - __fdividef(vx, vy)); }
-        } else {
-            if (vx < vy) { r = -vx; theta = qp * (4.0f + __fdividef(vy, vx)); }
-            else { r = -vy; theta = qp * (6.0f - __fdividef(vx, vy)); }
-        }
-        float s, c;
-        __sincosf(theta, &s, &c);
-        sx = r * c;
-        sy = r * s;
-    }
-    const float z2 = 1.0f - sx * sx - sy * sy;
-    return f3(sx, sy, sqrtf(fmaxf(z2, 0.0f)));
-}
-
-// Math::OrthonormalBasis (math.h:2355-2359): columns (b, c, a) map local to world.
-__device__ __forceinline__ void basis(float3 a, float3& b, float3& c)
-{
-    c = fabsf(a.x) > fabsf(a.y) ? normalize3(f3(a.z, 0.0f, -a.x)) : normalize3(f3(0.0f, a.z, -a.y));
-    b = cross3(c, a);
-}
-
-// Pinhole direction for raster position (rx, ry) in [0,1]^2 (sensor_pinhole.cpp:86-89).
-__device__ __forceinline__ float3 camera_dir(const CameraGPU& cam, float rx, float ry)
-{
-    const float px = 2.0f * rx - 1.0f, py = 2.0f * ry - 1.0f;
-    const float3 we = normalize3(f3(cam.aspect * cam.tan_fov * px, cam.tan_fov * py, -1.0f));
-    return cam.vx * we.x + cam.vy * we.y + cam.vz * we.z;
-}
 
 __global__ void k_pt_generate(CameraGPU cam, uint64_t p0, uint32_t n, uint32_t seed, float4* __restrict__ rays,
                               PathState* __restrict__ state)
@@ -103,119 +54,12 @@ __global__ void k_pt_generate(CameraGPU cam, uint64_t p0, uint32_t n, uint32_t s
     state[i] = s;
 }
 
-// BSDF_Flesnel::EvaluateFresnelTerm (bsdf_flesnel.cpp:243-257).
-__device__ __forceinline__ float fresnel_dielectric(float wiDotN, float etaI, float etaT)
-{
-    const float eta = etaI / etaT;
-    const float cosThetaTSq = 1.0f - eta * eta * (1.0f - wiDotN * wiDotN);
-    if (cosThetaTSq <= 0.0f) return 1.0f;
-    const float ci = fabsf(wiDotN), ct = sqrtf(cosThetaTSq);
-    const float rs = (etaI * ci - etaT * ct) / (etaI * ci + etaT * ct);
-    const float rt = (etaI * ct - etaT * ci) / (etaI * ct + etaT * ci);
-    return (rs * rs + rt * rt) * 0.5f;
-}
-
-// BSDF_CookTorrance::EvaluateGGX (bsdf_cooktorrance.cpp:187-198).
-__device__ __forceinline__ float ggx_d(float3 H, float a)
-{
-    const float c = H.z;
-    if (c <= 0.0f) return 0.0f;
-    const float t = 1.0f - c * c;
-    const float tanH = t <= 0.0f ? 0.0f : sqrtf(t) / c;
-    const float q = a * a + tanH * tanH;
-    return (a * a) / (3.14159265358979f * c * c * c * c * q * q);
-}
-
-// BSDF_CookTorrance::SampleGGX (bsdf_cooktorrance.cpp:200-225); Math::Eps<float> = 1e-4.
-__device__ __forceinline__ float3 ggx_sample(float ua, float ub, float a)
-{
-    const float eps = 1e-4f;
-    const float u0 = (1.0f - eps) * ua + eps;
-    const float u1 = (1.0f - 2.0f * eps) * ub + eps;
-    const float den = sqrtf(1.0f - (1.0f - a * a) * u0);
-    const float cosT = sqrtf(1.0f - u0) / den;
-    const float sinT = a * (sqrtf(u0) / den);
-    float sp, cp;
-    sincosf(3.14159265358979f * (2.0f * u1 - 1.0f), &sp, &cp);
-    return f3(sinT * cp, sinT * sp, cosT);
-}
-
-// BSDF_CookTorrance::EvaluateFrConductor (bsdf_cooktorrance.cpp:283-291), one channel.
-__device__ __forceinline__ float fresnel_conductor(float c, float eta, float k)
-{
-    const float tmp = (eta * eta + k * k) * (c * c);
-    const float rParl2 = (tmp - eta * (2.0f * c) + 1.0f) / (tmp + eta * (2.0f * c) + 1.0f);
-    const float tmpF = eta * eta + k * k;
-    const float rPerp2 = (tmpF - eta * (2.0f * c) + c * c) / (tmpF + eta * (2.0f * c) + c * c);
-    return (rParl2 + rPerp2) * 0.5f;
-}
-
-// Samples the BSDF of P at a surface with normal n (shading normal = geometric
-// normal: meshes here carry no vertex normals) for the eye-to-light transport
-// direction.  Returns false when the path ends; otherwise the world-space
-// direction wo and the weight f = fs / pdf (projected solid angle).
-__device__ __forceinline__ bool sample_bsdf(const PrimGPU& P, float3 n, float3 wi, float u0, float u1, float u2,
-                                            float3& wo, float f[3])
-{
-    float3 bx, by;
-    basis(n, bx, by);
-    const float3 lwi = f3(dot3(wi, bx), dot3(wi, by), dot3(wi, n));
-    float3 lwo;
-    if (P.bsdf == LMGPU_BSDF_DIFFUSE) {
-        // bsdf_diffuse.cpp:69-104: one-sided, fs / pdf = R
-        if (lwi.z <= 0.0f) return false;
-        lwo = cosine_hemisphere(u0, u1);
-        if (lwo.z <= 0.0f) return false;
-        for (int k = 0; k < 3; k++) f[k] = P.R[k];
-    } else if (P.bsdf == LMGPU_BSDF_DIELECTRIC) {
-        // bsdf_flesnel.cpp:59-164: reflect with probability Fr, else refract;
-        // fs / pdf = R, or R (etaI / etaT)^2 for refraction (EL direction)
-        float etaI = P.eta1, etaT = P.eta2;
-        if (lwi.z < 0.0f) { const float t = etaI; etaI = etaT; etaT = t; }
-        const float Fr = fresnel_dielectric(lwi.z, etaI, etaT);
-        float scale = 1.0f;
-        if (u2 <= Fr) {
-            lwo = f3(-lwi.x, -lwi.y, lwi.z);
-        } else {
-            const float eta = etaI / etaT;
-            const float cosTSq = 1.0f - eta * eta * (1.0f - lwi.z * lwi.z);
-            const float cosT = sqrtf(fmaxf(cosTSq, 0.0f)) * (lwi.z > 0.0f ? -1.0f : 1.0f);
-            lwo = f3(-eta * lwi.x, -eta * lwi.y, cosT);
-            scale = eta * eta;
-        }
-        for (int k = 0; k < 3; k++) f[k] = P.R[k] * scale;
-    } else if (P.bsdf == LMGPU_BSDF_COOK_TORRANCE) {
-        // bsdf_cooktorrance.cpp:73-120, GGX; G uses |wo.H| in both terms
-        if (lwi.z <= 0.0f) return false;
-        const float3 H = ggx_sample(u0, u1, P.roughness);
-        const float dih = -dot3(lwi, H);
-        lwo = (lwi * -1.0f) - H * (2.0f * dih);
-        if (lwo.z <= 0.0f) return false;
-        const float3 Hn = normalize3(lwi + lwo);
-        const float D = ggx_d(Hn, P.roughness);
-        const float woH = fabsf(dot3(lwo, Hn));
-        const float G = fminf(1.0f, fminf(2.0f * Hn.z * lwo.z / woH, 2.0f * Hn.z * lwi.z / woH));
-        const float pdf = D * Hn.z / (4.0f * dot3(lwo, Hn)) / lwo.z;
-        if (!(pdf > 0.0f)) return false;
-        const float cih = dot3(lwi, Hn);
-        for (int k = 0; k < 3; k++) {
-            const float F = fresnel_conductor(cih, P.ct_eta[k], P.ct_k[k]);
-            f[k] = (P.R[k] * D * G * F / (4.0f * lwi.z) / lwo.z) / pdf;
-        }
-    } else {
-        return false;  // bsdf::null
-    }
-    if (f[0] == 0.0f && f[1] == 0.0f && f[2] == 0.0f) return false;
-    wo = bx * lwo.x + by * lwo.y + n * lwo.z;
-    return true;
-}
-
-__device__ __forceinline__ void splat(float* __restrict__ film, double* __restrict__ film_sq, uint32_t pixel,
+__device__ __forceinline__ void splat(double* __restrict__ film, double* __restrict__ film_sq, uint32_t pixel,
                                       const float c[3])
 {
     for (int k = 0; k < 3; k++) {
         if (c[k] != 0.0f) {
-            atomicAdd(&film[3 * (size_t)pixel + k], c[k]);
+            atomicAdd(&film[3 * (size_t)pixel + k], (double)c[k]);
             atomicAdd(&film_sq[3 * (size_t)pixel + k], (double)c[k] * (double)c[k]);
         }
     }
@@ -225,7 +69,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(const float4* __rest
                                                             const PathState* __restrict__ state,
                                                             const lmgpu_hit* __restrict__ hits, uint32_t n,
                                                             SceneGPU sc, int max_nv, uint32_t seed,
-                                                            float* __restrict__ film, double* __restrict__ film_sq,
+                                                            double* __restrict__ film, double* __restrict__ film_sq,
                                                             float4* __restrict__ out_rays,
                                                             PathState* __restrict__ out_state,
                                                             uint32_t* __restrict__ out_count)
@@ -293,19 +137,6 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(const float4* __rest
     }
 }
 
-__global__ void k_pt_finalize(const float* __restrict__ film, const double* __restrict__ film_sq, uint32_t n3,
-                              double spp, float* __restrict__ image, float* __restrict__ variance)
-{
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n3) return;
-    const double mean = (double)film[i] / spp;
-    image[i] = (float)mean;
-    if (variance) {
-        const double v = (film_sq[i] / spp - mean * mean) / spp;
-        variance[i] = (float)(v > 0.0 ? v : 0.0);
-    }
-}
-
 }  // namespace
 
 int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream)
@@ -314,17 +145,16 @@ int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float
     const uint64_t npix = (uint64_t)W * H;
     const uint64_t total = npix * prm->spp;
     if (total == 0) return LMGPU_OK;
-    int rc = ensure_film(sc, npix);
+    int rc = clear_film(sc, npix, stream);
     if (rc) return rc;
     rc = ensure_queues(sc, total < kWave ? total : kWave);
     if (rc) return rc;
-    LMGPU_CUDA_TRY(cudaMemsetAsync(sc->film, 0, sizeof(float) * 3 * npix, stream));
-    LMGPU_CUDA_TRY(cudaMemsetAsync(sc->film_sq, 0, sizeof(double) * 3 * npix, stream));
     const SceneGPU sg = scene_view(sc);
     for (uint64_t p0 = 0; p0 < total; p0 += kWave) {
         uint32_t n = (uint32_t)((total - p0) < kWave ? (total - p0) : kWave);
         k_pt_generate<<<(n + 255) / 256, 256, 0, stream>>>(sc->cam, p0, n, prm->seed, sc->q_ray[0], sc->q_state[0]);
         LMGPU_CUDA_TRY(cudaGetLastError());
+        sc->launches++;
         int cur = 0;
         while (n > 0) {
             rc = launch_trace(sc->accel, sc->q_ray[cur], sc->q_hit, n, false, false, stream);
@@ -334,17 +164,14 @@ int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float
                 sc->q_ray[cur], sc->q_state[cur], sc->q_hit, n, sg, prm->max_num_vertices, prm->seed, sc->film,
                 sc->film_sq, sc->q_ray[1 - cur], sc->q_state[1 - cur], sc->q_count);
             LMGPU_CUDA_TRY(cudaGetLastError());
+            sc->launches += 2;  // trace + shade
             LMGPU_CUDA_TRY(cudaMemcpyAsync(sc->h_count, sc->q_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
             LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
             n = *sc->h_count;
             cur = 1 - cur;
         }
     }
-    const uint32_t n3 = (uint32_t)(3 * npix);
-    k_pt_finalize<<<(n3 + 255) / 256, 256, 0, stream>>>(sc->film, sc->film_sq, n3, (double)prm->spp, d_image,
-                                                       d_variance);
-    LMGPU_CUDA_TRY(cudaGetLastError());
-    return LMGPU_OK;
+    return finalize_film(sc, prm->spp, d_image, d_variance, stream);
 }
 
 }  // namespace lmgpu

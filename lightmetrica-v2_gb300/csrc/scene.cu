@@ -3,6 +3,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 namespace lmgpu {
 
@@ -40,6 +41,7 @@ int ensure_film(lmgpu_scene* sc, uint64_t npix)
     if (sc->film_cap >= npix) return LMGPU_OK;
     int rc;
     if ((rc = grow(&sc->film, 3 * npix)) || (rc = grow(&sc->film_sq, 3 * npix)) ||
+        (rc = grow(&sc->film_x, 3 * npix)) || (rc = grow(&sc->film_x_sq, 3 * npix)) ||
         (rc = grow(&sc->d_image, 3 * npix)) || (rc = grow(&sc->d_variance, 3 * npix)))
         return rc;
     sc->film_cap = npix;
@@ -54,6 +56,118 @@ int ensure_queues(lmgpu_scene* sc, uint64_t n)
         if ((rc = grow(&sc->q_ray[i], 2 * n)) || (rc = grow(&sc->q_state[i], n))) return rc;
     if ((rc = grow(&sc->q_hit, n))) return rc;
     sc->q_cap = n;
+    return LMGPU_OK;
+}
+
+// Mean and variance of the film estimate I = (S_own + S_x) / spp, where
+// S_own sums the spp i.i.d. samples of the pixel's stratum and S_x the
+// spp * (pixels - 1) i.i.d. samples of the other strata that splat there:
+// Var(I) = [spp Var(X_own) + n_x Var(X_x)] / spp^2, each Var(X) estimated as
+// sum(x^2) / n - (sum(x) / n)^2.
+__global__ void k_film_finalize(const double* __restrict__ film, const double* __restrict__ film_sq,
+                                const double* __restrict__ film_x, const double* __restrict__ film_x_sq, uint32_t n3,
+                                double spp, double n_x, float* __restrict__ image, float* __restrict__ variance)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n3) return;
+    const double so = film[i], sx = film_x[i];
+    image[i] = (float)((so + sx) / spp);
+    if (variance) {
+        double v = film_sq[i] - so * so / spp;
+        if (n_x > 0.0) v += film_x_sq[i] - sx * sx / n_x;
+        v /= spp * spp;
+        variance[i] = (float)(v > 0.0 ? v : 0.0);
+    }
+}
+
+int clear_film(lmgpu_scene* sc, uint64_t npix, cudaStream_t stream)
+{
+    int rc = ensure_film(sc, npix);
+    if (rc) return rc;
+    LMGPU_CUDA_TRY(cudaMemsetAsync(sc->film, 0, sizeof(double) * 3 * npix, stream));
+    LMGPU_CUDA_TRY(cudaMemsetAsync(sc->film_sq, 0, sizeof(double) * 3 * npix, stream));
+    LMGPU_CUDA_TRY(cudaMemsetAsync(sc->film_x, 0, sizeof(double) * 3 * npix, stream));
+    LMGPU_CUDA_TRY(cudaMemsetAsync(sc->film_x_sq, 0, sizeof(double) * 3 * npix, stream));
+    return LMGPU_OK;
+}
+
+int finalize_film(lmgpu_scene* sc, uint64_t spp, float* d_image, float* d_variance, cudaStream_t stream)
+{
+    const uint64_t npix = (uint64_t)sc->cam.width * sc->cam.height;
+    const uint32_t n3 = (uint32_t)(3 * npix);
+    k_film_finalize<<<(n3 + 255) / 256, 256, 0, stream>>>(sc->film, sc->film_sq, sc->film_x, sc->film_x_sq, n3,
+                                                         (double)spp, (double)spp * (double)(npix - 1), d_image,
+                                                         d_variance);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+    sc->launches++;
+    return LMGPU_OK;
+}
+
+// Light tables: per light primitive its triangles and their normalised area
+// CDF (TriangleUtils::CreateTriangleAreaDist, triangleutils.h:40-77;
+// Distribution1D::Normalize, dist.h:55-67) and the inverse total area
+// (light_area.cpp:47-60), packed in one device allocation.
+int build_lights(lmgpu_scene* sc, const float* tris, const int32_t* tri_prim, uint64_t ntri, const lmgpu_prim* prims,
+                 uint32_t nprims)
+{
+    std::vector<int32_t> prim_light(nprims, -1), light_prims, tri_off(1, 0), ltris;
+    std::vector<float> cdf, inv_area;
+    for (uint32_t i = 0; i < nprims; i++)
+        if (prims[i].is_light) {
+            prim_light[i] = (int32_t)light_prims.size();
+            light_prims.push_back((int32_t)i);
+        }
+    std::vector<std::vector<int32_t>> by_light(light_prims.size());
+    for (uint64_t k = 0; k < ntri; k++)
+        if (prim_light[tri_prim[k]] >= 0) by_light[prim_light[tri_prim[k]]].push_back((int32_t)k);
+    for (size_t l = 0; l < light_prims.size(); l++) {
+        if (by_light[l].empty()) {
+            set_error("lmgpu_scene_create: light primitive " + std::to_string(light_prims[l]) + " has no triangles");
+            return LMGPU_ERR_INVALID;
+        }
+        const size_t c0 = cdf.size();
+        cdf.push_back(0.0f);
+        float sum = 0.0f;
+        for (int32_t k : by_light[l]) {
+            const float* T = tris + 9 * (size_t)k;
+            const float3 c = cross(sub3(make3(T + 3), make3(T)), sub3(make3(T + 6), make3(T)));
+            const float area = std::sqrt(c.x * c.x + c.y * c.y + c.z * c.z) * 0.5f;
+            cdf.push_back(cdf.back() + area);
+            sum += area;
+            ltris.push_back(k);
+        }
+        const float total = cdf.back();
+        for (size_t q = c0; q < cdf.size(); q++) cdf[q] /= total;
+        inv_area.push_back(1.0f / sum);
+        tri_off.push_back((int32_t)ltris.size());
+    }
+    const size_t nl = light_prims.size();
+    const size_t bytes = 4 * (nl + nprims + tri_off.size() + ltris.size() + cdf.size() + inv_area.size()) + 4;
+    std::vector<unsigned char> host(bytes);
+    size_t off = 0;
+    auto put = [&](const void* src, size_t n) {
+        const size_t at = off;
+        if (n) std::memcpy(host.data() + off, src, n);
+        off += n;
+        return at;
+    };
+    const size_t o_prims = put(light_prims.data(), 4 * nl), o_pl = put(prim_light.data(), 4 * (size_t)nprims),
+                 o_off = put(tri_off.data(), 4 * tri_off.size()), o_tris = put(ltris.data(), 4 * ltris.size()),
+                 o_cdf = put(cdf.data(), 4 * cdf.size()), o_ia = put(inv_area.data(), 4 * inv_area.size());
+    if (cudaMalloc(&sc->light_buf, bytes) != cudaSuccess ||
+        cudaMemcpy(sc->light_buf, host.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+        set_error("lmgpu_scene_create: light table upload failed");
+        return LMGPU_ERR_CUDA;
+    }
+    unsigned char* b = (unsigned char*)sc->light_buf;
+    LightsGPU& L = sc->lights;
+    L.count = (int32_t)nl;
+    L.prims = (const int32_t*)(b + o_prims);
+    L.prim_light = (const int32_t*)(b + o_pl);
+    L.tri_off = (const int32_t*)(b + o_off);
+    L.tris = (const int32_t*)(b + o_tris);
+    L.cdf = (const float*)(b + o_cdf);
+    L.inv_area = (const float*)(b + o_ia);
     return LMGPU_OK;
 }
 
@@ -126,6 +240,8 @@ int lmgpu_scene_create(const float* tris, const int32_t* tri_prim, uint64_t ntri
     }
     rc = build_bvh(sc->accel, sc->tris, ntri, sc->stream);
     if (rc) return fail(rc);
+    rc = build_lights(sc, tris, tri_prim, ntri, prims, nprims);
+    if (rc) return fail(rc);
     // lookat basis (scene3.cpp:213-221) and pinhole parameters (sensor_pinhole.cpp:46-62)
     const float3 eye = make3(cam->eye), center = make3(cam->center), up = make3(cam->up);
     CameraGPU& c = sc->cam;
@@ -172,13 +288,26 @@ void lmgpu_scene_destroy(lmgpu_scene* sc)
     if (!sc) return;
     if (sc->stream) cudaStreamSynchronize(sc->stream);
     lmgpu_accel_destroy(sc->accel);
-    void* ptrs[] = {sc->tris, sc->tri_prim, sc->prims, sc->film, sc->film_sq, sc->d_image, sc->d_variance,
-                    sc->q_ray[0], sc->q_ray[1], sc->q_state[0], sc->q_state[1], sc->q_hit, sc->q_count};
+    void* ptrs[] = {sc->tris, sc->tri_prim, sc->prims, sc->film, sc->film_sq, sc->film_x, sc->film_x_sq,
+                    sc->d_image, sc->d_variance,
+                    sc->q_ray[0], sc->q_ray[1], sc->q_state[0], sc->q_state[1], sc->q_hit, sc->q_count,
+                    sc->light_buf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (sc->h_count) cudaFreeHost(sc->h_count);
     if (sc->stream) cudaStreamDestroy(sc->stream);
     delete sc;
+}
+
+int lmgpu_scene_launch_count(const lmgpu_scene* sc, uint64_t* count)
+{
+    clear_error();
+    if (!sc || !count) {
+        set_error("lmgpu_scene_launch_count: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    *count = sc->launches;
+    return LMGPU_OK;
 }
 
 int lmgpu_scene_accel(const lmgpu_scene* sc, const lmgpu_accel** accel)
@@ -192,42 +321,47 @@ int lmgpu_scene_accel(const lmgpu_scene* sc, const lmgpu_accel** accel)
     return LMGPU_OK;
 }
 
-int lmgpu_render_pt_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance,
-                           void* stream)
+}  // extern "C"
+
+namespace {
+
+using RenderFn = int (*)(lmgpu_scene*, const lmgpu_pt_params*, float*, float*, cudaStream_t);
+
+int render_device(const char* name, RenderFn fn, lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image,
+                  float* d_variance, void* stream)
 {
-    clear_error();
     if (!sc || !prm || !d_image) {
-        set_error("lmgpu_render_pt_device: NULL argument");
+        set_error(std::string(name) + ": NULL argument");
         return LMGPU_ERR_INVALID;
     }
     if (prm->spp == 0 || (uint64_t)sc->cam.width * sc->cam.height * prm->spp > (1ull << 40)) {
-        set_error("lmgpu_render_pt_device: spp must be in [1, 2^40 / pixels]");
+        set_error(std::string(name) + ": spp must be in [1, 2^40 / pixels]");
         return LMGPU_ERR_INVALID;
     }
     cudaStream_t s = stream ? (cudaStream_t)stream : sc->stream;
-    int rc = render_pt(sc, prm, d_image, d_variance, s);
+    int rc = fn(sc, prm, d_image, d_variance, s);
     if (rc) return rc;
     uint32_t st = 0;
     LMGPU_CUDA_TRY(cudaMemcpyAsync(&st, sc->accel->status, sizeof(st), cudaMemcpyDeviceToHost, s));
     LMGPU_CUDA_TRY(cudaStreamSynchronize(s));
     if (st & (kStatusBadTree | kStatusStackOverflow)) {
-        set_error("lmgpu_render_pt: traversal status " + std::to_string(st));
+        set_error(std::string(name) + ": traversal status " + std::to_string(st));
         return LMGPU_ERR_OVERFLOW;
     }
     return LMGPU_OK;
 }
 
-int lmgpu_render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image, float* variance)
+int render_host(const char* name, RenderFn fn, lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image,
+                float* variance)
 {
-    clear_error();
     if (!sc || !prm || !image) {
-        set_error("lmgpu_render_pt: NULL argument");
+        set_error(std::string(name) + ": NULL argument");
         return LMGPU_ERR_INVALID;
     }
     const uint64_t npix = (uint64_t)sc->cam.width * sc->cam.height;
     int rc = ensure_film(sc, npix);
     if (rc) return rc;
-    rc = lmgpu_render_pt_device(sc, prm, sc->d_image, variance ? sc->d_variance : nullptr, sc->stream);
+    rc = render_device(name, fn, sc, prm, sc->d_image, variance ? sc->d_variance : nullptr, sc->stream);
     if (rc) return rc;
     LMGPU_CUDA_TRY(cudaMemcpyAsync(image, sc->d_image, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost, sc->stream));
     if (variance)
@@ -235,6 +369,36 @@ int lmgpu_render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image, f
                                        sc->stream));
     LMGPU_CUDA_TRY(cudaStreamSynchronize(sc->stream));
     return LMGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lmgpu_render_pt_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance,
+                           void* stream)
+{
+    clear_error();
+    return render_device("lmgpu_render_pt_device", render_pt, sc, prm, d_image, d_variance, stream);
+}
+
+int lmgpu_render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image, float* variance)
+{
+    clear_error();
+    return render_host("lmgpu_render_pt", render_pt, sc, prm, image, variance);
+}
+
+int lmgpu_render_bdpt_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance,
+                             void* stream)
+{
+    clear_error();
+    return render_device("lmgpu_render_bdpt_device", render_bdpt, sc, prm, d_image, d_variance, stream);
+}
+
+int lmgpu_render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image, float* variance)
+{
+    clear_error();
+    return render_host("lmgpu_render_bdpt", render_bdpt, sc, prm, image, variance);
 }
 
 }  // extern "C"

@@ -46,6 +46,19 @@ struct SceneGPU {
     float env_Le[3];
 };
 
+// Area lights for the bidirectional renderer: the primitives flagged as
+// lights, each with its triangles and their area CDF
+// (TriangleUtils::CreateTriangleAreaDist, triangleutils.h:40-77).
+struct LightsGPU {
+    int32_t count;
+    const int32_t* prims;       // light -> primitive
+    const int32_t* prim_light;  // primitive -> light, -1 if not a light
+    const int32_t* tri_off;     // light -> first entry in tris; count + 1 entries
+    const int32_t* tris;        // global triangle ids grouped by light
+    const float* cdf;           // per light (its triangle count + 1) entries, at tri_off[l] + l
+    const float* inv_area;      // light -> 1 / total area
+};
+
 }  // namespace lmgpu
 
 struct lmgpu_scene {
@@ -60,10 +73,21 @@ struct lmgpu_scene {
     float env_Le[3] = {0.0f, 0.0f, 0.0f};
     float sphere_center[3] = {0.0f, 0.0f, 0.0f};  // bounding sphere (scene3.cpp:74-78)
     float sphere_radius = 0.0f;
+    lmgpu::LightsGPU lights{};
+    void* light_buf = nullptr;  // one allocation behind the pointers of lights
 
-    // film: per-pixel sums of splats (FP32) and of their squares (FP64)
-    float* film = nullptr;
+    // film: per-pixel sums of splats and of their squares, in FP64 (splats
+    // are FP32 values; FP32 sums drop every splat below half an ulp of the
+    // running sum, a visible bias once a pixel holds ~10^4 samples).
+    // film / film_sq take the splats of the pixel's own samples (its
+    // stratum), film_x / film_x_sq the splats that samples of other pixels
+    // make there (light-to-camera connections); the two groups have
+    // different distributions, so the variance of the estimate is summed
+    // over them separately.
+    double* film = nullptr;
     double* film_sq = nullptr;
+    double* film_x = nullptr;
+    double* film_x_sq = nullptr;
     uint64_t film_cap = 0;
     float* d_image = nullptr;     // staging for the host-pointer render entry points
     float* d_variance = nullptr;
@@ -76,6 +100,7 @@ struct lmgpu_scene {
     uint32_t* h_count = nullptr;  // pinned host copy
     uint64_t q_cap = 0;
     cudaStream_t stream = nullptr;
+    uint64_t launches = 0;  // kernels launched by the renderers since creation
 };
 
 namespace lmgpu {
@@ -83,6 +108,9 @@ namespace lmgpu {
 int ensure_film(lmgpu_scene* sc, uint64_t npix);
 int ensure_queues(lmgpu_scene* sc, uint64_t n);
 SceneGPU scene_view(const lmgpu_scene* sc);
+int clear_film(lmgpu_scene* sc, uint64_t npix, cudaStream_t stream);
+int finalize_film(lmgpu_scene* sc, uint64_t spp, float* d_image, float* d_variance, cudaStream_t stream);
 int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream);
+int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream);
 
 }  // namespace lmgpu

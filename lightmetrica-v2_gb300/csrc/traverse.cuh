@@ -1,0 +1,228 @@
+// Device-side ray traversal primitives shared by the batch traversal kernel
+// (trace.cu) and the renderers' kernels: ray set-up, the 8-wide node test,
+// the watertight triangle test, and a per-thread closest/any-hit query.
+#pragma once
+
+#include "accel.cuh"
+
+namespace lmgpu {
+
+constexpr int kStack = 32;
+
+struct RayState {
+    float ox, oy, oz;
+    float tmin;
+    float idx, idy, idz;  // 1 / d (zero components replaced by a tiny value)
+    uint32_t oct_inv;     // 7 - octant; octant bit set = negative direction
+    // watertight setup
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+
+__device__ __forceinline__ float comp(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+__device__ __forceinline__ float safe_rcp(float d)
+{
+    const float tiny = 1e-20f;
+    return 1.0f / (fabsf(d) > tiny ? d : copysignf(tiny, d));
+}
+
+__device__ __forceinline__ void setup_ray(const float4 r0, const float4 r1, RayState& R)
+{
+    R.ox = r0.x; R.oy = r0.y; R.oz = r0.z; R.tmin = r0.w;
+    R.idx = safe_rcp(r1.x); R.idy = safe_rcp(r1.y); R.idz = safe_rcp(r1.z);
+    const uint32_t oct = (R.idx < 0.0f ? 1u : 0u) | (R.idy < 0.0f ? 2u : 0u) | (R.idz < 0.0f ? 4u : 0u);
+    R.oct_inv = 7u - oct;
+    const float ax = fabsf(r1.x), ay = fabsf(r1.y), az = fabsf(r1.z);
+    int kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    const float dkz = comp(r1.x, r1.y, r1.z, kz);
+    if (dkz < 0.0f) { const int t = kx; kx = ky; ky = t; }
+    R.kx = kx; R.ky = ky; R.kz = kz;
+    R.Sx = comp(r1.x, r1.y, r1.z, kx) / dkz;
+    R.Sy = comp(r1.x, r1.y, r1.z, ky) / dkz;
+    R.Sz = 1.0f / dkz;
+}
+
+// Byte k of w as a float: the byte becomes the low mantissa bits of 2^23,
+// and subtracting 2^23 leaves it exactly (PRMT + FADD instead of a
+// shift/mask and an int-to-float conversion).
+__device__ __forceinline__ float qbyte(uint32_t w, int k)
+{
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)k)) - 8388608.0f;
+}
+
+// Tests the eight child boxes of one node; returns the hit mask
+// (bits 24..31 inner children in permuted slot order, bits 0..23 triangles).
+__device__ __forceinline__ uint32_t intersect_node(const WNode* __restrict__ nodes, uint32_t ni, const RayState& R,
+                                                   float tmax, uint32_t& child_base, uint32_t& tri_base,
+                                                   uint32_t& imask)
+{
+    const uint4* np = reinterpret_cast<const uint4*>(nodes + ni);
+    const uint4 w0 = __ldg(np + 0);
+    const uint4 w1 = __ldg(np + 1);
+    const uint4 w2 = __ldg(np + 2);
+    const uint4 w3 = __ldg(np + 3);
+    const uint4 w4 = __ldg(np + 4);
+    const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+    const float sx = __uint_as_float((w0.w & 0xffu) << 23);
+    const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
+    const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+    imask = w0.w >> 24;
+    child_base = w1.x;
+    tri_base = w1.y;
+    const float ax = sx * R.idx, ay = sy * R.idy, az = sz * R.idz;
+    const float bx = (px - R.ox) * R.idx, by = (py - R.oy) * R.idy, bz = (pz - R.oz) * R.idz;
+    const bool nx = R.idx < 0.0f, ny = R.idy < 0.0f, nz = R.idz < 0.0f;
+    uint32_t hm = 0;
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        const uint32_t meta4 = half ? w1.w : w1.z;
+        const uint32_t lox = half ? w2.y : w2.x, loy = half ? w2.w : w2.z, loz = half ? w3.y : w3.x;
+        const uint32_t hix = half ? w3.w : w3.z, hiy = half ? w4.y : w4.x, hiz = half ? w4.w : w4.z;
+        const uint32_t nearx = nx ? hix : lox, farx = nx ? lox : hix;
+        const uint32_t neary = ny ? hiy : loy, fary = ny ? loy : hiy;
+        const uint32_t nearz = nz ? hiz : loz, farz = nz ? loz : hiz;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float tnx = fmaf(qbyte(nearx, k), ax, bx);
+            const float tny = fmaf(qbyte(neary, k), ay, by);
+            const float tnz = fmaf(qbyte(nearz, k), az, bz);
+            const float tfx = fmaf(qbyte(farx, k), ax, bx);
+            const float tfy = fmaf(qbyte(fary, k), ay, by);
+            const float tfz = fmaf(qbyte(farz, k), az, bz);
+            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, R.tmin));
+            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+            if (tn <= tf) {
+                const uint32_t meta = (meta4 >> (8 * k)) & 0xffu;
+                uint32_t bit = meta & 0x1fu;
+                if (bit >= 24u) bit ^= R.oct_inv;
+                hm |= (meta >> 5) << bit;
+            }
+        }
+    }
+    return hm;
+}
+
+// Watertight ray/triangle test.  Returns true and (t, b1, b2) when the ray
+// meets the triangle in [tmin, tmax].
+__device__ __forceinline__ bool intersect_tri(const WTri* __restrict__ tris, uint32_t ti, const RayState& R,
+                                              float tmax, float& t_out, float& b1_out, float& b2_out, int& id_out)
+{
+    const float4* tp = reinterpret_cast<const float4*>(tris + ti);
+    const float4 v0 = __ldg(tp + 0);
+    const float4 v1 = __ldg(tp + 1);
+    const float4 v2 = __ldg(tp + 2);
+    const float Ax3[3] = {v0.x - R.ox, v0.y - R.oy, v0.z - R.oz};
+    const float Bx3[3] = {v1.x - R.ox, v1.y - R.oy, v1.z - R.oz};
+    const float Cx3[3] = {v2.x - R.ox, v2.y - R.oy, v2.z - R.oz};
+    const float Akx = comp(Ax3[0], Ax3[1], Ax3[2], R.kx), Aky = comp(Ax3[0], Ax3[1], Ax3[2], R.ky),
+                Akz = comp(Ax3[0], Ax3[1], Ax3[2], R.kz);
+    const float Bkx = comp(Bx3[0], Bx3[1], Bx3[2], R.kx), Bky = comp(Bx3[0], Bx3[1], Bx3[2], R.ky),
+                Bkz = comp(Bx3[0], Bx3[1], Bx3[2], R.kz);
+    const float Ckx = comp(Cx3[0], Cx3[1], Cx3[2], R.kx), Cky = comp(Cx3[0], Cx3[1], Cx3[2], R.ky),
+                Ckz = comp(Cx3[0], Cx3[1], Cx3[2], R.kz);
+    const float Ax = fmaf(-R.Sx, Akz, Akx), Ay = fmaf(-R.Sy, Akz, Aky);
+    const float Bx = fmaf(-R.Sx, Bkz, Bkx), By = fmaf(-R.Sy, Bkz, Bky);
+    const float Cx = fmaf(-R.Sx, Ckz, Ckx), Cy = fmaf(-R.Sy, Ckz, Cky);
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = U + V + W;
+    if (det == 0.0f) return false;
+    const float Az = R.Sz * Akz, Bz = R.Sz * Bkz, Cz = R.Sz * Ckz;
+    const float T = fmaf(U, Az, fmaf(V, Bz, W * Cz));
+    const float t = __fdiv_rn(T, det);
+    if (!(t >= R.tmin && t <= tmax)) return false;
+    const float rdet = __frcp_rn(det);
+    t_out = t;
+    b1_out = V * rdet;
+    b2_out = W * rdet;
+    id_out = __float_as_int(v0.w);
+    return true;
+}
+
+// One ray, one thread: closest hit (anyhit = false) or any hit in
+// [tmin, tmax] against the wide BVH.  Returns false (no hit) and raises a
+// status bit if the tree is malformed or the stack overflows.
+struct TraceView {
+    const WNode* nodes;
+    const WTri* tris;
+    uint32_t num_nodes, num_tris;
+    uint32_t* status;
+};
+
+__device__ __forceinline__ bool trace_single(const TraceView& tv, float3 o, float tmin, float3 d, float tmax,
+                                             bool anyhit, float& t_out, int& id_out, float& b1_out, float& b2_out)
+{
+    RayState R;
+    setup_ray(make_float4(o.x, o.y, o.z, tmin), make_float4(d.x, d.y, d.z, tmax), R);
+    float best_t = tmax, bb1 = 0.0f, bb2 = 0.0f;
+    int best_id = -1;
+    uint2 stack[kStack];
+    int sp = 0;
+    uint2 ng = make_uint2(0u, tv.num_nodes > 0 ? 0x80000000u : 0u);
+    uint32_t budget = tv.num_nodes + 1;
+    while (true) {
+        if (ng.y & 0xff000000u) {
+            const uint32_t bit = 31u - __clz(ng.y & 0xff000000u);
+            ng.y &= ~(1u << bit);
+            const uint32_t slot = (bit - 24u) ^ R.oct_inv;
+            const uint32_t rel = __popc(ng.y & 0xffu & ((1u << slot) - 1u));
+            const uint32_t ni = ng.x + rel;
+            if (ni >= tv.num_nodes || budget-- == 0u) {
+                atomicOr(tv.status, kStatusBadTree);
+                return false;
+            }
+            if (ng.y & 0xff000000u) {
+                if (sp < kStack) stack[sp++] = ng;
+                else atomicOr(tv.status, kStatusStackOverflow);
+            }
+            uint32_t child_base, tri_base, imask;
+            const uint32_t hm = intersect_node(tv.nodes, ni, R, best_t, child_base, tri_base, imask);
+            ng = make_uint2(child_base, (hm & 0xff000000u) | imask);
+            uint32_t tmask = hm & 0x00ffffffu;
+            while (tmask) {
+                const uint32_t k = __ffs(tmask) - 1u;
+                tmask &= tmask - 1u;
+                if (tri_base + k >= tv.num_tris) {
+                    atomicOr(tv.status, kStatusBadTree);
+                    return false;
+                }
+                float t, b1, b2;
+                int id;
+                if (intersect_tri(tv.tris, tri_base + k, R, best_t, t, b1, b2, id)) {
+                    if (t < best_t || id > best_id) {
+                        best_t = t;
+                        best_id = id;
+                        bb1 = b1;
+                        bb2 = b2;
+                    }
+                    if (anyhit) {
+                        t_out = t; id_out = id; b1_out = b1; b2_out = b2;
+                        return true;
+                    }
+                }
+            }
+        } else if (sp > 0) {
+            ng = stack[--sp];
+        } else {
+            break;
+        }
+    }
+    if (best_id < 0) return false;
+    t_out = best_t;
+    id_out = best_id;
+    b1_out = bb1;
+    b2_out = bb2;
+    return true;
+}
+
+}  // namespace lmgpu

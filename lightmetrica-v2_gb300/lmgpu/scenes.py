@@ -230,3 +230,40 @@ def cornell_materials(width: int = 64, height: int = 64) -> dict:
                      "tris": tall_box["tris"] + lift}
     s["env"] = (0.2, 0.3, 0.5)
     return s
+
+
+def caustic_room(width: int = 1280, height: int = 720, sphere_level: int = 5) -> dict:
+    """Caustic scene of the bidirectional renderer: a closed room of 20
+    triangles facing in (x in [-1, 1], y in [0, 1.5], z in [-1.2, 1]; the
+    floor in 2 x 2 quads, the ceiling in two), a glass icosphere (level
+    `sphere_level`, radius 0.3, eta 1 -> 1.5) standing on the floor, a sphere
+    light of radius 0.05 (level-2 icosphere, facing out) and a thin grey
+    panel (12 triangles) that hides the light from the camera but not from
+    the glass; camera at (0, 0.7, -1.1) looking at (0, 0.3, 0.3), vertical
+    fov 45 degrees."""
+    x0, x1, y0, y1, z0, z1 = -1.0, 1.0, 0.0, 1.5, -1.2, 1.0
+    xm, zm = 0.5 * (x0 + x1), 0.5 * (z0 + z1)
+    floor = np.concatenate([_quad((a0, y0, b0), (a0, y0, b1), (a1, y0, b1), (a1, y0, b0))
+                            for a0, a1 in ((x0, xm), (xm, x1)) for b0, b1 in ((z0, zm), (zm, z1))])
+    ceiling = np.concatenate([_quad((a0, y1, z0), (a1, y1, z0), (a1, y1, z1), (a0, y1, z1))
+                              for a0, a1 in ((x0, xm), (xm, x1))])
+    walls = np.concatenate([
+        _quad((x0, y0, z1), (x0, y1, z1), (x1, y1, z1), (x1, y0, z1)),  # back, -z
+        _quad((x0, y0, z0), (x1, y0, z0), (x1, y1, z0), (x0, y1, z0)),  # front (behind the camera), +z
+        _quad((x0, y0, z0), (x0, y1, z0), (x0, y1, z1), (x0, y0, z1)),  # left, +x
+        _quad((x1, y0, z0), (x1, y0, z1), (x1, y1, z1), (x1, y1, z0)),  # right, -x
+    ])
+    room = np.concatenate([floor, ceiling, walls]).astype(np.float32)
+    assert room.shape[0] == 20
+    sphere = closed_icosphere(sphere_level, 0.3, (0.0, 0.301, 0.2))
+    light = closed_icosphere(2, 0.05, (0.35, 0.95, 0.55))
+    panel = _box((0.5, 0.35, 0.02), 0.0, (0.35, 0.35)) + np.array([0.0, 0.78, 0.0] * 3)
+    prims = [
+        {"bsdf": BSDF_DIFFUSE, "R": (0.75, 0.75, 0.75), "tris": room},
+        {"bsdf": BSDF_DIELECTRIC, "R": (1.0, 1.0, 1.0), "eta1": 1.0, "eta2": 1.5, "tris": sphere},
+        {"bsdf": BSDF_DIFFUSE, "R": (0.5, 0.5, 0.5), "tris": panel.astype(np.float32)},
+        {"bsdf": BSDF_NULL, "light": True, "Le": (400.0, 360.0, 300.0), "tris": light},
+    ]
+    camera = {"eye": (0.0, 0.7, -1.1), "center": (0.0, 0.3, 0.3), "up": (0.0, 1.0, 0.0), "fov": 45.0,
+              "width": width, "height": height}
+    return {"prims": prims, "camera": camera}

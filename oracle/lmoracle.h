@@ -101,6 +101,19 @@ uint64_t lmo_render_pt(const float* tris, const int32_t* tri_prim, size_t ntri, 
                        const lmo_pt_env* env, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
                        uint64_t seed, int threads, double* sum, double* sumsq);
 
+/* ---- renderer::bdpt (lmoracle_bdpt.c): area lights, pinhole, power heuristic ---- */
+uint64_t lmo_render_bdpt(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims, int nprims,
+                         const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices, uint64_t seed,
+                         int threads, double* sum, double* sumsq);
+
+/* As lmo_render_bdpt; independent_light_dir != 0 draws the light subpath's
+ * first direction from its own 2D sample instead of reusing the position's
+ * (the reference's light_area.cpp:73-80 reuses it).  A diagnostic that
+ * isolates the effect of that reuse on the estimate. */
+uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
+                            int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
+                            uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir);
+
 #ifdef __cplusplus
 }
 #endif

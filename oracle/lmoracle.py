@@ -52,6 +52,11 @@ def lib() -> ctypes.CDLL:
         L.lmo_render_pt.argtypes = [vp, vp, sz, vp, vp, vp, ctypes.c_uint64, ctypes.c_int, ctypes.c_uint64,
                                     ctypes.c_int, vp, vp]
         L.lmo_render_pt.restype = ctypes.c_uint64
+        L.lmo_render_bdpt.argtypes = [vp, vp, sz, vp, ctypes.c_int, vp, ctypes.c_uint64, ctypes.c_int, ctypes.c_uint64,
+                                      ctypes.c_int, vp, vp]
+        L.lmo_render_bdpt.restype = ctypes.c_uint64
+        L.lmo_render_bdpt_ex.argtypes = L.lmo_render_bdpt.argtypes + [ctypes.c_int]
+        L.lmo_render_bdpt_ex.restype = ctypes.c_uint64
         _lib = L
     return _lib
 
@@ -171,9 +176,10 @@ def write_render_scene(path: str, scene: dict, num_samples: int, max_num_vertice
 
 
 def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,
-                   double: bool = False) -> dict:
-    """Runs the reference renderer::pt (compiled from its sources) and returns
-    the film (H, W, 3), the per-pixel variance of that estimate and timing."""
+                   double: bool = False, renderer: str = "pt") -> dict:
+    """Runs the reference renderer::pt or renderer::bdpt (compiled from its
+    sources) and returns the film (H, W, 3), the per-pixel variance of that
+    estimate and timing."""
     import json
     import tempfile
 
@@ -183,7 +189,7 @@ def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: i
         ps, po = os.path.join(tmp, "scene.bin"), os.path.join(tmp, "out.bin")
         write_render_scene(ps, scene, num_samples, max_num_vertices, seed, threads)
         exe = REF_RENDER64 if double else REF_RENDER
-        out = subprocess.run([exe, ps, po], capture_output=True, text=True, check=True).stdout
+        out = subprocess.run([exe, ps, po, renderer], capture_output=True, text=True, check=True).stdout
         raw = open(po, "rb").read()
     n = W * H * 3
     img = np.frombuffer(raw[:4 * n], dtype=np.float32).reshape(H, W, 3)
@@ -261,5 +267,23 @@ def render_pt(scene: dict, num_samples: int, max_num_vertices: int, seed: int, t
     lib().lmo_render_pt(tris.ctypes.data, tri_prim.ctypes.data, tris.shape[0], ctypes.addressof(prims),
                         ctypes.addressof(env), ctypes.addressof(cam), num_samples, max_num_vertices, seed, threads,
                         s.ctypes.data, q.ctypes.data)
+    img = s * (W * H / num_samples)
+    return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}
+
+
+def render_bdpt(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,
+                independent_light_dir: bool = False) -> dict:
+    """The oracle's renderer::bdpt (power heuristic): film (H, W, 3) and per-pixel variance.
+    independent_light_dir: the diagnostic variant of lmo_render_bdpt_ex."""
+    tris = np.ascontiguousarray(np.concatenate([p["tris"] for p in scene["prims"]]), dtype=np.float32)
+    tri_prim = np.concatenate([np.full(p["tris"].shape[0], i, np.int32) for i, p in enumerate(scene["prims"])])
+    W, H = scene["camera"]["width"], scene["camera"]["height"]
+    s = np.zeros((H, W, 3), np.float64)
+    q = np.zeros((H, W, 3), np.float64)
+    prims = scene_prims(scene)
+    cam = scene_camera(scene)
+    lib().lmo_render_bdpt_ex(tris.ctypes.data, tri_prim.ctypes.data, tris.shape[0], ctypes.addressof(prims),
+                             len(scene["prims"]), ctypes.addressof(cam), num_samples, max_num_vertices, seed,
+                             threads, s.ctypes.data, q.ctypes.data, 1 if independent_light_dir else 0)
     img = s * (W * H / num_samples)
     return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}

@@ -9,8 +9,10 @@
 //   HarnessProp       PropertyNode over an in-memory map (property.h:47-215)
 //   HarnessAssets     Assets::AssetByIDAndType for the film only (assets.h:88)
 //   HarnessFilm       Film_HDR::Splat/Accumulate/Rescale/Clear
-//                     (film_hdr.cpp:218-305); additionally sums the squared
-//                     splat values per pixel, which the oracle needs for
+//                     (film_hdr.cpp:218-305); additionally sums, per pixel,
+//                     the square of each sample's total contribution there
+//                     (a sample's splats are merged by pixel when the
+//                     scheduler finishes it), which the oracle needs for
 //                     per-pixel variance
 //   HarnessScheduler  Scheduler_::Process (scheduler.cpp:78-295) with
 //                     std::thread: each worker seeds its Random from
@@ -28,7 +30,7 @@
 //                     environment hit; the harness sets it to the environment
 //                     light's primitive, as a fixed scene would.
 //
-// Usage: ref_render <scene.bin> <out.bin>
+// Usage: ref_render <scene.bin> <out.bin> [pt|bdpt]   (renderer::pt by default)
 //   scene.bin: u32 magic 'LMRS', u32 version 2, u32 W, H,
 //              f32 eye[3], center[3], up[3], fov_deg,
 //              u32 nprims, per primitive: i32 bsdf (0 null, 1 diffuse,
@@ -113,7 +115,7 @@ public:
         const int pY = Math::Clamp((int)(rasterPos.y * Float(height)), 0, height - 1);
         const Vec3 c = v.ToRGB();
         data[pY * width + pX] += c;
-        for (int k = 0; k < 3; k++) sumsq[3 * (pY * width + pX) + k] += (double)c[k] * (double)c[k];
+        pending.push_back({ pY * width + pX, { (double)c[0], (double)c[1], (double)c[2] } });
     };
     LM_IMPL_F(Save) = [this](const std::string&) -> bool { return true; };
     LM_IMPL_F(Accumulate) = [this](const Film* f_) -> void
@@ -130,9 +132,28 @@ public:
     };
 public:
     void Resize(int w, int h) { width = w; height = h; data.assign((size_t)w * h, Vec3()); sumsq.assign((size_t)w * h * 3, 0.0); }
+    // Called after every sample: squares of the sample's per-pixel totals.
+    void EndSample()
+    {
+        for (size_t i = 0; i < pending.size(); i++)
+        {
+            if (pending[i].pixel < 0) continue;
+            double c[3] = { pending[i].c[0], pending[i].c[1], pending[i].c[2] };
+            for (size_t j = i + 1; j < pending.size(); j++)
+            {
+                if (pending[j].pixel != pending[i].pixel) continue;
+                for (int k = 0; k < 3; k++) c[k] += pending[j].c[k];
+                pending[j].pixel = -1;
+            }
+            for (int k = 0; k < 3; k++) sumsq[3 * (size_t)pending[i].pixel + k] += c[k] * c[k];
+        }
+        pending.clear();
+    }
+    struct Pending { int pixel; double c[3]; };
     int width = 0, height = 0;
     std::vector<Vec3> data;
     std::vector<double> sumsq;
+    std::vector<Pending> pending;
 };
 
 class HarnessAssets : public Assets
@@ -174,7 +195,7 @@ public:
         for (int t = 0; t < T; t++)
         {
             const long long b = numSamples * t / T, e = numSamples * (t + 1) / T;
-            ts.emplace_back([&, t, b, e]() { for (long long s = b; s < e; s++) func(films[t].get(), rngs[t].get()); });
+            ts.emplace_back([&, t, b, e]() { for (long long s = b; s < e; s++) { func(films[t].get(), rngs[t].get()); films[t]->EndSample(); } });
         }
         for (auto& th : ts) th.join();
         film->Clear();
@@ -284,7 +305,8 @@ static std::string Vec3Str(const float* v)
 
 int main(int argc, char** argv)
 {
-    if (argc < 3) { std::fprintf(stderr, "usage: %s scene.bin out.bin\n", argv[0]); return 2; }
+    if (argc < 3) { std::fprintf(stderr, "usage: %s scene.bin out.bin [pt|bdpt]\n", argv[0]); return 2; }
+    const std::string rendererKey = std::string("renderer::") + (argc > 3 ? argv[3] : "pt");
     std::vector<char> buf;
     {
         FILE* f = std::fopen(argv[1], "rb");
@@ -454,7 +476,8 @@ int main(int argc, char** argv)
     if (!accel || !accel->Initialize(nullptr) || !accel->Build(&scene)) return 4;
     scene.accel = accel.get();
 
-    auto renderer = ComponentFactory::Create<Renderer>("renderer::pt");
+    auto renderer = ComponentFactory::Create<Renderer>(rendererKey);
+    if (!renderer) { std::fprintf(stderr, "unknown renderer %s\n", rendererKey.c_str()); return 5; }
     HarnessProp rprop;
     rprop.Set("num_samples", std::to_string(numSamples)).Set("max_num_vertices", std::to_string(maxNumVertices));
     if (!renderer->Initialize(&rprop)) return 5;
@@ -472,8 +495,8 @@ int main(int argc, char** argv)
     std::fwrite(film.sumsq.data(), sizeof(double), film.sumsq.size(), f);
     std::fwrite(&numSamples, sizeof(uint64_t), 1, f);
     std::fclose(f);
-    std::printf("{\"renderer\": \"renderer::pt\", \"accel\": \"%s\", \"samples\": %llu, \"threads\": %d, \"render_s\": %.6f, \"float_bytes\": %d}\n",
-                accelKey, (unsigned long long)numSamples, g_threads,
+    std::printf("{\"renderer\": \"%s\", \"accel\": \"%s\", \"samples\": %llu, \"threads\": %d, \"render_s\": %.6f, \"float_bytes\": %d}\n",
+                rendererKey.c_str(), accelKey, (unsigned long long)numSamples, g_threads,
                 std::chrono::duration<double>(t1 - t0).count(), (int)sizeof(Float));
     return 0;
 }

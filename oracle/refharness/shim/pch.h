@@ -25,4 +25,5 @@
 #include <tuple>
 #include <numeric>
 #include <algorithm>
+#include <boost/optional.hpp>
 #include <lightmetrica/macros.h>

@@ -3,7 +3,7 @@
 Run in a checkout that has the reference tree (default /root/reference) and
 the reference harness built by oracle/build_ref.sh (oracle/_ref/ref_accel):
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py [REFERENCE_ROOT] [--only NAME[,NAME...]]
 
 Fixtures written:
   accel3_simple.npz, accel3_simple2.npz
@@ -21,6 +21,11 @@ Fixtures written:
       The same box with a glass box (bsdf::flesnel), a GGX conductor box
       (bsdf::cook_torrance) and a constant environment light (light::env),
       reference films likewise.
+  cornell_bdpt.npz, materials_bdpt.npz
+      The same two boxes (the materials box without the environment light,
+      which renderer::bdpt does not sample) rendered by the reference's own
+      renderer::bdpt at 32x32 with max_num_vertices 10: films and
+      per-pixel variances in single and double precision.
   soup_small.npz
       A seeded three-primitive scene (random triangle soup, heightfield,
       duplicated triangles for exact-t ties, zero-area triangles) and rays
@@ -186,30 +191,53 @@ def scene_arrays(sc: dict) -> dict:
     return out
 
 
-def pt_case(sc: dict, spp: int, seed: int) -> dict:
+def pt_case(sc: dict, spp: int, seed: int, renderer: str = "pt", max_num_vertices: int = 9) -> dict:
     W, H = sc["camera"]["width"], sc["camera"]["height"]
     N = W * H * spp
-    f = lo.run_ref_render(sc, N, 9, seed, os.cpu_count() or 8)
-    d = lo.run_ref_render(sc, N, 9, seed + 1, os.cpu_count() or 8, double=True)
+    f = lo.run_ref_render(sc, N, max_num_vertices, seed, os.cpu_count() or 8, renderer=renderer)
+    d = lo.run_ref_render(sc, N, max_num_vertices, seed + 1, os.cpu_count() or 8, double=True, renderer=renderer)
     out = scene_arrays(sc)
-    out.update({"num_samples": np.int64(N), "max_num_vertices": np.int32(9),
+    out.update({"num_samples": np.int64(N), "max_num_vertices": np.int32(max_num_vertices),
                 "ref_image": f["image"].astype(np.float32), "ref_variance": f["variance"].astype(np.float32),
                 "ref64_image": d["image"].astype(np.float64), "ref64_variance": d["variance"].astype(np.float64)})
     return out
 
 
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = sys.argv[1:]
+    only = None
+    if "--only" in args:
+        i = args.index("--only")
+        only = set(args[i + 1].split(","))
+        del args[i:i + 2]
+    ref = args[0] if args else "/root/reference"
+    want = lambda name: only is None or name in only  # noqa: E731
     if not (os.path.exists(lo.REF_ACCEL) and os.path.exists(lo.REF_RENDER) and os.path.exists(lo.REF_RENDER64)):
         subprocess.run([os.path.join(REPO, "oracle", "build_ref.sh"), ref], check=True)
     src = open(os.path.join(ref, "src", "lightmetrica-test", "test_accel3.cpp")).read()
     with tempfile.TemporaryDirectory() as tmp:
-        np.savez_compressed(os.path.join(HERE, "accel3_simple.npz"), **accel3_case(src, "StubTriangleMesh_Simple", False, tmp))
-        np.savez_compressed(os.path.join(HERE, "accel3_simple2.npz"), **accel3_case(src, "StubTriangleMesh_Simple2", True, tmp))
-        np.savez_compressed(os.path.join(HERE, "soup_small.npz"), **soup_case(tmp))
-    np.savez_compressed(os.path.join(HERE, "cornell_pt.npz"), **pt_case(scenes.cornell_box(64, 64), 16384, 20240601))
-    np.savez_compressed(os.path.join(HERE, "materials_pt.npz"),
-                        **pt_case(scenes.cornell_materials(64, 64), 16384, 20240701))
+        if want("accel3_simple"):
+            np.savez_compressed(os.path.join(HERE, "accel3_simple.npz"),
+                                **accel3_case(src, "StubTriangleMesh_Simple", False, tmp))
+        if want("accel3_simple2"):
+            np.savez_compressed(os.path.join(HERE, "accel3_simple2.npz"),
+                                **accel3_case(src, "StubTriangleMesh_Simple2", True, tmp))
+        if want("soup_small"):
+            np.savez_compressed(os.path.join(HERE, "soup_small.npz"), **soup_case(tmp))
+    if want("cornell_pt"):
+        np.savez_compressed(os.path.join(HERE, "cornell_pt.npz"),
+                            **pt_case(scenes.cornell_box(64, 64), 16384, 20240601))
+    if want("materials_pt"):
+        np.savez_compressed(os.path.join(HERE, "materials_pt.npz"),
+                            **pt_case(scenes.cornell_materials(64, 64), 16384, 20240701))
+    if want("cornell_bdpt"):
+        np.savez_compressed(os.path.join(HERE, "cornell_bdpt.npz"),
+                            **pt_case(scenes.cornell_box(32, 32), 32768, 20240801, "bdpt", 10))
+    if want("materials_bdpt"):
+        sc = scenes.cornell_materials(32, 32)
+        sc.pop("env", None)
+        np.savez_compressed(os.path.join(HERE, "materials_bdpt.npz"),
+                            **pt_case(sc, 32768, 20240901, "bdpt", 10))
     print("fixtures written to", HERE)
 
 
