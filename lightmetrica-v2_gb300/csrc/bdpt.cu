@@ -15,22 +15,37 @@
 //     position (light_area.cpp:73-80) and the pinhole is a delta position, so
 //     t = 0 strategies carry no weight -- both kept as the reference has them.
 //
-// GPU structure: one thread per sample, the two subpaths in per-thread local
-// arrays (at most kMaxV vertices each), rays traced with the per-thread
-// traversal of traverse.cuh.  Contributions that land in the sample's own
-// pixel are summed in registers and splatted once; others (light-to-camera
-// connections) are splatted where they land.  Eye subpaths start from
-// per-pixel stratified raster positions; random numbers are Philox keyed by
-// (seed, sample).
+// GPU structure (wavefront), per wave of up to kWaveSamples samples:
+//   k_bd_start     vertex 0 of every light and eye subpath, and the rays of
+//                  step 1: the extension ray and the ray to the "direct"
+//                  endpoint candidate;
+//   per step k     closest-hit traversal of the extension rays and any-hit
+//                  traversal of the direct rays (trace.cu, persistent), then
+//                  k_bd_step: store the step's vertex, roulette, sample the
+//                  rays of step k + 1 for the surviving subpaths (compacted);
+//   k_bd_count     per sample: the s = 0 strategies (no ray needed) and the
+//                  number of s, t >= 1 connections, whose work items
+//                  k_bd_items lays out contiguously per sample;
+//   k_bd_connect   one thread per connection: contribution (unweighted
+//                  estimate, MIS weight, selection pdf) and its shadow ray;
+//                  any-hit traversal of all shadow rays; k_bd_splat adds the
+//                  unoccluded ones; k_bd_flush merges each sample's
+//                  own-pixel contributions into the film (the reference film
+//                  squares per-sample sums, so the variance estimate does too).
+// Subpath vertices live in HBM as 32-byte records, [vertex k][sample], so
+// the kernels of one step read and write them coalesced.  Eye subpaths start
+// at per-pixel stratified raster positions; random numbers are Philox keyed
+// by (seed, sample, subpath, step), so every kernel draws its own without
+// carried state.
 #include "bsdf.cuh"
 #include "rng.cuh"
 #include "scene.cuh"
-#include "traverse.cuh"
 
 namespace lmgpu {
 namespace {
 
 constexpr int kMaxV = 16;
+constexpr uint64_t kWaveSamples = 1ull << 19;
 constexpr int kBdptThreads = 128;
 constexpr uint32_t kKeyBdpt = 0x42445054u;
 
@@ -45,32 +60,10 @@ struct PV {  // 32 bytes
     short degen;
 };
 
-struct SV {
-    PV sv, direct;
-    int has_sv, has_direct;
-};
-
-struct Rng {
-    uint32_t c0, c1, seed, ctr;
-    float buf[4];
-    int left;
-};
-
-__device__ __forceinline__ float rnd(Rng& r)
-{
-    if (r.left == 0) {
-        const Philox4x32 x = philox4x32_10(r.c0, r.c1, r.ctr++, 0u, r.seed, kKeyBdpt);
-        for (int k = 0; k < 4; k++) r.buf[k] = u01(x.v[k]);
-        r.left = 4;
-    }
-    return r.buf[--r.left];
-}
-
 struct Ctx {
     SceneGPU sc;
     LightsGPU lights;
     CameraGPU cam;
-    TraceView tv;
     int max_v;     // subpath vertices, at most kMaxV
     int max_path;  // full-path vertices (the reference's max_num_vertices; -1 = unbounded)
 };
@@ -251,39 +244,6 @@ __device__ __forceinline__ void sensor_vertex(const Ctx& C, PV& v)
     v.degen = 1;
 }
 
-// One out-of-line copy of the traversal for every ray the kernel traces.
-__device__ __noinline__ bool trace_one(const TraceView& tv, float3 o, float tmin, float3 d, float tmax, bool anyhit,
-                                       float& t, int& id, float& b1, float& b2)
-{
-    return trace_single(tv, o, tmin, d, tmax, anyhit, t, id, b1, b2);
-}
-
-__device__ __noinline__ bool trace_vertex(const Ctx& C, float3 o, float3 d, PV& v)
-{
-    float t, b1, b2;
-    int id;
-    if (!trace_one(C.tv, o, 1e-4f, d, FLT_MAX, false, t, id, b1, b2)) return false;
-    const float* T = C.sc.tris + 9 * (size_t)id;
-    const float3 p1 = f3(T[0], T[1], T[2]), p2 = f3(T[3], T[4], T[5]), p3 = f3(T[6], T[7], T[8]);
-    v.p = o + d * t;
-    v.n = normalize3(cross3(p2 - p1, p3 - p1));
-    v.prim = C.sc.tri_prim[id];
-    v.type = bsdf_type(C.sc.prims[v.prim].bsdf);
-    v.degen = 0;
-    return true;
-}
-
-// Scene3::Visible (scene3.h:107-116): [EpsIsect, L (1 - EpsIsect)]
-__device__ __noinline__ bool visible(const Ctx& C, float3 a, float3 b)
-{
-    float3 d = b - a;
-    const float L = sqrtf(dot3(d, d));
-    d = d * (1.0f / L);
-    float t, b1, b2;
-    int id;
-    return !trace_one(C.tv, a, 1e-4f, d, L * (1.0f - 1e-4f), true, t, id, b1, b2);
-}
-
 // BSDF SampleDirection; false where the reference leaves wo unset.
 __device__ __noinline__ bool sample_dir(const Ctx& C, const PV& v, float3 wi, float u0, float u1, float uc, float3& wo)
 {
@@ -317,95 +277,6 @@ __device__ __noinline__ bool sample_dir(const Ctx& C, const PV& v, float3 wi, fl
     }
     wo = b * lwo.x + c * lwo.y + v.n * lwo.z;
     return true;
-}
-
-// Subpath::Sample (renderer_bdpt.cpp:80-220).  For the eye subpath the first
-// direction comes from the stratified raster position (rx0, ry0).
-__device__ __noinline__ int sample_subpath(const Ctx& C, Rng& rng, int dir, float rx0, float ry0, SV* out)
-{
-    int n = 0;
-    float3 initWo = zero3();
-    for (int step = 0; step < C.max_v; step++) {
-        if (step == 0) {
-            PV v;
-            if (dir == DIR_LE) {
-                const float us = rnd(rng), a0 = rnd(rng), a1 = rnd(rng);
-                sample_light(C, us, a0, a1, v);
-                // direction from the same 2D sample as the position (light_area.cpp:73-80)
-                const float3 l = cosine_hemisphere(a0, a1);
-                float3 b, c;
-                basis(v.n, b, c);
-                initWo = b * l.x + c * l.y + v.n * l.z;
-            } else {
-                sensor_vertex(C, v);
-                initWo = camera_dir(C.cam, rx0, ry0);
-            }
-            out[n].sv = v;
-            out[n].has_sv = 1;
-            out[n].has_direct = 0;
-            n++;
-            continue;
-        }
-        const PV pv = out[n - 1].sv;
-        SV nv;
-        nv.has_sv = 0;
-        nv.has_direct = 0;
-        {
-            const float3 wi = n > 1 ? dirto(pv, out[n - 2].sv) : zero3();
-            const float u0 = rnd(rng), u1 = rnd(rng), uc = rnd(rng);
-            float3 wo = zero3();
-            bool ok = true;
-            if (step == 1) wo = initWo;
-            else ok = sample_dir(C, pv, wi, u0, u1, uc, wo);
-            if (ok && !black(eval_dir(C, pv, pv.type, wi, wo, dir, false)) && trace_vertex(C, pv.p, wo, nv.sv))
-                nv.has_sv = 1;
-        }
-        {
-            const float us = rnd(rng), a0 = rnd(rng), a1 = rnd(rng);
-            PV v;
-            if (dir == DIR_LE) sensor_vertex(C, v);
-            else sample_light(C, us, a0, a1, v);
-            if (visible(C, pv.p, v.p)) {
-                nv.direct = v;
-                nv.has_direct = 1;
-            }
-        }
-        if (nv.has_sv || nv.has_direct) out[n++] = nv;
-        if (!nv.has_sv) break;
-        if (rnd(rng) > 0.5f) break;
-    }
-    return n;
-}
-
-// Path::Connect (renderer_bdpt.cpp:233-333)
-__device__ __noinline__ int connect(const Ctx& C, int s, int t, bool direct, const SV* L, const SV* E, PV* P)
-{
-    int n = 0;
-    if (s == 0 && t > 0) {
-        if (!direct) {
-            if (!E[t - 1].has_sv) return 0;
-            const int pr = E[t - 1].sv.prim;
-            if (pr < 0 || !C.sc.prims[pr].is_light) return 0;
-            for (int i = t - 1; i >= 0; i--) P[n++] = E[i].sv;
-        } else {
-            if (!E[t - 1].has_direct) return 0;
-            P[n++] = E[t - 1].direct;
-            for (int i = t - 2; i >= 0; i--) P[n++] = E[i].sv;
-        }
-        P[0].type = T_L;
-    } else if (s > 0 && t == 0) {
-        if (!direct) return 0;  // a light subpath vertex is never the pinhole
-        if (!L[s - 1].has_direct) return 0;
-        for (int i = 0; i < s - 1; i++) P[n++] = L[i].sv;
-        P[n++] = L[s - 1].direct;
-        P[n - 1].type = T_E;
-    } else {
-        if (!L[s - 1].has_sv || !E[t - 1].has_sv) return 0;
-        if (!visible(C, L[s - 1].sv.p, E[t - 1].sv.p)) return 0;
-        for (int i = 0; i < s; i++) P[n++] = L[i].sv;
-        for (int i = t - 1; i >= 0; i--) P[n++] = E[i].sv;
-    }
-    return n;
 }
 
 // EvaluateUnweightContribution (:489-591) with EvaluateCst (:375-406).
@@ -519,6 +390,247 @@ __device__ __noinline__ float mis_weight(const Ctx& C, const PV* P, int n, int s
     return 1.0f / inv;
 }
 
+
+// ---- wave storage --------------------------------------------------------
+
+// A stored subpath vertex: position and primitive, normal and type bits.
+struct __align__(16) BVtx {
+    float4 a;  // p, prim (int bits)
+    float4 b;  // n, type | degen << 8 | F_SV | F_DIRECT (bits)
+};
+constexpr uint32_t F_SV = 1u << 16;      // the step stored a BSDF-sampled vertex
+constexpr uint32_t F_DIRECT = 1u << 17;  // the step's direct endpoint was visible
+
+__device__ __forceinline__ BVtx pack(const PV& v, uint32_t flags)
+{
+    BVtx r;
+    r.a = make_float4(v.p.x, v.p.y, v.p.z, __int_as_float(v.prim));
+    r.b = make_float4(v.n.x, v.n.y, v.n.z,
+                      __uint_as_float(((uint32_t)v.type & 0xffu) | (((uint32_t)v.degen & 0xffu) << 8) | flags));
+    return r;
+}
+
+__device__ __forceinline__ PV unpack(const BVtx& r)
+{
+    PV v;
+    v.p = f3(r.a.x, r.a.y, r.a.z);
+    v.n = f3(r.b.x, r.b.y, r.b.z);
+    v.prim = __float_as_int(r.a.w);
+    const uint32_t w = __float_as_uint(r.b.w);
+    v.type = (short)(w & 0xffu);
+    v.degen = (short)((w >> 8) & 0xffu);
+    return v;
+}
+
+__device__ __forceinline__ uint32_t flags_of(const BVtx& r) { return __float_as_uint(r.b.w) & (F_SV | F_DIRECT); }
+
+// Device view of one wave.  Slot j in [0, 2n) is subpath j / n (0 light,
+// 1 eye) of sample j % n; vertex k of subpath d of sample i is at
+// sv[d][k * stride + i] (BSDF-sampled) and dv[d][k * stride + i] (direct).
+struct Wave {
+    uint64_t p0;       // global index of the wave's first sample
+    uint32_t n;        // samples in the wave
+    uint32_t stride;   // sample capacity of the vertex arrays
+    uint32_t npix;
+    uint32_t seed;
+    BVtx* sv[2];
+    BVtx* dv[2];
+    int32_t* count[2];  // vertices stored per subpath
+    BVtx* pend;         // [slot] the direct endpoint candidate of the current step
+    float* own;         // [3 i] sample i's contributions to its own pixel
+};
+
+// The random numbers of step k of subpath `dir` of sample p: extension
+// direction (u0, u1, uc), direct endpoint (us, a0, a1), roulette (rr).
+struct StepRand {
+    float u0, u1, uc, us, a0, a1, rr;
+};
+
+__device__ __forceinline__ StepRand step_rand(uint64_t p, int dir, int k, uint32_t seed)
+{
+    const uint32_t c2 = ((uint32_t)dir << 8) | (uint32_t)k;
+    const Philox4x32 A = philox4x32_10((uint32_t)p, (uint32_t)(p >> 32), c2, 0u, seed, kKeyBdpt);
+    const Philox4x32 B = philox4x32_10((uint32_t)p, (uint32_t)(p >> 32), c2, 1u, seed, kKeyBdpt);
+    return StepRand{u01(A.v[0]), u01(A.v[1]), u01(A.v[2]), u01(A.v[3]), u01(B.v[0]), u01(B.v[1]), u01(B.v[2])};
+}
+
+__device__ __forceinline__ void store_ray(float4* rays, uint32_t q, float3 o, float tmin, float3 d, float tmax)
+{
+    rays[2 * q] = make_float4(o.x, o.y, o.z, tmin);
+    rays[2 * q + 1] = make_float4(d.x, d.y, d.z, tmax);
+}
+
+// A ray that meets nothing (empty [tmin, tmax]).
+__device__ __forceinline__ void store_null_ray(float4* rays, uint32_t q)
+{
+    rays[2 * q] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    rays[2 * q + 1] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+}
+
+// Scene3::Visible (scene3.h:107-116) as a ray: [EpsIsect, L (1 - EpsIsect)].
+__device__ __forceinline__ void store_shadow_ray(float4* rays, uint32_t q, float3 a, float3 b)
+{
+    float3 d = b - a;
+    const float L = sqrtf(dot3(d, d));
+    d = d * (1.0f / L);
+    store_ray(rays, q, a, 1e-4f, d, L * (1.0f - 1e-4f));
+}
+
+// The rays of step k from vertex v (Subpath::Sample, renderer_bdpt.cpp:130-200):
+// the extension ray along wo (null if the direction was not sampled or its
+// BSDF value is black) and the ray to the direct endpoint, drawn with step
+// k's random numbers; the endpoint is kept in pend[slot].
+__device__ __forceinline__ void emit_step(const Ctx& C, const Wave& w, int dir, uint32_t slot, const PV& v, bool has_wo,
+                                          float3 wo, const StepRand& r, uint32_t q, float4* ext, float4* sh)
+{
+    if (has_wo) store_ray(ext, q, v.p, 1e-4f, wo, FLT_MAX);
+    else store_null_ray(ext, q);
+    PV e;
+    if (dir == DIR_LE) sensor_vertex(C, e);
+    else sample_light(C, r.us, r.a0, r.a1, e);
+    store_shadow_ray(sh, q, v.p, e.p);
+    w.pend[slot] = pack(e, 0u);
+}
+
+__global__ void __launch_bounds__(kBdptThreads) k_bd_start(Ctx C, Wave w, float4* __restrict__ ext,
+                                                           float4* __restrict__ sh, uint32_t* __restrict__ active)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= 2 * w.n) return;
+    const int dir = j >= w.n ? DIR_EL : DIR_LE;
+    const uint32_t i = dir == DIR_EL ? j - w.n : j;
+    const uint64_t p = w.p0 + i;
+    const StepRand r0 = step_rand(p, dir, 0, w.seed);
+    PV v;
+    float3 wo;
+    bool has_wo;
+    if (dir == DIR_LE) {
+        sample_light(C, r0.us, r0.a0, r0.a1, v);
+        // emission direction from the same 2D sample as the position (light_area.cpp:73-80)
+        const float3 l = cosine_hemisphere(r0.a0, r0.a1);
+        float3 b, c;
+        basis(v.n, b, c);
+        wo = b * l.x + c * l.y + v.n * l.z;
+        has_wo = !black(eval_dir(C, v, T_L, zero3(), wo, DIR_LE, false));
+    } else {
+        sensor_vertex(C, v);
+        const uint32_t W = (uint32_t)C.cam.width, H = (uint32_t)C.cam.height;
+        const uint32_t pixel = (uint32_t)(p % w.npix);
+        wo = camera_dir(C.cam, ((float)(pixel % W) + r0.u0) / (float)W, ((float)(pixel / W) + r0.u1) / (float)H);
+        has_wo = importance(C.cam, wo) > 0.0f;
+    }
+    w.sv[dir][i] = pack(v, F_SV);
+    w.count[dir][i] = 1;
+    active[j] = j;
+    emit_step(C, w, dir, j, v, has_wo, wo, step_rand(p, dir, 1, w.seed), j, ext, sh);
+}
+
+// Step k of the active subpaths: hits of the extension and direct rays in,
+// the vertex stored, roulette, the rays of step k + 1 out (compacted).
+__global__ void __launch_bounds__(kBdptThreads) k_bd_step(Ctx C, Wave w, int k, uint32_t n_active,
+                                                          const uint32_t* __restrict__ active_in,
+                                                          const float4* __restrict__ ext_in,
+                                                          const lmgpu_hit* __restrict__ ext_hit,
+                                                          const lmgpu_hit* __restrict__ sh_hit,
+                                                          uint32_t* __restrict__ active_out,
+                                                          uint32_t* __restrict__ n_out, float4* __restrict__ ext_out,
+                                                          float4* __restrict__ sh_out)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    bool keep = false;
+    uint32_t j = 0;
+    int dir = 0;
+    PV nv;
+    float3 wo = zero3();
+    bool has_wo = false;
+    StepRand rn{};
+    if (q < n_active) {
+        j = active_in[q];
+        dir = j >= w.n ? DIR_EL : DIR_LE;
+        const uint32_t i = dir == DIR_EL ? j - w.n : j;
+        const uint64_t p = w.p0 + i;
+        const int n = w.count[dir][i];
+        const lmgpu_hit he = ext_hit[q];
+        const bool has_sv = he.prim >= 0;
+        const bool has_direct = sh_hit[q].prim < 0;
+        if (has_sv) {
+            const float4 r0 = ext_in[2 * q], r1 = ext_in[2 * q + 1];
+            const float* T = C.sc.tris + 9 * (size_t)he.prim;
+            const float3 p1 = f3(T[0], T[1], T[2]), p2 = f3(T[3], T[4], T[5]), p3 = f3(T[6], T[7], T[8]);
+            nv.p = f3(r0.x, r0.y, r0.z) + f3(r1.x, r1.y, r1.z) * he.t;
+            nv.n = normalize3(cross3(p2 - p1, p3 - p1));
+            nv.prim = C.sc.tri_prim[he.prim];
+            nv.type = (short)bsdf_type(C.sc.prims[nv.prim].bsdf);
+            nv.degen = 0;
+        } else {
+            nv.p = zero3();
+            nv.n = zero3();
+            nv.prim = -1;
+            nv.type = 0;
+            nv.degen = 0;
+        }
+        if (has_sv || has_direct) {
+            const size_t at = (size_t)n * w.stride + i;
+            w.sv[dir][at] = pack(nv, (has_sv ? F_SV : 0u) | (has_direct ? F_DIRECT : 0u));
+            if (has_direct) w.dv[dir][at] = w.pend[j];
+            w.count[dir][i] = n + 1;
+        }
+        // roulette 0.5 after the step (renderer_bdpt.cpp:205-213); the step
+        // loop ends after max_num_vertices steps
+        keep = has_sv && step_rand(p, dir, k, w.seed).rr <= 0.5f && n + 1 < C.max_v;
+        if (keep) {
+            rn = step_rand(p, dir, k + 1, w.seed);
+            const PV pv = unpack(w.sv[dir][(size_t)(n - 1) * w.stride + i]);
+            const float3 wi = dirto(nv, pv);
+            has_wo = sample_dir(C, nv, wi, rn.u0, rn.u1, rn.uc, wo) &&
+                     !black(eval_dir(C, nv, nv.type, wi, wo, dir, false));
+        }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (m == 0u) return;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned leader = __ffs(m) - 1u;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(n_out, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (keep) {
+        const uint32_t o = base + __popc(m & ((1u << lane) - 1u));
+        active_out[o] = j;
+        emit_step(C, w, dir, j, nv, has_wo, wo, rn, o, ext_out, sh_out);
+    }
+}
+
+__device__ __forceinline__ uint32_t raster_pixel(const Ctx& C, const PV* P, int n)
+{
+    float rx = 0.0f, ry = 0.0f;
+    raster_pos(C.cam, dirto(P[n - 1], P[n - 2]), rx, ry);
+    const int W = C.cam.width, H = C.cam.height;
+    int ix = (int)(rx * (float)W), iy = (int)(ry * (float)H);
+    ix = ix < 0 ? 0 : (ix > W - 1 ? W - 1 : ix);
+    iy = iy < 0 ? 0 : (iy > H - 1 ? H - 1 : iy);
+    return (uint32_t)iy * (uint32_t)W + (uint32_t)ix;
+}
+
+// Contribution of one full path: unweighted estimate x MIS weight /
+// SelectionPDF (renderer_bdpt.cpp:348-368, :938-947); false if black.
+__device__ __forceinline__ bool path_contribution(const Ctx& C, const PV* P, int n, int s, bool d, float c[3])
+{
+    const Spd cs = unweighted(C, P, n, s, d);
+    if (black(cs)) return false;
+    const float wgt = mis_weight(C, P, n, s, d);
+    if (!(wgt == wgt)) return false;
+    const int t = n - s;
+    float sel = 1.0f;
+    for (int q = 1; q < s - 1; q++) sel *= 0.5f;
+    for (int q = 1; q < t - 1; q++) sel *= 0.5f;
+    bool any = false;
+    for (int k = 0; k < 3; k++) {
+        c[k] = cs.c[k] * wgt / sel;
+        any = any || (c[k] != 0.0f && c[k] == c[k]);
+    }
+    return any;
+}
+
 __device__ __forceinline__ void splat_px(double* film, double* film_sq, uint32_t pix, const float c[3])
 {
     for (int k = 0; k < 3; k++) {
@@ -529,68 +641,210 @@ __device__ __forceinline__ void splat_px(double* film, double* film_sq, uint32_t
     }
 }
 
-__global__ void __launch_bounds__(kBdptThreads) k_bdpt(Ctx C, uint64_t p0, uint32_t count, uint32_t seed,
-                                                       double* __restrict__ film, double* __restrict__ film_sq,
-                                                       double* __restrict__ film_x, double* __restrict__ film_x_sq)
+__device__ __forceinline__ int num_connections(int nL, int nE, int max_path)
+{
+    int c = 0;
+    for (int s = 1; s <= nL; s++) {
+        int t = nE;
+        if (max_path >= 0 && t > max_path - s) t = max_path - s;
+        c += t > 0 ? t : 0;
+    }
+    return c;
+}
+
+// Per sample: the strategies with s = 0 (the eye subpath reaches a light, or
+// its direct vertex is a light; Path::Connect, :245-275) need no further ray
+// and are evaluated here; the s, t >= 1 connections are counted and given a
+// contiguous range of work items.  t = 0 strategies carry no weight with a
+// pinhole sensor (its position cannot be hit and EvaluateCst is 0).
+__global__ void __launch_bounds__(kBdptThreads) k_bd_count(Ctx C, Wave w, uint32_t* __restrict__ base,
+                                                           uint32_t* __restrict__ total,
+                                                           double* __restrict__ film_x,
+                                                           double* __restrict__ film_x_sq)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    const uint64_t p = p0 + i;
-    const uint32_t W = (uint32_t)C.cam.width, H = (uint32_t)C.cam.height;
-    const uint32_t pixel = (uint32_t)(p % ((uint64_t)W * H));
-    Rng rng;
-    rng.c0 = (uint32_t)p;
-    rng.c1 = (uint32_t)(p >> 32);
-    rng.seed = seed;
-    rng.ctr = 0;
-    rng.left = 0;
-    const float rx0 = ((float)(pixel % W) + rnd(rng)) / (float)W;
-    const float ry0 = ((float)(pixel / W) + rnd(rng)) / (float)H;
-    SV L[kMaxV], E[kMaxV];
-    PV P[2 * kMaxV];
-    const int nL = sample_subpath(C, rng, DIR_LE, 0.0f, 0.0f, L);
-    const int nE = sample_subpath(C, rng, DIR_EL, rx0, ry0, E);
-    float own[3] = {0.0f, 0.0f, 0.0f};
-    for (int n = 2; n <= nE + nL; n++) {
-        if (C.max_path >= 0 && n > C.max_path) continue;
-        const int minS = n - nE > 0 ? n - nE : 0;
-        const int maxS = nL < n ? nL : n;
-        for (int s = minS; s <= maxS; s++)
+    uint32_t cnt = 0;
+    if (i < w.n) {
+        const int nL = w.count[0][i], nE = w.count[1][i];
+        cnt = (uint32_t)num_connections(nL, nE, C.max_path);
+        const uint32_t own_pix = (uint32_t)((w.p0 + i) % w.npix);
+        float own[3] = {0.0f, 0.0f, 0.0f};
+        PV P[kMaxV];
+        for (int t = 2; t <= nE; t++) {
+            if (C.max_path >= 0 && t > C.max_path) break;
+            const BVtx last = w.sv[1][(size_t)(t - 1) * w.stride + i];
             for (int d = 0; d < 2; d++) {
-                const int t = n - s;
-                if (s > 0 && t > 0 && d) continue;
-                const int np = connect(C, s, t, d != 0, L, E, P);
-                if (!np) continue;
-                const Spd cs = unweighted(C, P, np, s, d != 0);
-                if (black(cs)) continue;
-                const float w = mis_weight(C, P, np, s, d != 0);
-                float sel = 1.0f;
-                for (int q = 1; q < s - 1; q++) sel *= 0.5f;
-                for (int q = 1; q < t - 1; q++) sel *= 0.5f;
-                float c[3];
-                bool any = false;
-                for (int k = 0; k < 3; k++) {
-                    c[k] = cs.c[k] * w / sel;
-                    any = any || (c[k] != 0.0f && c[k] == c[k]);
+                if (d == 0) {
+                    if (!(flags_of(last) & F_SV)) continue;
+                    P[0] = unpack(last);
+                    if (P[0].prim < 0 || !C.sc.prims[P[0].prim].is_light) continue;
+                } else {
+                    if (!(flags_of(last) & F_DIRECT)) continue;
+                    P[0] = unpack(w.dv[1][(size_t)(t - 1) * w.stride + i]);
                 }
-                if (!any || !(w == w)) continue;
-                float rx = 0.0f, ry = 0.0f;
-                raster_pos(C.cam, dirto(P[np - 1], P[np - 2]), rx, ry);
-                int ix = (int)(rx * (float)W), iy = (int)(ry * (float)H);
-                ix = ix < 0 ? 0 : (ix > (int)W - 1 ? (int)W - 1 : ix);
-                iy = iy < 0 ? 0 : (iy > (int)H - 1 ? (int)H - 1 : iy);
-                const uint32_t pix = (uint32_t)iy * W + (uint32_t)ix;
-                if (pix == pixel) {
+                P[0].type = T_L;
+                for (int q = 1; q < t; q++) P[q] = unpack(w.sv[1][(size_t)(t - 1 - q) * w.stride + i]);
+                float c[3];
+                if (!path_contribution(C, P, t, 0, d != 0, c)) continue;
+                const uint32_t pix = raster_pixel(C, P, t);
+                if (pix == own_pix) {
                     for (int k = 0; k < 3; k++) own[k] += c[k];
                 } else {
                     splat_px(film_x, film_x_sq, pix, c);
                 }
             }
+        }
+        for (int k = 0; k < 3; k++) w.own[3 * (size_t)i + k] = own[k];
     }
-    splat_px(film, film_sq, pixel, own);
+    // contiguous item ranges: warp-aggregated allocation
+    const unsigned lane = threadIdx.x & 31u;
+    uint32_t incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (unsigned)o) incl += v;
+    }
+    uint32_t wbase = 0;
+    if (lane == 31u && incl > 0u) wbase = atomicAdd(total, incl);
+    wbase = __shfl_sync(0xffffffffu, wbase, 31);
+    if (i < w.n) base[i] = wbase + incl - cnt;
 }
 
+// Work items of the s, t >= 1 connections: sample | s << 20 | t << 26.
+__global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ base, uint32_t* __restrict__ items)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.n) return;
+    const int nL = w.count[0][i], nE = w.count[1][i];
+    uint32_t o = base[i];
+    for (int s = 1; s <= nL; s++) {
+        int tmax = nE;
+        if (C.max_path >= 0 && tmax > C.max_path - s) tmax = C.max_path - s;
+        for (int t = 1; t <= tmax; t++) items[o++] = i | ((uint32_t)s << 20) | ((uint32_t)t << 26);
+    }
+}
+
+// One connection (Path::Connect, :298-330): the full path L[0..s-1] E[t-1..0],
+// its contribution and the shadow ray between the two subpath ends.
+__global__ void __launch_bounds__(kBdptThreads) k_bd_connect(Ctx C, Wave w, const uint32_t* __restrict__ items,
+                                                             uint32_t n_items, float4* __restrict__ rays,
+                                                             float4* __restrict__ rec)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_items) return;
+    const uint32_t it = items[q];
+    const uint32_t i = it & 0xfffffu;
+    const int s = (int)((it >> 20) & 0x3fu), t = (int)(it >> 26);
+    const BVtx lend = w.sv[0][(size_t)(s - 1) * w.stride + i], eend = w.sv[1][(size_t)(t - 1) * w.stride + i];
+    float c[3] = {0.0f, 0.0f, 0.0f};
+    bool ok = (flags_of(lend) & F_SV) && (flags_of(eend) & F_SV);
+    PV P[2 * kMaxV];
+    const int n = s + t;
+    if (ok) {
+        for (int k = 0; k < s; k++) P[k] = unpack(w.sv[0][(size_t)k * w.stride + i]);
+        for (int k = 0; k < t; k++) P[s + k] = unpack(w.sv[1][(size_t)(t - 1 - k) * w.stride + i]);
+        ok = path_contribution(C, P, n, s, false, c);
+    }
+    if (ok) {
+        store_shadow_ray(rays, q, P[s - 1].p, P[s].p);
+        rec[q] = make_float4(c[0], c[1], c[2], __uint_as_float(raster_pixel(C, P, n)));
+    } else {
+        store_null_ray(rays, q);
+        rec[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+__global__ void k_bd_splat(Wave w, const uint32_t* __restrict__ items, uint32_t n_items,
+                           const float4* __restrict__ rec, const lmgpu_hit* __restrict__ hits,
+                           double* __restrict__ film_x, double* __restrict__ film_x_sq)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_items) return;
+    const float4 r = rec[q];
+    if ((r.x == 0.0f && r.y == 0.0f && r.z == 0.0f) || hits[q].prim >= 0) return;
+    const uint32_t i = items[q] & 0xfffffu;
+    const uint32_t pix = __float_as_uint(r.w);
+    const float c[3] = {r.x, r.y, r.z};
+    if (pix == (uint32_t)((w.p0 + i) % w.npix)) {
+        for (int k = 0; k < 3; k++)
+            if (c[k] != 0.0f) atomicAdd(&w.own[3 * (size_t)i + k], c[k]);
+    } else {
+        splat_px(film_x, film_x_sq, pix, c);
+    }
+}
+
+__global__ void k_bd_flush(Wave w, double* __restrict__ film, double* __restrict__ film_sq)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.n) return;
+    const float c[3] = {w.own[3 * (size_t)i], w.own[3 * (size_t)i + 1], w.own[3 * (size_t)i + 2]};
+    splat_px(film, film_sq, (uint32_t)((w.p0 + i) % w.npix), c);
+}
+
+template <typename T>
+int grow_dev(T** p, uint64_t* cap, uint64_t count)
+{
+    if (*cap >= count) return LMGPU_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    const cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        return LMGPU_ERR_CUDA;
+    }
+    *cap = count;
+    return LMGPU_OK;
+}
+
+inline unsigned blocks(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
 }  // namespace
+
+// Device buffers of the bidirectional renderer, kept by the scene between calls.
+struct BdptState {
+    BVtx* verts = nullptr;  // sv[0], dv[0], sv[1], dv[1], each levels * stride
+    uint64_t verts_cap = 0;
+    BVtx* pend = nullptr;
+    uint64_t pend_cap = 0;
+    int32_t* counts = nullptr;
+    uint64_t counts_cap = 0;
+    float* own = nullptr;
+    uint64_t own_cap = 0;
+    uint32_t* active[2] = {nullptr, nullptr};
+    uint64_t active_cap[2] = {0, 0};
+    float4* ext[2] = {nullptr, nullptr};
+    uint64_t ext_cap[2] = {0, 0};
+    float4* sh = nullptr;
+    uint64_t sh_cap = 0;
+    lmgpu_hit* ext_hit = nullptr;
+    uint64_t ext_hit_cap = 0;
+    lmgpu_hit* sh_hit = nullptr;
+    uint64_t sh_hit_cap = 0;
+    uint32_t* base = nullptr;
+    uint64_t base_cap = 0;
+    uint32_t* counter = nullptr;  // [0] active / item counter
+    uint64_t counter_cap = 0;
+    uint32_t* h_counter = nullptr;
+    uint32_t* items = nullptr;
+    uint64_t items_cap = 0;
+    float4* c_rays = nullptr;
+    uint64_t c_rays_cap = 0;
+    float4* c_rec = nullptr;
+    uint64_t c_rec_cap = 0;
+    lmgpu_hit* c_hit = nullptr;
+    uint64_t c_hit_cap = 0;
+};
+
+void free_bdpt(BdptState* b)
+{
+    if (!b) return;
+    void* ptrs[] = {b->verts, b->pend, b->counts, b->own, b->active[0], b->active[1], b->ext[0], b->ext[1],
+                    b->sh, b->ext_hit, b->sh_hit, b->base, b->counter, b->items, b->c_rays, b->c_rec, b->c_hit};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (b->h_counter) cudaFreeHost(b->h_counter);
+    delete b;
+}
 
 int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream)
 {
@@ -604,33 +858,115 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
     }
     int rc = clear_film(sc, npix, stream);
     if (rc) return rc;
-    // The kernel keeps both subpaths in per-thread local memory (~4 KB):
-    // raise the per-thread stack limit once, up front, rather than have the
+    // The connection kernels keep a full path in per-thread local memory:
+    // raise the per-thread stack limit once, up front, rather than have a
     // launch resize the device's local-memory pool.
-    cudaFuncAttributes fa{};
-    LMGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, k_bdpt));
-    size_t stack = 0;
-    LMGPU_CUDA_TRY(cudaDeviceGetLimit(&stack, cudaLimitStackSize));
-    if (stack < fa.localSizeBytes) LMGPU_CUDA_TRY(cudaDeviceSetLimit(cudaLimitStackSize, fa.localSizeBytes));
+    {
+        size_t need = 0;
+        const void* fns[] = {(const void*)k_bd_connect, (const void*)k_bd_count, (const void*)k_bd_step};
+        for (const void* f : fns) {
+            cudaFuncAttributes fa{};
+            LMGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, f));
+            need = fa.localSizeBytes > need ? fa.localSizeBytes : need;
+        }
+        size_t stack = 0;
+        LMGPU_CUDA_TRY(cudaDeviceGetLimit(&stack, cudaLimitStackSize));
+        if (stack < need) LMGPU_CUDA_TRY(cudaDeviceSetLimit(cudaLimitStackSize, need));
+    }
     Ctx C;
     C.sc = scene_view(sc);
     C.lights = sc->lights;
     C.cam = sc->cam;
-    C.tv.nodes = sc->accel->nodes;
-    C.tv.tris = sc->accel->tris;
-    C.tv.num_nodes = sc->ntri > 0 ? (uint32_t)sc->accel->num_wide : 0u;
-    C.tv.num_tris = (uint32_t)sc->ntri;
-    C.tv.status = sc->accel->status;
     C.max_v = prm->max_num_vertices < 0 || prm->max_num_vertices > kMaxV ? kMaxV : prm->max_num_vertices;
     C.max_path = prm->max_num_vertices;
-    const uint64_t wave = 1ull << 20;
-    for (uint64_t p0 = 0; p0 < total; p0 += wave) {
-        const uint32_t n = (uint32_t)((total - p0) < wave ? (total - p0) : wave);
-        k_bdpt<<<(n + kBdptThreads - 1) / kBdptThreads, kBdptThreads, 0, stream>>>(C, p0, n, prm->seed, sc->film,
-                                                                                  sc->film_sq, sc->film_x,
-                                                                                  sc->film_x_sq);
+    if (C.max_v < 1) return finalize_film(sc, prm->spp, d_image, d_variance, stream);
+
+    if (!sc->bdpt) sc->bdpt = new BdptState();
+    BdptState& B = *sc->bdpt;
+    // wave size: the vertex arrays (4 x levels x 32 bytes per sample) within ~512 MB
+    const uint64_t levels = (uint64_t)C.max_v;
+    uint64_t stride = (512ull << 20) / (4 * levels * sizeof(BVtx));
+    stride = stride > kWaveSamples ? kWaveSamples : stride;
+    stride = stride < total ? stride : total;
+    if ((rc = grow_dev(&B.verts, &B.verts_cap, 4 * levels * stride)) ||
+        (rc = grow_dev(&B.pend, &B.pend_cap, 2 * stride)) || (rc = grow_dev(&B.counts, &B.counts_cap, 2 * stride)) ||
+        (rc = grow_dev(&B.own, &B.own_cap, 3 * stride)) ||
+        (rc = grow_dev(&B.active[0], &B.active_cap[0], 2 * stride)) ||
+        (rc = grow_dev(&B.active[1], &B.active_cap[1], 2 * stride)) ||
+        (rc = grow_dev(&B.ext[0], &B.ext_cap[0], 4 * stride)) || (rc = grow_dev(&B.ext[1], &B.ext_cap[1], 4 * stride)) ||
+        (rc = grow_dev(&B.sh, &B.sh_cap, 4 * stride)) || (rc = grow_dev(&B.ext_hit, &B.ext_hit_cap, 2 * stride)) ||
+        (rc = grow_dev(&B.sh_hit, &B.sh_hit_cap, 2 * stride)) || (rc = grow_dev(&B.base, &B.base_cap, stride)) ||
+        (rc = grow_dev(&B.counter, &B.counter_cap, 1)))
+        return rc;
+    if (!B.h_counter && cudaMallocHost((void**)&B.h_counter, sizeof(uint32_t)) != cudaSuccess) {
+        set_error("lmgpu_render_bdpt: pinned allocation failed");
+        return LMGPU_ERR_CUDA;
+    }
+    Wave w;
+    w.stride = (uint32_t)stride;
+    w.npix = (uint32_t)npix;
+    w.seed = prm->seed;
+    w.sv[0] = B.verts;
+    w.dv[0] = B.verts + levels * stride;
+    w.sv[1] = B.verts + 2 * levels * stride;
+    w.dv[1] = B.verts + 3 * levels * stride;
+    w.count[0] = B.counts;
+    w.count[1] = B.counts + stride;
+    w.pend = B.pend;
+    w.own = B.own;
+    auto read_counter = [&](uint32_t& out) -> int {
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(B.h_counter, B.counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+        out = *B.h_counter;
+        return LMGPU_OK;
+    };
+    for (uint64_t p0 = 0; p0 < total; p0 += stride) {
+        w.p0 = p0;
+        w.n = (uint32_t)((total - p0) < stride ? (total - p0) : stride);
+        // subpaths
+        k_bd_start<<<blocks(2ull * w.n, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.ext[0], B.sh, B.active[0]);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
+        uint32_t n_active = C.max_v > 1 ? 2 * w.n : 0;
+        int cur = 0;
+        for (int k = 1; n_active > 0; k++) {
+            if ((rc = launch_trace(sc->accel, B.ext[cur], B.ext_hit, n_active, false, false, stream)) ||
+                (rc = launch_trace(sc->accel, B.sh, B.sh_hit, n_active, true, false, stream)))
+                return rc;
+            LMGPU_CUDA_TRY(cudaMemsetAsync(B.counter, 0, sizeof(uint32_t), stream));
+            k_bd_step<<<blocks(n_active, kBdptThreads), kBdptThreads, 0, stream>>>(
+                C, w, k, n_active, B.active[cur], B.ext[cur], B.ext_hit, B.sh_hit, B.active[1 - cur], B.counter,
+                B.ext[1 - cur], B.sh);
+            LMGPU_CUDA_TRY(cudaGetLastError());
+            sc->launches += 3;
+            if ((rc = read_counter(n_active))) return rc;
+            cur = 1 - cur;
+        }
+        // connections
+        LMGPU_CUDA_TRY(cudaMemsetAsync(B.counter, 0, sizeof(uint32_t), stream));
+        k_bd_count<<<blocks(w.n, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.base, B.counter, sc->film_x,
+                                                                         sc->film_x_sq);
+        LMGPU_CUDA_TRY(cudaGetLastError());
+        uint32_t n_items = 0;
+        if ((rc = read_counter(n_items))) return rc;
+        if (n_items > 0) {
+            if ((rc = grow_dev(&B.items, &B.items_cap, n_items)) ||
+                (rc = grow_dev(&B.c_rays, &B.c_rays_cap, 2ull * n_items)) ||
+                (rc = grow_dev(&B.c_rec, &B.c_rec_cap, n_items)) || (rc = grow_dev(&B.c_hit, &B.c_hit_cap, n_items)))
+                return rc;
+            k_bd_items<<<blocks(w.n, 256), 256, 0, stream>>>(C, w, B.base, B.items);
+            k_bd_connect<<<blocks(n_items, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.items, n_items,
+                                                                                   B.c_rays, B.c_rec);
+            LMGPU_CUDA_TRY(cudaGetLastError());
+            if ((rc = launch_trace(sc->accel, B.c_rays, B.c_hit, n_items, true, false, stream))) return rc;
+            k_bd_splat<<<blocks(n_items, 256), 256, 0, stream>>>(w, B.items, n_items, B.c_rec, B.c_hit, sc->film_x,
+                                                                  sc->film_x_sq);
+            LMGPU_CUDA_TRY(cudaGetLastError());
+            sc->launches += 4;
+        }
+        k_bd_flush<<<blocks(w.n, 256), 256, 0, stream>>>(w, sc->film, sc->film_sq);
+        LMGPU_CUDA_TRY(cudaGetLastError());
+        sc->launches += 2;
     }
     return finalize_film(sc, prm->spp, d_image, d_variance, stream);
 }

@@ -49,6 +49,9 @@ struct SceneGPU {
 // Area lights for the bidirectional renderer: the primitives flagged as
 // lights, each with its triangles and their area CDF
 // (TriangleUtils::CreateTriangleAreaDist, triangleutils.h:40-77).
+struct BdptState;
+void free_bdpt(BdptState* b);
+
 struct LightsGPU {
     int32_t count;
     const int32_t* prims;       // light -> primitive
@@ -101,6 +104,7 @@ struct lmgpu_scene {
     uint64_t q_cap = 0;
     cudaStream_t stream = nullptr;
     uint64_t launches = 0;  // kernels launched by the renderers since creation
+    lmgpu::BdptState* bdpt = nullptr;  // buffers of the bidirectional renderer
 };
 
 namespace lmgpu {
