@@ -327,9 +327,10 @@ RENDER_WORKLOADS = {
     # renderer::pt on the Cornell-style box: 256 x 256, 64 spp, max_num_vertices 9 (8 segments)
     "pt": {"renderer": "pt", "workload": "pt_cornell_256x256_64spp", "width": 256, "height": 256, "spp": 64,
            "max_num_vertices": 9, "data": "synthetic (procedural Cornell box)", "cpu_spp": 8},
-    # renderer::bdpt on the caustic room: 1280 x 720, 32 spp, path length 10, all (s, t) strategies
+    # renderer::bdpt on the caustic room: 1280 x 720, 32 spp, path length 10 (10 segments, so
+    # max_num_vertices 11), all (s, t) strategies
     "bdpt": {"renderer": "bdpt", "workload": "bdpt_caustic_room_1280x720_32spp", "width": 1280, "height": 720,
-             "spp": 32, "max_num_vertices": 10,
+             "spp": 32, "max_num_vertices": 11,
              "data": "synthetic (procedural room, level-5 glass icosphere, sphere light behind a panel)",
              "cpu_spp": 1},
 }
@@ -347,6 +348,8 @@ def run_render(args) -> None:
 
     cfg = RENDER_WORKLOADS[args.workload]
     W, H, spp, max_nv = cfg["width"], cfg["height"], cfg["spp"], cfg["max_num_vertices"]
+    if args.spp:
+        spp = args.spp
     scene = scenes.cornell_box(W, H) if cfg["renderer"] == "pt" else scenes.caustic_room(W, H)
     stream = torch.cuda.Stream()
     sc = lmgpu.Scene(scene)
@@ -358,19 +361,23 @@ def run_render(args) -> None:
     for k in range(args.warmup):
         render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, k, stream.cuda_stream)
     torch.cuda.synchronize()
+    # each step timed alone with events on the render stream; L2 flushed
+    # (a 256 MiB write, untimed) before every step
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     l0 = sc.launch_count()
-    ev0.record(stream)
-    for k in range(args.steps):
-        render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, 1000 + k, stream.cuda_stream)
-    ev1.record(stream)
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            evs[k][0].record(stream)
+            render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, 1000 + k, stream.cuda_stream)
+            evs[k][1].record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
     launches = sc.launch_count() - l0
-    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
     t0 = time.perf_counter()
     for k in range(args.steps):
         render_host(spp, max_nv, 2000 + k)
@@ -379,9 +386,10 @@ def run_render(args) -> None:
     line = {"metric": f"Msamples/s (renderer::{cfg['renderer']})", "value": samples / ms / 1e3,
             "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": cfg["data"],
-            "config": {"workload": cfg["workload"], "width": W, "height": H, "spp": spp,
+            "config": {"workload": cfg["workload"] if spp == cfg["spp"] else f"{cfg['workload']} at {spp} spp",
+                       "width": W, "height": H, "spp": spp,
                        "max_num_vertices": max_nv, "triangles": ntri,
-                       "l2": "film and scene stay resident (the workload's working set)"},
+                       "l2": "flushed before every timed step (256 MiB write, untimed)"},
             "e2e": {"value": samples / e2e_s / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": W * H * 3 * 4 * 2, "api": f"lmgpu_render_{cfg['renderer']} (host film)"},
             "gpu_launches": launches, "clocks": clk}
@@ -412,6 +420,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling of smaller cases)")
     ap.add_argument("--anyhit", action="store_true", help="time any-hit queries instead of closest hit")
+    ap.add_argument("--spp", type=int, default=0, help="samples per pixel of the render workloads (profiling of "
+                                                        "smaller cases; default: the workload's own)")
     ap.add_argument("--workload", choices=["raycast", "pt", "bdpt"], default="raycast",
                     help="raycast: the BVH ray-cast configuration (default); pt: renderer::pt on the Cornell "
                          "box; bdpt: renderer::bdpt on the caustic room")

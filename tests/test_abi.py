@@ -60,17 +60,18 @@ def test_null_arguments_rejected(gpu_lib):
     assert L.lmgpu_last_error()
 
 
-def test_reference_plugin_compiles_against_reference_headers(repo_dir):
-    """plugin/accel_cuda.cpp, the binding a maintainer adds to the reference
-    tree, compiles against the reference's own headers (x86-64 only: the
-    reference forces SSE)."""
+@pytest.mark.parametrize("plugin", ["accel_cuda", "renderer_pt_cuda", "renderer_bdpt_cuda"])
+def test_reference_plugin_compiles_against_reference_headers(repo_dir, plugin):
+    """plugin/*.cpp, the bindings a maintainer adds to the reference tree
+    (accel::cuda, renderer::pt_cuda, renderer::bdpt_cuda), compile against the
+    reference's own headers (x86-64 only: the reference forces SSE)."""
     import platform
     import shutil
 
     ref = "/root/reference/include"
     if not os.path.isdir(ref) or platform.machine() != "x86_64" or not shutil.which("g++"):
         pytest.skip("reference headers or x86-64 g++ not available")
-    src = os.path.join(repo_dir, "lightmetrica-v2_gb300", "plugin", "accel_cuda.cpp")
+    src = os.path.join(repo_dir, "lightmetrica-v2_gb300", "plugin", plugin + ".cpp")
     cmd = ["g++", "-std=c++14", "-fsyntax-only", "-w", "-DLM_USE_SINGLE_PRECISION", "-msse4.2",
            "-I", os.path.join(repo_dir, "oracle", "refharness", "shim"), "-I", ref,
            "-I", os.path.join(repo_dir, "include"), src]
