@@ -197,6 +197,19 @@ int lmgpu_render_pt(lmgpu_scene* scene, const lmgpu_pt_params* params, float* im
 int lmgpu_render_pt_device(lmgpu_scene* scene, const lmgpu_pt_params* params, float* d_image, float* d_variance,
                            void* stream);
 
+/* Renders the scene with path tracing plus next-event estimation: one light
+ * sample per vertex (the sensor included) combined with BSDF sampling by the
+ * balance heuristic.  Stands in for Renderer::Render of renderer::ptmis
+ * (src/liblightmetrica/renderer/renderer_ptmis.cpp:68-325).  The scene needs
+ * at least one area light; environment lights are not sampled by this
+ * renderer (LMGPU_ERR_INVALID if the scene has one). */
+int lmgpu_render_ptmis(lmgpu_scene* scene, const lmgpu_pt_params* params, float* image, float* variance);
+
+/* As lmgpu_render_ptmis into device buffers on `stream` (NULL: the scene's
+ * stream); returns after the render has finished. */
+int lmgpu_render_ptmis_device(lmgpu_scene* scene, const lmgpu_pt_params* params, float* d_image, float* d_variance,
+                              void* stream);
+
 /* Renders the scene with bidirectional path tracing (all (s, t) strategies,
  * power-heuristic MIS) and writes the film as lmgpu_render_pt does.  Stands
  * in for Renderer::Render of renderer::bdpt

@@ -1,126 +1,270 @@
-// Wavefront path tracer: the GPU form of renderer::pt.
+// Wavefront path tracers: the GPU forms of renderer::pt and renderer::ptmis.
 //
-// Reference behaviour (src/liblightmetrica/renderer/renderer_pt.cpp:68-231):
-// a path starts at the pinhole sensor with throughput 1 (importance / pdf),
-// extends by BSDF sampling (fs / pdf), splats throughput * Le whenever it
-// hits the front side of an area light (no next-event estimation), applies
-// Russian roulette with probability 0.5 after every hit, and stops after
+// renderer::pt (src/liblightmetrica/renderer/renderer_pt.cpp:68-231): a path
+// starts at the pinhole sensor with throughput 1 (importance / pdf), extends
+// by BSDF sampling (fs / pdf), splats throughput * Le whenever it hits the
+// front side of an area light (no next-event estimation), applies Russian
+// roulette with probability 0.5 after every hit, and stops after
 // max_num_vertices vertices or at a surface whose BSDF is null.
+//
+// renderer::ptmis (renderer_ptmis.cpp:68-305) adds, at every vertex before
+// its BSDF sample (the sensor included), one light sample: a light primitive
+// chosen uniformly, a triangle by its area CDF, a uniform point on it; the
+// contribution fs G V Le / (pdf_light pdf_area) is weighted by the balance
+// heuristic pdf_light / (pdf_light + pdf_bsdf) in projected solid angle, and
+// BSDF-sampled light hits by pdf_bsdf / (pdf_bsdf + pdf_light), with
+// pdf_light = 0 after a specular vertex.  Environment lights are not sampled
+// by this form (the entry point rejects scenes that have one).
 //
 // BSDFs: bsdf::null, bsdf::diffuse, bsdf::flesnel (dielectric) and
 // bsdf::cook_torrance (GGX conductor); lights: light::area on primitives and a
-// constant light::env reached by rays that leave the geometry.
+// constant light::env reached by rays that leave the geometry (pt only).
 //
 // GPU structure, one wave of up to kWave paths at a time:
-//   k_pt_generate   camera rays for paths [p0, p0 + n) (sensor_pinhole.cpp:79-90)
-//   k_trace         closest hit for the queue (trace.cu)
-//   k_pt_shade      emission splat, roulette, diffuse sampling
-//                   (bsdf_diffuse.cpp:69-104, sampler.h:44-67); surviving
-//                   paths are appended to the next queue (warp-aggregated
-//                   atomics, so queues stay compact)
+//   k_pt_generate   camera rays for paths [p0, p0 + n) (sensor_pinhole.cpp:79-90);
+//                   ptmis: the sensor's light sample
+//   per bounce      k_trace (closest hit, trace.cu) over the compacted queue;
+//                   k_pt_shade: emission (MIS-weighted for ptmis), roulette,
+//                   BSDF sampling, warp-aggregated append of surviving paths;
+//                   ptmis: the new vertex's light sample as a shadow ray plus
+//                   a pending contribution, then k_trace (any hit) over the
+//                   shadow rays and k_pt_nee_splat
+//   k_pt_flush      each path's own-pixel sum into the film (sum and square:
+//                   the reference film squares per-sample sums)
 //   k_film_finalize per-pixel mean and FP64 variance of the mean (scene.cu)
 // Sampling differs from the reference only in ways that keep the estimator's
 // expectation: raster positions are stratified per pixel (spp jittered
 // samples in each pixel instead of W*H*spp uniform positions over the film),
 // and random numbers come from Philox keyed by (seed, path, bounce).
 #include "accel.cuh"
+#include "interact.cuh"
 #include "rng.cuh"
-#include "scene.cuh"
-#include "bsdf.cuh"
 
 namespace lmgpu {
 namespace {
 
 constexpr int kShadeThreads = 256;
 
-__global__ void k_pt_generate(CameraGPU cam, uint64_t p0, uint32_t n, uint32_t seed, float4* __restrict__ rays,
-                              PathState* __restrict__ state)
+// PathState.id.w holds, for ptmis, the BSDF pdf of the last sampled
+// direction times |cos| at the vertex it left (projected solid angle to
+// solid angle at that end; 1 for the pinhole), or -1 after a specular vertex.
+__device__ __forceinline__ float light_pdf_proj(const Ctx& C, int prim, float d2, float cos_light)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint64_t p = p0 + i;
-    const uint32_t npix = (uint32_t)cam.width * (uint32_t)cam.height;
-    const uint32_t pixel = (uint32_t)(p % npix);
-    const uint32_t x = pixel % (uint32_t)cam.width, y = pixel / (uint32_t)cam.width;
-    const Philox4x32 r = philox4x32_10((uint32_t)p, (uint32_t)(p >> 32), 0u, 0u, seed, kKeyCamera);
-    const float rx = ((float)x + u01(r.v[0])) / (float)cam.width;
-    const float ry = ((float)y + u01(r.v[1])) / (float)cam.height;
-    const float3 d = camera_dir(cam, rx, ry);
-    rays[2 * i] = make_float4(cam.eye.x, cam.eye.y, cam.eye.z, 1e-4f);
-    rays[2 * i + 1] = make_float4(d.x, d.y, d.z, FLT_MAX);
-    PathState s;
-    s.thr = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pixel));
-    s.id = make_uint4((uint32_t)p, (uint32_t)(p >> 32), 1u, 0u);
-    state[i] = s;
+    // pdf_light of reaching `prim` at distance^2 d2, without the previous
+    // vertex's cosine: (1 / area) (1 / #lights) d^2 / |cos_light|
+    return C.lights.inv_area[C.lights.prim_light[prim]] / (float)C.lights.count * d2 / cos_light;
 }
 
-__device__ __forceinline__ void splat(double* __restrict__ film, double* __restrict__ film_sq, uint32_t pixel,
-                                      const float c[3])
+// A light sample from vertex v (Renderer_PTMIS, renderer_ptmis.cpp:131-193):
+// the weighted contribution (before visibility) and the light point, or
+// false when it is black.
+__device__ __forceinline__ bool nee_sample(const Ctx& C, const PV& v, int type, float3 wi, float us, float a0,
+                                           float a1, const float thr[3], float c[3], PV& L, float3& ppL)
 {
+    sample_light(C, us, a0, a1, L);
+    ppL = normalize3(L.p - v.p);
+    const Spd fsE = eval_dir(C, v, type, wi, ppL, DIR_EL, true);
+    if (black(fsE)) return false;
+    const Spd fsL = eval_dir(C, L, T_L, zero3(), ppL * -1.0f, DIR_LE, false);
+    if (black(fsL)) return false;
+    const float G = geometry_term(v, L);
+    const float pdfL = 1.0f / (float)C.lights.count;
+    const float pdfPL = C.lights.inv_area[C.lights.prim_light[L.prim]];
+    const float pdfDL = pdfPL / G * pdfL;
+    const float pdfB = pdf_dir(C, v, type, wi, ppL);
+    const float w = pdfDL / (pdfDL + pdfB);
+    bool any = false;
     for (int k = 0; k < 3; k++) {
-        if (c[k] != 0.0f) {
-            atomicAdd(&film[3 * (size_t)pixel + k], (double)c[k]);
-            atomicAdd(&film_sq[3 * (size_t)pixel + k], (double)c[k] * (double)c[k]);
-        }
+        c[k] = thr[k] * fsE.c[k] * G * fsL.c[k] / pdfL / pdfPL * w;
+        any = any || (c[k] != 0.0f && c[k] == c[k]);
+    }
+    return any;
+}
+
+// Appends a pending light-sample contribution (shadow ray v -> L) with
+// warp-aggregated atomics; every lane of the warp must call it.
+__device__ __forceinline__ void append_nee(bool has, const PV& v, const PV& L, const float c[3], uint32_t pix,
+                                           uint32_t path, float4* __restrict__ rays, float4* __restrict__ rec,
+                                           uint32_t* __restrict__ rec_path, uint32_t* __restrict__ count)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, has);
+    if (m == 0u) return;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned leader = __ffs(m) - 1u;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (has) {
+        const uint32_t o = base + __popc(m & ((1u << lane) - 1u));
+        float3 d = L.p - v.p;
+        const float len = sqrtf(dot3(d, d));
+        d = d * (1.0f / len);
+        rays[2 * o] = make_float4(v.p.x, v.p.y, v.p.z, 1e-4f);
+        rays[2 * o + 1] = make_float4(d.x, d.y, d.z, len * (1.0f - 1e-4f));
+        rec[o] = make_float4(c[0], c[1], c[2], __uint_as_float(pix));
+        rec_path[o] = path;
     }
 }
 
-__global__ void __launch_bounds__(kShadeThreads) k_pt_shade(const float4* __restrict__ rays,
-                                                            const PathState* __restrict__ state,
-                                                            const lmgpu_hit* __restrict__ hits, uint32_t n,
-                                                            SceneGPU sc, int max_nv, uint32_t seed,
-                                                            double* __restrict__ film, double* __restrict__ film_sq,
-                                                            float4* __restrict__ out_rays,
-                                                            PathState* __restrict__ out_state,
-                                                            uint32_t* __restrict__ out_count)
+__device__ __forceinline__ uint32_t pixel_at(const CameraGPU& cam, float rx, float ry)
+{
+    int ix = (int)(rx * (float)cam.width), iy = (int)(ry * (float)cam.height);
+    ix = ix < 0 ? 0 : (ix > cam.width - 1 ? cam.width - 1 : ix);
+    iy = iy < 0 ? 0 : (iy > cam.height - 1 ? cam.height - 1 : iy);
+    return (uint32_t)iy * (uint32_t)cam.width + (uint32_t)ix;
+}
+
+template <bool NEE>
+__global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p0, uint32_t n, uint32_t seed,
+                                                               float4* __restrict__ rays,
+                                                               PathState* __restrict__ state,
+                                                               float* __restrict__ own, float4* __restrict__ nrays,
+                                                               float4* __restrict__ nrec,
+                                                               uint32_t* __restrict__ npath,
+                                                               uint32_t* __restrict__ ncount)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool keep = false;
+    const CameraGPU& cam = C.cam;
+    bool has_nee = false;
+    PV v, L;
+    float c[3] = {0.0f, 0.0f, 0.0f};
+    uint32_t nee_pix = 0;
+    if (i < n) {
+        const uint64_t p = p0 + i;
+        const uint32_t npix = (uint32_t)cam.width * (uint32_t)cam.height;
+        const uint32_t pixel = (uint32_t)(p % npix);
+        const uint32_t x = pixel % (uint32_t)cam.width, y = pixel / (uint32_t)cam.width;
+        const Philox4x32 r = philox4x32_10((uint32_t)p, (uint32_t)(p >> 32), 0u, 0u, seed, kKeyCamera);
+        const float rx = ((float)x + u01(r.v[0])) / (float)cam.width;
+        const float ry = ((float)y + u01(r.v[1])) / (float)cam.height;
+        const float3 d = camera_dir(cam, rx, ry);
+        rays[2 * i] = make_float4(cam.eye.x, cam.eye.y, cam.eye.z, 1e-4f);
+        rays[2 * i + 1] = make_float4(d.x, d.y, d.z, FLT_MAX);
+        PathState s;
+        s.thr = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pixel));
+        // pinhole: pdf of the direction = importance, |cos| = 1 (degenerate end)
+        s.id = make_uint4((uint32_t)p, (uint32_t)(p >> 32), 1u, __float_as_uint(NEE ? importance(cam, d) : 0.0f));
+        state[i] = s;
+        own[3 * (size_t)i] = 0.0f;
+        own[3 * (size_t)i + 1] = 0.0f;
+        own[3 * (size_t)i + 2] = 0.0f;
+        if (NEE && (C.max_path < 0 || 1 < C.max_path)) {
+            // the sensor's light sample; it lands where ppL meets the film
+            sensor_vertex(C, v);
+            const Philox4x32 q = philox4x32_10((uint32_t)p, (uint32_t)(p >> 32), 0u, 1u, seed, kKeyCamera);
+            const float one[3] = {1.0f, 1.0f, 1.0f};
+            float3 ppL;
+            has_nee = nee_sample(C, v, T_E, zero3(), u01(q.v[0]), u01(q.v[1]), u01(q.v[2]), one, c, L, ppL);
+            if (has_nee) {
+                float px, py;
+                raster_pos(cam, ppL, px, py);
+                nee_pix = pixel_at(cam, px, py);
+            }
+        }
+    }
+    if (NEE) append_nee(has_nee, v, L, c, nee_pix, i, nrays, nrec, npath, ncount);
+}
+
+template <bool NEE>
+__global__ void __launch_bounds__(kShadeThreads) k_pt_shade(Ctx C, const float4* __restrict__ rays,
+                                                            const PathState* __restrict__ state,
+                                                            const lmgpu_hit* __restrict__ hits, uint32_t n,
+                                                            uint64_t p0, uint32_t seed, float* __restrict__ own,
+                                                            float4* __restrict__ out_rays,
+                                                            PathState* __restrict__ out_state,
+                                                            uint32_t* __restrict__ out_count,
+                                                            float4* __restrict__ nrays, float4* __restrict__ nrec,
+                                                            uint32_t* __restrict__ npath,
+                                                            uint32_t* __restrict__ ncount)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool keep = false, has_nee = false;
     float4 nr0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), nr1 = nr0;
     PathState ns;
+    PV v, L;
+    float c[3] = {0.0f, 0.0f, 0.0f};
+    uint32_t pixel = 0, path = 0;
     if (i < n) {
         const lmgpu_hit h = hits[i];
         const PathState s = state[i];
-        const uint32_t pixel = __float_as_uint(s.thr.w);
+        pixel = __float_as_uint(s.thr.w);
+        const uint64_t p = (uint64_t)s.id.x | ((uint64_t)s.id.y << 32);
+        path = (uint32_t)(p - p0);
+        float* acc = own + 3 * (size_t)path;
         if (h.prim < 0) {
             // miss: the environment light, if any (scene3.cpp:464-475); the
             // path ends there (renderer_pt.cpp:200-203)
-            if (sc.has_env) {
-                const float c[3] = {s.thr.x * sc.env_Le[0], s.thr.y * sc.env_Le[1], s.thr.z * sc.env_Le[2]};
-                splat(film, film_sq, pixel, c);
+            if (!NEE && C.sc.has_env) {
+                acc[0] += s.thr.x * C.sc.env_Le[0];
+                acc[1] += s.thr.y * C.sc.env_Le[1];
+                acc[2] += s.thr.z * C.sc.env_Le[2];
             }
         } else {
             const float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
             const float3 o = f3(r0.x, r0.y, r0.z), d = f3(r1.x, r1.y, r1.z);
-            const float* T = sc.tris + 9 * (size_t)h.prim;
+            const float* T = C.sc.tris + 9 * (size_t)h.prim;
             const float3 p1 = f3(T[0], T[1], T[2]), p2 = f3(T[3], T[4], T[5]), p3 = f3(T[6], T[7], T[8]);
-            const float3 gn = normalize3(cross3(p2 - p1, p3 - p1));
-            const PrimGPU P = sc.prims[sc.tri_prim[h.prim]];
-            const float3 pos = o + d * h.t;
+            v.p = o + d * h.t;
+            v.n = normalize3(cross3(p2 - p1, p3 - p1));
+            v.prim = C.sc.tri_prim[h.prim];
+            const PrimGPU& P = C.sc.prims[v.prim];
+            v.type = (short)bsdf_type(P.bsdf);
+            v.degen = 0;
             uint32_t nv = s.id.z;
-            if (P.is_light && -dot3(d, gn) > 0.0f) {
-                // throughput * Le(-d) * EvaluatePosition (= 1), renderer_pt.cpp:183-194
-                const float c[3] = {s.thr.x * P.Le[0], s.thr.y * P.Le[1], s.thr.z * P.Le[2]};
-                splat(film, film_sq, pixel, c);
+            const float cos_l = -dot3(d, v.n);
+            if (P.is_light && cos_l > 0.0f) {
+                // throughput * Le(-d) * EvaluatePosition (= 1), renderer_pt.cpp:183-194;
+                // ptmis: weight pdf_bsdf / (pdf_bsdf + pdf_light), renderer_ptmis.cpp:246-270
+                float w = 1.0f;
+                if (NEE) {
+                    const float q = __uint_as_float(s.id.w);
+                    w = q < 0.0f ? 1.0f : q / (q + light_pdf_proj(C, v.prim, h.t * h.t, cos_l));
+                }
+                acc[0] += s.thr.x * P.Le[0] * w;
+                acc[1] += s.thr.y * P.Le[1] * w;
+                acc[2] += s.thr.z * P.Le[2] * w;
             }
             const Philox4x32 r = philox4x32_10(s.id.x, s.id.y, nv, 0u, seed, kKeyBounce);
             // Russian roulette, probability 0.5 (renderer_pt.cpp:207-216)
             if (u01(r.v[3]) <= 0.5f) {
                 nv++;
-                const bool more = max_nv < 0 || (int)nv < max_nv;
+                const bool more = C.max_path < 0 || (int)nv < C.max_path;
+                const float thr[3] = {2.0f * s.thr.x, 2.0f * s.thr.y, 2.0f * s.thr.z};
+                const float3 wi = d * -1.0f;
+                if (more && NEE) {
+                    const Philox4x32 q = philox4x32_10(s.id.x, s.id.y, nv, 1u, seed, kKeyBounce);
+                    float3 ppL;
+                    has_nee = nee_sample(C, v, v.type, wi, u01(q.v[0]), u01(q.v[1]), u01(q.v[2]), thr, c, L, ppL);
+                }
                 float3 wo;
                 float f[3];
-                if (more && sample_bsdf(P, gn, d * -1.0f, u01(r.v[0]), u01(r.v[1]), u01(r.v[2]), wo, f)) {
+                float q_next = 0.0f;
+                bool ok = false;
+                if (more) {
+                    if (NEE) {
+                        ok = sample_dir(C, v, wi, u01(r.v[0]), u01(r.v[1]), u01(r.v[2]), wo);
+                        if (ok) {
+                            const Spd fs = eval_dir(C, v, v.type, wi, wo, DIR_EL, false);
+                            const float pdfD = pdf_dir(C, v, v.type, wi, wo);
+                            ok = !black(fs) && pdfD > 0.0f;
+                            for (int k = 0; k < 3; k++) f[k] = fs.c[k] / pdfD;
+                            q_next = delta_dir(C, v, v.type) ? -1.0f : pdfD * fabsf(dot3(v.n, wo));
+                        }
+                    } else {
+                        ok = sample_bsdf(P, v.n, wi, u01(r.v[0]), u01(r.v[1]), u01(r.v[2]), wo, f);
+                    }
+                }
+                if (ok) {
                     keep = true;
-                    nr0 = make_float4(pos.x, pos.y, pos.z, 1e-4f);
+                    nr0 = make_float4(v.p.x, v.p.y, v.p.z, 1e-4f);
                     nr1 = make_float4(wo.x, wo.y, wo.z, FLT_MAX);
-                    ns.thr = make_float4(2.0f * s.thr.x * f[0], 2.0f * s.thr.y * f[1], 2.0f * s.thr.z * f[2],
-                                         s.thr.w);
-                    ns.id = make_uint4(s.id.x, s.id.y, nv, 0u);
+                    ns.thr = make_float4(thr[0] * f[0], thr[1] * f[1], thr[2] * f[2], s.thr.w);
+                    ns.id = make_uint4(s.id.x, s.id.y, nv, __float_as_uint(q_next));
                 }
             }
         }
     }
+    if (NEE) append_nee(has_nee, v, L, c, pixel, path, nrays, nrec, npath, ncount);
     // warp-aggregated append to the next queue
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     if (m == 0u) return;
@@ -137,39 +281,128 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(const float4* __rest
     }
 }
 
+__device__ __forceinline__ void splat_px(double* film, double* film_sq, uint32_t pix, const float c[3])
+{
+    for (int k = 0; k < 3; k++) {
+        if (c[k] != 0.0f) {
+            atomicAdd(&film[3 * (size_t)pix + k], (double)c[k]);
+            atomicAdd(&film_sq[3 * (size_t)pix + k], (double)c[k] * (double)c[k]);
+        }
+    }
+}
+
+// Unoccluded light samples: into the path's own-pixel sum, or (the sensor's
+// light samples that land elsewhere) into the film of other samples' splats.
+__global__ void k_pt_nee_splat(uint64_t p0, uint32_t npix, uint32_t n, const float4* __restrict__ rec,
+                               const uint32_t* __restrict__ rec_path, const lmgpu_hit* __restrict__ hits,
+                               float* __restrict__ own, double* __restrict__ film_x, double* __restrict__ film_x_sq)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n || hits[q].prim >= 0) return;
+    const float4 r = rec[q];
+    const uint32_t path = rec_path[q];
+    const uint32_t pix = __float_as_uint(r.w);
+    const float c[3] = {r.x, r.y, r.z};
+    if (pix == (uint32_t)((p0 + path) % npix)) {
+        for (int k = 0; k < 3; k++) atomicAdd(&own[3 * (size_t)path + k], c[k]);
+    } else {
+        splat_px(film_x, film_x_sq, pix, c);
+    }
+}
+
+__global__ void k_pt_flush(uint64_t p0, uint32_t npix, uint32_t n, const float* __restrict__ own,
+                           double* __restrict__ film, double* __restrict__ film_sq)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float c[3] = {own[3 * (size_t)i], own[3 * (size_t)i + 1], own[3 * (size_t)i + 2]};
+    splat_px(film, film_sq, (uint32_t)((p0 + i) % npix), c);
+}
+
 }  // namespace
 
-int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream)
+int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream,
+              bool nee)
 {
     const uint32_t W = (uint32_t)sc->cam.width, H = (uint32_t)sc->cam.height;
     const uint64_t npix = (uint64_t)W * H;
     const uint64_t total = npix * prm->spp;
     if (total == 0) return LMGPU_OK;
+    if (nee && sc->lights.count == 0) {
+        set_error("lmgpu_render_ptmis: the scene has no area light");
+        return LMGPU_ERR_INVALID;
+    }
+    if (nee && sc->has_env) {
+        set_error("lmgpu_render_ptmis: environment lights are not sampled by this renderer");
+        return LMGPU_ERR_INVALID;
+    }
     int rc = clear_film(sc, npix, stream);
     if (rc) return rc;
     rc = ensure_queues(sc, total < kWave ? total : kWave);
     if (rc) return rc;
-    const SceneGPU sg = scene_view(sc);
+    Ctx C;
+    C.sc = scene_view(sc);
+    C.lights = sc->lights;
+    C.cam = sc->cam;
+    C.max_v = 0;
+    C.max_path = prm->max_num_vertices;
+    const uint32_t np = (uint32_t)npix;
     for (uint64_t p0 = 0; p0 < total; p0 += kWave) {
         uint32_t n = (uint32_t)((total - p0) < kWave ? (total - p0) : kWave);
-        k_pt_generate<<<(n + 255) / 256, 256, 0, stream>>>(sc->cam, p0, n, prm->seed, sc->q_ray[0], sc->q_state[0]);
+        const uint32_t n_wave = n;
+        LMGPU_CUDA_TRY(cudaMemsetAsync(sc->q_count, 0, 2 * sizeof(uint32_t), stream));
+        if (nee)
+            k_pt_generate<true><<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
+                C, p0, n, prm->seed, sc->q_ray[0], sc->q_state[0], sc->q_own, sc->q_nray, sc->q_nrec, sc->q_npath,
+                sc->q_count + 1);
+        else
+            k_pt_generate<false><<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
+                C, p0, n, prm->seed, sc->q_ray[0], sc->q_state[0], sc->q_own, sc->q_nray, sc->q_nrec, sc->q_npath,
+                sc->q_count + 1);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
         int cur = 0;
-        while (n > 0) {
+        uint32_t n_nee = 0;
+        if (nee) {
+            LMGPU_CUDA_TRY(cudaMemcpyAsync(sc->h_count, sc->q_count, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                           stream));
+            LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+            n_nee = sc->h_count[1];
+        }
+        while (n > 0 || n_nee > 0) {
+            if (n_nee > 0) {
+                rc = launch_trace(sc->accel, sc->q_nray, sc->q_nhit, n_nee, true, false, stream);
+                if (rc) return rc;
+                k_pt_nee_splat<<<(n_nee + 255) / 256, 256, 0, stream>>>(p0, np, n_nee, sc->q_nrec, sc->q_npath,
+                                                                        sc->q_nhit, sc->q_own, sc->film_x,
+                                                                        sc->film_x_sq);
+                LMGPU_CUDA_TRY(cudaGetLastError());
+                sc->launches += 2;
+            }
+            if (n == 0) break;
             rc = launch_trace(sc->accel, sc->q_ray[cur], sc->q_hit, n, false, false, stream);
             if (rc) return rc;
-            LMGPU_CUDA_TRY(cudaMemsetAsync(sc->q_count, 0, sizeof(uint32_t), stream));
-            k_pt_shade<<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
-                sc->q_ray[cur], sc->q_state[cur], sc->q_hit, n, sg, prm->max_num_vertices, prm->seed, sc->film,
-                sc->film_sq, sc->q_ray[1 - cur], sc->q_state[1 - cur], sc->q_count);
+            LMGPU_CUDA_TRY(cudaMemsetAsync(sc->q_count, 0, 2 * sizeof(uint32_t), stream));
+            if (nee)
+                k_pt_shade<true><<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
+                    C, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, n, p0, prm->seed, sc->q_own, sc->q_ray[1 - cur],
+                    sc->q_state[1 - cur], sc->q_count, sc->q_nray, sc->q_nrec, sc->q_npath, sc->q_count + 1);
+            else
+                k_pt_shade<false><<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
+                    C, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, n, p0, prm->seed, sc->q_own, sc->q_ray[1 - cur],
+                    sc->q_state[1 - cur], sc->q_count, sc->q_nray, sc->q_nrec, sc->q_npath, sc->q_count + 1);
             LMGPU_CUDA_TRY(cudaGetLastError());
             sc->launches += 2;  // trace + shade
-            LMGPU_CUDA_TRY(cudaMemcpyAsync(sc->h_count, sc->q_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+            LMGPU_CUDA_TRY(cudaMemcpyAsync(sc->h_count, sc->q_count, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                           stream));
             LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
-            n = *sc->h_count;
+            n = sc->h_count[0];
+            n_nee = nee ? sc->h_count[1] : 0u;
             cur = 1 - cur;
         }
+        k_pt_flush<<<(n_wave + 255) / 256, 256, 0, stream>>>(p0, np, n_wave, sc->q_own, sc->film, sc->film_sq);
+        LMGPU_CUDA_TRY(cudaGetLastError());
+        sc->launches++;
     }
     return finalize_film(sc, prm->spp, d_image, d_variance, stream);
 }

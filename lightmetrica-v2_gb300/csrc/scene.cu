@@ -54,7 +54,9 @@ int ensure_queues(lmgpu_scene* sc, uint64_t n)
     int rc;
     for (int i = 0; i < 2; i++)
         if ((rc = grow(&sc->q_ray[i], 2 * n)) || (rc = grow(&sc->q_state[i], n))) return rc;
-    if ((rc = grow(&sc->q_hit, n))) return rc;
+    if ((rc = grow(&sc->q_hit, n)) || (rc = grow(&sc->q_own, 3 * n)) || (rc = grow(&sc->q_nray, 2 * n)) ||
+        (rc = grow(&sc->q_nrec, n)) || (rc = grow(&sc->q_npath, n)) || (rc = grow(&sc->q_nhit, n)))
+        return rc;
     sc->q_cap = n;
     return LMGPU_OK;
 }
@@ -222,8 +224,8 @@ int lmgpu_scene_create(const float* tris, const int32_t* tri_prim, uint64_t ntri
     int rc = lmgpu_accel_create(&sc->accel);
     if (rc) return fail(rc);
     if (cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMallocHost((void**)&sc->h_count, sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc((void**)&sc->q_count, sizeof(uint32_t)) != cudaSuccess) {
+        cudaMallocHost((void**)&sc->h_count, 2 * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc((void**)&sc->q_count, 2 * sizeof(uint32_t)) != cudaSuccess) {
         set_error("lmgpu_scene_create: stream or buffer allocation failed");
         return fail(LMGPU_ERR_CUDA);
     }
@@ -292,6 +294,7 @@ void lmgpu_scene_destroy(lmgpu_scene* sc)
     void* ptrs[] = {sc->tris, sc->tri_prim, sc->prims, sc->film, sc->film_sq, sc->film_x, sc->film_x_sq,
                     sc->d_image, sc->d_variance,
                     sc->q_ray[0], sc->q_ray[1], sc->q_state[0], sc->q_state[1], sc->q_hit, sc->q_count,
+                    sc->q_own, sc->q_nray, sc->q_nrec, sc->q_npath, sc->q_nhit,
                     sc->light_buf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -327,6 +330,16 @@ int lmgpu_scene_accel(const lmgpu_scene* sc, const lmgpu_accel** accel)
 namespace {
 
 using RenderFn = int (*)(lmgpu_scene*, const lmgpu_pt_params*, float*, float*, cudaStream_t);
+
+int render_pt_plain(lmgpu_scene* sc, const lmgpu_pt_params* p, float* img, float* var, cudaStream_t s)
+{
+    return render_pt(sc, p, img, var, s, false);
+}
+
+int render_pt_nee(lmgpu_scene* sc, const lmgpu_pt_params* p, float* img, float* var, cudaStream_t s)
+{
+    return render_pt(sc, p, img, var, s, true);
+}
 
 int render_device(const char* name, RenderFn fn, lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image,
                   float* d_variance, void* stream)
@@ -380,13 +393,26 @@ int lmgpu_render_pt_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d
                            void* stream)
 {
     clear_error();
-    return render_device("lmgpu_render_pt_device", render_pt, sc, prm, d_image, d_variance, stream);
+    return render_device("lmgpu_render_pt_device", render_pt_plain, sc, prm, d_image, d_variance, stream);
 }
 
 int lmgpu_render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image, float* variance)
 {
     clear_error();
-    return render_host("lmgpu_render_pt", render_pt, sc, prm, image, variance);
+    return render_host("lmgpu_render_pt", render_pt_plain, sc, prm, image, variance);
+}
+
+int lmgpu_render_ptmis_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance,
+                              void* stream)
+{
+    clear_error();
+    return render_device("lmgpu_render_ptmis_device", render_pt_nee, sc, prm, d_image, d_variance, stream);
+}
+
+int lmgpu_render_ptmis(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image, float* variance)
+{
+    clear_error();
+    return render_host("lmgpu_render_ptmis", render_pt_nee, sc, prm, image, variance);
 }
 
 int lmgpu_render_bdpt_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance,

@@ -99,8 +99,14 @@ struct lmgpu_scene {
     float4* q_ray[2] = {nullptr, nullptr};
     lmgpu::PathState* q_state[2] = {nullptr, nullptr};
     lmgpu_hit* q_hit = nullptr;
-    uint32_t* q_count = nullptr;
-    uint32_t* h_count = nullptr;  // pinned host copy
+    uint32_t* q_count = nullptr;  // [0] next path queue, [1] light-sample queue
+    uint32_t* h_count = nullptr;  // pinned host copy of both
+    float* q_own = nullptr;       // [3 path] each path's contributions to its own pixel
+    // pending light samples (renderer::ptmis): shadow rays, contributions + pixel, path, hits
+    float4* q_nray = nullptr;
+    float4* q_nrec = nullptr;
+    uint32_t* q_npath = nullptr;
+    lmgpu_hit* q_nhit = nullptr;
     uint64_t q_cap = 0;
     cudaStream_t stream = nullptr;
     uint64_t launches = 0;  // kernels launched by the renderers since creation
@@ -114,7 +120,8 @@ int ensure_queues(lmgpu_scene* sc, uint64_t n);
 SceneGPU scene_view(const lmgpu_scene* sc);
 int clear_film(lmgpu_scene* sc, uint64_t npix, cudaStream_t stream);
 int finalize_film(lmgpu_scene* sc, uint64_t spp, float* d_image, float* d_variance, cudaStream_t stream);
-int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream);
+int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream,
+              bool nee);
 int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream);
 
 }  // namespace lmgpu

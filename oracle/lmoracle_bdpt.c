@@ -1,5 +1,7 @@
 /*
- * CPU oracle: renderer::bdpt (bidirectional path tracing, power heuristic).
+ * CPU oracle: renderer::bdpt (bidirectional path tracing, power heuristic)
+ * and renderer::ptmis (path tracing with next-event estimation and the
+ * balance heuristic), which share the surface interactions below.
  *
  * TEST INFRASTRUCTURE ONLY (see lmoracle.h).  Restates, in C, the estimator
  * of src/liblightmetrica/renderer/renderer_bdpt.cpp:
@@ -25,6 +27,12 @@
  *                       1 / (4 tan^2 aspect cos^3))
  *   BSDF_Diffuse, BSDF_Flesnel (delta direction), BSDF_CookTorrance, BSDF_Null
  *   GeometryTerm        renderutils.h:46-56; PDFVal conversions probability.h:55-110
+ * renderer::ptmis (src/liblightmetrica/renderer/renderer_ptmis.cpp:68-305):
+ *   at every vertex before the BSDF sample (the sensor included), one light
+ *   sample (primitive uniform, area-CDF triangle, uniform point), weighted
+ *   pdf_light / (pdf_light + pdf_bsdf) in projected solid angle (:133-190);
+ *   BSDF-sampled light hits weighted pdf_bsdf / (pdf_bsdf + pdf_light), with
+ *   pdf_light = 0 after a specular vertex (:246-270); roulette 0.5 (:285-293).
  * Scene3::Intersect / Visible through the oracle's accel::bvh_sahbin.
  * Environment lights are not part of this restatement.
  */
@@ -104,6 +112,7 @@ typedef struct {
     int W, H;
     int max_v;
     int independent_light_dir;
+    int ptmis;
     uint64_t num_samples, seed;
     int threads;
     double *sum, *sumsq;
@@ -720,6 +729,145 @@ static void* bd_worker(void* arg)
     return NULL;
 }
 
+/* Splat accumulation of one sample: contributions merged per pixel before
+ * their squares are summed, as the reference film does per sample. */
+typedef struct {
+    int n;
+    int pix[4 * MAXV];
+    double val[4 * MAXV][3];
+} splat_list;
+
+static void splat_add(splat_list* L, int pix, spd C)
+{
+    int k;
+    for (k = 0; k < L->n; k++)
+        if (L->pix[k] == pix) break;
+    if (k == L->n) {
+        if (L->n == 4 * MAXV) return;
+        L->pix[k] = pix;
+        L->val[k][0] = L->val[k][1] = L->val[k][2] = 0.0;
+        L->n++;
+    }
+    for (int c = 0; c < 3; c++) L->val[k][c] += C.c[c];
+}
+
+static int pixel_of(const bd_job* J, float rx, float ry)
+{
+    int ix = (int)(rx * (float)J->W), iy = (int)(ry * (float)J->H);
+    ix = ix < 0 ? 0 : (ix > J->W - 1 ? J->W - 1 : ix);
+    iy = iy < 0 ? 0 : (iy > J->H - 1 ? J->H - 1 : iy);
+    return iy * J->W + ix;
+}
+
+/* Renderer_PTMIS sample closure (renderer_ptmis.cpp:80-305) */
+static void* ptmis_worker(void* arg)
+{
+    void** a = (void**)arg;
+    bd_job* J = (bd_job*)a[0];
+    const int wi_ = (int)(intptr_t)a[1];
+    const int W = J->W, H = J->H;
+    double* sum = (double*)calloc((size_t)W * H * 3, sizeof(double));
+    double* sumsq = (double*)calloc((size_t)W * H * 3, sizeof(double));
+    uint64_t rng = J->seed ^ 0x3C6EF372FE94F82Bull;
+    rng = splitmix64(&rng) ^ ((uint64_t)wi_ * 0xA0761D6478BD642Full);
+    rng = splitmix64(&rng);
+    splat_list* sl = (splat_list*)malloc(sizeof(splat_list));
+    const float pdfL = 1.0f / (float)J->nlights;
+    const uint64_t b = J->num_samples * (uint64_t)wi_ / (uint64_t)J->threads;
+    const uint64_t e = J->num_samples * (uint64_t)(wi_ + 1) / (uint64_t)J->threads;
+    for (uint64_t smp = b; smp < e; smp++) {
+        sl->n = 0;
+        /* sensor: uniform raster position over the film (sensor_pinhole.cpp:79-90) */
+        pvx cur;
+        cur.p = J->eye;
+        cur.n = J->vz;
+        cur.prim = -1;
+        cur.type = T_E;
+        cur.degenerated = 1;
+        const float r0 = 2.0f * rnd(&rng) - 1.0f, r1 = 2.0f * rnd(&rng) - 1.0f;
+        const v3 we = normalize(V(J->aspect * J->tan_fov * r0, J->tan_fov * r1, -1.0f));
+        const v3 initWo = add(add(mul(J->vx, we.x), mul(J->vy, we.y)), mul(J->vz, we.z));
+        float rx0, ry0;
+        if (!raster_pos(J, initWo, &rx0, &ry0)) continue;
+        const int pix0 = pixel_of(J, rx0, ry0);
+        spd thr = S1(1.0f);
+        v3 wi = zero3();
+        int nv = 1;
+        for (;;) {
+            if (J->max_v != -1 && nv >= J->max_v) break;
+            /* direct light sampling (:131-193) */
+            {
+                const float us = rnd(&rng), u0 = rnd(&rng), u1 = rnd(&rng);
+                pvx L;
+                sample_light_pos(J, us, u0, u1, &L, NULL);
+                L.type = T_L;
+                const v3 ppL = normalize(sub(L.p, cur.p));
+                const spd fsE = eval_dir(J, &cur, cur.type, wi, ppL, DIR_EL, 1);
+                const spd fsL = eval_dir(J, &L, T_L, zero3(), mul(ppL, -1.0f), DIR_LE, 0);
+                const float G = geometry_term(&cur, &L);
+                const float pdfPL = J->light_inv_area[J->prim_light[L.prim]];
+                spd C = smul(thr, smul(fsE, fsL));
+                C = sscale(C, G / pdfL / pdfPL);
+                if (!sblack(C) && visible(J, cur.p, L.p)) {
+                    const float pdfDL = pdfPL / G * pdfL;
+                    const float pdfB = pdf_dir(J, &cur, cur.type, wi, ppL, 1);
+                    const float w = pdfDL / (pdfDL + pdfB);
+                    int pix = pix0;
+                    if (cur.type == T_E) {
+                        float rx, ry;
+                        if (raster_pos(J, ppL, &rx, &ry)) pix = pixel_of(J, rx, ry);
+                    }
+                    splat_add(sl, pix, sscale(C, w));
+                }
+            }
+            /* next direction (:197-224) */
+            v3 wo;
+            if (cur.type == T_E) {
+                wo = initWo;
+            } else {
+                const float u0 = rnd(&rng), u1 = rnd(&rng), uc = rnd(&rng);
+                if (!sample_dir(J, &cur, wi, u0, u1, uc, &wo)) break;
+            }
+            const float pdfD = pdf_dir(J, &cur, cur.type, wi, wo, 0);
+            const spd fs = eval_dir(J, &cur, cur.type, wi, wo, DIR_EL, 0);
+            if (sblack(fs)) break;
+            thr = smul(thr, sscale(fs, 1.0f / pdfD));
+            pvx hit;
+            if (!trace(J, cur.p, wo, &hit)) break;
+            /* BSDF-sampled light hit (:240-273) */
+            if (J->prims[hit.prim].is_light) {
+                const float pdfDL = (cur.type & T_S)
+                                        ? 0.0f
+                                        : J->light_inv_area[J->prim_light[hit.prim]] / geometry_term(&hit, &cur) * pdfL;
+                const float w = pdfD / (pdfD + pdfDL);
+                pvx hl = hit;
+                hl.type = T_L;
+                const spd Le = eval_dir(J, &hl, T_L, zero3(), mul(wo, -1.0f), DIR_EL, 0);
+                const spd C = smul(thr, Le);
+                if (!sblack(C)) splat_add(sl, pix0, sscale(C, w));
+            }
+            /* roulette (:285-293) */
+            if (rnd(&rng) > 0.5f) break;
+            thr = sscale(thr, 2.0f);
+            cur = hit;
+            wi = mul(wo, -1.0f);
+            nv++;
+        }
+        for (int k = 0; k < sl->n; k++)
+            for (int c = 0; c < 3; c++) {
+                sum[3 * (size_t)sl->pix[k] + c] += sl->val[k][c];
+                sumsq[3 * (size_t)sl->pix[k] + c] += sl->val[k][c] * sl->val[k][c];
+            }
+    }
+    pthread_mutex_lock(&J->lock);
+    for (size_t i = 0; i < (size_t)W * H * 3; i++) { J->sum[i] += sum[i]; J->sumsq[i] += sumsq[i]; }
+    pthread_mutex_unlock(&J->lock);
+    free(sl);
+    free(sum);
+    free(sumsq);
+    return NULL;
+}
+
 uint64_t lmo_render_bdpt(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims, int nprims,
                          const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices, uint64_t seed,
                          int threads, double* sum, double* sumsq)
@@ -728,6 +876,15 @@ uint64_t lmo_render_bdpt(const float* tris, const int32_t* tri_prim, size_t ntri
                               sum, sumsq, 0);
 }
 
+uint64_t lmo_render_ptmis(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims, int nprims,
+                          const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices, uint64_t seed,
+                          int threads, double* sum, double* sumsq)
+{
+    return lmo_render_bdpt_ex(tris, tri_prim, ntri, prims, nprims, cam, num_samples, max_num_vertices, seed, threads,
+                              sum, sumsq, -1);
+}
+
+/* independent_light_dir: 0 / 1 select the BDPT variants; -1 runs renderer::ptmis */
 uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
                             uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir)
@@ -788,7 +945,8 @@ uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t n
     J.W = cam->width;
     J.H = cam->height;
     J.max_v = max_num_vertices;
-    J.independent_light_dir = independent_light_dir;
+    J.independent_light_dir = independent_light_dir > 0;
+    J.ptmis = independent_light_dir < 0;
     J.num_samples = num_samples;
     J.seed = seed;
     J.threads = threads < 1 ? 1 : threads;
@@ -806,7 +964,7 @@ uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t n
         for (int i = 0; i < J.threads; i++) {
             args[2 * i] = &J;
             args[2 * i + 1] = (void*)(intptr_t)i;
-            pthread_create(&th[i], &attr, bd_worker, &args[2 * i]);
+            pthread_create(&th[i], &attr, J.ptmis ? ptmis_worker : bd_worker, &args[2 * i]);
         }
         for (int i = 0; i < J.threads; i++) pthread_join(th[i], NULL);
     }

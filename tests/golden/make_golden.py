@@ -26,6 +26,11 @@ Fixtures written:
       which renderer::bdpt does not sample) rendered by the reference's own
       renderer::bdpt at 32x32 with max_num_vertices 10: films and
       per-pixel variances in single and double precision.
+  cornell_ptmis.npz, materials_ptmis.npz
+      The same two boxes (no environment light) rendered by the reference's
+      own renderer::ptmis (next-event estimation, balance heuristic) at
+      64x64, 16,384 samples per pixel, max_num_vertices 9, single and double
+      precision.
   soup_small.npz
       A seeded three-primitive scene (random triangle soup, heightfield,
       duplicated triangles for exact-t ties, zero-area triangles) and rays
@@ -238,6 +243,12 @@ def main() -> None:
         sc.pop("env", None)
         np.savez_compressed(os.path.join(HERE, "materials_bdpt.npz"),
                             **pt_case(sc, 32768, 20240901, "bdpt", 10))
+    for name, make in (("cornell_ptmis", scenes.cornell_box), ("materials_ptmis", scenes.cornell_materials)):
+        if want(name):
+            sc = make(64, 64)
+            sc.pop("env", None)
+            np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                                **pt_case(sc, 16384, 20241001 if name.startswith("cornell") else 20241101, "ptmis", 9))
     print("fixtures written to", HERE)
 
 

@@ -60,10 +60,11 @@ def test_null_arguments_rejected(gpu_lib):
     assert L.lmgpu_last_error()
 
 
-@pytest.mark.parametrize("plugin", ["accel_cuda", "renderer_pt_cuda", "renderer_bdpt_cuda"])
+@pytest.mark.parametrize("plugin", ["accel_cuda", "renderer_pt_cuda", "renderer_ptmis_cuda", "renderer_bdpt_cuda"])
 def test_reference_plugin_compiles_against_reference_headers(repo_dir, plugin):
     """plugin/*.cpp, the bindings a maintainer adds to the reference tree
-    (accel::cuda, renderer::pt_cuda, renderer::bdpt_cuda), compile against the
+    (accel::cuda, renderer::pt_cuda, renderer::ptmis_cuda,
+    renderer::bdpt_cuda), compile against the
     reference's own headers (x86-64 only: the reference forces SSE)."""
     import platform
     import shutil
