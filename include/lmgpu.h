@@ -210,6 +210,17 @@ int lmgpu_render_ptmis(lmgpu_scene* scene, const lmgpu_pt_params* params, float*
 int lmgpu_render_ptmis_device(lmgpu_scene* scene, const lmgpu_pt_params* params, float* d_image, float* d_variance,
                               void* stream);
 
+/* Renders the scene with path tracing by light samples only: one light
+ * sample per vertex (the sensor included) with weight 1, and no emission
+ * counted on BSDF-sampled hits.  Stands in for Renderer::Render of
+ * renderer::ptdirect (src/liblightmetrica/renderer/renderer_ptdirect.cpp:72-291).
+ * Same scene requirements as lmgpu_render_ptmis. */
+int lmgpu_render_ptdirect(lmgpu_scene* scene, const lmgpu_pt_params* params, float* image, float* variance);
+
+/* As lmgpu_render_ptdirect into device buffers on `stream`. */
+int lmgpu_render_ptdirect_device(lmgpu_scene* scene, const lmgpu_pt_params* params, float* d_image,
+                                 float* d_variance, void* stream);
+
 /* Renders the scene with bidirectional path tracing (all (s, t) strategies,
  * power-heuristic MIS) and writes the film as lmgpu_render_pt does.  Stands
  * in for Renderer::Render of renderer::bdpt

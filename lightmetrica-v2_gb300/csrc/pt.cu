@@ -1,4 +1,5 @@
-// Wavefront path tracers: the GPU forms of renderer::pt and renderer::ptmis.
+// Wavefront path tracers: the GPU forms of renderer::pt, renderer::ptmis and
+// renderer::ptdirect.
 //
 // renderer::pt (src/liblightmetrica/renderer/renderer_pt.cpp:68-231): a path
 // starts at the pinhole sensor with throughput 1 (importance / pdf), extends
@@ -13,8 +14,10 @@
 // contribution fs G V Le / (pdf_light pdf_area) is weighted by the balance
 // heuristic pdf_light / (pdf_light + pdf_bsdf) in projected solid angle, and
 // BSDF-sampled light hits by pdf_bsdf / (pdf_bsdf + pdf_light), with
-// pdf_light = 0 after a specular vertex.  Environment lights are not sampled
-// by this form (the entry point rejects scenes that have one).
+// pdf_light = 0 after a specular vertex.  renderer::ptdirect
+// (renderer_ptdirect.cpp:72-291) keeps the light samples with weight 1 and
+// counts no BSDF-sampled emission at all.  Environment lights are not
+// sampled by these two forms (the entry points reject scenes that have one).
 //
 // BSDFs: bsdf::null, bsdf::diffuse, bsdf::flesnel (dielectric) and
 // bsdf::cook_torrance (GGX conductor); lights: light::area on primitives and a
@@ -45,6 +48,9 @@ namespace {
 
 constexpr int kShadeThreads = 256;
 
+// Estimators of the wavefront tracer.
+enum : int { MODE_PT = 0, MODE_PTMIS = 1, MODE_PTDIRECT = 2 };
+
 // PathState.id.w holds, for ptmis, the BSDF pdf of the last sampled
 // direction times |cos| at the vertex it left (projected solid angle to
 // solid angle at that end; 1 for the pinhole), or -1 after a specular vertex.
@@ -58,6 +64,7 @@ __device__ __forceinline__ float light_pdf_proj(const Ctx& C, int prim, float d2
 // A light sample from vertex v (Renderer_PTMIS, renderer_ptmis.cpp:131-193):
 // the weighted contribution (before visibility) and the light point, or
 // false when it is black.
+template <bool MIS>
 __device__ __forceinline__ bool nee_sample(const Ctx& C, const PV& v, int type, float3 wi, float us, float a0,
                                            float a1, const float thr[3], float c[3], PV& L, float3& ppL)
 {
@@ -70,9 +77,12 @@ __device__ __forceinline__ bool nee_sample(const Ctx& C, const PV& v, int type, 
     const float G = geometry_term(v, L);
     const float pdfL = 1.0f / (float)C.lights.count;
     const float pdfPL = C.lights.inv_area[C.lights.prim_light[L.prim]];
-    const float pdfDL = pdfPL / G * pdfL;
-    const float pdfB = pdf_dir(C, v, type, wi, ppL);
-    const float w = pdfDL / (pdfDL + pdfB);
+    float w = 1.0f;
+    if (MIS) {
+        const float pdfDL = pdfPL / G * pdfL;
+        const float pdfB = pdf_dir(C, v, type, wi, ppL);
+        w = pdfDL / (pdfDL + pdfB);
+    }
     bool any = false;
     for (int k = 0; k < 3; k++) {
         c[k] = thr[k] * fsE.c[k] * G * fsL.c[k] / pdfL / pdfPL * w;
@@ -114,7 +124,7 @@ __device__ __forceinline__ uint32_t pixel_at(const CameraGPU& cam, float rx, flo
     return (uint32_t)iy * (uint32_t)cam.width + (uint32_t)ix;
 }
 
-template <bool NEE>
+template <int MODE>
 __global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p0, uint32_t n, uint32_t seed,
                                                                float4* __restrict__ rays,
                                                                PathState* __restrict__ state,
@@ -123,6 +133,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p
                                                                uint32_t* __restrict__ npath,
                                                                uint32_t* __restrict__ ncount)
 {
+    constexpr bool NEE = MODE != MODE_PT;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const CameraGPU& cam = C.cam;
     bool has_nee = false;
@@ -154,7 +165,8 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p
             const Philox4x32 q = philox4x32_10((uint32_t)p, (uint32_t)(p >> 32), 0u, 1u, seed, kKeyCamera);
             const float one[3] = {1.0f, 1.0f, 1.0f};
             float3 ppL;
-            has_nee = nee_sample(C, v, T_E, zero3(), u01(q.v[0]), u01(q.v[1]), u01(q.v[2]), one, c, L, ppL);
+            has_nee = nee_sample<MODE == MODE_PTMIS>(C, v, T_E, zero3(), u01(q.v[0]), u01(q.v[1]), u01(q.v[2]),
+                                                     one, c, L, ppL);
             if (has_nee) {
                 float px, py;
                 raster_pos(cam, ppL, px, py);
@@ -165,7 +177,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p
     if (NEE) append_nee(has_nee, v, L, c, nee_pix, i, nrays, nrec, npath, ncount);
 }
 
-template <bool NEE>
+template <int MODE>
 __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(Ctx C, const float4* __restrict__ rays,
                                                             const PathState* __restrict__ state,
                                                             const lmgpu_hit* __restrict__ hits, uint32_t n,
@@ -177,6 +189,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(Ctx C, const float4*
                                                             uint32_t* __restrict__ npath,
                                                             uint32_t* __restrict__ ncount)
 {
+    constexpr bool NEE = MODE != MODE_PT;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool keep = false, has_nee = false;
     float4 nr0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), nr1 = nr0;
@@ -212,11 +225,11 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(Ctx C, const float4*
             v.degen = 0;
             uint32_t nv = s.id.z;
             const float cos_l = -dot3(d, v.n);
-            if (P.is_light && cos_l > 0.0f) {
+            if (MODE != MODE_PTDIRECT && P.is_light && cos_l > 0.0f) {
                 // throughput * Le(-d) * EvaluatePosition (= 1), renderer_pt.cpp:183-194;
                 // ptmis: weight pdf_bsdf / (pdf_bsdf + pdf_light), renderer_ptmis.cpp:246-270
                 float w = 1.0f;
-                if (NEE) {
+                if (MODE == MODE_PTMIS) {
                     const float q = __uint_as_float(s.id.w);
                     w = q < 0.0f ? 1.0f : q / (q + light_pdf_proj(C, v.prim, h.t * h.t, cos_l));
                 }
@@ -234,7 +247,8 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(Ctx C, const float4*
                 if (more && NEE) {
                     const Philox4x32 q = philox4x32_10(s.id.x, s.id.y, nv, 1u, seed, kKeyBounce);
                     float3 ppL;
-                    has_nee = nee_sample(C, v, v.type, wi, u01(q.v[0]), u01(q.v[1]), u01(q.v[2]), thr, c, L, ppL);
+                    has_nee = nee_sample<MODE == MODE_PTMIS>(C, v, v.type, wi, u01(q.v[0]), u01(q.v[1]),
+                                                             u01(q.v[2]), thr, c, L, ppL);
                 }
                 float3 wo;
                 float f[3];
@@ -322,18 +336,20 @@ __global__ void k_pt_flush(uint64_t p0, uint32_t npix, uint32_t n, const float* 
 }  // namespace
 
 int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream,
-              bool nee)
+              int mode)
 {
+    const bool nee = mode != MODE_PT;
+    const char* name = mode == MODE_PTMIS ? "lmgpu_render_ptmis" : "lmgpu_render_ptdirect";
     const uint32_t W = (uint32_t)sc->cam.width, H = (uint32_t)sc->cam.height;
     const uint64_t npix = (uint64_t)W * H;
     const uint64_t total = npix * prm->spp;
     if (total == 0) return LMGPU_OK;
     if (nee && sc->lights.count == 0) {
-        set_error("lmgpu_render_ptmis: the scene has no area light");
+        set_error(std::string(name) + ": the scene has no area light");
         return LMGPU_ERR_INVALID;
     }
     if (nee && sc->has_env) {
-        set_error("lmgpu_render_ptmis: environment lights are not sampled by this renderer");
+        set_error(std::string(name) + ": environment lights are not sampled by this renderer");
         return LMGPU_ERR_INVALID;
     }
     int rc = clear_film(sc, npix, stream);
@@ -351,14 +367,13 @@ int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float
         uint32_t n = (uint32_t)((total - p0) < kWave ? (total - p0) : kWave);
         const uint32_t n_wave = n;
         LMGPU_CUDA_TRY(cudaMemsetAsync(sc->q_count, 0, 2 * sizeof(uint32_t), stream));
-        if (nee)
-            k_pt_generate<true><<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
+        {
+            auto gen = mode == MODE_PTMIS ? k_pt_generate<MODE_PTMIS>
+                                          : (mode == MODE_PTDIRECT ? k_pt_generate<MODE_PTDIRECT> : k_pt_generate<MODE_PT>);
+            gen<<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
                 C, p0, n, prm->seed, sc->q_ray[0], sc->q_state[0], sc->q_own, sc->q_nray, sc->q_nrec, sc->q_npath,
                 sc->q_count + 1);
-        else
-            k_pt_generate<false><<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
-                C, p0, n, prm->seed, sc->q_ray[0], sc->q_state[0], sc->q_own, sc->q_nray, sc->q_nrec, sc->q_npath,
-                sc->q_count + 1);
+        }
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
         int cur = 0;
@@ -383,14 +398,13 @@ int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float
             rc = launch_trace(sc->accel, sc->q_ray[cur], sc->q_hit, n, false, false, stream);
             if (rc) return rc;
             LMGPU_CUDA_TRY(cudaMemsetAsync(sc->q_count, 0, 2 * sizeof(uint32_t), stream));
-            if (nee)
-                k_pt_shade<true><<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
+            {
+                auto shade = mode == MODE_PTMIS ? k_pt_shade<MODE_PTMIS>
+                                                : (mode == MODE_PTDIRECT ? k_pt_shade<MODE_PTDIRECT> : k_pt_shade<MODE_PT>);
+                shade<<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
                     C, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, n, p0, prm->seed, sc->q_own, sc->q_ray[1 - cur],
                     sc->q_state[1 - cur], sc->q_count, sc->q_nray, sc->q_nrec, sc->q_npath, sc->q_count + 1);
-            else
-                k_pt_shade<false><<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
-                    C, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, n, p0, prm->seed, sc->q_own, sc->q_ray[1 - cur],
-                    sc->q_state[1 - cur], sc->q_count, sc->q_nray, sc->q_nrec, sc->q_npath, sc->q_count + 1);
+            }
             LMGPU_CUDA_TRY(cudaGetLastError());
             sc->launches += 2;  // trace + shade
             LMGPU_CUDA_TRY(cudaMemcpyAsync(sc->h_count, sc->q_count, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost,

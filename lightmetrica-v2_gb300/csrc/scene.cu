@@ -333,12 +333,17 @@ using RenderFn = int (*)(lmgpu_scene*, const lmgpu_pt_params*, float*, float*, c
 
 int render_pt_plain(lmgpu_scene* sc, const lmgpu_pt_params* p, float* img, float* var, cudaStream_t s)
 {
-    return render_pt(sc, p, img, var, s, false);
+    return render_pt(sc, p, img, var, s, 0);
 }
 
 int render_pt_nee(lmgpu_scene* sc, const lmgpu_pt_params* p, float* img, float* var, cudaStream_t s)
 {
-    return render_pt(sc, p, img, var, s, true);
+    return render_pt(sc, p, img, var, s, 1);
+}
+
+int render_pt_direct(lmgpu_scene* sc, const lmgpu_pt_params* p, float* img, float* var, cudaStream_t s)
+{
+    return render_pt(sc, p, img, var, s, 2);
 }
 
 int render_device(const char* name, RenderFn fn, lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image,
@@ -413,6 +418,19 @@ int lmgpu_render_ptmis(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image
 {
     clear_error();
     return render_host("lmgpu_render_ptmis", render_pt_nee, sc, prm, image, variance);
+}
+
+int lmgpu_render_ptdirect_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance,
+                                 void* stream)
+{
+    clear_error();
+    return render_device("lmgpu_render_ptdirect_device", render_pt_direct, sc, prm, d_image, d_variance, stream);
+}
+
+int lmgpu_render_ptdirect(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image, float* variance)
+{
+    clear_error();
+    return render_host("lmgpu_render_ptdirect", render_pt_direct, sc, prm, image, variance);
 }
 
 int lmgpu_render_bdpt_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance,

@@ -120,8 +120,9 @@ int ensure_queues(lmgpu_scene* sc, uint64_t n);
 SceneGPU scene_view(const lmgpu_scene* sc);
 int clear_film(lmgpu_scene* sc, uint64_t npix, cudaStream_t stream);
 int finalize_film(lmgpu_scene* sc, uint64_t spp, float* d_image, float* d_variance, cudaStream_t stream);
+// mode: 0 renderer::pt, 1 renderer::ptmis, 2 renderer::ptdirect
 int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream,
-              bool nee);
+              int mode);
 int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream);
 
 }  // namespace lmgpu

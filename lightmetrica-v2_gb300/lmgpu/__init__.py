@@ -93,6 +93,8 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_render_pt_device.argtypes = [vp, vp, vp, vp, vp]
     L.lmgpu_render_bdpt.argtypes = [vp, vp, vp, vp]
     L.lmgpu_render_ptmis.argtypes = [vp, vp, vp, vp]
+    L.lmgpu_render_ptdirect.argtypes = [vp, vp, vp, vp]
+    L.lmgpu_render_ptdirect_device.argtypes = [vp, vp, vp, vp, vp]
     L.lmgpu_render_ptmis_device.argtypes = [vp, vp, vp, vp, vp]
     L.lmgpu_scene_launch_count.argtypes = [vp, ctypes.POINTER(u64)]
     L.lmgpu_render_bdpt_device.argtypes = [vp, vp, vp, vp, vp]
@@ -100,7 +102,8 @@ def lib() -> ctypes.CDLL:
                  "lmgpu_trace", "lmgpu_trace_device", "lmgpu_trace_stats_device", "lmgpu_accel_check",
                  "lmgpu_trace_static_scene", "lmgpu_accel_set_tuning", "lmgpu_scene_create", "lmgpu_scene_accel",
                  "lmgpu_render_pt", "lmgpu_render_pt_device", "lmgpu_render_bdpt", "lmgpu_render_bdpt_device", "lmgpu_scene_launch_count",
-                 "lmgpu_render_ptmis", "lmgpu_render_ptmis_device",
+                 "lmgpu_render_ptmis", "lmgpu_render_ptmis_device", "lmgpu_render_ptdirect",
+                 "lmgpu_render_ptdirect_device",
                  "lmgpu_scene_set_environment"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
@@ -280,6 +283,14 @@ class Scene:
                             seed: int = 0, stream: int = 0) -> None:
         prm = PtParams(spp, max_num_vertices, seed)
         _check(lib().lmgpu_render_ptmis_device(self._h, ctypes.byref(prm), d_image, d_variance, stream))
+
+    def render_ptdirect(self, spp: int, max_num_vertices: int = -1, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        """renderer::ptdirect: film (H, W, 3) and per-pixel variance of the estimate."""
+        img = np.empty((self.height, self.width, 3), np.float32)
+        var = np.empty((self.height, self.width, 3), np.float32)
+        prm = PtParams(spp, max_num_vertices, seed)
+        _check(lib().lmgpu_render_ptdirect(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
+        return img, var
 
     def launch_count(self) -> int:
         """Kernels launched by the renderers for this scene so far."""

@@ -1,0 +1,41 @@
+/*
+    Accel3Batch -- the batch query interface a GPU accel adds to the
+    reference's Accel3 (include/lightmetrica/accel3.h:39-71).  Not part of
+    the reference: its renderers call Accel3::Intersect once per ray; callers
+    aware of this interface hand the accel whole ray batches instead.
+
+    Slot numbering follows the reference's cumulative interface IDs
+    (Accel: Initialize = 0, Build = 1; Accel3: Intersect = 2), so
+    IntersectBatch occupies slot 3.
+*/
+#pragma once
+
+#include <lightmetrica/accel3.h>
+
+LM_NAMESPACE_BEGIN
+
+class Accel3Batch : public Accel3
+{
+public:
+
+    LM_INTERFACE_CLASS(Accel3Batch, Accel3, 1);
+
+public:
+
+    Accel3Batch() = default;
+    LM_DISABLE_COPY_AND_MOVE(Accel3Batch);
+
+public:
+
+    /*!
+        Closest (anyHit = false) or any (anyHit = true) hit of n rays.
+        rays: n x (ox, oy, oz, tmin, dx, dy, dz, tmax) floats, host memory;
+        hits: n x (float t, int32 prim, float b1, float b2), prim = -1 for a
+        miss, with (b1, b2) the barycentrics of vertices 2 and 3 of global
+        triangle prim (the order of accel_naive.cpp:62-87).
+    */
+    LM_INTERFACE_F(0, IntersectBatch, bool(const float* rays, void* hits, long long n, bool anyHit));
+
+};
+
+LM_NAMESPACE_END

@@ -15,6 +15,7 @@
       Accel::Initialize      include/lightmetrica/accel.h:67
       Accel::Build           include/lightmetrica/accel.h:79
       Accel3::Intersect      include/lightmetrica/accel3.h:68
+      Accel3Batch::IntersectBatch  accel3_batch.h (this plugin's batch extension)
     Geometry is read the way accel_naive.cpp:59-90 reads it (primitive
     transform applied to every vertex, global triangle id = faces of
     primitive 0, then primitive 1, ...), and hits are turned into an
@@ -22,7 +23,7 @@
     (intersectionutils.h:59), exactly as the in-tree accels do.
 */
 #include <pch.h>
-#include <lightmetrica/accel3.h>
+#include "accel3_batch.h"
 #include <lightmetrica/scene3.h>
 #include <lightmetrica/primitive.h>
 #include <lightmetrica/trianglemesh.h>
@@ -36,11 +37,11 @@
 
 LM_NAMESPACE_BEGIN
 
-class Accel_CUDA final : public Accel3
+class Accel_CUDA final : public Accel3Batch
 {
 public:
 
-    LM_IMPL_CLASS(Accel_CUDA, Accel3);
+    LM_IMPL_CLASS(Accel_CUDA, Accel3Batch);
 
 public:
 
@@ -114,14 +115,17 @@ public:
         return true;
     };
 
-public:
-
-    // Batch query for GPU-aware callers: n rays (ox,oy,oz,tmin,dx,dy,dz,tmax)
-    // in host memory, one lmgpu_hit per ray.  Not part of the Accel3 vtable.
-    auto IntersectBatch(const float* rays, lmgpu_hit* hits, size_t n, bool anyHit) const -> bool
+    // Accel3Batch::IntersectBatch (slot 3): n rays in host memory, one
+    // lmgpu_hit per ray.
+    LM_IMPL_F(IntersectBatch) = [this](const float* rays, void* hits, long long n, bool anyHit) -> bool
     {
-        return lmgpu_trace(accel_, rays, hits, (uint64_t)n, anyHit ? 1 : 0) == LMGPU_OK;
-    }
+        if (lmgpu_trace(accel_, rays, static_cast<lmgpu_hit*>(hits), (uint64_t)n, anyHit ? 1 : 0) != LMGPU_OK)
+        {
+            LM_LOG_ERROR(std::string("accel::cuda: ") + lmgpu_last_error());
+            return false;
+        }
+        return true;
+    };
 
 private:
 

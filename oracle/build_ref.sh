@@ -40,7 +40,7 @@ FLAGS="-std=c++14 -O3 -msse4.2 -ffp-contract=off -w"
 L="$REF/src/liblightmetrica"
 
 ACCEL_SRCS=("$L/accel/accel_naive.cpp" "$L/accel/accel_bvh_sahbin.cpp" "$L/accel/accel_qbvh.cpp" "$HERE/refharness/ref_runtime.cpp")
-RENDER_SRCS=("$L/renderer/renderer_pt.cpp" "$L/renderer/renderer_bdpt.cpp" "$L/renderer/renderer_ptmis.cpp" "$L/asset/bsdf/bsdf_diffuse.cpp" "$L/asset/bsdf/bsdf_null.cpp"
+RENDER_SRCS=("$L/renderer/renderer_pt.cpp" "$L/renderer/renderer_bdpt.cpp" "$L/renderer/renderer_ptmis.cpp" "$L/renderer/renderer_ptdirect.cpp" "$L/asset/bsdf/bsdf_diffuse.cpp" "$L/asset/bsdf/bsdf_null.cpp"
              "$L/asset/bsdf/bsdf_flesnel.cpp" "$L/asset/bsdf/bsdf_cooktorrance.cpp"
              "$L/asset/light/light_area.cpp" "$L/asset/light/light_env.cpp" "$L/asset/sensor/sensor_pinhole.cpp"
              "$L/random.cpp" "$HERE/refharness/ref_render_cli.cpp")

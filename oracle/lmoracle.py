@@ -59,6 +59,8 @@ def lib() -> ctypes.CDLL:
         L.lmo_render_bdpt_ex.restype = ctypes.c_uint64
         L.lmo_render_ptmis.argtypes = L.lmo_render_bdpt.argtypes
         L.lmo_render_ptmis.restype = ctypes.c_uint64
+        L.lmo_render_ptdirect.argtypes = L.lmo_render_bdpt.argtypes
+        L.lmo_render_ptdirect.restype = ctypes.c_uint64
         _lib = L
     return _lib
 
@@ -291,9 +293,10 @@ def render_bdpt(scene: dict, num_samples: int, max_num_vertices: int, seed: int,
     return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}
 
 
-def render_ptmis(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int) -> dict:
-    """The oracle's renderer::ptmis (NEE + balance heuristic, area lights):
-    film (H, W, 3) and per-pixel variance."""
+def render_ptmis(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,
+                 direct_only: bool = False) -> dict:
+    """The oracle's renderer::ptmis (NEE + balance heuristic, area lights), or
+    with direct_only renderer::ptdirect: film (H, W, 3) and per-pixel variance."""
     tris = np.ascontiguousarray(np.concatenate([p["tris"] for p in scene["prims"]]), dtype=np.float32)
     tri_prim = np.concatenate([np.full(p["tris"].shape[0], i, np.int32) for i, p in enumerate(scene["prims"])])
     W, H = scene["camera"]["width"], scene["camera"]["height"]
@@ -301,8 +304,9 @@ def render_ptmis(scene: dict, num_samples: int, max_num_vertices: int, seed: int
     q = np.zeros((H, W, 3), np.float64)
     prims = scene_prims(scene)
     cam = scene_camera(scene)
-    lib().lmo_render_ptmis(tris.ctypes.data, tri_prim.ctypes.data, tris.shape[0], ctypes.addressof(prims),
-                           len(scene["prims"]), ctypes.addressof(cam), num_samples, max_num_vertices, seed, threads,
-                           s.ctypes.data, q.ctypes.data)
+    fn = lib().lmo_render_ptdirect if direct_only else lib().lmo_render_ptmis
+    fn(tris.ctypes.data, tri_prim.ctypes.data, tris.shape[0], ctypes.addressof(prims),
+       len(scene["prims"]), ctypes.addressof(cam), num_samples, max_num_vertices, seed, threads,
+       s.ctypes.data, q.ctypes.data)
     img = s * (W * H / num_samples)
     return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}

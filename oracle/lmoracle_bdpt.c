@@ -33,6 +33,8 @@
  *   pdf_light / (pdf_light + pdf_bsdf) in projected solid angle (:133-190);
  *   BSDF-sampled light hits weighted pdf_bsdf / (pdf_bsdf + pdf_light), with
  *   pdf_light = 0 after a specular vertex (:246-270); roulette 0.5 (:285-293).
+ * renderer::ptdirect (renderer_ptdirect.cpp:72-291): the same light samples
+ *   with weight 1, and no emission counted on BSDF-sampled hits.
  * Scene3::Intersect / Visible through the oracle's accel::bvh_sahbin.
  * Environment lights are not part of this restatement.
  */
@@ -112,7 +114,7 @@ typedef struct {
     int W, H;
     int max_v;
     int independent_light_dir;
-    int ptmis;
+    int ptmis;     /* 1: renderer::ptmis, 2: renderer::ptdirect */
     uint64_t num_samples, seed;
     int threads;
     double *sum, *sumsq;
@@ -759,7 +761,8 @@ static int pixel_of(const bd_job* J, float rx, float ry)
     return iy * J->W + ix;
 }
 
-/* Renderer_PTMIS sample closure (renderer_ptmis.cpp:80-305) */
+/* Renderer_PTMIS sample closure (renderer_ptmis.cpp:80-305); with
+ * J->ptmis == 2 the Renderer_PTDirect one (renderer_ptdirect.cpp:84-276). */
 static void* ptmis_worker(void* arg)
 {
     void** a = (void**)arg;
@@ -811,7 +814,7 @@ static void* ptmis_worker(void* arg)
                 if (!sblack(C) && visible(J, cur.p, L.p)) {
                     const float pdfDL = pdfPL / G * pdfL;
                     const float pdfB = pdf_dir(J, &cur, cur.type, wi, ppL, 1);
-                    const float w = pdfDL / (pdfDL + pdfB);
+                    const float w = J->ptmis == 2 ? 1.0f : pdfDL / (pdfDL + pdfB);
                     int pix = pix0;
                     if (cur.type == T_E) {
                         float rx, ry;
@@ -835,7 +838,7 @@ static void* ptmis_worker(void* arg)
             pvx hit;
             if (!trace(J, cur.p, wo, &hit)) break;
             /* BSDF-sampled light hit (:240-273) */
-            if (J->prims[hit.prim].is_light) {
+            if (J->ptmis == 1 && J->prims[hit.prim].is_light) {
                 const float pdfDL = (cur.type & T_S)
                                         ? 0.0f
                                         : J->light_inv_area[J->prim_light[hit.prim]] / geometry_term(&hit, &cur) * pdfL;
@@ -884,7 +887,16 @@ uint64_t lmo_render_ptmis(const float* tris, const int32_t* tri_prim, size_t ntr
                               sum, sumsq, -1);
 }
 
-/* independent_light_dir: 0 / 1 select the BDPT variants; -1 runs renderer::ptmis */
+uint64_t lmo_render_ptdirect(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
+                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
+                             uint64_t seed, int threads, double* sum, double* sumsq)
+{
+    return lmo_render_bdpt_ex(tris, tri_prim, ntri, prims, nprims, cam, num_samples, max_num_vertices, seed, threads,
+                              sum, sumsq, -2);
+}
+
+/* independent_light_dir: 0 / 1 select the BDPT variants; -1 runs
+ * renderer::ptmis, -2 renderer::ptdirect */
 uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
                             uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir)
@@ -946,7 +958,7 @@ uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t n
     J.H = cam->height;
     J.max_v = max_num_vertices;
     J.independent_light_dir = independent_light_dir > 0;
-    J.ptmis = independent_light_dir < 0;
+    J.ptmis = independent_light_dir < 0 ? -independent_light_dir : 0;
     J.num_samples = num_samples;
     J.seed = seed;
     J.threads = threads < 1 ? 1 : threads;

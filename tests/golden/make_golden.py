@@ -31,6 +31,10 @@ Fixtures written:
       own renderer::ptmis (next-event estimation, balance heuristic) at
       64x64, 16,384 samples per pixel, max_num_vertices 9, single and double
       precision.
+  cornell_ptdirect.npz
+      The Cornell box rendered by the reference's own renderer::ptdirect
+      (light samples only) at 64x64, 16,384 samples per pixel,
+      max_num_vertices 9, single and double precision.
   soup_small.npz
       A seeded three-primitive scene (random triangle soup, heightfield,
       duplicated triangles for exact-t ties, zero-area triangles) and rays
@@ -249,6 +253,9 @@ def main() -> None:
             sc.pop("env", None)
             np.savez_compressed(os.path.join(HERE, name + ".npz"),
                                 **pt_case(sc, 16384, 20241001 if name.startswith("cornell") else 20241101, "ptmis", 9))
+    if want("cornell_ptdirect"):
+        np.savez_compressed(os.path.join(HERE, "cornell_ptdirect.npz"),
+                            **pt_case(scenes.cornell_box(64, 64), 16384, 20241201, "ptdirect", 9))
     print("fixtures written to", HERE)
 
 

@@ -1,5 +1,5 @@
 """renderer::ptmis on the GPU (lmgpu_render_ptmis: next-event estimation,
-balance heuristic) against the reference's own renderer::ptmis
+balance heuristic) and renderer::ptdirect (lmgpu_render_ptdirect) against the reference's own renderer::ptmis
 (double-precision build, tests/golden/*_ptmis.npz) and the oracle, per pixel
 within the statistical bar of tests/imgcheck.py."""
 import os
@@ -28,6 +28,16 @@ def test_ptmis_matches_reference_film(gpu_lib, golden_dir, name):
     t = img.astype(np.float64).sum(axis=(0, 1))
     t32 = z["ref_image"].astype(np.float64).sum(axis=(0, 1))
     assert np.all(np.abs(t / t32 - 1.0) < 5e-3), (t, t32)
+    print("vs f64", s64, "\nrelMSE vs FP64 reference", imgcheck.relmse(img, z["ref64_image"]))
+
+
+def test_ptdirect_matches_reference_film(gpu_lib, golden_dir):
+    """renderer::ptdirect (light samples only) against the reference's film."""
+    scene, z = ptscene.load_scene(golden_dir, "cornell_ptdirect")
+    sc = gpu_lib.Scene(scene)
+    img, var = sc.render_ptdirect(16384, int(z["max_num_vertices"]), 7)
+    sc.close()
+    s64 = imgcheck.assert_same_image(img, var, z["ref64_image"], z["ref64_variance"], "gpu vs ref64 (ptdirect)")
     print("vs f64", s64, "\nrelMSE vs FP64 reference", imgcheck.relmse(img, z["ref64_image"]))
 
 

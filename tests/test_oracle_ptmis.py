@@ -1,4 +1,4 @@
-"""Pins the oracle's renderer::ptmis restatement (oracle/lmoracle_bdpt.c,
+"""Pins the oracle's renderer::ptmis and renderer::ptdirect restatement (oracle/lmoracle_bdpt.c,
 next-event estimation with the balance heuristic) against the films of the
 reference's own renderer::ptmis (tests/golden/cornell_ptmis.npz,
 materials_ptmis.npz; 64x64, 16,384 samples per pixel, made by
@@ -34,6 +34,18 @@ def test_oracle_ptmis_matches_reference(oracle_lib, golden_dir, name):
     a, va = ptscene.downsample(r["image"], r["variance"], 2)
     b, vb = ptscene.downsample(z["ref64_image"], z["ref64_variance"], 2)
     print(imgcheck.assert_same_image(a, va, b, vb, f"oracle vs ref64 ({name})"))
+
+
+def test_oracle_ptdirect_matches_reference(oracle_lib, golden_dir):
+    """renderer::ptdirect (light samples only, weight 1) against the
+    reference's own ptdirect film."""
+    scene, z = ptscene.load_scene(golden_dir, "cornell_ptdirect")
+    W, H = scene["camera"]["width"], scene["camera"]["height"]
+    r = oracle_lib.render_ptmis(scene, W * H * 4096, int(z["max_num_vertices"]), 4321, os.cpu_count() or 4,
+                                direct_only=True)
+    a, va = ptscene.downsample(r["image"], r["variance"], 2)
+    b, vb = ptscene.downsample(z["ref64_image"], z["ref64_variance"], 2)
+    print(imgcheck.assert_same_image(a, va, b, vb, "oracle vs ref64 (ptdirect)"))
 
 
 def test_ptmis_and_pt_agree(golden_dir):
