@@ -411,6 +411,92 @@ def run_render(args) -> None:
     sc.close()
 
 
+def run_batch(args) -> None:
+    """Batched configuration: 12 seeded sphere-grid scenes (~1.31M triangles
+    each, mixed 640x360 / 1280x720 / 1920x1080), 64 spp, max depth 16
+    (max_num_vertices 17), roulette after depth 3, all views in one wavefront
+    with graph-replayed bounces and autotuned traversal / wave parameters.
+    Metric Msamples/s over all views; value = films left on the device, e2e =
+    lmgpu_batch_render_pt with host films."""
+    import torch
+
+    import lmgpu
+    from lmgpu import scenes
+
+    spp = args.spp or 64
+    max_nv, rr_depth = 17, 3
+    t0 = time.perf_counter()
+    scene_dicts = scenes.batch_scenes(0x5EED, 12)
+    scs = [lmgpu.Scene(d) for d in scene_dicts]
+    b = lmgpu.Batch(scs)
+    setup_s = time.perf_counter() - t0
+    npix = sum(s.width * s.height for s in scs)
+    samples = npix * spp
+    tuning = b.autotune(1, max_nv, 99, rr_depth)
+    d_img = torch.empty(3 * npix, dtype=torch.float32, device="cuda")
+    d_var = torch.empty(3 * npix, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    for k in range(args.warmup):
+        b.render_pt_device(d_img.data_ptr(), d_var.data_ptr(), spp, max_nv, k, rr_depth, stream.cuda_stream)
+    torch.cuda.synchronize()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    l0 = b.launch_count()
+    total_ms = 0.0
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+        torch.cuda.synchronize()
+        # the batch renders on its own stream and returns once finished
+        t1 = time.perf_counter()
+        b.render_pt_device(d_img.data_ptr(), d_var.data_ptr(), spp, max_nv, 1000 + k, rr_depth, stream.cuda_stream)
+        torch.cuda.synchronize()
+        total_ms += (time.perf_counter() - t1) * 1e3
+    clk = clocks.stop()
+    launches = b.launch_count() - l0
+    ms = total_ms / args.steps
+    t1 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for k in range(e2e_steps):
+        b.render_pt(spp, max_nv, 2000 + k, rr_depth)
+    e2e_s = (time.perf_counter() - t1) / e2e_steps
+    ntri = int(sum(sum(p["tris"].shape[0] for p in d["prims"]) for d in scene_dicts))
+    line = {"metric": "Msamples/s (batched renderer::pt, 12 views)", "value": samples / ms / 1e3,
+            "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (12 seeded sphere-grid scenes)",
+            "config": {"workload": "batch_pt_12_scenes_64spp" if spp == 64 else f"batch_pt_12_scenes_{spp}spp",
+                       "views": len(scs), "resolutions": [[s.width, s.height] for s in scs], "pixels": npix,
+                       "spp": spp, "max_num_vertices": max_nv, "rr_depth": rr_depth, "triangles": ntri,
+                       "tuning": tuning, "scene_setup_s": setup_s,
+                       "timing": "host wall clock around each device-resident render (the render synchronises its "
+                                 "own stream); L2 flushed before every step",
+                       "l2": "flushed before every timed step (256 MiB write, untimed)"},
+            "e2e": {"value": samples / e2e_s / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": npix * 3 * 4 * 2, "api": "lmgpu_batch_render_pt (host films)"},
+            "gpu_launches": launches, "clocks": clk}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import lmoracle
+
+        threads = os.cpu_count() or 1
+        d = dict(scene_dicts[0])
+        d["camera"] = dict(d["camera"], width=160, height=90)
+        n_cpu = 160 * 90 * 4
+        t1 = time.perf_counter()
+        lmoracle.render_pt(d, n_cpu, max_nv, 5, threads)
+        cpu_s = time.perf_counter() - t1
+        line["cpu_baseline"] = {
+            "value": n_cpu / cpu_s / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"{n_cpu} samples of scene 0 at 160x90 (4 spp), oracle restatement of renderer::pt "
+                      f"(roulette at every hit), {threads} threads, BVH build included"}
+    print(json.dumps(line), flush=True)
+    b.close()
+    for sc in scs:
+        sc.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -422,9 +508,9 @@ def main() -> None:
     ap.add_argument("--anyhit", action="store_true", help="time any-hit queries instead of closest hit")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel of the render workloads (profiling of "
                                                         "smaller cases; default: the workload's own)")
-    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt"], default="raycast",
+    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt", "batch"], default="raycast",
                     help="raycast: the BVH ray-cast configuration (default); pt: renderer::pt on the Cornell "
-                         "box; bdpt: renderer::bdpt on the caustic room")
+                         "box; bdpt: renderer::bdpt on the caustic room; batch: 12 scenes in one wavefront")
     ap.add_argument("--use-ref-binary", action="store_true",
                     help="reference arm: time the reference's own qbvh (x86-64 harness) if built")
     args = ap.parse_args()
@@ -434,6 +520,8 @@ def main() -> None:
         run_reference(args)
     elif args.workload in RENDER_WORKLOADS:
         run_render(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_gpu(args)
 

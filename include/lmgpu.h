@@ -237,6 +237,65 @@ int lmgpu_render_bdpt(lmgpu_scene* scene, const lmgpu_pt_params* params, float* 
 int lmgpu_render_bdpt_device(lmgpu_scene* scene, const lmgpu_pt_params* params, float* d_image, float* d_variance,
                              void* stream);
 
+/* ---- Batched path tracing: many scenes / views in one wavefront -------- */
+
+typedef struct lmgpu_batch lmgpu_batch;
+
+/* renderer::pt parameters for a batch (all views share them).  rr_depth:
+ * Russian roulette (probability 0.5) applies once a path has more than
+ * rr_depth segments; 0 reproduces renderer::pt (roulette at every hit,
+ * renderer_pt.cpp:207-216).  Both are unbiased. */
+typedef struct {
+    uint64_t spp;
+    int32_t max_num_vertices;
+    uint32_t seed;
+    int32_t rr_depth;
+} lmgpu_batch_params;
+
+/* Scheduling knobs of a batch: traversal refill / postpone thresholds (see
+ * lmgpu_accel_set_tuning) and the number of paths per wave; probe_ms is the
+ * autotuner's best probe time (output only). */
+typedef struct {
+    int32_t refill;
+    int32_t postpone;
+    uint64_t wave_paths;
+    double probe_ms;
+} lmgpu_batch_tuning;
+
+/* Groups n scenes (each with its own geometry, BVH, camera and resolution;
+ * 1 <= n <= 255, fewer than 2^24 pixels each) for lmgpu_batch_render_pt.  The
+ * scenes are borrowed and must outlive the batch.  No counterpart in the
+ * reference (its renderers render one scene per process). */
+int lmgpu_batch_create(lmgpu_scene* const* scenes, uint32_t n, lmgpu_batch** out);
+
+/* Frees a batch (not its scenes).  NULL is ignored. */
+void lmgpu_batch_destroy(lmgpu_batch* batch);
+
+/* Renders every view of the batch with renderer::pt's estimator in one
+ * wavefront (paths of all views share the queues and the traversal
+ * launches; the per-bounce work is replayed from CUDA graphs).  images[v]
+ * (and variances[v] if variances is not NULL) receive view v's film, laid
+ * out as lmgpu_render_pt's. */
+int lmgpu_batch_render_pt(lmgpu_batch* batch, const lmgpu_batch_params* params, float* const* images,
+                          float* const* variances);
+
+/* As lmgpu_batch_render_pt into device buffers: the views' films one after
+ * another in d_images (and d_variances, may be NULL).  The caller's
+ * `stream` (may be NULL) is made to wait for the render. */
+int lmgpu_batch_render_pt_device(lmgpu_batch* batch, const lmgpu_batch_params* params, float* d_images,
+                                 float* d_variances, void* stream);
+
+/* Measures renders of `probe` over candidate tunings (coordinate descent over
+ * refill, postpone and wave size), keeps the fastest and returns it. */
+int lmgpu_batch_autotune(lmgpu_batch* batch, const lmgpu_batch_params* probe, lmgpu_batch_tuning* out);
+
+/* Sets / reads the batch's tuning. */
+int lmgpu_batch_set_tuning(lmgpu_batch* batch, const lmgpu_batch_tuning* tuning);
+int lmgpu_batch_get_tuning(const lmgpu_batch* batch, lmgpu_batch_tuning* tuning);
+
+/* Kernels the batch renderer has launched so far (a diagnostic). */
+int lmgpu_batch_launch_count(const lmgpu_batch* batch, uint64_t* count);
+
 /* Largest scene lmgpu_trace_static_scene accepts. */
 #define LMGPU_STATIC_MAX_TRIANGLES 16384
 

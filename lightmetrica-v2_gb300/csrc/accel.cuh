@@ -57,4 +57,21 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
 int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, uint64_t n, bool anyhit,
                  bool stats, cudaStream_t stream);
 
+// Blocks of the persistent traversal grid (SMs x resident blocks); looked up
+// once per process.  Negative on a CUDA error.
+int trace_grid_cap();
+
+// One scene's BVH as the multi-scene traversal sees it.
+struct AccelView {
+    const WNode* nodes;
+    const WTri* tris;
+    uint32_t num_nodes, num_tris;
+};
+
+// Traversal of rays from several scenes in one launch (ray i against
+// d_tab[d_ray_scene[i]]), the ray count read from d_n on the device.
+int launch_trace_multi(const AccelView* d_tab, uint32_t ntab, const float4* d_rays, const uint8_t* d_ray_scene,
+                       lmgpu_hit* d_hits, const uint32_t* d_n, uint64_t max_n, bool anyhit, TraceConfig cfg,
+                       uint32_t* d_status, cudaStream_t stream);
+
 }  // namespace lmgpu

@@ -41,14 +41,22 @@ constexpr int kTraceThreads = 128;
 //      fewer do, lanes that also have node work push their triangles back on
 //      the stack and go on traversing (after Aila & Laine 2009 and Ylitie,
 //      Karras & Laine 2017), so the warp keeps doing one kind of work at once.
-template <bool ANYHIT, bool STATS>
+//
+// MULTI: rays of several scenes in one launch; ray i is traced against the
+// BVH tab[ray_scene[i]] (the batch renderer's views).  d_n, when not null,
+// holds the ray count on the device (launches captured in CUDA graphs).
+template <bool ANYHIT, bool STATS, bool MULTI>
 __global__ void __launch_bounds__(kTraceThreads) k_trace(const WNode* __restrict__ nodes, const WTri* __restrict__ tris,
                                                          const float4* __restrict__ rays, lmgpu_hit* __restrict__ hits,
                                                          uint64_t n, uint32_t num_nodes, uint32_t num_tris,
                                                          int refill, int postpone, uint32_t* __restrict__ status,
-                                                         unsigned long long* __restrict__ counters)
+                                                         unsigned long long* __restrict__ counters,
+                                                         const AccelView* __restrict__ tab, uint32_t ntab,
+                                                         const uint8_t* __restrict__ ray_scene,
+                                                         const uint32_t* __restrict__ d_n)
 {
     __shared__ unsigned long long s_next;
+    if (d_n) n = *d_n;
     const uint64_t begin = (uint64_t)blockIdx.x * n / gridDim.x;
     const uint64_t end = (uint64_t)(blockIdx.x + 1) * n / gridDim.x;
     if (threadIdx.x == 0) s_next = begin;
@@ -67,6 +75,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const WNode* __restrict
     int sp = 0;
     uint32_t budget = 0;
     uint32_t node_fetch = 0, tri_fetch = 0, nrays = 0, nhits = 0;
+    // the BVH of the lane's current ray
+    const WNode* lnodes = nodes;
+    const WTri* ltris = tris;
+    uint32_t lnn = num_nodes, lnt = num_tris;
 
     while (true) {
         // 1. refill idle lanes
@@ -83,14 +95,28 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const WNode* __restrict
                     rid = id;
                     const float4 r0 = __ldg(rays + 2 * id);
                     const float4 r1 = __ldg(rays + 2 * id + 1);
+                    if (MULTI) {
+                        const uint32_t sidx = ray_scene[id];
+                        if (sidx < ntab) {
+                            const AccelView av = tab[sidx];
+                            lnodes = av.nodes;
+                            ltris = av.tris;
+                            lnn = av.num_nodes;
+                            lnt = av.num_tris;
+                        } else {
+                            atomicOr(status, kStatusBadTree);
+                            lnn = 0;
+                            lnt = 0;
+                        }
+                    }
                     setup_ray(r0, r1, R);
                     best_t = r1.w;
                     best_id = -1;
                     best_b1 = best_b2 = 0.0f;
-                    ng = make_uint2(0u, num_nodes > 0 ? 0x80000000u : 0u);
+                    ng = make_uint2(0u, lnn > 0 ? 0x80000000u : 0u);
                     tg = make_uint2(0u, 0u);
                     sp = 0;
-                    budget = num_nodes + 1;
+                    budget = lnn + 1;
                     active = true;
                     if (STATS) nrays++;
                 }
@@ -106,7 +132,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const WNode* __restrict
                 const uint32_t slot = (bit - 24u) ^ R.oct_inv;
                 const uint32_t rel = __popc(ng.y & 0xffu & ((1u << slot) - 1u));
                 const uint32_t ni = ng.x + rel;
-                if (ni >= num_nodes || budget-- == 0u) {
+                if (ni >= lnn || budget-- == 0u) {
                     atomicOr(status, kStatusBadTree);
                     ng.y = 0u;
                     sp = 0;
@@ -116,7 +142,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const WNode* __restrict
                         else atomicOr(status, kStatusStackOverflow);
                     }
                     uint32_t child_base, tri_base, imask;
-                    const uint32_t hm = intersect_node(nodes, ni, R, best_t, child_base, tri_base, imask);
+                    const uint32_t hm = intersect_node(lnodes, ni, R, best_t, child_base, tri_base, imask);
                     if (STATS) node_fetch++;
                     ng = make_uint2(child_base, (hm & 0xff000000u) | imask);
                     tg = make_uint2(tri_base, hm & 0x00ffffffu);
@@ -150,14 +176,14 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const WNode* __restrict
             if (active && tg.y != 0u) {
                 const uint32_t k = __ffs(tg.y) - 1u;
                 tg.y &= tg.y - 1u;
-                if (tg.x + k >= num_tris) {
+                if (tg.x + k >= lnt) {
                     atomicOr(status, kStatusBadTree);
                     tg.y = 0u;
                 } else {
                     float t, b1, b2;
                     int id;
                     if (STATS) tri_fetch++;
-                    if (intersect_tri(tris, tg.x + k, R, best_t, t, b1, b2, id)) {
+                    if (intersect_tri(ltris, tg.x + k, R, best_t, t, b1, b2, id)) {
                         if (t < best_t || id > best_id) {
                             best_t = t;
                             best_id = id;
@@ -187,18 +213,26 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const WNode* __restrict
 
 }  // namespace
 
-int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, uint64_t n, bool anyhit, bool stats,
-                 cudaStream_t stream)
+int trace_grid_cap()
 {
-    if (n == 0) return LMGPU_OK;
     static int grid_cap = 0;
     if (grid_cap == 0) {
         int dev = 0, sms = 0, per_sm = 0;
         LMGPU_CUDA_TRY(cudaGetDevice(&dev));
         LMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        LMGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false, false>, kTraceThreads, 0));
+        LMGPU_CUDA_TRY(
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false, false, false>, kTraceThreads, 0));
         grid_cap = sms * (per_sm > 0 ? per_sm : 1);
     }
+    return grid_cap;
+}
+
+int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, uint64_t n, bool anyhit, bool stats,
+                 cudaStream_t stream)
+{
+    if (n == 0) return LMGPU_OK;
+    const int grid_cap = trace_grid_cap();
+    if (grid_cap <= 0) return LMGPU_ERR_CUDA;
     const TraceConfig cfg = a->tune;
     // at least ~4 warps' worth of rays per block
     const uint64_t by_rays = (n + 4 * kTraceThreads - 1) / (4 * kTraceThreads);
@@ -206,13 +240,27 @@ int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, 
     const uint32_t nn = a->ntri > 0 ? (uint32_t)a->num_wide : 0u;
     const uint32_t nt = (uint32_t)a->ntri;
     auto* cnt = a->counters;
-    if (anyhit) {
-        if (stats) k_trace<true, true><<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, cfg.refill, cfg.postpone, a->status, cnt);
-        else k_trace<true, false><<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, cfg.refill, cfg.postpone, a->status, cnt);
-    } else {
-        if (stats) k_trace<false, true><<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, cfg.refill, cfg.postpone, a->status, cnt);
-        else k_trace<false, false><<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, cfg.refill, cfg.postpone, a->status, cnt);
-    }
+    auto k = anyhit ? (stats ? k_trace<true, true, false> : k_trace<true, false, false>)
+                    : (stats ? k_trace<false, true, false> : k_trace<false, false, false>);
+    k<<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, cfg.refill, cfg.postpone,
+                                          a->status, cnt, nullptr, 0u, nullptr, nullptr);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+    return LMGPU_OK;
+}
+
+int launch_trace_multi(const AccelView* d_tab, uint32_t ntab, const float4* d_rays, const uint8_t* d_ray_scene,
+                       lmgpu_hit* d_hits, const uint32_t* d_n, uint64_t max_n, bool anyhit, TraceConfig cfg,
+                       uint32_t* d_status, cudaStream_t stream)
+{
+    if (max_n == 0) return LMGPU_OK;
+    const int grid_cap = trace_grid_cap();
+    if (grid_cap <= 0) return LMGPU_ERR_CUDA;
+    // the ray count is read on the device: the full persistent grid, each
+    // block taking its share of whatever count the launch finds
+    auto k = anyhit ? k_trace<true, false, true> : k_trace<false, false, true>;
+    k<<<(unsigned)grid_cap, kTraceThreads, 0, stream>>>(nullptr, nullptr, d_rays, d_hits, max_n, 0u, 0u, cfg.refill,
+                                                         cfg.postpone, d_status, nullptr, d_tab, ntab, d_ray_scene,
+                                                         d_n);
     LMGPU_CUDA_TRY(cudaGetLastError());
     return LMGPU_OK;
 }

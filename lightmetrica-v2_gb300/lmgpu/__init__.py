@@ -94,6 +94,15 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_render_bdpt.argtypes = [vp, vp, vp, vp]
     L.lmgpu_render_ptmis.argtypes = [vp, vp, vp, vp]
     L.lmgpu_render_ptdirect.argtypes = [vp, vp, vp, vp]
+    L.lmgpu_batch_create.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(vp)]
+    L.lmgpu_batch_destroy.argtypes = [vp]
+    L.lmgpu_batch_destroy.restype = None
+    L.lmgpu_batch_render_pt.argtypes = [vp, vp, vp, vp]
+    L.lmgpu_batch_render_pt_device.argtypes = [vp, vp, vp, vp, vp]
+    L.lmgpu_batch_autotune.argtypes = [vp, vp, vp]
+    L.lmgpu_batch_set_tuning.argtypes = [vp, vp]
+    L.lmgpu_batch_get_tuning.argtypes = [vp, vp]
+    L.lmgpu_batch_launch_count.argtypes = [vp, ctypes.POINTER(u64)]
     L.lmgpu_render_ptdirect_device.argtypes = [vp, vp, vp, vp, vp]
     L.lmgpu_render_ptmis_device.argtypes = [vp, vp, vp, vp, vp]
     L.lmgpu_scene_launch_count.argtypes = [vp, ctypes.POINTER(u64)]
@@ -103,6 +112,9 @@ def lib() -> ctypes.CDLL:
                  "lmgpu_trace_static_scene", "lmgpu_accel_set_tuning", "lmgpu_scene_create", "lmgpu_scene_accel",
                  "lmgpu_render_pt", "lmgpu_render_pt_device", "lmgpu_render_bdpt", "lmgpu_render_bdpt_device", "lmgpu_scene_launch_count",
                  "lmgpu_render_ptmis", "lmgpu_render_ptmis_device", "lmgpu_render_ptdirect",
+                 "lmgpu_batch_create", "lmgpu_batch_render_pt", "lmgpu_batch_render_pt_device",
+                 "lmgpu_batch_autotune", "lmgpu_batch_set_tuning", "lmgpu_batch_get_tuning",
+                 "lmgpu_batch_launch_count",
                  "lmgpu_render_ptdirect_device",
                  "lmgpu_scene_set_environment"):
         getattr(L, name).restype = ctypes.c_int
@@ -310,6 +322,78 @@ class Scene:
                            seed: int = 0, stream: int = 0) -> None:
         prm = PtParams(spp, max_num_vertices, seed)
         _check(lib().lmgpu_render_bdpt_device(self._h, ctypes.byref(prm), d_image, d_variance, stream))
+
+
+class BatchParams(ctypes.Structure):
+    _fields_ = [("spp", ctypes.c_uint64), ("max_num_vertices", ctypes.c_int32), ("seed", ctypes.c_uint32),
+                ("rr_depth", ctypes.c_int32)]
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("refill", ctypes.c_int32), ("postpone", ctypes.c_int32), ("wave_paths", ctypes.c_uint64),
+                ("probe_ms", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Batch:
+    """Several scenes (views) rendered by one wavefront (lmgpu_batch).  The
+    Scene objects must stay alive while the batch is used."""
+
+    def __init__(self, scenes: list) -> None:
+        self.scenes = list(scenes)
+        arr = (ctypes.c_void_p * len(self.scenes))(*[s._h.value for s in self.scenes])
+        h = ctypes.c_void_p()
+        _check(lib().lmgpu_batch_create(ctypes.addressof(arr), len(self.scenes), ctypes.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().lmgpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render_pt(self, spp: int, max_num_vertices: int = -1, seed: int = 0, rr_depth: int = 0) -> list:
+        """Films and per-pixel variances of every view: [(img, var), ...]."""
+        out = [(np.empty((s.height, s.width, 3), np.float32), np.empty((s.height, s.width, 3), np.float32))
+               for s in self.scenes]
+        imgs = (ctypes.c_void_p * len(out))(*[o[0].ctypes.data for o in out])
+        vars_ = (ctypes.c_void_p * len(out))(*[o[1].ctypes.data for o in out])
+        prm = BatchParams(spp, max_num_vertices, seed, rr_depth)
+        _check(lib().lmgpu_batch_render_pt(self._h, ctypes.byref(prm), ctypes.addressof(imgs),
+                                           ctypes.addressof(vars_)))
+        return out
+
+    def render_pt_device(self, d_images: int, d_variances: int, spp: int, max_num_vertices: int = -1,
+                         seed: int = 0, rr_depth: int = 0, stream: int = 0) -> None:
+        prm = BatchParams(spp, max_num_vertices, seed, rr_depth)
+        _check(lib().lmgpu_batch_render_pt_device(self._h, ctypes.byref(prm), d_images, d_variances, stream))
+
+    def autotune(self, spp: int, max_num_vertices: int = -1, seed: int = 0, rr_depth: int = 0) -> dict:
+        prm = BatchParams(spp, max_num_vertices, seed, rr_depth)
+        t = BatchTuning()
+        _check(lib().lmgpu_batch_autotune(self._h, ctypes.byref(prm), ctypes.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, refill: int, postpone: int, wave_paths: int) -> None:
+        t = BatchTuning(refill, postpone, wave_paths, 0.0)
+        _check(lib().lmgpu_batch_set_tuning(self._h, ctypes.byref(t)))
+
+    def tuning(self) -> dict:
+        t = BatchTuning()
+        _check(lib().lmgpu_batch_get_tuning(self._h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def launch_count(self) -> int:
+        n = ctypes.c_uint64()
+        _check(lib().lmgpu_batch_launch_count(self._h, ctypes.byref(n)))
+        return n.value
 
 
 def version() -> str:

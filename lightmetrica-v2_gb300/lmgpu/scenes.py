@@ -267,3 +267,69 @@ def caustic_room(width: int = 1280, height: int = 720, sphere_level: int = 5) ->
     camera = {"eye": (0.0, 0.7, -1.1), "center": (0.0, 0.3, 0.3), "up": (0.0, 1.0, 0.0), "fov": 45.0,
               "width": width, "height": height}
     return {"prims": prims, "camera": camera}
+
+
+_ICO4 = None
+
+
+def _icosphere4() -> np.ndarray:
+    """Unit level-4 icosphere (5120 triangles), built once."""
+    global _ICO4
+    if _ICO4 is None:
+        _ICO4 = closed_icosphere(4).astype(np.float64)
+    return _ICO4
+
+
+def phong_to_ggx_roughness(n: float) -> float:
+    """GGX roughness standing in for a Phong exponent n: alpha = sqrt(2 / (n + 2))
+    (the reference has no Phong BSDF; bsdf::cook_torrance takes its place)."""
+    return float(np.sqrt(2.0 / (n + 2.0)))
+
+
+def sphere_grid_scene(seed: int, index: int, width: int | None = None, height: int | None = None,
+                      grid: int = 16) -> dict:
+    """One scene of the batched configuration: a grid x grid array of level-4
+    icospheres (5120 triangles each, radius U[0.2, 0.5], spacing 1.2) on a
+    ground plane, each sphere Lambertian (albedo U[0.2, 0.9]^3), glossy
+    (Phong exponent U[10, 1000] as GGX roughness sqrt(2 / (n + 2)), default
+    conductor) or glass (eta 1 -> 1.5); one sphere light (level-2 icosphere,
+    radius 1, Le 60) above the grid and a constant environment (0.3, 0.35,
+    0.45).  The resolution is drawn from {640x360, 1280x720, 1920x1080} unless
+    given.  Seeded by (seed, index)."""
+    g = rng(seed, 1000 + index)
+    ico = _icosphere4()
+    prims = []
+    span = (grid - 1) * 1.2
+    ground = _quad((-2.0, 0.0, -2.0), (-2.0, 0.0, span + 2.0), (span + 2.0, 0.0, span + 2.0), (span + 2.0, 0.0, -2.0))
+    prims.append({"bsdf": BSDF_DIFFUSE, "R": (0.6, 0.6, 0.6), "tris": ground.astype(np.float32)})
+    radii = g.uniform(0.2, 0.5, size=grid * grid)
+    kinds = g.integers(0, 3, size=grid * grid)
+    albedo = g.uniform(0.2, 0.9, size=(grid * grid, 3))
+    expo = g.uniform(10.0, 1000.0, size=grid * grid)
+    for k in range(grid * grid):
+        cx, cz = (k % grid) * 1.2, (k // grid) * 1.2
+        r = radii[k]
+        tris = (ico.reshape(-1, 3) * r + np.array([cx, r + 1e-3, cz])).reshape(-1, 9).astype(np.float32)
+        if kinds[k] == 0:
+            prims.append({"bsdf": BSDF_DIFFUSE, "R": tuple(albedo[k]), "tris": tris})
+        elif kinds[k] == 1:
+            prims.append({"bsdf": BSDF_COOK_TORRANCE, "R": tuple(albedo[k]),
+                          "roughness": phong_to_ggx_roughness(expo[k]), "tris": tris})
+        else:
+            prims.append({"bsdf": BSDF_DIELECTRIC, "R": (1.0, 1.0, 1.0), "eta1": 1.0, "eta2": 1.5, "tris": tris})
+    light = closed_icosphere(2, 1.0, (span * 0.5, 8.0, span * 0.5))
+    prims.append({"bsdf": BSDF_NULL, "light": True, "Le": (60.0, 55.0, 50.0), "tris": light})
+    res = [(640, 360), (1280, 720), (1920, 1080)]
+    w, h = res[int(g.integers(0, 3))]
+    if width is not None:
+        w, h = width, height
+    eye = (span * 0.5 + float(g.uniform(-3, 3)), float(g.uniform(4, 7)), -6.0)
+    camera = {"eye": eye, "center": (span * 0.5, 0.0, span * 0.5), "up": (0.0, 1.0, 0.0), "fov": 50.0,
+              "width": w, "height": h}
+    return {"prims": prims, "camera": camera, "env": (0.3, 0.35, 0.45)}
+
+
+def batch_scenes(seed: int = 0x5EED, count: int = 12, grid: int = 16, size: tuple | None = None) -> list:
+    """The batched configuration: `count` seeded sphere-grid scenes
+    (sphere_grid_scene), ~1.31M triangles each at grid 16."""
+    return [sphere_grid_scene(seed, i, *(size or (None, None)), grid=grid) for i in range(count)]
