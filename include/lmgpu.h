@@ -280,8 +280,8 @@ int lmgpu_batch_render_pt(lmgpu_batch* batch, const lmgpu_batch_params* params, 
                           float* const* variances);
 
 /* As lmgpu_batch_render_pt into device buffers: the views' films one after
- * another in d_images (and d_variances, may be NULL).  The caller's
- * `stream` (may be NULL) is made to wait for the render. */
+ * another in d_images (and d_variances, may be NULL), rendered on `stream`
+ * (NULL: the batch's own stream); returns after the render has finished. */
 int lmgpu_batch_render_pt_device(lmgpu_batch* batch, const lmgpu_batch_params* params, float* d_images,
                                  float* d_variances, void* stream);
 

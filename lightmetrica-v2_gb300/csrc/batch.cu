@@ -32,6 +32,7 @@ namespace {
 constexpr int kBtThreads = 256;
 constexpr uint32_t kMaxViews = 255;
 constexpr int kBouncesPerSync = 8;
+constexpr int kMaxBounces = 1024;
 
 struct BatchView {
     SceneGPU sc;
@@ -327,13 +328,12 @@ int capture_bounces(lmgpu_batch* b)
     return LMGPU_OK;
 }
 
-int batch_render(lmgpu_batch* b, const lmgpu_batch_params* prm, float* d_image, float* d_variance)
+int batch_render(lmgpu_batch* b, const lmgpu_batch_params* prm, float* d_image, float* d_variance, cudaStream_t s)
 {
-    if (prm->spp == 0) {
-        set_error("lmgpu_batch_render_pt: spp must be > 0");
+    if (prm->spp == 0 || prm->rr_depth < 0 || prm->rr_depth > kMaxBounces / 2) {
+        set_error("lmgpu_batch_render_pt: spp must be > 0 and rr_depth in [0, 512]");
         return LMGPU_ERR_INVALID;
     }
-    cudaStream_t s = b->stream;
     // sample ranges of the views
     uint64_t begin = 0;
     for (uint32_t v = 0; v < b->nviews; v++) {
@@ -345,13 +345,16 @@ int batch_render(lmgpu_batch* b, const lmgpu_batch_params* prm, float* d_image, 
         cudaMemcpyAsync(b->d_views, b->h_views.data(), sizeof(BatchView) * b->nviews, cudaMemcpyHostToDevice, s));
     const RenderArgs ra{prm->seed, prm->max_num_vertices, prm->rr_depth, 0u};
     LMGPU_CUDA_TRY(cudaMemcpyAsync(b->d_args, &ra, sizeof(ra), cudaMemcpyHostToDevice, s));
+    LMGPU_CUDA_TRY(cudaMemsetAsync(b->d_status, 0, sizeof(uint32_t), s));
     LMGPU_CUDA_TRY(cudaMemsetAsync(b->film, 0, sizeof(double) * 3 * b->total_pix, s));
     LMGPU_CUDA_TRY(cudaMemsetAsync(b->film_sq, 0, sizeof(double) * 3 * b->total_pix, s));
     const uint64_t wave = b->wave < total ? b->wave : total;
     int rc = ensure_batch_queues(b, wave);
     if (rc) return rc;
     if ((rc = capture_bounces(b))) return rc;
-    const int max_bounces = prm->max_num_vertices < 0 ? -1 : prm->max_num_vertices - 1;
+    // unbounded paths (max_num_vertices -1) stop after kMaxBounces segments;
+    // with roulette the survivors are a 2^-(kMaxBounces - rr_depth) fraction
+    const int max_bounces = prm->max_num_vertices < 0 ? kMaxBounces : prm->max_num_vertices - 1;
     for (uint64_t p0 = 0; p0 < total; p0 += wave) {
         const uint32_t n = (uint32_t)((total - p0) < wave ? (total - p0) : wave);
         k_bt_generate<<<(n + kBtThreads - 1) / kBtThreads, kBtThreads, 0, s>>>(
@@ -359,11 +362,11 @@ int batch_render(lmgpu_batch* b, const lmgpu_batch_params* prm, float* d_image, 
         LMGPU_CUDA_TRY(cudaGetLastError());
         b->launches++;
         int cur = 0;
-        for (int k = 0; max_bounces < 0 || k < max_bounces; k++) {
+        for (int k = 0; k < max_bounces; k++) {
             LMGPU_CUDA_TRY(cudaGraphLaunch(b->bounce[cur], s));
             b->launches += 2;  // traversal + shading
             cur = 1 - cur;
-            const bool last = max_bounces >= 0 && k + 1 == max_bounces;
+            const bool last = k + 1 == max_bounces;
             if (!last && (k + 1) % kBouncesPerSync == 0) {
                 // every few bounces: stop once the queue has emptied
                 LMGPU_CUDA_TRY(cudaMemcpyAsync(b->h_n, b->d_n + cur, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -512,17 +515,7 @@ int lmgpu_batch_render_pt_device(lmgpu_batch* b, const lmgpu_batch_params* prm, 
         set_error("lmgpu_batch_render_pt_device: NULL argument");
         return LMGPU_ERR_INVALID;
     }
-    int rc = batch_render(b, prm, d_images, d_variances);
-    if (rc) return rc;
-    if (stream) {
-        // hand-off: the caller's stream waits for the batch's work
-        cudaEvent_t ev;
-        LMGPU_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-        cudaEventRecord(ev, b->stream);
-        cudaStreamWaitEvent((cudaStream_t)stream, ev, 0);
-        cudaEventDestroy(ev);
-    }
-    return LMGPU_OK;
+    return batch_render(b, prm, d_images, d_variances, stream ? (cudaStream_t)stream : b->stream);
 }
 
 int lmgpu_batch_render_pt(lmgpu_batch* b, const lmgpu_batch_params* prm, float* const* images,
@@ -538,7 +531,7 @@ int lmgpu_batch_render_pt(lmgpu_batch* b, const lmgpu_batch_params* prm, float* 
             set_error("lmgpu_batch_render_pt: NULL image");
             return LMGPU_ERR_INVALID;
         }
-    int rc = batch_render(b, prm, b->d_image, variances ? b->d_variance : nullptr);
+    int rc = batch_render(b, prm, b->d_image, variances ? b->d_variance : nullptr, b->stream);
     if (rc) return rc;
     for (uint32_t v = 0; v < b->nviews; v++) {
         const uint64_t o = 3 * b->film_off[v], cnt = 3 * (uint64_t)b->h_views[v].npix;
@@ -571,7 +564,7 @@ int lmgpu_batch_autotune(lmgpu_batch* b, const lmgpu_batch_params* probe, lmgpu_
         ms = 1e30f;
         for (int rep = 0; rep < 2; rep++) {
             cudaEventRecord(e0, b->stream);
-            int rc = batch_render(b, probe, b->d_image, nullptr);
+            int rc = batch_render(b, probe, b->d_image, nullptr, b->stream);
             if (rc) return rc;
             cudaEventRecord(e1, b->stream);
             cudaEventSynchronize(e1);
