@@ -296,6 +296,41 @@ int lmgpu_batch_get_tuning(const lmgpu_batch* batch, lmgpu_batch_tuning* tuning)
 /* Kernels the batch renderer has launched so far (a diagnostic). */
 int lmgpu_batch_launch_count(const lmgpu_batch* batch, uint64_t* count);
 
+/* ---- Learned path guiding: the network ----------------------------------
+ * A small MLP (input: position with a 16-frequency encoding, normal,
+ * outgoing direction; 4 x 64 ReLU; output: 8 von Mises-Fisher lobes) run on
+ * the tensor cores, trained online with Adam.  No counterpart in the
+ * reference.  Queries are float[9] each: position, normal, outgoing
+ * direction; raw outputs float[40] each: per lobe (mean 3, kappa
+ * pre-activation, weight logit). */
+
+typedef struct lmgpu_guide lmgpu_guide;
+
+/* Number of FP32 parameters (the layout is documented in guide_net.cuh). */
+int lmgpu_guide_num_params(uint64_t* n);
+
+/* Creates a network with seeded initial weights for positions in the box
+ * box_lo_hi = (lo.x, lo.y, lo.z, hi.x, hi.y, hi.z). */
+int lmgpu_guide_create(const float* box_lo_hi, uint32_t seed, lmgpu_guide** out);
+void lmgpu_guide_destroy(lmgpu_guide* guide);
+
+/* Copies the FP32 master parameters out / in (n = lmgpu_guide_num_params). */
+int lmgpu_guide_get_params(const lmgpu_guide* guide, float* params, uint64_t n);
+int lmgpu_guide_set_params(lmgpu_guide* guide, const float* params, uint64_t n);
+
+/* Raw outputs of n queries (host buffers). */
+int lmgpu_guide_forward(lmgpu_guide* guide, const float* queries, uint64_t n, float* raw);
+
+/* Gradient of the mean loss -(1/n) sum_i weights[i] log q(dirs[i] | query i)
+ * with respect to the parameters (float[num_params]) and the loss value;
+ * the parameters are not changed. */
+int lmgpu_guide_gradient(lmgpu_guide* guide, const float* queries, const float* dirs, const float* weights,
+                         uint64_t n, float* grad, float* loss);
+
+/* One Adam step (beta 0.9 / 0.999, learning rate lr) on that loss. */
+int lmgpu_guide_train_step(lmgpu_guide* guide, const float* queries, const float* dirs, const float* weights,
+                           uint64_t n, float lr, float* loss);
+
 /* Largest scene lmgpu_trace_static_scene accepts. */
 #define LMGPU_STATIC_MAX_TRIANGLES 16384
 

@@ -1,0 +1,672 @@
+// The guiding network on the 5th-generation tensor cores (tcgen05, sm_103a):
+// forward, backward and Adam kernels for the MLP of guide_net.cuh, BF16
+// operands with FP32 accumulation in tensor memory.
+//
+// k_guide_fwd   one CTA (4 warps) per 128-query tile at a time, persistent
+//               over tiles.  The five weight matrices stay in shared memory
+//               (BF16, K-major canonical layout); the tile's activations
+//               ping-pong between two shared-memory buffers; each layer is
+//               K/16 MMAs of M = 128 into a 64-column tensor-memory
+//               accumulator, issued by one thread and completed through an
+//               mbarrier; the epilogue (bias, ReLU, BF16 pack) runs on all
+//               128 threads, one row each, reading its row with tcgen05.ld.
+//               MODE_TRAIN also writes every layer's input (BF16) and the raw
+//               outputs to global memory for the backward pass.
+// k_guide_bwd   per 128-sample tile: the loss gradient of the outputs, then
+//               for each layer, from the last: dH = dZ W (M = 128 MMA
+//               against W^T kept in shared memory) and dW = dZ^T H.  The
+//               weight gradient has M = 64 rows; it is computed as one
+//               M = 128 MMA by splitting the tile into two 64-sample halves:
+//               A' = [dZ_1^T ; dZ_2^T], B' = [H_1^T ; H_2^T], whose product's
+//               two diagonal blocks are the halves' dW and are added into the
+//               FP32 gradient with atomics.
+// k_guide_adam  Adam on the FP32 master parameters (gradients zeroed).
+//
+// Every mbarrier wait has an iteration limit; on time-out a kernel raises
+// kStatusTimeout in its status word, still frees its tensor memory, and
+// returns.
+#include "common.cuh"
+#include "lmgpu.h"
+#include "guide_net.cuh"
+#include "tc.cuh"
+
+#include <cuda_bf16.h>
+#include <cstring>
+#include <vector>
+
+namespace lmgpu {
+namespace {
+
+using namespace guide;
+
+constexpr uint32_t kStatusTimeout = 16;
+constexpr uint32_t kWaitLimit = 1u << 24;
+constexpr int kTile = 128;
+constexpr int kThreads = 128;
+constexpr int kActs = kIn + 4 * kHid;  // stored activations per sample (bf16)
+
+// shared-memory plan of the forward kernel (bytes)
+// W1 (64x128) at 0, W2..W4 (64x64) at 16384 + 8192 (l - 1), W5 (48x64) at 40960
+__host__ __device__ constexpr uint32_t fwd_w(int l) { return l == 0 ? 0u : 16384u + 8192u * (uint32_t)(l - 1); }
+constexpr uint32_t kFwdA = 47104;                              // 128 x 128 activations
+constexpr uint32_t kFwdB = kFwdA + 32768;                      // 128 x 64 activations
+constexpr uint32_t kFwdBias = kFwdB + 16384;                   // 304 floats
+constexpr uint32_t kFwdBar = kFwdBias + 1280;
+constexpr uint32_t kFwdSmem = kFwdBar + 64;
+
+// shared-memory plan of the backward kernel (bytes)
+// W_l^T for l = 1..4 (W2^T..W4^T 64x64, W5^T 64x48) at 8192 (l - 1)
+__host__ __device__ constexpr uint32_t bwd_wt(int l) { return 8192u * (uint32_t)(l - 1); }
+constexpr uint32_t kBwdDZ = 30720;                           // dZ, 128 x 64 (K-major, K = layer width)
+constexpr uint32_t kBwdDZT = kBwdDZ + 16384;                 // [dZ_1^T ; dZ_2^T], 128 x 64
+constexpr uint32_t kBwdHT = kBwdDZT + 16384;                 // [H_1^T ; H_2^T], up to 256 x 64
+constexpr uint32_t kBwdBar = kBwdHT + 32768;
+constexpr uint32_t kBwdSmem = 122880;  // above the plan (96 KB): one CTA per SM, so 512 TMEM columns are free
+
+enum : int { MODE_RAW = 0, MODE_TRAIN = 1 };
+
+struct Box {
+    float lo[3], inv_ext[3];
+};
+
+__device__ __forceinline__ uint32_t pack2(float a, float b)
+{
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// 8 consecutive values of row r into a K-major canonical tile (one 16-byte store).
+__device__ __forceinline__ void put8(unsigned char* tile, uint32_t r, uint32_t k, uint32_t K, const float v[8])
+{
+    uint4 q;
+    q.x = pack2(v[0], v[1]);
+    q.y = pack2(v[2], v[3]);
+    q.z = pack2(v[4], v[5]);
+    q.w = pack2(v[6], v[7]);
+    *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(r, k, K)) = q;
+}
+
+__device__ __forceinline__ void put1(unsigned char* tile, uint32_t r, uint32_t k, uint32_t K, float v)
+{
+    *reinterpret_cast<__nv_bfloat16*>(tile + tc::kmajor_offset(r, k, K)) = __float2bfloat16_rn(v);
+}
+
+// W (rows x cols, fp32 row-major; transpose: stored as W^T) into a K-major tile.
+__device__ void load_matrix(unsigned char* tile, const float* __restrict__ W, int rows, int cols, bool transpose)
+{
+    if (!transpose) {
+        for (int idx = threadIdx.x; idx < rows * cols / 8; idx += blockDim.x) {
+            const int r = idx / (cols / 8), c = (idx % (cols / 8)) * 8;
+            float v[8];
+            for (int q = 0; q < 8; q++) v[q] = W[r * cols + c + q];
+            put8(tile, r, c, cols, v);
+        }
+    } else {
+        // tile rows = W columns (cols of them), tile K = W rows
+        for (int idx = threadIdx.x; idx < rows * cols / 8; idx += blockDim.x) {
+            const int r = idx / (rows / 8), c = (idx % (rows / 8)) * 8;
+            float v[8];
+            for (int q = 0; q < 8; q++) v[q] = W[(c + q) * cols + r];
+            put8(tile, r, c, rows, v);
+        }
+    }
+}
+
+// Issues the K / 16 MMAs of one M = 128 layer and commits them to the mbarrier.
+__device__ __forceinline__ void issue_layer(uint32_t d_tmem, uint32_t a_saddr, uint32_t K, uint32_t b_saddr,
+                                            uint32_t N, uint64_t* bar)
+{
+    const uint32_t idesc = tc::idesc_bf16_f32(128, N);
+    for (uint32_t ks = 0; ks < K / 16; ks++)
+        tc::mma_bf16(d_tmem, tc::kmajor_desc(a_saddr + ks * 256u, K), tc::kmajor_desc(b_saddr + ks * 256u, K), idesc,
+                     ks > 0 ? 1u : 0u);
+    tc::mma_commit(bar);
+}
+
+// All threads: wait for the committed MMAs (bounded), agree on the outcome,
+// then order tensor-memory reads after them.
+__device__ __forceinline__ bool wait_layer(uint64_t* bar, uint32_t& phase, uint32_t* status)
+{
+    const bool mine = tc::mbar_wait(bar, phase, kWaitLimit);
+    phase ^= 1u;
+    const bool ok = __syncthreads_and(mine ? 1 : 0) != 0;
+    if (!ok && threadIdx.x == 0) atomicOr(status, kStatusTimeout);
+    tc::fence_after_sync();
+    return ok;
+}
+
+// End of a kernel: after a time-out, one more bounded wait for the MMAs
+// still in flight; then the allocating warp frees its tensor memory.
+__device__ __forceinline__ void release_tmem(uint64_t* bar, uint32_t phase, bool alive, uint32_t tmem, uint32_t ncols)
+{
+    if (!alive) tc::mbar_wait(bar, phase ^ 1u, kWaitLimit);
+    tc::fence_before_sync();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, ncols);
+        tc::tmem_relinquish();
+    }
+}
+
+__device__ __forceinline__ void block_sync_for_mma()
+{
+    tc::fence_smem_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads, 1) k_guide_fwd(const float* __restrict__ params, Box box,
+                                                           const float* __restrict__ queries, uint32_t n,
+                                                           float* __restrict__ raw_out,
+                                                           __nv_bfloat16* __restrict__ acts,
+                                                           uint32_t* __restrict__ status)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    float* sbias = reinterpret_cast<float*>(smem + kFwdBias);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kFwdBar);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kFwdBar + 8);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+
+    for (int l = 0; l < 5; l++) load_matrix(smem + fwd_w(l), params + w_off(l), layer_out(l), layer_in(l), false);
+    for (int i = tid; i < 4 * kHid + kOut; i += kThreads) {
+        const int l = i / kHid < 4 ? i / kHid : 4, j = i - l * kHid;
+        sbias[i] = params[b_off(l) + j];
+    }
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        tc::mbar_init_fence();
+    }
+    if (warp == 0) tc::tmem_alloc(s_tmem, 64);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *s_tmem;
+    const uint32_t sA = tc::smem_addr(smem + kFwdA), sB = tc::smem_addr(smem + kFwdB);
+    uint32_t phase = 0;
+    bool alive = true;
+
+    const uint32_t ntiles = (n + kTile - 1) / kTile;
+    for (uint32_t tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x) {
+        const uint32_t row = tile * kTile + tid;
+        // features of the row's query
+        {
+            float f[kIn];
+            if (row < n) {
+                const float* q = queries + 9 * (size_t)row;
+                const float x[3] = {q[0], q[1], q[2]}, nn[3] = {q[3], q[4], q[5]}, wo[3] = {q[6], q[7], q[8]};
+                features(x, nn, wo, box.lo, box.inv_ext, f);
+            } else {
+                for (int k = 0; k < kIn; k++) f[k] = 0.0f;
+            }
+            for (int k = 0; k < kIn; k += 8) put8(smem + kFwdA, tid, k, kIn, f + k);
+            if (MODE == MODE_TRAIN && row < n) {
+                uint4* dst = reinterpret_cast<uint4*>(acts + (size_t)row * kActs);
+                for (int k = 0; k < kIn; k += 8)
+                    dst[k / 8] = make_uint4(pack2(f[k], f[k + 1]), pack2(f[k + 2], f[k + 3]), pack2(f[k + 4], f[k + 5]),
+                                            pack2(f[k + 6], f[k + 7]));
+            }
+        }
+        block_sync_for_mma();
+        for (int l = 0; l < 5 && alive; l++) {
+            // layer l reads buffer A (l even) or B (l odd)
+            const uint32_t a_in = (l & 1) ? sB : sA;
+            unsigned char* out_tile = smem + ((l & 1) ? kFwdA : kFwdB);
+            const uint32_t K = layer_in(l), N = layer_out(l);
+            if (tid == 0) issue_layer(tmem, a_in, K, tc::smem_addr(smem + fwd_w(l)), N, bar);
+            alive = wait_layer(bar, phase, status);
+            if (!alive) break;
+            const float* bias = sbias + l * kHid;
+            if (l < 4) {
+                float h[kHid];
+                for (int c = 0; c < kHid; c += 16) tc::tmem_load16(tc::tmem_at(tmem, warp * 32, c), h + c);
+                tc::tmem_wait_ld();
+                for (int c = 0; c < kHid; c++) h[c] = fmaxf(h[c] + bias[c], 0.0f);
+                for (int c = 0; c < kHid; c += 8) put8(out_tile, tid, c, kHid, h + c);
+                if (MODE == MODE_TRAIN && row < n) {
+                    uint4* dst = reinterpret_cast<uint4*>(acts + (size_t)row * kActs + kIn + l * kHid);
+                    for (int c = 0; c < kHid; c += 8)
+                        dst[c / 8] = make_uint4(pack2(h[c], h[c + 1]), pack2(h[c + 2], h[c + 3]),
+                                                pack2(h[c + 4], h[c + 5]), pack2(h[c + 6], h[c + 7]));
+                }
+            } else {
+                float z[kOut];
+                for (int c = 0; c < kOut; c += 16) tc::tmem_load16(tc::tmem_at(tmem, warp * 32, c), z + c);
+                tc::tmem_wait_ld();
+                if (row < n) {
+                    float4* dst = reinterpret_cast<float4*>(raw_out + (size_t)row * kOutUsed);
+                    for (int c = 0; c < kOutUsed; c += 4)
+                        dst[c / 4] = make_float4(z[c] + bias[c], z[c + 1] + bias[c + 1], z[c + 2] + bias[c + 2],
+                                                 z[c + 3] + bias[c + 3]);
+                }
+            }
+            block_sync_for_mma();
+        }
+    }
+    release_tmem(bar, phase, alive, tmem, 64);
+}
+
+// Adds the 32 lanes' values of v into *dst (one atomic per warp).
+__device__ __forceinline__ void warp_atomic_add(float* dst, float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31u) == 0u && v != 0.0f) atomicAdd(dst, v);
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restrict__ params,
+                                                           const float* __restrict__ raw,
+                                                           const __nv_bfloat16* __restrict__ acts,
+                                                           const float* __restrict__ dirs,
+                                                           const float* __restrict__ weights, uint32_t n,
+                                                           float inv_batch, float* __restrict__ grad,
+                                                           float* __restrict__ loss, uint32_t* __restrict__ status)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kBwdBar);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kBwdBar + 8);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    // W_l^T for l = 2..5 (tile rows = layer inputs, K = layer outputs)
+    for (int l = 1; l < 5; l++) load_matrix(smem + bwd_wt(l), params + w_off(l), layer_out(l), layer_in(l), true);
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        tc::mbar_init_fence();
+    }
+    if (warp == 0) tc::tmem_alloc(s_tmem, 512);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *s_tmem;
+    const uint32_t dh_col = 0, dw_col = 256;
+    unsigned char* sDZ = smem + kBwdDZ;
+    unsigned char* sDZT = smem + kBwdDZT;
+    unsigned char* sHT = smem + kBwdHT;
+    uint32_t phase = 0;
+    bool alive = true;
+    const uint32_t half = tid >> 6, k_in_half = tid & 63u;
+
+    const uint32_t ntiles = (n + kTile - 1) / kTile;
+    for (uint32_t tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x) {
+        const uint32_t row = tile * kTile + tid;
+        const bool valid = row < n;
+        // dL/dz of the output layer (rows 40..47 and invalid samples are zero)
+        float dz[kHid];
+        for (int c = 0; c < kHid; c++) dz[c] = 0.0f;
+        float lsum = 0.0f;
+        if (valid) {
+            float z[kOutUsed];
+            for (int c = 0; c < kOutUsed; c++) z[c] = raw[(size_t)row * kOutUsed + c];
+            Lobes L;
+            lobes_from_raw(z, L);
+            const float w3[3] = {dirs[3 * (size_t)row], dirs[3 * (size_t)row + 1], dirs[3 * (size_t)row + 2]};
+            lsum = loss_grad(L, w3, weights[row] * inv_batch, dz);
+        }
+        warp_atomic_add(loss, lsum);
+        // layers 5..1 (l = 4..0)
+        for (int l = 4; l >= 0 && alive; l--) {
+            const uint32_t Nl = layer_out(l), Kin = layer_in(l);
+            // dZ_l: bias gradient, K-major copy (A of dH) and the two-halves transpose (A' of dW)
+            for (uint32_t c = 0; c < Nl; c++) warp_atomic_add(grad + b_off(l) + c, dz[c]);
+            for (uint32_t c = 0; c < Nl; c += 8) put8(sDZ, tid, c, Nl, dz + c);
+            for (uint32_t c = 0; c < kHid; c++) put1(sDZT, c + 64u * half, k_in_half, 64, c < Nl ? dz[c] : 0.0f);
+            // H_{l-1}^T two-halves (B' of dW): the layer's input activations of this tile
+            {
+                const __nv_bfloat16* h = acts + (size_t)(valid ? row : 0) * kActs + (l == 0 ? 0 : kIn + (l - 1) * kHid);
+                for (uint32_t i = 0; i < Kin; i++) {
+                    const float v = valid ? __bfloat162float(h[i]) : 0.0f;
+                    put1(sHT, i + Kin * half, k_in_half, 64, v);
+                }
+            }
+            block_sync_for_mma();
+            if (tid == 0) {
+                // dW: [dZ_1^T ; dZ_2^T] (128 x 64) x [H_1^T ; H_2^T]^T -> 128 x 2 Kin
+                const uint32_t idesc_w = tc::idesc_bf16_f32(128, 2 * Kin);
+                const uint32_t a0 = tc::smem_addr(sDZT), b0 = tc::smem_addr(sHT);
+                for (uint32_t ks = 0; ks < 4; ks++)
+                    tc::mma_bf16(tmem + dw_col, tc::kmajor_desc(a0 + ks * 256u, 64), tc::kmajor_desc(b0 + ks * 256u, 64),
+                                 idesc_w, ks > 0 ? 1u : 0u);
+                // dH_{l-1} = dZ_l (128 x Nl) x (W_l^T, Kin x Nl)^T
+                if (l > 0) {
+                    const uint32_t idesc_h = tc::idesc_bf16_f32(128, Kin);
+                    const uint32_t a1 = tc::smem_addr(sDZ), b1 = tc::smem_addr(smem + bwd_wt(l));
+                    for (uint32_t ks = 0; ks < Nl / 16; ks++)
+                        tc::mma_bf16(tmem + dh_col, tc::kmajor_desc(a1 + ks * 256u, Nl),
+                                     tc::kmajor_desc(b1 + ks * 256u, Nl), idesc_h, ks > 0 ? 1u : 0u);
+                }
+                tc::mma_commit(bar);
+            }
+            alive = wait_layer(bar, phase, status);
+            if (!alive) break;
+            // dW block of this thread's row: output feature o of its half
+            {
+                const uint32_t o = tid & 63u;
+                const uint32_t col0 = dw_col + Kin * half;
+                float* gW = grad + w_off(l);
+                for (uint32_t c = 0; c < Kin; c += 16) {
+                    float v[16];
+                    tc::tmem_load16(tc::tmem_at(tmem, warp * 32, col0 + c), v);
+                    tc::tmem_wait_ld();
+                    if (o < (l == 4 ? (uint32_t)kOutUsed : Nl))
+                        for (int q = 0; q < 16; q++)
+                            if (v[q] != 0.0f) atomicAdd(gW + o * Kin + c + q, v[q]);
+                }
+            }
+            if (l > 0) {
+                // dZ_{l-1} = dH_{l-1} * relu'(H_{l-1})
+                float dh[kHid];
+                for (int c = 0; c < kHid; c += 16) tc::tmem_load16(tc::tmem_at(tmem, warp * 32, dh_col + c), dh + c);
+                tc::tmem_wait_ld();
+                const __nv_bfloat16* h = acts + (size_t)(valid ? row : 0) * kActs + kIn + (l - 1) * kHid;
+                for (int c = 0; c < kHid; c++) dz[c] = (valid && __bfloat162float(h[c]) > 0.0f) ? dh[c] : 0.0f;
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+        }
+    }
+    release_tmem(bar, phase, alive, tmem, 512);
+}
+
+__global__ void k_guide_adam(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m,
+                             float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    g[i] = 0.0f;
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+}  // namespace
+}  // namespace lmgpu
+
+using namespace lmgpu;
+
+struct lmgpu_guide {
+    float* params = nullptr;  // FP32 master parameters
+    float* grad = nullptr;
+    float* m = nullptr;
+    float* v = nullptr;
+    float* loss = nullptr;    // [1]
+    uint32_t* status = nullptr;
+    Box box{};
+    uint64_t step = 0;
+    // scratch of the host-pointer entry points and of training
+    uint64_t cap = 0;
+    float* d_q = nullptr;
+    float* d_raw = nullptr;
+    float* d_dir = nullptr;
+    float* d_w = nullptr;
+    __nv_bfloat16* d_acts = nullptr;
+    int grid = 0;
+};
+
+namespace lmgpu {
+namespace {
+
+int ensure_scratch(lmgpu_guide* g, uint64_t n)
+{
+    if (g->cap >= n) return LMGPU_OK;
+    void* ptrs[] = {g->d_q, g->d_raw, g->d_dir, g->d_w, g->d_acts};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    g->d_q = g->d_raw = g->d_dir = g->d_w = nullptr;
+    g->d_acts = nullptr;
+    g->cap = 0;
+    if (cudaMalloc(&g->d_q, sizeof(float) * 9 * n) != cudaSuccess ||
+        cudaMalloc(&g->d_raw, sizeof(float) * kOutUsed * n) != cudaSuccess ||
+        cudaMalloc(&g->d_dir, sizeof(float) * 3 * n) != cudaSuccess ||
+        cudaMalloc(&g->d_w, sizeof(float) * n) != cudaSuccess ||
+        cudaMalloc(&g->d_acts, sizeof(__nv_bfloat16) * kActs * n) != cudaSuccess) {
+        set_error("lmgpu_guide: scratch allocation failed");
+        return LMGPU_ERR_CUDA;
+    }
+    g->cap = n;
+    return LMGPU_OK;
+}
+
+int guide_grid(lmgpu_guide* g)
+{
+    if (g->grid == 0) {
+        int dev = 0, sms = 0;
+        LMGPU_CUDA_TRY(cudaGetDevice(&dev));
+        LMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        LMGPU_CUDA_TRY(cudaFuncSetAttribute(k_guide_fwd<MODE_RAW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)kFwdSmem));
+        LMGPU_CUDA_TRY(cudaFuncSetAttribute(k_guide_fwd<MODE_TRAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)kFwdSmem));
+        LMGPU_CUDA_TRY(
+            cudaFuncSetAttribute(k_guide_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
+        g->grid = sms;
+    }
+    return LMGPU_OK;
+}
+
+unsigned tiles_grid(lmgpu_guide* g, uint64_t n)
+{
+    const uint64_t tiles = (n + kTile - 1) / kTile;
+    return (unsigned)(tiles < (uint64_t)g->grid ? tiles : (uint64_t)g->grid);
+}
+
+int check_status(lmgpu_guide* g, cudaStream_t s, const char* name)
+{
+    uint32_t st = 0;
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(&st, g->status, sizeof(st), cudaMemcpyDeviceToHost, s));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    if (st) {
+        set_error(std::string(name) + ": tensor-core wait timed out (status " + std::to_string(st) + ")");
+        return LMGPU_ERR_OVERFLOW;
+    }
+    return LMGPU_OK;
+}
+
+}  // namespace
+
+// Device-buffer forward of the raw outputs, used by the guided renderer.
+int guide_forward_device(lmgpu_guide* g, const float* d_queries, uint64_t n, float* d_raw, cudaStream_t s)
+{
+    if (n == 0) return LMGPU_OK;
+    int rc = guide_grid(g);
+    if (rc) return rc;
+    k_guide_fwd<MODE_RAW><<<tiles_grid(g, n), kThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
+                                                                      d_raw, nullptr, g->status);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+    return LMGPU_OK;
+}
+
+// Forward (training) + backward into g->grad for n device samples; the
+// mean loss is accumulated into g->loss.
+int guide_gradient_device(lmgpu_guide* g, const float* d_queries, const float* d_dirs, const float* d_weights,
+                          uint64_t n, cudaStream_t s)
+{
+    if (n == 0) return LMGPU_OK;
+    int rc = guide_grid(g);
+    if (rc || (rc = ensure_scratch(g, n))) return rc;
+    k_guide_fwd<MODE_TRAIN><<<tiles_grid(g, n), kThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
+                                                                        g->d_raw, g->d_acts, g->status);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+    k_guide_bwd<<<tiles_grid(g, n), kThreads, kBwdSmem, s>>>(g->params, g->d_raw, g->d_acts, d_dirs, d_weights,
+                                                             (uint32_t)n, 1.0f / (float)n, g->grad, g->loss,
+                                                             g->status);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+    return LMGPU_OK;
+}
+
+int guide_adam_device(lmgpu_guide* g, float lr, cudaStream_t s)
+{
+    g->step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f - powf(b1, (float)g->step), c2 = 1.0f - powf(b2, (float)g->step);
+    k_guide_adam<<<(kNumParams + 255) / 256, 256, 0, s>>>(g->params, g->grad, g->m, g->v, kNumParams, lr, b1, b2,
+                                                          1e-8f, c1, c2);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+    return LMGPU_OK;
+}
+
+}  // namespace lmgpu
+
+extern "C" {
+
+int lmgpu_guide_num_params(uint64_t* n)
+{
+    clear_error();
+    if (!n) {
+        set_error("lmgpu_guide_num_params: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    *n = kNumParams;
+    return LMGPU_OK;
+}
+
+int lmgpu_guide_create(const float* box_lo_hi, uint32_t seed, lmgpu_guide** out)
+{
+    clear_error();
+    if (!box_lo_hi || !out) {
+        set_error("lmgpu_guide_create: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    *out = nullptr;
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+        set_error("lmgpu_guide_create: no CUDA device");
+        return LMGPU_ERR_NO_DEVICE;
+    }
+    lmgpu_guide* g = new lmgpu_guide();
+    for (int d = 0; d < 3; d++) {
+        const float ext = box_lo_hi[3 + d] - box_lo_hi[d];
+        g->box.lo[d] = box_lo_hi[d];
+        g->box.inv_ext[d] = ext > 0.0f ? 1.0f / ext : 1.0f;
+    }
+    // He-uniform initial weights from a seeded generator, zero biases;
+    // layer-5 padding rows stay zero
+    std::vector<float> p(kNumParams, 0.0f);
+    uint64_t st = 0x9E3779B97F4A7C15ull ^ seed;
+    auto next = [&]() {
+        st += 0x9E3779B97F4A7C15ull;
+        uint64_t z = st;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (float)(z >> 40) * (1.0f / 16777216.0f);
+    };
+    for (int l = 0; l < 5; l++) {
+        const int fan_in = l == 0 ? 6 * kFreqs + 6 : kHid;
+        const float lim = sqrtf(6.0f / (float)fan_in) * (l == 4 ? 0.1f : 1.0f);
+        const int rows = l == 4 ? kOutUsed : layer_out(l);
+        for (int o = 0; o < rows; o++)
+            for (int i = 0; i < layer_in(l); i++) p[w_off(l) + o * layer_in(l) + i] = (2.0f * next() - 1.0f) * lim;
+    }
+    const size_t bytes = sizeof(float) * kNumParams;
+    if (cudaMalloc(&g->params, bytes) != cudaSuccess || cudaMalloc(&g->grad, bytes) != cudaSuccess ||
+        cudaMalloc(&g->m, bytes) != cudaSuccess || cudaMalloc(&g->v, bytes) != cudaSuccess ||
+        cudaMalloc(&g->loss, sizeof(float)) != cudaSuccess || cudaMalloc(&g->status, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMemcpy(g->params, p.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(g->grad, 0, bytes) != cudaSuccess || cudaMemset(g->m, 0, bytes) != cudaSuccess ||
+        cudaMemset(g->v, 0, bytes) != cudaSuccess || cudaMemset(g->loss, 0, sizeof(float)) != cudaSuccess ||
+        cudaMemset(g->status, 0, sizeof(uint32_t)) != cudaSuccess) {
+        set_error("lmgpu_guide_create: allocation failed");
+        lmgpu_guide_destroy(g);
+        return LMGPU_ERR_CUDA;
+    }
+    *out = g;
+    return LMGPU_OK;
+}
+
+void lmgpu_guide_destroy(lmgpu_guide* g)
+{
+    if (!g) return;
+    cudaDeviceSynchronize();
+    void* ptrs[] = {g->params, g->grad, g->m, g->v, g->loss, g->status, g->d_q, g->d_raw, g->d_dir, g->d_w, g->d_acts};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete g;
+}
+
+int lmgpu_guide_get_params(const lmgpu_guide* g, float* out, uint64_t n)
+{
+    clear_error();
+    if (!g || !out || n != (uint64_t)kNumParams) {
+        set_error("lmgpu_guide_get_params: need lmgpu_guide_num_params floats");
+        return LMGPU_ERR_INVALID;
+    }
+    LMGPU_CUDA_TRY(cudaMemcpy(out, g->params, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    return LMGPU_OK;
+}
+
+int lmgpu_guide_set_params(lmgpu_guide* g, const float* in, uint64_t n)
+{
+    clear_error();
+    if (!g || !in || n != (uint64_t)kNumParams) {
+        set_error("lmgpu_guide_set_params: need lmgpu_guide_num_params floats");
+        return LMGPU_ERR_INVALID;
+    }
+    LMGPU_CUDA_TRY(cudaMemcpy(g->params, in, sizeof(float) * n, cudaMemcpyHostToDevice));
+    return LMGPU_OK;
+}
+
+int lmgpu_guide_forward(lmgpu_guide* g, const float* queries, uint64_t n, float* raw)
+{
+    clear_error();
+    if (!g || (n && (!queries || !raw))) {
+        set_error("lmgpu_guide_forward: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    int rc = ensure_scratch(g, n);
+    if (rc) return rc;
+    LMGPU_CUDA_TRY(cudaMemcpy(g->d_q, queries, sizeof(float) * 9 * n, cudaMemcpyHostToDevice));
+    if ((rc = guide_forward_device(g, g->d_q, n, g->d_raw, 0))) return rc;
+    if ((rc = check_status(g, 0, "lmgpu_guide_forward"))) return rc;
+    LMGPU_CUDA_TRY(cudaMemcpy(raw, g->d_raw, sizeof(float) * kOutUsed * n, cudaMemcpyDeviceToHost));
+    return LMGPU_OK;
+}
+
+int lmgpu_guide_gradient(lmgpu_guide* g, const float* queries, const float* dirs, const float* weights, uint64_t n,
+                         float* grad, float* loss)
+{
+    clear_error();
+    if (!g || !grad || (n && (!queries || !dirs || !weights))) {
+        set_error("lmgpu_guide_gradient: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    int rc = ensure_scratch(g, n);
+    if (rc) return rc;
+    LMGPU_CUDA_TRY(cudaMemcpy(g->d_q, queries, sizeof(float) * 9 * n, cudaMemcpyHostToDevice));
+    LMGPU_CUDA_TRY(cudaMemcpy(g->d_dir, dirs, sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
+    LMGPU_CUDA_TRY(cudaMemcpy(g->d_w, weights, sizeof(float) * n, cudaMemcpyHostToDevice));
+    LMGPU_CUDA_TRY(cudaMemset(g->grad, 0, sizeof(float) * kNumParams));
+    LMGPU_CUDA_TRY(cudaMemset(g->loss, 0, sizeof(float)));
+    if ((rc = guide_gradient_device(g, g->d_q, g->d_dir, g->d_w, n, 0))) return rc;
+    if ((rc = check_status(g, 0, "lmgpu_guide_gradient"))) return rc;
+    LMGPU_CUDA_TRY(cudaMemcpy(grad, g->grad, sizeof(float) * kNumParams, cudaMemcpyDeviceToHost));
+    if (loss) LMGPU_CUDA_TRY(cudaMemcpy(loss, g->loss, sizeof(float), cudaMemcpyDeviceToHost));
+    LMGPU_CUDA_TRY(cudaMemset(g->grad, 0, sizeof(float) * kNumParams));
+    return LMGPU_OK;
+}
+
+int lmgpu_guide_train_step(lmgpu_guide* g, const float* queries, const float* dirs, const float* weights, uint64_t n,
+                           float lr, float* loss)
+{
+    clear_error();
+    if (!g || (n && (!queries || !dirs || !weights))) {
+        set_error("lmgpu_guide_train_step: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    int rc = ensure_scratch(g, n);
+    if (rc) return rc;
+    LMGPU_CUDA_TRY(cudaMemcpy(g->d_q, queries, sizeof(float) * 9 * n, cudaMemcpyHostToDevice));
+    LMGPU_CUDA_TRY(cudaMemcpy(g->d_dir, dirs, sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
+    LMGPU_CUDA_TRY(cudaMemcpy(g->d_w, weights, sizeof(float) * n, cudaMemcpyHostToDevice));
+    LMGPU_CUDA_TRY(cudaMemset(g->loss, 0, sizeof(float)));
+    if ((rc = guide_gradient_device(g, g->d_q, g->d_dir, g->d_w, n, 0)) || (rc = guide_adam_device(g, lr, 0)))
+        return rc;
+    if ((rc = check_status(g, 0, "lmgpu_guide_train_step"))) return rc;
+    if (loss) LMGPU_CUDA_TRY(cudaMemcpy(loss, g->loss, sizeof(float), cudaMemcpyDeviceToHost));
+    return LMGPU_OK;
+}
+
+}  // extern "C"

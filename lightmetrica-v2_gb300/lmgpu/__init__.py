@@ -94,6 +94,15 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_render_bdpt.argtypes = [vp, vp, vp, vp]
     L.lmgpu_render_ptmis.argtypes = [vp, vp, vp, vp]
     L.lmgpu_render_ptdirect.argtypes = [vp, vp, vp, vp]
+    L.lmgpu_guide_num_params.argtypes = [ctypes.POINTER(u64)]
+    L.lmgpu_guide_create.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(vp)]
+    L.lmgpu_guide_destroy.argtypes = [vp]
+    L.lmgpu_guide_destroy.restype = None
+    L.lmgpu_guide_get_params.argtypes = [vp, vp, u64]
+    L.lmgpu_guide_set_params.argtypes = [vp, vp, u64]
+    L.lmgpu_guide_forward.argtypes = [vp, vp, u64, vp]
+    L.lmgpu_guide_gradient.argtypes = [vp, vp, vp, vp, u64, vp, vp]
+    L.lmgpu_guide_train_step.argtypes = [vp, vp, vp, vp, u64, ctypes.c_float, vp]
     L.lmgpu_batch_create.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(vp)]
     L.lmgpu_batch_destroy.argtypes = [vp]
     L.lmgpu_batch_destroy.restype = None
@@ -114,7 +123,9 @@ def lib() -> ctypes.CDLL:
                  "lmgpu_render_ptmis", "lmgpu_render_ptmis_device", "lmgpu_render_ptdirect",
                  "lmgpu_batch_create", "lmgpu_batch_render_pt", "lmgpu_batch_render_pt_device",
                  "lmgpu_batch_autotune", "lmgpu_batch_set_tuning", "lmgpu_batch_get_tuning",
-                 "lmgpu_batch_launch_count",
+                 "lmgpu_batch_launch_count", "lmgpu_guide_num_params", "lmgpu_guide_create",
+                 "lmgpu_guide_get_params", "lmgpu_guide_set_params", "lmgpu_guide_forward", "lmgpu_guide_gradient",
+                 "lmgpu_guide_train_step",
                  "lmgpu_render_ptdirect_device",
                  "lmgpu_scene_set_environment"):
         getattr(L, name).restype = ctypes.c_int
@@ -394,6 +405,68 @@ class Batch:
         n = ctypes.c_uint64()
         _check(lib().lmgpu_batch_launch_count(self._h, ctypes.byref(n)))
         return n.value
+
+
+class Guide:
+    """The path-guiding network (lmgpu_guide): 8-lobe vMF mixture from an MLP
+    on the tensor cores.  box = (lo.x, lo.y, lo.z, hi.x, hi.y, hi.z)."""
+
+    def __init__(self, box, seed: int = 0) -> None:
+        b = (ctypes.c_float * 6)(*box)
+        h = ctypes.c_void_p()
+        _check(lib().lmgpu_guide_create(b, seed, ctypes.byref(h)))
+        self._h = h
+
+    @staticmethod
+    def num_params() -> int:
+        n = ctypes.c_uint64()
+        _check(lib().lmgpu_guide_num_params(ctypes.byref(n)))
+        return n.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().lmgpu_guide_destroy(self._h)
+            self._h = None
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        p = np.empty(self.num_params(), np.float32)
+        _check(lib().lmgpu_guide_get_params(self._h, p.ctypes.data, p.size))
+        return p
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        _check(lib().lmgpu_guide_set_params(self._h, p.ctypes.data, p.size))
+
+    def forward(self, queries: np.ndarray) -> np.ndarray:
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 9)
+        raw = np.empty((q.shape[0], 40), np.float32)
+        _check(lib().lmgpu_guide_forward(self._h, q.ctypes.data, q.shape[0], raw.ctypes.data))
+        return raw
+
+    def gradient(self, queries, dirs, weights) -> tuple[float, np.ndarray]:
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 9)
+        d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        w = np.ascontiguousarray(weights, np.float32).reshape(-1)
+        g = np.empty(self.num_params(), np.float32)
+        loss = ctypes.c_float()
+        _check(lib().lmgpu_guide_gradient(self._h, q.ctypes.data, d.ctypes.data, w.ctypes.data, q.shape[0],
+                                          g.ctypes.data, ctypes.byref(loss)))
+        return loss.value, g
+
+    def train_step(self, queries, dirs, weights, lr: float = 1e-3) -> float:
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 9)
+        d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        w = np.ascontiguousarray(weights, np.float32).reshape(-1)
+        loss = ctypes.c_float()
+        _check(lib().lmgpu_guide_train_step(self._h, q.ctypes.data, d.ctypes.data, w.ctypes.data, q.shape[0], lr,
+                                            ctypes.byref(loss)))
+        return loss.value
 
 
 def version() -> str:
