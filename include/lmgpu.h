@@ -331,6 +331,34 @@ int lmgpu_guide_gradient(lmgpu_guide* guide, const float* queries, const float* 
 int lmgpu_guide_train_step(lmgpu_guide* guide, const float* queries, const float* dirs, const float* weights,
                            uint64_t n, float lr, float* loss);
 
+/* ---- Guided path tracing -------------------------------------------------- */
+
+/* alpha: probability of BSDF sampling in the one-sample MIS mixture with the
+ * network (0.5); learning_rate: Adam's (1e-3); train: nonzero to train the
+ * network after every pass; batch: training minibatch (2^18);
+ * max_steps_per_pass: Adam steps after a pass at most. */
+typedef struct {
+    float alpha;
+    float learning_rate;
+    uint32_t train;
+    uint32_t batch;
+    uint32_t max_steps_per_pass;
+} lmgpu_guiding_params;
+
+/* Renders renderer::pt's image with guided direction sampling at diffuse
+ * vertices (one-sample MIS of BSDF sampling and the guide's mixture; every
+ * pass unbiased), params->spp passes of one sample per pixel, training the
+ * guide online between passes.  The film is written as lmgpu_render_pt's;
+ * last_loss (may be NULL) receives the last training step's loss.  Films of
+ * at most 2^21 pixels.  No counterpart in the reference. */
+int lmgpu_render_pt_guided(lmgpu_scene* scene, lmgpu_guide* guide, const lmgpu_pt_params* params,
+                           const lmgpu_guiding_params* guiding, float* image, float* variance, float* last_loss);
+
+/* As lmgpu_render_pt_guided into device buffers on `stream`. */
+int lmgpu_render_pt_guided_device(lmgpu_scene* scene, lmgpu_guide* guide, const lmgpu_pt_params* params,
+                                  const lmgpu_guiding_params* guiding, float* d_image, float* d_variance,
+                                  void* stream, float* last_loss);
+
 /* Largest scene lmgpu_trace_static_scene accepts. */
 #define LMGPU_STATIC_MAX_TRIANGLES 16384
 

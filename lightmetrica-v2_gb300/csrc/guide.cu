@@ -26,6 +26,7 @@
 // kStatusTimeout in its status word, still frees its tensor memory, and
 // returns.
 #include "common.cuh"
+#include "guide_api.cuh"
 #include "lmgpu.h"
 #include "guide_net.cuh"
 #include "tc.cuh"
@@ -495,6 +496,24 @@ int guide_gradient_device(lmgpu_guide* g, const float* d_queries, const float* d
                                                              g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
     return LMGPU_OK;
+}
+
+void guide_box(const lmgpu_guide* g, float lo[3], float inv_ext[3])
+{
+    for (int d = 0; d < 3; d++) {
+        lo[d] = g->box.lo[d];
+        inv_ext[d] = g->box.inv_ext[d];
+    }
+}
+
+int guide_take_loss(lmgpu_guide* g, cudaStream_t s, float* loss)
+{
+    float l = 0.0f;
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(&l, g->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+    LMGPU_CUDA_TRY(cudaMemsetAsync(g->loss, 0, sizeof(float), s));
+    int rc = check_status(g, s, "lmgpu_guide");
+    if (loss) *loss = l;
+    return rc;
 }
 
 int guide_adam_device(lmgpu_guide* g, float lr, cudaStream_t s)

@@ -291,6 +291,7 @@ void lmgpu_scene_destroy(lmgpu_scene* sc)
     if (sc->stream) cudaStreamSynchronize(sc->stream);
     lmgpu_accel_destroy(sc->accel);
     free_bdpt(sc->bdpt);
+    free_guided(sc->guided);
     void* ptrs[] = {sc->tris, sc->tri_prim, sc->prims, sc->film, sc->film_sq, sc->film_x, sc->film_x_sq,
                     sc->d_image, sc->d_variance,
                     sc->q_ray[0], sc->q_ray[1], sc->q_state[0], sc->q_state[1], sc->q_hit, sc->q_count,

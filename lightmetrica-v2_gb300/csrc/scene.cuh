@@ -51,6 +51,8 @@ struct SceneGPU {
 // (TriangleUtils::CreateTriangleAreaDist, triangleutils.h:40-77).
 struct BdptState;
 void free_bdpt(BdptState* b);
+struct GuidedState;
+void free_guided(GuidedState* g);
 
 struct LightsGPU {
     int32_t count;
@@ -110,7 +112,8 @@ struct lmgpu_scene {
     uint64_t q_cap = 0;
     cudaStream_t stream = nullptr;
     uint64_t launches = 0;  // kernels launched by the renderers since creation
-    lmgpu::BdptState* bdpt = nullptr;  // buffers of the bidirectional renderer
+    lmgpu::BdptState* bdpt = nullptr;      // buffers of the bidirectional renderer
+    lmgpu::GuidedState* guided = nullptr;  // buffers of the guided renderer
 };
 
 namespace lmgpu {

@@ -103,6 +103,8 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_guide_forward.argtypes = [vp, vp, u64, vp]
     L.lmgpu_guide_gradient.argtypes = [vp, vp, vp, vp, u64, vp, vp]
     L.lmgpu_guide_train_step.argtypes = [vp, vp, vp, vp, u64, ctypes.c_float, vp]
+    L.lmgpu_render_pt_guided.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.lmgpu_render_pt_guided_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     L.lmgpu_batch_create.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(vp)]
     L.lmgpu_batch_destroy.argtypes = [vp]
     L.lmgpu_batch_destroy.restype = None
@@ -125,7 +127,7 @@ def lib() -> ctypes.CDLL:
                  "lmgpu_batch_autotune", "lmgpu_batch_set_tuning", "lmgpu_batch_get_tuning",
                  "lmgpu_batch_launch_count", "lmgpu_guide_num_params", "lmgpu_guide_create",
                  "lmgpu_guide_get_params", "lmgpu_guide_set_params", "lmgpu_guide_forward", "lmgpu_guide_gradient",
-                 "lmgpu_guide_train_step",
+                 "lmgpu_guide_train_step", "lmgpu_render_pt_guided", "lmgpu_render_pt_guided_device",
                  "lmgpu_render_ptdirect_device",
                  "lmgpu_scene_set_environment"):
         getattr(L, name).restype = ctypes.c_int
@@ -232,6 +234,11 @@ class PtParams(ctypes.Structure):
 BSDF_NULL, BSDF_DIFFUSE, BSDF_DIELECTRIC, BSDF_COOK_TORRANCE = 0, 1, 2, 3
 
 
+class GuidingParams(ctypes.Structure):
+    _fields_ = [("alpha", ctypes.c_float), ("learning_rate", ctypes.c_float), ("train", ctypes.c_uint32),
+                ("batch", ctypes.c_uint32), ("max_steps_per_pass", ctypes.c_uint32)]
+
+
 class Scene:
     """A device-resident scene (lmgpu_scene): triangles, primitives, camera, BVH.
 
@@ -314,6 +321,29 @@ class Scene:
         prm = PtParams(spp, max_num_vertices, seed)
         _check(lib().lmgpu_render_ptdirect(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
         return img, var
+
+    def render_pt_guided(self, guide, spp: int, max_num_vertices: int = -1, seed: int = 0, alpha: float = 0.5,
+                         learning_rate: float = 1e-3, train: bool = True, batch: int = 1 << 18,
+                         max_steps_per_pass: int = 4) -> tuple[np.ndarray, np.ndarray, float]:
+        """Guided renderer::pt: film, per-pixel variance, last training loss."""
+        img = np.empty((self.height, self.width, 3), np.float32)
+        var = np.empty((self.height, self.width, 3), np.float32)
+        prm = PtParams(spp, max_num_vertices, seed)
+        gp = GuidingParams(alpha, learning_rate, 1 if train else 0, batch, max_steps_per_pass)
+        loss = ctypes.c_float()
+        _check(lib().lmgpu_render_pt_guided(self._h, guide._h, ctypes.byref(prm), ctypes.byref(gp), img.ctypes.data,
+                                            var.ctypes.data, ctypes.byref(loss)))
+        return img, var, loss.value
+
+    def render_pt_guided_device(self, guide, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,
+                                seed: int = 0, alpha: float = 0.5, learning_rate: float = 1e-3, train: bool = True,
+                                batch: int = 1 << 18, max_steps_per_pass: int = 4, stream: int = 0) -> float:
+        prm = PtParams(spp, max_num_vertices, seed)
+        gp = GuidingParams(alpha, learning_rate, 1 if train else 0, batch, max_steps_per_pass)
+        loss = ctypes.c_float()
+        _check(lib().lmgpu_render_pt_guided_device(self._h, guide._h, ctypes.byref(prm), ctypes.byref(gp), d_image,
+                                                   d_variance, stream, ctypes.byref(loss)))
+        return loss.value
 
     def launch_count(self) -> int:
         """Kernels launched by the renderers for this scene so far."""

@@ -333,3 +333,53 @@ def batch_scenes(seed: int = 0x5EED, count: int = 12, grid: int = 16, size: tupl
     """The batched configuration: `count` seeded sphere-grid scenes
     (sphere_grid_scene), ~1.31M triangles each at grid 16."""
     return [sphere_grid_scene(seed, i, *(size or (None, None)), grid=grid) for i in range(count)]
+
+
+def narrow_gap_room(width: int = 1920, height: int = 1080, n_boxes: int = 16666, seed: int = 0x5EED) -> dict:
+    """Learned-guiding scene: a closed 10 x 4 x 10 room (walls facing in,
+    Lambertian albedo 0.8) whose x = 10 wall has a 0.2-wide vertical slit at
+    z in [4.9, 5.1] (the wall is two quads around it: 14 room triangles);
+    outside, a 2 x 2 area light of radiance 50 at x = 10.5 faces the slit,
+    the only light; inside, n_boxes seeded boxes (12 triangles each, sides
+    U[0.03, 0.15], random height in [0, 3], rotated about y; 16,666 boxes =
+    ~200k triangles), albedo 0.8.  Camera at (1, 2, 5) looking at the slit
+    wall, vertical fov 60 degrees."""
+    g = rng(seed, 5005)
+    X, Y, Z = 10.0, 4.0, 10.0
+    z0, z1 = 4.9, 5.1
+    room = np.concatenate([
+        _quad((0, 0, 0), (0, 0, Z), (X, 0, Z), (X, 0, 0)),      # floor, +y
+        _quad((0, Y, 0), (X, Y, 0), (X, Y, Z), (0, Y, Z)),      # ceiling, -y
+        _quad((0, 0, 0), (0, Y, 0), (0, Y, Z), (0, 0, Z)),      # x = 0, +x
+        _quad((0, 0, 0), (X, 0, 0), (X, Y, 0), (0, Y, 0)),      # z = 0, +z
+        _quad((0, 0, Z), (0, Y, Z), (X, Y, Z), (X, 0, Z)),      # z = 10, -z
+        _quad((X, 0, 0), (X, 0, z0), (X, Y, z0), (X, Y, 0)),    # x = 10 below the slit, -x
+        _quad((X, 0, z1), (X, 0, Z), (X, Y, Z), (X, Y, z1)),    # x = 10 beyond the slit, -x
+    ]).astype(np.float32)
+    light = _quad((X + 0.5, 1.0, 4.0), (X + 0.5, 3.0, 4.0), (X + 0.5, 3.0, 6.0), (X + 0.5, 1.0, 6.0)).astype(np.float32)
+    sizes = g.uniform(0.03, 0.15, size=(n_boxes, 3))
+    pos = np.stack([g.uniform(0.3, X - 0.6, n_boxes), g.uniform(0.0, 3.0, n_boxes),
+                    g.uniform(0.3, Z - 0.3, n_boxes)], axis=1)
+    ang = g.uniform(0.0, 360.0, n_boxes)
+    unit = _box((1.0, 1.0, 1.0), 0.0, (0.0, 0.0)).reshape(-1, 3)  # the 36 vertices of the unit box
+    a = np.radians(ang)[:, None]
+    v = unit[None, :, :] * sizes[:, None, :]
+    x = v[:, :, 0] * np.cos(a) + v[:, :, 2] * np.sin(a)
+    zz = -v[:, :, 0] * np.sin(a) + v[:, :, 2] * np.cos(a)
+    boxes = np.stack([x + pos[:, 0:1], v[:, :, 1] + pos[:, 1:2], zz + pos[:, 2:3]], axis=2).reshape(-1, 9)
+    prims = [
+        {"bsdf": BSDF_DIFFUSE, "R": (0.8, 0.8, 0.8), "tris": room},
+        {"bsdf": BSDF_DIFFUSE, "R": (0.8, 0.8, 0.8), "tris": boxes.astype(np.float32)},
+        {"bsdf": BSDF_NULL, "light": True, "Le": (50.0, 50.0, 50.0), "tris": light},
+    ]
+    camera = {"eye": (1.0, 2.0, 5.0), "center": (10.0, 1.5, 5.0), "up": (0.0, 1.0, 0.0), "fov": 60.0,
+              "width": width, "height": height}
+    return {"prims": prims, "camera": camera}
+
+
+def scene_box(scene: dict, pad: float = 1e-3) -> tuple:
+    """Axis-aligned bounds (lo, hi) of a scene's triangles, padded."""
+    tris, _ = scene_triangles(scene)
+    v = tris.reshape(-1, 3)
+    lo, hi = v.min(axis=0) - pad, v.max(axis=0) + pad
+    return tuple(float(x) for x in lo) + tuple(float(x) for x in hi)

@@ -1,0 +1,67 @@
+"""Guided path tracing (lmgpu_render_pt_guided): the one-sample MIS of BSDF
+sampling and the learned vMF mixture keeps renderer::pt's expectation, and
+the trained network lowers the error against a converged image in the scene
+it is built for (light through a narrow slit)."""
+import numpy as np
+import pytest
+
+import imgcheck
+import ptscene
+
+pytestmark = pytest.mark.gpu
+
+
+def small_room(w=64, h=36, boxes=300):
+    from lmgpu import scenes
+
+    return scenes.narrow_gap_room(w, h, n_boxes=boxes, seed=3)
+
+
+def test_guided_alpha_one_is_plain_pt(gpu_lib):
+    """alpha = 1 samples the BSDF only: the same estimator as lmgpu_render_pt."""
+    from lmgpu import scenes
+
+    s = small_room()
+    sc = gpu_lib.Scene(s)
+    g = gpu_lib.Guide(scenes.scene_box(s), 1)
+    a, va, _ = sc.render_pt_guided(g, 2048, -1, 5, alpha=1.0, train=False)
+    b, vb = sc.render_pt(2048, -1, 6)
+    print(imgcheck.assert_same_aggregates(a.astype(np.float64), va.astype(np.float64), b.astype(np.float64),
+                                          vb.astype(np.float64), "guided(alpha=1) vs pt"))
+    sc.close()
+    g.close()
+
+
+def test_guided_is_unbiased_while_training(gpu_lib):
+    """Online training between passes: the guided film agrees with plain PT's."""
+    from lmgpu import scenes
+
+    s = small_room()
+    sc = gpu_lib.Scene(s)
+    g = gpu_lib.Guide(scenes.scene_box(s), 2)
+    a, va, loss = sc.render_pt_guided(g, 1024, -1, 7, alpha=0.5, train=True, batch=1 << 14)
+    b, vb = sc.render_pt(8192, -1, 8)
+    print("last loss", loss)
+    print(imgcheck.assert_same_aggregates(a.astype(np.float64), va.astype(np.float64), b.astype(np.float64),
+                                          vb.astype(np.float64), "guided vs pt"))
+    sc.close()
+    g.close()
+
+
+def test_trained_guide_lowers_error(gpu_lib):
+    """After training, guided passes reach a lower relMSE against a converged
+    plain-PT image than plain PT with the same samples per pixel."""
+    from lmgpu import scenes
+
+    s = small_room(96, 54, 600)
+    sc = gpu_lib.Scene(s)
+    ref, _ = sc.render_pt(32768, -1, 1)
+    g = gpu_lib.Guide(scenes.scene_box(s), 3)
+    sc.render_pt_guided(g, 256, -1, 2, alpha=0.5, train=True, batch=1 << 15)  # training passes
+    gi, _, _ = sc.render_pt_guided(g, 64, -1, 3, alpha=0.5, train=False)
+    pi, _ = sc.render_pt(64, -1, 4)
+    eg, ep = imgcheck.relmse(gi, ref), imgcheck.relmse(pi, ref)
+    print("relMSE at 64 spp: guided", eg, "plain", ep, "ratio", ep / eg)
+    assert eg < 0.7 * ep
+    sc.close()
+    g.close()
