@@ -356,7 +356,8 @@ def narrow_gap_room(width: int = 1920, height: int = 1080, n_boxes: int = 16666,
         _quad((X, 0, 0), (X, 0, z0), (X, Y, z0), (X, Y, 0)),    # x = 10 below the slit, -x
         _quad((X, 0, z1), (X, 0, Z), (X, Y, Z), (X, Y, z1)),    # x = 10 beyond the slit, -x
     ]).astype(np.float32)
-    light = _quad((X + 0.5, 1.0, 4.0), (X + 0.5, 3.0, 4.0), (X + 0.5, 3.0, 6.0), (X + 0.5, 1.0, 6.0)).astype(np.float32)
+    # facing -x, towards the slit
+    light = _quad((X + 0.5, 1.0, 4.0), (X + 0.5, 1.0, 6.0), (X + 0.5, 3.0, 6.0), (X + 0.5, 3.0, 4.0)).astype(np.float32)
     sizes = g.uniform(0.03, 0.15, size=(n_boxes, 3))
     pos = np.stack([g.uniform(0.3, X - 0.6, n_boxes), g.uniform(0.0, 3.0, n_boxes),
                     g.uniform(0.3, Z - 0.3, n_boxes)], axis=1)

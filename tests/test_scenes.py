@@ -38,3 +38,17 @@ def test_caustic_room_shape():
     assert s["prims"][0]["tris"].shape[0] == 20
     assert s["prims"][1]["tris"].shape[0] == 20 * 4 ** 5
     assert tris.shape[0] == 20 + 20480 + 12 + 320
+
+
+def test_narrow_gap_room_shape():
+    s = scenes.narrow_gap_room(64, 36)
+    tris, _ = scenes.scene_triangles(s)
+    assert tris.shape[0] == 14 + 16666 * 12 + 2
+    light = s["prims"][2]["tris"].reshape(-1, 3, 3)
+    n = np.cross(light[:, 1] - light[:, 0], light[:, 2] - light[:, 0])
+    assert np.all(n[:, 0] < 0)  # the light faces the slit (-x)
+    room = s["prims"][0]["tris"].reshape(-1, 3, 3)
+    c = room.mean(axis=1)
+    rn = np.cross(room[:, 1] - room[:, 0], room[:, 2] - room[:, 0])
+    # every wall faces the room's centre
+    assert np.all(((np.array([5.0, 2.0, 5.0]) - c) * rn).sum(axis=1) > 0)
