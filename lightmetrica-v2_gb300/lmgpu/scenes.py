@@ -335,15 +335,45 @@ def batch_scenes(seed: int = 0x5EED, count: int = 12, grid: int = 16, size: tupl
     return [sphere_grid_scene(seed, i, *(size or (None, None)), grid=grid) for i in range(count)]
 
 
-def narrow_gap_room(width: int = 1920, height: int = 1080, n_boxes: int = 16666, seed: int = 0x5EED) -> dict:
+def _tess_box(size, angle_deg, base_xz, k: int) -> np.ndarray:
+    """Box as _box, with every face tessellated into k x k quads (12 k^2
+    triangles, outward facing)."""
+    sx, sy, sz = size
+    x0, x1, y0, y1, z0, z1 = -sx / 2, sx / 2, 0.0, sy, -sz / 2, sz / 2
+    faces = [  # (origin, edge u, edge v) with u x v pointing out
+        ((x0, y1, z0), (0, 0, sz), (sx, 0, 0)),   # top (+y)
+        ((x0, y0, z0), (sx, 0, 0), (0, 0, sz)),   # bottom (-y)
+        ((x0, y0, z0), (0, sy, 0), (sx, 0, 0)),   # front (-z)
+        ((x0, y0, z1), (sx, 0, 0), (0, sy, 0)),   # back (+z)
+        ((x0, y0, z0), (0, 0, sz), (0, sy, 0)),   # left (-x)
+        ((x1, y0, z0), (0, sy, 0), (0, 0, sz)),   # right (+x)
+    ]
+    t = np.linspace(0.0, 1.0, k + 1)
+    out = []
+    for o, u, v in faces:
+        o, u, v = np.array(o), np.array(u), np.array(v)
+        P = o + t[:, None, None] * u + t[None, :, None] * v  # (k+1, k+1, 3)
+        a, b_, c, d = P[:-1, :-1], P[1:, :-1], P[1:, 1:], P[:-1, 1:]
+        out.append(np.concatenate([a, b_, c], axis=2).reshape(-1, 9))
+        out.append(np.concatenate([a, c, d], axis=2).reshape(-1, 9))
+    tri = np.concatenate(out).reshape(-1, 3)
+    ang = np.radians(angle_deg)
+    R = np.array([[np.cos(ang), 0, np.sin(ang)], [0, 1, 0], [-np.sin(ang), 0, np.cos(ang)]])
+    tri = tri @ R.T + np.array([base_xz[0], 0.0, base_xz[1]])
+    return tri.reshape(-1, 9)
+
+
+def narrow_gap_room(width: int = 1920, height: int = 1080, n_furniture: int = 100, tess: int = 13,
+                    seed: int = 0x5EED) -> dict:
     """Learned-guiding scene: a closed 10 x 4 x 10 room (walls facing in,
     Lambertian albedo 0.8) whose x = 10 wall has a 0.2-wide vertical slit at
     z in [4.9, 5.1] (the wall is two quads around it: 14 room triangles);
     outside, a 2 x 2 area light of radiance 50 at x = 10.5 faces the slit,
-    the only light; inside, n_boxes seeded boxes (12 triangles each, sides
-    U[0.03, 0.15], random height in [0, 3], rotated about y; 16,666 boxes =
-    ~200k triangles), albedo 0.8.  Camera at (1, 2, 5) looking at the slit
-    wall, vertical fov 60 degrees."""
+    the only light; inside, n_furniture seeded furniture boxes standing on the
+    floor (footprint U[0.3, 1.2]^2, height U[0.3, 1.5], rotated about y,
+    albedo 0.8), each face tessellated into tess x tess quads (100 boxes at
+    tess 13: ~203k triangles).  Camera at (1, 2, 5) looking at the slit wall,
+    vertical fov 60 degrees."""
     g = rng(seed, 5005)
     X, Y, Z = 10.0, 4.0, 10.0
     z0, z1 = 4.9, 5.1
@@ -358,19 +388,14 @@ def narrow_gap_room(width: int = 1920, height: int = 1080, n_boxes: int = 16666,
     ]).astype(np.float32)
     # facing -x, towards the slit
     light = _quad((X + 0.5, 1.0, 4.0), (X + 0.5, 1.0, 6.0), (X + 0.5, 3.0, 6.0), (X + 0.5, 3.0, 4.0)).astype(np.float32)
-    sizes = g.uniform(0.03, 0.15, size=(n_boxes, 3))
-    pos = np.stack([g.uniform(0.3, X - 0.6, n_boxes), g.uniform(0.0, 3.0, n_boxes),
-                    g.uniform(0.3, Z - 0.3, n_boxes)], axis=1)
-    ang = g.uniform(0.0, 360.0, n_boxes)
-    unit = _box((1.0, 1.0, 1.0), 0.0, (0.0, 0.0)).reshape(-1, 3)  # the 36 vertices of the unit box
-    a = np.radians(ang)[:, None]
-    v = unit[None, :, :] * sizes[:, None, :]
-    x = v[:, :, 0] * np.cos(a) + v[:, :, 2] * np.sin(a)
-    zz = -v[:, :, 0] * np.sin(a) + v[:, :, 2] * np.cos(a)
-    boxes = np.stack([x + pos[:, 0:1], v[:, :, 1] + pos[:, 1:2], zz + pos[:, 2:3]], axis=2).reshape(-1, 9)
+    boxes = []
+    for _ in range(n_furniture):
+        size = (float(g.uniform(0.3, 1.2)), float(g.uniform(0.3, 1.5)), float(g.uniform(0.3, 1.2)))
+        pos = (float(g.uniform(1.0, X - 1.5)), float(g.uniform(0.8, Z - 0.8)))
+        boxes.append(_tess_box(size, float(g.uniform(0.0, 90.0)), pos, tess))
     prims = [
         {"bsdf": BSDF_DIFFUSE, "R": (0.8, 0.8, 0.8), "tris": room},
-        {"bsdf": BSDF_DIFFUSE, "R": (0.8, 0.8, 0.8), "tris": boxes.astype(np.float32)},
+        {"bsdf": BSDF_DIFFUSE, "R": (0.8, 0.8, 0.8), "tris": np.concatenate(boxes).astype(np.float32)},
         {"bsdf": BSDF_NULL, "light": True, "Le": (50.0, 50.0, 50.0), "tris": light},
     ]
     camera = {"eye": (1.0, 2.0, 5.0), "center": (10.0, 1.5, 5.0), "up": (0.0, 1.0, 0.0), "fov": 60.0,

@@ -11,10 +11,10 @@ import ptscene
 pytestmark = pytest.mark.gpu
 
 
-def small_room(w=64, h=36, boxes=300):
+def small_room(w=64, h=36, furniture=20):
     from lmgpu import scenes
 
-    return scenes.narrow_gap_room(w, h, n_boxes=boxes, seed=3)
+    return scenes.narrow_gap_room(w, h, n_furniture=furniture, tess=4, seed=3)
 
 
 def test_guided_alpha_one_is_plain_pt(gpu_lib):
@@ -53,7 +53,7 @@ def test_trained_guide_lowers_error(gpu_lib):
     plain-PT image than plain PT with the same samples per pixel."""
     from lmgpu import scenes
 
-    s = small_room(96, 54, 600)
+    s = small_room(96, 54, 40)
     sc = gpu_lib.Scene(s)
     ref, _ = sc.render_pt(32768, -1, 1)
     g = gpu_lib.Guide(scenes.scene_box(s), 3)

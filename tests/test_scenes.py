@@ -43,7 +43,7 @@ def test_caustic_room_shape():
 def test_narrow_gap_room_shape():
     s = scenes.narrow_gap_room(64, 36)
     tris, _ = scenes.scene_triangles(s)
-    assert tris.shape[0] == 14 + 16666 * 12 + 2
+    assert tris.shape[0] == 14 + 100 * 12 * 13 * 13 + 2
     light = s["prims"][2]["tris"].reshape(-1, 3, 3)
     n = np.cross(light[:, 1] - light[:, 0], light[:, 2] - light[:, 0])
     assert np.all(n[:, 0] < 0)  # the light faces the slit (-x)
@@ -52,3 +52,12 @@ def test_narrow_gap_room_shape():
     rn = np.cross(room[:, 1] - room[:, 0], room[:, 2] - room[:, 0])
     # every wall faces the room's centre
     assert np.all(((np.array([5.0, 2.0, 5.0]) - c) * rn).sum(axis=1) > 0)
+
+
+def test_tessellated_box_faces_out():
+    t = scenes._tess_box((1.0, 2.0, 0.5), 30.0, (3.0, 4.0), 3).reshape(-1, 3, 3)
+    assert t.shape[0] == 12 * 9
+    c = t.mean(axis=1)
+    n = np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0])
+    centre = np.array([3.0, 1.0, 4.0])
+    assert np.all(((c - centre) * n).sum(axis=1) > 0)
