@@ -4,8 +4,9 @@
 // samples.
 //
 //   input   128 features: position normalised to the scene box and encoded
-//           by 16 frequencies (sin, cos of 2^f pi x per axis: 96), normal (3),
-//           outgoing direction (3), zero padding (26)
+//           by 16 frequencies half an octave apart (sin, cos of 2^(f/2) pi x,
+//           f = 0..15, per axis: 96), normal (3), outgoing direction (3), zero
+//           padding (26)
 //   hidden  4 x 64 ReLU
 //   output  8 lobes x (mean 3, kappa 1, weight 1) = 40 (padded to 48)
 //   lobe    mean = m / |m|, kappa = 0.01 + softplus(b) (b clamped to
@@ -67,13 +68,13 @@ __device__ __forceinline__ void features(const float x[3], const float n[3], con
 {
     for (int d = 0; d < 3; d++) {
         const float u = (x[d] - lo[d]) * inv_ext[d];
-        float scale = 1.0f;
         for (int k = 0; k < kFreqs; k++) {
+            // 2^(k/2): whole octaves times 1 or sqrt(2)
+            const float scale = (float)(1u << (k >> 1)) * ((k & 1) ? 1.41421356237309505f : 1.0f);
             float s, c;
             sincospif(u * scale, &s, &c);
             f[d * 2 * kFreqs + 2 * k] = s;
             f[d * 2 * kFreqs + 2 * k + 1] = c;
-            scale *= 2.0f;
         }
     }
     for (int d = 0; d < 3; d++) {

@@ -8,7 +8,9 @@
 // with probability alpha, else from the network's mixture q; its weight is
 // f cos / (alpha cos / pi + (1 - alpha) q(w)), so every pass is unbiased for
 // whatever network it used.  Other BSDFs sample as in renderer::pt.  Each
-// pass is one sample per pixel; the film averages all passes.
+// pass is one sample per pixel; a wave holds as many passes as fit in 2^21
+// paths (the network is trained after each wave); the film averages all
+// passes.
 //
 // Training data: every guided vertex records its query (position, normal,
 // outgoing direction), the sampled direction, the mixture pdf and the
@@ -391,7 +393,9 @@ int render_pt_guided(lmgpu_scene* sc, lmgpu_guide* guide, const lmgpu_pt_params*
     if (rc || (rc = ensure_queues(sc, npix))) return rc;
     if (!sc->guided) sc->guided = new GuidedState();
     GuidedState& G = *sc->guided;
-    const uint64_t W = npix;  // one pass = one wave = one sample per pixel
+    // a wave: whole passes (one sample per pixel each), up to kWave paths
+    const uint64_t per_wave = kWave / npix;
+    const uint64_t W = npix * (per_wave < prm->spp ? per_wave : prm->spp);
     if ((rc = grow_buf(&G.rec, &G.rec_cap, (uint64_t)kMaxRec * W)) || (rc = grow_buf(&G.nrec, &G.nrec_cap, W)) ||
         (rc = grow_buf(&G.queries, &G.queries_cap, 9 * W)) || (rc = grow_buf(&G.q_state, &G.q_state_cap, W)) ||
         (rc = grow_buf(&G.q_prim, &G.q_prim_cap, W)) || (rc = grow_buf(&G.raw, &G.raw_cap, (uint64_t)kOutUsed * W)))
@@ -414,19 +418,20 @@ int render_pt_guided(lmgpu_scene* sc, lmgpu_guide* guide, const lmgpu_pt_params*
         return LMGPU_OK;
     };
     float loss = 0.0f;
-    for (uint64_t pass = 0; pass < prm->spp; pass++) {
+    const uint64_t total = npix * prm->spp;
+    for (uint64_t p0 = 0; p0 < total; p0 += W) {
         Wave w;
-        w.p0 = pass * W;
-        w.n = (uint32_t)W;
+        w.p0 = p0;
+        w.n = (uint32_t)((total - p0) < W ? (total - p0) : W);
         w.npix = (uint32_t)npix;
         w.rec = G.rec;
         w.nrec = G.nrec;
         w.own = sc->q_own;
-        k_gd_generate<<<(unsigned)((W + kGdThreads - 1) / kGdThreads), kGdThreads, 0, stream>>>(
+        k_gd_generate<<<(unsigned)((w.n + kGdThreads - 1) / kGdThreads), kGdThreads, 0, stream>>>(
             sc->cam, w, prm->seed, sc->q_ray[0], sc->q_state[0]);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
-        uint32_t n = (uint32_t)W;
+        uint32_t n = w.n;
         int cur = 0;
         while (n > 0) {
             if ((rc = launch_trace(sc->accel, sc->q_ray[cur], sc->q_hit, n, false, false, stream))) return rc;
@@ -450,13 +455,13 @@ int render_pt_guided(lmgpu_scene* sc, lmgpu_guide* guide, const lmgpu_pt_params*
             n = G.h_counts[0];
             cur = 1 - cur;
         }
-        k_gd_flush<<<(unsigned)((W + 255) / 256), 256, 0, stream>>>(w, sc->film, sc->film_sq);
+        k_gd_flush<<<(w.n + 255) / 256, 256, 0, stream>>>(w, sc->film, sc->film_sq);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
         if (!gp->train) continue;
         // training samples of this pass, then up to max_steps_per_pass Adam steps
         LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts + 2, 0, sizeof(uint32_t), stream));
-        k_gd_collect<<<(unsigned)((W + 255) / 256), 256, 0, stream>>>(w, G.tq, G.tdir, G.tw, (uint32_t)tcap,
+        k_gd_collect<<<(w.n + 255) / 256, 256, 0, stream>>>(w, G.tq, G.tdir, G.tw, (uint32_t)tcap,
                                                                        G.counts + 2);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;

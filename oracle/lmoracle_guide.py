@@ -50,9 +50,9 @@ def bf16(x: np.ndarray) -> np.ndarray:
 
 
 def features(queries: np.ndarray, box_lo_hi) -> np.ndarray:
-    """(n, 128) input features: sin/cos(2^f pi u) of the box-normalised
-    position per axis (axis-major, frequency, then sin/cos), normal,
-    outgoing direction, zeros."""
+    """(n, 128) input features: sin/cos(2^(f/2) pi u), f = 0..15, of the
+    box-normalised position per axis (axis-major, frequency, then sin/cos),
+    normal, outgoing direction, zeros."""
     q = np.asarray(queries, np.float64).reshape(-1, 9)
     lo = np.asarray(box_lo_hi[:3], np.float64)
     hi = np.asarray(box_lo_hi[3:], np.float64)
@@ -60,7 +60,7 @@ def features(queries: np.ndarray, box_lo_hi) -> np.ndarray:
     f = np.zeros((q.shape[0], IN))
     for d in range(3):
         for k in range(FREQS):
-            a = np.pi * u[:, d] * (2.0 ** k)
+            a = np.pi * u[:, d] * (2.0 ** (k // 2)) * (np.sqrt(2.0) if k % 2 else 1.0)
             f[:, d * 2 * FREQS + 2 * k] = np.sin(a)
             f[:, d * 2 * FREQS + 2 * k + 1] = np.cos(a)
     f[:, 6 * FREQS:6 * FREQS + 3] = q[:, 3:6]

@@ -67,8 +67,14 @@ def assert_same_aggregates(a, va, b, vb, label=""):
     return s
 
 
-def relmse(img, ref, eps=1e-2):
-    """Relative MSE of img against ref: mean((img - ref)^2 / (ref^2 + eps))."""
+def relmse(img, ref, eps=1e-2, trim=0.0):
+    """Relative MSE of img against ref: mean((img - ref)^2 / (ref^2 + eps)),
+    per pixel on the channel mean; trim > 0 drops that fraction of the
+    largest per-pixel errors first (outlier-robust form, for images whose
+    error is dominated by a few fireflies)."""
     img = np.asarray(img, np.float64)
     ref = np.asarray(ref, np.float64)
-    return float(np.mean((img - ref) ** 2 / (ref * ref + eps)))
+    e = ((img - ref) ** 2 / (ref * ref + eps)).reshape(-1, img.shape[-1]).mean(axis=1)
+    if trim > 0.0:
+        e = np.sort(e)[: max(1, int(round(e.size * (1.0 - trim))))]
+    return float(e.mean())

@@ -49,19 +49,21 @@ def test_guided_is_unbiased_while_training(gpu_lib):
 
 
 def test_trained_guide_lowers_error(gpu_lib):
-    """After training, guided passes reach a lower relMSE against a converged
-    plain-PT image than plain PT with the same samples per pixel."""
+    """After training, guided passes reach a lower relMSE (0.1 % outlier
+    trimmed) against a converged plain-PT image than plain PT with the same
+    samples per pixel; without training the guide gains nothing."""
     from lmgpu import scenes
 
     s = small_room(96, 54, 40)
     sc = gpu_lib.Scene(s)
-    ref, _ = sc.render_pt(32768, -1, 1)
+    ref, _ = sc.render_pt(65536, -1, 1)
+    pi, _ = sc.render_pt(256, -1, 4)
     g = gpu_lib.Guide(scenes.scene_box(s), 3)
-    sc.render_pt_guided(g, 256, -1, 2, alpha=0.5, train=True, batch=1 << 15)  # training passes
-    gi, _, _ = sc.render_pt_guided(g, 64, -1, 3, alpha=0.5, train=False)
-    pi, _ = sc.render_pt(64, -1, 4)
-    eg, ep = imgcheck.relmse(gi, ref), imgcheck.relmse(pi, ref)
-    print("relMSE at 64 spp: guided", eg, "plain", ep, "ratio", ep / eg)
+    u, _, _ = sc.render_pt_guided(g, 256, -1, 5, alpha=0.5, train=False)
+    sc.render_pt_guided(g, 2048, -1, 2, alpha=0.5, train=True, batch=1 << 16)  # training passes
+    gi, _, _ = sc.render_pt_guided(g, 256, -1, 3, alpha=0.5, train=False)
+    eg, ep, eu = (imgcheck.relmse(x, ref, trim=1e-3) for x in (gi, pi, u))
+    print("trimmed relMSE at 256 spp: guided", eg, "plain", ep, "untrained guide", eu, "gain", ep / eg)
     assert eg < 0.7 * ep
     sc.close()
     g.close()
