@@ -335,14 +335,17 @@ int lmgpu_guide_train_step(lmgpu_guide* guide, const float* queries, const float
 
 /* alpha: probability of BSDF sampling in the one-sample MIS mixture with the
  * network (0.5); learning_rate: Adam's (1e-3); train: nonzero to train the
- * network after every pass; batch: training minibatch (2^18);
- * max_steps_per_pass: Adam steps after a pass at most. */
+ * network after every wave of passes; batch: training minibatch (2^18);
+ * max_steps_per_pass: Adam steps after a wave at most; rr_mode: 0 Russian
+ * roulette with survival 0.5 as renderer::pt, 1 survival min(1, max
+ * throughput component). */
 typedef struct {
     float alpha;
     float learning_rate;
     uint32_t train;
     uint32_t batch;
     uint32_t max_steps_per_pass;
+    uint32_t rr_mode;
 } lmgpu_guiding_params;
 
 /* Renders renderer::pt's image with guided direction sampling at diffuse

@@ -8,7 +8,10 @@
 // with probability alpha, else from the network's mixture q; its weight is
 // f cos / (alpha cos / pi + (1 - alpha) q(w)), so every pass is unbiased for
 // whatever network it used.  Other BSDFs sample as in renderer::pt.  Each
-// pass is one sample per pixel; a wave holds as many passes as fit in 2^21
+// pass is one sample per pixel.  Russian roulette is renderer::pt's (survival
+// 0.5, rr_mode 0) or survival min(1, max throughput) (rr_mode 1), which keeps
+// path weights near 1 where guided weights would otherwise compound (up to
+// 1 / alpha per vertex); both are unbiased.  A wave holds as many passes as fit in 2^21
 // paths (the network is trained after each wave); the film averages all
 // passes.
 //
@@ -98,7 +101,7 @@ __device__ __forceinline__ uint32_t append_slot(bool take, uint32_t* count)
 }
 
 // counts: [0] next path queue, [1] diffuse queries
-__global__ void __launch_bounds__(kGdThreads) k_gd_shade(SceneGPU sc, Wave w, int max_nv, uint32_t seed,
+__global__ void __launch_bounds__(kGdThreads) k_gd_shade(SceneGPU sc, Wave w, int max_nv, uint32_t seed, int rr_mode,
                                                          const float4* __restrict__ rays,
                                                          const PathState* __restrict__ state,
                                                          const lmgpu_hit* __restrict__ hits, uint32_t n,
@@ -164,7 +167,10 @@ __global__ void __launch_bounds__(kGdThreads) k_gd_shade(SceneGPU sc, Wave w, in
             const PrimGPU& P = sc.prims[prim];
             uint32_t nv = s.id.z;
             const Philox4x32 r = philox4x32_10(s.id.x, s.id.y, nv, 0u, seed, kKeyBounce);
-            if (u01(r.v[3]) <= 0.5f) {
+            // roulette: renderer::pt's fixed 0.5, or survival min(1, max(throughput))
+            const float survive = rr_mode == 0 ? 0.5f : fminf(1.0f, fmaxf(s.thr.x, fmaxf(s.thr.y, s.thr.z)));
+            const float rs = 1.0f / survive;
+            if (survive > 0.0f && u01(r.v[3]) <= survive) {
                 nv++;
                 const bool more = max_nv < 0 || (int)nv < max_nv;
                 const float3 wi = d * -1.0f;
@@ -175,7 +181,7 @@ __global__ void __launch_bounds__(kGdThreads) k_gd_shade(SceneGPU sc, Wave w, in
                     qv[3] = gn.x; qv[4] = gn.y; qv[5] = gn.z;
                     qv[6] = wi.x; qv[7] = wi.y; qv[8] = wi.z;
                     qprim = prim;
-                    ns.thr = make_float4(2.0f * s.thr.x, 2.0f * s.thr.y, 2.0f * s.thr.z, s.thr.w);
+                    ns.thr = make_float4(rs * s.thr.x, rs * s.thr.y, rs * s.thr.z, s.thr.w);
                     ns.id = make_uint4(s.id.x, s.id.y, nv, s.id.w);
                 } else if (more) {
                     float3 wo;
@@ -184,7 +190,7 @@ __global__ void __launch_bounds__(kGdThreads) k_gd_shade(SceneGPU sc, Wave w, in
                         keep = true;
                         nr0 = make_float4(pos.x, pos.y, pos.z, 1e-4f);
                         nr1 = make_float4(wo.x, wo.y, wo.z, FLT_MAX);
-                        ns.thr = make_float4(2.0f * s.thr.x * f[0], 2.0f * s.thr.y * f[1], 2.0f * s.thr.z * f[2],
+                        ns.thr = make_float4(rs * s.thr.x * f[0], rs * s.thr.y * f[1], rs * s.thr.z * f[2],
                                              s.thr.w);
                         ns.id = make_uint4(s.id.x, s.id.y, nv, s.id.w);
                     }
@@ -390,12 +396,14 @@ int render_pt_guided(lmgpu_scene* sc, lmgpu_guide* guide, const lmgpu_pt_params*
         return LMGPU_ERR_INVALID;
     }
     int rc = clear_film(sc, npix, stream);
-    if (rc || (rc = ensure_queues(sc, npix))) return rc;
+    if (rc) return rc;
     if (!sc->guided) sc->guided = new GuidedState();
     GuidedState& G = *sc->guided;
     // a wave: whole passes (one sample per pixel each), up to kWave paths
     const uint64_t per_wave = kWave / npix;
     const uint64_t W = npix * (per_wave < prm->spp ? per_wave : prm->spp);
+    // the path queues hold a whole wave
+    if ((rc = ensure_queues(sc, W))) return rc;
     if ((rc = grow_buf(&G.rec, &G.rec_cap, (uint64_t)kMaxRec * W)) || (rc = grow_buf(&G.nrec, &G.nrec_cap, W)) ||
         (rc = grow_buf(&G.queries, &G.queries_cap, 9 * W)) || (rc = grow_buf(&G.q_state, &G.q_state_cap, W)) ||
         (rc = grow_buf(&G.q_prim, &G.q_prim_cap, W)) || (rc = grow_buf(&G.raw, &G.raw_cap, (uint64_t)kOutUsed * W)))
@@ -437,7 +445,7 @@ int render_pt_guided(lmgpu_scene* sc, lmgpu_guide* guide, const lmgpu_pt_params*
             if ((rc = launch_trace(sc->accel, sc->q_ray[cur], sc->q_hit, n, false, false, stream))) return rc;
             LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts, 0, 2 * sizeof(uint32_t), stream));
             k_gd_shade<<<(n + kGdThreads - 1) / kGdThreads, kGdThreads, 0, stream>>>(
-                sg, w, prm->max_num_vertices, prm->seed, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, n,
+                sg, w, prm->max_num_vertices, prm->seed, (int)gp->rr_mode, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, n,
                 sc->q_ray[1 - cur], sc->q_state[1 - cur], G.queries, G.q_state, G.q_prim, G.counts);
             LMGPU_CUDA_TRY(cudaGetLastError());
             sc->launches += 2;

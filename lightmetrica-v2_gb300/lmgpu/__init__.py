@@ -236,7 +236,7 @@ BSDF_NULL, BSDF_DIFFUSE, BSDF_DIELECTRIC, BSDF_COOK_TORRANCE = 0, 1, 2, 3
 
 class GuidingParams(ctypes.Structure):
     _fields_ = [("alpha", ctypes.c_float), ("learning_rate", ctypes.c_float), ("train", ctypes.c_uint32),
-                ("batch", ctypes.c_uint32), ("max_steps_per_pass", ctypes.c_uint32)]
+                ("batch", ctypes.c_uint32), ("max_steps_per_pass", ctypes.c_uint32), ("rr_mode", ctypes.c_uint32)]
 
 
 class Scene:
@@ -324,12 +324,12 @@ class Scene:
 
     def render_pt_guided(self, guide, spp: int, max_num_vertices: int = -1, seed: int = 0, alpha: float = 0.5,
                          learning_rate: float = 1e-3, train: bool = True, batch: int = 1 << 18,
-                         max_steps_per_pass: int = 4) -> tuple[np.ndarray, np.ndarray, float]:
+                         max_steps_per_pass: int = 4, rr_mode: int = 1) -> tuple[np.ndarray, np.ndarray, float]:
         """Guided renderer::pt: film, per-pixel variance, last training loss."""
         img = np.empty((self.height, self.width, 3), np.float32)
         var = np.empty((self.height, self.width, 3), np.float32)
         prm = PtParams(spp, max_num_vertices, seed)
-        gp = GuidingParams(alpha, learning_rate, 1 if train else 0, batch, max_steps_per_pass)
+        gp = GuidingParams(alpha, learning_rate, 1 if train else 0, batch, max_steps_per_pass, rr_mode)
         loss = ctypes.c_float()
         _check(lib().lmgpu_render_pt_guided(self._h, guide._h, ctypes.byref(prm), ctypes.byref(gp), img.ctypes.data,
                                             var.ctypes.data, ctypes.byref(loss)))
@@ -337,9 +337,10 @@ class Scene:
 
     def render_pt_guided_device(self, guide, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,
                                 seed: int = 0, alpha: float = 0.5, learning_rate: float = 1e-3, train: bool = True,
-                                batch: int = 1 << 18, max_steps_per_pass: int = 4, stream: int = 0) -> float:
+                                batch: int = 1 << 18, max_steps_per_pass: int = 4, rr_mode: int = 1,
+                                stream: int = 0) -> float:
         prm = PtParams(spp, max_num_vertices, seed)
-        gp = GuidingParams(alpha, learning_rate, 1 if train else 0, batch, max_steps_per_pass)
+        gp = GuidingParams(alpha, learning_rate, 1 if train else 0, batch, max_steps_per_pass, rr_mode)
         loss = ctypes.c_float()
         _check(lib().lmgpu_render_pt_guided_device(self._h, guide._h, ctypes.byref(prm), ctypes.byref(gp), d_image,
                                                    d_variance, stream, ctypes.byref(loss)))

@@ -24,7 +24,7 @@ def test_guided_alpha_one_is_plain_pt(gpu_lib):
     s = small_room()
     sc = gpu_lib.Scene(s)
     g = gpu_lib.Guide(scenes.scene_box(s), 1)
-    a, va, _ = sc.render_pt_guided(g, 2048, -1, 5, alpha=1.0, train=False)
+    a, va, _ = sc.render_pt_guided(g, 2048, -1, 5, alpha=1.0, train=False, rr_mode=0)
     b, vb = sc.render_pt(2048, -1, 6)
     print(imgcheck.assert_same_aggregates(a.astype(np.float64), va.astype(np.float64), b.astype(np.float64),
                                           vb.astype(np.float64), "guided(alpha=1) vs pt"))
