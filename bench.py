@@ -108,11 +108,13 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def measured_peak() -> tuple[float, str]:
+def measured_peak(key: str = "hbm_gbs") -> tuple[float, str]:
+    """A measured peak of the GB300s (hbm_gbs: copy GB/s; bf16_tflops:
+    cuBLAS bf16 burst TFLOP/s), else the stated fallback."""
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(p):
-        return float(json.load(open(p))["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, burst)"
-    return 6800.0, "fallback"
+        return float(json.load(open(p))[key]), f"measured (MEASURED_PEAKS.json {key}, burst)"
+    return (6800.0 if key == "hbm_gbs" else 1900.0), "fallback"
 
 
 def traffic_per_launch() -> float | None:
@@ -494,6 +496,138 @@ def run_batch(args) -> None:
         sc.close()
 
 
+def run_guiding(args) -> None:
+    """Learned path guiding vs plain PT on the narrow-gap room: equal-time
+    relMSE.  The room is rendered at 480x270 (the configuration's 1920x1080
+    reduced 16x so that the FP64 reference converges inside the run): the
+    reference is path tracing with throughput-based roulette (unguided,
+    unbiased, 16,384 spp, FP64 film).  Plain renderer::pt (the drop-in, fixed
+    0.5 roulette) and the guided tracer (online training, throughput
+    roulette) each run for the same wall time T; value = relMSE(plain) /
+    relMSE(guided).  Also reported: the unguided tracer with the guided one's
+    roulette at equal time (what the roulette alone gives), the trained
+    guide frozen, and the tensor-core MLP kernels' throughput."""
+    import torch
+
+    import lmgpu
+    from lmgpu import scenes
+
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    W, H = 480, 270
+    T = float(os.environ.get("LMGPU_GUIDING_SECONDS", "4"))
+    s = scenes.narrow_gap_room(W, H)
+    sc = lmgpu.Scene(s)
+    box = scenes.scene_box(s)
+
+    def relmse(img, ref, trim=0.0):
+        e = ((img.astype(np.float64) - ref) ** 2 / (ref * ref + 1e-2)).mean(axis=2).ravel()
+        if trim > 0:
+            e = np.sort(e)[: int(e.size * (1 - trim))]
+        return float(e.mean())
+
+    g0 = lmgpu.Guide(box, 1)
+    t0 = time.perf_counter()
+    ref, _, _ = sc.render_pt_guided(g0, 16384, -1, 1, alpha=1.0, train=False, rr_mode=1)
+    ref_s = time.perf_counter() - t0
+    ref = ref.astype(np.float64)
+
+    def timed(fn, spp):
+        t1 = time.perf_counter()
+        out = fn(spp)
+        return out, time.perf_counter() - t1
+
+    def equal_time(fn, probe_spp=64):
+        _, dt = timed(fn, probe_spp)
+        spp = max(1, int(probe_spp * T / dt))
+        return timed(fn, spp), spp
+
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    l0 = sc.launch_count()
+    (plain, tp), spp_p = equal_time(lambda n: sc.render_pt(n, -1, 11)[0])
+    (unguided, tu), spp_u = equal_time(lambda n: sc.render_pt_guided(g0, n, -1, 12, alpha=1.0, train=False,
+                                                                      rr_mode=1)[0])
+    g = lmgpu.Guide(box, 3)
+    probe = lmgpu.Guide(box, 3)
+    _, dtp = timed(lambda n: sc.render_pt_guided(probe, n, -1, 13, train=True), 64)
+    spp_g = max(1, int(64 * T / dtp))
+    (guided, tg) = timed(lambda n: sc.render_pt_guided(g, n, -1, 14, train=True)[0], spp_g)
+    frozen, tf = timed(lambda n: sc.render_pt_guided(g, n, -1, 15, train=False)[0], spp_g)
+    launches = sc.launch_count() - l0
+    clk = clocks.stop()
+    e_p, e_u, e_g, e_f = relmse(plain, ref), relmse(unguided, ref), relmse(guided, ref), relmse(frozen, ref)
+    # equal time exactly: relMSE of a Monte Carlo estimate falls as 1 / time
+    e_p_at_g = e_p * tp / tg
+    e_u_at_g = e_u * tu / tg
+
+    # tensor-core MLP kernels: forward and one training step on 2^20 / 2^18 samples
+    nq, nt = 1 << 20, 1 << 18
+    gen = np.random.default_rng(3)
+    q = np.zeros((nq, 9), np.float32)
+    lo, hi = np.array(box[:3]), np.array(box[3:])
+    q[:, :3] = gen.uniform(lo, hi, size=(nq, 3))
+    for c in (3, 6):
+        v = gen.normal(size=(nq, 3))
+        q[:, c:c + 3] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    d_q = torch.from_numpy(q).cuda()
+    d_raw = torch.empty((nq, 40), dtype=torch.float32, device="cuda")
+    d_dir = torch.from_numpy(q[:nt, 6:9].copy()).cuda()
+    d_w = torch.ones(nt, dtype=torch.float32, device="cuda")
+    st = torch.cuda.Stream()
+    for _ in range(3):
+        g.forward_device(d_q.data_ptr(), nq, d_raw.data_ptr(), st.cuda_stream)
+        g.train_step_device(d_q.data_ptr(), d_dir.data_ptr(), d_w.data_ptr(), nt, 1e-6, st.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    reps = 10
+    e0.record(st)
+    for _ in range(reps):
+        g.forward_device(d_q.data_ptr(), nq, d_raw.data_ptr(), st.cuda_stream)
+    e1.record(st)
+    for _ in range(reps):
+        g.train_step_device(d_q.data_ptr(), d_dir.data_ptr(), d_w.data_ptr(), nt, 1e-6, st.cuda_stream)
+    e2.record(st)
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / reps
+    train_ms = e1.elapsed_time(e2) / reps
+    flop_fwd = 2 * (128 * 64 + 3 * 64 * 64 + 64 * 48)  # per query, padded shapes as issued
+    peak, peak_src = measured_peak(key="bf16_tflops")
+    fwd_tflops = nq * flop_fwd / (fwd_ms * 1e-3) / 1e12
+
+    line = {"metric": "equal-time relMSE ratio, plain renderer::pt / guided (narrow-gap room)",
+            "value": e_p_at_g / e_g, "unit": "x", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": tg * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 path arithmetic; bf16 MLP with f32 accumulation",
+            "data": "synthetic (narrow-gap room: 14-triangle room with a 0.2-wide slit, 2x2 exterior light Le 50, "
+                    "100 tessellated furniture boxes, ~203k triangles)",
+            "config": {"workload": "guiding_narrow_gap_room", "width": W, "height": H,
+                       "resolution_note": "1920x1080 reduced 16x so the FP64 reference converges within the run",
+                       "seconds_per_method": T, "alpha": 0.5, "learning_rate": 1e-3, "batch": 1 << 18,
+                       "reference": {"spp": 16384, "seconds": ref_s,
+                                     "tracer": "path tracing, throughput roulette, unguided, FP64 film"},
+                       "plain_pt": {"spp": spp_p, "seconds": tp, "relmse": e_p, "relmse_trim_0.1pct": relmse(plain, ref, 1e-3),
+                                    "relmse_at_guided_time": e_p_at_g},
+                       "unguided_throughput_roulette": {"spp": spp_u, "seconds": tu, "relmse": e_u,
+                                                        "relmse_at_guided_time": e_u_at_g},
+                       "guided_online": {"spp": spp_g, "seconds": tg, "relmse": e_g,
+                                         "relmse_trim_0.1pct": relmse(guided, ref, 1e-3)},
+                       "guided_frozen_after_training": {"spp": spp_g, "seconds": tf, "relmse": e_f},
+                       "time_to_plain_relmse_fraction": e_g / e_p_at_g,
+                       "gain_over_unguided_same_roulette": e_u_at_g / e_g},
+            "e2e": {"value": e_p_at_g / e_g, "unit": "x", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": W * H * 3 * 4 * 2, "api": "lmgpu_render_pt / lmgpu_render_pt_guided (host films)"},
+            "gpu_launches": launches, "clocks": clk,
+            "mlp": {"forward_queries": nq, "forward_ms": fwd_ms, "forward_Mqueries_per_s": nq / fwd_ms / 1e3,
+                    "train_step_samples": nt, "train_step_ms": train_ms,
+                    "roofline": {"bound": "tensor", "achieved": fwd_tflops, "peak": peak, "unit": "TFLOP/s",
+                                 "frac": fwd_tflops / peak, "peak_source": peak_src,
+                                 "note": "forward FLOPs as issued (128-wide input, 48-wide output)"}}}
+    print(json.dumps(line), flush=True)
+    for x in (g, g0, probe):
+        x.close()
+    sc.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -505,9 +639,10 @@ def main() -> None:
     ap.add_argument("--anyhit", action="store_true", help="time any-hit queries instead of closest hit")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel of the render workloads (profiling of "
                                                         "smaller cases; default: the workload's own)")
-    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt", "batch"], default="raycast",
+    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt", "batch", "guiding"], default="raycast",
                     help="raycast: the BVH ray-cast configuration (default); pt: renderer::pt on the Cornell "
-                         "box; bdpt: renderer::bdpt on the caustic room; batch: 12 scenes in one wavefront")
+                         "box; bdpt: renderer::bdpt on the caustic room; batch: 12 scenes in one wavefront; "
+                         "guiding: learned path guiding vs plain PT at equal time")
     ap.add_argument("--use-ref-binary", action="store_true",
                     help="reference arm: time the reference's own qbvh (x86-64 harness) if built")
     args = ap.parse_args()
@@ -519,6 +654,8 @@ def main() -> None:
         run_render(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "guiding":
+        run_guiding(args)
     else:
         run_gpu(args)
 

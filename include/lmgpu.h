@@ -327,6 +327,12 @@ int lmgpu_guide_forward(lmgpu_guide* guide, const float* queries, uint64_t n, fl
 int lmgpu_guide_gradient(lmgpu_guide* guide, const float* queries, const float* dirs, const float* weights,
                          uint64_t n, float* grad, float* loss);
 
+/* Device-buffer forms, asynchronous on `stream` (no status check; a later
+ * host-buffer call reports tensor-core time-outs). */
+int lmgpu_guide_forward_device(lmgpu_guide* guide, const float* d_queries, uint64_t n, float* d_raw, void* stream);
+int lmgpu_guide_train_step_device(lmgpu_guide* guide, const float* d_queries, const float* d_dirs,
+                                  const float* d_weights, uint64_t n, float lr, void* stream);
+
 /* One Adam step (beta 0.9 / 0.999, learning rate lr) on that loss. */
 int lmgpu_guide_train_step(lmgpu_guide* guide, const float* queries, const float* dirs, const float* weights,
                            uint64_t n, float lr, float* loss);

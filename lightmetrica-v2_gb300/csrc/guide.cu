@@ -667,6 +667,29 @@ int lmgpu_guide_gradient(lmgpu_guide* g, const float* queries, const float* dirs
     return LMGPU_OK;
 }
 
+int lmgpu_guide_forward_device(lmgpu_guide* g, const float* d_queries, uint64_t n, float* d_raw, void* stream)
+{
+    clear_error();
+    if (!g || (n && (!d_queries || !d_raw))) {
+        set_error("lmgpu_guide_forward_device: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    return guide_forward_device(g, d_queries, n, d_raw, (cudaStream_t)stream);
+}
+
+int lmgpu_guide_train_step_device(lmgpu_guide* g, const float* d_queries, const float* d_dirs, const float* d_weights,
+                                  uint64_t n, float lr, void* stream)
+{
+    clear_error();
+    if (!g || (n && (!d_queries || !d_dirs || !d_weights))) {
+        set_error("lmgpu_guide_train_step_device: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    int rc = guide_gradient_device(g, d_queries, d_dirs, d_weights, n, (cudaStream_t)stream);
+    if (rc) return rc;
+    return guide_adam_device(g, lr, (cudaStream_t)stream);
+}
+
 int lmgpu_guide_train_step(lmgpu_guide* g, const float* queries, const float* dirs, const float* weights, uint64_t n,
                            float lr, float* loss)
 {

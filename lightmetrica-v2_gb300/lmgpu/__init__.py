@@ -103,6 +103,8 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_guide_forward.argtypes = [vp, vp, u64, vp]
     L.lmgpu_guide_gradient.argtypes = [vp, vp, vp, vp, u64, vp, vp]
     L.lmgpu_guide_train_step.argtypes = [vp, vp, vp, vp, u64, ctypes.c_float, vp]
+    L.lmgpu_guide_forward_device.argtypes = [vp, vp, u64, vp, vp]
+    L.lmgpu_guide_train_step_device.argtypes = [vp, vp, vp, vp, u64, ctypes.c_float, vp]
     L.lmgpu_render_pt_guided.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.lmgpu_render_pt_guided_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     L.lmgpu_batch_create.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(vp)]
@@ -127,7 +129,8 @@ def lib() -> ctypes.CDLL:
                  "lmgpu_batch_autotune", "lmgpu_batch_set_tuning", "lmgpu_batch_get_tuning",
                  "lmgpu_batch_launch_count", "lmgpu_guide_num_params", "lmgpu_guide_create",
                  "lmgpu_guide_get_params", "lmgpu_guide_set_params", "lmgpu_guide_forward", "lmgpu_guide_gradient",
-                 "lmgpu_guide_train_step", "lmgpu_render_pt_guided", "lmgpu_render_pt_guided_device",
+                 "lmgpu_guide_train_step", "lmgpu_guide_forward_device", "lmgpu_guide_train_step_device",
+                 "lmgpu_render_pt_guided", "lmgpu_render_pt_guided_device",
                  "lmgpu_render_ptdirect_device",
                  "lmgpu_scene_set_environment"):
         getattr(L, name).restype = ctypes.c_int
@@ -489,6 +492,13 @@ class Guide:
         _check(lib().lmgpu_guide_gradient(self._h, q.ctypes.data, d.ctypes.data, w.ctypes.data, q.shape[0],
                                           g.ctypes.data, ctypes.byref(loss)))
         return loss.value, g
+
+    def forward_device(self, d_queries: int, n: int, d_raw: int, stream: int = 0) -> None:
+        _check(lib().lmgpu_guide_forward_device(self._h, d_queries, n, d_raw, stream))
+
+    def train_step_device(self, d_queries: int, d_dirs: int, d_weights: int, n: int, lr: float = 1e-3,
+                          stream: int = 0) -> None:
+        _check(lib().lmgpu_guide_train_step_device(self._h, d_queries, d_dirs, d_weights, n, lr, stream))
 
     def train_step(self, queries, dirs, weights, lr: float = 1e-3) -> float:
         q = np.ascontiguousarray(queries, np.float32).reshape(-1, 9)
