@@ -434,7 +434,7 @@ def run_batch(args) -> None:
     setup_s = time.perf_counter() - t0
     npix = sum(s.width * s.height for s in scs)
     samples = npix * spp
-    tuning = b.autotune(1, max_nv, 99, rr_depth)
+    tuning = b.tuning() if args.no_autotune else b.autotune(1, max_nv, 99, rr_depth)
     d_img = torch.empty(3 * npix, dtype=torch.float32, device="cuda")
     d_var = torch.empty(3 * npix, dtype=torch.float32, device="cuda")
     stream = torch.cuda.Stream()
@@ -496,6 +496,51 @@ def run_batch(args) -> None:
         sc.close()
 
 
+def mlp_timing(g, box) -> dict:
+    """Tensor-core MLP kernels: forward on 2^20 queries and one training step
+    (forward, backward, Adam) on 2^18 samples, CUDA events, after warm-up."""
+    import torch
+
+    nq, nt = 1 << 20, 1 << 18
+    gen = np.random.default_rng(3)
+    q = np.zeros((nq, 9), np.float32)
+    lo, hi = np.array(box[:3]), np.array(box[3:])
+    q[:, :3] = gen.uniform(lo, hi, size=(nq, 3))
+    for c in (3, 6):
+        v = gen.normal(size=(nq, 3))
+        q[:, c:c + 3] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    d_q = torch.from_numpy(q).cuda()
+    d_raw = torch.empty((nq, 40), dtype=torch.float32, device="cuda")
+    d_dir = torch.from_numpy(q[:nt, 6:9].copy()).cuda()
+    d_w = torch.ones(nt, dtype=torch.float32, device="cuda")
+    st = torch.cuda.Stream()
+    for _ in range(3):
+        g.forward_device(d_q.data_ptr(), nq, d_raw.data_ptr(), st.cuda_stream)
+        g.train_step_device(d_q.data_ptr(), d_dir.data_ptr(), d_w.data_ptr(), nt, 1e-6, st.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    reps = 10
+    e0.record(st)
+    for _ in range(reps):
+        g.forward_device(d_q.data_ptr(), nq, d_raw.data_ptr(), st.cuda_stream)
+    e1.record(st)
+    for _ in range(reps):
+        g.train_step_device(d_q.data_ptr(), d_dir.data_ptr(), d_w.data_ptr(), nt, 1e-6, st.cuda_stream)
+    e2.record(st)
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / reps
+    train_ms = e1.elapsed_time(e2) / reps
+    flop_fwd = 2 * (128 * 64 + 3 * 64 * 64 + 64 * 48)  # per query, padded shapes as issued
+    peak, peak_src = measured_peak(key="bf16_tflops")
+    fwd_tflops = nq * flop_fwd / (fwd_ms * 1e-3) / 1e12
+
+    return {"forward_queries": nq, "forward_ms": fwd_ms, "forward_Mqueries_per_s": nq / fwd_ms / 1e3,
+            "train_step_samples": nt, "train_step_ms": train_ms,
+            "roofline": {"bound": "tensor", "achieved": fwd_tflops, "peak": peak, "unit": "TFLOP/s",
+                         "frac": fwd_tflops / peak, "peak_source": peak_src,
+                         "note": "forward FLOPs as issued (128-wide input, 48-wide output)"}}
+
+
 def run_guiding(args) -> None:
     """Learned path guiding vs plain PT on the narrow-gap room: equal-time
     relMSE.  The room is rendered at 480x270 (the configuration's 1920x1080
@@ -516,8 +561,13 @@ def run_guiding(args) -> None:
     W, H = 480, 270
     T = float(os.environ.get("LMGPU_GUIDING_SECONDS", "4"))
     s = scenes.narrow_gap_room(W, H)
-    sc = lmgpu.Scene(s)
     box = scenes.scene_box(s)
+    if args.mlp_only:
+        g = lmgpu.Guide(box, 3)
+        print(json.dumps({"workload": "guiding MLP kernels only", "mlp": mlp_timing(g, box)}), flush=True)
+        g.close()
+        return
+    sc = lmgpu.Scene(s)
 
     def relmse(img, ref, trim=0.0):
         e = ((img.astype(np.float64) - ref) ** 2 / (ref * ref + 1e-2)).mean(axis=2).ravel()
@@ -560,39 +610,7 @@ def run_guiding(args) -> None:
     e_p_at_g = e_p * tp / tg
     e_u_at_g = e_u * tu / tg
 
-    # tensor-core MLP kernels: forward and one training step on 2^20 / 2^18 samples
-    nq, nt = 1 << 20, 1 << 18
-    gen = np.random.default_rng(3)
-    q = np.zeros((nq, 9), np.float32)
-    lo, hi = np.array(box[:3]), np.array(box[3:])
-    q[:, :3] = gen.uniform(lo, hi, size=(nq, 3))
-    for c in (3, 6):
-        v = gen.normal(size=(nq, 3))
-        q[:, c:c + 3] = v / np.linalg.norm(v, axis=1, keepdims=True)
-    d_q = torch.from_numpy(q).cuda()
-    d_raw = torch.empty((nq, 40), dtype=torch.float32, device="cuda")
-    d_dir = torch.from_numpy(q[:nt, 6:9].copy()).cuda()
-    d_w = torch.ones(nt, dtype=torch.float32, device="cuda")
-    st = torch.cuda.Stream()
-    for _ in range(3):
-        g.forward_device(d_q.data_ptr(), nq, d_raw.data_ptr(), st.cuda_stream)
-        g.train_step_device(d_q.data_ptr(), d_dir.data_ptr(), d_w.data_ptr(), nt, 1e-6, st.cuda_stream)
-    torch.cuda.synchronize()
-    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-    reps = 10
-    e0.record(st)
-    for _ in range(reps):
-        g.forward_device(d_q.data_ptr(), nq, d_raw.data_ptr(), st.cuda_stream)
-    e1.record(st)
-    for _ in range(reps):
-        g.train_step_device(d_q.data_ptr(), d_dir.data_ptr(), d_w.data_ptr(), nt, 1e-6, st.cuda_stream)
-    e2.record(st)
-    torch.cuda.synchronize()
-    fwd_ms = e0.elapsed_time(e1) / reps
-    train_ms = e1.elapsed_time(e2) / reps
-    flop_fwd = 2 * (128 * 64 + 3 * 64 * 64 + 64 * 48)  # per query, padded shapes as issued
-    peak, peak_src = measured_peak(key="bf16_tflops")
-    fwd_tflops = nq * flop_fwd / (fwd_ms * 1e-3) / 1e12
+    mlp = mlp_timing(g, box)
 
     line = {"metric": "equal-time relMSE ratio, plain renderer::pt / guided (narrow-gap room)",
             "value": e_p_at_g / e_g, "unit": "x", "n_gpus": 1, "steps": 1, "warmup": 1,
@@ -617,11 +635,7 @@ def run_guiding(args) -> None:
             "e2e": {"value": e_p_at_g / e_g, "unit": "x", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": W * H * 3 * 4 * 2, "api": "lmgpu_render_pt / lmgpu_render_pt_guided (host films)"},
             "gpu_launches": launches, "clocks": clk,
-            "mlp": {"forward_queries": nq, "forward_ms": fwd_ms, "forward_Mqueries_per_s": nq / fwd_ms / 1e3,
-                    "train_step_samples": nt, "train_step_ms": train_ms,
-                    "roofline": {"bound": "tensor", "achieved": fwd_tflops, "peak": peak, "unit": "TFLOP/s",
-                                 "frac": fwd_tflops / peak, "peak_source": peak_src,
-                                 "note": "forward FLOPs as issued (128-wide input, 48-wide output)"}}}
+            "mlp": mlp}
     print(json.dumps(line), flush=True)
     for x in (g, g0, probe):
         x.close()
@@ -643,6 +657,8 @@ def main() -> None:
                     help="raycast: the BVH ray-cast configuration (default); pt: renderer::pt on the Cornell "
                          "box; bdpt: renderer::bdpt on the caustic room; batch: 12 scenes in one wavefront; "
                          "guiding: learned path guiding vs plain PT at equal time")
+    ap.add_argument("--mlp-only", action="store_true", help="guiding: time the MLP kernels only")
+    ap.add_argument("--no-autotune", action="store_true", help="batch: keep the default tuning (profiling runs)")
     ap.add_argument("--use-ref-binary", action="store_true",
                     help="reference arm: time the reference's own qbvh (x86-64 harness) if built")
     args = ap.parse_args()
