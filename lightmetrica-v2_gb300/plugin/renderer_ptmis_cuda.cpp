@@ -47,6 +47,15 @@ public:
     {
         numSamples_ = prop->ChildAs<long long>("num_samples", 10000000L);
         maxNumVertices_ = prop->ChildAs("max_num_vertices", -1);
+        // min_num_vertices (default 0) suppresses contributions of shorter
+        // paths; values up to 2 suppress nothing, larger ones are not
+        // supported by the GPU form
+        const int minNumVertices = prop->ChildAs("min_num_vertices", 0);
+        if (minNumVertices > 2)
+        {
+            LM_LOG_ERROR("renderer::ptmis_cuda: min_num_vertices > 2 is not supported");
+            return false;
+        }
         return true;
     };
 
