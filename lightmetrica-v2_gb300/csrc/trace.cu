@@ -11,7 +11,8 @@
 //     children in octant slots);
 //   * each 80-byte node is fetched as five 16-byte read-only loads, and all
 //     eight child boxes are tested with one FMA per slab
-//     (t = q * (2^e / d) + (p - o) / d);
+//     (t = q * (2^e / d) + (p - o) / d), two children per packed FP32 pair
+//     instruction;
 //   * triangles are 48-byte records, tested with the watertight algorithm of
 //     Woop, Benthin and Wald (JCGT 2013): shear to ray space, edge functions
 //     with unfused products (so shared edges give exactly negated values),
@@ -25,6 +26,8 @@ namespace lmgpu {
 namespace {
 
 constexpr int kTraceThreads = 128;
+// Resident blocks per SM the kernel is compiled for (64 registers a thread).
+constexpr int kTraceBlocksPerSM = 8;
 
 // Persistent traversal.  Each block owns the contiguous ray range
 // [blockIdx * n / grid, (blockIdx + 1) * n / grid) and its warps take rays
@@ -46,7 +49,7 @@ constexpr int kTraceThreads = 128;
 // BVH tab[ray_scene[i]] (the batch renderer's views).  d_n, when not null,
 // holds the ray count on the device (launches captured in CUDA graphs).
 template <bool ANYHIT, bool STATS, bool MULTI>
-__global__ void __launch_bounds__(kTraceThreads) k_trace(const WNode* __restrict__ nodes, const WTri* __restrict__ tris,
+__global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(const WNode* __restrict__ nodes, const WTri* __restrict__ tris,
                                                          const float4* __restrict__ rays, lmgpu_hit* __restrict__ hits,
                                                          uint64_t n, uint32_t num_nodes, uint32_t num_tris,
                                                          int refill, int postpone, uint32_t* __restrict__ status,
@@ -213,25 +216,43 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const WNode* __restrict
 
 }  // namespace
 
-int trace_grid_cap()
+namespace {
+
+// Blocks of the persistent grid of one instantiation (SMs x resident blocks),
+// looked up once per process.
+template <bool ANYHIT, bool STATS, bool MULTI>
+int grid_cap_of()
 {
-    static int grid_cap = 0;
-    if (grid_cap == 0) {
+    static int cap = 0;
+    if (cap == 0) {
         int dev = 0, sms = 0, per_sm = 0;
         LMGPU_CUDA_TRY(cudaGetDevice(&dev));
         LMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         LMGPU_CUDA_TRY(
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false, false, false>, kTraceThreads, 0));
-        grid_cap = sms * (per_sm > 0 ? per_sm : 1);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<ANYHIT, STATS, MULTI>, kTraceThreads, 0));
+        cap = sms * (per_sm > 0 ? per_sm : 1);
     }
-    return grid_cap;
+    return cap;
+}
+
+}  // namespace
+
+int trace_grid_cap()
+{
+    const int caps[] = {grid_cap_of<false, false, false>(), grid_cap_of<true, false, false>(),
+                        grid_cap_of<false, true, false>(),  grid_cap_of<true, true, false>(),
+                        grid_cap_of<false, false, true>(),  grid_cap_of<true, false, true>()};
+    int m = caps[0];
+    for (int c : caps) m = c < m ? c : m;
+    return m;
 }
 
 int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, uint64_t n, bool anyhit, bool stats,
                  cudaStream_t stream)
 {
     if (n == 0) return LMGPU_OK;
-    const int grid_cap = trace_grid_cap();
+    const int grid_cap = anyhit ? (stats ? grid_cap_of<true, true, false>() : grid_cap_of<true, false, false>())
+                                : (stats ? grid_cap_of<false, true, false>() : grid_cap_of<false, false, false>());
     if (grid_cap <= 0) return LMGPU_ERR_CUDA;
     const TraceConfig cfg = a->tune;
     // at least ~4 warps' worth of rays per block
@@ -253,7 +274,7 @@ int launch_trace_multi(const AccelView* d_tab, uint32_t ntab, const float4* d_ra
                        uint32_t* d_status, cudaStream_t stream)
 {
     if (max_n == 0) return LMGPU_OK;
-    const int grid_cap = trace_grid_cap();
+    const int grid_cap = anyhit ? grid_cap_of<true, false, true>() : grid_cap_of<false, false, true>();
     if (grid_cap <= 0) return LMGPU_ERR_CUDA;
     // the ray count is read on the device: the full persistent grid, each
     // block taking its share of whatever count the launch finds

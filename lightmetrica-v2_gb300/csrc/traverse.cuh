@@ -1,6 +1,5 @@
-// Device-side ray traversal primitives shared by the batch traversal kernel
-// (trace.cu) and the renderers' kernels: ray set-up, the 8-wide node test,
-// the watertight triangle test, and a per-thread closest/any-hit query.
+// Device-side ray traversal primitives of the traversal kernel (trace.cu):
+// ray set-up, the 8-wide node test and the watertight triangle test.
 #pragma once
 
 #include "accel.cuh"
@@ -45,16 +44,51 @@ __device__ __forceinline__ void setup_ray(const float4 r0, const float4 r1, RayS
     R.Sz = 1.0f / dkz;
 }
 
-// Byte k of w as a float: the byte becomes the low mantissa bits of 2^23,
-// and subtracting 2^23 leaves it exactly (PRMT + FADD instead of a
-// shift/mask and an int-to-float conversion).
-__device__ __forceinline__ float qbyte(uint32_t w, int k)
+// Packed FP32 pairs (sm_100 and later): one instruction computes two
+// IEEE single-precision results, each rounded as the scalar form would be.
+__device__ __forceinline__ unsigned long long pk2(float lo, float hi)
 {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)k)) - 8388608.0f;
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk2(unsigned long long v, float& lo, float& hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b)
+{
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+// 2^23 + byte k of w, as a float: the byte becomes the low mantissa bits of
+// 2^23 (one PRMT instead of a shift/mask and an int-to-float conversion);
+// subtracting 2^23 afterwards leaves the byte exactly.
+__device__ __forceinline__ float qbyte23(uint32_t w, int k)
+{
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)k));
+}
+
+// Slab distances of children k and k + 1 along one axis: q * a + b for the
+// two quantised planes q in bytes k, k + 1 of w, as one packed pair.
+__device__ __forceinline__ unsigned long long slab2(uint32_t w, int k, unsigned long long a2, unsigned long long b2)
+{
+    const unsigned long long m2 = 0xCB000000CB000000ull;  // (-2^23, -2^23)
+    return fma2(add2(pk2(qbyte23(w, k), qbyte23(w, k + 1)), m2), a2, b2);
 }
 
 // Tests the eight child boxes of one node; returns the hit mask
 // (bits 24..31 inner children in permuted slot order, bits 0..23 triangles).
+// Children are tested in pairs with packed FP32 arithmetic; every distance is
+// the same correctly rounded q * a + b as a scalar FMA would give.
 __device__ __forceinline__ uint32_t intersect_node(const WNode* __restrict__ nodes, uint32_t ni, const RayState& R,
                                                    float tmax, uint32_t& child_base, uint32_t& tri_base,
                                                    uint32_t& imask)
@@ -74,6 +108,8 @@ __device__ __forceinline__ uint32_t intersect_node(const WNode* __restrict__ nod
     tri_base = w1.y;
     const float ax = sx * R.idx, ay = sy * R.idy, az = sz * R.idz;
     const float bx = (px - R.ox) * R.idx, by = (py - R.oy) * R.idy, bz = (pz - R.oz) * R.idz;
+    const unsigned long long ax2 = pk2(ax, ax), ay2 = pk2(ay, ay), az2 = pk2(az, az);
+    const unsigned long long bx2 = pk2(bx, bx), by2 = pk2(by, by), bz2 = pk2(bz, bz);
     const bool nx = R.idx < 0.0f, ny = R.idy < 0.0f, nz = R.idz < 0.0f;
     uint32_t hm = 0;
 #pragma unroll
@@ -85,20 +121,24 @@ __device__ __forceinline__ uint32_t intersect_node(const WNode* __restrict__ nod
         const uint32_t neary = ny ? hiy : loy, fary = ny ? loy : hiy;
         const uint32_t nearz = nz ? hiz : loz, farz = nz ? loz : hiz;
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const float tnx = fmaf(qbyte(nearx, k), ax, bx);
-            const float tny = fmaf(qbyte(neary, k), ay, by);
-            const float tnz = fmaf(qbyte(nearz, k), az, bz);
-            const float tfx = fmaf(qbyte(farx, k), ax, bx);
-            const float tfy = fmaf(qbyte(fary, k), ay, by);
-            const float tfz = fmaf(qbyte(farz, k), az, bz);
-            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, R.tmin));
-            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
-            if (tn <= tf) {
-                const uint32_t meta = (meta4 >> (8 * k)) & 0xffu;
-                uint32_t bit = meta & 0x1fu;
-                if (bit >= 24u) bit ^= R.oct_inv;
-                hm |= (meta >> 5) << bit;
+        for (int k = 0; k < 4; k += 2) {
+            float tnx[2], tny[2], tnz[2], tfx[2], tfy[2], tfz[2];
+            upk2(slab2(nearx, k, ax2, bx2), tnx[0], tnx[1]);
+            upk2(slab2(neary, k, ay2, by2), tny[0], tny[1]);
+            upk2(slab2(nearz, k, az2, bz2), tnz[0], tnz[1]);
+            upk2(slab2(farx, k, ax2, bx2), tfx[0], tfx[1]);
+            upk2(slab2(fary, k, ay2, by2), tfy[0], tfy[1]);
+            upk2(slab2(farz, k, az2, bz2), tfz[0], tfz[1]);
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const float tn = fmaxf(fmaxf(tnx[j], tny[j]), fmaxf(tnz[j], R.tmin));
+                const float tf = fminf(fminf(tfx[j], tfy[j]), fminf(tfz[j], tmax));
+                if (tn <= tf) {
+                    const uint32_t meta = (meta4 >> (8 * (k + j))) & 0xffu;
+                    uint32_t bit = meta & 0x1fu;
+                    if (bit >= 24u) bit ^= R.oct_inv;
+                    hm |= (meta >> 5) << bit;
+                }
             }
         }
     }
@@ -146,82 +186,6 @@ __device__ __forceinline__ bool intersect_tri(const WTri* __restrict__ tris, uin
     b1_out = V * rdet;
     b2_out = W * rdet;
     id_out = __float_as_int(v0.w);
-    return true;
-}
-
-// One ray, one thread: closest hit (anyhit = false) or any hit in
-// [tmin, tmax] against the wide BVH.  Returns false (no hit) and raises a
-// status bit if the tree is malformed or the stack overflows.
-struct TraceView {
-    const WNode* nodes;
-    const WTri* tris;
-    uint32_t num_nodes, num_tris;
-    uint32_t* status;
-};
-
-__device__ __forceinline__ bool trace_single(const TraceView& tv, float3 o, float tmin, float3 d, float tmax,
-                                             bool anyhit, float& t_out, int& id_out, float& b1_out, float& b2_out)
-{
-    RayState R;
-    setup_ray(make_float4(o.x, o.y, o.z, tmin), make_float4(d.x, d.y, d.z, tmax), R);
-    float best_t = tmax, bb1 = 0.0f, bb2 = 0.0f;
-    int best_id = -1;
-    uint2 stack[kStack];
-    int sp = 0;
-    uint2 ng = make_uint2(0u, tv.num_nodes > 0 ? 0x80000000u : 0u);
-    uint32_t budget = tv.num_nodes + 1;
-    while (true) {
-        if (ng.y & 0xff000000u) {
-            const uint32_t bit = 31u - __clz(ng.y & 0xff000000u);
-            ng.y &= ~(1u << bit);
-            const uint32_t slot = (bit - 24u) ^ R.oct_inv;
-            const uint32_t rel = __popc(ng.y & 0xffu & ((1u << slot) - 1u));
-            const uint32_t ni = ng.x + rel;
-            if (ni >= tv.num_nodes || budget-- == 0u) {
-                atomicOr(tv.status, kStatusBadTree);
-                return false;
-            }
-            if (ng.y & 0xff000000u) {
-                if (sp < kStack) stack[sp++] = ng;
-                else atomicOr(tv.status, kStatusStackOverflow);
-            }
-            uint32_t child_base, tri_base, imask;
-            const uint32_t hm = intersect_node(tv.nodes, ni, R, best_t, child_base, tri_base, imask);
-            ng = make_uint2(child_base, (hm & 0xff000000u) | imask);
-            uint32_t tmask = hm & 0x00ffffffu;
-            while (tmask) {
-                const uint32_t k = __ffs(tmask) - 1u;
-                tmask &= tmask - 1u;
-                if (tri_base + k >= tv.num_tris) {
-                    atomicOr(tv.status, kStatusBadTree);
-                    return false;
-                }
-                float t, b1, b2;
-                int id;
-                if (intersect_tri(tv.tris, tri_base + k, R, best_t, t, b1, b2, id)) {
-                    if (t < best_t || id > best_id) {
-                        best_t = t;
-                        best_id = id;
-                        bb1 = b1;
-                        bb2 = b2;
-                    }
-                    if (anyhit) {
-                        t_out = t; id_out = id; b1_out = b1; b2_out = b2;
-                        return true;
-                    }
-                }
-            }
-        } else if (sp > 0) {
-            ng = stack[--sp];
-        } else {
-            break;
-        }
-    }
-    if (best_id < 0) return false;
-    t_out = best_t;
-    id_out = best_id;
-    b1_out = bb1;
-    b2_out = bb2;
     return true;
 }
 
