@@ -16,9 +16,9 @@
 //      shared memory (16 bins per axis, stable block partition);
 //   3. collapse: a top-down pass turns the binary tree into 8-wide nodes,
 //      expanding the child of largest surface area until 8 children exist,
-//      ordering children by ray octant, quantising child boxes to 8 bits
-//      against a padded frame, and writing each node's leaf triangles
-//      contiguously.
+//      ordering children by ray octant, quantising child boxes outward to
+//      8 bits against a frame one step below the node's lower corner, and
+//      writing each node's leaf triangles contiguously.
 //
 // Leaves hold at most kMaxLeaf = 3 triangles (a wide-node leaf slot encodes
 // its count in 3 unary bits).  The tree topology is deterministic; node
@@ -930,8 +930,10 @@ __global__ void k_collapse(const CollapseItem* __restrict__ in, int nin, Collaps
         if (child_at[s] < 0) continue;
         const BNode b = bnodes[child_at[s]];
         for (int k = 0; k < 3; k++) {
-            double lo = floor(((double)b.lo[k] - (double)p[k]) / sc[k]) - 1.0;
-            double hi = ceil(((double)b.hi[k] - (double)p[k]) / sc[k]) + 1.0;
+            // conservative (floor / ceil) and otherwise tight: the traversal's
+            // slab test carries the margin for its own rounding
+            double lo = floor(((double)b.lo[k] - (double)p[k]) / sc[k]);
+            double hi = ceil(((double)b.hi[k] - (double)p[k]) / sc[k]);
             lo = lo < 0.0 ? 0.0 : (lo > 255.0 ? 255.0 : lo);
             hi = hi < 0.0 ? 0.0 : (hi > 255.0 ? 255.0 : hi);
             qlo[k][s] = (uint8_t)lo;

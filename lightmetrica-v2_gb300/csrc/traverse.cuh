@@ -133,7 +133,10 @@ __device__ __forceinline__ uint32_t intersect_node(const WNode* __restrict__ nod
             for (int j = 0; j < 2; j++) {
                 const float tn = fmaxf(fmaxf(tnx[j], tny[j]), fmaxf(tnz[j], R.tmin));
                 const float tf = fminf(fminf(tfx[j], tfy[j]), fminf(tfz[j], tmax));
-                if (tn <= tf) {
+                // margin 2^-19 relative: above the rounding of both distances
+                // (a few ulps of t each, Ize 2013), so a box the ray meets is
+                // never rejected although the quantised boxes are tight
+                if (tn <= tf * (1.0f + 0x1p-19f)) {
                     const uint32_t meta = (meta4 >> (8 * (k + j))) & 0xffu;
                     uint32_t bit = meta & 0x1fu;
                     if (bit >= 24u) bit ^= R.oct_inv;
