@@ -13,15 +13,18 @@
 //      chosen by one warp per task, and the range is partitioned stably
 //      (chunk counts -> per-task scan -> scatter);
 //   2. small phase: one block per remaining task builds its whole subtree in
-//      shared memory (16 bins per axis, stable block partition);
+//      shared memory (32 bins per axis, stable block partition);
 //   3. collapse: a top-down pass turns the binary tree into 8-wide nodes,
 //      expanding the child of largest surface area until 8 children exist,
 //      ordering children by ray octant, quantising child boxes outward to
 //      8 bits against a frame one step below the node's lower corner, and
 //      writing each node's leaf triangles contiguously.
 //
-// Leaves hold at most kMaxLeaf = 3 triangles (a wide-node leaf slot encodes
-// its count in 3 unary bits).  The tree topology is deterministic; node
+// Leaves hold kMaxLeaf = 1 triangle, so every triangle is a child slot of a
+// wide node with its own quantised box (a slot's meta byte encodes a count
+// of up to 3 in unary bits; measured on the 1.5M-triangle ray-cast scene, 1
+// beats 2 and 3: 4.1 triangle tests and 22.2 node fetches per ray against
+// 13.9 and 20.4 at 3, +16 % rays/s).  The tree topology is deterministic; node
 // storage order depends on atomic allocation order, which changes no query
 // result.
 #include "accel.cuh"
@@ -35,13 +38,13 @@ namespace lmgpu {
 namespace {
 
 constexpr int kBinsLarge = 32;
-constexpr int kBinsSmall = 16;
+constexpr int kBinsSmall = 32;
 constexpr int kBinWords = 13;  // count, aabb lo[3], aabb hi[3], centroid lo[3], centroid hi[3]
 constexpr int kChunk = 2048;   // primitives per block in the large phase
 constexpr int kLargeThreads = 256;
 constexpr int kSmallTask = 1024;
 constexpr int kSmallThreads = 128;
-constexpr int kMaxLeaf = 3;
+constexpr int kMaxLeaf = 1;
 constexpr int kSmallStack = 48;
 
 struct Task {

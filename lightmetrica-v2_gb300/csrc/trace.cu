@@ -96,8 +96,10 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(cons
                 const uint64_t id = base + __popc(idle & lt_mask);
                 if (id < end) {
                     rid = id;
-                    const float4 r0 = __ldg(rays + 2 * id);
-                    const float4 r1 = __ldg(rays + 2 * id + 1);
+                    // rays and hits stream through once: cache-streaming
+                    // accesses leave L1 / L2 to the BVH
+                    const float4 r0 = __ldcs(rays + 2 * id);
+                    const float4 r1 = __ldcs(rays + 2 * id + 1);
                     if (MULTI) {
                         const uint32_t sidx = ray_scene[id];
                         if (sidx < ntab) {
@@ -160,7 +162,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(cons
                 h.prim = best_id;
                 h.b1 = best_b1;
                 h.b2 = best_b2;
-                reinterpret_cast<float4*>(hits)[rid] = *reinterpret_cast<const float4*>(&h);
+                __stcs(reinterpret_cast<float4*>(hits) + rid, *reinterpret_cast<const float4*>(&h));
                 if (STATS && best_id >= 0) nhits++;
                 active = false;
             }
