@@ -21,10 +21,10 @@
 //      writing each node's leaf triangles contiguously.
 //
 // Leaves hold kMaxLeaf = 1 triangle, so every triangle is a child slot of a
-// wide node with its own quantised box (a slot's meta byte encodes a count
-// of up to 3 in unary bits; measured on the 1.5M-triangle ray-cast scene, 1
-// beats 2 and 3: 4.1 triangle tests and 22.2 node fetches per ray against
-// 13.9 and 20.4 at 3, +16 % rays/s).  The tree topology is deterministic; node
+// wide node with its own quantised box, and a node marks its triangle slots
+// with one 8-bit mask.  Measured on the 1.5M-triangle ray-cast scene, leaves
+// of 1 beat leaves of up to 2 or 3: 4.1 triangle tests and 22.2 node
+// fetches per ray against 13.9 and 20.4 at 3, +16 % rays/s.  The tree topology is deterministic; node
 // storage order depends on atomic allocation order, which changes no query
 // result.
 #include "accel.cuh"
@@ -44,7 +44,7 @@ constexpr int kChunk = 2048;   // primitives per block in the large phase
 constexpr int kLargeThreads = 256;
 constexpr int kSmallTask = 1024;
 constexpr int kSmallThreads = 128;
-constexpr int kMaxLeaf = 1;
+constexpr int kMaxLeaf = 1;  // the node format (one triangle per leaf slot) relies on it
 constexpr int kSmallStack = 48;
 
 struct Task {
@@ -924,11 +924,10 @@ __global__ void k_collapse(const CollapseItem* __restrict__ in, int nin, Collaps
         return;
     }
 
-    uint8_t meta[8], qlo[3][8], qhi[3][8];
-    uint32_t imask = 0;
+    uint8_t qlo[3][8], qhi[3][8];
+    uint32_t imask = 0, lmask = 0;
     int inner_rank = 0, tri_off = 0;
     for (int s = 0; s < 8; s++) {
-        meta[s] = 0;
         for (int k = 0; k < 3; k++) { qlo[k][s] = 0; qhi[k][s] = 0; }
         if (child_at[s] < 0) continue;
         const BNode b = bnodes[child_at[s]];
@@ -948,7 +947,7 @@ __global__ void k_collapse(const CollapseItem* __restrict__ in, int nin, Collaps
                 atomicOr(status, kStatusBuildOverflow);
                 return;
             }
-            meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | (uint32_t)tri_off);
+            lmask |= 1u << s;
             for (int j = 0; j < cnt; j++) {
                 const int g = idx[b.begin + j];
                 const float* v = tris + 9 * (size_t)g;
@@ -960,7 +959,6 @@ __global__ void k_collapse(const CollapseItem* __restrict__ in, int nin, Collaps
             }
             tri_off += cnt;
         } else {
-            meta[s] = (uint8_t)((1u << 5) | (24u + (uint32_t)s));
             imask |= 1u << s;
             const int wn = child_base + inner_rank++;
             const int o = atomicAdd(&counters[2], 1);
@@ -975,7 +973,7 @@ __global__ void k_collapse(const CollapseItem* __restrict__ in, int nin, Collaps
     w.w[0] = make_uint4(__float_as_uint(p[0]), __float_as_uint(p[1]), __float_as_uint(p[2]),
                         (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) |
                             (imask << 24));
-    w.w[1] = make_uint4((uint32_t)child_base, (uint32_t)tri_base, pack4(meta), pack4(meta + 4));
+    w.w[1] = make_uint4((uint32_t)child_base, (uint32_t)tri_base, lmask, 0u);
     w.w[2] = make_uint4(pack4(qlo[0]), pack4(qlo[0] + 4), pack4(qlo[1]), pack4(qlo[1] + 4));
     w.w[3] = make_uint4(pack4(qlo[2]), pack4(qlo[2] + 4), pack4(qhi[0]), pack4(qhi[0] + 4));
     w.w[4] = make_uint4(pack4(qhi[1]), pack4(qhi[1] + 4), pack4(qhi[2]), pack4(qhi[2] + 4));

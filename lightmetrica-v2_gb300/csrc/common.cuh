@@ -77,13 +77,14 @@ static_assert(sizeof(BNode) == 48, "BNode layout");
 
 // 8-wide compressed node (80 bytes, five 16-byte words).
 //   w0: origin p (3 floats), byte exponents ex, ey, ez, inner mask imask
-//   w1: child_base, tri_base, meta[0..3], meta[4..7]
+//   w1: child_base, tri_base, leaf mask lmask, 0
 //   w2: qlo_x[0..7], qlo_y[0..7]
 //   w3: qlo_z[0..7], qhi_x[0..7]
 //   w4: qhi_y[0..7], qhi_z[0..7]
 // Child box of slot i on axis a: [p_a + qlo_a[i] * 2^e_a, p_a + qhi_a[i] * 2^e_a].
-// meta[i]: 0 = empty slot; inner child = 0b001_11sss (24 + slot);
-// leaf = unary triangle count (001, 011, 111) << 5 | offset from tri_base.
+// Slot i holds an inner child (imask bit i: wide node child_base + number of
+// inner slots below i), one triangle (lmask bit i: triangle tri_base + number
+// of leaf slots below i), or nothing.
 struct __align__(16) WNode {
     uint4 w[5];
 };

@@ -5,6 +5,7 @@
 // accel_qbvh.cpp:398-497) with a batch kernel, one thread per ray:
 //
 //   * node groups (child base index + 8-bit hit mask + the node's inner mask)
+//     and triangle groups (triangle base + hit mask + the node's leaf mask)
 //     live in a short per-thread stack; the next child is the highest set hit
 //     bit, and hit bits of inner children are permuted by the ray octant so
 //     that this visits children roughly front to back (the build stores
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(cons
         if (!__any_sync(FULL, active)) break;
 
         // 2. node step
-        if (active && tg.y == 0u) {
+        if (active && (tg.y & 0xffu) == 0u) {
             if (ng.y & 0xff000000u) {
                 const uint32_t bit = 31u - __clz(ng.y & 0xff000000u);
                 ng.y &= ~(1u << bit);
@@ -146,11 +147,11 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(cons
                         if (sp < kStack) stack[sp++] = ng;
                         else atomicOr(status, kStatusStackOverflow);
                     }
-                    uint32_t child_base, tri_base, imask;
-                    const uint32_t hm = intersect_node(lnodes, ni, R, best_t, child_base, tri_base, imask);
+                    uint32_t child_base, tri_base, imask, lmask;
+                    const uint32_t h8 = intersect_node(lnodes, ni, R, best_t, child_base, tri_base, imask, lmask);
                     if (STATS) node_fetch++;
-                    ng = make_uint2(child_base, (hm & 0xff000000u) | imask);
-                    tg = make_uint2(tri_base, hm & 0x00ffffffu);
+                    ng = make_uint2(child_base, (permute_octant(h8 & imask, R.oct_inv) << 24) | imask);
+                    tg = make_uint2(tri_base, (h8 & lmask) | (lmask << 8));
                 }
             } else if (sp > 0) {
                 const uint2 g = stack[--sp];
@@ -170,7 +171,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(cons
 
         // 3. triangle steps
         while (true) {
-            const bool has = active && tg.y != 0u;
+            const bool has = active && (tg.y & 0xffu) != 0u;
             const unsigned m = __ballot_sync(FULL, has);
             if (m == 0u) break;
             const bool few = __popc(m) < postpone;
@@ -178,9 +179,10 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(cons
                 stack[sp++] = tg;
                 tg.y = 0u;
             }
-            if (active && tg.y != 0u) {
-                const uint32_t k = __ffs(tg.y) - 1u;
+            if (active && (tg.y & 0xffu) != 0u) {
+                const uint32_t slot = __ffs(tg.y) - 1u;
                 tg.y &= tg.y - 1u;
+                const uint32_t k = __popc((tg.y >> 8) & ((1u << slot) - 1u));
                 if (tg.x + k >= lnt) {
                     atomicOr(status, kStatusBadTree);
                     tg.y = 0u;

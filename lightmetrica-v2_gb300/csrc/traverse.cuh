@@ -85,13 +85,13 @@ __device__ __forceinline__ unsigned long long slab2(uint32_t w, int k, unsigned 
     return fma2(add2(pk2(qbyte23(w, k), qbyte23(w, k + 1)), m2), a2, b2);
 }
 
-// Tests the eight child boxes of one node; returns the hit mask
-// (bits 24..31 inner children in permuted slot order, bits 0..23 triangles).
+// Tests the eight child boxes of one node; returns the 8-bit mask of the
+// child slots the ray meets, and the node's inner-slot and leaf-slot masks.
 // Children are tested in pairs with packed FP32 arithmetic; every distance is
 // the same correctly rounded q * a + b as a scalar FMA would give.
 __device__ __forceinline__ uint32_t intersect_node(const WNode* __restrict__ nodes, uint32_t ni, const RayState& R,
                                                    float tmax, uint32_t& child_base, uint32_t& tri_base,
-                                                   uint32_t& imask)
+                                                   uint32_t& imask, uint32_t& lmask)
 {
     const uint4* np = reinterpret_cast<const uint4*>(nodes + ni);
     const uint4 w0 = __ldg(np + 0);
@@ -106,15 +106,15 @@ __device__ __forceinline__ uint32_t intersect_node(const WNode* __restrict__ nod
     imask = w0.w >> 24;
     child_base = w1.x;
     tri_base = w1.y;
+    lmask = w1.z;
     const float ax = sx * R.idx, ay = sy * R.idy, az = sz * R.idz;
     const float bx = (px - R.ox) * R.idx, by = (py - R.oy) * R.idy, bz = (pz - R.oz) * R.idz;
     const unsigned long long ax2 = pk2(ax, ax), ay2 = pk2(ay, ay), az2 = pk2(az, az);
     const unsigned long long bx2 = pk2(bx, bx), by2 = pk2(by, by), bz2 = pk2(bz, bz);
     const bool nx = R.idx < 0.0f, ny = R.idy < 0.0f, nz = R.idz < 0.0f;
-    uint32_t hm = 0;
+    uint32_t h8 = 0;
 #pragma unroll
     for (int half = 0; half < 2; half++) {
-        const uint32_t meta4 = half ? w1.w : w1.z;
         const uint32_t lox = half ? w2.y : w2.x, loy = half ? w2.w : w2.z, loz = half ? w3.y : w3.x;
         const uint32_t hix = half ? w3.w : w3.z, hiy = half ? w4.y : w4.x, hiz = half ? w4.w : w4.z;
         const uint32_t nearx = nx ? hix : lox, farx = nx ? lox : hix;
@@ -136,16 +136,21 @@ __device__ __forceinline__ uint32_t intersect_node(const WNode* __restrict__ nod
                 // margin 2^-19 relative: above the rounding of both distances
                 // (a few ulps of t each, Ize 2013), so a box the ray meets is
                 // never rejected although the quantised boxes are tight
-                if (tn <= tf * (1.0f + 0x1p-19f)) {
-                    const uint32_t meta = (meta4 >> (8 * (k + j))) & 0xffu;
-                    uint32_t bit = meta & 0x1fu;
-                    if (bit >= 24u) bit ^= R.oct_inv;
-                    hm |= (meta >> 5) << bit;
-                }
+                if (tn <= tf * (1.0f + 0x1p-19f)) h8 |= 1u << (4 * half + k + j);
             }
         }
     }
-    return hm;
+    return h8;
+}
+
+// Moves bit s of an 8-bit mask to bit s ^ o (o < 8): inner children in the
+// order a ray of octant 7 - o meets them.
+__device__ __forceinline__ uint32_t permute_octant(uint32_t h, uint32_t o)
+{
+    if (o & 1u) h = ((h & 0x55u) << 1) | ((h >> 1) & 0x55u);
+    if (o & 2u) h = ((h & 0x33u) << 2) | ((h >> 2) & 0x33u);
+    if (o & 4u) h = ((h & 0x0fu) << 4) | ((h >> 4) & 0x0fu);
+    return h;
 }
 
 // Watertight ray/triangle test.  Returns true and (t, b1, b2) when the ray
