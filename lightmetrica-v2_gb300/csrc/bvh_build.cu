@@ -13,7 +13,8 @@
 //      chosen by one warp per task, and the range is partitioned stably
 //      (chunk counts -> per-task scan -> scatter);
 //   2. small phase: one block per remaining task builds its whole subtree in
-//      shared memory (32 bins per axis, stable block partition);
+//      shared memory (32 bins per axis, stable block partition); subtrees of
+//      at most kTinyTask triangles are finished by one thread;
 //   3. collapse: a top-down pass turns the binary tree into 8-wide nodes,
 //      expanding the child of largest surface area until 8 children exist,
 //      ordering children by ray octant, quantising child boxes outward to
@@ -46,6 +47,10 @@ constexpr int kSmallTask = 1024;
 constexpr int kSmallThreads = 128;
 constexpr int kMaxLeaf = 1;  // the node format (one triangle per leaf slot) relies on it
 constexpr int kSmallStack = 48;
+// Subtrees of at most this many triangles are finished by one thread with an
+// exact SAH sweep over the sorted centroids of each axis, without the
+// block-wide binning and barriers of larger nodes.
+constexpr int kTinyTask = 16;
 
 struct Task {
     int32_t node;
@@ -640,6 +645,81 @@ __global__ void __launch_bounds__(kSmallThreads) k_build_small(const Task* __res
         if (cur.n < 0) break;
         if (cur.n <= kMaxLeaf) {
             // leaf: node already carries begin/count/bounds; left stays -1
+            __syncthreads();
+            continue;
+        }
+        if (cur.n <= kTinyTask) {
+            if (threadIdx.x == 0) {
+                // serial exact-SAH splits
+                int4 st[kTinyTask];  // node, first, count, depth
+                int sp = 0;
+                st[sp++] = make_int4(cur.node, cur.b, cur.n, cur.depth);
+                while (sp > 0 && !s_abort) {
+                    const int4 t = st[--sp];
+                    // exact SAH over the sorted centroids of each axis
+                    int16_t ord[3][kTinyTask];
+                    float best = FLT_MAX;
+                    int axis = 0, m = t.z / 2;
+                    for (int a = 0; a < 3; a++) {
+                        for (int i = 0; i < t.z; i++) {  // stable insertion sort by centroid
+                            const int16_t v = s_idx[t.y + i];
+                            const float cv = s_lo[a][v] + s_hi[a][v];
+                            int j = i - 1;
+                            while (j >= 0 && s_lo[a][ord[a][j]] + s_hi[a][ord[a][j]] > cv) {
+                                ord[a][j + 1] = ord[a][j];
+                                j--;
+                            }
+                            ord[a][j + 1] = v;
+                        }
+                        float rarea[kTinyTask];
+                        float rlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+                        for (int i = t.z - 1; i > 0; i--) {
+                            for (int k = 0; k < 3; k++) {
+                                rlo[k] = fminf(rlo[k], s_lo[k][ord[a][i]]);
+                                rhi[k] = fmaxf(rhi[k], s_hi[k][ord[a][i]]);
+                            }
+                            rarea[i] = area_of(rlo, rhi);
+                        }
+                        float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+                        for (int i = 1; i < t.z; i++) {  // split before position i
+                            for (int k = 0; k < 3; k++) {
+                                llo[k] = fminf(llo[k], s_lo[k][ord[a][i - 1]]);
+                                lhi[k] = fmaxf(lhi[k], s_hi[k][ord[a][i - 1]]);
+                            }
+                            const float c = area_of(llo, lhi) * (float)i + rarea[i] * (float)(t.z - i);
+                            if (c < best) { best = c; axis = a; m = i; }
+                        }
+                    }
+                    for (int i = 0; i < t.z; i++) s_idx[t.y + i] = ord[axis][i];
+                    const int child = atomicAdd(&counters[0], 2);
+                    if (child + 2 > max_nodes) {
+                        atomicOr(status, kStatusBuildOverflow);
+                        s_abort = 1;
+                        break;
+                    }
+                    nodes[t.x].left = child;
+                    atomicMax(&counters[3], t.w + 1);
+                    for (int sd = 0; sd < 2; sd++) {
+                        const int first = sd ? t.y + m : t.y, n = sd ? t.z - m : m;
+                        BNode bn;
+                        for (int k = 0; k < 3; k++) { bn.lo[k] = FLT_MAX; bn.hi[k] = -FLT_MAX; }
+                        for (int i = 0; i < n; i++) {
+                            const int li = s_idx[first + i];
+                            for (int k = 0; k < 3; k++) {
+                                bn.lo[k] = fminf(bn.lo[k], s_lo[k][li]);
+                                bn.hi[k] = fmaxf(bn.hi[k], s_hi[k][li]);
+                            }
+                        }
+                        bn.left = -1;
+                        bn.begin = task.begin + first;
+                        bn.count = n;
+                        bn.depth = t.w + 1;
+                        bn.pad[0] = bn.pad[1] = 0;
+                        nodes[child + sd] = bn;
+                        if (n > kMaxLeaf) st[sp++] = make_int4(child + sd, first, n, t.w + 1);
+                    }
+                }
+            }
             __syncthreads();
             continue;
         }
