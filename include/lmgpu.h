@@ -368,6 +368,37 @@ int lmgpu_render_pt_guided_device(lmgpu_scene* scene, lmgpu_guide* guide, const 
                                   const lmgpu_guiding_params* guiding, float* d_image, float* d_variance,
                                   void* stream, float* last_loss);
 
+/* ---- Surface geometry at hits ---------------------------------------------- */
+
+/* Shading attributes for lmgpu_surface, per triangle in global order (the
+ * order lmgpu_accel_build received): normals [ntri*9] = the three vertex
+ * normals through the primitive's normal transform (intersectionutils.h:91-93),
+ * or NULL; texcoords [ntri*6] = the three vertices' (u, v), or NULL; flags
+ * [ntri] (bit 0 the triangle has normals, bit 1 texcoords) or NULL for
+ * every triangle having what is given.  Host memory; call after a build
+ * (a rebuild drops them).  Without attributes every triangle uses its
+ * geometric normal and uv (0, 0), as for a mesh without normals or
+ * texcoords.  Stands in for the per-hit mesh lookups of
+ * IntersectionUtils::CreateTriangleIntersection (intersectionutils.h:59-135). */
+int lmgpu_accel_set_attributes(lmgpu_accel* accel, const float* normals, const float* texcoords,
+                               const uint8_t* flags, uint64_t ntri);
+
+/* Planes of lmgpu_surface's output. */
+#define LMGPU_SURFACE_PLANES 23
+
+/* Surface geometry of n hits (lmgpu_hit from lmgpu_trace for the same rays):
+ * what IntersectionUtils::CreateTriangleIntersection (intersectionutils.h:59)
+ * puts in Intersection::geom for each, as LMGPU_SURFACE_PLANES planes of n
+ * floats (plane k of hit i at surface[k * n + i]): p (planes 0-2, o + d t),
+ * gn (3-5), sn (6-8), dpdu (9-11), dpdv (12-14), dndu (15-17), dndv (18-20),
+ * uv (21-22).  ToWorld is the matrix of columns (dpdu, dpdv, sn) and ToLocal
+ * its transpose.  Misses (prim < 0) give zeros.  Host buffers. */
+int lmgpu_surface(const lmgpu_accel* accel, const float* rays, const lmgpu_hit* hits, uint64_t n, float* surface);
+
+/* As lmgpu_surface on device buffers, asynchronous on `stream`. */
+int lmgpu_surface_device(const lmgpu_accel* accel, const float* d_rays, const lmgpu_hit* d_hits, uint64_t n,
+                         float* d_surface, void* stream);
+
 /* Largest scene lmgpu_trace_static_scene accepts. */
 #define LMGPU_STATIC_MAX_TRIANGLES 16384
 

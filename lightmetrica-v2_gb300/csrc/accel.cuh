@@ -29,6 +29,16 @@ struct lmgpu_accel {
     uint64_t cap_wide = 0;
     uint64_t cap_tris = 0;
 
+    // Global triangle id -> its WTri record (surface geometry at hits).
+    int32_t* tri_slot = nullptr;
+    // Shading attributes of lmgpu_surface, global triangle order: vertex
+    // normals [ntri*9], texcoords [ntri*6], flags [ntri] (bit 0 normals,
+    // bit 1 texcoords); attr_ntri = 0 when none are set.
+    float* attr_normals = nullptr;
+    float* attr_texcoords = nullptr;
+    uint8_t* attr_flags = nullptr;
+    uint64_t attr_ntri = 0;
+
     // Device status word raised by traversal kernels (stack overflow).
     uint32_t* status = nullptr;
     // Traversal counters of the instrumented kernel (4 x u64).

@@ -908,7 +908,7 @@ __global__ void k_collapse(const CollapseItem* __restrict__ in, int nin, Collaps
                            const BNode* __restrict__ bnodes, const int32_t* __restrict__ idx,
                            const float* __restrict__ tris, WNode* __restrict__ wnodes, WTri* __restrict__ wtris,
                            int32_t* __restrict__ counters /* [0] wide count, [1] tri count, [2] out count */,
-                           int max_wide, uint32_t* __restrict__ status)
+                           int max_wide, uint32_t* __restrict__ status, int32_t* __restrict__ tri_slot)
 {
     const int it = blockIdx.x * blockDim.x + threadIdx.x;
     if (it >= nin) return;
@@ -1036,6 +1036,7 @@ __global__ void k_collapse(const CollapseItem* __restrict__ in, int nin, Collaps
                 w.v1 = make_float4(v[3], v[4], v[5], 0.0f);
                 w.v2 = make_float4(v[6], v[7], v[8], 0.0f);
                 wtris[tri_base + tri_off + j] = w;
+                if (tri_slot) tri_slot[g] = tri_base + tri_off + j;
             }
             tri_off += cnt;
         } else {
@@ -1094,6 +1095,7 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
     a->built = false;
     a->ntri = ntri;
     a->num_wide = 0;
+    a->attr_ntri = 0;  // shading attributes belong to the previous triangles
     a->info = lmgpu_accel_info{};
     a->info.num_triangles = ntri;
     if (ntri == 0) {
@@ -1204,9 +1206,11 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
     }
     if (ntri > a->cap_tris) {
         if (a->tris) cudaFree(a->tris);
+        if (a->tri_slot) cudaFree(a->tri_slot);
         a->tris = nullptr;
+        a->tri_slot = nullptr;
         a->cap_tris = 0;
-        if ((rc = dalloc(&a->tris, ntri))) return rc;
+        if ((rc = dalloc(&a->tris, ntri)) || (rc = dalloc(&a->tri_slot, ntri))) return rc;
         a->cap_tris = ntri;
     }
     CollapseItem *qa, *qb;
@@ -1220,7 +1224,7 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
     while (nin > 0) {
         LMGPU_CUDA_TRY(cudaMemsetAsync(ccount + 2, 0, sizeof(int32_t), stream));
         k_collapse<<<(nin + 127) / 128, 128, 0, stream>>>(qa, nin, qb, bnodes, idx, d_tris, a->nodes, a->tris, ccount,
-                                                         max_wide, a->status);
+                                                         max_wide, a->status, a->tri_slot);
         LMGPU_CUDA_TRY(cudaGetLastError());
         int32_t next = 0;
         LMGPU_CUDA_TRY(cudaMemcpyAsync(&next, ccount + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
@@ -1449,7 +1453,7 @@ int build_static(unsigned char* base, const float* d_tris, int n, cudaStream_t s
     while (nin > 0) {
         LMGPU_CUDA_TRY(cudaMemsetAsync(ccount + 2, 0, sizeof(int32_t), stream));
         k_collapse<<<(nin + 127) / 128, 128, 0, stream>>>(qa, nin, qb, bnodes, idx, d_tris, wnodes, wtris, ccount, kSWide,
-                                                         status);
+                                                         status, nullptr);
         LMGPU_CUDA_TRY(cudaGetLastError());
         int32_t next = 0;
         LMGPU_CUDA_TRY(cudaMemcpyAsync(&next, ccount + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));

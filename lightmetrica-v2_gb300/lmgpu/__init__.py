@@ -84,6 +84,9 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_accel_check.argtypes = [vp, vp]
     L.lmgpu_trace_static_scene.argtypes = [vp, u64, vp, vp, u64, i32, vp]
     L.lmgpu_accel_set_tuning.argtypes = [vp, i32, i32]
+    L.lmgpu_accel_set_attributes.argtypes = [vp, vp, vp, vp, u64]
+    L.lmgpu_surface.argtypes = [vp, vp, vp, u64, vp]
+    L.lmgpu_surface_device.argtypes = [vp, vp, vp, u64, vp, vp]
     L.lmgpu_scene_create.argtypes = [vp, vp, u64, vp, ctypes.c_uint32, vp, ctypes.POINTER(vp)]
     L.lmgpu_scene_destroy.argtypes = [vp]
     L.lmgpu_scene_destroy.restype = None
@@ -205,6 +208,32 @@ class Accel:
 
     def set_tuning(self, refill: int, postpone: int) -> None:
         _check(lib().lmgpu_accel_set_tuning(self._h, refill, postpone))
+
+    def set_attributes(self, normals=None, texcoords=None, flags=None, ntri: int | None = None) -> None:
+        """Per-triangle vertex normals (ntri, 9), texcoords (ntri, 6) and
+        flags (ntri,) of lmgpu_surface (global triangle order)."""
+        n = np.ascontiguousarray(normals, np.float32).reshape(-1, 9) if normals is not None else None
+        t = np.ascontiguousarray(texcoords, np.float32).reshape(-1, 6) if texcoords is not None else None
+        f = np.ascontiguousarray(flags, np.uint8) if flags is not None else None
+        if ntri is None:
+            ntri = next(a.shape[0] for a in (n, t, f) if a is not None)
+        ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+        _check(lib().lmgpu_accel_set_attributes(self._h, ptr(n), ptr(t), ptr(f), ntri))
+
+    def surface(self, rays: np.ndarray, hits: np.ndarray) -> np.ndarray:
+        """Surface geometry (n, 23) of hits: p, gn, sn, dpdu, dpdv, dndu,
+        dndv, uv (IntersectionUtils::CreateTriangleIntersection)."""
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        h = np.ascontiguousarray(hits)
+        if h.dtype != HIT_DTYPE or h.shape != (r.shape[0],):
+            raise ValueError("hits: one HIT_DTYPE record per ray")
+        n = r.shape[0]
+        out = np.empty((23, n), np.float32)
+        _check(lib().lmgpu_surface(self._h, r.ctypes.data, h.ctypes.data, n, out.ctypes.data))
+        return out.T.copy()
+
+    def surface_device(self, d_rays_ptr: int, d_hits_ptr: int, n: int, d_out_ptr: int, stream: int = 0) -> None:
+        _check(lib().lmgpu_surface_device(self._h, d_rays_ptr, d_hits_ptr, n, d_out_ptr, stream))
 
     def check(self, stream: int = 0) -> None:
         _check(lib().lmgpu_accel_check(self._h, stream))

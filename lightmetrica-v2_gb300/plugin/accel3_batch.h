@@ -6,11 +6,13 @@
 
     Slot numbering follows the reference's cumulative interface IDs
     (Accel: Initialize = 0, Build = 1; Accel3: Intersect = 2), so
-    IntersectBatch occupies slot 3.
+    IntersectBatch occupies slot 3 and IntersectBatchGeometry slot 4.
 */
 #pragma once
 
 #include <lightmetrica/accel3.h>
+#include <lightmetrica/intersection.h>
+#include <lightmetrica/ray.h>
 
 LM_NAMESPACE_BEGIN
 
@@ -18,7 +20,7 @@ class Accel3Batch : public Accel3
 {
 public:
 
-    LM_INTERFACE_CLASS(Accel3Batch, Accel3, 1);
+    LM_INTERFACE_CLASS(Accel3Batch, Accel3, 2);
 
 public:
 
@@ -35,6 +37,17 @@ public:
         triangle prim (the order of accel_naive.cpp:62-87).
     */
     LM_INTERFACE_F(0, IntersectBatch, bool(const float* rays, void* hits, long long n, bool anyHit));
+
+    /*!
+        Closest hits of n rays with their full Intersection records: for
+        every ray, what Accel3::Intersect(scene, rays[i], isects[i], minT,
+        maxT) gives (hit[i] its return value), with the surface geometry of
+        IntersectionUtils::CreateTriangleIntersection computed for the
+        whole batch on the GPU.  The batched form of Scene3::Intersect for
+        CPU renderers.
+    */
+    LM_INTERFACE_F(1, IntersectBatchGeometry, bool(const Scene* scene, const Ray* rays, Intersection* isects,
+                                                   bool* hit, long long n, Float minT, Float maxT));
 
 };
 

@@ -15,7 +15,8 @@
       Accel::Initialize      include/lightmetrica/accel.h:67
       Accel::Build           include/lightmetrica/accel.h:79
       Accel3::Intersect      include/lightmetrica/accel3.h:68
-      Accel3Batch::IntersectBatch  accel3_batch.h (this plugin's batch extension)
+      Accel3Batch::IntersectBatch, IntersectBatchGeometry
+                             accel3_batch.h (this plugin's batch extension)
     Geometry is read the way accel_naive.cpp:59-90 reads it (primitive
     transform applied to every vertex, global triangle id = faces of
     primitive 0, then primitive 1, ...), and hits are turned into an
@@ -95,6 +96,41 @@ public:
             LM_LOG_ERROR(std::string("accel::cuda: ") + lmgpu_last_error());
             return false;
         }
+        // shading attributes for the batched surface geometry, per triangle
+        // as CreateTriangleIntersection reads them (intersectionutils.h:84-115)
+        std::vector<float> normals(9 * primOf_.size(), 0.0f), texcoords(6 * primOf_.size(), 0.0f);
+        std::vector<uint8_t> flags(primOf_.size(), 0);
+        for (size_t t = 0; t < primOf_.size(); t++)
+        {
+            const auto* prim = scene->PrimitiveAt(primOf_[t]);
+            const auto* mesh = prim->mesh;
+            const auto* fs = mesh->Faces();
+            const auto* ns = mesh->Normals();
+            const auto* tc = mesh->Texcoords();
+            for (int k = 0; k < 3; k++)
+            {
+                const unsigned int v = fs[3 * faceOf_[t] + k];
+                if (ns)
+                {
+                    const Vec3 n = prim->normalTransform * Vec3(ns[3 * v], ns[3 * v + 1], ns[3 * v + 2]);
+                    normals[9 * t + 3 * k] = (float)n.x;
+                    normals[9 * t + 3 * k + 1] = (float)n.y;
+                    normals[9 * t + 3 * k + 2] = (float)n.z;
+                }
+                if (tc)
+                {
+                    texcoords[6 * t + 2 * k] = (float)tc[2 * v];
+                    texcoords[6 * t + 2 * k + 1] = (float)tc[2 * v + 1];
+                }
+            }
+            flags[t] = (uint8_t)((ns ? 1 : 0) | (tc ? 2 : 0));
+        }
+        if (lmgpu_accel_set_attributes(accel_, normals.data(), texcoords.data(), flags.data(),
+                                       (uint64_t)primOf_.size()) != LMGPU_OK)
+        {
+            LM_LOG_ERROR(std::string("accel::cuda: ") + lmgpu_last_error());
+            return false;
+        }
         return true;
     };
 
@@ -123,6 +159,54 @@ public:
         {
             LM_LOG_ERROR(std::string("accel::cuda: ") + lmgpu_last_error());
             return false;
+        }
+        return true;
+    };
+
+    // Accel3Batch::IntersectBatchGeometry (slot 4): closest hits and their
+    // surface geometry for a whole batch, composed into Intersection records.
+    LM_IMPL_F(IntersectBatchGeometry) = [this](const Scene* scene_, const Ray* rays, Intersection* isects, bool* hit,
+                                               long long n, Float minT, Float maxT) -> bool
+    {
+        if (n <= 0) return true;
+        const auto* scene = static_cast<const Scene3*>(scene_);
+        std::vector<float> r(8 * (size_t)n);
+        for (long long i = 0; i < n; i++)
+        {
+            const float v[8] = { (float)rays[i].o.x, (float)rays[i].o.y, (float)rays[i].o.z, (float)minT,
+                                 (float)rays[i].d.x, (float)rays[i].d.y, (float)rays[i].d.z, (float)maxT };
+            std::copy(v, v + 8, &r[8 * (size_t)i]);
+        }
+        std::vector<lmgpu_hit> h((size_t)n);
+        std::vector<float> g((size_t)LMGPU_SURFACE_PLANES * (size_t)n);
+        if (lmgpu_trace(accel_, r.data(), h.data(), (uint64_t)n, 0) != LMGPU_OK ||
+            lmgpu_surface(accel_, r.data(), h.data(), (uint64_t)n, g.data()) != LMGPU_OK)
+        {
+            LM_LOG_ERROR(std::string("accel::cuda: ") + lmgpu_last_error());
+            return false;
+        }
+        const size_t N = (size_t)n;
+        auto plane3 = [&](int k, size_t i) { return Vec3((Float)g[k * N + i], (Float)g[(k + 1) * N + i], (Float)g[(k + 2) * N + i]); };
+        for (size_t i = 0; i < N; i++)
+        {
+            hit[i] = h[i].prim >= 0;
+            if (!hit[i]) continue;
+            Intersection& isect = isects[i];
+            isect = Intersection();
+            isect.primitive = scene->PrimitiveAt(primOf_[h[i].prim]);
+            SurfaceGeometry& geom = isect.geom;
+            geom.faceindex = faceOf_[h[i].prim];
+            geom.degenerated = false;
+            geom.p = plane3(0, i);
+            geom.gn = plane3(3, i);
+            geom.sn = plane3(6, i);
+            geom.dpdu = plane3(9, i);
+            geom.dpdv = plane3(12, i);
+            geom.dndu = plane3(15, i);
+            geom.dndv = plane3(18, i);
+            geom.uv = Vec2((Float)g[21 * N + i], (Float)g[22 * N + i]);
+            geom.ToWorld = Mat3(geom.dpdu, geom.dpdv, geom.sn);
+            geom.ToLocal = Math::Transpose(geom.ToWorld);
         }
         return true;
     };

@@ -7,6 +7,8 @@
 #                 sensor::pinhole, Random (dSFMT) and accel::qbvh (single)
 #   ref_render64  the same in double precision (LM_USE_DOUBLE_PRECISION,
 #                 cmake/LMBuildOptions.cmake:32-43) with accel::bvh_sahbin
+#   ref_isect / ref_isect64  IntersectionUtils::CreateTriangleIntersection
+#                 (single / double precision)
 # Test infrastructure only: nothing in the product links or runs them.
 #
 # The reference library cannot be built as shipped (boost, TBB, FreeImage,
@@ -64,13 +66,16 @@ compile_set() {
 
 S="-DLM_EXPORTS -DLM_USE_SINGLE_PRECISION -DNDEBUG"
 D="-DLM_EXPORTS -DLM_USE_DOUBLE_PRECISION -DNDEBUG"
-compile_set f "$S" "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}" "$HERE/refharness/ref_accel_cli.cpp"
-compile_set d "$D" "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}"
+ISECT="$HERE/refharness/ref_isect_cli.cpp"
+compile_set f "$S" "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}" "$HERE/refharness/ref_accel_cli.cpp" "$ISECT"
+compile_set d "$D" "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}" "$ISECT"
 $CC -O3 -msse2 -DDSFMT_MEXP=19937 -DNDEBUG -w -c "$REF/external-src/dSFMT-src-2.2.3/dSFMT.c" -o "$OUT/dsfmt.o"
 
 obj() { local tag="$1"; shift; for s in "$@"; do echo "$OUT/${tag}_$(basename "$s" .cpp).o"; done; }
 $CXX -O3 -o "$OUT/ref_accel" $(obj f "${ACCEL_SRCS[@]}" "$HERE/refharness/ref_accel_cli.cpp") -lpthread
 $CXX -O3 -o "$OUT/ref_render" $(obj f "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}") "$OUT/dsfmt.o" -lpthread
 $CXX -O3 -o "$OUT/ref_render64" $(obj d "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}") "$OUT/dsfmt.o" -lpthread
+$CXX -O3 -o "$OUT/ref_isect" $(obj f "$HERE/refharness/ref_runtime.cpp" "$ISECT") -lpthread
+$CXX -O3 -o "$OUT/ref_isect64" $(obj d "$HERE/refharness/ref_runtime.cpp" "$ISECT") -lpthread
 rm -f "$OUT"/*.o
-echo "built $OUT/ref_accel $OUT/ref_render $OUT/ref_render64"
+echo "built $OUT/ref_accel $OUT/ref_render $OUT/ref_render64 $OUT/ref_isect $OUT/ref_isect64"

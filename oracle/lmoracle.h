@@ -124,6 +124,16 @@ uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t n
                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
                             uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir);
 
+/* Surface geometry of n hits (IntersectionUtils::CreateTriangleIntersection,
+ * intersectionutils.h:59-135) in double precision.  tris / normals: [ntri*9]
+ * per triangle in global order, already through the primitive's transform /
+ * normal transform (normals may be NULL); texcoords [ntri*6] or NULL; flags
+ * [ntri] (bit 0 normals, bit 1 texcoords) or NULL; rays [n*8]; hits [n*4] =
+ * (t, prim, b1, b2), prim < 0 a miss.  out [n*23] per hit: p, gn, sn, dpdu,
+ * dpdv, dndu, dndv (3 each), u, v; zeros for misses. */
+void lmo_surface(const double* tris, const double* normals, const double* texcoords, const uint8_t* flags,
+                 const double* rays, const double* hits, size_t n, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -61,6 +61,8 @@ def lib() -> ctypes.CDLL:
         L.lmo_render_ptmis.restype = ctypes.c_uint64
         L.lmo_render_ptdirect.argtypes = L.lmo_render_bdpt.argtypes
         L.lmo_render_ptdirect.restype = ctypes.c_uint64
+        L.lmo_surface.argtypes = [vp, vp, vp, vp, vp, vp, sz, vp]
+        L.lmo_surface.restype = None
         _lib = L
     return _lib
 
@@ -310,3 +312,74 @@ def render_ptmis(scene: dict, num_samples: int, max_num_vertices: int, seed: int
        s.ctypes.data, q.ctypes.data)
     img = s * (W * H / num_samples)
     return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}
+
+
+SURFACE_FIELDS = ("p", "gn", "sn", "dpdu", "dpdv", "dndu", "dndv", "uv")
+
+
+def surface(tris, normals, texcoords, flags, rays, hits) -> np.ndarray:
+    """(n, 23) surface geometry of hits (t, prim, b1, b2) in FP64:
+    p, gn, sn, dpdu, dpdv, dndu, dndv, uv (see lmo_surface)."""
+    def d(a, w):
+        return None if a is None else np.ascontiguousarray(np.asarray(a, np.float64).reshape(-1, w))
+
+    t, r = d(tris, 9), d(rays, 8)
+    nrm, tc = d(normals, 9), d(texcoords, 6)
+    h = d(hits, 4)
+    fl = None if flags is None else np.ascontiguousarray(np.asarray(flags, np.uint8))
+    out = np.zeros((h.shape[0], 23), np.float64)
+    ptr = lambda a: None if a is None else a.ctypes.data
+    lib().lmo_surface(ptr(t), ptr(nrm), ptr(tc), ptr(fl), ptr(r), ptr(h), h.shape[0], out.ctypes.data)
+    return out
+
+
+def run_ref_isect(prims: list[dict], queries: np.ndarray, double: bool = True) -> dict:
+    """Runs the reference's CreateTriangleIntersection (oracle/_ref/ref_isect,
+    ref_isect64 for double) on primitives {"transform": (4, 4) row-major,
+    "positions": (nv, 3), "faces": (nf, 3), "normals": (nv, 3) or None,
+    "texcoords": (nv, 2) or None} and queries (n, 11) = prim, face, o[3],
+    d[3], t, b[2].  Returns the per-triangle arrays in global order (tris,
+    normals, texcoords, flags) and the per-query geometry (n, 23) and face
+    indices."""
+    import struct
+    import subprocess
+    import tempfile
+
+    exe = os.path.join(os.path.dirname(LIB_PATH), "_ref", "ref_isect64" if double else "ref_isect")
+    if not os.path.exists(exe):
+        raise FileNotFoundError(exe)
+    with tempfile.TemporaryDirectory() as td:
+        pin, pout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        with open(pin, "wb") as f:
+            f.write(struct.pack("<I", len(prims)))
+            for p in prims:
+                m = np.asarray(p["transform"], np.float64).reshape(4, 4)
+                f.write(m.T.astype("<f8").tobytes())  # column-major m[c][r]
+                pos = np.asarray(p["positions"], np.float64).reshape(-1, 3)
+                faces = np.asarray(p["faces"], np.uint32).reshape(-1, 3)
+                nrm, tc = p.get("normals"), p.get("texcoords")
+                flags = (1 if nrm is not None else 0) | (2 if tc is not None else 0)
+                f.write(struct.pack("<III", pos.shape[0], faces.shape[0], flags))
+                f.write(pos.astype("<f8").tobytes())
+                if nrm is not None:
+                    f.write(np.asarray(nrm, np.float64).reshape(-1, 3).astype("<f8").tobytes())
+                if tc is not None:
+                    f.write(np.asarray(tc, np.float64).reshape(-1, 2).astype("<f8").tobytes())
+                f.write(faces.astype("<u4").tobytes())
+            q = np.asarray(queries, np.float64).reshape(-1, 11)
+            f.write(struct.pack("<I", q.shape[0]))
+            for row in q:
+                f.write(struct.pack("<ii", int(row[0]), int(row[1])))
+                f.write(row[2:].astype("<f8").tobytes())
+        subprocess.run([exe, pin, pout], check=True)
+        b = open(pout, "rb").read()
+    ntri = struct.unpack_from("<I", b, 0)[0]
+    rec = np.dtype([("v", "<f8", 24), ("flags", "<u4")])
+    tri = np.frombuffer(b, rec, ntri, 4)
+    off = 4 + ntri * rec.itemsize
+    nq = struct.unpack_from("<I", b, off)[0]
+    qrec = np.dtype([("g", "<f8", 23), ("face", "<i4")])
+    qq = np.frombuffer(b, qrec, nq, off + 4)
+    return {"tris": tri["v"][:, 0:9].copy(), "normals": tri["v"][:, 9:18].copy(),
+            "texcoords": tri["v"][:, 18:24].copy(), "flags": tri["flags"].astype(np.uint8),
+            "geom": qq["g"].copy(), "face": qq["face"].copy()}

@@ -35,6 +35,17 @@ Fixtures written:
       The Cornell box rendered by the reference's own renderer::ptdirect
       (light samples only) at 64x64, 16,384 samples per pixel,
       max_num_vertices 9, single and double precision.
+  surface.npz
+      Surface geometry at hits from the reference's own
+      IntersectionUtils::CreateTriangleIntersection (intersectionutils.h),
+      compiled in single and double precision (oracle/_ref/ref_isect,
+      ref_isect64): four primitives under non-uniform scale / rotation /
+      translation transforms (a smooth icosphere with normals and texcoords,
+      a quad with texcoords only, a face with all-zero normals, a bare mesh)
+      and seeded queries (face, barycentrics including edges and vertices,
+      ray origin, direction and t).  Per triangle: the vertices, normals and
+      texcoords as the reference transforms them; per query: p, gn, sn,
+      dpdu, dpdv, dndu, dndv, uv.
   soup_small.npz
       A seeded three-primitive scene (random triangle soup, heightfield,
       duplicated triangles for exact-t ties, zero-area triangles) and rays
@@ -212,6 +223,71 @@ def pt_case(sc: dict, spp: int, seed: int, renderer: str = "pt", max_num_vertice
     return out
 
 
+def _rot(axis, ang):
+    a = np.asarray(axis, np.float64) / np.linalg.norm(axis)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + np.sin(ang) * K + (1 - np.cos(ang)) * K @ K
+
+
+def _affine(scale, axis, ang, trans):
+    m = np.eye(4)
+    m[:3, :3] = _rot(axis, ang) @ np.diag(scale)
+    m[:3, 3] = trans
+    return m
+
+
+def surface_case() -> dict:
+    g = np.random.default_rng(20241215)
+    ico = scenes.closed_icosphere(2, 1.0)  # (nf, 9), unshared vertices
+    pos = ico.reshape(-1, 3)
+    faces = np.arange(pos.shape[0], dtype=np.uint32).reshape(-1, 3)
+    nrm = pos / np.linalg.norm(pos, axis=1, keepdims=True)
+    tc = np.stack([0.5 + np.arctan2(nrm[:, 2], nrm[:, 0]) / (2 * np.pi), np.arccos(np.clip(nrm[:, 1], -1, 1)) / np.pi], 1)
+    quad = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], np.float64)
+    prims = [
+        {"transform": _affine((1.0, 2.0, 0.5), (0.3, 1.0, 0.2), 0.7, (0.5, -0.2, 3.0)), "positions": pos,
+         "faces": faces, "normals": nrm, "texcoords": tc},
+        {"transform": _affine((2.0, 0.5, 1.0), (1.0, 0.0, 0.5), -1.1, (-1.0, 0.4, 0.0)), "positions": quad,
+         "faces": np.array([[0, 1, 2], [0, 2, 3]], np.uint32), "normals": None,
+         "texcoords": np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float64)},
+        {"transform": _affine((1.0, 1.0, 1.0), (0.0, 1.0, 0.0), 0.4, (0.0, 0.0, -2.0)),
+         "positions": np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0.5]], np.float64),
+         "faces": np.array([[0, 1, 2], [1, 3, 2]], np.uint32),
+         "normals": np.array([[0, 0, 0], [0, 0, 0], [0, 0, 0], [0, 0.3, 1.0]], np.float64), "texcoords": None},
+        {"transform": _affine((0.7, 1.3, 1.0), (0.2, 0.2, 1.0), 2.0, (1.0, 1.0, 1.0)), "positions": quad + 0.25,
+         "faces": np.array([[0, 1, 2], [0, 2, 3]], np.uint32), "normals": None, "texcoords": None},
+    ]
+    nf = [p["faces"].shape[0] for p in prims]
+    base = np.concatenate([[0], np.cumsum(nf)[:-1]])
+    qs = []
+    for k in range(600):
+        pi = int(g.integers(len(prims))) if k >= 8 else k % 4
+        fi = int(g.integers(nf[pi]))
+        c = g.integers(4)
+        if c == 0:
+            b = g.dirichlet([1, 1, 1])[1:]
+        elif c == 1:
+            b = np.array([0.0, g.uniform()])  # on edge v1 - v3
+        elif c == 2:
+            b = [np.array([0.0, 0.0]), np.array([1.0, 0.0]), np.array([0.0, 1.0])][int(g.integers(3))]
+        else:
+            u = g.uniform()
+            b = np.array([u, 1.0 - u])  # on edge v2 - v3
+        o = g.normal(size=3) * 4.0
+        d = g.normal(size=3)
+        d /= np.linalg.norm(d)
+        t = float(g.uniform(0.1, 8.0))
+        qs.append([pi, fi, *o, *d, t, b[0], b[1]])
+    q = np.array(qs, np.float64)
+    r64 = lo.run_ref_isect(prims, q, double=True)
+    r32 = lo.run_ref_isect(prims, q, double=False)
+    return {"queries": q, "global_id": (base[q[:, 0].astype(int)] + q[:, 1]).astype(np.int32),
+            "tris64": r64["tris"], "normals64": r64["normals"], "texcoords64": r64["texcoords"],
+            "flags": r64["flags"], "geom64": r64["geom"], "face64": r64["face"],
+            "tris32": r32["tris"].astype(np.float32), "normals32": r32["normals"].astype(np.float32),
+            "texcoords32": r32["texcoords"].astype(np.float32), "geom32": r32["geom"]}
+
+
 def main() -> None:
     args = sys.argv[1:]
     only = None
@@ -233,6 +309,8 @@ def main() -> None:
                                 **accel3_case(src, "StubTriangleMesh_Simple2", True, tmp))
         if want("soup_small"):
             np.savez_compressed(os.path.join(HERE, "soup_small.npz"), **soup_case(tmp))
+    if want("surface"):
+        np.savez_compressed(os.path.join(HERE, "surface.npz"), **surface_case())
     if want("cornell_pt"):
         np.savez_compressed(os.path.join(HERE, "cornell_pt.npz"),
                             **pt_case(scenes.cornell_box(64, 64), 16384, 20240601))
