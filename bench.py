@@ -325,6 +325,109 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
+def run_surface(args) -> None:
+    """Surface geometry at hits (lmgpu_surface_device, the batched
+    IntersectionUtils::CreateTriangleIntersection): closest hits of the
+    ray-cast configuration's rays on its scene, every triangle with vertex
+    normals and texcoords.  Metric Mhits/s (rays per second through the
+    kernel, misses included); value = device-resident hits and planes, e2e =
+    the host-pointer lmgpu_surface (rays and hits in, 23 planes out)."""
+    import torch
+
+    import lmgpu
+    from lmgpu import scenes
+
+    tris = scenes.raycast_scene(N_RANDOM, HF_RES)
+    nt = tris.shape[0]
+    g = np.random.default_rng(0x5EED)
+    gn = np.cross(tris[:, 3:6] - tris[:, 0:3], tris[:, 6:9] - tris[:, 0:3])
+    gn /= np.maximum(np.linalg.norm(gn, axis=1, keepdims=True), 1e-30)
+    nrm = (np.repeat(gn, 3, axis=0).reshape(-1, 9) + g.normal(scale=0.1, size=(nt, 9))).astype(np.float32)
+    tc = g.uniform(size=(nt, 6)).astype(np.float32)
+    nr = args.rays
+    rays = scenes.raycast_rays(nr, stream=3)
+    stream = torch.cuda.Stream()
+    s = stream.cuda_stream
+    acc = lmgpu.Accel()
+    acc.build(tris)
+    acc.set_attributes(nrm, tc)
+    with torch.cuda.stream(stream):
+        d_rays = torch.from_numpy(rays).cuda()
+        d_hits = torch.empty((nr, 4), dtype=torch.float32, device="cuda")
+        d_out = torch.empty((23, nr), dtype=torch.float32, device="cuda")
+    acc.trace_device(d_rays.data_ptr(), d_hits.data_ptr(), nr, False, s)
+    acc.check(s)
+    hits = d_hits.cpu().numpy().view(np.int32)[:, 1]
+    n_hit = int((hits >= 0).sum())
+    for _ in range(args.warmup):
+        acc.surface_device(d_rays.data_ptr(), d_hits.data_ptr(), nr, d_out.data_ptr(), s)
+    acc.check(s)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)  # 256 MiB write: L2 holds none of the inputs when the step starts
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        acc.surface_device(d_rays.data_ptr(), d_hits.data_ptr(), nr, d_out.data_ptr(), s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    clk = clocks.stop()
+    acc.check(s)
+    per_s = total_ms / 1e3 / args.steps
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_hits = d_hits.cpu().pin_memory()
+    h_out = torch.empty((23, nr), dtype=torch.float32).pin_memory()
+    lib = lmgpu.lib()
+    e2e_steps = 3
+    lib.lmgpu_surface(acc.handle, h_rays.data_ptr(), h_hits.data_ptr(), nr, h_out.data_ptr())
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        if lib.lmgpu_surface(acc.handle, h_rays.data_ptr(), h_hits.data_ptr(), nr, h_out.data_ptr()) != 0:
+            raise RuntimeError(lib.lmgpu_last_error().decode())
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    # algorithmic bytes: a hit reads its record (16 B), ray (32 B), slot (4 B), triangle (48 B), normals
+    # (36 B), texcoords (24 B) and flags (1 B); a miss its record; every ray writes 23 floats (92 B)
+    hit_b, miss_b = 16 + 32 + 4 + 48 + 36 + 24 + 1 + 92, 16 + 92
+    alg = n_hit * hit_b + (nr - n_hit) * miss_b
+    peak, peak_src = measured_peak()
+    achieved = alg / per_s / 1e9
+    line = {"metric": "Mhits/s (surface geometry at hits)", "value": nr / per_s / 1e6, "unit": "Mhits/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded): the ray-cast scene with random vertex normals and texcoords",
+            "config": {"workload": "surface_geometry_raycast_hits", "triangles": nt, "rays_per_step": nr,
+                       "hit_fraction": n_hit / nr, "l2": "flushed before every timed step (256 MiB write)"},
+            "e2e": {"value": nr / e2e_s / 1e6, "unit": "Mhits/s", "h2d_bytes_per_step": nr * (32 + 16),
+                    "d2h_bytes_per_step": nr * 92, "steps": e2e_steps, "api": "lmgpu_surface (host pointers)"},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_src, "kernel": "k_surface",
+                         "bytes_per_ray": alg / nr,
+                         "note": "algorithmic bytes: hit 253 B (record, ray, slot, triangle, normals, texcoords, "
+                                 "flags, 92 B out), miss 108 B"},
+            "clocks": clk}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import lmoracle
+
+        m = min(nr, 1 << 21)
+        hh = d_hits[:m].cpu().numpy()
+        hin = np.stack([hh[:, 0], hh.view(np.int32)[:, 1].astype(np.float64), hh[:, 2], hh[:, 3]], 1)
+        t0 = time.perf_counter()
+        lmoracle.surface(tris, nrm, tc, None, rays[:m], hin)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": m / dt / 1e6, "unit": "Mhits/s", "cores": 1, "kind": "port",
+                                "sample": f"{m} hits of the step, oracle restatement of CreateTriangleIntersection "
+                                          f"(FP64, 1 thread), {dt:.1f} s"}
+    print(json.dumps(line), flush=True)
+    acc.close()
+
+
 RENDER_WORKLOADS = {
     # renderer::pt on the Cornell-style box: 256 x 256, 64 spp, max_num_vertices 9 (8 segments)
     "pt": {"renderer": "pt", "workload": "pt_cornell_256x256_64spp", "width": 256, "height": 256, "spp": 64,
@@ -653,10 +756,12 @@ def main() -> None:
     ap.add_argument("--anyhit", action="store_true", help="time any-hit queries instead of closest hit")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel of the render workloads (profiling of "
                                                         "smaller cases; default: the workload's own)")
-    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt", "batch", "guiding"], default="raycast",
+    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt", "batch", "guiding", "surface"],
+                    default="raycast",
                     help="raycast: the BVH ray-cast configuration (default); pt: renderer::pt on the Cornell "
                          "box; bdpt: renderer::bdpt on the caustic room; batch: 12 scenes in one wavefront; "
-                         "guiding: learned path guiding vs plain PT at equal time")
+                         "guiding: learned path guiding vs plain PT at equal time; surface: surface geometry "
+                         "at the ray-cast hits")
     ap.add_argument("--mlp-only", action="store_true", help="guiding: time the MLP kernels only")
     ap.add_argument("--no-autotune", action="store_true", help="batch: keep the default tuning (profiling runs)")
     ap.add_argument("--use-ref-binary", action="store_true",
@@ -672,6 +777,8 @@ def main() -> None:
         run_batch(args)
     elif args.workload == "guiding":
         run_guiding(args)
+    elif args.workload == "surface":
+        run_surface(args)
     else:
         run_gpu(args)
 

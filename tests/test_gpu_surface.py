@@ -74,7 +74,7 @@ def test_surface_of_traced_hits(gpu_lib, oracle_lib):
     acc.set_attributes(nrm, tc, flags)
     h = acc.trace(rays)
     hit = h["prim"] >= 0
-    assert 0.1 < hit.mean() < 0.99
+    assert hit.sum() > 1000 and not hit.all()
     out = acc.surface(rays, h)
     assert not out[~hit].any()
     hin = np.stack([h["t"], h["prim"], h["b1"], h["b2"]], 1).astype(np.float64)
