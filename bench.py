@@ -438,11 +438,15 @@ RENDER_WORKLOADS = {
              "spp": 32, "max_num_vertices": 11,
              "data": "synthetic (procedural room, level-5 glass icosphere, sphere light behind a panel)",
              "cpu_spp": 1},
+    # renderer::ltdirect (light tracing, a sensor connection per vertex) on the Cornell-style box:
+    # 256 x 256 x 64 light paths, max_num_vertices 9
+    "ltdirect": {"renderer": "ltdirect", "workload": "ltdirect_cornell_256x256_64spp", "width": 256, "height": 256,
+                 "spp": 64, "max_num_vertices": 9, "data": "synthetic (procedural Cornell box)", "cpu_spp": 8},
 }
 
 
 def run_render(args) -> None:
-    """Rendering configurations (renderer::pt, renderer::bdpt).  Metric
+    """Rendering configurations (renderer::pt, renderer::bdpt, renderer::ltdirect).  Metric
     Msamples/s; value = film left on the device (lmgpu_render_*_device),
     e2e = the host-pointer lmgpu_render_* (film and variance copied back
     every step)."""
@@ -455,11 +459,11 @@ def run_render(args) -> None:
     W, H, spp, max_nv = cfg["width"], cfg["height"], cfg["spp"], cfg["max_num_vertices"]
     if args.spp:
         spp = args.spp
-    scene = scenes.cornell_box(W, H) if cfg["renderer"] == "pt" else scenes.caustic_room(W, H)
+    scene = scenes.caustic_room(W, H) if cfg["renderer"] == "bdpt" else scenes.cornell_box(W, H)
     stream = torch.cuda.Stream()
     sc = lmgpu.Scene(scene)
-    render_dev = sc.render_pt_device if cfg["renderer"] == "pt" else sc.render_bdpt_device
-    render_host = sc.render_pt if cfg["renderer"] == "pt" else sc.render_bdpt
+    render_dev = getattr(sc, f"render_{cfg['renderer']}_device")
+    render_host = getattr(sc, f"render_{cfg['renderer']}")
     di = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
     dv = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
     samples = W * H * spp
@@ -504,7 +508,7 @@ def run_render(args) -> None:
 
         threads = os.cpu_count() or 1
         n_cpu = W * H * cfg["cpu_spp"]
-        fn = lmoracle.render_pt if cfg["renderer"] == "pt" else lmoracle.render_bdpt
+        fn = getattr(lmoracle, f"render_{cfg['renderer']}")
         t0 = time.perf_counter()
         fn(scene, n_cpu, max_nv, 5, threads)
         cpu_s = time.perf_counter() - t0
@@ -756,10 +760,11 @@ def main() -> None:
     ap.add_argument("--anyhit", action="store_true", help="time any-hit queries instead of closest hit")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel of the render workloads (profiling of "
                                                         "smaller cases; default: the workload's own)")
-    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt", "batch", "guiding", "surface"],
+    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt", "ltdirect", "batch", "guiding", "surface"],
                     default="raycast",
                     help="raycast: the BVH ray-cast configuration (default); pt: renderer::pt on the Cornell "
-                         "box; bdpt: renderer::bdpt on the caustic room; batch: 12 scenes in one wavefront; "
+                         "box; bdpt: renderer::bdpt on the caustic room; ltdirect: light tracing on the Cornell "
+                         "box; batch: 12 scenes in one wavefront; "
                          "guiding: learned path guiding vs plain PT at equal time; surface: surface geometry "
                          "at the ray-cast hits")
     ap.add_argument("--mlp-only", action="store_true", help="guiding: time the MLP kernels only")

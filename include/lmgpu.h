@@ -221,6 +221,19 @@ int lmgpu_render_ptdirect(lmgpu_scene* scene, const lmgpu_pt_params* params, flo
 int lmgpu_render_ptdirect_device(lmgpu_scene* scene, const lmgpu_pt_params* params, float* d_image,
                                  float* d_variance, void* stream);
 
+/* Renders the scene by light tracing: params->spp x W x H light paths, each
+ * connected to the pinhole at every vertex (weight 1), Russian roulette 0.5
+ * after every hit, at most max_num_vertices vertices per full path.  Stands
+ * in for Renderer::Render of renderer::ltdirect
+ * (src/liblightmetrica/renderer/renderer_ltdirect.cpp:72-279; num_samples =
+ * spp x W x H).  Needs an area light; scenes with an environment light are
+ * rejected.  The variance is that of the image's light-path estimate. */
+int lmgpu_render_ltdirect(lmgpu_scene* scene, const lmgpu_pt_params* params, float* image, float* variance);
+
+/* As lmgpu_render_ltdirect into device buffers on `stream`. */
+int lmgpu_render_ltdirect_device(lmgpu_scene* scene, const lmgpu_pt_params* params, float* d_image,
+                                 float* d_variance, void* stream);
+
 /* Renders the scene with bidirectional path tracing (all (s, t) strategies,
  * power-heuristic MIS) and writes the film as lmgpu_render_pt does.  Stands
  * in for Renderer::Render of renderer::bdpt

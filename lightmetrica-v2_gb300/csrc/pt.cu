@@ -91,39 +91,6 @@ __device__ __forceinline__ bool nee_sample(const Ctx& C, const PV& v, int type, 
     return any;
 }
 
-// Appends a pending light-sample contribution (shadow ray v -> L) with
-// warp-aggregated atomics; every lane of the warp must call it.
-__device__ __forceinline__ void append_nee(bool has, const PV& v, const PV& L, const float c[3], uint32_t pix,
-                                           uint32_t path, float4* __restrict__ rays, float4* __restrict__ rec,
-                                           uint32_t* __restrict__ rec_path, uint32_t* __restrict__ count)
-{
-    const unsigned m = __ballot_sync(0xffffffffu, has);
-    if (m == 0u) return;
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned leader = __ffs(m) - 1u;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (has) {
-        const uint32_t o = base + __popc(m & ((1u << lane) - 1u));
-        float3 d = L.p - v.p;
-        const float len = sqrtf(dot3(d, d));
-        d = d * (1.0f / len);
-        rays[2 * o] = make_float4(v.p.x, v.p.y, v.p.z, 1e-4f);
-        rays[2 * o + 1] = make_float4(d.x, d.y, d.z, len * (1.0f - 1e-4f));
-        rec[o] = make_float4(c[0], c[1], c[2], __uint_as_float(pix));
-        rec_path[o] = path;
-    }
-}
-
-__device__ __forceinline__ uint32_t pixel_at(const CameraGPU& cam, float rx, float ry)
-{
-    int ix = (int)(rx * (float)cam.width), iy = (int)(ry * (float)cam.height);
-    ix = ix < 0 ? 0 : (ix > cam.width - 1 ? cam.width - 1 : ix);
-    iy = iy < 0 ? 0 : (iy > cam.height - 1 ? cam.height - 1 : iy);
-    return (uint32_t)iy * (uint32_t)cam.width + (uint32_t)ix;
-}
-
 template <int MODE>
 __global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p0, uint32_t n, uint32_t seed,
                                                                float4* __restrict__ rays,

@@ -93,16 +93,23 @@ int clear_film(lmgpu_scene* sc, uint64_t npix, cudaStream_t stream)
     return LMGPU_OK;
 }
 
-int finalize_film(lmgpu_scene* sc, uint64_t spp, float* d_image, float* d_variance, cudaStream_t stream)
+int finalize_film_nx(lmgpu_scene* sc, uint64_t spp, double n_x, float* d_image, float* d_variance,
+                     cudaStream_t stream)
 {
     const uint64_t npix = (uint64_t)sc->cam.width * sc->cam.height;
     const uint32_t n3 = (uint32_t)(3 * npix);
     k_film_finalize<<<(n3 + 255) / 256, 256, 0, stream>>>(sc->film, sc->film_sq, sc->film_x, sc->film_x_sq, n3,
-                                                         (double)spp, (double)spp * (double)(npix - 1), d_image,
-                                                         d_variance);
+                                                         (double)spp, n_x, d_image, d_variance);
     LMGPU_CUDA_TRY(cudaGetLastError());
     sc->launches++;
     return LMGPU_OK;
+}
+
+int finalize_film(lmgpu_scene* sc, uint64_t spp, float* d_image, float* d_variance, cudaStream_t stream)
+{
+    // splats from other samples: those of the other pixels' strata
+    const uint64_t npix = (uint64_t)sc->cam.width * sc->cam.height;
+    return finalize_film_nx(sc, spp, (double)spp * (double)(npix - 1), d_image, d_variance, stream);
 }
 
 // Light tables: per light primitive its triangles and their normalised area
@@ -432,6 +439,19 @@ int lmgpu_render_ptdirect(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* im
 {
     clear_error();
     return render_host("lmgpu_render_ptdirect", render_pt_direct, sc, prm, image, variance);
+}
+
+int lmgpu_render_ltdirect_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance,
+                                 void* stream)
+{
+    clear_error();
+    return render_device("lmgpu_render_ltdirect_device", render_ltdirect, sc, prm, d_image, d_variance, stream);
+}
+
+int lmgpu_render_ltdirect(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image, float* variance)
+{
+    clear_error();
+    return render_host("lmgpu_render_ltdirect", render_ltdirect, sc, prm, image, variance);
 }
 
 int lmgpu_render_bdpt_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance,

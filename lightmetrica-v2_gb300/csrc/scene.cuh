@@ -123,9 +123,15 @@ int ensure_queues(lmgpu_scene* sc, uint64_t n);
 SceneGPU scene_view(const lmgpu_scene* sc);
 int clear_film(lmgpu_scene* sc, uint64_t npix, cudaStream_t stream);
 int finalize_film(lmgpu_scene* sc, uint64_t spp, float* d_image, float* d_variance, cudaStream_t stream);
+// As finalize_film with n_x samples behind the other-samples film.
+int finalize_film_nx(lmgpu_scene* sc, uint64_t spp, double n_x, float* d_image, float* d_variance,
+                     cudaStream_t stream);
 // mode: 0 renderer::pt, 1 renderer::ptmis, 2 renderer::ptdirect
 int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream,
               int mode);
 int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream);
+// renderer::ltdirect (lt.cu)
+int render_ltdirect(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance,
+                    cudaStream_t stream);
 
 }  // namespace lmgpu

@@ -97,6 +97,8 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_render_bdpt.argtypes = [vp, vp, vp, vp]
     L.lmgpu_render_ptmis.argtypes = [vp, vp, vp, vp]
     L.lmgpu_render_ptdirect.argtypes = [vp, vp, vp, vp]
+    L.lmgpu_render_ltdirect.argtypes = [vp, vp, vp, vp]
+    L.lmgpu_render_ltdirect_device.argtypes = [vp, vp, vp, vp, vp]
     L.lmgpu_guide_num_params.argtypes = [ctypes.POINTER(u64)]
     L.lmgpu_guide_create.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(vp)]
     L.lmgpu_guide_destroy.argtypes = [vp]
@@ -134,7 +136,8 @@ def lib() -> ctypes.CDLL:
                  "lmgpu_guide_get_params", "lmgpu_guide_set_params", "lmgpu_guide_forward", "lmgpu_guide_gradient",
                  "lmgpu_guide_train_step", "lmgpu_guide_forward_device", "lmgpu_guide_train_step_device",
                  "lmgpu_render_pt_guided", "lmgpu_render_pt_guided_device",
-                 "lmgpu_render_ptdirect_device",
+                 "lmgpu_render_ptdirect_device", "lmgpu_render_ltdirect", "lmgpu_render_ltdirect_device",
+                 "lmgpu_accel_set_attributes", "lmgpu_surface", "lmgpu_surface_device",
                  "lmgpu_scene_set_environment"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
@@ -353,6 +356,20 @@ class Scene:
         prm = PtParams(spp, max_num_vertices, seed)
         _check(lib().lmgpu_render_ptdirect(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
         return img, var
+
+    def render_ltdirect(self, spp: int, max_num_vertices: int = -1, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        """renderer::ltdirect with spp x W x H light paths: film (H, W, 3) and
+        per-pixel variance of the estimate."""
+        img = np.empty((self.height, self.width, 3), np.float32)
+        var = np.empty((self.height, self.width, 3), np.float32)
+        prm = PtParams(spp, max_num_vertices, seed)
+        _check(lib().lmgpu_render_ltdirect(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
+        return img, var
+
+    def render_ltdirect_device(self, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,
+                               seed: int = 0, stream: int = 0) -> None:
+        prm = PtParams(spp, max_num_vertices, seed)
+        _check(lib().lmgpu_render_ltdirect_device(self._h, ctypes.byref(prm), d_image, d_variance, stream))
 
     def render_pt_guided(self, guide, spp: int, max_num_vertices: int = -1, seed: int = 0, alpha: float = 0.5,
                          learning_rate: float = 1e-3, train: bool = True, batch: int = 1 << 18,

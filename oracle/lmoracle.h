@@ -116,6 +116,14 @@ uint64_t lmo_render_ptdirect(const float* tris, const int32_t* tri_prim, size_t 
                              int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
                              uint64_t seed, int threads, double* sum, double* sumsq);
 
+/* renderer::ltdirect (renderer_ltdirect.cpp:72-279): num_samples light paths,
+ * sensor connections at every vertex; films as lmo_render_bdpt.  (The
+ * variant with an independent emission-direction sample is
+ * lmo_render_bdpt_ex with independent_light_dir = -4.) */
+uint64_t lmo_render_ltdirect(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
+                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
+                             uint64_t seed, int threads, double* sum, double* sumsq);
+
 /* As lmo_render_bdpt; independent_light_dir != 0 draws the light subpath's
  * first direction from its own 2D sample instead of reusing the position's
  * (the reference's light_area.cpp:73-80 reuses it).  A diagnostic that

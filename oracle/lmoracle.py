@@ -61,6 +61,8 @@ def lib() -> ctypes.CDLL:
         L.lmo_render_ptmis.restype = ctypes.c_uint64
         L.lmo_render_ptdirect.argtypes = L.lmo_render_bdpt.argtypes
         L.lmo_render_ptdirect.restype = ctypes.c_uint64
+        L.lmo_render_ltdirect.argtypes = L.lmo_render_bdpt.argtypes
+        L.lmo_render_ltdirect.restype = ctypes.c_uint64
         L.lmo_surface.argtypes = [vp, vp, vp, vp, vp, vp, sz, vp]
         L.lmo_surface.restype = None
         _lib = L
@@ -310,6 +312,26 @@ def render_ptmis(scene: dict, num_samples: int, max_num_vertices: int, seed: int
     fn(tris.ctypes.data, tri_prim.ctypes.data, tris.shape[0], ctypes.addressof(prims),
        len(scene["prims"]), ctypes.addressof(cam), num_samples, max_num_vertices, seed, threads,
        s.ctypes.data, q.ctypes.data)
+    img = s * (W * H / num_samples)
+    return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}
+
+
+def render_ltdirect(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,
+                    independent_light_dir: bool = False) -> dict:
+    """The oracle's renderer::ltdirect (light paths connected to the sensor at
+    every vertex): film (H, W, 3) and per-pixel variance.
+    independent_light_dir: the diagnostic variant that draws the emission
+    direction from its own 2D sample."""
+    tris = np.ascontiguousarray(np.concatenate([p["tris"] for p in scene["prims"]]), dtype=np.float32)
+    tri_prim = np.concatenate([np.full(p["tris"].shape[0], i, np.int32) for i, p in enumerate(scene["prims"])])
+    W, H = scene["camera"]["width"], scene["camera"]["height"]
+    s = np.zeros((H, W, 3), np.float64)
+    q = np.zeros((H, W, 3), np.float64)
+    prims = scene_prims(scene)
+    cam = scene_camera(scene)
+    lib().lmo_render_bdpt_ex(tris.ctypes.data, tri_prim.ctypes.data, tris.shape[0], ctypes.addressof(prims),
+                             len(scene["prims"]), ctypes.addressof(cam), num_samples, max_num_vertices, seed,
+                             threads, s.ctypes.data, q.ctypes.data, -4 if independent_light_dir else -3)
     img = s * (W * H / num_samples)
     return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}
 

@@ -35,6 +35,8 @@
  *   pdf_light = 0 after a specular vertex (:246-270); roulette 0.5 (:285-293).
  * renderer::ptdirect (renderer_ptdirect.cpp:72-291): the same light samples
  *   with weight 1, and no emission counted on BSDF-sampled hits.
+ * renderer::ltdirect (renderer_ltdirect.cpp:72-279): light paths connected to
+ *   the sensor at every vertex with weight 1, roulette 0.5 after each hit.
  * Scene3::Intersect / Visible through the oracle's accel::bvh_sahbin.
  * Environment lights are not part of this restatement.
  */
@@ -114,7 +116,7 @@ typedef struct {
     int W, H;
     int max_v;
     int independent_light_dir;
-    int ptmis;     /* 1: renderer::ptmis, 2: renderer::ptdirect */
+    int ptmis;     /* 1: renderer::ptmis, 2: renderer::ptdirect, 3: renderer::ltdirect */
     uint64_t num_samples, seed;
     int threads;
     double *sum, *sumsq;
@@ -871,6 +873,98 @@ static void* ptmis_worker(void* arg)
     return NULL;
 }
 
+/* Renderer_LTDirect sample closure (renderer_ltdirect.cpp:74-276): a light
+ * path (light primitive uniformly, area-CDF triangle, uniform point, the
+ * emission direction from the same 2D sample as the position,
+ * light_area.cpp:73-80), connected to the sensor at every vertex with
+ * weight 1 (:118-168), extended by BSDF sampling (:170-205), Russian roulette
+ * 0.5 after each hit (:223-235).  Every splat lands where its connection
+ * meets the film. */
+static void* lt_worker(void* arg)
+{
+    void** a = (void**)arg;
+    bd_job* J = (bd_job*)a[0];
+    const int wi_ = (int)(intptr_t)a[1];
+    const int W = J->W, H = J->H;
+    double* sum = (double*)calloc((size_t)W * H * 3, sizeof(double));
+    double* sumsq = (double*)calloc((size_t)W * H * 3, sizeof(double));
+    uint64_t rng = J->seed ^ 0x510E527FADE682D1ull;
+    rng = splitmix64(&rng) ^ ((uint64_t)wi_ * 0xA0761D6478BD642Full);
+    rng = splitmix64(&rng);
+    splat_list* sl = (splat_list*)malloc(sizeof(splat_list));
+    const float pdfL = 1.0f / (float)J->nlights;
+    const uint64_t b = J->num_samples * (uint64_t)wi_ / (uint64_t)J->threads;
+    const uint64_t e = J->num_samples * (uint64_t)(wi_ + 1) / (uint64_t)J->threads;
+    pvx E;
+    E.p = J->eye;
+    E.n = J->vz;
+    E.prim = -1;
+    E.type = T_E;
+    E.degenerated = 1;
+    for (uint64_t smp = b; smp < e; smp++) {
+        sl->n = 0;
+        pvx cur;
+        const float us = rnd(&rng), a0 = rnd(&rng), a1 = rnd(&rng);
+        sample_light_pos(J, us, a0, a1, &cur, NULL);
+        cur.type = T_L;
+        /* the reference draws the emission direction from the position's 2D
+         * sample; the diagnostic variant draws a fresh one */
+        float d0 = a0, d1 = a1;
+        if (J->independent_light_dir) { d0 = rnd(&rng); d1 = rnd(&rng); }
+        const v3 initWo = to_world(cur.n, cosine_hemisphere(d0, d1));
+        const float pdfPL = J->light_inv_area[J->prim_light[cur.prim]];
+        spd thr = S1(1.0f / pdfPL / pdfL);
+        v3 wi = zero3();
+        int nv = 1;
+        for (;;) {
+            if (J->max_v != -1 && nv >= J->max_v) break;
+            /* sensor connection (:118-168); pdf_E = pdf_PE = We_P = 1 for the pinhole */
+            {
+                const v3 ppE = normalize(sub(E.p, cur.p));
+                const spd fsL = eval_dir(J, &cur, cur.type, wi, ppE, DIR_LE, 1);
+                const spd fsE = eval_dir(J, &E, T_E, zero3(), mul(ppE, -1.0f), DIR_EL, 0);
+                const float G = geometry_term(&cur, &E);
+                const spd C = sscale(smul(thr, smul(fsL, fsE)), G);
+                float rx, ry;
+                if (!sblack(C) && raster_pos(J, mul(ppE, -1.0f), &rx, &ry) && visible(J, cur.p, E.p))
+                    splat_add(sl, pixel_of(J, rx, ry), C);
+            }
+            /* next direction (:170-205) */
+            v3 wo;
+            if (cur.type == T_L) {
+                wo = initWo;
+            } else {
+                const float u0 = rnd(&rng), u1 = rnd(&rng), uc = rnd(&rng);
+                if (!sample_dir(J, &cur, wi, u0, u1, uc, &wo)) break;
+            }
+            const float pdfD = pdf_dir(J, &cur, cur.type, wi, wo, 0);
+            const spd fs = eval_dir(J, &cur, cur.type, wi, wo, DIR_LE, 0);
+            if (sblack(fs)) break;
+            thr = smul(thr, sscale(fs, 1.0f / pdfD));
+            pvx hit;
+            if (!trace(J, cur.p, wo, &hit)) break;
+            /* roulette (:223-235) */
+            if (rnd(&rng) > 0.5f) break;
+            thr = sscale(thr, 2.0f);
+            cur = hit;
+            wi = mul(wo, -1.0f);
+            nv++;
+        }
+        for (int k = 0; k < sl->n; k++)
+            for (int c = 0; c < 3; c++) {
+                sum[3 * (size_t)sl->pix[k] + c] += sl->val[k][c];
+                sumsq[3 * (size_t)sl->pix[k] + c] += sl->val[k][c] * sl->val[k][c];
+            }
+    }
+    pthread_mutex_lock(&J->lock);
+    for (size_t i = 0; i < (size_t)W * H * 3; i++) { J->sum[i] += sum[i]; J->sumsq[i] += sumsq[i]; }
+    pthread_mutex_unlock(&J->lock);
+    free(sl);
+    free(sum);
+    free(sumsq);
+    return NULL;
+}
+
 uint64_t lmo_render_bdpt(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims, int nprims,
                          const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices, uint64_t seed,
                          int threads, double* sum, double* sumsq)
@@ -895,8 +989,17 @@ uint64_t lmo_render_ptdirect(const float* tris, const int32_t* tri_prim, size_t 
                               sum, sumsq, -2);
 }
 
+uint64_t lmo_render_ltdirect(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
+                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
+                             uint64_t seed, int threads, double* sum, double* sumsq)
+{
+    return lmo_render_bdpt_ex(tris, tri_prim, ntri, prims, nprims, cam, num_samples, max_num_vertices, seed, threads,
+                              sum, sumsq, -3);
+}
+
 /* independent_light_dir: 0 / 1 select the BDPT variants; -1 runs
- * renderer::ptmis, -2 renderer::ptdirect */
+ * renderer::ptmis, -2 renderer::ptdirect, -3 renderer::ltdirect, -4
+ * renderer::ltdirect with an independent emission-direction sample */
 uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
                             uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir)
@@ -957,8 +1060,8 @@ uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t n
     J.W = cam->width;
     J.H = cam->height;
     J.max_v = max_num_vertices;
-    J.independent_light_dir = independent_light_dir > 0;
-    J.ptmis = independent_light_dir < 0 ? -independent_light_dir : 0;
+    J.independent_light_dir = independent_light_dir > 0 || independent_light_dir == -4;
+    J.ptmis = independent_light_dir == -4 ? 3 : (independent_light_dir < 0 ? -independent_light_dir : 0);
     J.num_samples = num_samples;
     J.seed = seed;
     J.threads = threads < 1 ? 1 : threads;
@@ -976,7 +1079,8 @@ uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t n
         for (int i = 0; i < J.threads; i++) {
             args[2 * i] = &J;
             args[2 * i + 1] = (void*)(intptr_t)i;
-            pthread_create(&th[i], &attr, J.ptmis ? ptmis_worker : bd_worker, &args[2 * i]);
+            pthread_create(&th[i], &attr, J.ptmis == 3 ? lt_worker : (J.ptmis ? ptmis_worker : bd_worker),
+                           &args[2 * i]);
         }
         for (int i = 0; i < J.threads; i++) pthread_join(th[i], NULL);
     }

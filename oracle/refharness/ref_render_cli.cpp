@@ -1,6 +1,6 @@
-// Command-line driver around the reference's own renderer::pt, renderer::bdpt
-// renderer::ptmis and renderer::ptdirect
-// (src/liblightmetrica/renderer/renderer_{pt,bdpt,ptmis,ptdirect}.cpp)
+// Command-line driver around the reference's own renderer::pt, renderer::bdpt,
+// renderer::ptmis, renderer::ptdirect and renderer::ltdirect
+// (src/liblightmetrica/renderer/renderer_{pt,bdpt,ptmis,ptdirect,ltdirect}.cpp)
 // with the reference's own
 // bsdf::diffuse, bsdf::null, light::area, sensor::pinhole, Random (dSFMT)
 // and accel components, compiled from the reference sources as a CPU oracle.
@@ -32,7 +32,7 @@
 //                     environment hit; the harness sets it to the environment
 //                     light's primitive, as a fixed scene would.
 //
-// Usage: ref_render <scene.bin> <out.bin> [pt|bdpt|ptmis|ptdirect]   (renderer::pt by default)
+// Usage: ref_render <scene.bin> <out.bin> [pt|bdpt|ptmis|ptdirect|ltdirect]   (renderer::pt by default)
 //   scene.bin: u32 magic 'LMRS', u32 version 2, u32 W, H,
 //              f32 eye[3], center[3], up[3], fov_deg,
 //              u32 nprims, per primitive: i32 bsdf (0 null, 1 diffuse,
@@ -307,7 +307,7 @@ static std::string Vec3Str(const float* v)
 
 int main(int argc, char** argv)
 {
-    if (argc < 3) { std::fprintf(stderr, "usage: %s scene.bin out.bin [pt|bdpt|ptmis|ptdirect]\n", argv[0]); return 2; }
+    if (argc < 3) { std::fprintf(stderr, "usage: %s scene.bin out.bin [pt|bdpt|ptmis|ptdirect|ltdirect]\n", argv[0]); return 2; }
     const std::string rendererKey = std::string("renderer::") + (argc > 3 ? argv[3] : "pt");
     std::vector<char> buf;
     {

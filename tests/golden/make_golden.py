@@ -35,6 +35,10 @@ Fixtures written:
       The Cornell box rendered by the reference's own renderer::ptdirect
       (light samples only) at 64x64, 16,384 samples per pixel,
       max_num_vertices 9, single and double precision.
+  cornell_ltdirect.npz
+      The Cornell box rendered by the reference's own renderer::ltdirect
+      (light tracing, a sensor connection at every vertex) with 64x64x16,384
+      light paths, max_num_vertices 9, single and double precision.
   surface.npz
       Surface geometry at hits from the reference's own
       IntersectionUtils::CreateTriangleIntersection (intersectionutils.h),
@@ -334,6 +338,9 @@ def main() -> None:
     if want("cornell_ptdirect"):
         np.savez_compressed(os.path.join(HERE, "cornell_ptdirect.npz"),
                             **pt_case(scenes.cornell_box(64, 64), 16384, 20241201, "ptdirect", 9))
+    if want("cornell_ltdirect"):
+        np.savez_compressed(os.path.join(HERE, "cornell_ltdirect.npz"),
+                            **pt_case(scenes.cornell_box(64, 64), 16384, 20241301, "ltdirect", 9))
     print("fixtures written to", HERE)
 
 

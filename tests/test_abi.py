@@ -61,11 +61,12 @@ def test_null_arguments_rejected(gpu_lib):
 
 
 @pytest.mark.parametrize("plugin", ["accel_cuda", "renderer_pt_cuda", "renderer_ptmis_cuda", "renderer_ptdirect_cuda",
-                                    "renderer_bdpt_cuda", "renderer_pt_guided_cuda"])
+                                    "renderer_ltdirect_cuda", "renderer_bdpt_cuda", "renderer_pt_guided_cuda"])
 def test_reference_plugin_compiles_against_reference_headers(repo_dir, plugin):
     """plugin/*.cpp, the bindings a maintainer adds to the reference tree
     (accel::cuda, renderer::pt_cuda, renderer::ptmis_cuda,
-    renderer::ptdirect_cuda, renderer::bdpt_cuda, renderer::pt_guided_cuda),
+    renderer::ptdirect_cuda, renderer::ltdirect_cuda, renderer::bdpt_cuda,
+    renderer::pt_guided_cuda),
     compile against the
     reference's own headers (x86-64 only: the reference forces SSE)."""
     import platform
