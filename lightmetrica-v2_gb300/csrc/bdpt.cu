@@ -44,6 +44,9 @@ namespace lmgpu {
 namespace {
 
 constexpr int kMaxV = 16;
+// Connection work items are grouped by strategy (s, t), bucket s * kStrideST + t.
+constexpr int kStrideST = kMaxV + 1;
+constexpr int kBuckets = kStrideST * kStrideST;
 constexpr uint64_t kWaveSamples = 1ull << 19;
 constexpr int kBdptThreads = 128;
 constexpr uint32_t kKeyBdpt = 0x42445054u;
@@ -410,6 +413,14 @@ __device__ __forceinline__ void splat_px(double* film, double* film_sq, uint32_t
     }
 }
 
+// Eye-subpath vertices t that light-subpath vertex count s connects to.
+__device__ __forceinline__ int t_limit(int s, int nE, int max_path)
+{
+    int t = nE;
+    if (max_path >= 0 && t > max_path - s) t = max_path - s;
+    return t > 0 ? t : 0;
+}
+
 __device__ __forceinline__ int num_connections(int nL, int nE, int max_path)
 {
     int c = 0;
@@ -426,15 +437,18 @@ __device__ __forceinline__ int num_connections(int nL, int nE, int max_path)
 // and are evaluated here; the s, t >= 1 connections are counted and given a
 // contiguous range of work items.  t = 0 strategies carry no weight with a
 // pinhole sensor (its position cannot be hit and EvaluateCst is 0).
-__global__ void __launch_bounds__(kBdptThreads) k_bd_count(Ctx C, Wave w, uint32_t* __restrict__ base,
+__global__ void __launch_bounds__(kBdptThreads) k_bd_count(Ctx C, Wave w, uint32_t* __restrict__ hist,
                                                            uint32_t* __restrict__ total,
                                                            double* __restrict__ film_x,
                                                            double* __restrict__ film_x_sq)
 {
+    __shared__ uint32_t s_hist[kBuckets];
+    for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) s_hist[k] = 0u;
+    __syncthreads();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t cnt = 0;
+    const int nL = i < w.n ? w.count[0][i] : 0, nE = i < w.n ? w.count[1][i] : 0;
     if (i < w.n) {
-        const int nL = w.count[0][i], nE = w.count[1][i];
         cnt = (uint32_t)num_connections(nL, nE, C.max_path);
         const uint32_t own_pix = (uint32_t)((w.p0 + i) % w.npix);
         float own[3] = {0.0f, 0.0f, 0.0f};
@@ -465,30 +479,58 @@ __global__ void __launch_bounds__(kBdptThreads) k_bd_count(Ctx C, Wave w, uint32
         }
         for (int k = 0; k < 3; k++) w.own[3 * (size_t)i + k] = own[k];
     }
-    // contiguous item ranges: warp-aggregated allocation
+    // item total, and the items per strategy (s, t) for the buckets
     const unsigned lane = threadIdx.x & 31u;
-    uint32_t incl = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= (unsigned)o) incl += v;
+    const uint32_t wsum = __reduce_add_sync(0xffffffffu, cnt);
+    if (lane == 0u && wsum > 0u) atomicAdd(total, wsum);
+    const int sw = __reduce_max_sync(0xffffffffu, nL);
+    for (int sl = 1; sl <= sw; sl++) {
+        const int tm = sl <= nL ? t_limit(sl, nE, C.max_path) : 0;
+        const int tw = __reduce_max_sync(0xffffffffu, tm);
+        for (int t = 1; t <= tw; t++) {
+            const unsigned m = __ballot_sync(0xffffffffu, t <= tm);
+            if (lane == 0u) atomicAdd(&s_hist[sl * kStrideST + t], (uint32_t)__popc(m));
+        }
     }
-    uint32_t wbase = 0;
-    if (lane == 31u && incl > 0u) wbase = atomicAdd(total, incl);
-    wbase = __shfl_sync(0xffffffffu, wbase, 31);
-    if (i < w.n) base[i] = wbase + incl - cnt;
+    __syncthreads();
+    for (int k = threadIdx.x; k < kBuckets; k += blockDim.x)
+        if (s_hist[k]) atomicAdd(&hist[k], s_hist[k]);
 }
 
-// Work items of the s, t >= 1 connections: sample | s << 20 | t << 26.
-__global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ base, uint32_t* __restrict__ items)
+// Bucket offsets: exclusive scan of the per-strategy counts; cursors reset.
+__global__ void k_bd_buckets(uint32_t* __restrict__ hist, uint32_t* __restrict__ offset, uint32_t* __restrict__ cursor)
+{
+    if (threadIdx.x != 0) return;
+    uint32_t acc = 0;
+    for (int k = 0; k < kBuckets; k++) {
+        offset[k] = acc;
+        acc += hist[k];
+        cursor[k] = 0u;
+    }
+}
+
+// Work items of the s, t >= 1 connections, sample | s << 20 | t << 26,
+// scattered into their strategy's bucket so that a warp of k_bd_connect
+// evaluates one strategy (same path length, same MIS loops) at a time.
+__global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ offset, uint32_t* __restrict__ cursor,
+                           uint32_t* __restrict__ items)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w.n) return;
-    const int nL = w.count[0][i], nE = w.count[1][i];
-    uint32_t o = base[i];
-    for (int s = 1; s <= nL; s++) {
-        int tmax = nE;
-        if (C.max_path >= 0 && tmax > C.max_path - s) tmax = C.max_path - s;
-        for (int t = 1; t <= tmax; t++) items[o++] = i | ((uint32_t)s << 20) | ((uint32_t)t << 26);
+    const unsigned lane = threadIdx.x & 31u;
+    const int nL = i < w.n ? w.count[0][i] : 0, nE = i < w.n ? w.count[1][i] : 0;
+    const int sw = __reduce_max_sync(0xffffffffu, nL);
+    for (int s = 1; s <= sw; s++) {
+        const int tm = s <= nL ? t_limit(s, nE, C.max_path) : 0;
+        const int tw = __reduce_max_sync(0xffffffffu, tm);
+        for (int t = 1; t <= tw; t++) {
+            const bool has = t <= tm;
+            const unsigned m = __ballot_sync(0xffffffffu, has);
+            const int b = s * kStrideST + t;
+            uint32_t base = 0;
+            if (lane == (unsigned)(__ffs(m) - 1)) base = atomicAdd(&cursor[b], (uint32_t)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+            if (has) items[offset[b] + base + __popc(m & ((1u << lane) - 1u))] = i | ((uint32_t)s << 20) | ((uint32_t)t << 26);
+        }
     }
 }
 
@@ -589,8 +631,6 @@ struct BdptState {
     uint64_t ext_hit_cap = 0;
     lmgpu_hit* sh_hit = nullptr;
     uint64_t sh_hit_cap = 0;
-    uint32_t* base = nullptr;
-    uint64_t base_cap = 0;
     uint32_t* counter = nullptr;  // [0] active / item counter
     uint64_t counter_cap = 0;
     uint32_t* h_counter = nullptr;
@@ -602,13 +642,16 @@ struct BdptState {
     uint64_t c_rec_cap = 0;
     lmgpu_hit* c_hit = nullptr;
     uint64_t c_hit_cap = 0;
+    uint32_t* buckets = nullptr;  // per strategy: counts, offsets, cursors
+    uint64_t buckets_cap = 0;
 };
 
 void free_bdpt(BdptState* b)
 {
     if (!b) return;
     void* ptrs[] = {b->verts, b->pend, b->counts, b->own, b->active[0], b->active[1], b->ext[0], b->ext[1],
-                    b->sh, b->ext_hit, b->sh_hit, b->base, b->counter, b->items, b->c_rays, b->c_rec, b->c_hit};
+                    b->sh, b->ext_hit, b->sh_hit, b->counter, b->items, b->c_rays, b->c_rec, b->c_hit,
+                    b->buckets};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->h_counter) cudaFreeHost(b->h_counter);
@@ -664,8 +707,8 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
         (rc = grow_dev(&B.active[1], &B.active_cap[1], 2 * stride)) ||
         (rc = grow_dev(&B.ext[0], &B.ext_cap[0], 4 * stride)) || (rc = grow_dev(&B.ext[1], &B.ext_cap[1], 4 * stride)) ||
         (rc = grow_dev(&B.sh, &B.sh_cap, 4 * stride)) || (rc = grow_dev(&B.ext_hit, &B.ext_hit_cap, 2 * stride)) ||
-        (rc = grow_dev(&B.sh_hit, &B.sh_hit_cap, 2 * stride)) || (rc = grow_dev(&B.base, &B.base_cap, stride)) ||
-        (rc = grow_dev(&B.counter, &B.counter_cap, 1)))
+        (rc = grow_dev(&B.sh_hit, &B.sh_hit_cap, 2 * stride)) || (rc = grow_dev(&B.counter, &B.counter_cap, 1)) ||
+        (rc = grow_dev(&B.buckets, &B.buckets_cap, 3 * kBuckets)))
         return rc;
     if (!B.h_counter && cudaMallocHost((void**)&B.h_counter, sizeof(uint32_t)) != cudaSuccess) {
         set_error("lmgpu_render_bdpt: pinned allocation failed");
@@ -713,7 +756,8 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
         }
         // connections
         LMGPU_CUDA_TRY(cudaMemsetAsync(B.counter, 0, sizeof(uint32_t), stream));
-        k_bd_count<<<blocks(w.n, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.base, B.counter, sc->film_x,
+        LMGPU_CUDA_TRY(cudaMemsetAsync(B.buckets, 0, sizeof(uint32_t) * kBuckets, stream));
+        k_bd_count<<<blocks(w.n, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.buckets, B.counter, sc->film_x,
                                                                          sc->film_x_sq);
         LMGPU_CUDA_TRY(cudaGetLastError());
         uint32_t n_items = 0;
@@ -723,7 +767,9 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
                 (rc = grow_dev(&B.c_rays, &B.c_rays_cap, 2ull * n_items)) ||
                 (rc = grow_dev(&B.c_rec, &B.c_rec_cap, n_items)) || (rc = grow_dev(&B.c_hit, &B.c_hit_cap, n_items)))
                 return rc;
-            k_bd_items<<<blocks(w.n, 256), 256, 0, stream>>>(C, w, B.base, B.items);
+            k_bd_buckets<<<1, 32, 0, stream>>>(B.buckets, B.buckets + kBuckets, B.buckets + 2 * kBuckets);
+            k_bd_items<<<blocks(w.n, 256), 256, 0, stream>>>(C, w, B.buckets + kBuckets, B.buckets + 2 * kBuckets,
+                                                            B.items);
             k_bd_connect<<<blocks(n_items, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.items, n_items,
                                                                                    B.c_rays, B.c_rec);
             LMGPU_CUDA_TRY(cudaGetLastError());
@@ -731,7 +777,7 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
             k_bd_splat<<<blocks(n_items, 256), 256, 0, stream>>>(w, B.items, n_items, B.c_rec, B.c_hit, sc->film_x,
                                                                   sc->film_x_sq);
             LMGPU_CUDA_TRY(cudaGetLastError());
-            sc->launches += 4;
+            sc->launches += 5;
         }
         k_bd_flush<<<blocks(w.n, 256), 256, 0, stream>>>(w, sc->film, sc->film_sq);
         LMGPU_CUDA_TRY(cudaGetLastError());
