@@ -23,15 +23,18 @@
 //                  traversal of the direct rays (trace.cu, persistent), then
 //                  k_bd_step: store the step's vertex, roulette, sample the
 //                  rays of step k + 1 for the surviving subpaths (compacted);
-//   k_bd_count     per sample: the s = 0 strategies (no ray needed) and the
-//                  number of s, t >= 1 connections, whose work items
-//                  k_bd_items lays out contiguously per sample;
-//   k_bd_connect   one thread per connection: contribution (unweighted
-//                  estimate, MIS weight, selection pdf) and its shadow ray;
-//                  any-hit traversal of all shadow rays; k_bd_splat adds the
-//                  unoccluded ones; k_bd_flush merges each sample's
-//                  own-pixel contributions into the film (the reference film
-//                  squares per-sample sums, so the variance estimate does too).
+//   k_bd_count     per sample: the number of work items per strategy (s, t)
+//                  -- the s = 0 strategies (no ray needed) and the s, t >= 1
+//                  connections -- into per-strategy buckets, which
+//                  k_bd_buckets lays out and k_bd_items fills, so that the
+//                  warps of the next kernel each evaluate one strategy;
+//   k_bd_connect   one thread per item: contribution (unweighted estimate,
+//                  MIS weight, selection pdf) and, for connections, the
+//                  shadow ray; any-hit traversal of all shadow rays;
+//                  k_bd_splat adds the unoccluded ones; k_bd_flush merges
+//                  each sample's own-pixel contributions into the film (the
+//                  reference film squares per-sample sums, so the variance
+//                  estimate does too).
 // Subpath vertices live in HBM as 32-byte records, [vertex k][sample], so
 // the kernels of one step read and write them coalesced.  Eye subpaths start
 // at per-pixel stratified raster positions; random numbers are Philox keyed
@@ -48,6 +51,8 @@ constexpr int kMaxV = 16;
 constexpr int kStrideST = kMaxV + 1;
 constexpr int kBuckets = kStrideST * kStrideST;
 constexpr uint64_t kWaveSamples = 1ull << 19;
+// Sample index bits of a connection work item (kWaveSamples samples).
+constexpr uint32_t kSampleMask = (uint32_t)kWaveSamples - 1u;
 constexpr int kBdptThreads = 128;
 constexpr uint32_t kKeyBdpt = 0x42445054u;
 
@@ -421,6 +426,17 @@ __device__ __forceinline__ int t_limit(int s, int nE, int max_path)
     return t > 0 ? t : 0;
 }
 
+// Eye-subpath lengths t of the s = 0 strategies (the eye subpath ends on a
+// light, d = 0, or its direct vertex is one, d = 1): 2 .. t_limit_s0.
+__device__ __forceinline__ int t_limit_s0(int nE, int max_path)
+{
+    return max_path >= 0 && nE > max_path ? max_path : nE;
+}
+
+// Bucket of the s = 0 items: (0, t) for d = 0, (t, 0) for d = 1 (bins no
+// connection uses).
+__device__ __forceinline__ int bucket_s0(int t, int d) { return d ? t * kStrideST : t; }
+
 __device__ __forceinline__ int num_connections(int nL, int nE, int max_path)
 {
     int c = 0;
@@ -432,15 +448,13 @@ __device__ __forceinline__ int num_connections(int nL, int nE, int max_path)
     return c;
 }
 
-// Per sample: the strategies with s = 0 (the eye subpath reaches a light, or
-// its direct vertex is a light; Path::Connect, :245-275) need no further ray
-// and are evaluated here; the s, t >= 1 connections are counted and given a
-// contiguous range of work items.  t = 0 strategies carry no weight with a
-// pinhole sensor (its position cannot be hit and EvaluateCst is 0).
+// Per sample: its work items are counted, in total and per strategy bucket
+// (the s = 0 strategies, where the eye subpath reaches a light or its direct
+// vertex is one, and the s, t >= 1 connections), and its own-pixel
+// accumulator is cleared.  t = 0 strategies carry no weight with a pinhole
+// sensor (its position cannot be hit and EvaluateCst is 0).
 __global__ void __launch_bounds__(kBdptThreads) k_bd_count(Ctx C, Wave w, uint32_t* __restrict__ hist,
-                                                           uint32_t* __restrict__ total,
-                                                           double* __restrict__ film_x,
-                                                           double* __restrict__ film_x_sq)
+                                                           uint32_t* __restrict__ total)
 {
     __shared__ uint32_t s_hist[kBuckets];
     for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) s_hist[k] = 0u;
@@ -448,36 +462,10 @@ __global__ void __launch_bounds__(kBdptThreads) k_bd_count(Ctx C, Wave w, uint32
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t cnt = 0;
     const int nL = i < w.n ? w.count[0][i] : 0, nE = i < w.n ? w.count[1][i] : 0;
+    const int t0 = t_limit_s0(nE, C.max_path);
     if (i < w.n) {
-        cnt = (uint32_t)num_connections(nL, nE, C.max_path);
-        const uint32_t own_pix = (uint32_t)((w.p0 + i) % w.npix);
-        float own[3] = {0.0f, 0.0f, 0.0f};
-        PV P[kMaxV];
-        for (int t = 2; t <= nE; t++) {
-            if (C.max_path >= 0 && t > C.max_path) break;
-            const BVtx last = w.sv[1][(size_t)(t - 1) * w.stride + i];
-            for (int d = 0; d < 2; d++) {
-                if (d == 0) {
-                    if (!(flags_of(last) & F_SV)) continue;
-                    P[0] = unpack(last);
-                    if (P[0].prim < 0 || !C.sc.prims[P[0].prim].is_light) continue;
-                } else {
-                    if (!(flags_of(last) & F_DIRECT)) continue;
-                    P[0] = unpack(w.dv[1][(size_t)(t - 1) * w.stride + i]);
-                }
-                P[0].type = T_L;
-                for (int q = 1; q < t; q++) P[q] = unpack(w.sv[1][(size_t)(t - 1 - q) * w.stride + i]);
-                float c[3];
-                if (!path_contribution(C, P, t, 0, d != 0, c)) continue;
-                const uint32_t pix = raster_pixel(C, P, t);
-                if (pix == own_pix) {
-                    for (int k = 0; k < 3; k++) own[k] += c[k];
-                } else {
-                    splat_px(film_x, film_x_sq, pix, c);
-                }
-            }
-        }
-        for (int k = 0; k < 3; k++) w.own[3 * (size_t)i + k] = own[k];
+        cnt = (uint32_t)(num_connections(nL, nE, C.max_path) + 2 * (t0 > 1 ? t0 - 1 : 0));
+        for (int k = 0; k < 3; k++) w.own[3 * (size_t)i + k] = 0.0f;
     }
     // item total, and the items per strategy (s, t) for the buckets
     const unsigned lane = threadIdx.x & 31u;
@@ -490,6 +478,14 @@ __global__ void __launch_bounds__(kBdptThreads) k_bd_count(Ctx C, Wave w, uint32
         for (int t = 1; t <= tw; t++) {
             const unsigned m = __ballot_sync(0xffffffffu, t <= tm);
             if (lane == 0u) atomicAdd(&s_hist[sl * kStrideST + t], (uint32_t)__popc(m));
+        }
+    }
+    const int t0w = __reduce_max_sync(0xffffffffu, t0);
+    for (int t = 2; t <= t0w; t++) {
+        const unsigned m = __ballot_sync(0xffffffffu, t <= t0);
+        if (lane == 0u) {
+            atomicAdd(&s_hist[bucket_s0(t, 0)], (uint32_t)__popc(m));
+            atomicAdd(&s_hist[bucket_s0(t, 1)], (uint32_t)__popc(m));
         }
     }
     __syncthreads();
@@ -509,9 +505,11 @@ __global__ void k_bd_buckets(uint32_t* __restrict__ hist, uint32_t* __restrict__
     }
 }
 
-// Work items of the s, t >= 1 connections, sample | s << 20 | t << 26,
-// scattered into their strategy's bucket so that a warp of k_bd_connect
-// evaluates one strategy (same path length, same MIS loops) at a time.
+// Work items, scattered into their strategy's bucket so that a warp of
+// k_bd_connect evaluates one strategy (same path length, same MIS loops) at
+// a time: the s, t >= 1 connections as sample | s << 20 | t << 26, and the
+// s = 0 strategies (Path::Connect, :245-275; no visibility ray: the eye
+// subpath's own rays found the light) as sample | d << 19 | t << 26.
 __global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ offset, uint32_t* __restrict__ cursor,
                            uint32_t* __restrict__ items)
 {
@@ -532,6 +530,20 @@ __global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ offset, u
             if (has) items[offset[b] + base + __popc(m & ((1u << lane) - 1u))] = i | ((uint32_t)s << 20) | ((uint32_t)t << 26);
         }
     }
+    // s = 0: i | d << 19 | t << 26
+    const int t0 = t_limit_s0(nE, C.max_path);
+    const int t0w = __reduce_max_sync(0xffffffffu, t0);
+    for (int t = 2; t <= t0w; t++) {
+        const bool has = t <= t0;
+        const unsigned m = __ballot_sync(0xffffffffu, has);
+        for (int d = 0; d < 2; d++) {
+            const int b = bucket_s0(t, d);
+            uint32_t base = 0;
+            if (lane == (unsigned)(__ffs(m) - 1)) base = atomicAdd(&cursor[b], (uint32_t)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+            if (has) items[offset[b] + base + __popc(m & ((1u << lane) - 1u))] = i | ((uint32_t)d << 19) | ((uint32_t)t << 26);
+        }
+    }
 }
 
 // One connection (Path::Connect, :298-330): the full path L[0..s-1] E[t-1..0],
@@ -543,12 +555,36 @@ __global__ void __launch_bounds__(kBdptThreads) k_bd_connect(Ctx C, Wave w, cons
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n_items) return;
     const uint32_t it = items[q];
-    const uint32_t i = it & 0xfffffu;
+    const uint32_t i = it & kSampleMask;
     const int s = (int)((it >> 20) & 0x3fu), t = (int)(it >> 26);
-    const BVtx lend = w.sv[0][(size_t)(s - 1) * w.stride + i], eend = w.sv[1][(size_t)(t - 1) * w.stride + i];
     float c[3] = {0.0f, 0.0f, 0.0f};
-    bool ok = (flags_of(lend) & F_SV) && (flags_of(eend) & F_SV);
     PV P[2 * kMaxV];
+    if (s == 0) {
+        // the eye subpath ends on a light (d = 0) or its direct vertex is one
+        const int d = (int)((it >> 19) & 1u);
+        const BVtx last = w.sv[1][(size_t)(t - 1) * w.stride + i];
+        bool ok0 = false;
+        if (d == 0) {
+            if (flags_of(last) & F_SV) {
+                P[0] = unpack(last);
+                ok0 = P[0].prim >= 0 && C.sc.prims[P[0].prim].is_light;
+            }
+        } else if (flags_of(last) & F_DIRECT) {
+            P[0] = unpack(w.dv[1][(size_t)(t - 1) * w.stride + i]);
+            ok0 = true;
+        }
+        if (ok0) {
+            P[0].type = T_L;
+            for (int k = 1; k < t; k++) P[k] = unpack(w.sv[1][(size_t)(t - 1 - k) * w.stride + i]);
+            ok0 = path_contribution(C, P, t, 0, d != 0, c);
+        }
+        store_null_ray(rays, q);  // visibility known already: the splat sees a miss
+        rec[q] = ok0 ? make_float4(c[0], c[1], c[2], __uint_as_float(raster_pixel(C, P, t)))
+                     : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    const BVtx lend = w.sv[0][(size_t)(s - 1) * w.stride + i], eend = w.sv[1][(size_t)(t - 1) * w.stride + i];
+    bool ok = (flags_of(lend) & F_SV) && (flags_of(eend) & F_SV);
     const int n = s + t;
     if (ok) {
         for (int k = 0; k < s; k++) P[k] = unpack(w.sv[0][(size_t)k * w.stride + i]);
@@ -572,7 +608,7 @@ __global__ void k_bd_splat(Wave w, const uint32_t* __restrict__ items, uint32_t 
     if (q >= n_items) return;
     const float4 r = rec[q];
     if ((r.x == 0.0f && r.y == 0.0f && r.z == 0.0f) || hits[q].prim >= 0) return;
-    const uint32_t i = items[q] & 0xfffffu;
+    const uint32_t i = items[q] & kSampleMask;
     const uint32_t pix = __float_as_uint(r.w);
     const float c[3] = {r.x, r.y, r.z};
     if (pix == (uint32_t)((w.p0 + i) % w.npix)) {
@@ -757,8 +793,7 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
         // connections
         LMGPU_CUDA_TRY(cudaMemsetAsync(B.counter, 0, sizeof(uint32_t), stream));
         LMGPU_CUDA_TRY(cudaMemsetAsync(B.buckets, 0, sizeof(uint32_t) * kBuckets, stream));
-        k_bd_count<<<blocks(w.n, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.buckets, B.counter, sc->film_x,
-                                                                         sc->film_x_sq);
+        k_bd_count<<<blocks(w.n, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.buckets, B.counter);
         LMGPU_CUDA_TRY(cudaGetLastError());
         uint32_t n_items = 0;
         if ((rc = read_counter(n_items))) return rc;
