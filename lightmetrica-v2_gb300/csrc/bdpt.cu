@@ -256,17 +256,34 @@ __device__ __forceinline__ void store_shadow_ray(float4* rays, uint32_t q, float
 // The rays of step k from vertex v (Subpath::Sample, renderer_bdpt.cpp:130-200):
 // the extension ray along wo (null if the direction was not sampled or its
 // BSDF value is black) and the ray to the direct endpoint, drawn with step
-// k's random numbers; the endpoint is kept in pend[slot].
+// k's random numbers; the endpoint is kept in pend[slot], flagged F_DIRECT
+// when its visibility is traced.  Visibility is traced only where the
+// endpoint can contribute:
+//   * light subpaths: the direct endpoint is the pinhole, used only by the
+//     t = 0 strategies, which carry no weight (delta sensor position), so no
+//     ray is traced;
+//   * eye subpaths: not when the sampled light point faces away from v (its
+//     emission towards v is zero, light_area.cpp EvaluateDirection) or v's
+//     BSDF is a delta or null one (zero under evalDelta), where the (s = 0,
+//     direct) strategy's contribution is zero whatever the visibility.
 __device__ __forceinline__ void emit_step(const Ctx& C, const Wave& w, int dir, uint32_t slot, const PV& v, bool has_wo,
                                           float3 wo, const StepRand& r, uint32_t q, float4* ext, float4* sh)
 {
     if (has_wo) store_ray(ext, q, v.p, 1e-4f, wo, FLT_MAX);
     else store_null_ray(ext, q);
     PV e;
-    if (dir == DIR_LE) sensor_vertex(C, e);
-    else sample_light(C, r.us, r.a0, r.a1, e);
-    store_shadow_ray(sh, q, v.p, e.p);
-    w.pend[slot] = pack(e, 0u);
+    bool trace = false;
+    if (dir == DIR_LE) {
+        sensor_vertex(C, e);
+    } else {
+        sample_light(C, r.us, r.a0, r.a1, e);
+        const bool front = dot3(v.p - e.p, e.n) > 0.0f;
+        const bool conn = (v.type & T_E) || (v.type != 0 && !delta_dir(C, v, v.type));
+        trace = front && conn;
+    }
+    if (trace) store_shadow_ray(sh, q, v.p, e.p);
+    else store_null_ray(sh, q);
+    w.pend[slot] = pack(e, trace ? F_DIRECT : 0u);
 }
 
 __global__ void __launch_bounds__(kBdptThreads) k_bd_start(Ctx C, Wave w, float4* __restrict__ ext,
@@ -329,7 +346,8 @@ __global__ void __launch_bounds__(kBdptThreads) k_bd_step(Ctx C, Wave w, int k, 
         const int n = w.count[dir][i];
         const lmgpu_hit he = ext_hit[q];
         const bool has_sv = he.prim >= 0;
-        const bool has_direct = sh_hit[q].prim < 0;
+        // a traced direct endpoint, and visible
+        const bool has_direct = (flags_of(w.pend[j]) & F_DIRECT) && sh_hit[q].prim < 0;
         if (has_sv) {
             const float4 r0 = ext_in[2 * q], r1 = ext_in[2 * q + 1];
             const float* T = C.sc.tris + 9 * (size_t)he.prim;
