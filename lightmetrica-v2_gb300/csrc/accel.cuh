@@ -67,6 +67,11 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
 int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, uint64_t n, bool anyhit,
                  bool stats, cudaStream_t stream);
 
+// As launch_trace with the ray count read from d_n on the device (at most
+// max_n), so that launches need no host round trip.
+int launch_trace_dn(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, const uint32_t* d_n,
+                    uint64_t max_n, bool anyhit, cudaStream_t stream);
+
 // Blocks of the persistent traversal grid (SMs x resident blocks); looked up
 // once per process.  Negative on a CUDA error.
 int trace_grid_cap();

@@ -25,7 +25,8 @@
 //   k_lt_generate   the light vertex: its sensor connection (a shadow ray and
 //                   a pending splat) and the first extension ray
 //   per bounce      k_trace (closest hit) over the compacted path queue, any
-//                   hit over the pending connections and k_lt_splat, then
+//                   hit over the pending connections and k_lt_splat (queue
+//                   lengths read on the device, no host round trip), then
 //                   k_lt_shade: roulette, the vertex's sensor connection,
 //                   BSDF sampling, warp-aggregated append
 #include "accel.cuh"
@@ -126,14 +127,16 @@ __global__ void __launch_bounds__(kLtThreads) k_lt_generate(Ctx C, uint64_t p0, 
 
 __global__ void __launch_bounds__(kLtThreads) k_lt_shade(Ctx C, const float4* __restrict__ rays,
                                                          const PathState* __restrict__ state,
-                                                         const lmgpu_hit* __restrict__ hits, uint32_t n,
-                                                         uint64_t p0, uint32_t seed, float4* __restrict__ out_rays,
+                                                         const lmgpu_hit* __restrict__ hits,
+                                                         const uint32_t* __restrict__ d_n, uint64_t p0,
+                                                         uint32_t seed, float4* __restrict__ out_rays,
                                                          PathState* __restrict__ out_state,
                                                          uint32_t* __restrict__ out_count, float4* __restrict__ nrays,
                                                          float4* __restrict__ nrec, uint32_t* __restrict__ npath,
                                                          uint32_t* __restrict__ ncount)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = *d_n;  // queue length, written by the previous kernel
     bool keep = false, has_nee = false;
     PV v, E;
     float c[3] = {0.0f, 0.0f, 0.0f};
@@ -182,11 +185,12 @@ __global__ void __launch_bounds__(kLtThreads) k_lt_shade(Ctx C, const float4* __
 }
 
 // Unoccluded sensor connections into the film of other samples' splats.
-__global__ void k_lt_splat(uint32_t n, const float4* __restrict__ rec, const lmgpu_hit* __restrict__ hits,
-                           double* __restrict__ film_x, double* __restrict__ film_x_sq)
+__global__ void k_lt_splat(const uint32_t* __restrict__ d_n, const float4* __restrict__ rec,
+                           const lmgpu_hit* __restrict__ hits, double* __restrict__ film_x,
+                           double* __restrict__ film_x_sq)
 {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n || hits[q].prim >= 0) return;
+    if (q >= *d_n || hits[q].prim >= 0) return;
     const float4 r = rec[q];
     const size_t pix = __float_as_uint(r.w);
     const float c[3] = {r.x, r.y, r.z};
@@ -225,44 +229,51 @@ int render_ltdirect(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image,
     C.cam = sc->cam;
     C.max_v = 0;
     C.max_path = prm->max_num_vertices;
+    // Queue lengths on the device (q_count: [0], [1] path queues, [2]
+    // pending sensor connections): a wave's bounces are queued without host
+    // round trips; with max_num_vertices bounded the queue is empty after
+    // max_num_vertices - 1 bounces, otherwise the host checks every
+    // kCheckEvery bounces.
+    constexpr int kCheckEvery = 8;
+    constexpr int kMaxBounces = 1 << 16;
+    const bool bounded = prm->max_num_vertices >= 0;
+    const int maxb = bounded ? (prm->max_num_vertices > 1 ? prm->max_num_vertices - 1 : 0) : kMaxBounces;
+    uint32_t* cnt = sc->q_count;
     for (uint64_t p0 = 0; p0 < total; p0 += kLtWave) {
-        uint32_t n = (uint32_t)((total - p0) < kLtWave ? (total - p0) : kLtWave);
-        LMGPU_CUDA_TRY(cudaMemsetAsync(sc->q_count, 0, 2 * sizeof(uint32_t), stream));
-        k_lt_generate<<<(n + kLtThreads - 1) / kLtThreads, kLtThreads, 0, stream>>>(
-            C, p0, n, prm->seed, sc->q_ray[0], sc->q_state[0], sc->q_count, sc->q_nray, sc->q_nrec, sc->q_npath,
-            sc->q_count + 1);
+        const uint32_t n_wave = (uint32_t)((total - p0) < kLtWave ? (total - p0) : kLtWave);
+        const unsigned gblocks = (n_wave + kLtThreads - 1) / kLtThreads;
+        LMGPU_CUDA_TRY(cudaMemsetAsync(cnt, 0, 4 * sizeof(uint32_t), stream));
+        k_lt_generate<<<gblocks, kLtThreads, 0, stream>>>(C, p0, n_wave, prm->seed, sc->q_ray[0], sc->q_state[0],
+                                                          cnt, sc->q_nray, sc->q_nrec, sc->q_npath, cnt + 2);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
         int cur = 0;
-        LMGPU_CUDA_TRY(
-            cudaMemcpyAsync(sc->h_count, sc->q_count, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-        LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
-        n = sc->h_count[0];
-        uint32_t n_nee = sc->h_count[1];
-        while (n > 0 || n_nee > 0) {
-            if (n_nee > 0) {
-                rc = launch_trace(sc->accel, sc->q_nray, sc->q_nhit, n_nee, true, false, stream);
-                if (rc) return rc;
-                k_lt_splat<<<(n_nee + 255) / 256, 256, 0, stream>>>(n_nee, sc->q_nrec, sc->q_nhit, sc->film_x,
-                                                                    sc->film_x_sq);
-                LMGPU_CUDA_TRY(cudaGetLastError());
-                sc->launches += 2;
-            }
-            if (n == 0) break;
-            rc = launch_trace(sc->accel, sc->q_ray[cur], sc->q_hit, n, false, false, stream);
+        for (int b = 0;; b++) {
+            // the sensor connections of the previous kernel
+            rc = launch_trace_dn(sc->accel, sc->q_nray, sc->q_nhit, cnt + 2, n_wave, true, stream);
             if (rc) return rc;
-            LMGPU_CUDA_TRY(cudaMemsetAsync(sc->q_count, 0, 2 * sizeof(uint32_t), stream));
-            k_lt_shade<<<(n + kLtThreads - 1) / kLtThreads, kLtThreads, 0, stream>>>(
-                C, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, n, p0, prm->seed, sc->q_ray[1 - cur],
-                sc->q_state[1 - cur], sc->q_count, sc->q_nray, sc->q_nrec, sc->q_npath, sc->q_count + 1);
+            k_lt_splat<<<gblocks, kLtThreads, 0, stream>>>(cnt + 2, sc->q_nrec, sc->q_nhit, sc->film_x,
+                                                           sc->film_x_sq);
             LMGPU_CUDA_TRY(cudaGetLastError());
             sc->launches += 2;
-            LMGPU_CUDA_TRY(
-                cudaMemcpyAsync(sc->h_count, sc->q_count, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-            LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
-            n = sc->h_count[0];
-            n_nee = sc->h_count[1];
+            if (b >= maxb) break;
+            rc = launch_trace_dn(sc->accel, sc->q_ray[cur], sc->q_hit, cnt + cur, n_wave, false, stream);
+            if (rc) return rc;
+            LMGPU_CUDA_TRY(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(uint32_t), stream));
+            LMGPU_CUDA_TRY(cudaMemsetAsync(cnt + 2, 0, sizeof(uint32_t), stream));
+            k_lt_shade<<<gblocks, kLtThreads, 0, stream>>>(C, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, cnt + cur,
+                                                           p0, prm->seed, sc->q_ray[1 - cur], sc->q_state[1 - cur],
+                                                           cnt + (1 - cur), sc->q_nray, sc->q_nrec, sc->q_npath,
+                                                           cnt + 2);
+            LMGPU_CUDA_TRY(cudaGetLastError());
+            sc->launches += 2;
             cur = 1 - cur;
+            if (!bounded && (b + 1) % kCheckEvery == 0) {
+                LMGPU_CUDA_TRY(
+                    cudaMemcpyAsync(sc->h_count, cnt, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+                LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+                if (sc->h_count[cur] == 0 && sc->h_count[2] == 0) break;
+            }
         }
     }
     // every splat is another sample's: n_x = all light paths

@@ -26,7 +26,8 @@
 // GPU structure, one wave of up to kWave paths at a time:
 //   k_pt_generate   camera rays for paths [p0, p0 + n) (sensor_pinhole.cpp:79-90);
 //                   ptmis: the sensor's light sample
-//   per bounce      k_trace (closest hit, trace.cu) over the compacted queue;
+//   per bounce      k_trace (closest hit, trace.cu) over the compacted queue,
+//                   its length read on the device (no host round trip);
 //                   k_pt_shade: emission (MIS-weighted for ptmis), roulette,
 //                   BSDF sampling, warp-aggregated append of surviving paths;
 //                   ptmis: the new vertex's light sample as a shadow ray plus
@@ -95,6 +96,7 @@ template <int MODE>
 __global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p0, uint32_t n, uint32_t seed,
                                                                float4* __restrict__ rays,
                                                                PathState* __restrict__ state,
+                                                               uint32_t* __restrict__ count,
                                                                float* __restrict__ own, float4* __restrict__ nrays,
                                                                float4* __restrict__ nrec,
                                                                uint32_t* __restrict__ npath,
@@ -102,6 +104,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p
 {
     constexpr bool NEE = MODE != MODE_PT;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *count = n;  // every path of the wave starts in the queue
     const CameraGPU& cam = C.cam;
     bool has_nee = false;
     PV v, L;
@@ -147,8 +150,9 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p
 template <int MODE>
 __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(Ctx C, const float4* __restrict__ rays,
                                                             const PathState* __restrict__ state,
-                                                            const lmgpu_hit* __restrict__ hits, uint32_t n,
-                                                            uint64_t p0, uint32_t seed, float* __restrict__ own,
+                                                            const lmgpu_hit* __restrict__ hits,
+                                                            const uint32_t* __restrict__ d_n, uint64_t p0,
+                                                            uint32_t seed, float* __restrict__ own,
                                                             float4* __restrict__ out_rays,
                                                             PathState* __restrict__ out_state,
                                                             uint32_t* __restrict__ out_count,
@@ -158,6 +162,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(Ctx C, const float4*
 {
     constexpr bool NEE = MODE != MODE_PT;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = *d_n;  // queue length, written by the previous kernel
     bool keep = false, has_nee = false;
     float4 nr0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), nr1 = nr0;
     PathState ns;
@@ -274,12 +279,13 @@ __device__ __forceinline__ void splat_px(double* film, double* film_sq, uint32_t
 
 // Unoccluded light samples: into the path's own-pixel sum, or (the sensor's
 // light samples that land elsewhere) into the film of other samples' splats.
-__global__ void k_pt_nee_splat(uint64_t p0, uint32_t npix, uint32_t n, const float4* __restrict__ rec,
-                               const uint32_t* __restrict__ rec_path, const lmgpu_hit* __restrict__ hits,
-                               float* __restrict__ own, double* __restrict__ film_x, double* __restrict__ film_x_sq)
+__global__ void k_pt_nee_splat(uint64_t p0, uint32_t npix, const uint32_t* __restrict__ d_n,
+                               const float4* __restrict__ rec, const uint32_t* __restrict__ rec_path,
+                               const lmgpu_hit* __restrict__ hits, float* __restrict__ own,
+                               double* __restrict__ film_x, double* __restrict__ film_x_sq)
 {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n || hits[q].prim >= 0) return;
+    if (q >= *d_n || hits[q].prim >= 0) return;
     const float4 r = rec[q];
     const uint32_t path = rec_path[q];
     const uint32_t pix = __float_as_uint(r.w);
@@ -330,58 +336,60 @@ int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float
     C.max_v = 0;
     C.max_path = prm->max_num_vertices;
     const uint32_t np = (uint32_t)npix;
+    // Queue lengths live on the device (q_count: [0], [1] path queues, [2]
+    // pending light samples), so a wave's bounces are queued without host
+    // round trips.  With max_num_vertices bounded, the queue is empty after
+    // max_num_vertices - 1 bounces; otherwise the host checks every
+    // kCheckEvery bounces.
+    constexpr int kCheckEvery = 8;
+    constexpr int kMaxBounces = 1 << 16;
+    const bool bounded = prm->max_num_vertices >= 0;
+    const int maxb = bounded ? (prm->max_num_vertices > 1 ? prm->max_num_vertices - 1 : 0) : kMaxBounces;
+    auto gen = mode == MODE_PTMIS ? k_pt_generate<MODE_PTMIS>
+                                  : (mode == MODE_PTDIRECT ? k_pt_generate<MODE_PTDIRECT> : k_pt_generate<MODE_PT>);
+    auto shade = mode == MODE_PTMIS ? k_pt_shade<MODE_PTMIS>
+                                    : (mode == MODE_PTDIRECT ? k_pt_shade<MODE_PTDIRECT> : k_pt_shade<MODE_PT>);
+    uint32_t* cnt = sc->q_count;
     for (uint64_t p0 = 0; p0 < total; p0 += kWave) {
-        uint32_t n = (uint32_t)((total - p0) < kWave ? (total - p0) : kWave);
-        const uint32_t n_wave = n;
-        LMGPU_CUDA_TRY(cudaMemsetAsync(sc->q_count, 0, 2 * sizeof(uint32_t), stream));
-        {
-            auto gen = mode == MODE_PTMIS ? k_pt_generate<MODE_PTMIS>
-                                          : (mode == MODE_PTDIRECT ? k_pt_generate<MODE_PTDIRECT> : k_pt_generate<MODE_PT>);
-            gen<<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
-                C, p0, n, prm->seed, sc->q_ray[0], sc->q_state[0], sc->q_own, sc->q_nray, sc->q_nrec, sc->q_npath,
-                sc->q_count + 1);
-        }
+        const uint32_t n_wave = (uint32_t)((total - p0) < kWave ? (total - p0) : kWave);
+        const unsigned gblocks = (n_wave + kShadeThreads - 1) / kShadeThreads;
+        LMGPU_CUDA_TRY(cudaMemsetAsync(cnt, 0, 4 * sizeof(uint32_t), stream));
+        gen<<<gblocks, kShadeThreads, 0, stream>>>(C, p0, n_wave, prm->seed, sc->q_ray[0], sc->q_state[0], cnt,
+                                                   sc->q_own, sc->q_nray, sc->q_nrec, sc->q_npath, cnt + 2);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
         int cur = 0;
-        uint32_t n_nee = 0;
-        if (nee) {
-            LMGPU_CUDA_TRY(cudaMemcpyAsync(sc->h_count, sc->q_count, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                                           stream));
-            LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
-            n_nee = sc->h_count[1];
-        }
-        while (n > 0 || n_nee > 0) {
-            if (n_nee > 0) {
-                rc = launch_trace(sc->accel, sc->q_nray, sc->q_nhit, n_nee, true, false, stream);
+        for (int b = 0;; b++) {
+            if (nee) {
+                // the light samples of the previous kernel
+                rc = launch_trace_dn(sc->accel, sc->q_nray, sc->q_nhit, cnt + 2, n_wave, true, stream);
                 if (rc) return rc;
-                k_pt_nee_splat<<<(n_nee + 255) / 256, 256, 0, stream>>>(p0, np, n_nee, sc->q_nrec, sc->q_npath,
-                                                                        sc->q_nhit, sc->q_own, sc->film_x,
-                                                                        sc->film_x_sq);
+                k_pt_nee_splat<<<gblocks, kShadeThreads, 0, stream>>>(p0, np, cnt + 2, sc->q_nrec, sc->q_npath,
+                                                                      sc->q_nhit, sc->q_own, sc->film_x,
+                                                                      sc->film_x_sq);
                 LMGPU_CUDA_TRY(cudaGetLastError());
                 sc->launches += 2;
             }
-            if (n == 0) break;
-            rc = launch_trace(sc->accel, sc->q_ray[cur], sc->q_hit, n, false, false, stream);
+            if (b >= maxb) break;
+            rc = launch_trace_dn(sc->accel, sc->q_ray[cur], sc->q_hit, cnt + cur, n_wave, false, stream);
             if (rc) return rc;
-            LMGPU_CUDA_TRY(cudaMemsetAsync(sc->q_count, 0, 2 * sizeof(uint32_t), stream));
-            {
-                auto shade = mode == MODE_PTMIS ? k_pt_shade<MODE_PTMIS>
-                                                : (mode == MODE_PTDIRECT ? k_pt_shade<MODE_PTDIRECT> : k_pt_shade<MODE_PT>);
-                shade<<<(n + kShadeThreads - 1) / kShadeThreads, kShadeThreads, 0, stream>>>(
-                    C, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, n, p0, prm->seed, sc->q_own, sc->q_ray[1 - cur],
-                    sc->q_state[1 - cur], sc->q_count, sc->q_nray, sc->q_nrec, sc->q_npath, sc->q_count + 1);
-            }
+            LMGPU_CUDA_TRY(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(uint32_t), stream));
+            LMGPU_CUDA_TRY(cudaMemsetAsync(cnt + 2, 0, sizeof(uint32_t), stream));
+            shade<<<gblocks, kShadeThreads, 0, stream>>>(C, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, cnt + cur,
+                                                         p0, prm->seed, sc->q_own, sc->q_ray[1 - cur],
+                                                         sc->q_state[1 - cur], cnt + (1 - cur), sc->q_nray,
+                                                         sc->q_nrec, sc->q_npath, cnt + 2);
             LMGPU_CUDA_TRY(cudaGetLastError());
             sc->launches += 2;  // trace + shade
-            LMGPU_CUDA_TRY(cudaMemcpyAsync(sc->h_count, sc->q_count, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                                           stream));
-            LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
-            n = sc->h_count[0];
-            n_nee = nee ? sc->h_count[1] : 0u;
             cur = 1 - cur;
+            if (!bounded && (b + 1) % kCheckEvery == 0) {
+                LMGPU_CUDA_TRY(
+                    cudaMemcpyAsync(sc->h_count, cnt, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+                LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+                if (sc->h_count[cur] == 0 && sc->h_count[2] == 0) break;
+            }
         }
-        k_pt_flush<<<(n_wave + 255) / 256, 256, 0, stream>>>(p0, np, n_wave, sc->q_own, sc->film, sc->film_sq);
+        k_pt_flush<<<gblocks, kShadeThreads, 0, stream>>>(p0, np, n_wave, sc->q_own, sc->film, sc->film_sq);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
     }

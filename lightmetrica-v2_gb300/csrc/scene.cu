@@ -231,8 +231,8 @@ int lmgpu_scene_create(const float* tris, const int32_t* tri_prim, uint64_t ntri
     int rc = lmgpu_accel_create(&sc->accel);
     if (rc) return fail(rc);
     if (cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMallocHost((void**)&sc->h_count, 2 * sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc((void**)&sc->q_count, 2 * sizeof(uint32_t)) != cudaSuccess) {
+        cudaMallocHost((void**)&sc->h_count, 4 * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc((void**)&sc->q_count, 4 * sizeof(uint32_t)) != cudaSuccess) {
         set_error("lmgpu_scene_create: stream or buffer allocation failed");
         return fail(LMGPU_ERR_CUDA);
     }

@@ -101,8 +101,8 @@ struct lmgpu_scene {
     float4* q_ray[2] = {nullptr, nullptr};
     lmgpu::PathState* q_state[2] = {nullptr, nullptr};
     lmgpu_hit* q_hit = nullptr;
-    uint32_t* q_count = nullptr;  // [0] next path queue, [1] light-sample queue
-    uint32_t* h_count = nullptr;  // pinned host copy of both
+    uint32_t* q_count = nullptr;  // [0], [1] the two path queues' lengths, [2] light-sample queue, [3] spare
+    uint32_t* h_count = nullptr;  // pinned host copy
     float* q_own = nullptr;       // [3 path] each path's contributions to its own pixel
     // pending light samples (renderer::ptmis): shadow rays, contributions + pixel, path, hits
     float4* q_nray = nullptr;

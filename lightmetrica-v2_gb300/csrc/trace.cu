@@ -273,6 +273,23 @@ int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, 
     return LMGPU_OK;
 }
 
+int launch_trace_dn(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, const uint32_t* d_n,
+                    uint64_t max_n, bool anyhit, cudaStream_t stream)
+{
+    if (max_n == 0) return LMGPU_OK;
+    const int grid_cap = anyhit ? grid_cap_of<true, false, false>() : grid_cap_of<false, false, false>();
+    if (grid_cap <= 0) return LMGPU_ERR_CUDA;
+    const uint64_t by_rays = (max_n + 4 * kTraceThreads - 1) / (4 * kTraceThreads);
+    const unsigned grid = (unsigned)(by_rays < (uint64_t)grid_cap ? by_rays : (uint64_t)grid_cap);
+    const uint32_t nn = a->ntri > 0 ? (uint32_t)a->num_wide : 0u;
+    const uint32_t nt = (uint32_t)a->ntri;
+    auto k = anyhit ? k_trace<true, false, false> : k_trace<false, false, false>;
+    k<<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, max_n, nn, nt, a->tune.refill,
+                                          a->tune.postpone, a->status, nullptr, nullptr, 0u, nullptr, d_n);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+    return LMGPU_OK;
+}
+
 int launch_trace_multi(const AccelView* d_tab, uint32_t ntab, const float4* d_rays, const uint8_t* d_ray_scene,
                        lmgpu_hit* d_hits, const uint32_t* d_n, uint64_t max_n, bool anyhit, TraceConfig cfg,
                        uint32_t* d_status, cudaStream_t stream)
