@@ -161,10 +161,12 @@ __device__ __forceinline__ void block_sync_for_mma()
 template <int MODE>
 __global__ void __launch_bounds__(kThreads, 1) k_guide_fwd(const float* __restrict__ params, Box box,
                                                            const float* __restrict__ queries, uint32_t n,
+                                                           const uint32_t* __restrict__ d_n,
                                                            float* __restrict__ raw_out,
                                                            __nv_bfloat16* __restrict__ acts,
                                                            uint32_t* __restrict__ status)
 {
+    if (d_n) n = *d_n;  // query count on the device (at most the n launched for)
     extern __shared__ __align__(1024) unsigned char smem[];
     float* sbias = reinterpret_cast<float*>(smem + kFwdBias);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kFwdBar);
@@ -475,7 +477,22 @@ int guide_forward_device(lmgpu_guide* g, const float* d_queries, uint64_t n, flo
     int rc = guide_grid(g);
     if (rc) return rc;
     k_guide_fwd<MODE_RAW><<<tiles_grid(g, n), kThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
-                                                                      d_raw, nullptr, g->status);
+                                                                      nullptr, d_raw, nullptr, g->status);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+    return LMGPU_OK;
+}
+
+// As guide_forward_device with the query count read from d_n on the device
+// (at most max_n), so the launch needs no host round trip.
+int guide_forward_device_dn(lmgpu_guide* g, const float* d_queries, const uint32_t* d_n, uint64_t max_n,
+                            float* d_raw, cudaStream_t s)
+{
+    if (max_n == 0) return LMGPU_OK;
+    int rc = guide_grid(g);
+    if (rc) return rc;
+    k_guide_fwd<MODE_RAW><<<tiles_grid(g, max_n), kThreads, kFwdSmem, s>>>(g->params, g->box, d_queries,
+                                                                          (uint32_t)max_n, d_n, d_raw, nullptr,
+                                                                          g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
     return LMGPU_OK;
 }
@@ -489,7 +506,7 @@ int guide_gradient_device(lmgpu_guide* g, const float* d_queries, const float* d
     int rc = guide_grid(g);
     if (rc || (rc = ensure_scratch(g, n))) return rc;
     k_guide_fwd<MODE_TRAIN><<<tiles_grid(g, n), kThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
-                                                                        g->d_raw, g->d_acts, g->status);
+                                                                        nullptr, g->d_raw, g->d_acts, g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
     k_guide_bwd<<<tiles_grid(g, n), kThreads, kBwdSmem, s>>>(g->params, g->d_raw, g->d_acts, d_dirs, d_weights,
                                                              (uint32_t)n, 1.0f / (float)n, g->grad, g->loss,

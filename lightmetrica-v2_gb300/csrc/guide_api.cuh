@@ -11,6 +11,9 @@ namespace lmgpu {
 
 // Raw outputs (float[40] per query) of n device queries (float[9] each).
 int guide_forward_device(lmgpu_guide* g, const float* d_queries, uint64_t n, float* d_raw, cudaStream_t s);
+// As guide_forward_device with the query count on the device (at most max_n).
+int guide_forward_device_dn(lmgpu_guide* g, const float* d_queries, const uint32_t* d_n, uint64_t max_n,
+                            float* d_raw, cudaStream_t s);
 
 // Forward + backward of the mean loss of n device samples into the
 // network's gradient; the loss is added to the network's loss word.

@@ -65,9 +65,11 @@ struct Wave {
 __device__ __forceinline__ float lum(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
 
 __global__ void __launch_bounds__(kGdThreads) k_gd_generate(CameraGPU cam, Wave w, uint32_t seed,
-                                                            float4* __restrict__ rays, PathState* __restrict__ state)
+                                                            float4* __restrict__ rays, PathState* __restrict__ state,
+                                                            uint32_t* __restrict__ count)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *count = w.n;  // every path of the wave starts in the queue
     if (i >= w.n) return;
     const uint64_t p = w.p0 + i;
     const uint32_t pixel = (uint32_t)(p % w.npix);
@@ -104,14 +106,17 @@ __device__ __forceinline__ uint32_t append_slot(bool take, uint32_t* count)
 __global__ void __launch_bounds__(kGdThreads) k_gd_shade(SceneGPU sc, Wave w, int max_nv, uint32_t seed, int rr_mode,
                                                          const float4* __restrict__ rays,
                                                          const PathState* __restrict__ state,
-                                                         const lmgpu_hit* __restrict__ hits, uint32_t n,
+                                                         const lmgpu_hit* __restrict__ hits,
+                                                         const uint32_t* __restrict__ d_n,
                                                          float4* __restrict__ out_rays,
                                                          PathState* __restrict__ out_state,
+                                                         uint32_t* __restrict__ out_count,
                                                          float* __restrict__ queries,
                                                          PathState* __restrict__ q_state,
-                                                         int32_t* __restrict__ q_prim, uint32_t* __restrict__ counts)
+                                                         int32_t* __restrict__ q_prim, uint32_t* __restrict__ q_count)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = *d_n;  // queue length, written by the previous kernels
     bool keep = false, query = false;
     float4 nr0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), nr1 = nr0;
     PathState ns;
@@ -198,13 +203,13 @@ __global__ void __launch_bounds__(kGdThreads) k_gd_shade(SceneGPU sc, Wave w, in
             }
         }
     }
-    const uint32_t o = append_slot(keep, counts);
+    const uint32_t o = append_slot(keep, out_count);
     if (keep) {
         out_rays[2 * o] = nr0;
         out_rays[2 * o + 1] = nr1;
         out_state[o] = ns;
     }
-    const uint32_t qo = append_slot(query, counts + 1);
+    const uint32_t qo = append_slot(query, q_count);
     if (query) {
         for (int k = 0; k < 9; k++) queries[9 * (size_t)qo + k] = qv[k];
         q_state[qo] = ns;
@@ -218,12 +223,14 @@ __global__ void __launch_bounds__(kGdThreads) k_gd_sample(SceneGPU sc, Wave w, f
                                                           const float* __restrict__ queries,
                                                           const PathState* __restrict__ q_state,
                                                           const int32_t* __restrict__ q_prim,
-                                                          const float* __restrict__ raw, uint32_t nq,
+                                                          const float* __restrict__ raw,
+                                                          const uint32_t* __restrict__ d_nq,
                                                           float4* __restrict__ out_rays,
                                                           PathState* __restrict__ out_state,
-                                                          uint32_t* __restrict__ counts)
+                                                          uint32_t* __restrict__ out_count)
 {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nq = *d_nq;
     bool keep = false;
     float4 nr0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), nr1 = nr0;
     PathState ns;
@@ -276,7 +283,7 @@ __global__ void __launch_bounds__(kGdThreads) k_gd_sample(SceneGPU sc, Wave w, f
             }
         }
     }
-    const uint32_t o = append_slot(keep, counts);
+    const uint32_t o = append_slot(keep, out_count);
     if (keep) {
         out_rays[2 * o] = nr0;
         out_rays[2 * o + 1] = nr1;
@@ -421,10 +428,13 @@ int render_pt_guided(lmgpu_scene* sc, lmgpu_guide* guide, const lmgpu_pt_params*
     }
     const SceneGPU sg = scene_view(sc);
     auto read_counts = [&]() -> int {
-        LMGPU_CUDA_TRY(cudaMemcpyAsync(G.h_counts, G.counts, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(G.h_counts, G.counts, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
         LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
         return LMGPU_OK;
     };
+    constexpr int kCheckEvery = 8;
+    const bool bounded = prm->max_num_vertices >= 0;
+    const int maxb = bounded ? (prm->max_num_vertices > 1 ? prm->max_num_vertices - 1 : 0) : (1 << 16);
     float loss = 0.0f;
     const uint64_t total = npix * prm->spp;
     for (uint64_t p0 = 0; p0 < total; p0 += W) {
@@ -435,46 +445,53 @@ int render_pt_guided(lmgpu_scene* sc, lmgpu_guide* guide, const lmgpu_pt_params*
         w.rec = G.rec;
         w.nrec = G.nrec;
         w.own = sc->q_own;
-        k_gd_generate<<<(unsigned)((w.n + kGdThreads - 1) / kGdThreads), kGdThreads, 0, stream>>>(
-            sc->cam, w, prm->seed, sc->q_ray[0], sc->q_state[0]);
+        // queue lengths on the device (counts: [0], [1] path queues, [2]
+        // network queries, [3] training samples): a wave's bounces are queued
+        // without host round trips; with max_num_vertices bounded the queue is
+        // empty after max_num_vertices - 1 bounces, otherwise the host checks
+        // every kCheckEvery bounces
+        const unsigned gblocks = (unsigned)((w.n + kGdThreads - 1) / kGdThreads);
+        LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts, 0, 4 * sizeof(uint32_t), stream));
+        k_gd_generate<<<gblocks, kGdThreads, 0, stream>>>(sc->cam, w, prm->seed, sc->q_ray[0], sc->q_state[0],
+                                                          G.counts);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
-        uint32_t n = w.n;
         int cur = 0;
-        while (n > 0) {
-            if ((rc = launch_trace(sc->accel, sc->q_ray[cur], sc->q_hit, n, false, false, stream))) return rc;
-            LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts, 0, 2 * sizeof(uint32_t), stream));
-            k_gd_shade<<<(n + kGdThreads - 1) / kGdThreads, kGdThreads, 0, stream>>>(
-                sg, w, prm->max_num_vertices, prm->seed, (int)gp->rr_mode, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, n,
-                sc->q_ray[1 - cur], sc->q_state[1 - cur], G.queries, G.q_state, G.q_prim, G.counts);
+        for (int b = 0; b < maxb; b++) {
+            if ((rc = launch_trace_dn(sc->accel, sc->q_ray[cur], sc->q_hit, G.counts + cur, w.n, false, stream)))
+                return rc;
+            LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts + (1 - cur), 0, sizeof(uint32_t), stream));
+            LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts + 2, 0, sizeof(uint32_t), stream));
+            k_gd_shade<<<gblocks, kGdThreads, 0, stream>>>(sg, w, prm->max_num_vertices, prm->seed, (int)gp->rr_mode,
+                                                           sc->q_ray[cur], sc->q_state[cur], sc->q_hit, G.counts + cur,
+                                                           sc->q_ray[1 - cur], sc->q_state[1 - cur],
+                                                           G.counts + (1 - cur), G.queries, G.q_state, G.q_prim,
+                                                           G.counts + 2);
             LMGPU_CUDA_TRY(cudaGetLastError());
-            sc->launches += 2;
-            if ((rc = read_counts())) return rc;
-            const uint32_t nq = G.h_counts[1];
-            if (nq > 0) {
-                if ((rc = guide_forward_device(guide, G.queries, nq, G.raw, stream))) return rc;
-                k_gd_sample<<<(nq + kGdThreads - 1) / kGdThreads, kGdThreads, 0, stream>>>(
-                    sg, w, gp->alpha, prm->seed, G.queries, G.q_state, G.q_prim, G.raw, nq, sc->q_ray[1 - cur],
-                    sc->q_state[1 - cur], G.counts);
-                LMGPU_CUDA_TRY(cudaGetLastError());
-                sc->launches += 2;
-                if ((rc = read_counts())) return rc;
-            }
-            n = G.h_counts[0];
+            if ((rc = guide_forward_device_dn(guide, G.queries, G.counts + 2, w.n, G.raw, stream))) return rc;
+            k_gd_sample<<<gblocks, kGdThreads, 0, stream>>>(sg, w, gp->alpha, prm->seed, G.queries, G.q_state,
+                                                            G.q_prim, G.raw, G.counts + 2, sc->q_ray[1 - cur],
+                                                            sc->q_state[1 - cur], G.counts + (1 - cur));
+            LMGPU_CUDA_TRY(cudaGetLastError());
+            sc->launches += 4;
             cur = 1 - cur;
+            if (!bounded && (b + 1) % kCheckEvery == 0) {
+                if ((rc = read_counts())) return rc;
+                if (G.h_counts[cur] == 0) break;
+            }
         }
         k_gd_flush<<<(w.n + 255) / 256, 256, 0, stream>>>(w, sc->film, sc->film_sq);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
         if (!gp->train) continue;
         // training samples of this pass, then up to max_steps_per_pass Adam steps
-        LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts + 2, 0, sizeof(uint32_t), stream));
+        LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts + 3, 0, sizeof(uint32_t), stream));
         k_gd_collect<<<(w.n + 255) / 256, 256, 0, stream>>>(w, G.tq, G.tdir, G.tw, (uint32_t)tcap,
-                                                                       G.counts + 2);
+                                                                       G.counts + 3);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
         if ((rc = read_counts())) return rc;
-        const uint64_t nt = G.h_counts[2] < tcap ? G.h_counts[2] : tcap;
+        const uint64_t nt = G.h_counts[3] < tcap ? G.h_counts[3] : tcap;
         for (uint64_t b0 = 0; b0 < nt; b0 += gp->batch) {
             const uint64_t nb = (nt - b0) < gp->batch ? (nt - b0) : gp->batch;
             if ((rc = guide_gradient_device(guide, G.tq + 9 * b0, G.tdir + 3 * b0, G.tw + b0, nb, stream)) ||
