@@ -250,6 +250,18 @@ int lmgpu_render_bdpt(lmgpu_scene* scene, const lmgpu_pt_params* params, float* 
 int lmgpu_render_bdpt_device(lmgpu_scene* scene, const lmgpu_pt_params* params, float* d_image, float* d_variance,
                              void* stream);
 
+/* MIS weights of renderer::bdpt's "mis" parameter. */
+#define LMGPU_MIS_POWER 0  /* misweight::powerheuristics (renderer_bdpt.cpp:747-784), the default */
+#define LMGPU_MIS_SIMPLE 1 /* misweight::simple (renderer_bdpt.cpp:711-744): one over the number of
+                              strategies that can sample the path */
+
+/* As lmgpu_render_bdpt / lmgpu_render_bdpt_device with the MIS weight
+ * chosen (LMGPU_MIS_*). */
+int lmgpu_render_bdpt_mis(lmgpu_scene* scene, const lmgpu_pt_params* params, int mis, float* image,
+                          float* variance);
+int lmgpu_render_bdpt_mis_device(lmgpu_scene* scene, const lmgpu_pt_params* params, int mis, float* d_image,
+                                 float* d_variance, void* stream);
+
 /* ---- Batched path tracing: many scenes / views in one wavefront -------- */
 
 typedef struct lmgpu_batch lmgpu_batch;

@@ -153,6 +153,16 @@ __device__ __noinline__ float mis_weight(const Ctx& C, const PV* P, int n, int s
         if (t > 0) pe = (s == 0 && d) ? sufE[2] * posL : sufE[s + 1];
         return pl * pe;
     };
+    if (C.mis == 1) {
+        // misweight::simple (renderer_bdpt.cpp:711-744)
+        int nonzero = 0;
+        for (int s = 0; s <= n; s++)
+            for (int d = 0; d < 2; d++) {
+                if (s > 0 && n - s > 0 && d) continue;
+                if (pdf(s, d != 0) > 0.0f) nonzero++;
+            }
+        return 1.0f / (float)nonzero;
+    }
     const float ps = pdf(s_, d_);
     float inv = 0.0f;
     for (int s = 0; s <= n; s++)
@@ -745,6 +755,7 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
     C.cam = sc->cam;
     C.max_v = prm->max_num_vertices < 0 || prm->max_num_vertices > kMaxV ? kMaxV : prm->max_num_vertices;
     C.max_path = prm->max_num_vertices;
+    C.mis = sc->bdpt_mis;
     if (C.max_v < 1) return finalize_film(sc, prm->spp, d_image, d_variance, stream);
 
     if (!sc->bdpt) sc->bdpt = new BdptState();

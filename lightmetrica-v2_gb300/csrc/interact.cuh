@@ -29,6 +29,7 @@ struct Ctx {
     CameraGPU cam;
     int max_v;     // BDPT: subpath vertices (capped); PT: unused
     int max_path;  // full-path vertices (the reference's max_num_vertices; -1 = unbounded)
+    int mis = 0;   // BDPT weight: 0 power heuristic, 1 one over the number of samplable strategies
 };
 
 __device__ __forceinline__ float3 zero3() { return f3(0.0f, 0.0f, 0.0f); }

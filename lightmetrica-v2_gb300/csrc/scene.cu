@@ -467,4 +467,31 @@ int lmgpu_render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* image,
     return render_host("lmgpu_render_bdpt", render_bdpt, sc, prm, image, variance);
 }
 
+int lmgpu_render_bdpt_mis(lmgpu_scene* sc, const lmgpu_pt_params* prm, int mis, float* image, float* variance)
+{
+    clear_error();
+    if (!sc || (mis != LMGPU_MIS_POWER && mis != LMGPU_MIS_SIMPLE)) {
+        set_error("lmgpu_render_bdpt_mis: NULL scene or unknown MIS weight");
+        return LMGPU_ERR_INVALID;
+    }
+    sc->bdpt_mis = mis;
+    const int rc = render_host("lmgpu_render_bdpt_mis", render_bdpt, sc, prm, image, variance);
+    sc->bdpt_mis = LMGPU_MIS_POWER;
+    return rc;
+}
+
+int lmgpu_render_bdpt_mis_device(lmgpu_scene* sc, const lmgpu_pt_params* prm, int mis, float* d_image,
+                                 float* d_variance, void* stream)
+{
+    clear_error();
+    if (!sc || (mis != LMGPU_MIS_POWER && mis != LMGPU_MIS_SIMPLE)) {
+        set_error("lmgpu_render_bdpt_mis_device: NULL scene or unknown MIS weight");
+        return LMGPU_ERR_INVALID;
+    }
+    sc->bdpt_mis = mis;
+    const int rc = render_device("lmgpu_render_bdpt_mis_device", render_bdpt, sc, prm, d_image, d_variance, stream);
+    sc->bdpt_mis = LMGPU_MIS_POWER;
+    return rc;
+}
+
 }  // extern "C"

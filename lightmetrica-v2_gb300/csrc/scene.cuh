@@ -112,7 +112,8 @@ struct lmgpu_scene {
     uint64_t q_cap = 0;
     cudaStream_t stream = nullptr;
     uint64_t launches = 0;  // kernels launched by the renderers since creation
-    lmgpu::BdptState* bdpt = nullptr;      // buffers of the bidirectional renderer
+    lmgpu::BdptState* bdpt = nullptr;
+    int bdpt_mis = 0;  // MIS weight of the render in progress (LMGPU_MIS_*)      // buffers of the bidirectional renderer
     lmgpu::GuidedState* guided = nullptr;  // buffers of the guided renderer
 };
 

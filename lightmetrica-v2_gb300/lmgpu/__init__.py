@@ -27,6 +27,9 @@ class Hit(ctypes.Structure):
     _fields_ = [("t", ctypes.c_float), ("prim", ctypes.c_int32), ("b1", ctypes.c_float), ("b2", ctypes.c_float)]
 
 
+# renderer::bdpt's "mis" parameter -> LMGPU_MIS_*
+MIS_WEIGHTS = {"powerheuristics": 0, "simple": 1}
+
 HIT_DTYPE = np.dtype([("t", "<f4"), ("prim", "<i4"), ("b1", "<f4"), ("b2", "<f4")])
 
 
@@ -98,6 +101,8 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_render_ptmis.argtypes = [vp, vp, vp, vp]
     L.lmgpu_render_ptdirect.argtypes = [vp, vp, vp, vp]
     L.lmgpu_render_ltdirect.argtypes = [vp, vp, vp, vp]
+    L.lmgpu_render_bdpt_mis.argtypes = [vp, vp, i32, vp, vp]
+    L.lmgpu_render_bdpt_mis_device.argtypes = [vp, vp, i32, vp, vp, vp]
     L.lmgpu_render_ltdirect_device.argtypes = [vp, vp, vp, vp, vp]
     L.lmgpu_guide_num_params.argtypes = [ctypes.POINTER(u64)]
     L.lmgpu_guide_create.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(vp)]
@@ -137,6 +142,7 @@ def lib() -> ctypes.CDLL:
                  "lmgpu_guide_train_step", "lmgpu_guide_forward_device", "lmgpu_guide_train_step_device",
                  "lmgpu_render_pt_guided", "lmgpu_render_pt_guided_device",
                  "lmgpu_render_ptdirect_device", "lmgpu_render_ltdirect", "lmgpu_render_ltdirect_device",
+                 "lmgpu_render_bdpt_mis", "lmgpu_render_bdpt_mis_device",
                  "lmgpu_accel_set_attributes", "lmgpu_surface", "lmgpu_surface_device",
                  "lmgpu_scene_set_environment"):
         getattr(L, name).restype = ctypes.c_int
@@ -401,12 +407,15 @@ class Scene:
         _check(lib().lmgpu_scene_launch_count(self._h, ctypes.byref(n)))
         return n.value
 
-    def render_bdpt(self, spp: int, max_num_vertices: int = -1, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
-        """renderer::bdpt: film (H, W, 3) and per-pixel variance of the estimate."""
+    def render_bdpt(self, spp: int, max_num_vertices: int = -1, seed: int = 0,
+                    mis: str = "powerheuristics") -> tuple[np.ndarray, np.ndarray]:
+        """renderer::bdpt: film (H, W, 3) and per-pixel variance of the
+        estimate; mis: the renderer's MIS weight, powerheuristics or simple."""
         img = np.empty((self.height, self.width, 3), np.float32)
         var = np.empty((self.height, self.width, 3), np.float32)
         prm = PtParams(spp, max_num_vertices, seed)
-        _check(lib().lmgpu_render_bdpt(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
+        _check(lib().lmgpu_render_bdpt_mis(self._h, ctypes.byref(prm), MIS_WEIGHTS[mis], img.ctypes.data,
+                                           var.ctypes.data))
         return img, var
 
     def render_bdpt_device(self, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,

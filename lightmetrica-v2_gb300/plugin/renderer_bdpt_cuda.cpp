@@ -15,9 +15,8 @@
 
     Interface followed:
       Renderer::Initialize   include/lightmetrica/renderer.h:68 (parameters of
-                             renderer::bdpt, renderer_bdpt.cpp:832-839, with
-                             mis = powerheuristics, the default and the only
-                             weighting implemented)
+                             renderer::bdpt, renderer_bdpt.cpp:832-839: mis =
+                             powerheuristics (the default) or simple)
       Renderer::Render       include/lightmetrica/renderer.h:81
     num_samples becomes ceil(num_samples / (W H)) samples per pixel.  Subpaths
     are capped at 16 vertices each (max_num_vertices = -1 included).
@@ -42,10 +41,13 @@ public:
     {
         numSamples_ = prop->ChildAs<long long>("num_samples", 10000000L);
         maxNumVertices_ = prop->ChildAs("max_num_vertices", -1);
+        // the MIS weight component, misweight::<mis> (renderer_bdpt.cpp:837)
         const auto mis = prop->ChildAs<std::string>("mis", "powerheuristics");
-        if (mis != "powerheuristics")
+        if (mis == "powerheuristics") mis_ = LMGPU_MIS_POWER;
+        else if (mis == "simple") mis_ = LMGPU_MIS_SIMPLE;
+        else
         {
-            LM_LOG_ERROR("renderer::bdpt_cuda: only mis = powerheuristics is implemented");
+            LM_LOG_ERROR("renderer::bdpt_cuda: unknown mis '" + mis + "'");
             return false;
         }
         return true;
@@ -65,7 +67,7 @@ public:
         prm.max_num_vertices = maxNumVertices_;
         prm.seed = initRng->NextUInt();
         std::vector<float> img((size_t)npix * 3);
-        if (lmgpu_render_bdpt(sc, &prm, img.data(), nullptr) != LMGPU_OK)
+        if (lmgpu_render_bdpt_mis(sc, &prm, mis_, img.data(), nullptr) != LMGPU_OK)
         {
             LM_LOG_ERROR(std::string("renderer::bdpt_cuda: ") + lmgpu_last_error());
             lmgpu_scene_destroy(sc);
@@ -80,6 +82,7 @@ private:
 
     long long numSamples_ = 0;
     int maxNumVertices_ = -1;
+    int mis_ = LMGPU_MIS_POWER;
 
 };
 

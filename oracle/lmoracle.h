@@ -132,6 +132,14 @@ uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t n
                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
                             uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir);
 
+/* As lmo_render_bdpt_ex with renderer::bdpt's MIS weight: mis 0
+ * misweight::powerheuristics (renderer_bdpt.cpp:747-784), 1 misweight::simple
+ * (:711-744). */
+uint64_t lmo_render_bdpt_mis(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
+                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
+                             uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir,
+                             int mis);
+
 /* Surface geometry of n hits (IntersectionUtils::CreateTriangleIntersection,
  * intersectionutils.h:59-135) in double precision.  tris / normals: [ntri*9]
  * per triangle in global order, already through the primitive's transform /

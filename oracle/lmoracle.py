@@ -57,6 +57,8 @@ def lib() -> ctypes.CDLL:
         L.lmo_render_bdpt.restype = ctypes.c_uint64
         L.lmo_render_bdpt_ex.argtypes = L.lmo_render_bdpt.argtypes + [ctypes.c_int]
         L.lmo_render_bdpt_ex.restype = ctypes.c_uint64
+        L.lmo_render_bdpt_mis.argtypes = L.lmo_render_bdpt.argtypes + [ctypes.c_int, ctypes.c_int]
+        L.lmo_render_bdpt_mis.restype = ctypes.c_uint64
         L.lmo_render_ptmis.argtypes = L.lmo_render_bdpt.argtypes
         L.lmo_render_ptmis.restype = ctypes.c_uint64
         L.lmo_render_ptdirect.argtypes = L.lmo_render_bdpt.argtypes
@@ -184,7 +186,7 @@ def write_render_scene(path: str, scene: dict, num_samples: int, max_num_vertice
 
 
 def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,
-                   double: bool = False, renderer: str = "pt") -> dict:
+                   double: bool = False, renderer: str = "pt", mis: str | None = None) -> dict:
     """Runs the reference renderer::pt or renderer::bdpt (compiled from its
     sources) and returns the film (H, W, 3), the per-pixel variance of that
     estimate and timing."""
@@ -197,7 +199,8 @@ def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: i
         ps, po = os.path.join(tmp, "scene.bin"), os.path.join(tmp, "out.bin")
         write_render_scene(ps, scene, num_samples, max_num_vertices, seed, threads)
         exe = REF_RENDER64 if double else REF_RENDER
-        out = subprocess.run([exe, ps, po, renderer], capture_output=True, text=True, check=True).stdout
+        cmd = [exe, ps, po, renderer] + ([mis] if mis else [])
+        out = subprocess.run(cmd, capture_output=True, text=True, check=True).stdout
         raw = open(po, "rb").read()
     n = W * H * 3
     img = np.frombuffer(raw[:4 * n], dtype=np.float32).reshape(H, W, 3)
@@ -280,9 +283,10 @@ def render_pt(scene: dict, num_samples: int, max_num_vertices: int, seed: int, t
 
 
 def render_bdpt(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,
-                independent_light_dir: bool = False) -> dict:
-    """The oracle's renderer::bdpt (power heuristic): film (H, W, 3) and per-pixel variance.
-    independent_light_dir: the diagnostic variant of lmo_render_bdpt_ex."""
+                independent_light_dir: bool = False, mis: str = "powerheuristics") -> dict:
+    """The oracle's renderer::bdpt: film (H, W, 3) and per-pixel variance.
+    independent_light_dir: the diagnostic variant of lmo_render_bdpt_ex;
+    mis: the renderer's "mis" parameter, powerheuristics or simple."""
     tris = np.ascontiguousarray(np.concatenate([p["tris"] for p in scene["prims"]]), dtype=np.float32)
     tri_prim = np.concatenate([np.full(p["tris"].shape[0], i, np.int32) for i, p in enumerate(scene["prims"])])
     W, H = scene["camera"]["width"], scene["camera"]["height"]
@@ -290,9 +294,10 @@ def render_bdpt(scene: dict, num_samples: int, max_num_vertices: int, seed: int,
     q = np.zeros((H, W, 3), np.float64)
     prims = scene_prims(scene)
     cam = scene_camera(scene)
-    lib().lmo_render_bdpt_ex(tris.ctypes.data, tri_prim.ctypes.data, tris.shape[0], ctypes.addressof(prims),
-                             len(scene["prims"]), ctypes.addressof(cam), num_samples, max_num_vertices, seed,
-                             threads, s.ctypes.data, q.ctypes.data, 1 if independent_light_dir else 0)
+    lib().lmo_render_bdpt_mis(tris.ctypes.data, tri_prim.ctypes.data, tris.shape[0], ctypes.addressof(prims),
+                              len(scene["prims"]), ctypes.addressof(cam), num_samples, max_num_vertices, seed,
+                              threads, s.ctypes.data, q.ctypes.data, 1 if independent_light_dir else 0,
+                              {"powerheuristics": 0, "simple": 1}[mis])
     img = s * (W * H / num_samples)
     return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}
 

@@ -117,6 +117,7 @@ typedef struct {
     int max_v;
     int independent_light_dir;
     int ptmis;     /* 1: renderer::ptmis, 2: renderer::ptdirect, 3: renderer::ltdirect */
+    int mis;       /* renderer::bdpt's weight: 0 misweight::powerheuristics, 1 misweight::simple */
     uint64_t num_samples, seed;
     int threads;
     double *sum, *sumsq;
@@ -642,9 +643,24 @@ static float eval_pdf(const bd_job* J, const pvx* P, int n, int s, int direct)
     return pdf;
 }
 
+/* MISWeight_Simple (renderer_bdpt.cpp:711-744): one over the number of
+ * strategies that can sample the path */
+static float mis_simple(const bd_job* J, const pvx* P, int n)
+{
+    int nonzero = 0;
+    for (int s = 0; s <= n; s++)
+        for (int d = 0; d < 2; d++) {
+            const int t = n - s;
+            if (s > 0 && t > 0 && d) continue;
+            if (eval_pdf(J, P, n, s, d) > 0.0f) nonzero++;
+        }
+    return 1.0f / (float)nonzero;
+}
+
 /* MISWeight_PowerHeuristics (renderer_bdpt.cpp:747-784) */
 static float mis_power(const bd_job* J, const pvx* P, int n, int s_, int d_)
 {
+    if (J->mis == 1) return mis_simple(J, P, n);
     const float ps = eval_pdf(J, P, n, s_, d_);
     float inv = 0.0f;
     for (int s = 0; s <= n; s++)
@@ -1004,8 +1020,18 @@ uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t n
                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
                             uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir)
 {
+    return lmo_render_bdpt_mis(tris, tri_prim, ntri, prims, nprims, cam, num_samples, max_num_vertices, seed, threads,
+                               sum, sumsq, independent_light_dir, 0);
+}
+
+uint64_t lmo_render_bdpt_mis(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
+                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
+                             uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir,
+                             int mis)
+{
     bd_job J;
     memset(&J, 0, sizeof(J));
+    J.mis = mis;
     if (max_num_vertices > MAXV || max_num_vertices == -1) max_num_vertices = MAXV;
     J.accel = lmo_accel_build(1, tris, ntri);
     J.tris = tris;

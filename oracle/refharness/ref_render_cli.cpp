@@ -32,7 +32,9 @@
 //                     environment hit; the harness sets it to the environment
 //                     light's primitive, as a fixed scene would.
 //
-// Usage: ref_render <scene.bin> <out.bin> [pt|bdpt|ptmis|ptdirect|ltdirect]   (renderer::pt by default)
+// Usage: ref_render <scene.bin> <out.bin> [pt|bdpt|ptmis|ptdirect|ltdirect] [mis]
+//        (renderer::pt by default; mis: renderer::bdpt's "mis" parameter,
+//        powerheuristics or simple)
 //   scene.bin: u32 magic 'LMRS', u32 version 2, u32 W, H,
 //              f32 eye[3], center[3], up[3], fov_deg,
 //              u32 nprims, per primitive: i32 bsdf (0 null, 1 diffuse,
@@ -482,6 +484,7 @@ int main(int argc, char** argv)
     if (!renderer) { std::fprintf(stderr, "unknown renderer %s\n", rendererKey.c_str()); return 5; }
     HarnessProp rprop;
     rprop.Set("num_samples", std::to_string(numSamples)).Set("max_num_vertices", std::to_string(maxNumVertices));
+    if (argc > 4) rprop.Set("mis", argv[4]);  // renderer::bdpt's MIS weight (misweight::<name>)
     if (!renderer->Initialize(&rprop)) return 5;
     Random initRng;
     initRng.SetSeed(seed);

@@ -35,6 +35,11 @@ Fixtures written:
       The Cornell box rendered by the reference's own renderer::ptdirect
       (light samples only) at 64x64, 16,384 samples per pixel,
       max_num_vertices 9, single and double precision.
+  cornell_bdpt_simple.npz
+      The Cornell box rendered by the reference's own renderer::bdpt with
+      mis: simple (misweight::simple, one over the number of strategies that
+      can sample the path) at 32x32, 32,768 samples per pixel,
+      max_num_vertices 10, single and double precision.
   cornell_ltdirect.npz
       The Cornell box rendered by the reference's own renderer::ltdirect
       (light tracing, a sensor connection at every vertex) with 64x64x16,384
@@ -215,11 +220,13 @@ def scene_arrays(sc: dict) -> dict:
     return out
 
 
-def pt_case(sc: dict, spp: int, seed: int, renderer: str = "pt", max_num_vertices: int = 9) -> dict:
+def pt_case(sc: dict, spp: int, seed: int, renderer: str = "pt", max_num_vertices: int = 9,
+            mis: str | None = None) -> dict:
     W, H = sc["camera"]["width"], sc["camera"]["height"]
     N = W * H * spp
-    f = lo.run_ref_render(sc, N, max_num_vertices, seed, os.cpu_count() or 8, renderer=renderer)
-    d = lo.run_ref_render(sc, N, max_num_vertices, seed + 1, os.cpu_count() or 8, double=True, renderer=renderer)
+    f = lo.run_ref_render(sc, N, max_num_vertices, seed, os.cpu_count() or 8, renderer=renderer, mis=mis)
+    d = lo.run_ref_render(sc, N, max_num_vertices, seed + 1, os.cpu_count() or 8, double=True, renderer=renderer,
+                          mis=mis)
     out = scene_arrays(sc)
     out.update({"num_samples": np.int64(N), "max_num_vertices": np.int32(max_num_vertices),
                 "ref_image": f["image"].astype(np.float32), "ref_variance": f["variance"].astype(np.float32),
@@ -338,6 +345,9 @@ def main() -> None:
     if want("cornell_ptdirect"):
         np.savez_compressed(os.path.join(HERE, "cornell_ptdirect.npz"),
                             **pt_case(scenes.cornell_box(64, 64), 16384, 20241201, "ptdirect", 9))
+    if want("cornell_bdpt_simple"):
+        np.savez_compressed(os.path.join(HERE, "cornell_bdpt_simple.npz"),
+                            **pt_case(scenes.cornell_box(32, 32), 32768, 20241401, "bdpt", 10, mis="simple"))
     if want("cornell_ltdirect"):
         np.savez_compressed(os.path.join(HERE, "cornell_ltdirect.npz"),
                             **pt_case(scenes.cornell_box(64, 64), 16384, 20241301, "ltdirect", 9))

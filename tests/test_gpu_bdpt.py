@@ -98,3 +98,16 @@ def test_bdpt_device_entry_matches_host_entry(gpu_lib, golden_dir):
     sc.close()
     assert np.allclose(di.cpu().numpy(), a, rtol=1e-4, atol=1e-5)
     assert np.allclose(dv.cpu().numpy(), va, rtol=1e-3, atol=1e-5)
+
+
+def test_bdpt_simple_weight_matches_reference_film(gpu_lib, golden_dir):
+    """mis: simple against the reference's own film with that weight.  (It is
+    not the power heuristic's image: the strategies that start on the light
+    carry the light::area sample-reuse bias, light_area.cpp:73-80, so
+    weighting them differently converges elsewhere, in the reference too.)"""
+    scene, z = ptscene.load_scene(golden_dir, "cornell_bdpt_simple")
+    sc = gpu_lib.Scene(scene)
+    img, var = sc.render_bdpt(32768, int(z["max_num_vertices"]), 9, mis="simple")
+    sc.close()
+    print(imgcheck.assert_same_image(img, var, z["ref64_image"], z["ref64_variance"], "gpu vs ref64 (simple)"))
+    print("relMSE vs FP64 reference", imgcheck.relmse(img, z["ref64_image"]))

@@ -63,3 +63,14 @@ def test_oracle_bdpt_no_light_is_black(oracle_lib, golden_dir):
             p["kind"] = 0
     r = oracle_lib.render_bdpt(scene, 32 * 32 * 4, 10, 1, 2)
     assert not r["image"].any()
+
+
+def test_oracle_bdpt_simple_weight_matches_reference(oracle_lib, golden_dir):
+    """mis: simple (misweight::simple, one over the number of strategies that
+    can sample the path) against the reference's own film with that weight."""
+    scene, z = ptscene.load_scene(golden_dir, "cornell_bdpt_simple")
+    W, H = scene["camera"]["width"], scene["camera"]["height"]
+    r = oracle_lib.render_bdpt(scene, W * H * 4096, int(z["max_num_vertices"]), 4321, os.cpu_count() or 4,
+                               mis="simple")
+    print(imgcheck.assert_same_image(r["image"], r["variance"], z["ref64_image"], z["ref64_variance"],
+                                     "oracle vs ref64 (bdpt, simple weight)"))
