@@ -152,13 +152,19 @@ typedef struct {
     int32_t width, height;
 } lmgpu_camera;
 
-/* renderer::pt parameters (renderer_pt.cpp:56-62): samples per pixel
- * (the reference's num_samples = width * height * spp), max_num_vertices
- * (-1 = unbounded), and the seed of the counter-based random numbers. */
+/* Renderer parameters (renderer_pt.cpp:56-62 and the same in the other
+ * renderers): samples per pixel (the reference's num_samples = width *
+ * height * spp), max_num_vertices (-1 = unbounded), the seed of the
+ * counter-based random numbers, and min_num_vertices (0 = none; paths with
+ * fewer vertices contribute nothing, as each renderer applies it:
+ * renderer_pt.cpp:186, renderer_ptmis.cpp:132, :247, renderer_bdpt.cpp:892;
+ * renderer::ptdirect and renderer::ltdirect have no minimum). */
 typedef struct {
     uint64_t spp;
     int32_t max_num_vertices;
     uint32_t seed;
+    int32_t min_num_vertices;
+    int32_t reserved;
 } lmgpu_pt_params;
 
 typedef struct lmgpu_scene lmgpu_scene;

@@ -420,6 +420,8 @@ __device__ __forceinline__ uint32_t raster_pixel(const Ctx& C, const PV* P, int 
 // SelectionPDF (renderer_bdpt.cpp:348-368, :938-947); false if black.
 __device__ __forceinline__ bool path_contribution(const Ctx& C, const PV* P, int n, int s, bool d, float c[3])
 {
+    // min_num_vertices applies only with max_num_vertices set (renderer_bdpt.cpp:892)
+    if (C.max_path >= 0 && n < C.min_path) return false;
     const Spd cs = unweighted(C, P, n, s, d);
     if (black(cs)) return false;
     const float wgt = mis_weight(C, P, n, s, d);
@@ -756,6 +758,7 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
     C.max_v = prm->max_num_vertices < 0 || prm->max_num_vertices > kMaxV ? kMaxV : prm->max_num_vertices;
     C.max_path = prm->max_num_vertices;
     C.mis = sc->bdpt_mis;
+    C.min_path = prm->min_num_vertices;
     if (C.max_v < 1) return finalize_film(sc, prm->spp, d_image, d_variance, stream);
 
     if (!sc->bdpt) sc->bdpt = new BdptState();

@@ -103,7 +103,8 @@ __device__ __forceinline__ uint32_t append_slot(bool take, uint32_t* count)
 }
 
 // counts: [0] next path queue, [1] diffuse queries
-__global__ void __launch_bounds__(kGdThreads) k_gd_shade(SceneGPU sc, Wave w, int max_nv, uint32_t seed, int rr_mode,
+__global__ void __launch_bounds__(kGdThreads) k_gd_shade(SceneGPU sc, Wave w, int max_nv, int min_nv, uint32_t seed,
+                                                         int rr_mode,
                                                          const float4* __restrict__ rays,
                                                          const PathState* __restrict__ state,
                                                          const lmgpu_hit* __restrict__ hits,
@@ -156,9 +157,11 @@ __global__ void __launch_bounds__(kGdThreads) k_gd_shade(SceneGPU sc, Wave w, in
             }
         }
         if (emit) {
-            acc[0] += c[0];
-            acc[1] += c[1];
-            acc[2] += c[2];
+            if ((int)s.id.z + 1 >= min_nv) {  // min_num_vertices, renderer_pt.cpp:186
+                acc[0] += c[0];
+                acc[1] += c[1];
+                acc[2] += c[2];
+            }
             // incident radiance at the path's recorded vertices
             const int nr = w.nrec[path];
             for (int k = 0; k < nr; k++) {
@@ -462,7 +465,8 @@ int render_pt_guided(lmgpu_scene* sc, lmgpu_guide* guide, const lmgpu_pt_params*
                 return rc;
             LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts + (1 - cur), 0, sizeof(uint32_t), stream));
             LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts + 2, 0, sizeof(uint32_t), stream));
-            k_gd_shade<<<gblocks, kGdThreads, 0, stream>>>(sg, w, prm->max_num_vertices, prm->seed, (int)gp->rr_mode,
+            k_gd_shade<<<gblocks, kGdThreads, 0, stream>>>(sg, w, prm->max_num_vertices, prm->min_num_vertices,
+                                                           prm->seed, (int)gp->rr_mode,
                                                            sc->q_ray[cur], sc->q_state[cur], sc->q_hit, G.counts + cur,
                                                            sc->q_ray[1 - cur], sc->q_state[1 - cur],
                                                            G.counts + (1 - cur), G.queries, G.q_state, G.q_prim,

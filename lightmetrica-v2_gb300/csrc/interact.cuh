@@ -30,6 +30,7 @@ struct Ctx {
     int max_v;     // BDPT: subpath vertices (capped); PT: unused
     int max_path;  // full-path vertices (the reference's max_num_vertices; -1 = unbounded)
     int mis = 0;   // BDPT weight: 0 power heuristic, 1 one over the number of samplable strategies
+    int min_path = 0;  // full paths with fewer vertices contribute nothing (the reference's min_num_vertices)
 };
 
 __device__ __forceinline__ float3 zero3() { return f3(0.0f, 0.0f, 0.0f); }

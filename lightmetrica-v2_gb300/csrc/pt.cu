@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p
         own[3 * (size_t)i] = 0.0f;
         own[3 * (size_t)i + 1] = 0.0f;
         own[3 * (size_t)i + 2] = 0.0f;
-        if (NEE && (C.max_path < 0 || 1 < C.max_path)) {
+        if (NEE && (C.max_path < 0 || 1 < C.max_path) && (MODE == MODE_PTDIRECT || 2 >= C.min_path)) {
             // the sensor's light sample; it lands where ppL meets the film
             sensor_vertex(C, v);
             const Philox4x32 q = philox4x32_10((uint32_t)p, (uint32_t)(p >> 32), 0u, 1u, seed, kKeyCamera);
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(Ctx C, const float4*
         if (h.prim < 0) {
             // miss: the environment light, if any (scene3.cpp:464-475); the
             // path ends there (renderer_pt.cpp:200-203)
-            if (!NEE && C.sc.has_env) {
+            if (!NEE && C.sc.has_env && (int)s.id.z + 1 >= C.min_path) {
                 acc[0] += s.thr.x * C.sc.env_Le[0];
                 acc[1] += s.thr.y * C.sc.env_Le[1];
                 acc[2] += s.thr.z * C.sc.env_Le[2];
@@ -197,7 +197,8 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(Ctx C, const float4*
             v.degen = 0;
             uint32_t nv = s.id.z;
             const float cos_l = -dot3(d, v.n);
-            if (MODE != MODE_PTDIRECT && P.is_light && cos_l > 0.0f) {
+            // min_num_vertices: renderer_pt.cpp:186, renderer_ptmis.cpp:247
+            if (MODE != MODE_PTDIRECT && P.is_light && cos_l > 0.0f && (int)nv + 1 >= C.min_path) {
                 // throughput * Le(-d) * EvaluatePosition (= 1), renderer_pt.cpp:183-194;
                 // ptmis: weight pdf_bsdf / (pdf_bsdf + pdf_light), renderer_ptmis.cpp:246-270
                 float w = 1.0f;
@@ -216,7 +217,9 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_shade(Ctx C, const float4*
                 const bool more = C.max_path < 0 || (int)nv < C.max_path;
                 const float thr[3] = {2.0f * s.thr.x, 2.0f * s.thr.y, 2.0f * s.thr.z};
                 const float3 wi = d * -1.0f;
-                if (more && NEE) {
+                // renderer::ptmis samples a light only for paths of at least
+                // min_num_vertices (renderer_ptmis.cpp:132); ptdirect ignores it
+                if (more && NEE && (MODE == MODE_PTDIRECT || (int)nv + 1 >= C.min_path)) {
                     const Philox4x32 q = philox4x32_10(s.id.x, s.id.y, nv, 1u, seed, kKeyBounce);
                     float3 ppL;
                     has_nee = nee_sample<MODE == MODE_PTMIS>(C, v, v.type, wi, u01(q.v[0]), u01(q.v[1]),
@@ -335,6 +338,7 @@ int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float
     C.cam = sc->cam;
     C.max_v = 0;
     C.max_path = prm->max_num_vertices;
+    C.min_path = prm->min_num_vertices;
     const uint32_t np = (uint32_t)npix;
     // Queue lengths live on the device (q_count: [0], [1] path queues, [2]
     // pending light samples), so a wave's bounces are queued without host

@@ -269,7 +269,8 @@ class Camera(ctypes.Structure):
 
 
 class PtParams(ctypes.Structure):
-    _fields_ = [("spp", ctypes.c_uint64), ("max_num_vertices", ctypes.c_int32), ("seed", ctypes.c_uint32)]
+    _fields_ = [("spp", ctypes.c_uint64), ("max_num_vertices", ctypes.c_int32), ("seed", ctypes.c_uint32),
+                ("min_num_vertices", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 BSDF_NULL, BSDF_DIFFUSE, BSDF_DIELECTRIC, BSDF_COOK_TORRANCE = 0, 1, 2, 3
@@ -329,61 +330,61 @@ class Scene:
         except Exception:
             pass
 
-    def render_pt(self, spp: int, max_num_vertices: int = -1, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    def render_pt(self, spp: int, max_num_vertices: int = -1, seed: int = 0, min_num_vertices: int = 0) -> tuple[np.ndarray, np.ndarray]:
         """renderer::pt: film (H, W, 3) and per-pixel variance of the estimate."""
         img = np.empty((self.height, self.width, 3), np.float32)
         var = np.empty((self.height, self.width, 3), np.float32)
-        prm = PtParams(spp, max_num_vertices, seed)
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         _check(lib().lmgpu_render_pt(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
         return img, var
 
     def render_pt_device(self, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,
-                         seed: int = 0, stream: int = 0) -> None:
-        prm = PtParams(spp, max_num_vertices, seed)
+                         seed: int = 0, stream: int = 0, min_num_vertices: int = 0) -> None:
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         _check(lib().lmgpu_render_pt_device(self._h, ctypes.byref(prm), d_image, d_variance, stream))
 
-    def render_ptmis(self, spp: int, max_num_vertices: int = -1, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    def render_ptmis(self, spp: int, max_num_vertices: int = -1, seed: int = 0, min_num_vertices: int = 0) -> tuple[np.ndarray, np.ndarray]:
         """renderer::ptmis: film (H, W, 3) and per-pixel variance of the estimate."""
         img = np.empty((self.height, self.width, 3), np.float32)
         var = np.empty((self.height, self.width, 3), np.float32)
-        prm = PtParams(spp, max_num_vertices, seed)
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         _check(lib().lmgpu_render_ptmis(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
         return img, var
 
     def render_ptmis_device(self, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,
-                            seed: int = 0, stream: int = 0) -> None:
-        prm = PtParams(spp, max_num_vertices, seed)
+                            seed: int = 0, stream: int = 0, min_num_vertices: int = 0) -> None:
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         _check(lib().lmgpu_render_ptmis_device(self._h, ctypes.byref(prm), d_image, d_variance, stream))
 
-    def render_ptdirect(self, spp: int, max_num_vertices: int = -1, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    def render_ptdirect(self, spp: int, max_num_vertices: int = -1, seed: int = 0, min_num_vertices: int = 0) -> tuple[np.ndarray, np.ndarray]:
         """renderer::ptdirect: film (H, W, 3) and per-pixel variance of the estimate."""
         img = np.empty((self.height, self.width, 3), np.float32)
         var = np.empty((self.height, self.width, 3), np.float32)
-        prm = PtParams(spp, max_num_vertices, seed)
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         _check(lib().lmgpu_render_ptdirect(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
         return img, var
 
-    def render_ltdirect(self, spp: int, max_num_vertices: int = -1, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    def render_ltdirect(self, spp: int, max_num_vertices: int = -1, seed: int = 0, min_num_vertices: int = 0) -> tuple[np.ndarray, np.ndarray]:
         """renderer::ltdirect with spp x W x H light paths: film (H, W, 3) and
         per-pixel variance of the estimate."""
         img = np.empty((self.height, self.width, 3), np.float32)
         var = np.empty((self.height, self.width, 3), np.float32)
-        prm = PtParams(spp, max_num_vertices, seed)
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         _check(lib().lmgpu_render_ltdirect(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
         return img, var
 
     def render_ltdirect_device(self, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,
-                               seed: int = 0, stream: int = 0) -> None:
-        prm = PtParams(spp, max_num_vertices, seed)
+                               seed: int = 0, stream: int = 0, min_num_vertices: int = 0) -> None:
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         _check(lib().lmgpu_render_ltdirect_device(self._h, ctypes.byref(prm), d_image, d_variance, stream))
 
     def render_pt_guided(self, guide, spp: int, max_num_vertices: int = -1, seed: int = 0, alpha: float = 0.5,
                          learning_rate: float = 1e-3, train: bool = True, batch: int = 1 << 18,
-                         max_steps_per_pass: int = 4, rr_mode: int = 1) -> tuple[np.ndarray, np.ndarray, float]:
+                         max_steps_per_pass: int = 4, rr_mode: int = 1, min_num_vertices: int = 0) -> tuple[np.ndarray, np.ndarray, float]:
         """Guided renderer::pt: film, per-pixel variance, last training loss."""
         img = np.empty((self.height, self.width, 3), np.float32)
         var = np.empty((self.height, self.width, 3), np.float32)
-        prm = PtParams(spp, max_num_vertices, seed)
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         gp = GuidingParams(alpha, learning_rate, 1 if train else 0, batch, max_steps_per_pass, rr_mode)
         loss = ctypes.c_float()
         _check(lib().lmgpu_render_pt_guided(self._h, guide._h, ctypes.byref(prm), ctypes.byref(gp), img.ctypes.data,
@@ -393,8 +394,8 @@ class Scene:
     def render_pt_guided_device(self, guide, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,
                                 seed: int = 0, alpha: float = 0.5, learning_rate: float = 1e-3, train: bool = True,
                                 batch: int = 1 << 18, max_steps_per_pass: int = 4, rr_mode: int = 1,
-                                stream: int = 0) -> float:
-        prm = PtParams(spp, max_num_vertices, seed)
+                                stream: int = 0, min_num_vertices: int = 0) -> float:
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         gp = GuidingParams(alpha, learning_rate, 1 if train else 0, batch, max_steps_per_pass, rr_mode)
         loss = ctypes.c_float()
         _check(lib().lmgpu_render_pt_guided_device(self._h, guide._h, ctypes.byref(prm), ctypes.byref(gp), d_image,
@@ -408,19 +409,19 @@ class Scene:
         return n.value
 
     def render_bdpt(self, spp: int, max_num_vertices: int = -1, seed: int = 0,
-                    mis: str = "powerheuristics") -> tuple[np.ndarray, np.ndarray]:
+                    mis: str = "powerheuristics", min_num_vertices: int = 0) -> tuple[np.ndarray, np.ndarray]:
         """renderer::bdpt: film (H, W, 3) and per-pixel variance of the
         estimate; mis: the renderer's MIS weight, powerheuristics or simple."""
         img = np.empty((self.height, self.width, 3), np.float32)
         var = np.empty((self.height, self.width, 3), np.float32)
-        prm = PtParams(spp, max_num_vertices, seed)
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         _check(lib().lmgpu_render_bdpt_mis(self._h, ctypes.byref(prm), MIS_WEIGHTS[mis], img.ctypes.data,
                                            var.ctypes.data))
         return img, var
 
     def render_bdpt_device(self, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,
-                           seed: int = 0, stream: int = 0) -> None:
-        prm = PtParams(spp, max_num_vertices, seed)
+                           seed: int = 0, stream: int = 0, min_num_vertices: int = 0) -> None:
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         _check(lib().lmgpu_render_bdpt_device(self._h, ctypes.byref(prm), d_image, d_variance, stream))
 
 

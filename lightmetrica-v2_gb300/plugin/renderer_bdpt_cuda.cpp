@@ -41,6 +41,7 @@ public:
     {
         numSamples_ = prop->ChildAs<long long>("num_samples", 10000000L);
         maxNumVertices_ = prop->ChildAs("max_num_vertices", -1);
+        minNumVertices_ = prop->ChildAs("min_num_vertices", 0);
         // the MIS weight component, misweight::<mis> (renderer_bdpt.cpp:837)
         const auto mis = prop->ChildAs<std::string>("mis", "powerheuristics");
         if (mis == "powerheuristics") mis_ = LMGPU_MIS_POWER;
@@ -61,10 +62,11 @@ public:
         lmgpu_scene* sc = lmgpu_export::Create(a);
         if (!sc) return;
         const long long npix = (long long)a.camera.width * a.camera.height;
-        lmgpu_pt_params prm;
+        lmgpu_pt_params prm = {};
         prm.spp = (uint64_t)((numSamples_ + npix - 1) / npix);
         prm.spp = prm.spp > 0 ? prm.spp : 1;
         prm.max_num_vertices = maxNumVertices_;
+        prm.min_num_vertices = minNumVertices_;
         prm.seed = initRng->NextUInt();
         std::vector<float> img((size_t)npix * 3);
         if (lmgpu_render_bdpt_mis(sc, &prm, mis_, img.data(), nullptr) != LMGPU_OK)
@@ -82,6 +84,7 @@ private:
 
     long long numSamples_ = 0;
     int maxNumVertices_ = -1;
+    int minNumVertices_ = 0;
     int mis_ = LMGPU_MIS_POWER;
 
 };

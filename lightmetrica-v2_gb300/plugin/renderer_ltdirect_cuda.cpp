@@ -56,7 +56,7 @@ public:
         lmgpu_scene* sc = lmgpu_export::Create(a);
         if (!sc) return;
         const long long npix = (long long)a.camera.width * a.camera.height;
-        lmgpu_pt_params prm;
+        lmgpu_pt_params prm = {};
         prm.spp = (uint64_t)((numSamples_ + npix - 1) / npix);
         prm.spp = prm.spp > 0 ? prm.spp : 1;
         prm.max_num_vertices = maxNumVertices_;

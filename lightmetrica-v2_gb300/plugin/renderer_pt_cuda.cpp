@@ -44,6 +44,7 @@ public:
     {
         numSamples_ = prop->ChildAs<long long>("num_samples", 10000000L);
         maxNumVertices_ = prop->ChildAs("max_num_vertices", -1);
+        minNumVertices_ = prop->ChildAs("min_num_vertices", 0);
         return true;
     };
 
@@ -55,10 +56,11 @@ public:
         lmgpu_scene* sc = lmgpu_export::Create(a);
         if (!sc) return;
         const long long npix = (long long)a.camera.width * a.camera.height;
-        lmgpu_pt_params prm;
+        lmgpu_pt_params prm = {};
         prm.spp = (uint64_t)((numSamples_ + npix - 1) / npix);
         prm.spp = prm.spp > 0 ? prm.spp : 1;
         prm.max_num_vertices = maxNumVertices_;
+        prm.min_num_vertices = minNumVertices_;
         prm.seed = initRng->NextUInt();
         std::vector<float> img((size_t)npix * 3);
         if (lmgpu_render_pt(sc, &prm, img.data(), nullptr) != LMGPU_OK)
@@ -76,6 +78,7 @@ private:
 
     long long numSamples_ = 0;
     int maxNumVertices_ = -1;
+    int minNumVertices_ = 0;
 
 };
 

@@ -47,6 +47,7 @@ public:
     {
         numSamples_ = prop->ChildAs<long long>("num_samples", 10000000L);
         maxNumVertices_ = prop->ChildAs("max_num_vertices", -1);
+        minNumVertices_ = prop->ChildAs("min_num_vertices", 0);
         alpha_ = prop->ChildAs<Float>("alpha", 0.5_f);
         learningRate_ = prop->ChildAs<Float>("learning_rate", 0.001_f);
         throughputRoulette_ = prop->ChildAs<bool>("throughput_roulette", true);
@@ -61,10 +62,11 @@ public:
         lmgpu_scene* sc = lmgpu_export::Create(a);
         if (!sc) return;
         const long long npix = (long long)a.camera.width * a.camera.height;
-        lmgpu_pt_params prm;
+        lmgpu_pt_params prm = {};
         prm.spp = (uint64_t)((numSamples_ + npix - 1) / npix);
         prm.spp = prm.spp > 0 ? prm.spp : 1;
         prm.max_num_vertices = maxNumVertices_;
+        prm.min_num_vertices = minNumVertices_;
         prm.seed = initRng->NextUInt();
         const Bound bound = scene->GetBound();
         const float box[6] = { (float)bound.min.x, (float)bound.min.y, (float)bound.min.z,
@@ -100,6 +102,7 @@ private:
 
     long long numSamples_ = 0;
     int maxNumVertices_ = -1;
+    int minNumVertices_ = 0;
     Float alpha_ = 0.5_f;
     Float learningRate_ = 0.001_f;
     bool throughputRoulette_ = true;

@@ -48,15 +48,7 @@ public:
     {
         numSamples_ = prop->ChildAs<long long>("num_samples", 10000000L);
         maxNumVertices_ = prop->ChildAs("max_num_vertices", -1);
-        // min_num_vertices (default 0) suppresses contributions of shorter
-        // paths; values up to 2 suppress nothing, larger ones are not
-        // supported by the GPU form
-        const int minNumVertices = prop->ChildAs("min_num_vertices", 0);
-        if (minNumVertices > 2)
-        {
-            LM_LOG_ERROR("renderer::ptdirect_cuda: min_num_vertices > 2 is not supported");
-            return false;
-        }
+        minNumVertices_ = prop->ChildAs("min_num_vertices", 0);
         return true;
     };
 
@@ -68,10 +60,11 @@ public:
         lmgpu_scene* sc = lmgpu_export::Create(a);
         if (!sc) return;
         const long long npix = (long long)a.camera.width * a.camera.height;
-        lmgpu_pt_params prm;
+        lmgpu_pt_params prm = {};
         prm.spp = (uint64_t)((numSamples_ + npix - 1) / npix);
         prm.spp = prm.spp > 0 ? prm.spp : 1;
         prm.max_num_vertices = maxNumVertices_;
+        prm.min_num_vertices = minNumVertices_;
         prm.seed = initRng->NextUInt();
         std::vector<float> img((size_t)npix * 3);
         if (lmgpu_render_ptdirect(sc, &prm, img.data(), nullptr) != LMGPU_OK)
@@ -89,6 +82,7 @@ private:
 
     long long numSamples_ = 0;
     int maxNumVertices_ = -1;
+    int minNumVertices_ = 0;
 
 };
 

@@ -186,7 +186,8 @@ def write_render_scene(path: str, scene: dict, num_samples: int, max_num_vertice
 
 
 def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,
-                   double: bool = False, renderer: str = "pt", mis: str | None = None) -> dict:
+                   double: bool = False, renderer: str = "pt", mis: str | None = None,
+                   params: dict | None = None) -> dict:
     """Runs the reference renderer::pt or renderer::bdpt (compiled from its
     sources) and returns the film (H, W, 3), the per-pixel variance of that
     estimate and timing."""
@@ -199,7 +200,10 @@ def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: i
         ps, po = os.path.join(tmp, "scene.bin"), os.path.join(tmp, "out.bin")
         write_render_scene(ps, scene, num_samples, max_num_vertices, seed, threads)
         exe = REF_RENDER64 if double else REF_RENDER
-        cmd = [exe, ps, po, renderer] + ([mis] if mis else [])
+        extra = dict(params or {})
+        if mis:
+            extra["mis"] = mis
+        cmd = [exe, ps, po, renderer] + [f"{k}={v}" for k, v in extra.items()]
         out = subprocess.run(cmd, capture_output=True, text=True, check=True).stdout
         raw = open(po, "rb").read()
     n = W * H * 3

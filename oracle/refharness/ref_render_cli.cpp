@@ -32,9 +32,9 @@
 //                     environment hit; the harness sets it to the environment
 //                     light's primitive, as a fixed scene would.
 //
-// Usage: ref_render <scene.bin> <out.bin> [pt|bdpt|ptmis|ptdirect|ltdirect] [mis]
-//        (renderer::pt by default; mis: renderer::bdpt's "mis" parameter,
-//        powerheuristics or simple)
+// Usage: ref_render <scene.bin> <out.bin> [pt|bdpt|ptmis|ptdirect|ltdirect] [key=value ...]
+//        (renderer::pt by default; key=value: further renderer parameters,
+//        e.g. mis=simple, min_num_vertices=3)
 //   scene.bin: u32 magic 'LMRS', u32 version 2, u32 W, H,
 //              f32 eye[3], center[3], up[3], fov_deg,
 //              u32 nprims, per primitive: i32 bsdf (0 null, 1 diffuse,
@@ -484,7 +484,14 @@ int main(int argc, char** argv)
     if (!renderer) { std::fprintf(stderr, "unknown renderer %s\n", rendererKey.c_str()); return 5; }
     HarnessProp rprop;
     rprop.Set("num_samples", std::to_string(numSamples)).Set("max_num_vertices", std::to_string(maxNumVertices));
-    if (argc > 4) rprop.Set("mis", argv[4]);  // renderer::bdpt's MIS weight (misweight::<name>)
+    // further renderer parameters as key=value (mis, min_num_vertices, ...)
+    for (int a = 4; a < argc; a++)
+    {
+        const std::string kv = argv[a];
+        const auto eq = kv.find('=');
+        if (eq == std::string::npos) { std::fprintf(stderr, "bad parameter %s\n", argv[a]); return 2; }
+        rprop.Set(kv.substr(0, eq), kv.substr(eq + 1));
+    }
     if (!renderer->Initialize(&rprop)) return 5;
     Random initRng;
     initRng.SetSeed(seed);

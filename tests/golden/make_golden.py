@@ -40,6 +40,11 @@ Fixtures written:
       mis: simple (misweight::simple, one over the number of strategies that
       can sample the path) at 32x32, 32,768 samples per pixel,
       max_num_vertices 10, single and double precision.
+  cornell_pt_min3.npz, cornell_ptmis_min3.npz, cornell_bdpt_min3.npz
+      The Cornell box with min_num_vertices 3 (paths of fewer vertices
+      contribute nothing, so the directly seen light is black), rendered by
+      the reference's own renderer::pt, renderer::ptmis (64x64) and
+      renderer::bdpt (32x32, max_num_vertices 10), single and double precision.
   cornell_ltdirect.npz
       The Cornell box rendered by the reference's own renderer::ltdirect
       (light tracing, a sensor connection at every vertex) with 64x64x16,384
@@ -221,14 +226,17 @@ def scene_arrays(sc: dict) -> dict:
 
 
 def pt_case(sc: dict, spp: int, seed: int, renderer: str = "pt", max_num_vertices: int = 9,
-            mis: str | None = None) -> dict:
+            mis: str | None = None, min_num_vertices: int = 0) -> dict:
     W, H = sc["camera"]["width"], sc["camera"]["height"]
     N = W * H * spp
-    f = lo.run_ref_render(sc, N, max_num_vertices, seed, os.cpu_count() or 8, renderer=renderer, mis=mis)
+    extra = {"min_num_vertices": min_num_vertices} if min_num_vertices else None
+    f = lo.run_ref_render(sc, N, max_num_vertices, seed, os.cpu_count() or 8, renderer=renderer, mis=mis,
+                          params=extra)
     d = lo.run_ref_render(sc, N, max_num_vertices, seed + 1, os.cpu_count() or 8, double=True, renderer=renderer,
-                          mis=mis)
+                          mis=mis, params=extra)
     out = scene_arrays(sc)
     out.update({"num_samples": np.int64(N), "max_num_vertices": np.int32(max_num_vertices),
+                "min_num_vertices": np.int32(min_num_vertices),
                 "ref_image": f["image"].astype(np.float32), "ref_variance": f["variance"].astype(np.float32),
                 "ref64_image": d["image"].astype(np.float64), "ref64_variance": d["variance"].astype(np.float64)})
     return out
@@ -348,6 +356,12 @@ def main() -> None:
     if want("cornell_bdpt_simple"):
         np.savez_compressed(os.path.join(HERE, "cornell_bdpt_simple.npz"),
                             **pt_case(scenes.cornell_box(32, 32), 32768, 20241401, "bdpt", 10, mis="simple"))
+    for name, rend, spp, res, mnv in (("cornell_pt_min3", "pt", 16384, 64, 9), ("cornell_ptmis_min3", "ptmis", 8192, 64, 9),
+                                      ("cornell_bdpt_min3", "bdpt", 16384, 32, 10)):
+        if want(name):
+            np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                                **pt_case(scenes.cornell_box(res, res), spp, 20241501 + len(name), rend, mnv,
+                                          min_num_vertices=3))
     if want("cornell_ltdirect"):
         np.savez_compressed(os.path.join(HERE, "cornell_ltdirect.npz"),
                             **pt_case(scenes.cornell_box(64, 64), 16384, 20241301, "ltdirect", 9))
