@@ -35,6 +35,8 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "lightmetrica-v2_gb300"))
 
+from lmgpu.dist import aggregate_rate, dist_env, max_over_ranks, ray_stream  # noqa: E402
+
 METRIC = "Mrays/s (BVH)"
 UNIT = "Mrays/s"
 N_RANDOM, HF_RES, N_RAYS = 1_000_000, 512, 1 << 24
@@ -48,13 +50,6 @@ def workload_config(extra: dict | None = None) -> dict:
     if extra:
         c.update(extra)
     return c
-
-
-def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
 
 
 class ClockSampler:
@@ -226,7 +221,7 @@ def run_gpu(args) -> None:
 
     tris = scenes.raycast_scene(N_RANDOM, HF_RES)
     nr = args.rays
-    rays = scenes.raycast_rays(nr, stream=3 + rank)
+    rays = scenes.raycast_rays(nr, stream=ray_stream(rank))
     stream = torch.cuda.Stream()
     s = stream.cuda_stream
     acc = lmgpu.Accel()
@@ -278,17 +273,13 @@ def run_gpu(args) -> None:
     e2e_s = time.perf_counter() - t0
     barrier()
 
-    if ws > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms, e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, e2e_s = float(t[0]), float(t[1])
+    # the slowest rank's times; the rate covers all ranks' rays
+    ms, e2e_s = max_over_ranks([ms, e2e_s], device="cuda")
 
     if rank == 0:
         per_launch_s = ms / 1e3 / args.steps
-        value = ws * nr / per_launch_s / 1e6
-        e2e_value = ws * nr * e2e_steps / e2e_s / 1e6
+        value = aggregate_rate(nr, ws, per_launch_s) / 1e6
+        e2e_value = aggregate_rate(nr * e2e_steps, ws, e2e_s) / 1e6
         peak, peak_src = measured_peak()
         achieved = nr * bytes_per_ray / per_launch_s / 1e9
         traffic = traffic_per_launch()
