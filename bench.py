@@ -511,6 +511,92 @@ def run_render(args) -> None:
     sc.close()
 
 
+# renderer::vcm on the Cornell-style box: 256 x 256, 4 passes of 262,144 eye samples (4 per pixel) and
+# 262,144 photon subpaths, max_num_vertices 8, initial radius 0.02 (the box is 1 unit wide), alpha 0.7
+VCM_WORKLOAD = {"workload": "vcm_cornell_256x256_4x4spp", "width": 256, "height": 256, "max_num_vertices": 8,
+                "passes": 4, "eye_spp": 4, "photons": 262144, "initial_radius": 0.02, "alpha": 0.7,
+                "data": "synthetic (procedural Cornell box)"}
+
+
+def run_vcm(args) -> None:
+    """renderer::vcm (vertex connection and merging).  Metric Msamples/s: eye
+    samples of all passes per second, photon subpaths and the grid build
+    included; value = film left on the device (lmgpu_render_vcm_device), e2e =
+    lmgpu_render_vcm with the film and variance copied back every step."""
+    import torch
+
+    import lmgpu
+    from lmgpu import scenes
+
+    cfg = VCM_WORKLOAD
+    W, H = cfg["width"], cfg["height"]
+    eye_spp = args.spp or cfg["eye_spp"]
+    prm = dict(max_num_vertices=cfg["max_num_vertices"], num_iteration_pass=cfg["passes"],
+               num_photon_trace_samples=cfg["photons"], num_eye_trace_samples=W * H * eye_spp,
+               initial_radius=cfg["initial_radius"], alpha=cfg["alpha"], mode="vcm")
+    samples = prm["num_iteration_pass"] * prm["num_eye_trace_samples"]
+    scene = scenes.cornell_box(W, H)
+    stream = torch.cuda.Stream()
+    sc = lmgpu.Scene(scene)
+    di = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    dv = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    for k in range(args.warmup):
+        sc.render_vcm_device(di.data_ptr(), dv.data_ptr(), stream.cuda_stream, seed=k, **prm)
+    torch.cuda.synchronize()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    l0 = sc.launch_count()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            evs[k][0].record(stream)
+            sc.render_vcm_device(di.data_ptr(), dv.data_ptr(), stream.cuda_stream, seed=1000 + k, **prm)
+            evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = sc.launch_count() - l0
+    ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        sc.render_vcm(seed=2000 + k, **prm)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    line = {"metric": "Msamples/s (renderer::vcm)", "value": samples / ms / 1e3, "unit": "Msamples/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": cfg["data"],
+            "config": {"workload": cfg["workload"] if eye_spp == cfg["eye_spp"] else f"{cfg['workload']} at "
+                                                                                     f"{eye_spp} spp per pass",
+                       "width": W, "height": H, **{k: v for k, v in prm.items()},
+                       "l2": "flushed before every timed step (256 MiB write, untimed)"},
+            "e2e": {"value": samples / e2e_s / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": W * H * 3 * 4 * 2, "api": "lmgpu_render_vcm (host film)"},
+            "gpu_launches": launches, "clocks": clk}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import lmoracle
+
+        # one pass with 1/32 of the eye samples and of the photons, the radius
+        # scaled by sqrt(32): the same expected merges per eye vertex
+        threads = os.cpu_count() or 1
+        f = 32
+        cprm = dict(prm, num_iteration_pass=1, num_photon_trace_samples=prm["num_photon_trace_samples"] // f,
+                    num_eye_trace_samples=prm["num_eye_trace_samples"] // f,
+                    initial_radius=prm["initial_radius"] * f ** 0.5)
+        t0 = time.perf_counter()
+        lmoracle.render_vcm(scene, 5, threads, **cprm)
+        cpu_s = time.perf_counter() - t0
+        line["cpu_baseline"] = {
+            "value": cprm["num_eye_trace_samples"] / cpu_s / 1e6, "unit": "Msamples/s", "cores": threads,
+            "kind": "port",
+            "sample": f"one pass of {cprm['num_eye_trace_samples']} eye samples and "
+                      f"{cprm['num_photon_trace_samples']} photon subpaths at radius "
+                      f"{cprm['initial_radius']:.4f} (the same merges per eye vertex as the workload), oracle "
+                      f"restatement of renderer::vcm (renderer_vcm.cpp), {threads} threads"}
+    print(json.dumps(line), flush=True)
+    sc.close()
+
+
 def run_batch(args) -> None:
     """Batched configuration: 12 seeded sphere-grid scenes (~1.31M triangles
     each, mixed 640x360 / 1280x720 / 1920x1080), 64 spp, max depth 16
@@ -751,11 +837,12 @@ def main() -> None:
     ap.add_argument("--anyhit", action="store_true", help="time any-hit queries instead of closest hit")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel of the render workloads (profiling of "
                                                         "smaller cases; default: the workload's own)")
-    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt", "ltdirect", "batch", "guiding", "surface"],
+    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt", "ltdirect", "vcm", "batch", "guiding", "surface"],
                     default="raycast",
                     help="raycast: the BVH ray-cast configuration (default); pt: renderer::pt on the Cornell "
                          "box; bdpt: renderer::bdpt on the caustic room; ltdirect: light tracing on the Cornell "
-                         "box; batch: 12 scenes in one wavefront; "
+                         "box; vcm: vertex connection and merging on the Cornell box; batch: 12 scenes in one "
+                         "wavefront; "
                          "guiding: learned path guiding vs plain PT at equal time; surface: surface geometry "
                          "at the ray-cast hits")
     ap.add_argument("--mlp-only", action="store_true", help="guiding: time the MLP kernels only")
@@ -769,6 +856,8 @@ def main() -> None:
         run_reference(args)
     elif args.workload in RENDER_WORKLOADS:
         run_render(args)
+    elif args.workload == "vcm":
+        run_vcm(args)
     elif args.workload == "batch":
         run_batch(args)
     elif args.workload == "guiding":

@@ -268,6 +268,47 @@ int lmgpu_render_bdpt_mis(lmgpu_scene* scene, const lmgpu_pt_params* params, int
 int lmgpu_render_bdpt_mis_device(lmgpu_scene* scene, const lmgpu_pt_params* params, int mis, float* d_image,
                                  float* d_variance, void* stream);
 
+/* ---- Vertex connection and merging (renderer::vcm) ---------------------- */
+
+/* Estimators of renderer::vcm's "mode" parameter (renderer_vcm.cpp:581-587). */
+#define LMGPU_VCM_MODE_VCM 0  /* connections and merges, EvaluateMISWeight_VCM */
+#define LMGPU_VCM_MODE_BDPT 1 /* connections only, EvaluateMISWeight_BDPT */
+#define LMGPU_VCM_MODE_BDPM 2 /* merges only, EvaluateMISWeight_BDPM */
+
+/* The parameters of Renderer_VCM::Initialize (renderer_vcm.cpp:573-593),
+ * whose defaults are max_num_vertices 10, min_num_vertices 0,
+ * num_iteration_pass 100, num_photon_trace_samples 10000,
+ * num_eye_trace_samples 10000, initial_radius 0.1, alpha 0.7, mode vcm. */
+typedef struct lmgpu_vcm_params {
+    int32_t max_num_vertices;          /* 1 .. 16: subpaths have no roulette, so the cap is required */
+    int32_t min_num_vertices;
+    uint64_t num_iteration_pass;
+    uint64_t num_photon_trace_samples; /* light subpaths per pass, < 2^28 */
+    uint64_t num_eye_trace_samples;    /* eye samples per pass */
+    float initial_radius;
+    float alpha;
+    int32_t mode;                      /* LMGPU_VCM_MODE_* */
+    uint32_t seed;
+} lmgpu_vcm_params;
+
+/* Renders the scene with vertex connection and merging and writes the film
+ * as lmgpu_render_pt does (the mean of the passes' images).  Stands in for
+ * Renderer::Render of renderer::vcm (src/liblightmetrica/renderer/
+ * renderer_vcm.cpp:596-790).  Per pass k the merge radius is initial_radius,
+ * then sqrt((alpha + k) / (1 + k)) times the previous one; the photon
+ * subpaths of the pass are put in a hashed grid of cells 2r wide; every eye
+ * sample traces an eye subpath and a light subpath and combines them by all
+ * connections and by merges with the photon vertices within r of each eye
+ * vertex.  Eye samples are stratified over the pixels when
+ * num_eye_trace_samples is a multiple of W x H, uniform over the film
+ * otherwise.  Needs an area light; environment lights are rejected. */
+int lmgpu_render_vcm(lmgpu_scene* scene, const lmgpu_vcm_params* params, float* image, float* variance);
+
+/* As lmgpu_render_vcm into device buffers on `stream` (NULL: the scene's
+ * stream); returns after the render has finished. */
+int lmgpu_render_vcm_device(lmgpu_scene* scene, const lmgpu_vcm_params* params, float* d_image, float* d_variance,
+                            void* stream);
+
 /* ---- Batched path tracing: many scenes / views in one wavefront -------- */
 
 typedef struct lmgpu_batch lmgpu_batch;

@@ -93,13 +93,13 @@ int clear_film(lmgpu_scene* sc, uint64_t npix, cudaStream_t stream)
     return LMGPU_OK;
 }
 
-int finalize_film_nx(lmgpu_scene* sc, uint64_t spp, double n_x, float* d_image, float* d_variance,
+int finalize_film_nx(lmgpu_scene* sc, double spp, double n_x, float* d_image, float* d_variance,
                      cudaStream_t stream)
 {
     const uint64_t npix = (uint64_t)sc->cam.width * sc->cam.height;
     const uint32_t n3 = (uint32_t)(3 * npix);
     k_film_finalize<<<(n3 + 255) / 256, 256, 0, stream>>>(sc->film, sc->film_sq, sc->film_x, sc->film_x_sq, n3,
-                                                         (double)spp, n_x, d_image, d_variance);
+                                                         spp, n_x, d_image, d_variance);
     LMGPU_CUDA_TRY(cudaGetLastError());
     sc->launches++;
     return LMGPU_OK;
@@ -299,6 +299,7 @@ void lmgpu_scene_destroy(lmgpu_scene* sc)
     lmgpu_accel_destroy(sc->accel);
     free_bdpt(sc->bdpt);
     free_guided(sc->guided);
+    free_vcm(sc->vcm);
     void* ptrs[] = {sc->tris, sc->tri_prim, sc->prims, sc->film, sc->film_sq, sc->film_x, sc->film_x_sq,
                     sc->d_image, sc->d_variance,
                     sc->q_ray[0], sc->q_ray[1], sc->q_state[0], sc->q_state[1], sc->q_hit, sc->q_count,

@@ -53,6 +53,8 @@ struct BdptState;
 void free_bdpt(BdptState* b);
 struct GuidedState;
 void free_guided(GuidedState* g);
+struct VcmState;
+void free_vcm(VcmState* v);
 
 struct LightsGPU {
     int32_t count;
@@ -115,6 +117,7 @@ struct lmgpu_scene {
     lmgpu::BdptState* bdpt = nullptr;
     int bdpt_mis = 0;  // MIS weight of the render in progress (LMGPU_MIS_*)      // buffers of the bidirectional renderer
     lmgpu::GuidedState* guided = nullptr;  // buffers of the guided renderer
+    lmgpu::VcmState* vcm = nullptr;        // buffers of the VCM renderer
 };
 
 namespace lmgpu {
@@ -124,8 +127,9 @@ int ensure_queues(lmgpu_scene* sc, uint64_t n);
 SceneGPU scene_view(const lmgpu_scene* sc);
 int clear_film(lmgpu_scene* sc, uint64_t npix, cudaStream_t stream);
 int finalize_film(lmgpu_scene* sc, uint64_t spp, float* d_image, float* d_variance, cudaStream_t stream);
-// As finalize_film with n_x samples behind the other-samples film.
-int finalize_film_nx(lmgpu_scene* sc, uint64_t spp, double n_x, float* d_image, float* d_variance,
+// As finalize_film with spp samples per pixel (not necessarily whole) and
+// n_x samples behind the other-samples film.
+int finalize_film_nx(lmgpu_scene* sc, double spp, double n_x, float* d_image, float* d_variance,
                      cudaStream_t stream);
 // mode: 0 renderer::pt, 1 renderer::ptmis, 2 renderer::ptdirect
 int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float* d_variance, cudaStream_t stream,

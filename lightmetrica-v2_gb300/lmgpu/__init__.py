@@ -29,6 +29,7 @@ class Hit(ctypes.Structure):
 
 # renderer::bdpt's "mis" parameter -> LMGPU_MIS_*
 MIS_WEIGHTS = {"powerheuristics": 0, "simple": 1}
+VCM_MODES = {"vcm": 0, "bdpt": 1, "bdpm": 2}
 
 HIT_DTYPE = np.dtype([("t", "<f4"), ("prim", "<i4"), ("b1", "<f4"), ("b2", "<f4")])
 
@@ -104,6 +105,8 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_render_bdpt_mis.argtypes = [vp, vp, i32, vp, vp]
     L.lmgpu_render_bdpt_mis_device.argtypes = [vp, vp, i32, vp, vp, vp]
     L.lmgpu_render_ltdirect_device.argtypes = [vp, vp, vp, vp, vp]
+    L.lmgpu_render_vcm.argtypes = [vp, vp, vp, vp]
+    L.lmgpu_render_vcm_device.argtypes = [vp, vp, vp, vp, vp]
     L.lmgpu_guide_num_params.argtypes = [ctypes.POINTER(u64)]
     L.lmgpu_guide_create.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(vp)]
     L.lmgpu_guide_destroy.argtypes = [vp]
@@ -142,7 +145,8 @@ def lib() -> ctypes.CDLL:
                  "lmgpu_guide_train_step", "lmgpu_guide_forward_device", "lmgpu_guide_train_step_device",
                  "lmgpu_render_pt_guided", "lmgpu_render_pt_guided_device",
                  "lmgpu_render_ptdirect_device", "lmgpu_render_ltdirect", "lmgpu_render_ltdirect_device",
-                 "lmgpu_render_bdpt_mis", "lmgpu_render_bdpt_mis_device",
+                 "lmgpu_render_bdpt_mis", "lmgpu_render_bdpt_mis_device", "lmgpu_render_vcm",
+                 "lmgpu_render_vcm_device",
                  "lmgpu_accel_set_attributes", "lmgpu_surface", "lmgpu_surface_device",
                  "lmgpu_scene_set_environment"):
         getattr(L, name).restype = ctypes.c_int
@@ -419,10 +423,39 @@ class Scene:
                                            var.ctypes.data))
         return img, var
 
+    def render_vcm(self, **params) -> tuple[np.ndarray, np.ndarray]:
+        """renderer::vcm (keyword parameters as vcm_params): film (H, W, 3)
+        and per-pixel variance of the estimate."""
+        prm = vcm_params(**params)
+        img = np.empty((self.height, self.width, 3), np.float32)
+        var = np.empty((self.height, self.width, 3), np.float32)
+        _check(lib().lmgpu_render_vcm(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
+        return img, var
+
+    def render_vcm_device(self, d_image: int, d_variance: int, stream: int = 0, **params) -> None:
+        prm = vcm_params(**params)
+        _check(lib().lmgpu_render_vcm_device(self._h, ctypes.byref(prm), d_image, d_variance, stream))
+
     def render_bdpt_device(self, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,
                            seed: int = 0, stream: int = 0, min_num_vertices: int = 0) -> None:
         prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
         _check(lib().lmgpu_render_bdpt_device(self._h, ctypes.byref(prm), d_image, d_variance, stream))
+
+
+class VcmParams(ctypes.Structure):
+    """lmgpu_vcm_params: renderer::vcm's parameters (renderer_vcm.cpp:573-593)."""
+    _fields_ = [("max_num_vertices", ctypes.c_int32), ("min_num_vertices", ctypes.c_int32),
+                ("num_iteration_pass", ctypes.c_uint64), ("num_photon_trace_samples", ctypes.c_uint64),
+                ("num_eye_trace_samples", ctypes.c_uint64), ("initial_radius", ctypes.c_float),
+                ("alpha", ctypes.c_float), ("mode", ctypes.c_int32), ("seed", ctypes.c_uint32)]
+
+
+def vcm_params(max_num_vertices: int = 10, min_num_vertices: int = 0, num_iteration_pass: int = 100,
+               num_photon_trace_samples: int = 10000, num_eye_trace_samples: int = 10000,
+               initial_radius: float = 0.1, alpha: float = 0.7, mode: str = "vcm", seed: int = 0) -> VcmParams:
+    """renderer::vcm's parameters with the reference's defaults."""
+    return VcmParams(max_num_vertices, min_num_vertices, num_iteration_pass, num_photon_trace_samples,
+                     num_eye_trace_samples, initial_radius, alpha, VCM_MODES[mode], seed)
 
 
 class BatchParams(ctypes.Structure):

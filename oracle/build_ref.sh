@@ -2,7 +2,7 @@
 # Compiles the reference's own accel and renderer sources, in place under the
 # reference tree, into CPU oracle binaries in oracle/_ref/:
 #   ref_accel     accel::naive / bvh_sahbin / qbvh driver (single precision)
-#   ref_render    renderer::pt, bdpt, ptmis, ptdirect and ltdirect with bsdf::diffuse, bsdf::null, bsdf::flesnel,
+#   ref_render    renderer::pt, bdpt, ptmis, ptdirect, ltdirect and vcm with bsdf::diffuse, bsdf::null, bsdf::flesnel,
 #                 bsdf::cook_torrance, light::area, light::env,
 #                 sensor::pinhole, Random (dSFMT) and accel::qbvh (single)
 #   ref_render64  the same in double precision (LM_USE_DOUBLE_PRECISION,
@@ -42,7 +42,7 @@ FLAGS="-std=c++14 -O3 -msse4.2 -ffp-contract=off -w"
 L="$REF/src/liblightmetrica"
 
 ACCEL_SRCS=("$L/accel/accel_naive.cpp" "$L/accel/accel_bvh_sahbin.cpp" "$L/accel/accel_qbvh.cpp" "$HERE/refharness/ref_runtime.cpp")
-RENDER_SRCS=("$L/renderer/renderer_pt.cpp" "$L/renderer/renderer_bdpt.cpp" "$L/renderer/renderer_ptmis.cpp" "$L/renderer/renderer_ptdirect.cpp" "$L/renderer/renderer_ltdirect.cpp" "$L/asset/bsdf/bsdf_diffuse.cpp" "$L/asset/bsdf/bsdf_null.cpp"
+RENDER_SRCS=("$L/renderer/renderer_pt.cpp" "$L/renderer/renderer_bdpt.cpp" "$L/renderer/renderer_ptmis.cpp" "$L/renderer/renderer_ptdirect.cpp" "$L/renderer/renderer_ltdirect.cpp" "$L/renderer/renderer_vcm.cpp" "$L/renderer/subpathsampler.cpp" "$L/asset/bsdf/bsdf_diffuse.cpp" "$L/asset/bsdf/bsdf_null.cpp"
              "$L/asset/bsdf/bsdf_flesnel.cpp" "$L/asset/bsdf/bsdf_cooktorrance.cpp"
              "$L/asset/light/light_area.cpp" "$L/asset/light/light_env.cpp" "$L/asset/sensor/sensor_pinhole.cpp"
              "$L/random.cpp" "$HERE/refharness/ref_render_cli.cpp")

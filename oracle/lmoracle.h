@@ -140,6 +140,29 @@ uint64_t lmo_render_bdpt_mis(const float* tris, const int32_t* tri_prim, size_t 
                              uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir,
                              int mis);
 
+/* renderer::vcm (renderer_vcm.cpp:536-797): the parameters of
+ * Renderer_VCM::Initialize (:573-593); mode 0 vcm, 1 bdpt, 2 bdpm. */
+typedef struct {
+    int32_t max_num_vertices;
+    int32_t min_num_vertices;
+    uint64_t num_iteration_pass;
+    uint64_t num_photon_trace_samples;
+    uint64_t num_eye_trace_samples;
+    float initial_radius;
+    float alpha;
+    int32_t mode;
+    int32_t reserved;
+} lmo_vcm_params;
+
+/* Sums over all passes of the per-sample splats (each already scaled by
+ * W H / num_eye_trace_samples) and of their per-pixel squares; the
+ * reference's film is sum / num_iteration_pass.  Returns the eye samples
+ * processed (passes x num_eye_trace_samples); max_num_vertices outside
+ * [1, 64] renders nothing. */
+uint64_t lmo_render_vcm(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims, int nprims,
+                        const lmo_pt_camera* cam, const lmo_vcm_params* prm, uint64_t seed, int threads, double* sum,
+                        double* sumsq);
+
 /* Surface geometry of n hits (IntersectionUtils::CreateTriangleIntersection,
  * intersectionutils.h:59-135) in double precision.  tris / normals: [ntri*9]
  * per triangle in global order, already through the primitive's transform /

@@ -59,6 +59,8 @@ def lib() -> ctypes.CDLL:
         L.lmo_render_bdpt_ex.restype = ctypes.c_uint64
         L.lmo_render_bdpt_mis.argtypes = L.lmo_render_bdpt.argtypes + [ctypes.c_int, ctypes.c_int]
         L.lmo_render_bdpt_mis.restype = ctypes.c_uint64
+        L.lmo_render_vcm.argtypes = [vp, vp, sz, vp, ctypes.c_int, vp, vp, ctypes.c_uint64, ctypes.c_int, vp, vp]
+        L.lmo_render_vcm.restype = ctypes.c_uint64
         L.lmo_render_ptmis.argtypes = L.lmo_render_bdpt.argtypes
         L.lmo_render_ptmis.restype = ctypes.c_uint64
         L.lmo_render_ptdirect.argtypes = L.lmo_render_bdpt.argtypes
@@ -211,7 +213,7 @@ def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: i
     sumsq = np.frombuffer(raw[4 * n:12 * n], dtype=np.float64).reshape(H, W, 3)
     N = int(np.frombuffer(raw[12 * n:12 * n + 8], dtype=np.uint64)[0])
     return {"image": img, "variance": pixel_variance(img.astype(np.float64), sumsq, N, W * H), "samples": N,
-            "info": json.loads(out.strip().splitlines()[-1])}
+            "raw_sumsq": sumsq, "info": json.loads(out.strip().splitlines()[-1])}
 
 
 def pixel_variance(image: np.ndarray, sumsq: np.ndarray, num_samples: int, num_pixels: int) -> np.ndarray:
@@ -304,6 +306,65 @@ def render_bdpt(scene: dict, num_samples: int, max_num_vertices: int, seed: int,
                               {"powerheuristics": 0, "simple": 1}[mis])
     img = s * (W * H / num_samples)
     return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}
+
+
+VCM_MODES = {"vcm": 0, "bdpt": 1, "bdpm": 2}
+
+
+class VcmParams(ctypes.Structure):
+    _fields_ = [("max_num_vertices", ctypes.c_int32), ("min_num_vertices", ctypes.c_int32),
+                ("num_iteration_pass", ctypes.c_uint64), ("num_photon_trace_samples", ctypes.c_uint64),
+                ("num_eye_trace_samples", ctypes.c_uint64), ("initial_radius", ctypes.c_float),
+                ("alpha", ctypes.c_float), ("mode", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+def vcm_variance(image: np.ndarray, sumsq: np.ndarray, passes: int, n_eye: int) -> np.ndarray:
+    """Variance of renderer::vcm's film I = (1 / P) sum_i X_i over the M = P N_E
+    eye samples of all passes, X_i a sample's splats on the pixel (already
+    scaled by W H / N_E), treated as independent: Var(I) = M Var(X) / P^2."""
+    M = passes * n_eye
+    ex = image * passes / M
+    ex2 = sumsq / M
+    return M * np.maximum(ex2 - ex * ex, 0.0) / (passes * passes)
+
+
+def render_vcm(scene: dict, seed: int, threads: int, max_num_vertices: int = 10, min_num_vertices: int = 0,
+               num_iteration_pass: int = 100, num_photon_trace_samples: int = 10000,
+               num_eye_trace_samples: int = 10000, initial_radius: float = 0.1, alpha: float = 0.7,
+               mode: str = "vcm") -> dict:
+    """The oracle's renderer::vcm (defaults: Renderer_VCM::Initialize,
+    renderer_vcm.cpp:573-593): film (H, W, 3) and per-pixel variance."""
+    tris = np.ascontiguousarray(np.concatenate([p["tris"] for p in scene["prims"]]), dtype=np.float32)
+    tri_prim = np.concatenate([np.full(p["tris"].shape[0], i, np.int32) for i, p in enumerate(scene["prims"])])
+    W, H = scene["camera"]["width"], scene["camera"]["height"]
+    s = np.zeros((H, W, 3), np.float64)
+    q = np.zeros((H, W, 3), np.float64)
+    prims = scene_prims(scene)
+    cam = scene_camera(scene)
+    prm = VcmParams(max_num_vertices, min_num_vertices, num_iteration_pass, num_photon_trace_samples,
+                    num_eye_trace_samples, initial_radius, alpha, VCM_MODES[mode], 0)
+    n = lib().lmo_render_vcm(tris.ctypes.data, tri_prim.ctypes.data, tris.shape[0], ctypes.addressof(prims),
+                             len(scene["prims"]), ctypes.addressof(cam), ctypes.addressof(prm), seed, threads,
+                             s.ctypes.data, q.ctypes.data)
+    P = max(num_iteration_pass, 1)
+    img = s / P
+    return {"image": img, "variance": vcm_variance(img, q, P, num_eye_trace_samples), "samples": int(n)}
+
+
+def run_ref_vcm(scene: dict, seed: int, threads: int, double: bool = False, **params) -> dict:
+    """The reference's own renderer::vcm (compiled from its sources): film and
+    per-pixel variance (vcm_variance); params are renderer::vcm's
+    (max_num_vertices, num_iteration_pass, num_photon_trace_samples, ...)."""
+    prm = dict(params)
+    mnv = int(prm.pop("max_num_vertices", 10))
+    r = run_ref_render(scene, 1, mnv, seed, threads, double=double, renderer="vcm", params=prm)
+    P = int(prm.get("num_iteration_pass", 100))
+    NE = int(prm.get("num_eye_trace_samples", 10000))
+    img = r["image"].astype(np.float64)
+    # the film's own squares: per pass, per sample (ref_render writes the
+    # sums of squares of the splats as splatted, W H / N_E included)
+    sumsq = r["raw_sumsq"]
+    return {"image": img, "variance": vcm_variance(img, sumsq, P, NE), "samples": P * NE, "info": r["info"]}
 
 
 def render_ptmis(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,

@@ -1024,67 +1024,104 @@ uint64_t lmo_render_bdpt_ex(const float* tris, const int32_t* tri_prim, size_t n
                                sum, sumsq, independent_light_dir, 0);
 }
 
-uint64_t lmo_render_bdpt_mis(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
-                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
-                             uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir,
-                             int mis)
+/* Scene tables of a job: the oracle's accel::bvh_sahbin, per-light triangle
+ * lists with their area CDFs and inverse areas, and the sensor basis
+ * (scene3.cpp:213-221). */
+static void bd_job_init(bd_job* J, const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
+                        int nprims, const lmo_pt_camera* cam)
 {
-    bd_job J;
-    memset(&J, 0, sizeof(J));
-    J.mis = mis;
-    if (max_num_vertices > MAXV || max_num_vertices == -1) max_num_vertices = MAXV;
-    J.accel = lmo_accel_build(1, tris, ntri);
-    J.tris = tris;
-    J.tri_prim = tri_prim;
-    J.ntri = ntri;
-    J.prims = prims;
-    J.nprims = nprims;
-    J.prim_light = (int*)malloc(sizeof(int) * (size_t)nprims);
+    memset(J, 0, sizeof(*J));
+    J->accel = lmo_accel_build(1, tris, ntri);
+    J->tris = tris;
+    J->tri_prim = tri_prim;
+    J->ntri = ntri;
+    J->prims = prims;
+    J->nprims = nprims;
+    J->prim_light = (int*)malloc(sizeof(int) * (size_t)nprims);
     for (int i = 0; i < nprims; i++) {
-        J.prim_light[i] = -1;
-        if (prims[i].is_light) J.prim_light[i] = J.nlights++;
+        J->prim_light[i] = -1;
+        if (prims[i].is_light) J->prim_light[i] = J->nlights++;
     }
-    J.light_prims = (int*)malloc(sizeof(int) * (size_t)(J.nlights + 1));
-    J.light_tris = (int**)calloc((size_t)(J.nlights + 1), sizeof(int*));
-    J.light_cdf = (float**)calloc((size_t)(J.nlights + 1), sizeof(float*));
-    J.light_ntris = (int*)calloc((size_t)(J.nlights + 1), sizeof(int));
-    J.light_inv_area = (float*)calloc((size_t)(J.nlights + 1), sizeof(float));
+    J->light_prims = (int*)malloc(sizeof(int) * (size_t)(J->nlights + 1));
+    J->light_tris = (int**)calloc((size_t)(J->nlights + 1), sizeof(int*));
+    J->light_cdf = (float**)calloc((size_t)(J->nlights + 1), sizeof(float*));
+    J->light_ntris = (int*)calloc((size_t)(J->nlights + 1), sizeof(int));
+    J->light_inv_area = (float*)calloc((size_t)(J->nlights + 1), sizeof(float));
     for (int i = 0; i < nprims; i++) {
-        const int li = J.prim_light[i];
+        const int li = J->prim_light[i];
         if (li < 0) continue;
-        J.light_prims[li] = i;
+        J->light_prims[li] = i;
         int cnt = 0;
         for (size_t k = 0; k < ntri; k++) cnt += tri_prim[k] == i;
-        J.light_ntris[li] = cnt;
-        J.light_tris[li] = (int*)malloc(sizeof(int) * (size_t)cnt);
-        J.light_cdf[li] = (float*)malloc(sizeof(float) * (size_t)(cnt + 1));
+        J->light_ntris[li] = cnt;
+        J->light_tris[li] = (int*)malloc(sizeof(int) * (size_t)cnt);
+        J->light_cdf[li] = (float*)malloc(sizeof(float) * (size_t)(cnt + 1));
         float sa = 0.0f;
         int j = 0;
-        J.light_cdf[li][0] = 0.0f;
+        J->light_cdf[li][0] = 0.0f;
         for (size_t k = 0; k < ntri; k++) {
             if (tri_prim[k] != i) continue;
             const float* T = tris + 9 * k;
             const v3 p1 = V(T[0], T[1], T[2]), p2 = V(T[3], T[4], T[5]), p3 = V(T[6], T[7], T[8]);
             const v3 c = cross(sub(p2, p1), sub(p3, p1));
             const float area = sqrtf(dot(c, c)) * 0.5f;
-            J.light_tris[li][j] = (int)k;
-            J.light_cdf[li][j + 1] = J.light_cdf[li][j] + area;
+            J->light_tris[li][j] = (int)k;
+            J->light_cdf[li][j + 1] = J->light_cdf[li][j] + area;
             sa += area;
             j++;
         }
-        for (int q = 0; q <= cnt; q++) J.light_cdf[li][q] /= J.light_cdf[li][cnt];
-        J.light_inv_area[li] = 1.0f / sa;
+        for (int q = 0; q <= cnt; q++) J->light_cdf[li][q] /= J->light_cdf[li][cnt];
+        J->light_inv_area[li] = 1.0f / sa;
     }
-    J.eye = V(cam->eye[0], cam->eye[1], cam->eye[2]);
+    J->eye = V(cam->eye[0], cam->eye[1], cam->eye[2]);
     const v3 c = V(cam->center[0], cam->center[1], cam->center[2]);
     const v3 up = V(cam->up[0], cam->up[1], cam->up[2]);
-    J.vz = normalize(sub(J.eye, c));
-    J.vx = normalize(cross(up, J.vz));
-    J.vy = cross(J.vz, J.vx);
-    J.tan_fov = tanf(cam->fov_deg * PI_F / 180.0f * 0.5f);
-    J.aspect = (float)cam->width / (float)cam->height;
-    J.W = cam->width;
-    J.H = cam->height;
+    J->vz = normalize(sub(J->eye, c));
+    J->vx = normalize(cross(up, J->vz));
+    J->vy = cross(J->vz, J->vx);
+    J->tan_fov = tanf(cam->fov_deg * PI_F / 180.0f * 0.5f);
+    J->aspect = (float)cam->width / (float)cam->height;
+    J->W = cam->width;
+    J->H = cam->height;
+}
+
+static void bd_job_release(bd_job* J)
+{
+    for (int li = 0; li < J->nlights; li++) { free(J->light_tris[li]); free(J->light_cdf[li]); }
+    free(J->light_prims); free(J->light_tris); free(J->light_cdf); free(J->light_ntris); free(J->light_inv_area);
+    free(J->prim_light);
+    lmo_accel_free((lmo_accel*)J->accel);
+}
+
+/* Runs fn on J->threads workers, each given (J, worker index). */
+static void bd_run_workers(bd_job* J, void* (*fn)(void*), void* ctx)
+{
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)J->threads);
+    void** args = (void**)malloc(sizeof(void*) * 3 * (size_t)J->threads);
+    pthread_attr_t attr;
+    pthread_attr_init(&attr);
+    pthread_attr_setstacksize(&attr, (size_t)64 << 20);
+    for (int i = 0; i < J->threads; i++) {
+        args[3 * i] = J;
+        args[3 * i + 1] = (void*)(intptr_t)i;
+        args[3 * i + 2] = ctx;
+        pthread_create(&th[i], &attr, fn, &args[3 * i]);
+    }
+    for (int i = 0; i < J->threads; i++) pthread_join(th[i], NULL);
+    pthread_attr_destroy(&attr);
+    free(th);
+    free(args);
+}
+
+uint64_t lmo_render_bdpt_mis(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims,
+                             int nprims, const lmo_pt_camera* cam, uint64_t num_samples, int max_num_vertices,
+                             uint64_t seed, int threads, double* sum, double* sumsq, int independent_light_dir,
+                             int mis)
+{
+    bd_job J;
+    bd_job_init(&J, tris, tri_prim, ntri, prims, nprims, cam);
+    J.mis = mis;
+    if (max_num_vertices > MAXV || max_num_vertices == -1) max_num_vertices = MAXV;
     J.max_v = max_num_vertices;
     J.independent_light_dir = independent_light_dir > 0 || independent_light_dir == -4;
     J.ptmis = independent_light_dir == -4 ? 3 : (independent_light_dir < 0 ? -independent_light_dir : 0);
@@ -1096,27 +1133,405 @@ uint64_t lmo_render_bdpt_mis(const float* tris, const int32_t* tri_prim, size_t 
     memset(sum, 0, sizeof(double) * (size_t)J.W * J.H * 3);
     memset(sumsq, 0, sizeof(double) * (size_t)J.W * J.H * 3);
     pthread_mutex_init(&J.lock, NULL);
-    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)J.threads);
-    void** args = (void**)malloc(sizeof(void*) * 2 * (size_t)J.threads);
-    pthread_attr_t attr;
-    pthread_attr_init(&attr);
-    pthread_attr_setstacksize(&attr, (size_t)64 << 20);
-    if (J.nlights > 0) {
-        for (int i = 0; i < J.threads; i++) {
-            args[2 * i] = &J;
-            args[2 * i + 1] = (void*)(intptr_t)i;
-            pthread_create(&th[i], &attr, J.ptmis == 3 ? lt_worker : (J.ptmis ? ptmis_worker : bd_worker),
-                           &args[2 * i]);
-        }
-        for (int i = 0; i < J.threads; i++) pthread_join(th[i], NULL);
-    }
-    pthread_attr_destroy(&attr);
+    if (J.nlights > 0) bd_run_workers(&J, J.ptmis == 3 ? lt_worker : (J.ptmis ? ptmis_worker : bd_worker), NULL);
     pthread_mutex_destroy(&J.lock);
-    for (int li = 0; li < J.nlights; li++) { free(J.light_tris[li]); free(J.light_cdf[li]); }
-    free(J.light_prims); free(J.light_tris); free(J.light_cdf); free(J.light_ntris); free(J.light_inv_area);
-    free(J.prim_light);
-    free(th);
-    free(args);
-    lmo_accel_free((lmo_accel*)J.accel);
+    bd_job_release(&J);
     return num_samples;
+}
+
+/* ======================= renderer::vcm ====================================
+ * Restates src/liblightmetrica/renderer/renderer_vcm.cpp, the reference's
+ * naive vertex connection and merging (Georgiev et al. 2012 in the path-space
+ * form of Hachisuka et al. 2012):
+ *   SubpathSampler::TraceSubpath  subpathsampler.cpp:41-190: no roulette; a
+ *       subpath ends on a miss, on a black BSDF value or after
+ *       max_num_vertices vertices; the emitter's position and direction both
+ *       come from the direction sample uED (light_area.cpp:73-80)
+ *   VCMPath::ConnectSubpaths  :73-100     MergeSubpaths  :102-113
+ *   VCMPath::EvaluateF        :115-211    EvaluatePathPDF :213-276
+ *   EvaluateMISWeight_VCM / _BDPT / _BDPM :278-338
+ *   VCMKdTree::Build / RangeQuery :355-465: light subpath vertices 1.. that
+ *       are neither a delta position nor a delta direction, |p - x|^2 < r^2
+ *   Render :596-790: per pass the radius r = r0, then sqrt((alpha + k) /
+ *       (1 + k)) r; num_photon_trace_samples light subpaths and their range
+ *       structure; num_eye_trace_samples samples, each an eye subpath and a
+ *       fresh light subpath: connections s in [max(0, 2 - t, min - t),
+ *       min(nL, max - t)], merges at each eye vertex that is not a delta
+ *       position; splats C W H / N_E; the film is the mean of the passes.
+ * The range structure here is a grid of cells 2r wide (entries sorted by
+ * cell), which returns the same vertex set as the kd-tree.  The reference's
+ * "if (p.v == 0) return;" in the connection loop (:698-702) ends the whole
+ * sample, and does so here too.  Random numbers: one stream per photon
+ * subpath and per eye sample, keyed by (seed, pass, index). */
+
+typedef struct {
+    int mode; /* 0 vcm, 1 bdpt, 2 bdpm */
+    int min_v;
+    uint64_t n_photon, n_eye;
+    float r, inv_cell;
+    uint64_t pass;
+    /* photon subpaths: vertex k of subpath i at pool_v[i * max_v + k] */
+    pvx* pool_v;
+    int* pool_n;
+    /* range structure: eligible photon vertices sorted by cell key */
+    int64_t* keys;
+    int32_t* ent; /* subpath * 64 + vertex */
+    size_t nent;
+} vcm_ctx;
+
+static uint64_t vcm_stream(uint64_t seed, uint64_t pass, uint64_t index, uint64_t kind)
+{
+    uint64_t s = seed ^ 0x9E3779B97F4A7C15ull;
+    s = splitmix64(&s) ^ (pass * 0xD1B54A32D192ED03ull);
+    s = splitmix64(&s) ^ (index * 0xA0761D6478BD642Full) ^ kind;
+    return splitmix64(&s);
+}
+
+/* SubpathSampler::TraceSubpath (subpathsampler.cpp:41-190) */
+static int vcm_subpath(const bd_job* J, uint64_t* rng, int dir, pvx* out)
+{
+    int n = 0;
+    v3 initWo = zero3();
+    for (int step = 0; step < J->max_v; step++) {
+        if (step == 0) {
+            /* uEP (2D), uEP_C, uED (2D), uED_C in this order (:67-76) */
+            (void)rnd(rng);
+            (void)rnd(rng);
+            const float uc = rnd(rng), d0 = rnd(rng), d1 = rnd(rng);
+            (void)rnd(rng);
+            pvx v;
+            memset(&v, 0, sizeof(v));
+            if (dir == DIR_LE) {
+                sample_light_pos(J, uc, d0, d1, &v, NULL);
+                v.type = T_L;
+                initWo = to_world(v.n, cosine_hemisphere(d0, d1));
+            } else {
+                v.p = J->eye;
+                v.n = J->vz;
+                v.prim = -1;
+                v.type = T_E;
+                v.degenerated = 1;
+                const float rx = 2.0f * d0 - 1.0f, ry = 2.0f * d1 - 1.0f;
+                const v3 we = normalize(V(J->aspect * J->tan_fov * rx, J->tan_fov * ry, -1.0f));
+                initWo = add(add(mul(J->vx, we.x), mul(J->vy, we.y)), mul(J->vz, we.z));
+            }
+            out[n++] = v;
+            continue;
+        }
+        const pvx* pv = &out[n - 1];
+        v3 wi = zero3(), wo = zero3();
+        if (step == 1) {
+            wo = initWo;
+        } else {
+            wi = normalize(sub(out[n - 2].p, pv->p));
+            const float u0 = rnd(rng), u1 = rnd(rng), uc = rnd(rng);
+            if (!sample_dir(J, pv, wi, u0, u1, uc, &wo)) break; /* wo left zero: black below */
+        }
+        if (sblack(eval_dir(J, pv, pv->type, wi, wo, dir, 0))) break;
+        pvx v;
+        if (!trace(J, pv->p, wo, &v)) break;
+        out[n++] = v;
+    }
+    return n;
+}
+
+/* VCMPath::EvaluateF (renderer_vcm.cpp:115-211).  EvaluatePosition is 1 for
+ * the area lights and the pinhole without evalDelta; with it, 0 for the
+ * pinhole (a delta position). */
+static spd vcm_eval_f(const bd_job* J, const pvx* P, int n, int s, int merge)
+{
+    const int t = n - s;
+    spd fL = S1(1.0f);
+    if (s > 0) {
+        const int m = merge ? s : s - 1;
+        for (int i = 0; i < m; i++) {
+            const v3 wi = i >= 1 ? dirto(&P[i], &P[i - 1]) : zero3();
+            fL = smul(fL, eval_dir(J, &P[i], P[i].type, wi, dirto(&P[i], &P[i + 1]), DIR_LE, 0));
+            fL = sscale(fL, geometry_term(&P[i], &P[i + 1]));
+        }
+    }
+    if (sblack(fL)) return S1(0.0f);
+    spd fE = S1(1.0f);
+    if (t > 0) {
+        for (int i = n - 1; i > s; i--) {
+            const v3 wi = i < n - 1 ? dirto(&P[i], &P[i + 1]) : zero3();
+            fE = smul(fE, eval_dir(J, &P[i], P[i].type, wi, dirto(&P[i], &P[i - 1]), DIR_EL, 0));
+            fE = sscale(fE, geometry_term(&P[i], &P[i - 1]));
+        }
+    }
+    if (sblack(fE)) return S1(0.0f);
+    spd cst;
+    if (!merge) {
+        if (s == 0 && t > 0) {
+            cst = sscale(eval_dir(J, &P[0], P[0].type, zero3(), dirto(&P[0], &P[1]), DIR_EL, 0),
+                         (P[0].type & T_E) ? 0.0f : 1.0f);
+        } else if (s > 0 && t == 0) {
+            cst = S1(0.0f); /* the pinhole end: EvaluatePosition(evalDelta = true) = 0 */
+        } else {
+            const pvx *vL = &P[s - 1], *vE = &P[s];
+            const spd fsL = eval_dir(J, vL, vL->type, s - 2 >= 0 ? dirto(vL, &P[s - 2]) : zero3(), dirto(vL, vE),
+                                     DIR_LE, 1);
+            const spd fsE = eval_dir(J, vE, vE->type, s + 1 < n ? dirto(vE, &P[s + 1]) : zero3(), dirto(vE, vL),
+                                     DIR_EL, 1);
+            cst = smul(sscale(fsL, geometry_term(vL, vE)), fsE);
+        }
+    } else {
+        const pvx* v = &P[s];
+        cst = eval_dir(J, v, v->type, dirto(v, &P[s + 1]), dirto(v, &P[s - 1]), DIR_EL, 1);
+    }
+    return smul(smul(fL, cst), fE);
+}
+
+/* VCMPath::EvaluatePathPDF (renderer_vcm.cpp:213-276), area product measure */
+static float vcm_path_pdf(const bd_job* J, const pvx* P, int n, int s, int merge, float r)
+{
+    const int t = n - s;
+    if (!merge) {
+        if (s == 0 && t > 0) {
+            if (is_delta_pos(P[0].type)) return 0.0f;
+        } else if (s > 0 && t == 0) {
+            if (is_delta_pos(P[n - 1].type)) return 0.0f;
+        } else if (s > 0 && t > 0) {
+            if (is_delta_dir(J, &P[s - 1], P[s - 1].type) || is_delta_dir(J, &P[s], P[s].type)) return 0.0f;
+        }
+    } else {
+        if (s == 0 || t == 0) return 0.0f;
+        if (is_delta_pos(P[s].type) || is_delta_dir(J, &P[s], P[s].type)) return 0.0f;
+    }
+    float pdf = 1.0f;
+    if (s > 0) {
+        pdf *= pdf_pos(J, &P[0]) * emitter_pdf(J, &P[0]);
+        const int m = merge ? s : s - 1;
+        for (int i = 0; i < m; i++) {
+            const v3 wi = i >= 1 ? dirto(&P[i], &P[i - 1]) : zero3();
+            pdf *= pdf_dir(J, &P[i], P[i].type, wi, dirto(&P[i], &P[i + 1]), 0) * geometry_term(&P[i], &P[i + 1]);
+        }
+    }
+    if (t > 0) {
+        pdf *= pdf_pos(J, &P[n - 1]) * emitter_pdf(J, &P[n - 1]);
+        for (int i = n - 1; i >= s + 1; i--) {
+            const v3 wi = i + 1 < n ? dirto(&P[i], &P[i + 1]) : zero3();
+            pdf *= pdf_dir(J, &P[i], P[i].type, wi, dirto(&P[i], &P[i - 1]), 0) * geometry_term(&P[i], &P[i - 1]);
+        }
+    }
+    if (merge) pdf *= PI_F * r * r;
+    return pdf;
+}
+
+/* EvaluateMISWeight_VCM (mode 0), _BDPT (1, connections only), _BDPM (2,
+ * merges only): power heuristic, merges counted num_photon_trace_samples
+ * times (renderer_vcm.cpp:278-338) */
+static float vcm_weight(const bd_job* J, const pvx* P, int n, int s_, int merge_, float r, float n_photon, int mode)
+{
+    const float ps = vcm_path_pdf(J, P, n, s_, merge_, r);
+    float invw = 0.0f;
+    for (int s = 0; s <= n; s++)
+        for (int type = 0; type < 2; type++) {
+            if ((mode == 1 && type == 1) || (mode == 2 && type == 0)) continue;
+            const float pi = vcm_path_pdf(J, P, n, s, type, type ? r : 0.0f);
+            if (pi > 0.0f) {
+                const float q = pi / ps;
+                invw += q * q * (type ? n_photon : 1.0f);
+            }
+        }
+    return 1.0f / invw;
+}
+
+static int64_t vcm_cell_key(int64_t x, int64_t y, int64_t z)
+{
+    return ((x + (1 << 20)) << 42) | ((y + (1 << 20)) << 21) | (z + (1 << 20));
+}
+
+static int64_t vcm_cell_of(float c) { return (int64_t)floorf(c); }
+
+typedef struct { int64_t key; int32_t ent; } vcm_kv;
+
+static int vcm_kv_cmp(const void* a, const void* b)
+{
+    const vcm_kv *x = (const vcm_kv*)a, *y = (const vcm_kv*)b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    return x->ent < y->ent ? -1 : (x->ent > y->ent);
+}
+
+static void* vcm_pool_worker(void* arg)
+{
+    void** a = (void**)arg;
+    const bd_job* J = (const bd_job*)a[0];
+    const int w = (int)(intptr_t)a[1];
+    vcm_ctx* X = (vcm_ctx*)a[2];
+    const uint64_t b = X->n_photon * (uint64_t)w / (uint64_t)J->threads;
+    const uint64_t e = X->n_photon * (uint64_t)(w + 1) / (uint64_t)J->threads;
+    for (uint64_t i = b; i < e; i++) {
+        uint64_t rng = vcm_stream(J->seed, X->pass, i, 1);
+        X->pool_n[i] = vcm_subpath(J, &rng, DIR_LE, X->pool_v + i * (size_t)J->max_v);
+    }
+    return NULL;
+}
+
+static void vcm_splat(const bd_job* J, const vcm_ctx* X, splat_list* sl, const pvx* P, int n, spd C)
+{
+    float rx = 0.0f, ry = 0.0f;
+    raster_pos(J, dirto(&P[n - 1], &P[n - 2]), &rx, &ry);
+    splat_add(sl, pixel_of(J, rx, ry), sscale(sscale(C, (float)(J->W * J->H)), 1.0f / (float)X->n_eye));
+}
+
+static void* vcm_eye_worker(void* arg)
+{
+    void** a = (void**)arg;
+    bd_job* J = (bd_job*)a[0];
+    const int w = (int)(intptr_t)a[1];
+    const vcm_ctx* X = (const vcm_ctx*)a[2];
+    const int W = J->W, H = J->H, maxv = J->max_v;
+    double* sum = (double*)calloc((size_t)W * H * 3, sizeof(double));
+    double* sumsq = (double*)calloc((size_t)W * H * 3, sizeof(double));
+    splat_list* sl = (splat_list*)malloc(sizeof(splat_list));
+    pvx E[MAXV], L[MAXV], P[2 * MAXV];
+    const float r2 = X->r * X->r, nph = (float)X->n_photon;
+    const uint64_t b = X->n_eye * (uint64_t)w / (uint64_t)J->threads;
+    const uint64_t e = X->n_eye * (uint64_t)(w + 1) / (uint64_t)J->threads;
+    for (uint64_t smp = b; smp < e; smp++) {
+        sl->n = 0;
+        uint64_t rng = vcm_stream(J->seed, X->pass, smp, 2);
+        const int nE = vcm_subpath(J, &rng, DIR_EL, E);
+        const int nL = vcm_subpath(J, &rng, DIR_LE, L);
+        for (int t = 1; t <= nE; t++) {
+            if (X->mode != 2) {
+                int minS = 2 - t > 0 ? 2 - t : 0;
+                if (X->min_v - t > minS) minS = X->min_v - t;
+                const int maxS = nL < maxv - t ? nL : maxv - t;
+                for (int s = minS; s <= maxS; s++) {
+                    /* VCMPath::ConnectSubpaths */
+                    int n = 0;
+                    if (s == 0) {
+                        const pvx* v = &E[t - 1];
+                        if (v->prim < 0 || !J->prims[v->prim].is_light) continue;
+                        for (int i = t - 1; i >= 0; i--) P[n++] = E[i];
+                        P[0].type = T_L;
+                    } else {
+                        if (!visible(J, L[s - 1].p, E[t - 1].p)) continue;
+                        for (int i = 0; i < s; i++) P[n++] = L[i];
+                        for (int i = t - 1; i >= 0; i--) P[n++] = E[i];
+                    }
+                    const spd f = vcm_eval_f(J, P, n, s, 0);
+                    if (sblack(f)) continue;
+                    const float p = vcm_path_pdf(J, P, n, s, 0, 0.0f);
+                    if (p == 0.0f) goto sample_done;
+                    const float wgt = vcm_weight(J, P, n, s, 0, X->r, nph, X->mode == 0 ? 0 : 1);
+                    vcm_splat(J, X, sl, P, n, sscale(sscale(f, wgt), 1.0f / p));
+                }
+            }
+            if (X->mode != 1) {
+                const pvx* vE = &E[t - 1];
+                if (is_delta_pos(vE->type)) continue;
+                const float ic = X->inv_cell;
+                int64_t lo[3], hi[3];
+                const float c[3] = {vE->p.x, vE->p.y, vE->p.z};
+                for (int k = 0; k < 3; k++) {
+                    lo[k] = vcm_cell_of(c[k] * ic - 0.5f - 1e-3f);
+                    hi[k] = vcm_cell_of(c[k] * ic + 0.5f + 1e-3f);
+                }
+                for (int64_t cx = lo[0]; cx <= hi[0]; cx++)
+                    for (int64_t cy = lo[1]; cy <= hi[1]; cy++)
+                        for (int64_t cz = lo[2]; cz <= hi[2]; cz++) {
+                            const int64_t key = vcm_cell_key(cx, cy, cz);
+                            size_t l = 0, h = X->nent;
+                            while (l < h) {
+                                const size_t m = (l + h) / 2;
+                                if (X->keys[m] < key) l = m + 1;
+                                else h = m;
+                            }
+                            for (size_t q = l; q < X->nent && X->keys[q] == key; q++) {
+                                const int si = X->ent[q] / 64, vi = X->ent[q] % 64;
+                                const pvx* pool = X->pool_v + (size_t)si * maxv;
+                                const v3 d = sub(pool[vi].p, vE->p);
+                                if (!(dot(d, d) < r2)) continue;
+                                /* the RangeQuery callback (:729-763) */
+                                const int s = vi + 1, n = s + t - 1;
+                                if (n < X->min_v || maxv < n) continue;
+                                if (is_delta_pos(pool[vi - 1].type) || is_delta_pos(vE->type)) continue;
+                                int np = 0;
+                                for (int i = 0; i < vi; i++) P[np++] = pool[i];
+                                for (int i = t - 1; i >= 0; i--) P[np++] = E[i];
+                                const spd f = vcm_eval_f(J, P, np, vi, 1);
+                                if (sblack(f)) continue;
+                                const float p = vcm_path_pdf(J, P, np, vi, 1, X->r);
+                                if (p == 0.0f) continue;
+                                const float wgt = vcm_weight(J, P, np, vi, 1, X->r, nph, X->mode == 0 ? 0 : 2);
+                                vcm_splat(J, X, sl, P, np, sscale(sscale(f, wgt), 1.0f / p));
+                            }
+                        }
+            }
+        }
+    sample_done:
+        for (int k = 0; k < sl->n; k++)
+            for (int ch = 0; ch < 3; ch++) {
+                sum[3 * (size_t)sl->pix[k] + ch] += sl->val[k][ch];
+                sumsq[3 * (size_t)sl->pix[k] + ch] += sl->val[k][ch] * sl->val[k][ch];
+            }
+    }
+    pthread_mutex_lock(&J->lock);
+    for (size_t i = 0; i < (size_t)W * H * 3; i++) { J->sum[i] += sum[i]; J->sumsq[i] += sumsq[i]; }
+    pthread_mutex_unlock(&J->lock);
+    free(sl);
+    free(sum);
+    free(sumsq);
+    return NULL;
+}
+
+uint64_t lmo_render_vcm(const float* tris, const int32_t* tri_prim, size_t ntri, const lmo_pt_prim* prims, int nprims,
+                        const lmo_pt_camera* cam, const lmo_vcm_params* prm, uint64_t seed, int threads, double* sum,
+                        double* sumsq)
+{
+    bd_job J;
+    bd_job_init(&J, tris, tri_prim, ntri, prims, nprims, cam);
+    J.max_v = prm->max_num_vertices;
+    J.seed = seed;
+    J.threads = threads < 1 ? 1 : threads;
+    J.sum = sum;
+    J.sumsq = sumsq;
+    memset(sum, 0, sizeof(double) * (size_t)J.W * J.H * 3);
+    memset(sumsq, 0, sizeof(double) * (size_t)J.W * J.H * 3);
+    pthread_mutex_init(&J.lock, NULL);
+    uint64_t done = 0;
+    if (J.nlights > 0 && J.max_v >= 1 && J.max_v <= MAXV) {
+        vcm_ctx X;
+        memset(&X, 0, sizeof(X));
+        X.mode = prm->mode;
+        X.min_v = prm->min_num_vertices;
+        X.n_photon = X.mode == 1 ? 0 : prm->num_photon_trace_samples;
+        X.n_eye = prm->num_eye_trace_samples;
+        X.pool_v = (pvx*)malloc(sizeof(pvx) * (size_t)J.max_v * (X.n_photon ? X.n_photon : 1));
+        X.pool_n = (int*)calloc(X.n_photon ? X.n_photon : 1, sizeof(int));
+        vcm_kv* kv = (vcm_kv*)malloc(sizeof(vcm_kv) * (size_t)J.max_v * (X.n_photon ? X.n_photon : 1));
+        X.keys = (int64_t*)malloc(sizeof(int64_t) * (size_t)J.max_v * (X.n_photon ? X.n_photon : 1));
+        X.ent = (int32_t*)malloc(sizeof(int32_t) * (size_t)J.max_v * (X.n_photon ? X.n_photon : 1));
+        float r = 0.0f;
+        for (uint64_t pass = 0; pass < prm->num_iteration_pass; pass++) {
+            r = pass == 0 ? prm->initial_radius : sqrtf((prm->alpha + (float)pass) / (1.0f + (float)pass)) * r;
+            X.r = r;
+            X.inv_cell = 1.0f / (2.0f * r);
+            X.pass = pass;
+            X.nent = 0;
+            if (X.n_photon) {
+                bd_run_workers(&J, vcm_pool_worker, &X);
+                for (uint64_t i = 0; i < X.n_photon; i++)
+                    for (int k = 1; k < X.pool_n[i]; k++) {
+                        const pvx* v = &X.pool_v[i * (size_t)J.max_v + k];
+                        if (is_delta_pos(v->type) || is_delta_dir(&J, v, v->type)) continue;
+                        kv[X.nent].key = vcm_cell_key(vcm_cell_of(v->p.x * X.inv_cell), vcm_cell_of(v->p.y * X.inv_cell),
+                                                      vcm_cell_of(v->p.z * X.inv_cell));
+                        kv[X.nent].ent = (int32_t)(i * 64 + (uint64_t)k);
+                        X.nent++;
+                    }
+                qsort(kv, X.nent, sizeof(vcm_kv), vcm_kv_cmp);
+                for (size_t q = 0; q < X.nent; q++) { X.keys[q] = kv[q].key; X.ent[q] = kv[q].ent; }
+            }
+            bd_run_workers(&J, vcm_eye_worker, &X);
+            done += X.n_eye;
+        }
+        free(X.pool_v); free(X.pool_n); free(kv); free(X.keys); free(X.ent);
+    }
+    pthread_mutex_destroy(&J.lock);
+    bd_job_release(&J);
+    return done;
 }

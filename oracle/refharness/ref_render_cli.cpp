@@ -1,6 +1,7 @@
 // Command-line driver around the reference's own renderer::pt, renderer::bdpt,
-// renderer::ptmis, renderer::ptdirect and renderer::ltdirect
-// (src/liblightmetrica/renderer/renderer_{pt,bdpt,ptmis,ptdirect,ltdirect}.cpp)
+// renderer::ptmis, renderer::ptdirect, renderer::ltdirect and renderer::vcm
+// (src/liblightmetrica/renderer/renderer_{pt,bdpt,ptmis,ptdirect,ltdirect,vcm}.cpp,
+// the last with SubpathSampler, subpathsampler.cpp)
 // with the reference's own
 // bsdf::diffuse, bsdf::null, light::area, sensor::pinhole, Random (dSFMT)
 // and accel components, compiled from the reference sources as a CPU oracle.
@@ -21,6 +22,13 @@
 //                     initRng->NextUInt() in worker order, renders into its
 //                     own film, then films are accumulated and rescaled by
 //                     W*H / processed samples
+//   Parallel          Parallel::GetNumThreads / For (parallel.h:44-71,
+//                     parallel.cpp) with std::thread over contiguous index
+//                     ranges; after each index the calling thread's cloned
+//                     film (Film clones are made by renderer::vcm, one per
+//                     thread, right before its sample loop) closes its sample
+//                     for the per-pixel squares
+//   HarnessFilm::Clone  Film_HDR::Clone (copies size and contents)
 //   HarnessScene      Scene3 queries (scene3.cpp:458-539): Intersect with
 //                     [EpsIsect, Inf] then the emitter shapes (environment),
 //                     uniform light-primitive selection, the sensor, lookat
@@ -32,7 +40,7 @@
 //                     environment hit; the harness sets it to the environment
 //                     light's primitive, as a fixed scene would.
 //
-// Usage: ref_render <scene.bin> <out.bin> [pt|bdpt|ptmis|ptdirect|ltdirect] [key=value ...]
+// Usage: ref_render <scene.bin> <out.bin> [pt|bdpt|ptmis|ptdirect|ltdirect|vcm] [key=value ...]
 //        (renderer::pt by default; key=value: further renderer parameters,
 //        e.g. mis=simple, min_num_vertices=3)
 //   scene.bin: u32 magic 'LMRS', u32 version 2, u32 W, H,
@@ -65,6 +73,7 @@
 #include <lightmetrica/spectrum.h>
 #include <lightmetrica/ray.h>
 #include <lightmetrica/emitter.h>
+#include <lightmetrica/detail/parallel.h>
 
 #include <cstdint>
 #include <map>
@@ -73,6 +82,9 @@
 LM_NAMESPACE_BEGIN
 
 namespace { int g_threads = 1; }
+
+class HarnessFilm;
+namespace { std::vector<HarnessFilm*> g_clones; }  // films cloned for the current Parallel::For, by thread
 
 class HarnessProp : public PropertyNode
 {
@@ -134,6 +146,15 @@ public:
         data.assign((size_t)width * height, Vec3());
         sumsq.assign((size_t)width * height * 3, 0.0);
     };
+    LM_IMPL_F(Clone) = [this](BasicComponent* o) -> void
+    {
+        auto* f = static_cast<HarnessFilm*>(o);
+        f->width = width;
+        f->height = height;
+        f->data = data;
+        f->sumsq = sumsq;
+        g_clones.push_back(f);
+    };
 public:
     void Resize(int w, int h) { width = w; height = h; data.assign((size_t)w * h, Vec3()); sumsq.assign((size_t)w * h * 3, 0.0); }
     // Called after every sample: squares of the sample's per-pixel totals.
@@ -159,6 +180,30 @@ public:
     std::vector<double> sumsq;
     std::vector<Pending> pending;
 };
+
+// Parallel (parallel.h:44-71): contiguous index ranges over g_threads
+// std::threads; `init` is true on a thread's first index.
+auto Parallel::SetNumThreads(int numThreads) -> void { g_threads = numThreads > 0 ? numThreads : 1; }
+auto Parallel::GetNumThreads() -> int { return g_threads; }
+auto Parallel::For(long long numSamples, const std::function<void(long long index, int threadid, bool init)>& processFunc) -> void
+{
+    const int T = g_threads;
+    std::vector<std::thread> ts;
+    for (int t = 0; t < T; t++)
+    {
+        const long long b = numSamples * t / T, e = numSamples * (t + 1) / T;
+        ts.emplace_back([&, t, b, e]()
+        {
+            for (long long i = b; i < e; i++)
+            {
+                processFunc(i, t, i == b);
+                if (t < (int)g_clones.size()) g_clones[t]->EndSample();
+            }
+        });
+    }
+    for (auto& th : ts) th.join();
+    g_clones.clear();
+}
 
 class HarnessAssets : public Assets
 {
@@ -309,7 +354,7 @@ static std::string Vec3Str(const float* v)
 
 int main(int argc, char** argv)
 {
-    if (argc < 3) { std::fprintf(stderr, "usage: %s scene.bin out.bin [pt|bdpt|ptmis|ptdirect|ltdirect]\n", argv[0]); return 2; }
+    if (argc < 3) { std::fprintf(stderr, "usage: %s scene.bin out.bin [pt|bdpt|ptmis|ptdirect|ltdirect|vcm]\n", argv[0]); return 2; }
     const std::string rendererKey = std::string("renderer::") + (argc > 3 ? argv[3] : "pt");
     std::vector<char> buf;
     {
@@ -330,6 +375,9 @@ int main(int argc, char** argv)
 
     HarnessFilm film;
     film.Resize(W, H);
+    // ComponentFactory::Clone (component.h:552-572) creates through these
+    film.createFunc = []() -> Component* { return new HarnessFilm; };
+    film.releaseFunc = [](Component* c) { delete static_cast<HarnessFilm*>(c); };
     HarnessAssets assets;
     assets.film = &film;
     HarnessScene scene;

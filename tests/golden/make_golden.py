@@ -49,6 +49,12 @@ Fixtures written:
       The Cornell box rendered by the reference's own renderer::ltdirect
       (light tracing, a sensor connection at every vertex) with 64x64x16,384
       light paths, max_num_vertices 9, single and double precision.
+  cornell_vcm.npz, cornell_bdpm.npz
+      The Cornell box rendered by the reference's own renderer::vcm (vertex
+      connection and merging; SubpathSampler) at 32x32 with mode vcm and mode
+      bdpm: max_num_vertices 8, 256 passes of 8,192 photon subpaths and
+      8,192 eye samples, initial_radius 0.05, alpha 0.7; films in single and
+      double precision with variances from the film's per-sample squares.
   surface.npz
       Surface geometry at hits from the reference's own
       IntersectionUtils::CreateTriangleIntersection (intersectionutils.h),
@@ -242,6 +248,23 @@ def pt_case(sc: dict, spp: int, seed: int, renderer: str = "pt", max_num_vertice
     return out
 
 
+VCM_FIXTURE = dict(max_num_vertices=8, num_iteration_pass=256, num_photon_trace_samples=8192,
+                   num_eye_trace_samples=8192, initial_radius=0.05, alpha=0.7)
+
+
+def vcm_case(mode: str, seed: int) -> dict:
+    sc = scenes.cornell_box(32, 32)
+    prm = dict(VCM_FIXTURE, mode=mode)
+    f = lo.run_ref_vcm(sc, seed, os.cpu_count() or 8, **prm)
+    d = lo.run_ref_vcm(sc, seed + 1, os.cpu_count() or 8, double=True, **prm)
+    out = scene_arrays(sc)
+    out.update({k: np.float64(v) if isinstance(v, float) else np.int64(v) for k, v in VCM_FIXTURE.items()})
+    out.update({"mode": np.array(mode),
+                "ref_image": f["image"].astype(np.float32), "ref_variance": f["variance"].astype(np.float32),
+                "ref64_image": d["image"].astype(np.float64), "ref64_variance": d["variance"].astype(np.float64)})
+    return out
+
+
 def _rot(axis, ang):
     a = np.asarray(axis, np.float64) / np.linalg.norm(axis)
     K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
@@ -365,6 +388,9 @@ def main() -> None:
     if want("cornell_ltdirect"):
         np.savez_compressed(os.path.join(HERE, "cornell_ltdirect.npz"),
                             **pt_case(scenes.cornell_box(64, 64), 16384, 20241301, "ltdirect", 9))
+    for mode in ("vcm", "bdpm"):
+        if want(f"cornell_{mode}"):
+            np.savez_compressed(os.path.join(HERE, f"cornell_{mode}.npz"), **vcm_case(mode, 20241601))
     print("fixtures written to", HERE)
 
 

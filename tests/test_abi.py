@@ -61,7 +61,8 @@ def test_null_arguments_rejected(gpu_lib):
 
 
 @pytest.mark.parametrize("plugin", ["accel_cuda", "renderer_pt_cuda", "renderer_ptmis_cuda", "renderer_ptdirect_cuda",
-                                    "renderer_ltdirect_cuda", "renderer_bdpt_cuda", "renderer_pt_guided_cuda"])
+                                    "renderer_ltdirect_cuda", "renderer_bdpt_cuda", "renderer_pt_guided_cuda",
+                                    "renderer_vcm_cuda"])
 def test_reference_plugin_compiles_against_reference_headers(repo_dir, plugin):
     """plugin/*.cpp, the bindings a maintainer adds to the reference tree
     (accel::cuda, renderer::pt_cuda, renderer::ptmis_cuda,
