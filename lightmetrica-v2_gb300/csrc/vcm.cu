@@ -101,6 +101,7 @@ struct Subs {
 // Constants of one pass.
 struct Pass {
     float r, r2, inv_cell;  // merge radius, its square, 1 / cell width (2 r)
+    float kernel;           // pi r^2, the merge strategies' pdf factor
     float n_photon;         // num_photon_trace_samples: the merge strategies' count
     uint32_t pass, seed;
     uint32_t table_mask;    // hashed cells - 1
@@ -235,6 +236,83 @@ __global__ void __launch_bounds__(kVcThreads) k_vc_step(Ctx C, Pass X, Subs L, S
     queue_push(has, j, o, wo, active_out, rays_out, n_out);
 }
 
+// Merge bookkeeping.  A merge at eye vertex vE with photon vertex vi makes the
+// path P = x_0 .. x_{s-1} (the photon subpath up to x = x_{s-1}, s = vi),
+// vE = P[s], then the eye subpath back to the sensor.  With the light-side
+// factors a_i = pdf_dir(P[i] -> P[i+1]) G and the eye-side factors
+// b_i = pdf_dir(P[i] -> P[i-1]) G of the reference's EvaluatePathPDF, every
+// strategy's pdf divided by the merge's own, p_own = PL(s-1) a_{s-1}
+// sufE(s+1) pi r^2, splits into
+//   photon-only factors  (a_i, b_i for i <= s - 2: the photon subpath alone),
+//   four junction factors J1 = a_{s-1}, J3 = b_s, J2 = a_s, J4 = b_{s-1}
+//                        (pdfs at x and vE towards each other),
+//   eye-only factors     (a_i, b_i for i >= s + 1: the eye subpath alone),
+// so the power-heuristic sum (EvaluateMISWeight_VCM / _BDPM) is
+//   (J3 / J1)^2 (A + J4^2 B) + N + [c(s)] / (J1 K)^2 + EC0 + J2^2 (EC2 + N EM)
+// with A, B per photon vertex (k_vc_prep), EC0, EC2, EM per eye vertex, N
+// the photon count and K = pi r^2.  The same decomposition as the recursive
+// MIS of [Georgiev 2012, "Implementing vertex connection and merging"],
+// written here for this reference's pdfs and samplability rules.
+constexpr int kRecWords = 5;  // float4s of a photon vertex's prefix record
+
+// Per photon subpath: for each vertex k >= 1, the record of the light side a
+// merge there needs, about x = x_{k-1}:
+//   [0] x.p, prim      [1] x.n, type | degen << 8
+//   [2] unit direction x -> x_{k-2} (zero for k = 1), PL(k-1)
+//   [3] TL(k-1) rgb, A(k-1)     [4] B(k-1), G(x_{k-1}, x_{k-2}), 0, 0
+// TL(j) = prod_{i<j} eval_dir(x_i, LE) G(x_i, x_{i+1}) (EvaluateF's fL up to
+// x_j, exclusive), PL(j) = pdf_pos(x_0) emitter_pdf(x_0) prod_{i<j} a_i,
+// A(j) the terms of strategies split at x_j (connection x_{j-1} -- x_j over
+// K^2, vcm mode only; merge at x_j, times N), B(j) those split before x_j,
+// B(j + 1) = (b_j^2 B(j) + A(j)) / a_j^2.
+__global__ void k_vc_prep(Ctx C, Pass X, Subs P, uint32_t n, float4* __restrict__ rec)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int nv = P.n[i];
+    if (nv < 2) return;
+    const float K2 = X.kernel * X.kernel;
+    const bool conn = X.mode == MODE_VCM;
+    PV w = vunpack(P.v[i]), x = w;  // w = x_{k-2}, x = x_{k-1}
+    float tl[3] = {1.0f, 1.0f, 1.0f};
+    float PL = pdf_pos(C, x) * emitter_pdf(C, x), PLprev = 1.0f, B = 0.0f, gxw = 0.0f;
+    float3 wdir = zero3();
+    for (int k = 1; k < nv; k++) {
+        // A(k - 1)
+        const int j = k - 1;
+        const bool csamp = j == 0 ? !(x.type & T_E) : (!delta_dir(C, w, w.type) && !delta_dir(C, x, x.type));
+        const bool msamp = j >= 1 && !(x.type & T_E) && !delta_dir(C, x, x.type);
+        float A = msamp ? X.n_photon : 0.0f;
+        if (conn && csamp) {
+            const float q = PLprev / PL;
+            A += q * q / K2;
+        }
+        float4* r = rec + ((size_t)k * n + i) * kRecWords;
+        const VVtx xv = vpack(x);
+        r[0] = xv.a;
+        r[1] = xv.b;
+        r[2] = make_float4(wdir.x, wdir.y, wdir.z, PL);
+        r[3] = make_float4(tl[0], tl[1], tl[2], A);
+        r[4] = make_float4(B, gxw, 0.0f, 0.0f);
+        // advance to x_k
+        const PV nx = vunpack(P.v[(size_t)k * P.stride + i]);
+        const float3 u = dirto(x, nx);
+        const float g = geometry_term(x, nx);
+        const float a = pdf_dir(C, x, x.type, wdir, u) * g;
+        const Spd fs = eval_dir(C, x, x.type, wdir, u, DIR_LE, false);
+        for (int c = 0; c < 3; c++) tl[c] = tl[c] * fs.c[c] * g;
+        float bb = 0.0f;
+        if (j >= 1) bb = pdf_dir(C, x, x.type, u, wdir) * gxw;
+        B = (bb * bb * B + A) / (a * a);
+        PLprev = PL;
+        PL *= a;
+        wdir = dirto(nx, x);
+        gxw = g;
+        w = x;
+        x = nx;
+    }
+}
+
 __device__ __forceinline__ int3 vc_cell(float3 p, float ic)
 {
     return make_int3((int)floorf(p.x * ic), (int)floorf(p.y * ic), (int)floorf(p.z * ic));
@@ -269,8 +347,12 @@ __global__ void k_vc_hash(Ctx C, Pass X, Subs P, uint32_t n, uint64_t nt, uint32
     atomicAdd(&cnt[vc_hash(vc_cell(v.p, X.inv_cell), X.table_mask)], 1u);
 }
 
+// Each mergeable photon vertex into its bucket's range: the entry (position,
+// subpath * 16 + vertex) and, alongside, the prefix record k_vc_prep made
+// for it, so a query reads both contiguously.
 __global__ void k_vc_scatter(Ctx C, Pass X, Subs P, uint32_t n, uint64_t nt, const uint32_t* __restrict__ start,
-                             uint32_t* __restrict__ cursor, float4* __restrict__ entries)
+                             uint32_t* __restrict__ cursor, const float4* __restrict__ rec,
+                             float4* __restrict__ entries, float4* __restrict__ srec)
 {
     const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (t >= nt) return;
@@ -281,6 +363,8 @@ __global__ void k_vc_scatter(Ctx C, Pass X, Subs P, uint32_t n, uint64_t nt, con
     const uint32_t h = vc_hash(vc_cell(v.p, X.inv_cell), X.table_mask);
     const uint32_t slot = start[h] + atomicAdd(&cursor[h], 1u);
     entries[slot] = make_float4(v.p.x, v.p.y, v.p.z, __uint_as_float(i * (uint32_t)kMaxV + (uint32_t)k));
+    const size_t src = ((size_t)k * n + i) * kRecWords;
+    for (int w = 0; w < kRecWords; w++) srec[(size_t)slot * kRecWords + w] = rec[src + w];
 }
 
 // VCMPath::EvaluateF (renderer_vcm.cpp:115-211).  EvaluatePosition is 1 for
@@ -526,10 +610,14 @@ __global__ void k_vc_csplat(const uint32_t* __restrict__ items, const uint32_t* 
 // Merges at eye vertex t >= 2 of sample i (thread (i, t)): the photon
 // vertices within r (RangeQuery, :418-461) in the cells the query sphere
 // meets, each joined as photon subpath [0, vi) + eye subpath [t - 1 .. 0]
-// (MergeSubpaths, :102-113, with the callback's checks, :729-763).
-__global__ void __launch_bounds__(kVcThreads) k_vc_merge(Ctx C, Pass X, Subs Ph, Subs E, uint32_t n,
+// (MergeSubpaths, :102-113, with the callback's checks, :729-763).  The
+// contribution f w / p of each merge (EvaluateF, EvaluatePathPDF and the MIS
+// weight with merge = true) is assembled from the photon vertex's prefix
+// record, this thread's eye-side constants and the junction factors.
+__global__ void __launch_bounds__(kVcThreads) k_vc_merge(Ctx C, Pass X, Subs E, uint32_t n,
                                                          const uint32_t* __restrict__ start,
                                                          const float4* __restrict__ entries,
+                                                         const float4* __restrict__ srec,
                                                          const uint32_t* __restrict__ own_pix, float* __restrict__ own,
                                                          double* __restrict__ film_x, double* __restrict__ film_x_sq)
 {
@@ -537,10 +625,56 @@ __global__ void __launch_bounds__(kVcThreads) k_vc_merge(Ctx C, Pass X, Subs Ph,
     const uint32_t i = (uint32_t)(tq % n);
     const int t = (int)(tq / n) + 2;
     if (t > C.max_v || t > E.n[i]) return;
-    PV Ev[kMaxV];
-    for (int k = 0; k < t; k++) Ev[k] = vunpack(E.v[(size_t)k * E.stride + i]);
-    const PV& vE = Ev[t - 1];
-    if (vE.type & T_E) return;  // IsDeltaPosition of the eye vertex
+    const PV vE = vunpack(E.v[(size_t)(t - 1) * E.stride + i]);
+    // IsDeltaPosition of the eye vertex; a delta-direction vE makes p_own 0
+    if ((vE.type & T_E) || delta_dir(C, vE, vE.type)) return;
+    const PV e2 = vunpack(E.v[(size_t)(t - 2) * E.stride + i]);  // E[t-2]
+    const float3 dE2 = dirto(vE, e2);
+    const float gE2 = geometry_term(vE, e2);
+    // eye-side constants: FE (EvaluateF's fE), SEc = sufE(s+1), and the
+    // strategy sums EC0 (connection vE -- E[t-2]), EC2 (connections further
+    // along the eye subpath) and EM (merges at eye vertices E[t-2] .. E[1])
+    float fe[3] = {1.0f, 1.0f, 1.0f};
+    float SEc = 1.0f;  // pdf_pos and emitter pdf of the pinhole are 1
+    float EC0 = 0.0f, EC2 = 0.0f, EM = 0.0f;
+    {
+        // walk E[t-2] .. E[0] (path indices s+1 .. n-1): bb = b at E[e], aa = a at E[e]
+        float Pb = 1.0f, Pa = 1.0f, Pa2 = 1.0f;  // prod b_{s+1..j}, prod a_{s+1..j-1}, prod a_{s+1..j-2}
+        bool dprev = delta_dir(C, vE, vE.type);
+        PV nxt = vE;  // P[j - 1]
+        for (int e = t - 2; e >= 0; e--) {
+            const PV cur = vunpack(E.v[(size_t)e * E.stride + i]);
+            const PV prv = e >= 1 ? vunpack(E.v[(size_t)(e - 1) * E.stride + i]) : cur;  // P[j + 1]
+            const float3 to_prev = e >= 1 ? dirto(cur, prv) : zero3();
+            const float3 to_next = dirto(cur, nxt);
+            const float g = geometry_term(cur, nxt);
+            const float bb = pdf_dir(C, cur, cur.type, to_prev, to_next) * g;
+            SEc *= bb;
+            const Spd fs = eval_dir(C, cur, cur.type, to_prev, to_next, DIR_EL, false);
+            for (int c = 0; c < 3; c++) fe[c] = fe[c] * fs.c[c] * g;
+            Pb *= bb;
+            const bool dcur = delta_dir(C, cur, cur.type);
+            const int m = t - 2 - e;  // j = s + 1 + m
+            if (X.mode == MODE_VCM && !dprev && !dcur) {
+                const float q = (m == 0 ? 1.0f : Pa2) / Pb;
+                if (m == 0) EC0 = q * q / (X.kernel * X.kernel);
+                else EC2 += q * q / (X.kernel * X.kernel);
+            }
+            if (e >= 1 && !dcur) {
+                const float q = Pa / Pb;
+                EM += q * q;
+            }
+            if (e >= 1) {
+                const float aa = pdf_dir(C, cur, cur.type, to_next, to_prev) * geometry_term(cur, prv);
+                Pa2 = Pa;
+                Pa *= aa;
+            }
+            dprev = dcur;
+            nxt = cur;
+        }
+    }
+    const float N = X.n_photon, K = X.kernel;
+    const bool vcm = X.mode == MODE_VCM;
     const float ic = X.inv_cell;
     int lo[3], hi[3];
     const float c3[3] = {vE.p.x, vE.p.y, vE.p.z};
@@ -549,14 +683,12 @@ __global__ void __launch_bounds__(kVcThreads) k_vc_merge(Ctx C, Pass X, Subs Ph,
         hi[a] = (int)floorf(c3[a] * ic + 0.5f + 1e-3f);
         if (hi[a] - lo[a] > 2 || hi[a] < lo[a]) return;  // excluded by the host's radius check
     }
-    PV P[kMaxV];
     float acc[3] = {0.0f, 0.0f, 0.0f};
     bool any = false;
     for (int cx = lo[0]; cx <= hi[0]; cx++)
         for (int cy = lo[1]; cy <= hi[1]; cy++)
             for (int cz = lo[2]; cz <= hi[2]; cz++) {
-                const int3 cell = make_int3(cx, cy, cz);
-                const uint32_t h = vc_hash(cell, X.table_mask);
+                const uint32_t h = vc_hash(make_int3(cx, cy, cz), X.table_mask);
                 const uint32_t e1 = start[h + 1];
                 for (uint32_t e = start[h]; e < e1; e++) {
                     const float4 en = entries[e];
@@ -565,23 +697,49 @@ __global__ void __launch_bounds__(kVcThreads) k_vc_merge(Ctx C, Pass X, Subs Ph,
                     if (lc.x != cx || lc.y != cy || lc.z != cz) continue;  // another cell of the bucket
                     const float3 d = lp - vE.p;
                     if (!(dot3(d, d) < X.r2)) continue;
-                    const uint32_t id = __float_as_uint(en.w);
-                    const uint32_t si = id / (uint32_t)kMaxV;
-                    const int vi = (int)(id % (uint32_t)kMaxV);
+                    const int vi = (int)(__float_as_uint(en.w) % (uint32_t)kMaxV);
                     const int np = vi + t;
                     if (np < C.min_path || C.max_path < np) continue;
-                    for (int k = 0; k < vi; k++) P[k] = vunpack(Ph.v[(size_t)k * Ph.stride + si]);
-                    if (P[vi - 1].type & T_E) continue;  // IsDeltaPosition of the photon side
-                    for (int k = 0; k < t; k++) P[vi + k] = Ev[t - 1 - k];
+                    const float4* r = srec + (size_t)e * kRecWords;
+                    const float4 r2 = r[2], r3 = r[3], r4 = r[4];
+                    const PV x = vunpack(VVtx{r[0], r[1]});
+                    const float3 wdir = f3(r2.x, r2.y, r2.z);
+                    const float3 u = dirto(x, vE);
+                    const float gxv = geometry_term(x, vE);
+                    const Spd fsx = eval_dir(C, x, x.type, wdir, u, DIR_LE, false);
+                    if (black(fsx)) continue;
+                    const Spd cst = eval_dir(C, vE, vE.type, dE2, u * -1.0f, DIR_EL, true);
+                    if (black(cst)) continue;
+                    const float J1 = pdf_dir(C, x, x.type, wdir, u) * gxv;
+                    const float J3 = pdf_dir(C, vE, vE.type, dE2, u * -1.0f) * gxv;
+                    const float J2 = pdf_dir(C, vE, vE.type, u * -1.0f, dE2) * gE2;
+                    const float J4 = vi >= 2 ? pdf_dir(C, x, x.type, u, wdir) * r4.y : 0.0f;
+                    const float p = r2.w * J1 * SEc * K;
+                    if (p == 0.0f) continue;
+                    const float q = J3 / J1;
+                    float inv = q * q * (r3.w + J4 * J4 * r4.x) + N + J2 * J2 * (EC2 + N * EM) + EC0;
+                    if (vcm && !delta_dir(C, x, x.type)) {
+                        const float qc = 1.0f / (J1 * K);
+                        inv += qc * qc;
+                    }
+                    const float wgt = 1.0f / inv;
+                    if (!(wgt == wgt)) continue;
+                    bool nz = false;
                     float c[3];
-                    if (vc_contribution(C, X, P, np, vi, true, c)) {
+                    for (int k = 0; k < 3; k++) {
+                        const float fL = (k == 0 ? r3.x : k == 1 ? r3.y : r3.z) * fsx.c[k] * gxv;
+                        c[k] = fL * cst.c[k] * fe[k] * wgt / p;
+                        nz = nz || (c[k] != 0.0f && c[k] == c[k]);
+                    }
+                    if (nz) {
                         for (int k = 0; k < 3; k++) acc[k] += c[k];
                         any = true;
                     }
                 }
             }
     if (!any) return;
-    const uint32_t pix = raster_pixel(C, Ev[0], Ev[1]);
+    const PV e0 = vunpack(E.v[i]), e1v = vunpack(E.v[(size_t)E.stride + i]);
+    const uint32_t pix = raster_pixel(C, e0, e1v);
     if (pix == own_pix[i]) {
         for (int k = 0; k < 3; k++)
             if (acc[k] != 0.0f) atomicAdd(&own[3 * (size_t)i + k], acc[k]);
@@ -645,6 +803,10 @@ struct VcmState {
     uint64_t cells_cap = 0;
     float4* entries = nullptr;
     uint64_t entries_cap = 0;
+    float4* rec = nullptr;  // photon prefix records, levels x photons x kRecWords
+    uint64_t rec_cap = 0;
+    float4* srec = nullptr;  // the same, in entry order
+    uint64_t srec_cap = 0;
     void* scan_tmp = nullptr;
     uint64_t scan_tmp_cap = 0;
     uint32_t* items = nullptr;
@@ -661,7 +823,8 @@ void free_vcm(VcmState* v)
 {
     if (!v) return;
     void* ptrs[] = {v->pool, v->pool_n, v->eye, v->eye_n, v->own_pix, v->own, v->active[0], v->active[1],
-                    v->rays[0], v->rays[1], v->hits, v->counter, v->cells, v->entries, v->scan_tmp, v->items,
+                    v->rays[0], v->rays[1], v->hits, v->counter, v->cells, v->entries, v->rec, v->srec,
+                    v->scan_tmp, v->items,
                     v->c_rays, v->c_rec, v->c_hit};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -716,7 +879,7 @@ int render_vcm(lmgpu_scene* sc, const lmgpu_vcm_params* prm, float* d_image, flo
     // raise the stack limit once, up front
     {
         size_t need = 0;
-        const void* fns[] = {(const void*)k_vc_connect, (const void*)k_vc_merge};
+        const void* fns[] = {(const void*)k_vc_connect, (const void*)k_vc_merge, (const void*)k_vc_prep};
         for (const void* f : fns) {
             cudaFuncAttributes fa{};
             LMGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, f));
@@ -756,6 +919,8 @@ int render_vcm(lmgpu_scene* sc, const lmgpu_vcm_params* prm, float* d_image, flo
         (rc = grow(&V.hits, &V.hits_cap, qcap)) || (rc = grow(&V.counter, &V.counter_cap, 4)) ||
         (rc = grow(&V.cells, &V.cells_cap, 2 * ((uint64_t)table + 1))) ||
         (rc = grow(&V.entries, &V.entries_cap, NL ? NL * (levels > 1 ? levels - 1 : 1) : 1)) ||
+        (rc = grow(&V.rec, &V.rec_cap, NL ? NL * levels * kRecWords : 1)) ||
+        (rc = grow(&V.srec, &V.srec_cap, NL ? NL * (levels > 1 ? levels - 1 : 1) * kRecWords : 1)) ||
         (rc = grow(&V.items, &V.items_cap, items_per * wave)) || (rc = grow(&V.c_rays, &V.c_rays_cap, 2 * items_per * wave)) ||
         (rc = grow(&V.c_rec, &V.c_rec_cap, items_per * wave)) || (rc = grow(&V.c_hit, &V.c_hit_cap, items_per * wave)))
         return rc;
@@ -782,19 +947,23 @@ int render_vcm(lmgpu_scene* sc, const lmgpu_vcm_params* prm, float* d_image, flo
                         : sqrtf((prm->alpha + (float)pass) / (1.0f + (float)pass)) * X.r;
         X.r2 = X.r * X.r;
         X.inv_cell = 1.0f / (2.0f * X.r);
+        X.kernel = 3.14159265358979323846f * X.r * X.r;
         X.pass = (uint32_t)pass;
         if (NL) {
             if ((rc = trace_subpaths(sc, V, C, X, pool, none, (uint32_t)NL, 0, 0, KIND_PHOTON, 0, stream))) return rc;
             const uint64_t nt = NL * (levels > 1 ? levels - 1 : 1);
+            k_vc_prep<<<blocks(NL, kVcThreads), kVcThreads, 0, stream>>>(C, X, pool, (uint32_t)NL, V.rec);
+            LMGPU_CUDA_TRY(cudaGetLastError());
             LMGPU_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * ((size_t)table + 1), stream));
             k_vc_hash<<<blocks(nt, 256), 256, 0, stream>>>(C, X, pool, (uint32_t)NL, nt, cnt);
             LMGPU_CUDA_TRY(cudaGetLastError());
             size_t tmp = (size_t)V.scan_tmp_cap;
             LMGPU_CUDA_TRY(cub::DeviceScan::ExclusiveSum(V.scan_tmp, tmp, cnt, start, (int)(table + 1), stream));
             LMGPU_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * ((size_t)table + 1), stream));
-            k_vc_scatter<<<blocks(nt, 256), 256, 0, stream>>>(C, X, pool, (uint32_t)NL, nt, start, cnt, V.entries);
+            k_vc_scatter<<<blocks(nt, 256), 256, 0, stream>>>(C, X, pool, (uint32_t)NL, nt, start, cnt, V.rec,
+                                                               V.entries, V.srec);
             LMGPU_CUDA_TRY(cudaGetLastError());
-            sc->launches += 3;
+            sc->launches += 4;
         }
         for (uint64_t p0 = 0; p0 < NE; p0 += wave) {
             const uint32_t n = (uint32_t)((NE - p0) < wave ? (NE - p0) : wave);
@@ -819,7 +988,7 @@ int render_vcm(lmgpu_scene* sc, const lmgpu_vcm_params* prm, float* d_image, flo
             }
             if (mode != MODE_BDPT && NL > 0 && C.max_v >= 2) {
                 const uint64_t nq = (uint64_t)n * (levels - 1);
-                k_vc_merge<<<blocks(nq, kVcThreads), kVcThreads, 0, stream>>>(C, X, pool, eE, n, start, V.entries,
+                k_vc_merge<<<blocks(nq, kVcThreads), kVcThreads, 0, stream>>>(C, X, eE, n, start, V.entries, V.srec,
                                                                              V.own_pix, V.own, sc->film_x,
                                                                              sc->film_x_sq);
                 LMGPU_CUDA_TRY(cudaGetLastError());

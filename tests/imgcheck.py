@@ -46,24 +46,28 @@ def compare(a, va, b, vb):
             "block_max_abs_z": float(np.abs(zb).max()) if zb.size else 0.0, "zero_both": int(np.sum(~m))}
 
 
-def assert_same_image(a, va, b, vb, label=""):
+def assert_same_image(a, va, b, vb, label="", block_limit=4.5):
+    """block_limit: the bound on 8 x 8 block means; renderers whose samples
+    share random state across pixels (VCM: every eye sample of a pass merges
+    with the same photon subpaths) make neighbouring pixels correlated, which
+    the per-pixel variances do not capture, and take a wider bound."""
     s = compare(a, va, b, vb)
     assert s["n"] > 0, (label, s)
     assert abs(s["mean_z"]) < 0.25, (label, s)
     assert 0.8 < s["std_z"] < 1.2, (label, s)
     assert s["frac_gt3"] < 0.015, (label, s)
     assert max(abs(x) for x in s["total_z"]) < 4.0, (label, s)
-    assert s["block_max_abs_z"] < 4.5, (label, s)
+    assert s["block_max_abs_z"] < block_limit, (label, s)
     return s
 
 
-def assert_same_aggregates(a, va, b, vb, label=""):
+def assert_same_aggregates(a, va, b, vb, label="", block_limit=4.5):
     """Bias check for low-sample renders, whose per-pixel statistics are not
     yet normal: image totals within 4 sigma and 8 x 8 block means within 4.5
     sigma, per channel."""
     s = compare(a, va, b, vb)
     assert max(abs(x) for x in s["total_z"]) < 4.0, (label, s)
-    assert s["block_max_abs_z"] < 4.5, (label, s)
+    assert s["block_max_abs_z"] < block_limit, (label, s)
     return s
 
 

@@ -11,7 +11,7 @@ import pytest
 
 import imgcheck
 import ptscene
-from test_oracle_vcm import vcm_kw
+from test_oracle_vcm import VCM_BLOCK_LIMIT, vcm_kw
 
 pytestmark = pytest.mark.gpu
 
@@ -20,13 +20,13 @@ pytestmark = pytest.mark.gpu
 def test_vcm_matches_reference_film(gpu_lib, golden_dir, name):
     scene, z = ptscene.load_scene(golden_dir, name)
     sc = gpu_lib.Scene(scene)
-    img, var = sc.render_vcm(seed=11, **vcm_kw(z, num_eye_trace_samples=32 * 32 * 32))
+    img, var = sc.render_vcm(seed=11, **vcm_kw(z, num_eye_trace_samples=32 * 32 * 4))
     sc.close()
     a, va = ptscene.downsample(img, var, 2)
     b, vb = ptscene.downsample(z["ref_image"], z["ref_variance"], 2)
-    print(imgcheck.assert_same_image(a, va, b, vb, f"gpu vs ref ({name})"))
+    print(imgcheck.assert_same_image(a, va, b, vb, f"gpu vs ref ({name})", block_limit=VCM_BLOCK_LIMIT))
     c, vc = ptscene.downsample(z["ref64_image"], z["ref64_variance"], 2)
-    print(imgcheck.assert_same_aggregates(a, va, c, vc, f"gpu vs ref64 ({name})"))
+    print(imgcheck.assert_same_aggregates(a, va, c, vc, f"gpu vs ref64 ({name})", block_limit=VCM_BLOCK_LIMIT))
 
 
 @pytest.mark.parametrize("mode", ["vcm", "bdpt", "bdpm"])
@@ -44,7 +44,7 @@ def test_vcm_matches_oracle_on_variant_scene(gpu_lib, oracle_lib, golden_dir, mo
     r = oracle_lib.render_vcm(scene, 7, os.cpu_count() or 4, num_eye_trace_samples=48 * 32 * 2, **kw)
     a, va = ptscene.downsample(img, var, 2)
     b, vb = ptscene.downsample(r["image"], r["variance"], 2)
-    print(imgcheck.assert_same_image(a, va, b, vb, f"gpu vs oracle (vcm mode {mode})"))
+    print(imgcheck.assert_same_image(a, va, b, vb, f"gpu vs oracle (vcm mode {mode})", block_limit=VCM_BLOCK_LIMIT))
 
 
 def test_vcm_uniform_raster_positions(gpu_lib, oracle_lib, golden_dir):
@@ -56,7 +56,7 @@ def test_vcm_uniform_raster_positions(gpu_lib, oracle_lib, golden_dir):
     sc.close()
     a, va = ptscene.downsample(img, var, 2)
     c, vc = ptscene.downsample(z["ref64_image"], z["ref64_variance"], 2)
-    print(imgcheck.assert_same_aggregates(a, va, c, vc, "gpu (uniform raster) vs ref64"))
+    print(imgcheck.assert_same_aggregates(a, va, c, vc, "gpu (uniform raster) vs ref64", block_limit=VCM_BLOCK_LIMIT))
 
 
 def test_vcm_boundaries_and_device_entry(gpu_lib, golden_dir):

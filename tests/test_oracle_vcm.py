@@ -15,6 +15,13 @@ import imgcheck
 import ptscene
 
 
+# Every eye sample of a pass merges with the same photon subpaths, so
+# neighbouring pixels are correlated within a pass and the per-pixel
+# variances understate the variance of 8 x 8 block means: the block bound is
+# wider than imgcheck's default 4.5.
+VCM_BLOCK_LIMIT = 6.0
+
+
 def vcm_kw(z, **over):
     kw = {k: (float(z[k]) if k in ("initial_radius", "alpha") else int(z[k]))
           for k in ("max_num_vertices", "num_iteration_pass", "num_photon_trace_samples", "num_eye_trace_samples",
@@ -30,9 +37,9 @@ def test_oracle_vcm_matches_reference(oracle_lib, golden_dir, name):
     r = oracle_lib.render_vcm(scene, 1357, os.cpu_count() or 4, **vcm_kw(z, num_eye_trace_samples=1024))
     a, va = ptscene.downsample(r["image"], r["variance"], 2)
     b, vb = ptscene.downsample(z["ref_image"], z["ref_variance"], 2)
-    print(imgcheck.assert_same_image(a, va, b, vb, f"oracle vs ref ({name})"))
+    print(imgcheck.assert_same_image(a, va, b, vb, f"oracle vs ref ({name})", block_limit=VCM_BLOCK_LIMIT))
     c, vc = ptscene.downsample(z["ref64_image"], z["ref64_variance"], 2)
-    print(imgcheck.assert_same_aggregates(a, va, c, vc, f"oracle vs ref64 ({name})"))
+    print(imgcheck.assert_same_aggregates(a, va, c, vc, f"oracle vs ref64 ({name})", block_limit=VCM_BLOCK_LIMIT))
 
 
 def test_vcm_without_merges_is_its_bdpt_mode(oracle_lib, golden_dir):
@@ -45,7 +52,7 @@ def test_vcm_without_merges_is_its_bdpt_mode(oracle_lib, golden_dir):
     b = oracle_lib.render_vcm(scene, 99, os.cpu_count() or 4, **dict(kw, mode="bdpt"))
     a, va = ptscene.downsample(b["image"], b["variance"], 2)
     c, vc = ptscene.downsample(z["ref64_image"], z["ref64_variance"], 2)
-    print(imgcheck.assert_same_aggregates(a, va, c, vc, "oracle bdpt mode vs ref64 vcm"))
+    print(imgcheck.assert_same_aggregates(a, va, c, vc, "oracle bdpt mode vs ref64 vcm", block_limit=VCM_BLOCK_LIMIT))
     _, zb = ptscene.load_scene(golden_dir, "cornell_bdpm")
     assert zb["ref64_image"].sum() < 0.8 * z["ref64_image"].sum()
     # the light itself is black in bdpm (no strategy samples a 2-vertex path)
