@@ -607,13 +607,77 @@ __global__ void k_vc_csplat(const uint32_t* __restrict__ items, const uint32_t* 
     }
 }
 
-// Merges at eye vertex t >= 2 of sample i (thread (i, t)): the photon
+// Eye-side constants of one merge query (k_vc_merge), kept in shared memory.
+struct MergeQuery {
+    float4 p;   // vE.p, prim (int bits)
+    float4 n;   // vE.n, type | degen << 8 (bits)
+    float4 d2;  // unit direction vE -> E[t-2], G(vE, E[t-2])
+    float4 fe;  // EvaluateF's eye-side product fE (rgb), SEc = sufE(s + 1)
+    float4 ec;  // EC0, EC2, EM, unused
+};
+
+// f w / p of one merge of query q with the photon vertex whose prefix
+// record is r (see the merge bookkeeping above k_vc_prep); vi: the photon
+// vertex's index.  False if black or undefined.
+__device__ __forceinline__ bool merge_eval(const Ctx& C, const Pass& X, const MergeQuery& q, const float4* r, int vi,
+                                           float c[3])
+{
+    PV vE;
+    vE.p = f3(q.p.x, q.p.y, q.p.z);
+    vE.n = f3(q.n.x, q.n.y, q.n.z);
+    vE.prim = __float_as_int(q.p.w);
+    const uint32_t tb = __float_as_uint(q.n.w);
+    vE.type = (short)(tb & 0xffu);
+    vE.degen = (short)((tb >> 8) & 0xffu);
+    const float3 dE2 = f3(q.d2.x, q.d2.y, q.d2.z);
+    const float4 r2 = r[2], r3 = r[3], r4 = r[4];
+    const PV x = vunpack(VVtx{r[0], r[1]});
+    const float3 wdir = f3(r2.x, r2.y, r2.z);
+    const float3 u = dirto(x, vE);
+    const float3 mu = u * -1.0f;
+    const float gxv = geometry_term(x, vE);
+    const Spd fsx = eval_dir(C, x, x.type, wdir, u, DIR_LE, false);
+    if (black(fsx)) return false;
+    const Spd cst = eval_dir(C, vE, vE.type, dE2, mu, DIR_EL, true);
+    if (black(cst)) return false;
+    const float J1 = pdf_dir(C, x, x.type, wdir, u) * gxv;
+    const float J3 = pdf_dir(C, vE, vE.type, dE2, mu) * gxv;
+    const float J2 = pdf_dir(C, vE, vE.type, mu, dE2) * q.d2.w;
+    const float J4 = vi >= 2 ? pdf_dir(C, x, x.type, u, wdir) * r4.y : 0.0f;
+    const float p = r2.w * J1 * q.fe.w * X.kernel;
+    if (p == 0.0f) return false;
+    const float a = J3 / J1;
+    float inv = a * a * (r3.w + J4 * J4 * r4.x) + X.n_photon + J2 * J2 * (q.ec.y + X.n_photon * q.ec.z) + q.ec.x;
+    if (X.mode == MODE_VCM && !delta_dir(C, x, x.type)) {
+        const float qc = 1.0f / (J1 * X.kernel);
+        inv += qc * qc;
+    }
+    const float wgt = 1.0f / inv;
+    if (!(wgt == wgt)) return false;
+    const float tl[3] = {r3.x, r3.y, r3.z};
+    const float fe[3] = {q.fe.x, q.fe.y, q.fe.z};
+    bool nz = false;
+    for (int k = 0; k < 3; k++) {
+        const float fL = tl[k] * fsx.c[k] * gxv;
+        c[k] = fL * cst.c[k] * fe[k] * wgt / p;
+        nz = nz || (c[k] != 0.0f && c[k] == c[k]);
+    }
+    return nz;
+}
+
+// Merges at eye vertex t >= 2 of sample i (lane (i, t)): the photon
 // vertices within r (RangeQuery, :418-461) in the cells the query sphere
 // meets, each joined as photon subpath [0, vi) + eye subpath [t - 1 .. 0]
-// (MergeSubpaths, :102-113, with the callback's checks, :729-763).  The
-// contribution f w / p of each merge (EvaluateF, EvaluatePathPDF and the MIS
-// weight with merge = true) is assembled from the photon vertex's prefix
-// record, this thread's eye-side constants and the junction factors.
+// (MergeSubpaths, :102-113, with the callback's checks, :729-763), its
+// contribution f w / p (EvaluateF, EvaluatePathPDF and the MIS weight with
+// merge = true) assembled from the photon vertex's prefix record, the query's
+// eye-side constants and the junction factors.  A warp works in two phases:
+// every lane scans its own cells one entry per step and queues the entries
+// that pass (within r, path length allowed) in shared memory; whenever 32
+// are queued the whole warp evaluates them, one per lane, and adds each to
+// its query's shared accumulator.  So the evaluation runs on full warps
+// however the candidates are spread over the lanes.
+constexpr int kMergeQueue = 64;
 __global__ void __launch_bounds__(kVcThreads) k_vc_merge(Ctx C, Pass X, Subs E, uint32_t n,
                                                          const uint32_t* __restrict__ start,
                                                          const float4* __restrict__ entries,
@@ -621,27 +685,42 @@ __global__ void __launch_bounds__(kVcThreads) k_vc_merge(Ctx C, Pass X, Subs E, 
                                                          const uint32_t* __restrict__ own_pix, float* __restrict__ own,
                                                          double* __restrict__ film_x, double* __restrict__ film_x_sq)
 {
+    __shared__ MergeQuery sq[kVcThreads];
+    __shared__ float sacc[kVcThreads][3];
+    __shared__ uint32_t qent[kVcThreads / 32][kMergeQueue];
+    __shared__ uint8_t qlane[kVcThreads / 32][kMergeQueue];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint64_t tq = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     const uint32_t i = (uint32_t)(tq % n);
     const int t = (int)(tq / n) + 2;
-    if (t > C.max_v || t > E.n[i]) return;
-    const PV vE = vunpack(E.v[(size_t)(t - 1) * E.stride + i]);
-    // IsDeltaPosition of the eye vertex; a delta-direction vE makes p_own 0
-    if ((vE.type & T_E) || delta_dir(C, vE, vE.type)) return;
-    const PV e2 = vunpack(E.v[(size_t)(t - 2) * E.stride + i]);  // E[t-2]
-    const float3 dE2 = dirto(vE, e2);
-    const float gE2 = geometry_term(vE, e2);
-    // eye-side constants: FE (EvaluateF's fE), SEc = sufE(s+1), and the
-    // strategy sums EC0 (connection vE -- E[t-2]), EC2 (connections further
-    // along the eye subpath) and EM (merges at eye vertices E[t-2] .. E[1])
-    float fe[3] = {1.0f, 1.0f, 1.0f};
-    float SEc = 1.0f;  // pdf_pos and emitter pdf of the pinhole are 1
-    float EC0 = 0.0f, EC2 = 0.0f, EM = 0.0f;
-    {
-        // walk E[t-2] .. E[0] (path indices s+1 .. n-1): bb = b at E[e], aa = a at E[e]
+    bool valid = t <= C.max_v && t <= E.n[i];
+    PV vE;
+    if (valid) {
+        vE = vunpack(E.v[(size_t)(t - 1) * E.stride + i]);
+        // IsDeltaPosition of the eye vertex; a delta-direction vE makes p_own 0
+        valid = !(vE.type & T_E) && !delta_dir(C, vE, vE.type);
+    }
+    sacc[threadIdx.x][0] = sacc[threadIdx.x][1] = sacc[threadIdx.x][2] = 0.0f;
+    int lo[3] = {0, 0, 0}, ext[3] = {1, 1, 1};
+    if (valid) {
+        const PV e2 = vunpack(E.v[(size_t)(t - 2) * E.stride + i]);  // E[t-2]
+        MergeQuery q;
+        const VVtx ev = vpack(vE);
+        q.p = ev.a;
+        q.n = ev.b;
+        const float3 dE2 = dirto(vE, e2);
+        q.d2 = make_float4(dE2.x, dE2.y, dE2.z, geometry_term(vE, e2));
+        // eye-side constants: FE (EvaluateF's fE), SEc = sufE(s+1), and the
+        // strategy sums EC0 (connection vE -- E[t-2]), EC2 (connections
+        // further along the eye subpath), EM (merges at E[t-2] .. E[1])
+        float fe[3] = {1.0f, 1.0f, 1.0f};
+        float SEc = 1.0f;  // pdf_pos and emitter pdf of the pinhole are 1
+        float EC0 = 0.0f, EC2 = 0.0f, EM = 0.0f;
+        // walk E[t-2] .. E[0] (path indices j = s+1 .. n-1)
         float Pb = 1.0f, Pa = 1.0f, Pa2 = 1.0f;  // prod b_{s+1..j}, prod a_{s+1..j-1}, prod a_{s+1..j-2}
-        bool dprev = delta_dir(C, vE, vE.type);
-        PV nxt = vE;  // P[j - 1]
+        bool dprev = false;  // vE is not a delta direction
+        PV nxt = vE;         // P[j - 1]
+        const float K2 = X.kernel * X.kernel;
         for (int e = t - 2; e >= 0; e--) {
             const PV cur = vunpack(E.v[(size_t)e * E.stride + i]);
             const PV prv = e >= 1 ? vunpack(E.v[(size_t)(e - 1) * E.stride + i]) : cur;  // P[j + 1]
@@ -651,18 +730,17 @@ __global__ void __launch_bounds__(kVcThreads) k_vc_merge(Ctx C, Pass X, Subs E, 
             const float bb = pdf_dir(C, cur, cur.type, to_prev, to_next) * g;
             SEc *= bb;
             const Spd fs = eval_dir(C, cur, cur.type, to_prev, to_next, DIR_EL, false);
-            for (int c = 0; c < 3; c++) fe[c] = fe[c] * fs.c[c] * g;
+            for (int k = 0; k < 3; k++) fe[k] = fe[k] * fs.c[k] * g;
             Pb *= bb;
             const bool dcur = delta_dir(C, cur, cur.type);
-            const int m = t - 2 - e;  // j = s + 1 + m
             if (X.mode == MODE_VCM && !dprev && !dcur) {
-                const float q = (m == 0 ? 1.0f : Pa2) / Pb;
-                if (m == 0) EC0 = q * q / (X.kernel * X.kernel);
-                else EC2 += q * q / (X.kernel * X.kernel);
+                const float qq = (e == t - 2 ? 1.0f : Pa2) / Pb;
+                if (e == t - 2) EC0 = qq * qq / K2;
+                else EC2 += qq * qq / K2;
             }
             if (e >= 1 && !dcur) {
-                const float q = Pa / Pb;
-                EM += q * q;
+                const float qq = Pa / Pb;
+                EM += qq * qq;
             }
             if (e >= 1) {
                 const float aa = pdf_dir(C, cur, cur.type, to_next, to_prev) * geometry_term(cur, prv);
@@ -672,72 +750,79 @@ __global__ void __launch_bounds__(kVcThreads) k_vc_merge(Ctx C, Pass X, Subs E, 
             dprev = dcur;
             nxt = cur;
         }
+        q.fe = make_float4(fe[0], fe[1], fe[2], SEc);
+        q.ec = make_float4(EC0, EC2, EM, 0.0f);
+        sq[threadIdx.x] = q;
+        const float c3[3] = {vE.p.x, vE.p.y, vE.p.z};
+        for (int a = 0; a < 3; a++) {
+            lo[a] = (int)floorf(c3[a] * X.inv_cell - 0.5f - 1e-3f);
+            const int hi = (int)floorf(c3[a] * X.inv_cell + 0.5f + 1e-3f);
+            ext[a] = hi - lo[a] + 1;
+            if (ext[a] > 3 || ext[a] < 1) valid = false;  // excluded by the host's radius check
+        }
     }
-    const float N = X.n_photon, K = X.kernel;
-    const bool vcm = X.mode == MODE_VCM;
-    const float ic = X.inv_cell;
-    int lo[3], hi[3];
-    const float c3[3] = {vE.p.x, vE.p.y, vE.p.z};
-    for (int a = 0; a < 3; a++) {
-        lo[a] = (int)floorf(c3[a] * ic - 0.5f - 1e-3f);
-        hi[a] = (int)floorf(c3[a] * ic + 0.5f + 1e-3f);
-        if (hi[a] - lo[a] > 2 || hi[a] < lo[a]) return;  // excluded by the host's radius check
-    }
-    float acc[3] = {0.0f, 0.0f, 0.0f};
-    bool any = false;
-    for (int cx = lo[0]; cx <= hi[0]; cx++)
-        for (int cy = lo[1]; cy <= hi[1]; cy++)
-            for (int cz = lo[2]; cz <= hi[2]; cz++) {
+    const int ncell = valid ? ext[0] * ext[1] * ext[2] : 0;
+    int cell = 0, cx = 0, cy = 0, cz = 0;
+    uint32_t e = 0, e1 = 0;
+    int qn = 0;  // queued entries (warp-uniform)
+    __syncwarp();
+    for (;;) {
+        // scan: the next entry of this lane's query, if any
+        bool has = false;
+        uint32_t he = 0;
+        if (valid) {
+            while (e >= e1 && cell < ncell) {
+                cx = lo[0] + cell % ext[0];
+                cy = lo[1] + (cell / ext[0]) % ext[1];
+                cz = lo[2] + cell / (ext[0] * ext[1]);
                 const uint32_t h = vc_hash(make_int3(cx, cy, cz), X.table_mask);
-                const uint32_t e1 = start[h + 1];
-                for (uint32_t e = start[h]; e < e1; e++) {
-                    const float4 en = entries[e];
-                    const float3 lp = f3(en.x, en.y, en.z);
-                    const int3 lc = vc_cell(lp, ic);
-                    if (lc.x != cx || lc.y != cy || lc.z != cz) continue;  // another cell of the bucket
-                    const float3 d = lp - vE.p;
-                    if (!(dot3(d, d) < X.r2)) continue;
-                    const int vi = (int)(__float_as_uint(en.w) % (uint32_t)kMaxV);
-                    const int np = vi + t;
-                    if (np < C.min_path || C.max_path < np) continue;
-                    const float4* r = srec + (size_t)e * kRecWords;
-                    const float4 r2 = r[2], r3 = r[3], r4 = r[4];
-                    const PV x = vunpack(VVtx{r[0], r[1]});
-                    const float3 wdir = f3(r2.x, r2.y, r2.z);
-                    const float3 u = dirto(x, vE);
-                    const float gxv = geometry_term(x, vE);
-                    const Spd fsx = eval_dir(C, x, x.type, wdir, u, DIR_LE, false);
-                    if (black(fsx)) continue;
-                    const Spd cst = eval_dir(C, vE, vE.type, dE2, u * -1.0f, DIR_EL, true);
-                    if (black(cst)) continue;
-                    const float J1 = pdf_dir(C, x, x.type, wdir, u) * gxv;
-                    const float J3 = pdf_dir(C, vE, vE.type, dE2, u * -1.0f) * gxv;
-                    const float J2 = pdf_dir(C, vE, vE.type, u * -1.0f, dE2) * gE2;
-                    const float J4 = vi >= 2 ? pdf_dir(C, x, x.type, u, wdir) * r4.y : 0.0f;
-                    const float p = r2.w * J1 * SEc * K;
-                    if (p == 0.0f) continue;
-                    const float q = J3 / J1;
-                    float inv = q * q * (r3.w + J4 * J4 * r4.x) + N + J2 * J2 * (EC2 + N * EM) + EC0;
-                    if (vcm && !delta_dir(C, x, x.type)) {
-                        const float qc = 1.0f / (J1 * K);
-                        inv += qc * qc;
-                    }
-                    const float wgt = 1.0f / inv;
-                    if (!(wgt == wgt)) continue;
-                    bool nz = false;
-                    float c[3];
-                    for (int k = 0; k < 3; k++) {
-                        const float fL = (k == 0 ? r3.x : k == 1 ? r3.y : r3.z) * fsx.c[k] * gxv;
-                        c[k] = fL * cst.c[k] * fe[k] * wgt / p;
-                        nz = nz || (c[k] != 0.0f && c[k] == c[k]);
-                    }
-                    if (nz) {
-                        for (int k = 0; k < 3; k++) acc[k] += c[k];
-                        any = true;
-                    }
-                }
+                e = start[h];
+                e1 = start[h + 1];
+                cell++;
             }
-    if (!any) return;
+            if (e < e1) {
+                const float4 en = entries[e];
+                const float3 lp = f3(en.x, en.y, en.z);
+                const int3 lc = vc_cell(lp, X.inv_cell);
+                const float3 d = lp - vE.p;
+                const int np = (int)(__float_as_uint(en.w) % (uint32_t)kMaxV) + t;
+                has = lc.x == cx && lc.y == cy && lc.z == cz && dot3(d, d) < X.r2 && np >= C.min_path &&
+                      np <= C.max_path;
+                he = e;
+                e++;
+            }
+        }
+        const bool more = valid && (e < e1 || cell < ncell);
+        const unsigned m = __ballot_sync(0xffffffffu, has);
+        if (has) {
+            const int pos = qn + __popc(m & ((1u << lane) - 1u));
+            qent[warp][pos] = he;
+            qlane[warp][pos] = (uint8_t)lane;
+        }
+        qn += __popc(m);
+        const bool any_more = __any_sync(0xffffffffu, more);
+        __syncwarp();
+        // evaluate: 32 queued entries at a time, or the rest at the end
+        while (qn >= 32 || (!any_more && qn > 0)) {
+            const int take = qn < 32 ? qn : 32;
+            if ((int)lane < take) {
+                const int idx = qn - take + (int)lane;
+                const uint32_t ee = qent[warp][idx];
+                const unsigned ql = qlane[warp][idx];
+                const int vi = (int)(__float_as_uint(entries[ee].w) % (uint32_t)kMaxV);
+                float c[3];
+                if (merge_eval(C, X, sq[warp * 32 + ql], srec + (size_t)ee * kRecWords, vi, c))
+                    for (int k = 0; k < 3; k++) atomicAdd(&sacc[warp * 32 + ql][k], c[k]);
+            }
+            qn -= take;
+            __syncwarp();
+        }
+        if (!any_more) break;
+    }
+    __syncwarp();
+    if (!valid) return;
+    const float acc[3] = {sacc[threadIdx.x][0], sacc[threadIdx.x][1], sacc[threadIdx.x][2]};
+    if (acc[0] == 0.0f && acc[1] == 0.0f && acc[2] == 0.0f) return;
     const PV e0 = vunpack(E.v[i]), e1v = vunpack(E.v[(size_t)E.stride + i]);
     const uint32_t pix = raster_pixel(C, e0, e1v);
     if (pix == own_pix[i]) {
