@@ -296,7 +296,7 @@ typedef struct lmgpu_vcm_params {
  * Renderer::Render of renderer::vcm (src/liblightmetrica/renderer/
  * renderer_vcm.cpp:596-790).  Per pass k the merge radius is initial_radius,
  * then sqrt((alpha + k) / (1 + k)) times the previous one; the photon
- * subpaths of the pass are put in a hashed grid of cells 2r wide; every eye
+ * subpaths of the pass are put in a hashed grid of cells r wide; every eye
  * sample traces an eye subpath and a light subpath and combines them by all
  * connections and by merges with the photon vertices within r of each eye
  * vertex.  Eye samples are stratified over the pixels when

@@ -30,7 +30,7 @@
 //   photons     k_vc_start, then (closest-hit traversal, k_vc_step) for each
 //               further vertex; queue lengths stay on the device;
 //   grid        k_vc_hash counts the mergeable photon vertices per hashed
-//               cell (cells 2r wide, so a query visits 2 x 2 x 2 cells), an
+//               cell (cells r wide, so a query visits 3 x 3 x 3 cells), an
 //               exclusive scan gives each bucket its range, k_vc_scatter
 //               writes (position, subpath | vertex) entries into the ranges;
 //   eye waves   eye and light subpaths of up to kWave samples (as for the
@@ -100,7 +100,7 @@ struct Subs {
 
 // Constants of one pass.
 struct Pass {
-    float r, r2, inv_cell;  // merge radius, its square, 1 / cell width (2 r)
+    float r, r2, inv_cell;  // merge radius, its square, 1 / cell width (r)
     float kernel;           // pi r^2, the merge strategies' pdf factor
     float n_photon;         // num_photon_trace_samples: the merge strategies' count
     uint32_t pass, seed;
@@ -755,10 +755,10 @@ __global__ void __launch_bounds__(kVcThreads) k_vc_merge(Ctx C, Pass X, Subs E, 
         sq[threadIdx.x] = q;
         const float c3[3] = {vE.p.x, vE.p.y, vE.p.z};
         for (int a = 0; a < 3; a++) {
-            lo[a] = (int)floorf(c3[a] * X.inv_cell - 0.5f - 1e-3f);
-            const int hi = (int)floorf(c3[a] * X.inv_cell + 0.5f + 1e-3f);
+            lo[a] = (int)floorf(c3[a] * X.inv_cell - 1.0f - 1e-3f);
+            const int hi = (int)floorf(c3[a] * X.inv_cell + 1.0f + 1e-3f);
             ext[a] = hi - lo[a] + 1;
-            if (ext[a] > 3 || ext[a] < 1) valid = false;  // excluded by the host's radius check
+            if (ext[a] > 4 || ext[a] < 1) valid = false;  // excluded by the host's radius check
         }
     }
     const int ncell = valid ? ext[0] * ext[1] * ext[2] : 0;
@@ -1031,7 +1031,7 @@ int render_vcm(lmgpu_scene* sc, const lmgpu_vcm_params* prm, float* d_image, flo
         X.r = pass == 0 ? prm->initial_radius
                         : sqrtf((prm->alpha + (float)pass) / (1.0f + (float)pass)) * X.r;
         X.r2 = X.r * X.r;
-        X.inv_cell = 1.0f / (2.0f * X.r);
+        X.inv_cell = 1.0f / X.r;
         X.kernel = 3.14159265358979323846f * X.r * X.r;
         X.pass = (uint32_t)pass;
         if (NL) {
@@ -1133,7 +1133,7 @@ int render_vcm_checked(const char* name, lmgpu_scene* sc, const lmgpu_vcm_params
             r = sqrtf((prm->alpha + (float)k) / (1.0f + (float)k)) * r;
         float extent = sc->sphere_radius;
         for (int a = 0; a < 3; a++) extent += fabsf(sc->sphere_center[a]);
-        if (!(r > 0.0f) || !(extent / (2.0f * r) < 4194304.0f)) {
+        if (!(r > 0.0f) || !(extent / r < 4194304.0f)) {
             set_error(std::string(name) + ": the merge radius schedule (initial_radius, alpha) falls to " +
                       std::to_string(r) + ", too small for the scene's extent");
             return LMGPU_ERR_INVALID;
