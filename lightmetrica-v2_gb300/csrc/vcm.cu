@@ -678,7 +678,9 @@ __device__ __forceinline__ bool merge_eval(const Ctx& C, const Pass& X, const Me
 // its query's shared accumulator.  So the evaluation runs on full warps
 // however the candidates are spread over the lanes.
 constexpr int kMergeQueue = 64;
-__global__ void __launch_bounds__(kVcThreads) k_vc_merge(Ctx C, Pass X, Subs E, uint32_t n,
+// 8 blocks per SM (64 registers, a few spills): the scan phase waits on
+// memory, and twice the warps of the unbounded 96-register build hide more of it.
+__global__ void __launch_bounds__(kVcThreads, 8) k_vc_merge(Ctx C, Pass X, Subs E, uint32_t n,
                                                          const uint32_t* __restrict__ start,
                                                          const float4* __restrict__ entries,
                                                          const float4* __restrict__ srec,
