@@ -40,12 +40,17 @@
 //                             counter;
 //               k_vc_connect  contribution and shadow ray per item, any-hit
 //                             traversal, k_vc_csplat adds the unoccluded;
-//               k_vc_merge    one thread per (sample, eye vertex t >= 2): the
-//                             cells around the vertex, each photon vertex
-//                             within r evaluated as a merge;
+//               k_vc_qkeys    the merge queries (sample, eye vertex t >= 2)
+//                             keyed by the Morton code of the eye vertex,
+//                             radix-sorted, so neighbouring lanes scan the
+//                             same cells;
+//               k_vc_merge    one lane per query: the cells around the
+//                             vertex, each photon vertex within r evaluated
+//                             as a merge;
 //               k_vc_flush    each sample's own-pixel sum into the film.
 // Subpath vertices are 32-byte records [vertex k][subpath] in HBM; random
 // numbers are Philox keyed by (seed, pass, subpath kind, index, step).
+#include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
 #include "interact.cuh"
@@ -607,6 +612,39 @@ __global__ void k_vc_csplat(const uint32_t* __restrict__ items, const uint32_t* 
     }
 }
 
+__device__ __forceinline__ uint32_t morton_spread10(uint32_t x)
+{
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000ffu;
+    x = (x | (x << 8)) & 0x0300f00fu;
+    x = (x | (x << 4)) & 0x030c30c3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+// Sort key of merge query q = (i, t), i = q mod n, t = q / n + 2: the Morton
+// code of its eye vertex in the scene's bounding cube (10 bits per axis), so
+// that the queries a warp takes after sorting lie close together and scan
+// the same cells; queries without an eye vertex t sort last.
+__global__ void k_vc_qkeys(Ctx C, Subs E, uint32_t n, uint32_t nq, float3 lo, float inv_size,
+                           uint32_t* __restrict__ keys, uint32_t* __restrict__ vals)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const uint32_t i = q % n;
+    const int t = (int)(q / n) + 2;
+    uint32_t key = 0xffffffffu;
+    if (t <= C.max_v && t <= E.n[i]) {
+        const float4 a = E.v[(size_t)(t - 1) * E.stride + i].a;
+        const float c[3] = {(a.x - lo.x) * inv_size, (a.y - lo.y) * inv_size, (a.z - lo.z) * inv_size};
+        uint32_t m[3];
+        for (int k = 0; k < 3; k++) m[k] = (uint32_t)fminf(fmaxf(c[k] * 1024.0f, 0.0f), 1023.0f);
+        key = morton_spread10(m[0]) | (morton_spread10(m[1]) << 1) | (morton_spread10(m[2]) << 2);
+    }
+    keys[q] = key;
+    vals[q] = q;
+}
+
 // Eye-side constants of one merge query (k_vc_merge), kept in shared memory.
 struct MergeQuery {
     float4 p;   // vE.p, prim (int bits)
@@ -680,7 +718,8 @@ __device__ __forceinline__ bool merge_eval(const Ctx& C, const Pass& X, const Me
 constexpr int kMergeQueue = 64;
 // 8 blocks per SM (64 registers, a few spills): the scan phase waits on
 // memory, and twice the warps of the unbounded 96-register build hide more of it.
-__global__ void __launch_bounds__(kVcThreads, 8) k_vc_merge(Ctx C, Pass X, Subs E, uint32_t n,
+__global__ void __launch_bounds__(kVcThreads, 8) k_vc_merge(Ctx C, Pass X, Subs E, uint32_t n, uint32_t nq,
+                                                         const uint32_t* __restrict__ order,
                                                          const uint32_t* __restrict__ start,
                                                          const float4* __restrict__ entries,
                                                          const float4* __restrict__ srec,
@@ -692,10 +731,11 @@ __global__ void __launch_bounds__(kVcThreads, 8) k_vc_merge(Ctx C, Pass X, Subs 
     __shared__ uint32_t qent[kVcThreads / 32][kMergeQueue];
     __shared__ uint8_t qlane[kVcThreads / 32][kMergeQueue];
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint64_t tq = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    const uint32_t i = (uint32_t)(tq % n);
-    const int t = (int)(tq / n) + 2;
-    bool valid = t <= C.max_v && t <= E.n[i];
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t qid = slot < nq ? order[slot] : 0u;
+    const uint32_t i = qid % n;
+    const int t = (int)(qid / n) + 2;
+    bool valid = slot < nq && t <= C.max_v && t <= E.n[i];
     PV vE;
     if (valid) {
         vE = vunpack(E.v[(size_t)(t - 1) * E.stride + i]);
@@ -896,6 +936,10 @@ struct VcmState {
     uint64_t srec_cap = 0;
     void* scan_tmp = nullptr;
     uint64_t scan_tmp_cap = 0;
+    uint32_t* qkeys = nullptr;  // merge query sort: keys and ids, double-buffered (4 x queries)
+    uint64_t qkeys_cap = 0;
+    void* sort_tmp = nullptr;
+    uint64_t sort_tmp_cap = 0;
     uint32_t* items = nullptr;
     uint64_t items_cap = 0;
     float4* c_rays = nullptr;
@@ -911,7 +955,7 @@ void free_vcm(VcmState* v)
     if (!v) return;
     void* ptrs[] = {v->pool, v->pool_n, v->eye, v->eye_n, v->own_pix, v->own, v->active[0], v->active[1],
                     v->rays[0], v->rays[1], v->hits, v->counter, v->cells, v->entries, v->rec, v->srec,
-                    v->scan_tmp, v->items,
+                    v->scan_tmp, v->qkeys, v->sort_tmp, v->items,
                     v->c_rays, v->c_rec, v->c_hit};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -1016,6 +1060,20 @@ int render_vcm(lmgpu_scene* sc, const lmgpu_vcm_params* prm, float* d_image, flo
     size_t scan_bytes = 0;
     LMGPU_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, cnt, start, (int)(table + 1), stream));
     if ((rc = grow((char**)&V.scan_tmp, &V.scan_tmp_cap, scan_bytes))) return rc;
+    // merge queries (sample, eye vertex t >= 2) of a wave, sorted by position
+    const uint64_t nq_max = wave * (levels > 1 ? levels - 1 : 1);
+    if ((rc = grow(&V.qkeys, &V.qkeys_cap, 4 * nq_max))) return rc;
+    size_t sort_bytes = 0;
+    LMGPU_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, V.qkeys, V.qkeys + nq_max, V.qkeys + 2 * nq_max,
+                                                   V.qkeys + 3 * nq_max, (int)nq_max, 0, 32, stream));
+    if ((rc = grow((char**)&V.sort_tmp, &V.sort_tmp_cap, sort_bytes))) return rc;
+    float3 scene_lo;
+    float scene_inv = 1.0f;
+    {
+        const float R = sc->sphere_radius > 0.0f ? sc->sphere_radius : 1.0f;
+        scene_lo = make_float3(sc->sphere_center[0] - R, sc->sphere_center[1] - R, sc->sphere_center[2] - R);
+        scene_inv = 1.0f / (2.0f * R);
+    }
 
     Subs pool{V.pool, V.pool_n, (uint32_t)(NL ? NL : 1)};
     Subs eL{V.eye, V.eye_n, (uint32_t)wave};
@@ -1074,12 +1132,19 @@ int render_vcm(lmgpu_scene* sc, const lmgpu_vcm_params* prm, float* d_image, flo
                 sc->launches += 3;
             }
             if (mode != MODE_BDPT && NL > 0 && C.max_v >= 2) {
-                const uint64_t nq = (uint64_t)n * (levels - 1);
-                k_vc_merge<<<blocks(nq, kVcThreads), kVcThreads, 0, stream>>>(C, X, eE, n, start, V.entries, V.srec,
-                                                                             V.own_pix, V.own, sc->film_x,
+                const uint32_t nq = (uint32_t)((uint64_t)n * (levels - 1));
+                uint32_t *kin = V.qkeys, *kout = V.qkeys + nq_max, *vin = V.qkeys + 2 * nq_max,
+                         *vout = V.qkeys + 3 * nq_max;
+                k_vc_qkeys<<<blocks(nq, 256), 256, 0, stream>>>(C, eE, n, nq, scene_lo, scene_inv, kin, vin);
+                LMGPU_CUDA_TRY(cudaGetLastError());
+                size_t sb = (size_t)V.sort_tmp_cap;
+                LMGPU_CUDA_TRY(cub::DeviceRadixSort::SortPairs(V.sort_tmp, sb, kin, kout, vin, vout, (int)nq, 0, 32,
+                                                               stream));
+                k_vc_merge<<<blocks(nq, kVcThreads), kVcThreads, 0, stream>>>(C, X, eE, n, nq, vout, start, V.entries,
+                                                                             V.srec, V.own_pix, V.own, sc->film_x,
                                                                              sc->film_x_sq);
                 LMGPU_CUDA_TRY(cudaGetLastError());
-                sc->launches++;
+                sc->launches += 2;
             }
             k_vc_flush<<<blocks(n, 256), 256, 0, stream>>>(n, V.own_pix, V.own, sc->film, sc->film_sq);
             LMGPU_CUDA_TRY(cudaGetLastError());
