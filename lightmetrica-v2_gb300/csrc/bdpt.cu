@@ -50,9 +50,11 @@ constexpr int kMaxV = 16;
 // Connection work items are grouped by strategy (s, t), bucket s * kStrideST + t.
 constexpr int kStrideST = kMaxV + 1;
 constexpr int kBuckets = kStrideST * kStrideST;
-constexpr uint64_t kWaveSamples = 1ull << 19;
-// Sample index bits of a connection work item (kWaveSamples samples).
+constexpr uint64_t kWaveSamples = 1ull << 21;
+// A work item: sample index (21 bits, kWaveSamples samples), d (bit 21),
+// s (bits 22..26) and t (bits 27..31).
 constexpr uint32_t kSampleMask = (uint32_t)kWaveSamples - 1u;
+constexpr int kItemD = 21, kItemS = 22, kItemT = 27;
 constexpr int kBdptThreads = 128;
 constexpr uint32_t kKeyBdpt = 0x42445054u;
 
@@ -297,9 +299,11 @@ __device__ __forceinline__ void emit_step(const Ctx& C, const Wave& w, int dir, 
 }
 
 __global__ void __launch_bounds__(kBdptThreads) k_bd_start(Ctx C, Wave w, float4* __restrict__ ext,
-                                                           float4* __restrict__ sh, uint32_t* __restrict__ active)
+                                                           float4* __restrict__ sh, uint32_t* __restrict__ active,
+                                                           uint32_t* __restrict__ n_out)
 {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j == 0) *n_out = C.max_v > 1 ? 2 * w.n : 0u;  // every subpath is queued for step 1
     if (j >= 2 * w.n) return;
     const int dir = j >= w.n ? DIR_EL : DIR_LE;
     const uint32_t i = dir == DIR_EL ? j - w.n : j;
@@ -331,7 +335,7 @@ __global__ void __launch_bounds__(kBdptThreads) k_bd_start(Ctx C, Wave w, float4
 
 // Step k of the active subpaths: hits of the extension and direct rays in,
 // the vertex stored, roulette, the rays of step k + 1 out (compacted).
-__global__ void __launch_bounds__(kBdptThreads) k_bd_step(Ctx C, Wave w, int k, uint32_t n_active,
+__global__ void __launch_bounds__(kBdptThreads) k_bd_step(Ctx C, Wave w, int k, const uint32_t* __restrict__ n_in,
                                                           const uint32_t* __restrict__ active_in,
                                                           const float4* __restrict__ ext_in,
                                                           const lmgpu_hit* __restrict__ ext_hit,
@@ -348,7 +352,7 @@ __global__ void __launch_bounds__(kBdptThreads) k_bd_step(Ctx C, Wave w, int k, 
     float3 wo = zero3();
     bool has_wo = false;
     StepRand rn{};
-    if (q < n_active) {
+    if (q < *n_in) {
         j = active_in[q];
         dir = j >= w.n ? DIR_EL : DIR_LE;
         const uint32_t i = dir == DIR_EL ? j - w.n : j;
@@ -537,9 +541,9 @@ __global__ void k_bd_buckets(uint32_t* __restrict__ hist, uint32_t* __restrict__
 
 // Work items, scattered into their strategy's bucket so that a warp of
 // k_bd_connect evaluates one strategy (same path length, same MIS loops) at
-// a time: the s, t >= 1 connections as sample | s << 20 | t << 26, and the
+// a time: the s, t >= 1 connections as sample | s << 22 | t << 27, and the
 // s = 0 strategies (Path::Connect, :245-275; no visibility ray: the eye
-// subpath's own rays found the light) as sample | d << 19 | t << 26.
+// subpath's own rays found the light) as sample | d << 21 | t << 27.
 __global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ offset, uint32_t* __restrict__ cursor,
                            uint32_t* __restrict__ items)
 {
@@ -557,10 +561,12 @@ __global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ offset, u
             uint32_t base = 0;
             if (lane == (unsigned)(__ffs(m) - 1)) base = atomicAdd(&cursor[b], (uint32_t)__popc(m));
             base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
-            if (has) items[offset[b] + base + __popc(m & ((1u << lane) - 1u))] = i | ((uint32_t)s << 20) | ((uint32_t)t << 26);
+            if (has)
+                items[offset[b] + base + __popc(m & ((1u << lane) - 1u))] =
+                    i | ((uint32_t)s << kItemS) | ((uint32_t)t << kItemT);
         }
     }
-    // s = 0: i | d << 19 | t << 26
+    // s = 0: i | d << 21 | t << 27
     const int t0 = t_limit_s0(nE, C.max_path);
     const int t0w = __reduce_max_sync(0xffffffffu, t0);
     for (int t = 2; t <= t0w; t++) {
@@ -571,7 +577,9 @@ __global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ offset, u
             uint32_t base = 0;
             if (lane == (unsigned)(__ffs(m) - 1)) base = atomicAdd(&cursor[b], (uint32_t)__popc(m));
             base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
-            if (has) items[offset[b] + base + __popc(m & ((1u << lane) - 1u))] = i | ((uint32_t)d << 19) | ((uint32_t)t << 26);
+            if (has)
+                items[offset[b] + base + __popc(m & ((1u << lane) - 1u))] =
+                    i | ((uint32_t)d << kItemD) | ((uint32_t)t << kItemT);
         }
     }
 }
@@ -586,12 +594,12 @@ __global__ void __launch_bounds__(kBdptThreads) k_bd_connect(Ctx C, Wave w, cons
     if (q >= n_items) return;
     const uint32_t it = items[q];
     const uint32_t i = it & kSampleMask;
-    const int s = (int)((it >> 20) & 0x3fu), t = (int)(it >> 26);
+    const int s = (int)((it >> kItemS) & 0x1fu), t = (int)(it >> kItemT);
     float c[3] = {0.0f, 0.0f, 0.0f};
     PV P[2 * kMaxV];
     if (s == 0) {
         // the eye subpath ends on a light (d = 0) or its direct vertex is one
-        const int d = (int)((it >> 19) & 1u);
+        const int d = (int)((it >> kItemD) & 1u);
         const BVtx last = w.sv[1][(size_t)(t - 1) * w.stride + i];
         bool ok0 = false;
         if (d == 0) {
@@ -697,7 +705,7 @@ struct BdptState {
     uint64_t ext_hit_cap = 0;
     lmgpu_hit* sh_hit = nullptr;
     uint64_t sh_hit_cap = 0;
-    uint32_t* counter = nullptr;  // [0] active / item counter
+    uint32_t* counter = nullptr;  // [0], [1] step queue lengths, [2] connection items
     uint64_t counter_cap = 0;
     uint32_t* h_counter = nullptr;
     uint32_t* items = nullptr;
@@ -763,9 +771,9 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
 
     if (!sc->bdpt) sc->bdpt = new BdptState();
     BdptState& B = *sc->bdpt;
-    // wave size: the vertex arrays (4 x levels x 32 bytes per sample) within ~512 MB
+    // wave size: the vertex arrays (4 x levels x 32 bytes per sample) within ~2 GB
     const uint64_t levels = (uint64_t)C.max_v;
-    uint64_t stride = (512ull << 20) / (4 * levels * sizeof(BVtx));
+    uint64_t stride = (2048ull << 20) / (4 * levels * sizeof(BVtx));
     stride = stride > kWaveSamples ? kWaveSamples : stride;
     stride = stride < total ? stride : total;
     if ((rc = grow_dev(&B.verts, &B.verts_cap, 4 * levels * stride)) ||
@@ -775,7 +783,7 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
         (rc = grow_dev(&B.active[1], &B.active_cap[1], 2 * stride)) ||
         (rc = grow_dev(&B.ext[0], &B.ext_cap[0], 4 * stride)) || (rc = grow_dev(&B.ext[1], &B.ext_cap[1], 4 * stride)) ||
         (rc = grow_dev(&B.sh, &B.sh_cap, 4 * stride)) || (rc = grow_dev(&B.ext_hit, &B.ext_hit_cap, 2 * stride)) ||
-        (rc = grow_dev(&B.sh_hit, &B.sh_hit_cap, 2 * stride)) || (rc = grow_dev(&B.counter, &B.counter_cap, 1)) ||
+        (rc = grow_dev(&B.sh_hit, &B.sh_hit_cap, 2 * stride)) || (rc = grow_dev(&B.counter, &B.counter_cap, 3)) ||
         (rc = grow_dev(&B.buckets, &B.buckets_cap, 3 * kBuckets)))
         return rc;
     if (!B.h_counter && cudaMallocHost((void**)&B.h_counter, sizeof(uint32_t)) != cudaSuccess) {
@@ -795,7 +803,7 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
     w.pend = B.pend;
     w.own = B.own;
     auto read_counter = [&](uint32_t& out) -> int {
-        LMGPU_CUDA_TRY(cudaMemcpyAsync(B.h_counter, B.counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(B.h_counter, B.counter + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
         LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
         out = *B.h_counter;
         return LMGPU_OK;
@@ -803,29 +811,31 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
     for (uint64_t p0 = 0; p0 < total; p0 += stride) {
         w.p0 = p0;
         w.n = (uint32_t)((total - p0) < stride ? (total - p0) : stride);
-        // subpaths
-        k_bd_start<<<blocks(2ull * w.n, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.ext[0], B.sh, B.active[0]);
+        // subpaths: queue lengths stay on the device (counter [0] and [1]
+        // alternate), the traversal and k_bd_step read them there; a bounded
+        // subpath takes at most max_v - 1 steps
+        uint32_t* qn = B.counter;
+        k_bd_start<<<blocks(2ull * w.n, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.ext[0], B.sh, B.active[0],
+                                                                                   qn);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
-        uint32_t n_active = C.max_v > 1 ? 2 * w.n : 0;
         int cur = 0;
-        for (int k = 1; n_active > 0; k++) {
-            if ((rc = launch_trace(sc->accel, B.ext[cur], B.ext_hit, n_active, false, false, stream)) ||
-                (rc = launch_trace(sc->accel, B.sh, B.sh_hit, n_active, true, false, stream)))
+        for (int k = 1; k < C.max_v; k++) {
+            if ((rc = launch_trace_dn(sc->accel, B.ext[cur], B.ext_hit, qn + cur, 2ull * w.n, false, stream)) ||
+                (rc = launch_trace_dn(sc->accel, B.sh, B.sh_hit, qn + cur, 2ull * w.n, true, stream)))
                 return rc;
-            LMGPU_CUDA_TRY(cudaMemsetAsync(B.counter, 0, sizeof(uint32_t), stream));
-            k_bd_step<<<blocks(n_active, kBdptThreads), kBdptThreads, 0, stream>>>(
-                C, w, k, n_active, B.active[cur], B.ext[cur], B.ext_hit, B.sh_hit, B.active[1 - cur], B.counter,
+            LMGPU_CUDA_TRY(cudaMemsetAsync(qn + (1 - cur), 0, sizeof(uint32_t), stream));
+            k_bd_step<<<blocks(2ull * w.n, kBdptThreads), kBdptThreads, 0, stream>>>(
+                C, w, k, qn + cur, B.active[cur], B.ext[cur], B.ext_hit, B.sh_hit, B.active[1 - cur], qn + (1 - cur),
                 B.ext[1 - cur], B.sh);
             LMGPU_CUDA_TRY(cudaGetLastError());
             sc->launches += 3;
-            if ((rc = read_counter(n_active))) return rc;
             cur = 1 - cur;
         }
         // connections
-        LMGPU_CUDA_TRY(cudaMemsetAsync(B.counter, 0, sizeof(uint32_t), stream));
+        LMGPU_CUDA_TRY(cudaMemsetAsync(B.counter + 2, 0, sizeof(uint32_t), stream));
         LMGPU_CUDA_TRY(cudaMemsetAsync(B.buckets, 0, sizeof(uint32_t) * kBuckets, stream));
-        k_bd_count<<<blocks(w.n, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.buckets, B.counter);
+        k_bd_count<<<blocks(w.n, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.buckets, B.counter + 2);
         LMGPU_CUDA_TRY(cudaGetLastError());
         uint32_t n_items = 0;
         if ((rc = read_counter(n_items))) return rc;
