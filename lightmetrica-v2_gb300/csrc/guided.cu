@@ -38,6 +38,9 @@
 namespace lmgpu {
 namespace {
 
+// Paths per wave of the guided tracer: whole passes, trained between waves.
+constexpr uint64_t kGuidedWave = 1ull << 21;
+
 using namespace guide;
 
 constexpr int kGdThreads = 256;
@@ -397,7 +400,7 @@ int render_pt_guided(lmgpu_scene* sc, lmgpu_guide* guide, const lmgpu_pt_params*
                      float* last_loss)
 {
     const uint64_t npix = (uint64_t)sc->cam.width * sc->cam.height;
-    if (npix > kWave) {
+    if (npix > kGuidedWave) {
         set_error("lmgpu_render_pt_guided: films above 2^21 pixels are not supported");
         return LMGPU_ERR_INVALID;
     }
@@ -409,8 +412,8 @@ int render_pt_guided(lmgpu_scene* sc, lmgpu_guide* guide, const lmgpu_pt_params*
     if (rc) return rc;
     if (!sc->guided) sc->guided = new GuidedState();
     GuidedState& G = *sc->guided;
-    // a wave: whole passes (one sample per pixel each), up to kWave paths
-    const uint64_t per_wave = kWave / npix;
+    // a wave: whole passes (one sample per pixel each), up to kGuidedWave paths
+    const uint64_t per_wave = kGuidedWave / npix;
     const uint64_t W = npix * (per_wave < prm->spp ? per_wave : prm->spp);
     // the path queues hold a whole wave
     if ((rc = ensure_queues(sc, W))) return rc;

@@ -37,7 +37,7 @@ namespace lmgpu {
 namespace {
 
 constexpr int kLtThreads = 256;
-constexpr uint32_t kLtWave = 1u << 21;
+constexpr uint32_t kLtWave = 1u << 22;
 constexpr uint32_t kKeyLightPath = 0x4C505448u;  // light selection, position + emission direction
 constexpr uint32_t kKeyLightStep = 0x4C535450u;  // BSDF sample + roulette per light-path vertex
 

@@ -6,7 +6,7 @@
 namespace lmgpu {
 
 // Paths in flight per wave of the wavefront renderers.
-constexpr uint64_t kWave = 1ull << 21;
+constexpr uint64_t kWave = 1ull << 22;
 
 // Philox key words separating the streams a path draws from.
 constexpr uint32_t kKeyCamera = 0x43414D45u;  // raster jitter
