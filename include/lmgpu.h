@@ -88,6 +88,39 @@ int lmgpu_accel_build(lmgpu_accel* accel, const float* triangles, uint64_t ntri)
 /* As lmgpu_accel_build, with the triangle buffer already on the device. */
 int lmgpu_accel_build_device(lmgpu_accel* accel, const float* d_triangles, uint64_t ntri, void* stream);
 
+/* One primitive's indexed triangle mesh (TriangleMesh::Positions / Faces,
+ * include/lightmetrica/trianglemesh.h:60-90) with the primitive's transform
+ * (Primitive::transform, include/lightmetrica/primitive.h:56-80):
+ * positions float[3 * num_vertices], faces uint32[3 * num_faces] (vertex
+ * indices), transform column-major m[column][row] = transform[4 column + row],
+ * the layout of the reference's Mat4. */
+typedef struct {
+    const float* positions;
+    const uint32_t* faces;
+    uint32_t num_vertices;
+    uint32_t num_faces;
+    float transform[16];
+} lmgpu_mesh;
+
+/* Flattens n meshes on the GPU into d_triangles (float[9 * total faces]) in
+ * global order -- meshes in order, faces in mesh order, as the reference's
+ * accels enumerate them (accel_naive.cpp:59-90) -- and, if d_tri_prim is not
+ * NULL, each triangle's mesh index into it.  positions and faces are device
+ * pointers.  Vertices go through the transform with the reference's
+ * single-precision arithmetic (Mat4 x Vec4, math.h:1268-1279: every product
+ * and sum rounded, no fused multiply-add), so the triangles equal the
+ * reference's bit for bit.  A face index outside its mesh returns
+ * LMGPU_ERR_INVALID.  Returns after the flattening has finished. */
+int lmgpu_flatten_meshes_device(const lmgpu_mesh* meshes, uint32_t n, float* d_triangles, int32_t* d_tri_prim,
+                                void* stream);
+
+/* Builds the accel from host meshes: checks the face indices, uploads
+ * positions and faces (12 bytes per vertex and per face instead of 36 per
+ * flattened triangle), flattens them on the GPU as
+ * lmgpu_flatten_meshes_device does, and builds.  Stands in for Accel::Build
+ * (include/lightmetrica/accel.h:79) with its triangle enumeration. */
+int lmgpu_accel_build_meshes(lmgpu_accel* accel, const lmgpu_mesh* meshes, uint32_t n);
+
 /* Fills *info for a built accel. */
 int lmgpu_accel_get_info(const lmgpu_accel* accel, lmgpu_accel_info* info);
 

@@ -81,6 +81,8 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_accel_destroy.restype = None
     L.lmgpu_accel_build.argtypes = [vp, vp, u64]
     L.lmgpu_accel_build_device.argtypes = [vp, vp, u64, vp]
+    L.lmgpu_flatten_meshes_device.argtypes = [vp, ctypes.c_uint32, vp, vp, vp]
+    L.lmgpu_accel_build_meshes.argtypes = [vp, vp, ctypes.c_uint32]
     L.lmgpu_accel_get_info.argtypes = [vp, ctypes.POINTER(AccelInfo)]
     L.lmgpu_trace.argtypes = [vp, vp, vp, u64, i32]
     L.lmgpu_trace_device.argtypes = [vp, vp, vp, u64, i32, vp]
@@ -146,6 +148,7 @@ def lib() -> ctypes.CDLL:
                  "lmgpu_render_pt_guided", "lmgpu_render_pt_guided_device",
                  "lmgpu_render_ptdirect_device", "lmgpu_render_ltdirect", "lmgpu_render_ltdirect_device",
                  "lmgpu_render_bdpt_mis", "lmgpu_render_bdpt_mis_device", "lmgpu_render_vcm",
+                 "lmgpu_flatten_meshes_device", "lmgpu_accel_build_meshes",
                  "lmgpu_render_vcm_device",
                  "lmgpu_accel_set_attributes", "lmgpu_surface", "lmgpu_surface_device",
                  "lmgpu_scene_set_environment"):
@@ -161,6 +164,35 @@ def _check(rc: int) -> None:
 
 def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data
+
+
+class Mesh(ctypes.Structure):
+    """lmgpu_mesh: an indexed triangle mesh with its column-major transform."""
+    _fields_ = [("positions", ctypes.c_void_p), ("faces", ctypes.c_void_p), ("num_vertices", ctypes.c_uint32),
+                ("num_faces", ctypes.c_uint32), ("transform", ctypes.c_float * 16)]
+
+
+def _mesh_table(meshes, ptrs) -> ctypes.Array:
+    """meshes: (positions, faces, transform) with ptrs giving the buffers' addresses."""
+    table = (Mesh * max(1, len(meshes)))()
+    for i, ((pos, faces, tr), (pp, fp)) in enumerate(zip(meshes, ptrs)):
+        table[i].positions = pp
+        table[i].faces = fp
+        table[i].num_vertices = int(np.asarray(pos).size // 3) if not hasattr(pos, "numel") else int(pos.numel() // 3)
+        table[i].num_faces = int(np.asarray(faces).size // 3) if not hasattr(faces, "numel") else int(faces.numel() // 3)
+        t = np.asarray(tr, np.float32).reshape(-1)
+        for k in range(16):
+            table[i].transform[k] = float(t[k])
+    return table
+
+
+def flatten_meshes_device(meshes, d_triangles: int, d_tri_prim: int = 0, stream: int = 0) -> None:
+    """lmgpu_flatten_meshes_device: meshes as (positions, faces, transform)
+    with positions / faces CUDA tensors (float32 / int32 holding uint32
+    indices) and transform 16 floats, column-major m[c][r]."""
+    table = _mesh_table(meshes, [(p.data_ptr(), f.data_ptr()) for p, f, _ in meshes])
+    _check(lib().lmgpu_flatten_meshes_device(ctypes.addressof(table), len(meshes), d_triangles, d_tri_prim or None,
+                                             stream or None))
 
 
 class Accel:
@@ -192,6 +224,13 @@ class Accel:
 
     def build_device(self, d_tris_ptr: int, ntri: int, stream: int = 0) -> None:
         _check(lib().lmgpu_accel_build_device(self._h, d_tris_ptr, ntri, stream))
+
+    def build_meshes(self, meshes) -> None:
+        """lmgpu_accel_build_meshes: meshes as (positions (nv, 3) float32,
+        faces (nf, 3) uint32, transform 16 floats column-major m[c][r])."""
+        keep = [(np.ascontiguousarray(p, np.float32), np.ascontiguousarray(f, np.uint32), t) for p, f, t in meshes]
+        table = _mesh_table(keep, [(_ptr(p), _ptr(f)) for p, f, _ in keep])
+        _check(lib().lmgpu_accel_build_meshes(self._h, ctypes.addressof(table), len(keep)))
 
     def info(self) -> dict:
         i = AccelInfo()

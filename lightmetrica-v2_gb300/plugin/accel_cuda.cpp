@@ -66,32 +66,40 @@ public:
     LM_IMPL_F(Build) = [this](const Scene* scene_) -> bool
     {
         const auto* scene = static_cast<const Scene3*>(scene_);
-        std::vector<float> tris;
+        // the meshes as the primitives hold them, flattened and transformed
+        // on the GPU (lmgpu_accel_build_meshes) in the global order the
+        // reference's accels use (accel_naive.cpp:59-90)
         primOf_.clear();
         faceOf_.clear();
+        std::vector<lmgpu_mesh> meshes;
+        std::vector<std::vector<float>> pos32;       // Float -> float where Float is double
+        std::vector<std::vector<uint32_t>> faces32;  // unsigned int -> uint32_t where they differ
         const int np = scene->NumPrimitives();
         for (int i = 0; i < np; i++)
         {
             const auto* prim = scene->PrimitiveAt(i);
             const auto* mesh = prim->mesh;
             if (!mesh) continue;
-            const auto* ps = mesh->Positions();
-            const auto* fs = mesh->Faces();
+            lmgpu_mesh m = {};
+            m.num_vertices = (uint32_t)mesh->NumVertices();
+            m.num_faces = (uint32_t)mesh->NumFaces();
+            pos32.emplace_back(mesh->Positions(), mesh->Positions() + 3 * (size_t)m.num_vertices);
+            faces32.emplace_back(mesh->Faces(), mesh->Faces() + 3 * (size_t)m.num_faces);
+            for (int c = 0; c < 4; c++)
+                for (int r = 0; r < 4; r++) m.transform[4 * c + r] = (float)prim->transform[c][r];
+            meshes.push_back(m);
             for (int j = 0; j < mesh->NumFaces(); j++)
             {
-                for (int k = 0; k < 3; k++)
-                {
-                    const unsigned int v = fs[3 * j + k];
-                    const Vec3 p(prim->transform * Vec4(ps[3 * v], ps[3 * v + 1], ps[3 * v + 2], 1_f));
-                    tris.push_back((float)p.x);
-                    tris.push_back((float)p.y);
-                    tris.push_back((float)p.z);
-                }
                 primOf_.push_back(i);
                 faceOf_.push_back(j);
             }
         }
-        if (lmgpu_accel_build(accel_, tris.data(), (uint64_t)primOf_.size()) != LMGPU_OK)
+        for (size_t k = 0; k < meshes.size(); k++)
+        {
+            meshes[k].positions = pos32[k].data();
+            meshes[k].faces = faces32[k].data();
+        }
+        if (lmgpu_accel_build_meshes(accel_, meshes.data(), (uint32_t)meshes.size()) != LMGPU_OK)
         {
             LM_LOG_ERROR(std::string("accel::cuda: ") + lmgpu_last_error());
             return false;

@@ -63,7 +63,9 @@ Fixtures written:
       translation transforms (a smooth icosphere with normals and texcoords,
       a quad with texcoords only, a face with all-zero normals, a bare mesh)
       and seeded queries (face, barycentrics including edges and vertices,
-      ray origin, direction and t).  Per triangle: the vertices, normals and
+      ray origin, direction and t).  Also the meshes' single-precision
+      inputs (mesh<i>_positions, _faces, _transform column-major), whose
+      transformed triangles tris32 pin the GPU mesh flattening.  Per triangle: the vertices, normals and
       texcoords as the reference transforms them; per query: p, gn, sn,
       dpdu, dpdv, dndu, dndv, uv.
   soup_small.npz
@@ -323,7 +325,15 @@ def surface_case() -> dict:
     q = np.array(qs, np.float64)
     r64 = lo.run_ref_isect(prims, q, double=True)
     r32 = lo.run_ref_isect(prims, q, double=False)
-    return {"queries": q, "global_id": (base[q[:, 0].astype(int)] + q[:, 1]).astype(np.int32),
+    meshes = {}
+    for i, p in enumerate(prims):
+        # the harness's inputs in single precision: positions and the column-major transform m[c][r]
+        meshes[f"mesh{i}_positions"] = np.asarray(p["positions"], np.float32)
+        meshes[f"mesh{i}_faces"] = np.asarray(p["faces"], np.uint32)
+        meshes[f"mesh{i}_transform"] = np.asarray(p["transform"], np.float64).reshape(4, 4).T.reshape(-1).astype(
+            np.float32)
+    return {**meshes, "num_meshes": np.int32(len(prims)),
+            "queries": q, "global_id": (base[q[:, 0].astype(int)] + q[:, 1]).astype(np.int32),
             "tris64": r64["tris"], "normals64": r64["normals"], "texcoords64": r64["texcoords"],
             "flags": r64["flags"], "geom64": r64["geom"], "face64": r64["face"],
             "tris32": r32["tris"].astype(np.float32), "normals32": r32["normals"].astype(np.float32),
