@@ -556,7 +556,7 @@ int lmgpu_batch_autotune(lmgpu_batch* b, const lmgpu_batch_params* probe, lmgpu_
     // as the best of two renders of the probe with CUDA events
     const int refills[] = {2, 4, 8, 16};
     const int postpones[] = {0, 8, 12, 16, 24};
-    const uint64_t waves[] = {1ull << 20, 1ull << 21, 1ull << 22};
+    const uint64_t waves[] = {1ull << 20, 1ull << 21, 1ull << 22, 1ull << 23};
     cudaEvent_t e0, e1;
     LMGPU_CUDA_TRY(cudaEventCreate(&e0));
     LMGPU_CUDA_TRY(cudaEventCreate(&e1));
