@@ -100,3 +100,20 @@ def test_vcm_boundaries_and_device_entry(gpu_lib, golden_dir):
     with pytest.raises(gpu_lib.LmgpuError):
         sc.render_vcm(**small)
     sc.close()
+
+
+def test_vcm_several_eye_waves_per_pass(gpu_lib, golden_dir):
+    """At max_num_vertices 8 a wave holds ~355,000 eye samples: 1,048,576
+    per pass take three waves, 262,144 one.  Same seed, so both renders share
+    their photon subpaths and the first 262,144 eye samples (random numbers
+    are keyed by global index); the expected images are equal."""
+    scene, _ = ptscene.load_scene(golden_dir, "cornell_vcm")
+    common = dict(max_num_vertices=8, num_iteration_pass=8, num_photon_trace_samples=8192, initial_radius=0.05,
+                  alpha=0.7, seed=17)
+    sc = gpu_lib.Scene(scene)
+    a, va = sc.render_vcm(num_eye_trace_samples=32 * 32 * 256, **common)
+    b, vb = sc.render_vcm(num_eye_trace_samples=32 * 32 * 1024, **common)
+    sc.close()
+    print(imgcheck.assert_same_aggregates(a, va, b, vb, "one wave vs three waves per pass",
+                                          block_limit=VCM_BLOCK_LIMIT))
+    assert np.isfinite(b).all() and (b >= 0).all()
