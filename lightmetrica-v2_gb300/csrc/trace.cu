@@ -49,7 +49,9 @@ constexpr int kTraceBlocksPerSM = 8;
 // MULTI: rays of several scenes in one launch; ray i is traced against the
 // BVH tab[ray_scene[i]] (the batch renderer's views).  d_n, when not null,
 // holds the ray count on the device (launches captured in CUDA graphs).
-template <bool ANYHIT, bool STATS, bool MULTI>
+// SMALL: the same kernel as a separate function whose shared-memory
+// carveout is set to the largest L1, launched for BVHs that fit in L1.
+template <bool ANYHIT, bool STATS, bool MULTI, bool SMALL = false>
 __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(const WNode* __restrict__ nodes, const WTri* __restrict__ tris,
                                                          const float4* __restrict__ rays, lmgpu_hit* __restrict__ hits,
                                                          uint64_t n, uint32_t num_nodes, uint32_t num_tris,
@@ -224,7 +226,7 @@ namespace {
 
 // Blocks of the persistent grid of one instantiation (SMs x resident blocks),
 // looked up once per process.
-template <bool ANYHIT, bool STATS, bool MULTI>
+template <bool ANYHIT, bool STATS, bool MULTI, bool SMALL = false>
 int grid_cap_of()
 {
     static int cap = 0;
@@ -232,8 +234,12 @@ int grid_cap_of()
         int dev = 0, sms = 0, per_sm = 0;
         LMGPU_CUDA_TRY(cudaGetDevice(&dev));
         LMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        LMGPU_CUDA_TRY(
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<ANYHIT, STATS, MULTI>, kTraceThreads, 0));
+        if (SMALL)
+            LMGPU_CUDA_TRY(cudaFuncSetAttribute(k_trace<ANYHIT, STATS, MULTI, SMALL>,
+                                                cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                (int)cudaSharedmemCarveoutMaxL1));
+        LMGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<ANYHIT, STATS, MULTI, SMALL>,
+                                                                     kTraceThreads, 0));
         cap = sms * (per_sm > 0 ? per_sm : 1);
     }
     return cap;
@@ -277,13 +283,18 @@ int launch_trace_dn(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hit
                     uint64_t max_n, bool anyhit, cudaStream_t stream)
 {
     if (max_n == 0) return LMGPU_OK;
-    const int grid_cap = anyhit ? grid_cap_of<true, false, false>() : grid_cap_of<false, false, false>();
+    // closest hit in a BVH that fits in L1 (nodes and triangles within 96 KiB)
+    // runs the SMALL instantiation: largest-L1 carveout, measured +4 % on a
+    // 36-triangle scene and -6 % on the 1.5M-triangle ray-cast scene
+    const bool small = !anyhit && (uint64_t)a->num_wide * sizeof(WNode) + a->ntri * sizeof(WTri) <= (96u << 10);
+    const int grid_cap = small ? grid_cap_of<false, false, false, true>()
+                               : (anyhit ? grid_cap_of<true, false, false>() : grid_cap_of<false, false, false>());
     if (grid_cap <= 0) return LMGPU_ERR_CUDA;
     const uint64_t by_rays = (max_n + 4 * kTraceThreads - 1) / (4 * kTraceThreads);
     const unsigned grid = (unsigned)(by_rays < (uint64_t)grid_cap ? by_rays : (uint64_t)grid_cap);
     const uint32_t nn = a->ntri > 0 ? (uint32_t)a->num_wide : 0u;
     const uint32_t nt = (uint32_t)a->ntri;
-    auto k = anyhit ? k_trace<true, false, false> : k_trace<false, false, false>;
+    auto k = small ? k_trace<false, false, false, true> : (anyhit ? k_trace<true, false, false> : k_trace<false, false, false>);
     k<<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, max_n, nn, nt, a->tune.refill,
                                           a->tune.postpone, a->status, nullptr, nullptr, 0u, nullptr, d_n);
     LMGPU_CUDA_TRY(cudaGetLastError());
