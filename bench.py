@@ -381,9 +381,10 @@ def run_surface(args) -> None:
         if lib.lmgpu_surface(acc.handle, h_rays.data_ptr(), h_hits.data_ptr(), nr, h_out.data_ptr()) != 0:
             raise RuntimeError(lib.lmgpu_last_error().decode())
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    # algorithmic bytes: a hit reads its record (16 B), ray (32 B), slot (4 B), triangle (48 B), normals
-    # (36 B), texcoords (24 B) and flags (1 B); a miss its record; every ray writes 23 floats (92 B)
-    hit_b, miss_b = 16 + 32 + 4 + 48 + 36 + 24 + 1 + 92, 16 + 92
+    # algorithmic bytes, whatever the layout: a hit reads its hit record (16 B), ray (32 B), the
+    # triangle's vertices (36 B), vertex normals (36 B), texcoords (24 B) and flags (1 B); a miss its
+    # hit record; every ray writes 23 floats (92 B)
+    hit_b, miss_b = 16 + 32 + 36 + 36 + 24 + 1 + 92, 16 + 92
     alg = n_hit * hit_b + (nr - n_hit) * miss_b
     peak, peak_src = measured_peak()
     achieved = alg / per_s / 1e9
@@ -399,8 +400,9 @@ def run_surface(args) -> None:
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_src, "kernel": "k_surface",
                          "bytes_per_ray": alg / nr,
-                         "note": "algorithmic bytes: hit 253 B (record, ray, slot, triangle, normals, texcoords, "
-                                 "flags, 92 B out), miss 108 B"},
+                         "note": "algorithmic bytes: hit 237 B (hit record, ray, vertices, normals, texcoords, "
+                                 "flags, 92 B out), miss 108 B; the kernel reads one 128-byte surface record "
+                                 "per hit"},
             "clocks": clk}
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))

@@ -38,6 +38,13 @@ struct lmgpu_accel {
     float* attr_texcoords = nullptr;
     uint8_t* attr_flags = nullptr;
     uint64_t attr_ntri = 0;
+    // Surface records read by lmgpu_surface: per global triangle one 128-byte
+    // line (positions, vertex normals, texcoords, flags), packed on the device
+    // from the triangles and the attributes; surf_ntri = 0 until packed for
+    // the current build.
+    float4* surf = nullptr;
+    uint64_t surf_cap = 0;
+    uint64_t surf_ntri = 0;
 
     // Device status word raised by traversal kernels (stack overflow).
     uint32_t* status = nullptr;

@@ -91,6 +91,7 @@ void lmgpu_accel_destroy(lmgpu_accel* a)
     if (a->attr_normals) cudaFree(a->attr_normals);
     if (a->attr_texcoords) cudaFree(a->attr_texcoords);
     if (a->attr_flags) cudaFree(a->attr_flags);
+    if (a->surf) cudaFree(a->surf);
     if (a->status) cudaFree(a->status);
     if (a->counters) cudaFree(a->counters);
     if (a->stage_rays) cudaFree(a->stage_rays);

@@ -1096,6 +1096,7 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
     a->ntri = ntri;
     a->num_wide = 0;
     a->attr_ntri = 0;  // shading attributes belong to the previous triangles
+    a->surf_ntri = 0;
     a->info = lmgpu_accel_info{};
     a->info.num_triangles = ntri;
     if (ntri == 0) {

@@ -49,11 +49,52 @@ __device__ __forceinline__ F3 normalize3(F3 a)
 }
 __device__ __forceinline__ F3 ld3(const float* p) { return f3(p[0], p[1], p[2]); }
 
+// One 128-byte record per global triangle, so a hit reads one aligned line
+// instead of gathering the triangle (through tri_slot), its normals, its
+// texcoords and its flags from four arrays:
+//   [0] p1, flags (bit 0 normals, bit 1 texcoords, bit 2 bad slot)
+//   [1] p2, n1.x   [2] p3, n1.y   [3] n1.z, n2   [4] n3, uv1.u
+//   [5] uv1.v, uv2, uv3.u   [6] uv3.v, 0, 0, 0   [7] unused
+constexpr int kSurfRec = 8;  // float4s per record
+
+__global__ void k_surface_pack(const WTri* __restrict__ tris, const int32_t* __restrict__ tri_slot, uint64_t ntri,
+                               const float* __restrict__ normals, const float* __restrict__ texcoords,
+                               const uint8_t* __restrict__ flags, float4* __restrict__ rec)
+{
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ntri) return;
+    float4 r[kSurfRec];
+    for (int k = 0; k < kSurfRec; k++) r[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint32_t fl = flags ? (uint32_t)(flags[g] & 3u) : 0u;
+    const int32_t slot = tri_slot[g];
+    if (slot < 0 || (uint64_t)slot >= ntri) {
+        fl |= 4u;
+    } else {
+        const WTri w = tris[slot];
+        r[0] = make_float4(w.v0.x, w.v0.y, w.v0.z, 0.0f);
+        r[1] = make_float4(w.v1.x, w.v1.y, w.v1.z, 0.0f);
+        r[2] = make_float4(w.v2.x, w.v2.y, w.v2.z, 0.0f);
+    }
+    r[0].w = __uint_as_float(fl);
+    if ((fl & 1u) && normals) {
+        const float* n = normals + 9 * g;
+        r[1].w = n[0];
+        r[2].w = n[1];
+        r[3] = make_float4(n[2], n[3], n[4], n[5]);
+        r[4] = make_float4(n[6], n[7], n[8], 0.0f);
+    }
+    if ((fl & 2u) && texcoords) {
+        const float* t = texcoords + 6 * g;
+        r[4].w = t[0];
+        r[5] = make_float4(t[1], t[2], t[3], t[4]);
+        r[6] = make_float4(t[5], 0.0f, 0.0f, 0.0f);
+    }
+    for (int k = 0; k < kSurfRec; k++) rec[kSurfRec * g + k] = r[k];
+}
+
 __global__ void __launch_bounds__(kSurfaceThreads)
-    k_surface(const WTri* __restrict__ tris, const int32_t* __restrict__ tri_slot, uint64_t ntri,
-              const float* __restrict__ normals, const float* __restrict__ texcoords, const uint8_t* __restrict__ flags,
-              uint8_t default_flags, const float4* __restrict__ rays, const lmgpu_hit* __restrict__ hits, uint64_t n,
-              float* __restrict__ out, uint32_t* __restrict__ status)
+    k_surface(const float4* __restrict__ rec, uint64_t ntri, const float4* __restrict__ rays,
+              const lmgpu_hit* __restrict__ hits, uint64_t n, float* __restrict__ out, uint32_t* __restrict__ status)
 {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -65,29 +106,33 @@ __global__ void __launch_bounds__(kSurfaceThreads)
         const float t = hv.x, b0 = hv.z, b1 = hv.w;
         const float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
         const F3 p = add3(f3(r0.x, r0.y, r0.z), scl3(f3(r1.x, r1.y, r1.z), t));
-        const int32_t slot = tri_slot[prim];
+        const float4* R = rec + (size_t)kSurfRec * prim;
+        const float4 ra = R[0], rb = R[1], rc = R[2];
+        const uint32_t fl = __float_as_uint(ra.w);
         F3 gn = f3(0.0f, 0.0f, 0.0f), n1 = gn, n2 = gn, n3 = gn, sn = gn;
-        if (slot < 0 || (uint64_t)slot >= ntri) {
+        if (fl & 4u) {
             atomicOr(status, kStatusBadTree);
         } else {
-            const WTri w = tris[slot];
-            const F3 p1 = f3(w.v0.x, w.v0.y, w.v0.z), p2 = f3(w.v1.x, w.v1.y, w.v1.z), p3 = f3(w.v2.x, w.v2.y, w.v2.z);
+            const F3 p1 = f3(ra.x, ra.y, ra.z), p2 = f3(rb.x, rb.y, rb.z), p3 = f3(rc.x, rc.y, rc.z);
             gn = normalize3(cross3(sub3(p2, p1), sub3(p3, p1)));
             n1 = n2 = n3 = sn = gn;
         }
-        const uint8_t fl = flags ? flags[prim] : default_flags;
         const float w0 = __fsub_rn(__fsub_rn(1.0f, b0), b1);
-        if ((fl & 1u) && normals) {
-            const float* nv = normals + 9 * (size_t)prim;
-            n1 = ld3(nv);
-            n2 = ld3(nv + 3);
-            n3 = ld3(nv + 6);
+        float4 re = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (fl & 1u) {
+            const float4 rd = R[3];
+            re = R[4];
+            n1 = f3(rb.w, rc.w, rd.x);
+            n2 = f3(rd.y, rd.z, rd.w);
+            n3 = f3(re.x, re.y, re.z);
             sn = normalize3(add3(add3(scl3(n1, w0), scl3(n2, b0)), scl3(n3, b1)));
             if (isnan(sn.x) || isnan(sn.y) || isnan(sn.z)) sn = gn;
         }
         float u = 0.0f, uvv = 0.0f;
-        if ((fl & 2u) && texcoords) {
-            const float* tc = texcoords + 6 * (size_t)prim;
+        if (fl & 2u) {
+            if (!(fl & 1u)) re = R[4];
+            const float4 rf = R[5], rg = R[6];
+            const float tc[6] = {re.w, rf.x, rf.y, rf.z, rf.w, rg.x};
             u = __fadd_rn(__fadd_rn(__fmul_rn(tc[0], w0), __fmul_rn(tc[2], b0)), __fmul_rn(tc[4], b1));
             uvv = __fadd_rn(__fadd_rn(__fmul_rn(tc[1], w0), __fmul_rn(tc[3], b0)), __fmul_rn(tc[5], b1));
         }
@@ -110,6 +155,26 @@ __global__ void __launch_bounds__(kSurfaceThreads)
     for (int k = 0; k < 23; k++) out[(uint64_t)k * n + i] = v[k];
 }
 
+// Packs the surface records of the current build (attributes if set).
+int pack_surface(lmgpu_accel* a, cudaStream_t stream)
+{
+    if (a->surf_cap < a->ntri) {
+        if (a->surf) cudaFree(a->surf);
+        a->surf = nullptr;
+        a->surf_cap = 0;
+        LMGPU_CUDA_TRY(cudaMalloc((void**)&a->surf, sizeof(float4) * kSurfRec * a->ntri));
+        a->surf_cap = a->ntri;
+    }
+    const bool attrs = a->attr_ntri == a->ntri;
+    const uint64_t blocks = (a->ntri + kSurfaceThreads - 1) / kSurfaceThreads;
+    k_surface_pack<<<(unsigned)blocks, kSurfaceThreads, 0, stream>>>(
+        a->tris, a->tri_slot, a->ntri, attrs ? a->attr_normals : nullptr, attrs ? a->attr_texcoords : nullptr,
+        attrs ? a->attr_flags : nullptr, a->surf);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+    a->surf_ntri = a->ntri;
+    return LMGPU_OK;
+}
+
 int check_surface_args(const lmgpu_accel* a, const char* who)
 {
     if (!a->built) {
@@ -119,19 +184,22 @@ int check_surface_args(const lmgpu_accel* a, const char* who)
     return LMGPU_OK;
 }
 
-int launch_surface(const lmgpu_accel* a, const float* d_rays, const lmgpu_hit* d_hits, uint64_t n, float* d_out,
+int launch_surface(const lmgpu_accel* ca, const float* d_rays, const lmgpu_hit* d_hits, uint64_t n, float* d_out,
                    cudaStream_t stream)
 {
-    if (n == 0 || a->ntri == 0) {
+    if (n == 0 || ca->ntri == 0) {
         if (n) LMGPU_CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(float) * LMGPU_SURFACE_PLANES * n, stream));
         return LMGPU_OK;
     }
-    const bool attrs = a->attr_ntri == a->ntri;
-    const uint8_t def = 0;
+    // the records are derived state of the accel, packed on first use after a build
+    lmgpu_accel* a = const_cast<lmgpu_accel*>(ca);
+    if (a->surf_ntri != a->ntri) {
+        const int rc = pack_surface(a, stream);
+        if (rc) return rc;
+    }
     const uint64_t blocks = (n + kSurfaceThreads - 1) / kSurfaceThreads;
-    k_surface<<<(unsigned)blocks, kSurfaceThreads, 0, stream>>>(
-        a->tris, a->tri_slot, a->ntri, attrs ? a->attr_normals : nullptr, attrs ? a->attr_texcoords : nullptr,
-        attrs ? a->attr_flags : nullptr, def, reinterpret_cast<const float4*>(d_rays), d_hits, n, d_out, a->status);
+    k_surface<<<(unsigned)blocks, kSurfaceThreads, 0, stream>>>(a->surf, a->ntri, reinterpret_cast<const float4*>(d_rays),
+                                                                d_hits, n, d_out, a->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
     return LMGPU_OK;
 }
@@ -163,6 +231,7 @@ int lmgpu_accel_set_attributes(lmgpu_accel* a, const float* normals, const float
     a->attr_normals = a->attr_texcoords = nullptr;
     a->attr_flags = nullptr;
     a->attr_ntri = 0;
+    a->surf_ntri = 0;
     if (ntri == 0) return LMGPU_OK;
     std::vector<uint8_t> fl(ntri);
     for (uint64_t i = 0; i < ntri; i++)
@@ -182,6 +251,9 @@ int lmgpu_accel_set_attributes(lmgpu_accel* a, const float* normals, const float
     LMGPU_CUDA_TRY(cudaMalloc((void**)&a->attr_flags, ntri));
     LMGPU_CUDA_TRY(cudaMemcpy(a->attr_flags, fl.data(), ntri, cudaMemcpyHostToDevice));
     a->attr_ntri = ntri;
+    int rc = pack_surface(a, nullptr);
+    if (rc) return rc;
+    LMGPU_CUDA_TRY(cudaDeviceSynchronize());
     return LMGPU_OK;
 }
 
