@@ -586,7 +586,8 @@ __global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ offset, u
 
 // One connection (Path::Connect, :298-330): the full path L[0..s-1] E[t-1..0],
 // its contribution and the shadow ray between the two subpath ends.
-__global__ void __launch_bounds__(kBdptThreads) k_bd_connect(Ctx C, Wave w, const uint32_t* __restrict__ items,
+// 8 blocks per SM (64 registers): +1.5 % over the unbounded 72-register build
+__global__ void __launch_bounds__(kBdptThreads, 8) k_bd_connect(Ctx C, Wave w, const uint32_t* __restrict__ items,
                                                              uint32_t n_items, float4* __restrict__ rays,
                                                              float4* __restrict__ rec)
 {

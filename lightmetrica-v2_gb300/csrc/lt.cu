@@ -125,7 +125,8 @@ __global__ void __launch_bounds__(kLtThreads) k_lt_generate(Ctx C, uint64_t p0, 
     append_path(keep, r0, r1, s, rays, state, count);
 }
 
-__global__ void __launch_bounds__(kLtThreads) k_lt_shade(Ctx C, const float4* __restrict__ rays,
+// 4 blocks of 256 per SM (64 registers): +2.6 % over the unbounded 91-register build
+__global__ void __launch_bounds__(kLtThreads, 4) k_lt_shade(Ctx C, const float4* __restrict__ rays,
                                                          const PathState* __restrict__ state,
                                                          const lmgpu_hit* __restrict__ hits,
                                                          const uint32_t* __restrict__ d_n, uint64_t p0,
