@@ -431,6 +431,12 @@ RENDER_WORKLOADS = {
              "spp": 32, "max_num_vertices": 11,
              "data": "synthetic (procedural room, level-5 glass icosphere, sphere light behind a panel)",
              "cpu_spp": 1},
+    # renderer::ptmis / renderer::ptdirect (next-event estimation) on the Cornell-style box:
+    # 256 x 256, 64 spp, max_num_vertices 9
+    "ptmis": {"renderer": "ptmis", "workload": "ptmis_cornell_256x256_64spp", "width": 256, "height": 256,
+              "spp": 64, "max_num_vertices": 9, "data": "synthetic (procedural Cornell box)", "cpu_spp": 4},
+    "ptdirect": {"renderer": "ptdirect", "workload": "ptdirect_cornell_256x256_64spp", "width": 256, "height": 256,
+                 "spp": 64, "max_num_vertices": 9, "data": "synthetic (procedural Cornell box)", "cpu_spp": 4},
     # renderer::ltdirect (light tracing, a sensor connection per vertex) on the Cornell-style box:
     # 256 x 256 x 64 light paths, max_num_vertices 9
     "ltdirect": {"renderer": "ltdirect", "workload": "ltdirect_cornell_256x256_64spp", "width": 256, "height": 256,
@@ -839,10 +845,11 @@ def main() -> None:
     ap.add_argument("--anyhit", action="store_true", help="time any-hit queries instead of closest hit")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel of the render workloads (profiling of "
                                                         "smaller cases; default: the workload's own)")
-    ap.add_argument("--workload", choices=["raycast", "pt", "bdpt", "ltdirect", "vcm", "batch", "guiding", "surface"],
+    ap.add_argument("--workload", choices=["raycast", "pt", "ptmis", "ptdirect", "bdpt", "ltdirect", "vcm", "batch",
+                                           "guiding", "surface"],
                     default="raycast",
                     help="raycast: the BVH ray-cast configuration (default); pt: renderer::pt on the Cornell "
-                         "box; bdpt: renderer::bdpt on the caustic room; ltdirect: light tracing on the Cornell "
+                         "box; ptmis / ptdirect: next-event estimation on the Cornell box; bdpt: renderer::bdpt on the caustic room; ltdirect: light tracing on the Cornell "
                          "box; vcm: vertex connection and merging on the Cornell box; batch: 12 scenes in one "
                          "wavefront; "
                          "guiding: learned path guiding vs plain PT at equal time; surface: surface geometry "

@@ -407,6 +407,11 @@ class Scene:
         _check(lib().lmgpu_render_ptdirect(self._h, ctypes.byref(prm), img.ctypes.data, var.ctypes.data))
         return img, var
 
+    def render_ptdirect_device(self, d_image: int, d_variance: int, spp: int, max_num_vertices: int = -1,
+                               seed: int = 0, stream: int = 0, min_num_vertices: int = 0) -> None:
+        prm = PtParams(spp, max_num_vertices, seed, min_num_vertices)
+        _check(lib().lmgpu_render_ptdirect_device(self._h, ctypes.byref(prm), d_image, d_variance, stream))
+
     def render_ltdirect(self, spp: int, max_num_vertices: int = -1, seed: int = 0, min_num_vertices: int = 0) -> tuple[np.ndarray, np.ndarray]:
         """renderer::ltdirect with spp x W x H light paths: film (H, W, 3) and
         per-pixel variance of the estimate."""

@@ -386,6 +386,11 @@ def render_ptmis(scene: dict, num_samples: int, max_num_vertices: int, seed: int
     return {"image": img, "variance": pixel_variance(img, q, num_samples, W * H), "samples": num_samples}
 
 
+def render_ptdirect(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int) -> dict:
+    """The oracle's renderer::ptdirect (light samples only, weight 1)."""
+    return render_ptmis(scene, num_samples, max_num_vertices, seed, threads, direct_only=True)
+
+
 def render_ltdirect(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,
                     independent_light_dir: bool = False) -> dict:
     """The oracle's renderer::ltdirect (light paths connected to the sensor at
