@@ -904,11 +904,72 @@ __device__ int frame_exponent(float ext, float max_ext, float mag)
     return min(max(e, -126), 127);
 }
 
+// SAH-optimal collapse to 8-wide nodes [Ylitie, Karras, Laine 2017, "Efficient
+// incoherent ray traversal on GPUs through compressed wide BVHs", sec. 4.1]:
+// per binary node n and slot budget i = 1..8, the least SAH cost of covering
+// its subtree with at most i children of the wide node above,
+//   C(n, i) = min(C_wide(n), min_k C(l, k) + C(r, i - k))   (i >= 2)
+//   C(n, 1) = C_wide(n) = c_node A(n) + min_k C(l, k) + C(r, 8 - k)
+// and a leaf (one triangle per slot) costs c_tri A(n) per triangle.  Run
+// level by level from the deepest; dec[8 n + i - 1] keeps the split k of
+// budget i (0: n stays one child), dec[8 n] the split of n's own 8 slots.
+constexpr float kCostNode = 1.0f, kCostTri = 0.3f;
+
+__global__ void k_collapse_cost(const BNode* __restrict__ bnodes, int nbin, int depth, float* __restrict__ cost,
+                                uint8_t* __restrict__ dec)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nbin) return;
+    const BNode b = bnodes[n];
+    if (b.depth != depth) return;
+    float* C = cost + 8 * (size_t)n;
+    uint8_t* D = dec + 8 * (size_t)n;
+    const float A = node_area(b);
+    if (is_leafish(b)) {
+        const float c = kCostTri * A * (float)(b.count > 1 ? b.count : 1);
+        for (int i = 0; i < 8; i++) {
+            C[i] = c;
+            D[i] = 0;
+        }
+        return;
+    }
+    const float* L = cost + 8 * (size_t)b.left;
+    const float* R = cost + 8 * ((size_t)b.left + 1);
+    float dist[9];
+    uint8_t kd[9];
+    for (int j = 2; j <= 8; j++) {
+        float best = INFINITY;
+        uint8_t bk = 1;
+        for (int k = 1; k < j; k++) {
+            const float v = L[k - 1] + R[j - k - 1];
+            if (v < best) {
+                best = v;
+                bk = (uint8_t)k;
+            }
+        }
+        dist[j] = best;
+        kd[j] = bk;
+    }
+    const float cw = kCostNode * A + dist[8];
+    C[0] = cw;
+    D[0] = kd[8];
+    for (int i = 2; i <= 8; i++) {
+        if (dist[i] < cw) {
+            C[i - 1] = dist[i];
+            D[i - 1] = kd[i];
+        } else {
+            C[i - 1] = cw;
+            D[i - 1] = 0;
+        }
+    }
+}
+
 __global__ void k_collapse(const CollapseItem* __restrict__ in, int nin, CollapseItem* __restrict__ out,
                            const BNode* __restrict__ bnodes, const int32_t* __restrict__ idx,
                            const float* __restrict__ tris, WNode* __restrict__ wnodes, WTri* __restrict__ wtris,
                            int32_t* __restrict__ counters /* [0] wide count, [1] tri count, [2] out count */,
-                           int max_wide, uint32_t* __restrict__ status, int32_t* __restrict__ tri_slot)
+                           int max_wide, uint32_t* __restrict__ status, int32_t* __restrict__ tri_slot,
+                           const uint8_t* __restrict__ dec)
 {
     const int it = blockIdx.x * blockDim.x + threadIdx.x;
     if (it >= nin) return;
@@ -919,11 +980,32 @@ __global__ void k_collapse(const CollapseItem* __restrict__ in, int nin, Collaps
     int n = 0;
     if (parent.left < 0) {
         ch[n++] = item.bnode;
+    } else if (dec) {
+        // the children the SAH-optimal split assigns to this node's 8 slots
+        int sn[8], sb[8], top = 0;
+        const int k0 = dec[8 * (size_t)item.bnode];
+        sn[top] = parent.left + 1;
+        sb[top++] = 8 - k0;
+        sn[top] = parent.left;
+        sb[top++] = k0;
+        while (top > 0 && n < 8) {
+            const int m = sn[--top], j = sb[top];
+            const BNode bm = bnodes[m];
+            const int d = (j <= 1 || is_leafish(bm)) ? 0 : dec[8 * (size_t)m + j - 1];
+            if (d == 0 || top + 2 > 8) {
+                ch[n++] = m;
+            } else {
+                sn[top] = bm.left + 1;
+                sb[top++] = j - d;
+                sn[top] = bm.left;
+                sb[top++] = d;
+            }
+        }
     } else {
         ch[n++] = parent.left;
         ch[n++] = parent.left + 1;
     }
-    while (n < 8) {
+    while (!dec && n < 8) {
         int best = -1;
         float best_a = -1.0f;
         for (int i = 0; i < n; i++) {
@@ -1216,7 +1298,16 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
     }
     CollapseItem *qa, *qb;
     int32_t* ccount;
-    if ((rc = S.get(&qa, max_wide)) || (rc = S.get(&qb, max_wide)) || (rc = S.get(&ccount, 4))) return rc;
+    float* ccost;
+    uint8_t* cdec;
+    if ((rc = S.get(&qa, max_wide)) || (rc = S.get(&qb, max_wide)) || (rc = S.get(&ccount, 4)) ||
+        (rc = S.get(&ccost, 8 * (size_t)nbin)) || (rc = S.get(&cdec, 8 * (size_t)nbin)))
+        return rc;
+    // collapse costs, deepest level first
+    for (int d = hc[3]; d >= 0; d--) {
+        k_collapse_cost<<<(nbin + 255) / 256, 256, 0, stream>>>(bnodes, nbin, d, ccost, cdec);
+        LMGPU_CUDA_TRY(cudaGetLastError());
+    }
     const CollapseItem root_item{0, 0};
     LMGPU_CUDA_TRY(cudaMemcpyAsync(qa, &root_item, sizeof(root_item), cudaMemcpyHostToDevice, stream));
     int32_t cinit[4] = {1, 0, 0, 0};
@@ -1225,7 +1316,7 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
     while (nin > 0) {
         LMGPU_CUDA_TRY(cudaMemsetAsync(ccount + 2, 0, sizeof(int32_t), stream));
         k_collapse<<<(nin + 127) / 128, 128, 0, stream>>>(qa, nin, qb, bnodes, idx, d_tris, a->nodes, a->tris, ccount,
-                                                         max_wide, a->status, a->tri_slot);
+                                                         max_wide, a->status, a->tri_slot, cdec);
         LMGPU_CUDA_TRY(cudaGetLastError());
         int32_t next = 0;
         LMGPU_CUDA_TRY(cudaMemcpyAsync(&next, ccount + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
@@ -1454,7 +1545,7 @@ int build_static(unsigned char* base, const float* d_tris, int n, cudaStream_t s
     while (nin > 0) {
         LMGPU_CUDA_TRY(cudaMemsetAsync(ccount + 2, 0, sizeof(int32_t), stream));
         k_collapse<<<(nin + 127) / 128, 128, 0, stream>>>(qa, nin, qb, bnodes, idx, d_tris, wnodes, wtris, ccount, kSWide,
-                                                         status, nullptr);
+                                                         status, nullptr, nullptr);
         LMGPU_CUDA_TRY(cudaGetLastError());
         int32_t next = 0;
         LMGPU_CUDA_TRY(cudaMemcpyAsync(&next, ccount + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
