@@ -914,6 +914,11 @@ __device__ int frame_exponent(float ext, float max_ext, float mag)
 // level by level from the deepest; dec[8 n + i - 1] keeps the split k of
 // budget i (0: n stays one child), dec[8 n] the split of n's own 8 slots.
 constexpr float kCostNode = 1.0f, kCostTri = 0.3f;
+// Below this many triangles the greedy expansion is kept: on a 36-triangle
+// scene the SAH-optimal tree measured 1-5 % slower (per-node overhead, not
+// the SAH estimate, dominates a handful of wide nodes), on 20,832 triangles
+// even and on 1.5M triangles 3.9 % faster.
+constexpr uint64_t kSahCollapseMinTris = 4096;
 
 __global__ void k_collapse_cost(const BNode* __restrict__ bnodes, int nbin, int depth, float* __restrict__ cost,
                                 uint8_t* __restrict__ dec)
@@ -1303,8 +1308,9 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
     if ((rc = S.get(&qa, max_wide)) || (rc = S.get(&qb, max_wide)) || (rc = S.get(&ccount, 4)) ||
         (rc = S.get(&ccost, 8 * (size_t)nbin)) || (rc = S.get(&cdec, 8 * (size_t)nbin)))
         return rc;
-    // collapse costs, deepest level first
-    for (int d = hc[3]; d >= 0; d--) {
+    // collapse costs, deepest level first (large BVHs only)
+    const bool sah_collapse = ntri >= kSahCollapseMinTris;
+    for (int d = hc[3]; sah_collapse && d >= 0; d--) {
         k_collapse_cost<<<(nbin + 255) / 256, 256, 0, stream>>>(bnodes, nbin, d, ccost, cdec);
         LMGPU_CUDA_TRY(cudaGetLastError());
     }
@@ -1316,7 +1322,8 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
     while (nin > 0) {
         LMGPU_CUDA_TRY(cudaMemsetAsync(ccount + 2, 0, sizeof(int32_t), stream));
         k_collapse<<<(nin + 127) / 128, 128, 0, stream>>>(qa, nin, qb, bnodes, idx, d_tris, a->nodes, a->tris, ccount,
-                                                         max_wide, a->status, a->tri_slot, cdec);
+                                                         max_wide, a->status, a->tri_slot,
+                                                         sah_collapse ? cdec : nullptr);
         LMGPU_CUDA_TRY(cudaGetLastError());
         int32_t next = 0;
         LMGPU_CUDA_TRY(cudaMemcpyAsync(&next, ccount + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
