@@ -497,7 +497,11 @@ int lmgpu_accel_set_attributes(lmgpu_accel* accel, const float* normals, const f
  * floats (plane k of hit i at surface[k * n + i]): p (planes 0-2, o + d t),
  * gn (3-5), sn (6-8), dpdu (9-11), dpdv (12-14), dndu (15-17), dndv (18-20),
  * uv (21-22).  ToWorld is the matrix of columns (dpdu, dpdv, sn) and ToLocal
- * its transpose.  Misses (prim < 0) give zeros.  Host buffers. */
+ * its transpose.  Misses (prim < 0) give zeros.  Host buffers.
+ * The per-triangle records these queries read are packed by
+ * lmgpu_accel_set_attributes, or else by the first query after a build,
+ * which then waits for them; queries on one accel from several threads
+ * need one of the two to have returned first. */
 int lmgpu_surface(const lmgpu_accel* accel, const float* rays, const lmgpu_hit* hits, uint64_t n, float* surface);
 
 /* As lmgpu_surface on device buffers, asynchronous on `stream`. */

@@ -191,11 +191,13 @@ int launch_surface(const lmgpu_accel* ca, const float* d_rays, const lmgpu_hit* 
         if (n) LMGPU_CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(float) * LMGPU_SURFACE_PLANES * n, stream));
         return LMGPU_OK;
     }
-    // the records are derived state of the accel, packed on first use after a build
+    // the records are derived state of the accel, packed on first use after a
+    // build; the wait makes them visible to later queries on any stream
     lmgpu_accel* a = const_cast<lmgpu_accel*>(ca);
     if (a->surf_ntri != a->ntri) {
         const int rc = pack_surface(a, stream);
         if (rc) return rc;
+        LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
     }
     const uint64_t blocks = (n + kSurfaceThreads - 1) / kSurfaceThreads;
     k_surface<<<(unsigned)blocks, kSurfaceThreads, 0, stream>>>(a->surf, a->ntri, reinterpret_cast<const float4*>(d_rays),
