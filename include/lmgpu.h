@@ -500,8 +500,8 @@ int lmgpu_accel_set_attributes(lmgpu_accel* accel, const float* normals, const f
  * its transpose.  Misses (prim < 0) give zeros.  Host buffers.
  * The per-triangle records these queries read are packed by
  * lmgpu_accel_set_attributes, or else by the first query after a build,
- * which then waits for them; queries on one accel from several threads
- * need one of the two to have returned first. */
+ * which then waits for them (under the accel's lock, so concurrent queries
+ * from several threads are safe). */
 int lmgpu_surface(const lmgpu_accel* accel, const float* rays, const lmgpu_hit* hits, uint64_t n, float* surface);
 
 /* As lmgpu_surface on device buffers, asynchronous on `stream`. */

@@ -192,12 +192,16 @@ int launch_surface(const lmgpu_accel* ca, const float* d_rays, const lmgpu_hit* 
         return LMGPU_OK;
     }
     // the records are derived state of the accel, packed on first use after a
-    // build; the wait makes them visible to later queries on any stream
+    // build, under the accel's host lock; the wait makes them visible to
+    // later queries on any stream
     lmgpu_accel* a = const_cast<lmgpu_accel*>(ca);
-    if (a->surf_ntri != a->ntri) {
-        const int rc = pack_surface(a, stream);
-        if (rc) return rc;
-        LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    {
+        std::lock_guard<std::mutex> lock(a->host_mu);
+        if (a->surf_ntri != a->ntri) {
+            const int rc = pack_surface(a, stream);
+            if (rc) return rc;
+            LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+        }
     }
     const uint64_t blocks = (n + kSurfaceThreads - 1) / kSurfaceThreads;
     k_surface<<<(unsigned)blocks, kSurfaceThreads, 0, stream>>>(a->surf, a->ntri, reinterpret_cast<const float4*>(d_rays),
