@@ -217,7 +217,13 @@ int lmgpu_accel_build_meshes(lmgpu_accel* a, const lmgpu_mesh* meshes, uint32_t 
     }
     int rc = lmgpu::flatten(dev.data(), n, d_tris, nullptr, nullptr, name);
     if (rc == LMGPU_OK) rc = lmgpu_accel_build_device(a, d_tris, nf, nullptr);
-    if (rc == LMGPU_OK && cudaDeviceSynchronize() != cudaSuccess) rc = LMGPU_ERR_CUDA;
+    if (rc == LMGPU_OK) {
+        const cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) {
+            lmgpu::set_error(std::string(name) + ": " + cudaGetErrorString(e));
+            rc = LMGPU_ERR_CUDA;
+        }
+    }
     release();
     return rc;
 }
