@@ -34,7 +34,9 @@ extern "C" {
 #define LMGPU_ERR_INVALID 1     /* bad argument */
 #define LMGPU_ERR_CUDA 2        /* a CUDA runtime call failed */
 #define LMGPU_ERR_NOT_BUILT 3   /* accel used before a successful build */
-#define LMGPU_ERR_OVERFLOW 4    /* a device-side bound (traversal stack) was exceeded */
+#define LMGPU_ERR_OVERFLOW 4    /* a device-side bound (traversal stack) was exceeded, or the
+                                   tree is malformed; the accel keeps this state until its next
+                                   build, so later queries on it return it too */
 #define LMGPU_ERR_NO_DEVICE 5   /* no CUDA device visible */
 
 typedef struct {
