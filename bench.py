@@ -12,9 +12,10 @@ built once on the GPU.  Metric: Mrays/s.
          pinned host buffers: host->device rays, traversal, device->host hits
          inside the timed region.
 
-`--impl reference` times the CPU oracle of the reference's accel on the host
-cores (the reference's own sources when their x86-64 harness exists here,
-else the C restatement of accel::bvh_sahbin) on a bounded sample of the rays.
+`--impl reference` times the reference's fastest native accel, accel::qbvh,
+on all host cores over the same rays: the oracle's C restatement of it
+(bit-identical hits), or with --use-ref-binary on an x86-64 host the
+reference's own sources compiled by oracle/build_ref.sh.
 
 Under torchrun each rank traces its own 16.8M rays against a replicated BVH
 (weak scaling); rank 0 prints the JSON line with the max time over ranks.
@@ -124,12 +125,13 @@ def traffic_per_launch() -> float | None:
 
 
 class CpuReference:
-    """The CPU oracle of the reference's accel on the host cores.
+    """The reference's fastest native accel, accel::qbvh, on the host cores.
 
-    kind "port": the C restatement of accel::bvh_sahbin (oracle/), the only
-    form that runs on an aarch64 host; kind "reference": the reference's own
-    accel::qbvh compiled from its sources by oracle/build_ref.sh (x86-64
-    only), used when --use-ref-binary is given and the binary exists.
+    kind "port": the oracle's C restatement of accel::qbvh (oracle/, pinned
+    bit for bit to the reference's own qbvh: hit ids and points), which runs
+    on any host; kind "reference": the reference's own accel::qbvh compiled
+    from its sources by oracle/build_ref.sh (x86-64 only: the reference forces
+    SSE), used when --use-ref-binary is given and the binary exists.
     """
 
     def __init__(self, tris: np.ndarray, threads: int, use_ref_binary: bool = False):
@@ -140,39 +142,49 @@ class CpuReference:
         self.tris = tris
         self.threads = threads
         self.kind = "port"
+        self.build_s = None
         if use_ref_binary and os.path.exists(lmoracle.REF_ACCEL) and os.access(lmoracle.REF_ACCEL, os.X_OK):
             self.kind = "reference"
             self.acc = None
         else:
-            self.acc = lmoracle.OracleAccel(lmoracle.BVH_SAHBIN, tris)
+            t0 = time.perf_counter()
+            self.acc = lmoracle.OracleAccel(lmoracle.QBVH, tris)
+            self.build_s = time.perf_counter() - t0
+
+    def describe(self) -> str:
+        if self.kind == "reference":
+            return f"reference accel::qbvh compiled from its sources, {self.threads} threads, build excluded"
+        return (f"oracle restatement of accel::qbvh (accel_qbvh.cpp:152-497; bit-identical hits to the "
+                f"reference's), {self.threads} threads, build excluded")
+
+    def trace(self, rays: np.ndarray) -> float:
+        """Traces every ray; returns the seconds spent tracing."""
+        if self.kind == "reference":
+            with tempfile.TemporaryDirectory() as tmp:
+                ps, pr, po = (os.path.join(tmp, x) for x in ("s.bin", "r.bin", "o.bin"))
+                self.lo.write_ref_inputs(ps, pr, [self.tris], rays)
+                out = subprocess.run([self.lo.REF_ACCEL, "accel::qbvh", ps, pr, po, str(self.threads)],
+                                     capture_output=True, text=True, check=True).stdout
+            return float(json.loads(out.strip().splitlines()[-1])["trace_s"])
+        t0 = time.perf_counter()
+        self.acc.trace(rays, threads=self.threads)
+        return time.perf_counter() - t0
 
     def time_sample(self, rays: np.ndarray, budget_s: float) -> dict:
         """Traces a prefix of `rays` sized to about budget_s seconds."""
-        if self.kind == "reference":
-            n = min(len(rays), 1 << 18)
-            with tempfile.TemporaryDirectory() as tmp:
-                ps, pr, po = (os.path.join(tmp, x) for x in ("s.bin", "r.bin", "o.bin"))
-                self.lo.write_ref_inputs(ps, pr, [self.tris], rays[:n])
-                out = subprocess.run([self.lo.REF_ACCEL, "accel::qbvh", ps, pr, po, str(self.threads)],
-                                     capture_output=True, text=True, check=True).stdout
-            rec = json.loads(out.strip().splitlines()[-1])
-            return {"rays_per_s": n / rec["trace_s"], "n": n, "s": rec["trace_s"],
-                    "sample": f"{n} rays of the step, reference accel::qbvh compiled from its sources, "
-                              f"{self.threads} threads, build excluded"}
-        n = min(len(rays), 1 << 13)
-        t0 = time.perf_counter()
-        self.acc.trace(rays[:n], threads=self.threads)
-        est = n / max(time.perf_counter() - t0, 1e-9)
+        n = min(len(rays), 1 << 14)
+        est = n / max(self.trace(rays[:n]), 1e-9)
         m = int(min(len(rays), max(n, est * budget_s)))
-        t0 = time.perf_counter()
-        self.acc.trace(rays[:m], threads=self.threads)
-        dt = time.perf_counter() - t0
+        dt = self.trace(rays[:m])
         return {"rays_per_s": m / dt, "n": m, "s": dt,
-                "sample": f"{m} rays of the step, oracle restatement of accel::bvh_sahbin "
-                          f"(accel_bvh_sahbin.cpp), {self.threads} threads, {dt:.1f} s, build excluded"}
+                "sample": f"{m} rays of the step, {self.describe()}, {dt:.1f} s"}
 
 
 def run_reference(args) -> None:
+    """The reference arm: accel::qbvh on all host cores over the same scene
+    and rays.  Warm-up steps trace 2^16 rays each; every timed step traces
+    all 16,777,216 rays of the step when the whole run fits in about four
+    minutes, else the same prefix of each step's rays (marked sampled)."""
     ws, rank, _ = dist_env()
     if ws > 1 and rank != 0:
         return
@@ -182,21 +194,24 @@ def run_reference(args) -> None:
     rays = scenes.raycast_rays(N_RAYS)
     threads = os.cpu_count() or 1
     ref = CpuReference(tris, threads, use_ref_binary=args.use_ref_binary)
-    budget = max(0.5, 60.0 / max(1, args.steps + args.warmup))
-    vals = []
-    res = None
-    for k in range(args.warmup + args.steps):
-        off = (k * 1_000_003) % (N_RAYS // 2)
-        res = ref.time_sample(rays[off:], budget)
-        if k >= args.warmup:
-            vals.append(res["rays_per_s"] / 1e6)
-    v = statistics.median(vals)
+    for k in range(args.warmup):
+        ref.trace(rays[k << 16:(k + 1) << 16])
+    probe = 1 << 18
+    est = probe / ref.trace(rays[:probe])
+    per_step = int(min(N_RAYS, max(probe, est * 240.0 / max(1, args.steps))))
+    per_step = N_RAYS if per_step >= N_RAYS else per_step
+    secs = [ref.trace(rays[:per_step]) for _ in range(args.steps)]
+    total = float(sum(secs))
+    v = per_step * args.steps / total / 1e6
+    sample = (f"per step: {'all' if per_step == N_RAYS else 'the first'} {per_step} rays of the step, "
+              f"{ref.describe()}")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": N_RAYS / (v * 1e6) * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": workload_config(), "impl": "reference",
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": ref.kind,
-                             "sample": "per step: " + res["sample"]},
+            "sampled": per_step < N_RAYS, "rays_traced_per_step": per_step,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": ref.kind, "sample": sample,
+                             "accel": "accel::qbvh", "build_s": ref.build_s},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -308,7 +323,7 @@ def run_gpu(args) -> None:
             threads = os.cpu_count() or 1
             cb = CpuReference(tris, threads).time_sample(rays, 15.0)
             line["cpu_baseline"] = {"value": cb["rays_per_s"] / 1e6, "unit": UNIT, "cores": threads,
-                                    "kind": "port", "sample": cb["sample"]}
+                                    "kind": "port", "accel": "accel::qbvh", "sample": cb["sample"]}
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -733,25 +748,82 @@ def mlp_timing(g, box) -> dict:
                          "note": "forward FLOPs as issued (128-wide input, 48-wide output)"}}
 
 
+def relmse_image(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2) -> float:
+    """relMSE of a film against the reference: mean over pixels and channels
+    of (img - ref)^2 / (ref^2 + eps)."""
+    return float((((img.astype(np.float64) - ref) ** 2) / (ref * ref + eps)).mean())
+
+
+class Progressive:
+    """FP64 accumulation of a renderer's films over calls of growing sample
+    counts: the mean image, the variance of that mean, the render wall time
+    (the render calls only, film read-back included) and a curve of relMSE
+    against time."""
+
+    def __init__(self, shape):
+        self.sum = np.zeros(shape, np.float64)
+        self.var_sum = np.zeros(shape, np.float64)
+        self.spp = 0
+        self.seconds = 0.0
+        self.curve = []
+
+    def add(self, img, var, spp, seconds):
+        self.sum += img.astype(np.float64) * spp
+        self.var_sum += var.astype(np.float64) * float(spp) * float(spp)
+        self.spp += spp
+        self.seconds += seconds
+
+    def mean(self):
+        return self.sum / self.spp
+
+    def variance(self):
+        return self.var_sum / float(self.spp) ** 2
+
+
+def time_to_target(curve, target):
+    """Wall time at which relMSE (reference noise removed) first reaches
+    target: interpolated in log-log between the checkpoints that bracket it,
+    else extrapolated from the last checkpoints with relMSE proportional to
+    1 / time (the Monte Carlo rate).  Returns (seconds, extrapolated)."""
+    for (t0, _, _, e0), (t1, _, _, e1) in zip(curve, curve[1:]):
+        if e1 <= target < e0 and e0 > 0 and e1 > 0:
+            f = (np.log(e0) - np.log(target)) / (np.log(e0) - np.log(e1))
+            return float(np.exp(np.log(t0) + f * (np.log(t1) - np.log(t0)))), False
+    if curve and curve[0][3] <= target:
+        return float(curve[0][0]), False
+    tail = [c for c in curve[len(curve) // 2:] if c[3] > 0]
+    if not tail:
+        return None, True
+    c = float(np.median([t * e for t, _, _, e in tail]))
+    return c / target, True
+
+
 def run_guiding(args) -> None:
-    """Learned path guiding vs plain PT on the narrow-gap room: equal-time
-    relMSE.  The room is rendered at 480x270 (the configuration's 1920x1080
-    reduced 16x so that the FP64 reference converges inside the run): the
-    reference is path tracing with throughput-based roulette (unguided,
-    unbiased, 16,384 spp, FP64 film).  Plain renderer::pt (the drop-in, fixed
-    0.5 roulette) and the guided tracer (online training, throughput
-    roulette) each run for the same wall time T; value = relMSE(plain) /
-    relMSE(guided).  Also reported: the unguided tracer with the guided one's
-    roulette at equal time (what the roulette alone gives), the trained
-    guide frozen, and the tensor-core MLP kernels' throughput."""
-    import torch
+    """Learned path guiding vs plain PT on the narrow-gap room: the wall time
+    each method needs to reach relMSE 1e-2 against a converged FP64 image.
+
+    Reference: the unguided BSDF-sampling path tracer with throughput-based
+    roulette (unbiased, the integrand of renderer::pt) accumulated in FP64;
+    its own remaining noise (the mean of var / (ref^2 + eps)) is subtracted
+    from every measured relMSE.  Arms, each accumulated in FP64 over render
+    calls of doubling sample counts, timed around the render calls:
+      plain      renderer::pt as the drop-in (lmgpu_render_pt, roulette 0.5);
+      unguided   the guided tracer's code with no network (alpha 1) and the
+                 guided arm's throughput roulette;
+      guided     the guided tracer trained online from a fresh network
+                 (alpha 0.5, Adam lr 1e-3, batch 2^18).
+    An arm that does not reach the target within its time cap is
+    extrapolated at relMSE ~ 1 / time from its last checkpoints (marked).
+    value = time(guided) / time(plain); the target is <= 0.5."""
+    import torch  # noqa: F401  (CUDA context for the MLP timing)
 
     import lmgpu
     from lmgpu import scenes
 
-    sys.path.insert(0, os.path.join(REPO, "tests"))
-    W, H = 480, 270
-    T = float(os.environ.get("LMGPU_GUIDING_SECONDS", "4"))
+    W, H = (int(x) for x in os.environ.get("LMGPU_GUIDING_RES", "480x270").split("x"))
+    target = 1e-2
+    cap = float(os.environ.get("LMGPU_GUIDING_CAP_SECONDS", "120"))
+    ref_spp = int(os.environ.get("LMGPU_GUIDING_REF_SPP", "65536"))
     s = scenes.narrow_gap_room(W, H)
     box = scenes.scene_box(s)
     if args.mlp_only:
@@ -760,76 +832,76 @@ def run_guiding(args) -> None:
         g.close()
         return
     sc = lmgpu.Scene(s)
+    shape = (H, W, 3)
+    eps = 1e-2
 
-    def relmse(img, ref, trim=0.0):
-        e = ((img.astype(np.float64) - ref) ** 2 / (ref * ref + 1e-2)).mean(axis=2).ravel()
-        if trim > 0:
-            e = np.sort(e)[: int(e.size * (1 - trim))]
-        return float(e.mean())
-
+    # reference: FP64 accumulation in chunks of 4,096 spp
     g0 = lmgpu.Guide(box, 1)
-    t0 = time.perf_counter()
-    ref, _, _ = sc.render_pt_guided(g0, 16384, -1, 1, alpha=1.0, train=False, rr_mode=1)
-    ref_s = time.perf_counter() - t0
-    ref = ref.astype(np.float64)
+    ref = Progressive(shape)
+    chunk, seed = 4096, 1000
+    while ref.spp < ref_spp:
+        n = min(chunk, ref_spp - ref.spp)
+        t0 = time.perf_counter()
+        img, var, _ = sc.render_pt_guided(g0, n, -1, seed, alpha=1.0, train=False, rr_mode=1)
+        ref.add(img, var, n, time.perf_counter() - t0)
+        seed += 1
+    R = ref.mean()
+    floor = float((ref.variance() / (R * R + eps)).mean())
 
-    def timed(fn, spp):
-        t1 = time.perf_counter()
-        out = fn(spp)
-        return out, time.perf_counter() - t1
-
-    def equal_time(fn, probe_spp=64):
-        _, dt = timed(fn, probe_spp)
-        spp = max(1, int(probe_spp * T / dt))
-        return timed(fn, spp), spp
+    def progressive(render, first_spp, max_chunk, seed0):
+        acc = Progressive(shape)
+        spp, seed = first_spp, seed0
+        while True:
+            t0 = time.perf_counter()
+            img, var = render(spp, seed)
+            acc.add(img, var, spp, time.perf_counter() - t0)
+            raw = relmse_image(acc.mean(), R, eps)
+            acc.curve.append((acc.seconds, acc.spp, raw, raw - floor))
+            if raw - floor <= target or acc.seconds >= cap:
+                break
+            spp, seed = min(2 * spp, max_chunk), seed + 1
+        t, extrap = time_to_target(acc.curve, target)
+        return {"time_to_target_s": t, "extrapolated": extrap, "seconds_run": acc.seconds, "spp": acc.spp,
+                "final_relmse": acc.curve[-1][3], "final_relmse_raw": acc.curve[-1][2],
+                "curve": [[round(a, 4), b, round(c, 6), round(d, 6)] for a, b, c, d in acc.curve]}
 
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     l0 = sc.launch_count()
-    (plain, tp), spp_p = equal_time(lambda n: sc.render_pt(n, -1, 11)[0])
-    (unguided, tu), spp_u = equal_time(lambda n: sc.render_pt_guided(g0, n, -1, 12, alpha=1.0, train=False,
-                                                                      rr_mode=1)[0])
-    g = lmgpu.Guide(box, 3)
-    probe = lmgpu.Guide(box, 3)
-    _, dtp = timed(lambda n: sc.render_pt_guided(probe, n, -1, 13, train=True), 64)
-    spp_g = max(1, int(64 * T / dtp))
-    (guided, tg) = timed(lambda n: sc.render_pt_guided(g, n, -1, 14, train=True)[0], spp_g)
-    frozen, tf = timed(lambda n: sc.render_pt_guided(g, n, -1, 15, train=False)[0], spp_g)
+    guide = lmgpu.Guide(box, 3)
+    guided = progressive(lambda n, sd: sc.render_pt_guided(guide, n, -1, sd, train=True)[:2], 8, 1024, 20000)
+    unguided = progressive(lambda n, sd: sc.render_pt_guided(g0, n, -1, sd, alpha=1.0, train=False, rr_mode=1)[:2],
+                           8, 2048, 30000)
+    plain = progressive(lambda n, sd: sc.render_pt(n, -1, sd), 8, 4096, 40000)
     launches = sc.launch_count() - l0
     clk = clocks.stop()
-    e_p, e_u, e_g, e_f = relmse(plain, ref), relmse(unguided, ref), relmse(guided, ref), relmse(frozen, ref)
-    # equal time exactly: relMSE of a Monte Carlo estimate falls as 1 / time
-    e_p_at_g = e_p * tp / tg
-    e_u_at_g = e_u * tu / tg
+    mlp = mlp_timing(guide, box)
 
-    mlp = mlp_timing(g, box)
-
-    line = {"metric": "equal-time relMSE ratio, plain renderer::pt / guided (narrow-gap room)",
-            "value": e_p_at_g / e_g, "unit": "x", "n_gpus": 1, "steps": 1, "warmup": 1,
-            "ms_per_step": tg * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 path arithmetic; bf16 MLP with f32 accumulation",
+    tg, tu, tp = guided["time_to_target_s"], unguided["time_to_target_s"], plain["time_to_target_s"]
+    ratio = tg / tp
+    line = {"metric": "time to relMSE 1e-2, guided PT / plain renderer::pt (narrow-gap room)",
+            "value": ratio, "unit": "x", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "ms_per_step": tg * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 path arithmetic; bf16 MLP with f32 accumulation; f64 film accumulation",
             "data": "synthetic (narrow-gap room: 14-triangle room with a 0.2-wide slit, 2x2 exterior light Le 50, "
                     "100 tessellated furniture boxes, ~203k triangles)",
-            "config": {"workload": "guiding_narrow_gap_room", "width": W, "height": H,
-                       "resolution_note": "1920x1080 reduced 16x so the FP64 reference converges within the run",
-                       "seconds_per_method": T, "alpha": 0.5, "learning_rate": 1e-3, "batch": 1 << 18,
-                       "reference": {"spp": 16384, "seconds": ref_s,
-                                     "tracer": "path tracing, throughput roulette, unguided, FP64 film"},
-                       "plain_pt": {"spp": spp_p, "seconds": tp, "relmse": e_p, "relmse_trim_0.1pct": relmse(plain, ref, 1e-3),
-                                    "relmse_at_guided_time": e_p_at_g},
-                       "unguided_throughput_roulette": {"spp": spp_u, "seconds": tu, "relmse": e_u,
-                                                        "relmse_at_guided_time": e_u_at_g},
-                       "guided_online": {"spp": spp_g, "seconds": tg, "relmse": e_g,
-                                         "relmse_trim_0.1pct": relmse(guided, ref, 1e-3)},
-                       "guided_frozen_after_training": {"spp": spp_g, "seconds": tf, "relmse": e_f},
-                       "time_to_plain_relmse_fraction": e_g / e_p_at_g,
-                       "gain_over_unguided_same_roulette": e_u_at_g / e_g},
-            "e2e": {"value": e_p_at_g / e_g, "unit": "x", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": W * H * 3 * 4 * 2, "api": "lmgpu_render_pt / lmgpu_render_pt_guided (host films)"},
-            "gpu_launches": launches, "clocks": clk,
-            "mlp": mlp}
+            "config": {"workload": "guiding_narrow_gap_room", "width": W, "height": H, "target_relmse": target,
+                       "relmse": "mean over pixels and channels of (img - ref)^2 / (ref^2 + 1e-2), minus the "
+                                 "reference's own noise",
+                       "alpha": 0.5, "learning_rate": 1e-3, "batch": 1 << 18, "time_cap_s": cap,
+                       "reference": {"spp": ref.spp, "seconds": ref.seconds, "noise_relmse": floor,
+                                     "tracer": "unguided BSDF-sampling path tracing, throughput roulette, FP64 "
+                                               "accumulation"},
+                       "target_met": bool(ratio <= 0.5),
+                       "guided_over_unguided_same_roulette": tg / tu,
+                       "unguided_over_plain": tu / tp},
+            "arms": {"guided": guided, "unguided_same_roulette": unguided, "plain_renderer_pt": plain},
+            "e2e": {"value": ratio, "unit": "x", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": W * H * 3 * 4 * 2,
+                    "api": "lmgpu_render_pt / lmgpu_render_pt_guided (host films)"},
+            "gpu_launches": launches, "clocks": clk, "mlp": mlp}
     print(json.dumps(line), flush=True)
-    for x in (g, g0, probe):
+    for x in (guide, g0):
         x.close()
     sc.close()
 

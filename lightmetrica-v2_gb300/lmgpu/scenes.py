@@ -280,6 +280,14 @@ def _icosphere4() -> np.ndarray:
     return _ICO4
 
 
+def instance_tris(unit: np.ndarray, scale: float, shift) -> np.ndarray:
+    """Triangles of an instanced primitive: the float32 unit mesh widened to
+    float64, scaled, shifted and rounded back to float32 (the same arithmetic
+    as the sphere grid, so the result is bit-identical on any machine)."""
+    v = np.asarray(unit, np.float32).astype(np.float64).reshape(-1, 3) * float(scale) + np.asarray(shift, np.float64)
+    return v.reshape(-1, 9).astype(np.float32)
+
+
 def phong_to_ggx_roughness(n: float) -> float:
     """GGX roughness standing in for a Phong exponent n: alpha = sqrt(2 / (n + 2))
     (the reference has no Phong BSDF; bsdf::cook_torrance takes its place)."""
@@ -309,14 +317,19 @@ def sphere_grid_scene(seed: int, index: int, width: int | None = None, height: i
     for k in range(grid * grid):
         cx, cz = (k % grid) * 1.2, (k // grid) * 1.2
         r = radii[k]
-        tris = (ico.reshape(-1, 3) * r + np.array([cx, r + 1e-3, cz])).reshape(-1, 9).astype(np.float32)
+        shift = np.array([cx, r + 1e-3, cz])
+        tris = (ico.reshape(-1, 3) * r + shift).reshape(-1, 9).astype(np.float32)
+        # how the triangles were made: the unit level-4 icosphere scaled by r
+        # and shifted (lets a fixture store the sphere once)
+        inst = ("ico4", float(r), tuple(float(x) for x in shift))
         if kinds[k] == 0:
-            prims.append({"bsdf": BSDF_DIFFUSE, "R": tuple(albedo[k]), "tris": tris})
+            prims.append({"bsdf": BSDF_DIFFUSE, "R": tuple(albedo[k]), "tris": tris, "instance": inst})
         elif kinds[k] == 1:
             prims.append({"bsdf": BSDF_COOK_TORRANCE, "R": tuple(albedo[k]),
-                          "roughness": phong_to_ggx_roughness(expo[k]), "tris": tris})
+                          "roughness": phong_to_ggx_roughness(expo[k]), "tris": tris, "instance": inst})
         else:
-            prims.append({"bsdf": BSDF_DIELECTRIC, "R": (1.0, 1.0, 1.0), "eta1": 1.0, "eta2": 1.5, "tris": tris})
+            prims.append({"bsdf": BSDF_DIELECTRIC, "R": (1.0, 1.0, 1.0), "eta1": 1.0, "eta2": 1.5, "tris": tris,
+                          "instance": inst})
     light = closed_icosphere(2, 1.0, (span * 0.5, 8.0, span * 0.5))
     prims.append({"bsdf": BSDF_NULL, "light": True, "Le": (60.0, 55.0, 50.0), "tris": light})
     res = [(640, 360), (1280, 720), (1920, 1080)]

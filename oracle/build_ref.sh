@@ -21,10 +21,11 @@
 #     property tree, assets, film, scheduler and scene of liblightmetrica.
 # x86-64 only: the reference forces SSE intrinsics (math.h:69, accel_qbvh.cpp:34).
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   default: $LM_REFERENCE_ROOT, else a `reference` directory beside the repository
 set -euo pipefail
-REF="${1:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${1:-${LM_REFERENCE_ROOT:-$HERE/../../reference}}"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src/liblightmetrica" ]; then
   echo "reference tree not found at $REF; nothing to build" >&2
@@ -41,7 +42,7 @@ INC="-I$HERE/refharness/shim -I$REF/include -I$REF/external-src/dSFMT-src-2.2.3"
 FLAGS="-std=c++14 -O3 -msse4.2 -ffp-contract=off -w"
 L="$REF/src/liblightmetrica"
 
-ACCEL_SRCS=("$L/accel/accel_naive.cpp" "$L/accel/accel_bvh_sahbin.cpp" "$L/accel/accel_qbvh.cpp" "$HERE/refharness/ref_runtime.cpp")
+ACCEL_SRCS=("$L/accel/accel_naive.cpp" "$L/accel/accel_bvh_sahbin.cpp" "$L/accel/accel_bvh_sah.cpp" "$L/accel/accel_qbvh.cpp" "$HERE/refharness/ref_runtime.cpp")
 RENDER_SRCS=("$L/renderer/renderer_pt.cpp" "$L/renderer/renderer_bdpt.cpp" "$L/renderer/renderer_ptmis.cpp" "$L/renderer/renderer_ptdirect.cpp" "$L/renderer/renderer_ltdirect.cpp" "$L/renderer/renderer_vcm.cpp" "$L/renderer/subpathsampler.cpp" "$L/asset/bsdf/bsdf_diffuse.cpp" "$L/asset/bsdf/bsdf_null.cpp"
              "$L/asset/bsdf/bsdf_flesnel.cpp" "$L/asset/bsdf/bsdf_cooktorrance.cpp"
              "$L/asset/light/light_area.cpp" "$L/asset/light/light_env.cpp" "$L/asset/sensor/sensor_pinhole.cpp"

@@ -52,12 +52,13 @@ int  lmo_triaccel_intersect(const lmo_triaccel* tri, const float o[3], const flo
  * (v1, v2, v3 in global triangle order). */
 typedef struct lmo_accel lmo_accel;
 
-/* kind: 0 = accel::naive (accel_naive.cpp), 1 = accel::bvh_sahbin (accel_bvh_sahbin.cpp) */
+/* kind: 0 = accel::naive (accel_naive.cpp), 1 = accel::bvh_sahbin (accel_bvh_sahbin.cpp),
+ *       2 = accel::qbvh (accel_qbvh.cpp) */
 lmo_accel* lmo_accel_build(int kind, const float* tris, size_t ntri);
 void       lmo_accel_free(lmo_accel* a);
 /* Closest hit for n rays using `threads` POSIX threads. */
 void       lmo_accel_trace(const lmo_accel* a, const float* rays, size_t n, lmo_hit* out, int threads);
-/* Counts of the binary BVH (bvh_sahbin only): nodes, leaves, max depth. */
+/* Counts of the BVH: nodes, leaves, max binary depth (bvh_sahbin: binary nodes; qbvh: 4-wide nodes). */
 void       lmo_accel_stats(const lmo_accel* a, size_t* nodes, size_t* leaves, int* depth);
 
 /* FP64 recomputation of the ray parameter t at which the ray meets the plane

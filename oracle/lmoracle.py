@@ -19,6 +19,7 @@ HIT_DTYPE = np.dtype([("id", "<i4"), ("t", "<f4"), ("b0", "<f4"), ("b1", "<f4"),
 
 NAIVE = 0
 BVH_SAHBIN = 1
+QBVH = 2
 
 
 def build() -> str:
@@ -74,7 +75,7 @@ def lib() -> ctypes.CDLL:
 
 
 class OracleAccel:
-    """accel::naive (kind 0) or accel::bvh_sahbin (kind 1), restated in C."""
+    """accel::naive (kind 0), accel::bvh_sahbin (kind 1) or accel::qbvh (kind 2), restated in C."""
 
     def __init__(self, kind: int, tris: np.ndarray):
         self.tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
@@ -189,15 +190,20 @@ def write_render_scene(path: str, scene: dict, num_samples: int, max_num_vertice
 
 def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,
                    double: bool = False, renderer: str = "pt", mis: str | None = None,
-                   params: dict | None = None) -> dict:
+                   params: dict | None = None, accel: str | None = None) -> dict:
     """Runs the reference renderer::pt or renderer::bdpt (compiled from its
     sources) and returns the film (H, W, 3), the per-pixel variance of that
-    estimate and timing."""
+    estimate and timing.  accel overrides the harness's accel component
+    (accel::qbvh in single precision, accel::bvh_sahbin in double); every
+    accel returns the same closest hits, so the film does not depend on it."""
     import json
     import tempfile
 
     cam = scene["camera"]
     W, H = cam["width"], cam["height"]
+    env = dict(os.environ)
+    if accel:
+        env["LM_REF_ACCEL"] = accel
     with tempfile.TemporaryDirectory() as tmp:
         ps, po = os.path.join(tmp, "scene.bin"), os.path.join(tmp, "out.bin")
         write_render_scene(ps, scene, num_samples, max_num_vertices, seed, threads)
@@ -206,7 +212,7 @@ def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: i
         if mis:
             extra["mis"] = mis
         cmd = [exe, ps, po, renderer] + [f"{k}={v}" for k, v in extra.items()]
-        out = subprocess.run(cmd, capture_output=True, text=True, check=True).stdout
+        out = subprocess.run(cmd, capture_output=True, text=True, check=True, env=env).stdout
         raw = open(po, "rb").read()
     n = W * H * 3
     img = np.frombuffer(raw[:4 * n], dtype=np.float32).reshape(H, W, 3)

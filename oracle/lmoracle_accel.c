@@ -6,6 +6,7 @@
  *   Bound::Intersect / SurfaceArea / ... include/lightmetrica/bound.h:39-91
  *   Accel_Naive::Build / Intersect       src/liblightmetrica/accel/accel_naive.cpp:59-124
  *   Accel_BVHSAHBin::Build / Intersect   src/liblightmetrica/accel/accel_bvh_sahbin.cpp:70-288
+ *   Accel_QBVH::Build / Intersect        src/liblightmetrica/accel/accel_qbvh.cpp:152-497
  * in single precision with the reference's operation order.  Must be built
  * with -ffp-contract=off.
  */
@@ -153,16 +154,30 @@ typedef struct {
     int a, b; /* leaf: begin, end ; internal: child1, child2 */
 } lmo_node;
 
+/* 4-wide node of accel::qbvh (accel_qbvh.cpp:56-128): child bounds in
+ * structure-of-arrays form, bmin/bmax[axis][child]; children[c] is a node
+ * index (>= 0), a leaf (bit 31 set, bits 30:27 = size - 1, bits 26:0 = first
+ * index into `indices`) or QBVH_EMPTY. */
+typedef struct {
+    float b[2][3][4];
+    int children[4];
+} lmo_qnode;
+
+#define QBVH_EMPTY ((int)0xffffffff)
+
 struct lmo_accel {
     int kind;
     size_t ntri;
     lmo_triaccel* tris;
-    /* bvh_sahbin */
+    /* bvh_sahbin and qbvh */
     lmo_bound* bounds;
     int* indices;
     lmo_node* nodes;
     size_t nnodes, cap;
     int depth;
+    /* qbvh */
+    lmo_qnode* qnodes;
+    size_t nq, qcap;
 };
 
 #define NUM_BINS 100
@@ -281,13 +296,16 @@ done:;
     return idx;
 }
 
+static int qbvh_push(lmo_accel* A);
+static void qbvh_build_rec(lmo_accel* A, int begin, int end, int parent, int child, int depth);
+
 lmo_accel* lmo_accel_build(int kind, const float* tris, size_t ntri)
 {
     lmo_accel* A = (lmo_accel*)calloc(1, sizeof(lmo_accel));
     A->kind = kind;
     A->ntri = ntri;
     A->tris = (lmo_triaccel*)malloc(sizeof(lmo_triaccel) * (ntri ? ntri : 1));
-    if (kind == 1) {
+    if (kind == 1 || kind == 2) {
         A->bounds = (lmo_bound*)malloc(sizeof(lmo_bound) * (ntri ? ntri : 1));
         A->indices = (int*)malloc(sizeof(int) * (ntri ? ntri : 1));
     }
@@ -296,7 +314,7 @@ lmo_accel* lmo_accel_build(int kind, const float* tris, size_t ntri)
         lmo_triaccel_load(&A->tris[i], p, p + 3, p + 6);
         A->tris[i].face_index = (uint32_t)i;
         A->tris[i].prim_index = 0;
-        if (kind == 1) {
+        if (kind == 1 || kind == 2) {
             lmo_bound b;
             bound_empty(&b);
             bound_union_p(&b, p);
@@ -308,19 +326,31 @@ lmo_accel* lmo_accel_build(int kind, const float* tris, size_t ntri)
         }
     }
     if (kind == 1 && ntri > 0) build_rec(A, 0, (int)ntri, 0);
+    if (kind == 2) {
+        qbvh_push(A);
+        qbvh_build_rec(A, 0, (int)ntri, 0, 0, 0);
+    }
     return A;
 }
 
 void lmo_accel_free(lmo_accel* A)
 {
     if (!A) return;
-    free(A->tris); free(A->bounds); free(A->indices); free(A->nodes);
+    free(A->tris); free(A->bounds); free(A->indices); free(A->nodes); free(A->qnodes);
     free(A);
 }
 
 void lmo_accel_stats(const lmo_accel* A, size_t* nodes, size_t* leaves, int* depth)
 {
     size_t nl = 0;
+    if (A->kind == 2) {
+        for (size_t i = 0; i < A->nq; i++)
+            for (int c = 0; c < 4; c++) nl += (A->qnodes[i].children[c] < 0 && A->qnodes[i].children[c] != QBVH_EMPTY);
+        if (nodes) *nodes = A->nq;
+        if (leaves) *leaves = nl;
+        if (depth) *depth = A->depth;
+        return;
+    }
     for (size_t i = 0; i < A->nnodes; i++) nl += A->nodes[i].isleaf ? 1 : 0;
     if (nodes) *nodes = A->nnodes;
     if (leaves) *leaves = nl;
@@ -335,6 +365,207 @@ static void finish_hit(lmo_hit* h, const float o[3], const float d[3], int id, f
     h->b1 = b1;
     /* ray.o + ray.d * maxT (accel_naive.cpp:118) */
     for (int k = 0; k < 3; k++) h->p[k] = o[k] + d[k] * t;
+}
+
+
+/* ------------------------------------------------------------------------- */
+/* accel::qbvh                                                                */
+
+static int qbvh_push(lmo_accel* A)
+{
+    if (A->nq == A->qcap) {
+        A->qcap = A->qcap ? A->qcap * 2 : 1024;
+        A->qnodes = (lmo_qnode*)realloc(A->qnodes, A->qcap * sizeof(lmo_qnode));
+    }
+    lmo_qnode* q = &A->qnodes[A->nq];
+    /* QBVHNode() (accel_qbvh.cpp:75-86): +inf / -inf bounds, empty children */
+    for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 4; c++) { q->b[0][a][c] = INFINITY; q->b[1][a][c] = -INFINITY; }
+    for (int c = 0; c < 4; c++) q->children[c] = QBVH_EMPTY;
+    return (int)(A->nq++);
+}
+
+/* QBVHNode::SetBound (accel_qbvh.cpp:88-95) */
+static void qbvh_set_bound(lmo_qnode* q, int c, const lmo_bound* b)
+{
+    for (int a = 0; a < 3; a++) { q->b[0][a][c] = b->mn[a]; q->b[1][a][c] = b->mx[a]; }
+}
+
+/* One call of the recursive Build_ lambda (accel_qbvh.cpp:200-373): binned
+ * SAH over the longest axis of the centroid bound, leaves below 10
+ * triangles, and two binary levels folded into one 4-wide node (even depths
+ * open a node whose children 0 and 2 the two halves fill; odd depths fill
+ * the parent's slots `child` and `child + 1`). */
+static void qbvh_build_rec(lmo_accel* A, int begin, int end, int parent, int child, int depth)
+{
+    if (depth > A->depth) A->depth = depth;
+    lmo_bound nb;
+    bound_empty(&nb);
+    for (int i = begin; i < end; i++) bound_union_b(&nb, &A->bounds[A->indices[i]]);
+    if (end - begin < LEAF_NUM) {
+        lmo_qnode* q = &A->qnodes[parent];
+        qbvh_set_bound(q, child, &nb);
+        /* QBVHNode::CreateLeaf (accel_qbvh.cpp:97-110) */
+        const int size = end - begin;
+        q->children[child] = size == 0 ? QBVH_EMPTY
+                                       : (int)(0x80000000u | ((unsigned)((size - 1) & 0xf) << 27) |
+                                               ((unsigned)begin & 0x07ffffffu));
+        return;
+    }
+    lmo_bound cb;
+    bound_empty(&cb);
+    for (int i = begin; i < end; i++) {
+        const lmo_bound* b = &A->bounds[A->indices[i]];
+        float c[3] = {bound_centroid(b, 0), bound_centroid(b, 1), bound_centroid(b, 2)};
+        bound_union_p(&cb, c);
+    }
+    const int axis = bound_longest_axis(&cb);
+    const float mn = cb.mn[axis], mx = cb.mx[axis];
+    int mid;
+    if (!(mx > mn)) {
+        /* Every centroid coincides: the reference divides 0 by 0 here and
+         * indexes its bins with the converted NaN (undefined behaviour, a
+         * crash on x86-64); the oracle halves the range in index order. */
+        mid = begin + (end - begin) / 2;
+    } else {
+        lmo_bound bins[NUM_BINS];
+        int counts[NUM_BINS];
+        for (int i = 0; i < NUM_BINS; i++) { bound_empty(&bins[i]); counts[i] = 0; }
+        for (int i = begin; i < end; i++) {
+            const lmo_bound* b = &A->bounds[A->indices[i]];
+            int t = bin_of(bound_centroid(b, axis), mn, mx);
+            bound_union_b(&bins[t], b);
+            counts[t]++;
+        }
+        /* prefix / suffix unions give the reference's per-split re-unions
+         * (accel_qbvh.cpp:263-291) bit for bit: unions are exact min / max */
+        lmo_bound pre[NUM_BINS], suf[NUM_BINS];
+        int npre[NUM_BINS], nsuf[NUM_BINS];
+        lmo_bound acc;
+        int cnt = 0;
+        bound_empty(&acc);
+        for (int i = 0; i < NUM_BINS; i++) { bound_union_b(&acc, &bins[i]); cnt += counts[i]; pre[i] = acc; npre[i] = cnt; }
+        bound_empty(&acc);
+        cnt = 0;
+        for (int i = NUM_BINS - 1; i >= 0; i--) { bound_union_b(&acc, &bins[i]); cnt += counts[i]; suf[i] = acc; nsuf[i] = cnt; }
+        const float area = bound_area(&nb);
+        int best = 0;
+        float best_cost = 0.0f;
+        for (int split = 0; split < NUM_BINS - 1; split++) {
+            const int n1 = npre[split], n2 = nsuf[split + 1];
+            const float C1 = n1 > 0 ? bound_area(&pre[split]) * (float)n1 : 0.0f;
+            const float C2 = n2 > 0 ? bound_area(&suf[split + 1]) * (float)n2 : 0.0f;
+            const float cost = 0.125f + (C1 + C2) / area;
+            if (split == 0 || cost < best_cost) { best = split; best_cost = cost; } /* std::min_element */
+        }
+        /* std::partition (libstdc++'s bidirectional form): the same swaps */
+        int* first = A->indices + begin;
+        int* last = A->indices + end;
+        for (;;) {
+            for (;;) {
+                if (first == last) goto done;
+                if (bin_of(bound_centroid(&A->bounds[*first], axis), mn, mx) <= best) ++first;
+                else break;
+            }
+            --last;
+            for (;;) {
+                if (first == last) goto done;
+                if (!(bin_of(bound_centroid(&A->bounds[*last], axis), mn, mx) <= best)) --last;
+                else break;
+            }
+            { int tmp = *first; *first = *last; *last = tmp; }
+            ++first;
+        }
+done:
+        mid = (int)(first - A->indices);
+    }
+    int current, c1, c2;
+    if (depth % 2 == 1) {
+        current = parent; c1 = child; c2 = child + 1;
+    } else {
+        current = qbvh_push(A);
+        A->qnodes[parent].children[child] = current;   /* CreateIntermediateNode */
+        qbvh_set_bound(&A->qnodes[parent], child, &nb);
+        c1 = 0; c2 = 2;
+    }
+    qbvh_build_rec(A, begin, mid, current, c1, depth + 1);
+    qbvh_build_rec(A, mid, end, current, c2, depth + 1);
+}
+
+/* Four-lane float vectors (SSE on x86-64, NEON on aarch64, by the compiler). */
+typedef float lmo_v4f __attribute__((vector_size(16)));
+typedef int lmo_v4i __attribute__((vector_size(16)));
+
+/* _mm_max_ps / _mm_min_ps lane rule: a > b ? a : b and a < b ? a : b
+ * (the second operand when either is NaN). */
+static inline lmo_v4f v4_max(lmo_v4f a, lmo_v4f b)
+{
+    lmo_v4i m = a > b;
+    return (lmo_v4f)(((lmo_v4i)a & m) | ((lmo_v4i)b & ~m));
+}
+static inline lmo_v4f v4_min(lmo_v4f a, lmo_v4f b)
+{
+    lmo_v4i m = a < b;
+    return (lmo_v4f)(((lmo_v4i)a & m) | ((lmo_v4i)b & ~m));
+}
+
+/* QBVHNode::Intersect (accel_qbvh.cpp:117-128) and Accel_QBVH::Intersect
+ * (accel_qbvh.cpp:398-497): iterative traversal with a stack of node words,
+ * children pushed 0..3 as their slabs are hit (popped in reverse), maxT
+ * narrowed by every accepted triangle, ties resolved by the last accepted. */
+static void trace_qbvh(const lmo_accel* A, const float* r, lmo_hit* h)
+{
+    const float* o = r;
+    const float* d = r + 4;
+    float minT = r[3], maxT = r[7];
+    int hit = 0, minIndex = 0;
+    float mb0 = 0, mb1 = 0;
+    lmo_v4f inv_min[3], inv_max[3], org[3];
+    int sign[3];
+    for (int k = 0; k < 3; k++) {
+        const float im = d[k] == 0.0f ? 1e-3f /* Math::EpsLarge<float> */ : 1.0f / d[k];
+        const float iM = d[k] == 0.0f ? LMO_FLT_INF : 1.0f / d[k];
+        inv_min[k] = (lmo_v4f){im, im, im, im};
+        inv_max[k] = (lmo_v4f){iM, iM, iM, iM};
+        org[k] = (lmo_v4f){o[k], o[k], o[k], o[k]};
+        sign[k] = d[k] < 0.0f;
+    }
+    int stack[128];
+    int sp = 0;
+    stack[0] = 0;
+    while (sp >= 0) {
+        const int data = stack[sp--];
+        if (data < 0) {
+            if (data == QBVH_EMPTY) continue;
+            const unsigned size = (unsigned)(((data >> 27) & 0xf) + 1);
+            const unsigned offset = (unsigned)data & 0x07ffffffu;
+            for (unsigned i = offset; i < offset + size; i++) {
+                float t, b0, b1;
+                const int ti = A->indices[i];
+                if (lmo_triaccel_intersect(&A->tris[ti], o, d, minT, maxT, &b0, &b1, &t)) {
+                    hit = 1; maxT = t; minIndex = ti; mb0 = b0; mb1 = b1;
+                }
+            }
+            continue;
+        }
+        const lmo_qnode* q = &A->qnodes[data];
+        lmo_v4f vmin = (lmo_v4f){minT, minT, minT, minT};
+        lmo_v4f vmax = (lmo_v4f){maxT, maxT, maxT, maxT};
+        for (int k = 0; k < 3; k++) {
+            lmo_v4f lo, hi;
+            memcpy(&lo, q->b[sign[k]][k], 16);
+            memcpy(&hi, q->b[1 - sign[k]][k], 16);
+            vmin = v4_max(vmin, (lo - org[k]) * inv_min[k]);
+            vmax = v4_min(vmax, (hi - org[k]) * inv_max[k]);
+        }
+        lmo_v4i m = vmax >= vmin;
+        if (m[0]) stack[++sp] = q->children[0];
+        if (m[1]) stack[++sp] = q->children[1];
+        if (m[2]) stack[++sp] = q->children[2];
+        if (m[3]) stack[++sp] = q->children[3];
+    }
+    if (!hit) { memset(h, 0, sizeof(*h)); h->id = -1; return; }
+    finish_hit(h, o, d, minIndex, maxT, mb0, mb1);
 }
 
 /* accel_naive.cpp:92-124 */
@@ -407,6 +638,7 @@ static void* trace_worker(void* p)
         size_t e = b + TRACE_CHUNK < J->n ? b + TRACE_CHUNK : J->n;
         for (size_t i = b; i < e; i++) {
             if (J->A->kind == 0) trace_naive(J->A, J->rays + 8 * i, &J->out[i]);
+            else if (J->A->kind == 2) trace_qbvh(J->A, J->rays + 8 * i, &J->out[i]);
             else trace_bvh(J->A, J->rays + 8 * i, &J->out[i]);
         }
     }

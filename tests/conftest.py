@@ -19,6 +19,13 @@ def repo_dir():
 
 
 @pytest.fixture(scope="session")
+def reference_root():
+    """The reference source tree: $LM_REFERENCE_ROOT, else a `reference`
+    directory beside the repository (absent on machines without it)."""
+    return os.environ.get("LM_REFERENCE_ROOT", os.path.join(os.path.dirname(REPO), "reference"))
+
+
+@pytest.fixture(scope="session")
 def golden_dir():
     return os.path.join(REPO, "tests", "golden")
 

@@ -1,6 +1,7 @@
 """Generates the golden fixtures of tests/golden/ from the reference itself.
 
-Run in a checkout that has the reference tree (default /root/reference) and
+Run in a checkout that has the reference tree (default: $LM_REFERENCE_ROOT, else
+a `reference` directory beside the repository) and
 the reference harness built by oracle/build_ref.sh (oracle/_ref/ref_accel):
 
     python tests/golden/make_golden.py [REFERENCE_ROOT] [--only NAME[,NAME...]]
@@ -212,12 +213,33 @@ def soup_case(tmp: str) -> dict:
     return out
 
 
+INSTANCE_MESHES = {"ico4": lambda: scenes.closed_icosphere(4)}
+
+
 def scene_arrays(sc: dict) -> dict:
-    """A path-tracing scene as flat arrays (read back by tests/ptscene.py)."""
+    """A path-tracing scene as flat arrays (read back by tests/ptscene.py).
+    Primitives made by scaling and shifting a unit mesh (the sphere grid's
+    icospheres) are stored as that mesh once plus a scale and a shift each;
+    tris_sha256 pins the regenerated triangles."""
+    import hashlib
+
     out = {"nprims": np.int32(len(sc["prims"]))}
+    digest = hashlib.sha256()
     for i, p0 in enumerate(sc["prims"]):
         p = scenes.prim_params(p0)
-        out[f"prim{i}_tris"] = np.asarray(p["tris"], np.float32)
+        tris = np.ascontiguousarray(p["tris"], np.float32)
+        digest.update(tris.tobytes())
+        inst = p0.get("instance")
+        if inst is not None:
+            name, scale, shift = inst
+            unit = INSTANCE_MESHES[name]()
+            assert np.array_equal(scenes.instance_tris(unit, scale, shift), tris)
+            out[f"mesh_{name}"] = unit
+            out[f"prim{i}_inst_mesh"] = np.array(name)
+            out[f"prim{i}_inst_scale"] = np.float64(scale)
+            out[f"prim{i}_inst_shift"] = np.array(shift, np.float64)
+        else:
+            out[f"prim{i}_tris"] = tris
         out[f"prim{i}_bsdf"] = np.int32(p["bsdf"])
         out[f"prim{i}_light"] = np.int32(1 if p["light"] else 0)
         for k in ("R", "Le", "ct_eta", "ct_k"):
@@ -230,18 +252,25 @@ def scene_arrays(sc: dict) -> dict:
     out["width"], out["height"] = np.int32(c["width"]), np.int32(c["height"])
     out["has_env"] = np.int32(1 if sc.get("env") is not None else 0)
     out["env_Le"] = np.array(sc.get("env") or (0.0, 0.0, 0.0), np.float32)
+    out["tris_sha256"] = np.array(digest.hexdigest())
     return out
 
 
 def pt_case(sc: dict, spp: int, seed: int, renderer: str = "pt", max_num_vertices: int = 9,
-            mis: str | None = None, min_num_vertices: int = 0) -> dict:
+            mis: str | None = None, min_num_vertices: int = 0, accel64: str | None = None) -> dict:
+    """accel64: the accel of the double-precision run (default the harness's
+    accel::bvh_sahbin).  accel::bvh_sahbin divides 0 by 0 when the centroids
+    of a node's triangles coincide on its split axis
+    (accel_bvh_sahbin.cpp:155-157) and crashes on such scenes (the caustic
+    room, the sphere grid); accel::bvh_sah (sorted object splits) has no such
+    case and returns the same closest hits."""
     W, H = sc["camera"]["width"], sc["camera"]["height"]
     N = W * H * spp
     extra = {"min_num_vertices": min_num_vertices} if min_num_vertices else None
     f = lo.run_ref_render(sc, N, max_num_vertices, seed, os.cpu_count() or 8, renderer=renderer, mis=mis,
                           params=extra)
     d = lo.run_ref_render(sc, N, max_num_vertices, seed + 1, os.cpu_count() or 8, double=True, renderer=renderer,
-                          mis=mis, params=extra)
+                          mis=mis, params=extra, accel=accel64)
     out = scene_arrays(sc)
     out.update({"num_samples": np.int64(N), "max_num_vertices": np.int32(max_num_vertices),
                 "min_num_vertices": np.int32(min_num_vertices),
@@ -347,7 +376,7 @@ def main() -> None:
         i = args.index("--only")
         only = set(args[i + 1].split(","))
         del args[i:i + 2]
-    ref = args[0] if args else "/root/reference"
+    ref = args[0] if args else os.environ.get("LM_REFERENCE_ROOT", os.path.join(os.path.dirname(REPO), "reference"))
     want = lambda name: only is None or name in only  # noqa: E731
     if not (os.path.exists(lo.REF_ACCEL) and os.path.exists(lo.REF_RENDER) and os.path.exists(lo.REF_RENDER64)):
         subprocess.run([os.path.join(REPO, "oracle", "build_ref.sh"), ref], check=True)
@@ -401,6 +430,18 @@ def main() -> None:
     for mode in ("vcm", "bdpm"):
         if want(f"cornell_{mode}"):
             np.savez_compressed(os.path.join(HERE, f"cornell_{mode}.npz"), **vcm_case(mode, 20241601))
+    if want("caustic_bdpt"):
+        # the bidirectional configuration's own scene on a 48 x 27 film
+        np.savez_compressed(os.path.join(HERE, "caustic_bdpt.npz"),
+                            **pt_case(scenes.caustic_room(48, 27), 16384, 20250101, "bdpt", 11,
+                                      accel64="accel::bvh_sah"))
+    if want("grid_pt"):
+        # one view of the batched configuration: a 4 x 4 sphere grid (every
+        # BSDF kind, icosphere light, constant environment), 96 x 54, paths of
+        # up to 16 segments
+        np.savez_compressed(os.path.join(HERE, "grid_pt.npz"),
+                            **pt_case(scenes.sphere_grid_scene(7, 0, 96, 54, grid=4), 16384, 20250201, "pt", 17,
+                                      accel64="accel::bvh_sah"))
     print("fixtures written to", HERE)
 
 

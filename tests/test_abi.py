@@ -63,7 +63,7 @@ def test_null_arguments_rejected(gpu_lib):
 @pytest.mark.parametrize("plugin", ["accel_cuda", "renderer_pt_cuda", "renderer_ptmis_cuda", "renderer_ptdirect_cuda",
                                     "renderer_ltdirect_cuda", "renderer_bdpt_cuda", "renderer_pt_guided_cuda",
                                     "renderer_vcm_cuda"])
-def test_reference_plugin_compiles_against_reference_headers(repo_dir, plugin):
+def test_reference_plugin_compiles_against_reference_headers(repo_dir, reference_root, plugin):
     """plugin/*.cpp, the bindings a maintainer adds to the reference tree
     (accel::cuda, renderer::pt_cuda, renderer::ptmis_cuda,
     renderer::ptdirect_cuda, renderer::ltdirect_cuda, renderer::bdpt_cuda,
@@ -73,7 +73,7 @@ def test_reference_plugin_compiles_against_reference_headers(repo_dir, plugin):
     import platform
     import shutil
 
-    ref = "/root/reference/include"
+    ref = os.path.join(reference_root, "include")
     if not os.path.isdir(ref) or platform.machine() != "x86_64" or not shutil.which("g++"):
         pytest.skip("reference headers or x86-64 g++ not available")
     src = os.path.join(repo_dir, "lightmetrica-v2_gb300", "plugin", plugin + ".cpp")

@@ -87,3 +87,29 @@ def test_batch_autotune_and_device_entry(gpu_lib, golden_dir):
     b.close()
     for sc in scs:
         sc.close()
+
+
+def test_sphere_grid_view_matches_reference_film(gpu_lib, golden_dir):
+    """One view of the batched configuration (a 4 x 4 grid of level-4
+    icospheres in Lambertian, GGX-for-Phong and glass BSDFs on a ground
+    plane, an icosphere light and a constant environment; 96 x 54, paths of
+    up to 16 segments) batched with the Cornell box: the batched renderer
+    (roulette after 3 segments) and lmgpu_render_pt (the reference's
+    roulette) each against the reference's own renderer::pt film (double
+    precision, 16,384 samples per pixel)."""
+    grid, z = ptscene.load_scene(golden_dir, "grid_pt")
+    mnv = int(z["max_num_vertices"])
+    assert mnv == 17
+    cb, _ = ptscene.load_cornell(golden_dir)
+    cb["camera"].update(width=40, height=24)
+    scs = [gpu_lib.Scene(grid), gpu_lib.Scene(cb)]
+    b = gpu_lib.Batch(scs)
+    (img, var), _ = b.render_pt(32768, mnv, 41, rr_depth=3)
+    s = imgcheck.assert_same_image(img, var, z["ref64_image"], z["ref64_variance"], "batch vs ref64 (sphere grid)")
+    print("batch", s, "relMSE", imgcheck.relmse(img, z["ref64_image"]))
+    b.close()
+    img, var = scs[0].render_pt(32768, mnv, 43)
+    s = imgcheck.assert_same_image(img, var, z["ref64_image"], z["ref64_variance"], "pt vs ref64 (sphere grid)")
+    print("pt", s, "relMSE", imgcheck.relmse(img, z["ref64_image"]))
+    for sc in scs:
+        sc.close()

@@ -111,3 +111,30 @@ def test_bdpt_simple_weight_matches_reference_film(gpu_lib, golden_dir):
     sc.close()
     print(imgcheck.assert_same_image(img, var, z["ref64_image"], z["ref64_variance"], "gpu vs ref64 (simple)"))
     print("relMSE vs FP64 reference", imgcheck.relmse(img, z["ref64_image"]))
+
+
+def test_bdpt_caustic_room_matches_reference_film(gpu_lib, golden_dir):
+    """The bidirectional configuration's own scene (a level-5 glass
+    icosphere on the floor of a closed 20-triangle room, a 0.05-radius sphere
+    light hidden from the camera by a thin panel), max_num_vertices 11, power
+    heuristic, on a 48 x 27 film: per pixel against the reference's own
+    renderer::bdpt (double precision, 16,384 samples per pixel), and the image
+    totals against its single-precision film."""
+    scene, z = ptscene.load_scene(golden_dir, "caustic_bdpt")
+    assert int(z["max_num_vertices"]) == 11
+    img, var = render(gpu_lib, scene, 65536, 11, 23)
+    s64 = imgcheck.assert_same_image(img, var, z["ref64_image"], z["ref64_variance"], "gpu vs ref64 (caustic room)")
+    s32 = imgcheck.compare(img, var, z["ref_image"], z["ref_variance"])
+    assert max(abs(x) for x in s32["total_z"]) < 4.0, s32
+    print("vs f64", s64, "\nvs f32", s32, "\nrelMSE vs FP64 reference", imgcheck.relmse(img, z["ref64_image"]))
+
+
+def test_bdpt_caustic_room_matches_oracle(gpu_lib, oracle_lib, golden_dir):
+    """The same scene on a 24 x 14 film with another camera aim: the GPU
+    against the oracle's renderer::bdpt (aggregates: the oracle's sample
+    count keeps per-pixel statistics short of normal)."""
+    scene, _ = ptscene.load_scene(golden_dir, "caustic_bdpt")
+    scene["camera"].update(width=24, height=14, center=(0.1, 0.35, 0.2))
+    img, var = render(gpu_lib, scene, 32768, 11, 29)
+    r = oracle_lib.render_bdpt(scene, 24 * 14 * 2048, 11, 31, os.cpu_count() or 4)
+    print(imgcheck.assert_same_aggregates(img, var, r["image"], r["variance"], "gpu vs oracle (caustic room)"))

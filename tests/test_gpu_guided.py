@@ -49,21 +49,27 @@ def test_guided_is_unbiased_while_training(gpu_lib):
 
 
 def test_trained_guide_lowers_error(gpu_lib):
-    """After training, guided passes reach a lower relMSE (0.1 % outlier
-    trimmed) against a converged plain-PT image than plain PT with the same
-    samples per pixel; without training the guide gains nothing."""
+    """What the trained network gains over the same tracer without it: at
+    equal samples per pixel and with the same (throughput) roulette, guided
+    passes after training reach a lower relMSE (0.1 % outlier trimmed)
+    against a converged image than BSDF sampling alone (alpha = 1) and than
+    the untrained network (alpha = 0.5, no training)."""
     from lmgpu import scenes
 
     s = small_room(96, 54, 40)
     sc = gpu_lib.Scene(s)
-    ref, _ = sc.render_pt(65536, -1, 1)
-    pi, _ = sc.render_pt(256, -1, 4)
+    g0 = gpu_lib.Guide(scenes.scene_box(s), 1)
+    ref, _, _ = sc.render_pt_guided(g0, 65536, -1, 1, alpha=1.0, train=False, rr_mode=1)
+    nonet, _, _ = sc.render_pt_guided(g0, 256, -1, 4, alpha=1.0, train=False, rr_mode=1)
     g = gpu_lib.Guide(scenes.scene_box(s), 3)
-    u, _, _ = sc.render_pt_guided(g, 256, -1, 5, alpha=0.5, train=False)
-    sc.render_pt_guided(g, 2048, -1, 2, alpha=0.5, train=True, batch=1 << 16)  # training passes
-    gi, _, _ = sc.render_pt_guided(g, 256, -1, 3, alpha=0.5, train=False)
-    eg, ep, eu = (imgcheck.relmse(x, ref, trim=1e-3) for x in (gi, pi, u))
-    print("trimmed relMSE at 256 spp: guided", eg, "plain", ep, "untrained guide", eu, "gain", ep / eg)
-    assert eg < 0.7 * ep
+    untrained, _, _ = sc.render_pt_guided(g, 256, -1, 5, alpha=0.5, train=False, rr_mode=1)
+    sc.render_pt_guided(g, 2048, -1, 2, alpha=0.5, train=True, batch=1 << 16, rr_mode=1)  # training passes
+    trained, _, _ = sc.render_pt_guided(g, 256, -1, 3, alpha=0.5, train=False, rr_mode=1)
+    et, en, eu = (imgcheck.relmse(x, ref, trim=1e-3) for x in (trained, nonet, untrained))
+    print("trimmed relMSE at 256 spp: trained", et, "no network", en, "untrained network", eu,
+          "gain over no network", en / et, "over untrained", eu / et)
+    assert et < 0.7 * en
+    assert et < 0.7 * eu
     sc.close()
     g.close()
+    g0.close()

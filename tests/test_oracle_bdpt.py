@@ -74,3 +74,15 @@ def test_oracle_bdpt_simple_weight_matches_reference(oracle_lib, golden_dir):
                                mis="simple")
     print(imgcheck.assert_same_image(r["image"], r["variance"], z["ref64_image"], z["ref64_variance"],
                                      "oracle vs ref64 (bdpt, simple weight)"))
+
+
+def test_oracle_bdpt_matches_reference_on_caustic_room(oracle_lib, golden_dir):
+    """The bidirectional configuration's caustic room (glass icosphere,
+    sphere light behind a panel), max_num_vertices 11, power heuristic: the
+    oracle's renderer::bdpt against the reference's own film (aggregates at
+    the oracle's 256 samples per pixel)."""
+    scene, z = ptscene.load_scene(golden_dir, "caustic_bdpt")
+    W, H = scene["camera"]["width"], scene["camera"]["height"]
+    r = oracle_lib.render_bdpt(scene, W * H * 256, int(z["max_num_vertices"]), 78, os.cpu_count() or 4)
+    print(imgcheck.assert_same_aggregates(r["image"], r["variance"], z["ref64_image"], z["ref64_variance"],
+                                          "oracle vs ref64 (caustic room)"))

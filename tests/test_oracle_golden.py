@@ -2,7 +2,8 @@
 itself (tests/golden/make_golden.py runs the reference's accel sources).
 
 The oracle must reproduce the reference bit for bit: same hit ids, hit
-points and barycentrics for accel::naive and accel::bvh_sahbin.  The accel
+points and barycentrics for accel::naive, accel::bvh_sahbin and accel::qbvh
+(the reference's fastest native accel, which the benchmark's CPU arm times).  The accel
 test cases additionally check the analytic values the reference's own test
 asserts (src/lightmetrica-test/test_accel3.cpp:272-345) within its 1e-3.
 """
@@ -19,7 +20,7 @@ def load(golden_dir, name):
 
 
 @pytest.mark.parametrize("case", ["accel3_simple", "accel3_simple2", "soup_small"])
-@pytest.mark.parametrize("kind,tag", [(0, "naive"), (1, "bvh_sahbin")])
+@pytest.mark.parametrize("kind,tag", [(0, "naive"), (1, "bvh_sahbin"), (2, "qbvh")])
 def test_oracle_matches_reference_bitwise(oracle_lib, golden_dir, case, kind, tag):
     z = load(golden_dir, case)
     acc = oracle_lib.OracleAccel(kind, z["tris"])
@@ -60,9 +61,46 @@ def test_reference_accels_agree_up_to_classified_cases(oracle_lib, golden_dir):
         assert c["unexplained"] == [], (other, c)
 
 
+def test_oracle_qbvh_matches_live_reference(oracle_lib):
+    """accel::qbvh on a 100k-triangle soup and heightfield, 65,536 rays: the
+    oracle against the reference's own qbvh compiled from its sources
+    (oracle/_ref/ref_accel, built where the reference tree is present)."""
+    import subprocess
+    import tempfile
+
+    from lmgpu import scenes
+
+    if not os.access(oracle_lib.REF_ACCEL, os.X_OK):
+        pytest.skip("reference harness oracle/_ref/ref_accel not built here")
+    tris = scenes.raycast_scene(100_000, 96, seed=21)
+    rays = scenes.raycast_rays(1 << 16, seed=22)
+    with tempfile.TemporaryDirectory() as tmp:
+        ps, pr, po = (os.path.join(tmp, x) for x in ("s.bin", "r.bin", "o.bin"))
+        oracle_lib.write_ref_inputs(ps, pr, [tris], rays)
+        subprocess.run([oracle_lib.REF_ACCEL, "accel::qbvh", ps, pr, po, "4"], check=True, capture_output=True)
+        ref = oracle_lib.read_ref_output(po)
+    h = oracle_lib.OracleAccel(oracle_lib.QBVH, tris).trace(rays, threads=4)
+    assert np.array_equal(h["id"], ref["id"])
+    hit = h["id"] >= 0
+    assert hit.mean() > 0.3
+    assert np.array_equal(h["p"][hit], ref["p"][hit])
+    assert np.array_equal(h["b0"][hit], ref["b"][hit, 0])
+
+
+def test_oracle_qbvh_coincident_centroids(oracle_lib):
+    """Twenty copies of one triangle (every centroid equal: the reference's
+    qbvh build divides 0 by 0 there) build and trace; the tie goes to one of
+    the copies."""
+    tri = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0], dtype=np.float32)
+    tris = np.tile(tri, (20, 1))
+    rays = np.array([[0.25, 0.25, 1, 1e-4, 0, 0, -1, 3.4e38]], dtype=np.float32)
+    h = oracle_lib.OracleAccel(2, tris).trace(rays)
+    assert 0 <= h["id"][0] < 20 and abs(h["t"][0] - 1.0) < 1e-6
+
+
 def test_oracle_empty_scene(oracle_lib):
     rays = np.array([[0, 0, 0, 1e-4, 0, 0, 1, 3.4e38]], dtype=np.float32)
-    for kind in (0, 1):
+    for kind in (0, 1, 2):
         h = oracle_lib.OracleAccel(kind, np.zeros((0, 9), np.float32)).trace(rays)
         assert h["id"][0] == -1
 

@@ -48,3 +48,15 @@ def test_oracle_pt_materials_match_reference(oracle_lib, golden_dir):
     a, va = ptscene.downsample(r["image"], r["variance"], 2)
     b, vb = ptscene.downsample(z["ref_image"].astype(np.float64), z["ref_variance"].astype(np.float64), 2)
     print(imgcheck.assert_same_image(a, va, b, vb, "oracle vs ref (materials)"))
+
+
+def test_oracle_pt_matches_reference_on_sphere_grid(oracle_lib, golden_dir):
+    """A view of the batched configuration's sphere grid (every BSDF kind,
+    an icosphere light, the environment; paths of up to 16 segments): the
+    oracle's renderer::pt against the reference's own film (aggregates at the
+    oracle's 256 samples per pixel)."""
+    scene, z = ptscene.load_scene(golden_dir, "grid_pt")
+    W, H = scene["camera"]["width"], scene["camera"]["height"]
+    r = oracle_lib.render_pt(scene, W * H * 256, int(z["max_num_vertices"]), 77, os.cpu_count() or 4)
+    print(imgcheck.assert_same_aggregates(r["image"], r["variance"], z["ref64_image"], z["ref64_variance"],
+                                          "oracle vs ref64 (sphere grid)"))
