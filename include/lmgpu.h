@@ -506,7 +506,11 @@ int lmgpu_accel_set_attributes(lmgpu_accel* accel, const float* normals, const f
  * from several threads are safe). */
 int lmgpu_surface(const lmgpu_accel* accel, const float* rays, const lmgpu_hit* hits, uint64_t n, float* surface);
 
-/* As lmgpu_surface on device buffers, asynchronous on `stream`. */
+/* As lmgpu_surface on device buffers, asynchronous on `stream`, except the
+ * first query after a build (or after lmgpu_accel_set_attributes failed to
+ * pack): it allocates the per-triangle records and synchronises `stream`
+ * while packing them, so make it before capturing surface queries into a
+ * CUDA graph. */
 int lmgpu_surface_device(const lmgpu_accel* accel, const float* d_rays, const lmgpu_hit* d_hits, uint64_t n,
                          float* d_surface, void* stream);
 
@@ -527,8 +531,12 @@ int lmgpu_surface_device(const lmgpu_accel* accel, const float* d_rays, const lm
  * make it before any stream capture.  Every call shares the array and it
  * keeps the previous call's contents: calls that overlap on the GPU (other
  * host threads or streams) race and must be serialised by the caller.
- * Synchronises `stream` before returning.  Results equal those of
- * lmgpu_accel_build_device + lmgpu_trace_device on the same inputs. */
+ * Synchronises `stream` before returning.  Closest-hit results (the
+ * triangle and t) equal those of lmgpu_accel_build_device +
+ * lmgpu_trace_device on the same inputs; any-hit results agree on hit or
+ * miss only, since which blocking triangle an any-hit query reports depends
+ * on the tree, and this path always collapses its BVH greedily (the
+ * allocating path uses the SAH-optimal collapse from 4,096 triangles on). */
 int lmgpu_trace_static_scene(const float* d_triangles, uint64_t ntri, const float* d_rays, lmgpu_hit* d_hits,
                              uint64_t nrays, int anyhit, void* stream);
 

@@ -4,6 +4,7 @@
 #include "common.cuh"
 #include "../../include/lmgpu.h"
 
+#include <atomic>
 #include <mutex>
 
 namespace lmgpu {
@@ -41,10 +42,10 @@ struct lmgpu_accel {
     // Surface records read by lmgpu_surface: per global triangle one 128-byte
     // line (positions, vertex normals, texcoords, flags), packed on the device
     // from the triangles and the attributes; surf_ntri = 0 until packed for
-    // the current build.
+    // the current build (read without the lock by queries, so atomic).
     float4* surf = nullptr;
     uint64_t surf_cap = 0;
-    uint64_t surf_ntri = 0;
+    std::atomic<uint64_t> surf_ntri{0};
 
     // Device status word raised by traversal kernels (stack overflow).
     uint32_t* status = nullptr;

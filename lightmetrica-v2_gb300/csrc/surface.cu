@@ -171,7 +171,6 @@ int pack_surface(lmgpu_accel* a, cudaStream_t stream)
         a->tris, a->tri_slot, a->ntri, attrs ? a->attr_normals : nullptr, attrs ? a->attr_texcoords : nullptr,
         attrs ? a->attr_flags : nullptr, a->surf);
     LMGPU_CUDA_TRY(cudaGetLastError());
-    a->surf_ntri = a->ntri;
     return LMGPU_OK;
 }
 
@@ -192,15 +191,18 @@ int launch_surface(const lmgpu_accel* ca, const float* d_rays, const lmgpu_hit* 
         return LMGPU_OK;
     }
     // the records are derived state of the accel, packed on first use after a
-    // build, under the accel's host lock; the wait makes them visible to
-    // later queries on any stream
+    // build under the accel's host lock; the wait makes them visible to later
+    // queries on any stream.  Once packed (surf_ntri published with release
+    // order after the wait) queries take no lock, so they do not queue behind
+    // a host trace that holds it.
     lmgpu_accel* a = const_cast<lmgpu_accel*>(ca);
-    {
+    if (a->surf_ntri.load(std::memory_order_acquire) != a->ntri) {
         std::lock_guard<std::mutex> lock(a->host_mu);
-        if (a->surf_ntri != a->ntri) {
+        if (a->surf_ntri.load(std::memory_order_relaxed) != a->ntri) {
             const int rc = pack_surface(a, stream);
             if (rc) return rc;
             LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+            a->surf_ntri.store(a->ntri, std::memory_order_release);
         }
     }
     const uint64_t blocks = (n + kSurfaceThreads - 1) / kSurfaceThreads;
@@ -260,6 +262,7 @@ int lmgpu_accel_set_attributes(lmgpu_accel* a, const float* normals, const float
     int rc = pack_surface(a, nullptr);
     if (rc) return rc;
     LMGPU_CUDA_TRY(cudaDeviceSynchronize());
+    a->surf_ntri.store(ntri, std::memory_order_release);
     return LMGPU_OK;
 }
 

@@ -18,7 +18,7 @@
             max_num_vertices: -1
             alpha: 0.5            # probability of BSDF sampling
             learning_rate: 0.001
-            throughput_roulette: true
+            throughput_roulette: 1
 
     Interface followed:
       Renderer::Initialize   include/lightmetrica/renderer.h:68
@@ -50,7 +50,8 @@ public:
         minNumVertices_ = prop->ChildAs("min_num_vertices", 0);
         alpha_ = prop->ChildAs<Float>("alpha", 0.5_f);
         learningRate_ = prop->ChildAs<Float>("learning_rate", 0.001_f);
-        throughputRoulette_ = prop->ChildAs<bool>("throughput_roulette", true);
+        // an int flag: PropertyNode::As has no bool form (property.h:151-156)
+        throughputRoulette_ = prop->ChildAs<int>("throughput_roulette", 1) != 0;
         return true;
     };
 

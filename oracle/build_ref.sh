@@ -9,6 +9,13 @@
 #                 cmake/LMBuildOptions.cmake:32-43) with accel::bvh_sahbin
 #   ref_isect / ref_isect64  IntersectionUtils::CreateTriangleIntersection
 #                 (single / double precision)
+#   ref_plugin    the reference-side accel plugin (plugin/accel_cuda.cpp)
+#                 driven through the reference's component interfaces
+#   ref_render_plugins  the render harness with the renderer plugins
+#                 (plugin/renderer_*_cuda.cpp) registered beside the
+#                 reference's renderers
+#   (both link oracle/refharness/lmgpu_cpu_fake.cpp, a CPU stand-in for the
+#   C ABI of include/lmgpu.h, since this machine has no GPU)
 # Test infrastructure only: nothing in the product links or runs them.
 #
 # The reference library cannot be built as shipped (boost, TBB, FreeImage,
@@ -38,7 +45,9 @@ esac
 mkdir -p "$OUT"
 CXX="${CXX:-g++}"
 CC="${CC:-gcc}"
-INC="-I$HERE/refharness/shim -I$REF/include -I$REF/external-src/dSFMT-src-2.2.3"
+REPO_ROOT="$(cd "$HERE/.." && pwd)"
+PLUGIN="$REPO_ROOT/lightmetrica-v2_gb300/plugin"
+INC="-I$HERE/refharness/shim -I$REF/include -I$REF/external-src/dSFMT-src-2.2.3 -I$REPO_ROOT/include -I$PLUGIN"
 FLAGS="-std=c++14 -O3 -msse4.2 -ffp-contract=off -w"
 L="$REF/src/liblightmetrica"
 
@@ -68,7 +77,18 @@ compile_set() {
 S="-DLM_EXPORTS -DLM_USE_SINGLE_PRECISION -DNDEBUG"
 D="-DLM_EXPORTS -DLM_USE_DOUBLE_PRECISION -DNDEBUG"
 ISECT="$HERE/refharness/ref_isect_cli.cpp"
-compile_set f "$S" "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}" "$HERE/refharness/ref_accel_cli.cpp" "$ISECT"
+PLUGIN_SRCS=("$PLUGIN/accel_cuda.cpp" "$PLUGIN/renderer_pt_cuda.cpp" "$PLUGIN/renderer_ptmis_cuda.cpp"
+             "$PLUGIN/renderer_ptdirect_cuda.cpp" "$PLUGIN/renderer_ltdirect_cuda.cpp" "$PLUGIN/renderer_bdpt_cuda.cpp"
+             "$PLUGIN/renderer_vcm_cuda.cpp" "$PLUGIN/renderer_pt_guided_cuda.cpp")
+compile_set f "$S" "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}" "$HERE/refharness/ref_accel_cli.cpp" "$ISECT" \
+  "${PLUGIN_SRCS[@]}" "$HERE/refharness/ref_plugin_cli.cpp"
+# the C-ABI stand-in and the oracle it runs on (plain C/C++, no reference headers)
+ORACLE_C=("$HERE/lmoracle_accel.c" "$HERE/lmoracle_pt.c" "$HERE/lmoracle_bdpt.c" "$HERE/lmoracle_surface.c")
+for c in "${ORACLE_C[@]}"; do
+  $CC -O2 -std=c11 -ffp-contract=off -fno-fast-math -w -c "$c" -o "$OUT/o_$(basename "$c" .c).o" &
+done
+$CXX -std=c++14 -O2 -ffp-contract=off -w -I"$REPO_ROOT/include" -c "$HERE/refharness/lmgpu_cpu_fake.cpp" -o "$OUT/fake_lmgpu.o" &
+wait
 compile_set d "$D" "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}" "$ISECT"
 $CC -O3 -msse2 -DDSFMT_MEXP=19937 -DNDEBUG -w -c "$REF/external-src/dSFMT-src-2.2.3/dSFMT.c" -o "$OUT/dsfmt.o"
 
@@ -78,5 +98,10 @@ $CXX -O3 -o "$OUT/ref_render" $(obj f "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}") "$
 $CXX -O3 -o "$OUT/ref_render64" $(obj d "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}") "$OUT/dsfmt.o" -lpthread
 $CXX -O3 -o "$OUT/ref_isect" $(obj f "$HERE/refharness/ref_runtime.cpp" "$ISECT") -lpthread
 $CXX -O3 -o "$OUT/ref_isect64" $(obj d "$HERE/refharness/ref_runtime.cpp" "$ISECT") -lpthread
+FAKE=("$OUT/fake_lmgpu.o" "$OUT"/o_*.o)
+$CXX -O3 -o "$OUT/ref_plugin" $(obj f "$HERE/refharness/ref_runtime.cpp" "$PLUGIN/accel_cuda.cpp" "$HERE/refharness/ref_plugin_cli.cpp") \
+  "${FAKE[@]}" -lpthread -lm
+$CXX -O3 -o "$OUT/ref_render_plugins" $(obj f "${ACCEL_SRCS[@]}" "${RENDER_SRCS[@]}" "${PLUGIN_SRCS[@]}") "$OUT/dsfmt.o" \
+  "${FAKE[@]}" -lpthread -lm
 rm -f "$OUT"/*.o
-echo "built $OUT/ref_accel $OUT/ref_render $OUT/ref_render64 $OUT/ref_isect $OUT/ref_isect64"
+echo "built $OUT/ref_accel $OUT/ref_render $OUT/ref_render64 $OUT/ref_isect $OUT/ref_isect64 $OUT/ref_plugin $OUT/ref_render_plugins"

@@ -151,6 +151,8 @@ def read_ref_output(path: str) -> np.ndarray:
 
 REF_RENDER = os.path.join(HERE, "_ref", "ref_render")
 REF_RENDER64 = os.path.join(HERE, "_ref", "ref_render64")
+REF_RENDER_PLUGINS = os.path.join(HERE, "_ref", "ref_render_plugins")
+REF_PLUGIN = os.path.join(HERE, "_ref", "ref_plugin")
 
 
 def _prim_full(p: dict) -> dict:
@@ -190,12 +192,13 @@ def write_render_scene(path: str, scene: dict, num_samples: int, max_num_vertice
 
 def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: int, threads: int,
                    double: bool = False, renderer: str = "pt", mis: str | None = None,
-                   params: dict | None = None, accel: str | None = None) -> dict:
+                   params: dict | None = None, accel: str | None = None, exe: str | None = None) -> dict:
     """Runs the reference renderer::pt or renderer::bdpt (compiled from its
     sources) and returns the film (H, W, 3), the per-pixel variance of that
     estimate and timing.  accel overrides the harness's accel component
     (accel::qbvh in single precision, accel::bvh_sahbin in double); every
-    accel returns the same closest hits, so the film does not depend on it."""
+    accel returns the same closest hits, so the film does not depend on it.
+    exe: another build of the harness (the one with the renderer plugins)."""
     import json
     import tempfile
 
@@ -207,7 +210,7 @@ def run_ref_render(scene: dict, num_samples: int, max_num_vertices: int, seed: i
     with tempfile.TemporaryDirectory() as tmp:
         ps, po = os.path.join(tmp, "scene.bin"), os.path.join(tmp, "out.bin")
         write_render_scene(ps, scene, num_samples, max_num_vertices, seed, threads)
-        exe = REF_RENDER64 if double else REF_RENDER
+        exe = exe or (REF_RENDER64 if double else REF_RENDER)
         extra = dict(params or {})
         if mis:
             extra["mis"] = mis

@@ -134,6 +134,9 @@ public:
         pending.push_back({ pY * width + pX, { (double)c[0], (double)c[1], (double)c[2] } });
     };
     LM_IMPL_F(Save) = [this](const std::string&) -> bool { return true; };
+    // film_hdr.cpp's SetPixel: the pixel's value replaced (the GPU renderer
+    // plugins write their finished image this way)
+    LM_IMPL_F(SetPixel) = [this](int x, int y, const SPD& v) -> void { data[(size_t)y * width + x] = v.ToRGB(); };
     LM_IMPL_F(Accumulate) = [this](const Film* f_) -> void
     {
         const auto* f = static_cast<const HarnessFilm*>(f_);

@@ -4,7 +4,11 @@ pool, or a query path that must not pay the device-wide synchronisation of
 cudaMalloc/cudaFree).  It keeps its scratch and the BVH in one fixed
 library-owned device array, so its results must equal those of the
 allocating path (lmgpu_accel_build_device + lmgpu_trace_device) on the same
-inputs, call after call, although every call reuses the same memory.
+inputs, call after call, although every call reuses the same memory: closest
+hits exactly, any-hit queries on hit or miss (the blocking triangle an any-hit
+query reports depends on the tree, and this path collapses its BVH greedily).
+And it must not allocate: after a first call, further calls leave the
+device's free memory unchanged.
 
 This file is collected last on purpose: if it fails, a run that stops at the
 first failure has already run every other test.
@@ -60,6 +64,31 @@ def test_static_scene_matches_allocating_path_two_calls(gpu_lib):
             assert rel.max() <= T_REL_TOL
             assert np.allclose(got["b1"][hit], ref["b1"][hit], atol=1e-6)
             assert np.allclose(got["b2"][hit], ref["b2"][hit], atol=1e-6)
+
+
+def test_static_scene_allocates_nothing(gpu_lib):
+    """After one call (which looks up the library's array), more calls on
+    scenes up to the size limit leave cudaMemGetInfo's free bytes as they
+    were."""
+    import torch
+    from lmgpu import scenes
+
+    stream = torch.cuda.current_stream().cuda_stream
+    tris = scenes.random_soup(gpu_lib.STATIC_MAX_TRIANGLES, seed=505)
+    rays = scenes.raycast_rays(1 << 16, seed=506)
+    dt = torch.from_numpy(tris).cuda()
+    dr = torch.from_numpy(rays).cuda()
+    dh = torch.empty((rays.shape[0], 4), dtype=torch.float32, device="cuda")
+    gpu_lib.trace_static_scene(dt.data_ptr(), tris.shape[0], dr.data_ptr(), dh.data_ptr(), rays.shape[0], False,
+                               stream)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for anyhit in (False, True, False):
+        gpu_lib.trace_static_scene(dt.data_ptr(), tris.shape[0], dr.data_ptr(), dh.data_ptr(), rays.shape[0],
+                                   anyhit, stream)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
 
 
 def test_static_scene_rejects_oversize(gpu_lib):
