@@ -2,24 +2,31 @@
 // forward, backward and Adam kernels for the MLP of guide_net.cuh, BF16
 // operands with FP32 accumulation in tensor memory.
 //
-// k_guide_fwd   one CTA (4 warps) per 128-query tile at a time, persistent
-//               over tiles.  The five weight matrices stay in shared memory
-//               (BF16, K-major canonical layout); the tile's activations
+// k_guide_fwd   one CTA (8 warps, two threads per query) per 128-query tile
+//               at a time, two CTAs per SM, persistent over tiles.  The five
+//               weight matrices stay in shared memory (BF16, K-major
+//               canonical layout); the tile's activations
 //               ping-pong between two shared-memory buffers; each layer is
 //               K/16 MMAs of M = 128 into a 64-column tensor-memory
 //               accumulator, issued by one thread and completed through an
-//               mbarrier; the epilogue (bias, ReLU, BF16 pack) runs on all
-//               128 threads, one row each, reading its row with tcgen05.ld.
+//               mbarrier; the feature encoding and the epilogue (bias, ReLU,
+//               BF16 pack) run on all 256 threads, two per row (half the
+//               features and half the columns each), reading the row's
+//               columns with tcgen05.ld.
 //               MODE_TRAIN also writes every layer's input (BF16) and the raw
 //               outputs to global memory for the backward pass.
-// k_guide_bwd   per 128-sample tile: the loss gradient of the outputs, then
-//               for each layer, from the last: dH = dZ W (M = 128 MMA
-//               against W^T kept in shared memory) and dW = dZ^T H.  The
-//               weight gradient has M = 64 rows; it is computed as one
-//               M = 128 MMA by splitting the tile into two 64-sample halves:
-//               A' = [dZ_1^T ; dZ_2^T], B' = [H_1^T ; H_2^T], whose product's
-//               two diagonal blocks are the halves' dW and are added into the
-//               FP32 gradient with atomics.
+// k_guide_bwd   one CTA per SM, persistent over 128-sample tiles: the loss
+//               gradient of the outputs, then for each layer, from the last,
+//               dH = dZ W (M = 128 MMA against W^T kept in shared memory) and
+//               dW += dZ^T H, an M = 128 MMA (dZ^T's 64 rows padded with
+//               zeros) over the tile's 128 samples as K, accumulated in tensor
+//               memory across every tile the CTA processes.  For layers 2..5
+//               H^T carries an extra row of ones, so the same MMA also sums
+//               the bias gradient (column 64 of the layer's accumulator);
+//               layer 1's bias gradient is summed in shared memory.  After
+//               its last tile each CTA writes its gradient once to its own
+//               slice of a partials buffer.
+// k_guide_reduce  adds the CTAs' partial gradients into the FP32 gradient.
 // k_guide_adam  Adam on the FP32 master parameters (gradients zeroed).
 //
 // Every mbarrier wait has an iteration limit; on time-out a kernel raises
@@ -43,7 +50,8 @@ using namespace guide;
 constexpr uint32_t kStatusTimeout = 16;
 constexpr uint32_t kWaitLimit = 1u << 24;
 constexpr int kTile = 128;
-constexpr int kThreads = 128;
+constexpr int kThreads = 128;      // backward: one thread per sample of a tile
+constexpr int kFwdThreads = 256;   // forward: two threads per query of a tile
 constexpr int kActs = kIn + 4 * kHid;  // stored activations per sample (bf16)
 
 // shared-memory plan of the forward kernel (bytes)
@@ -58,11 +66,17 @@ constexpr uint32_t kFwdSmem = kFwdBar + 64;
 // shared-memory plan of the backward kernel (bytes)
 // W_l^T for l = 1..4 (W2^T..W4^T 64x64, W5^T 64x48) at 8192 (l - 1)
 __host__ __device__ constexpr uint32_t bwd_wt(int l) { return 8192u * (uint32_t)(l - 1); }
-constexpr uint32_t kBwdDZ = 30720;                           // dZ, 128 x 64 (K-major, K = layer width)
-constexpr uint32_t kBwdDZT = kBwdDZ + 16384;                 // [dZ_1^T ; dZ_2^T], 128 x 64
-constexpr uint32_t kBwdHT = kBwdDZT + 16384;                 // [H_1^T ; H_2^T], up to 256 x 64
-constexpr uint32_t kBwdBar = kBwdHT + 32768;
-constexpr uint32_t kBwdSmem = 122880;  // above the plan (96 KB): one CTA per SM, so 512 TMEM columns are free
+constexpr uint32_t kBwdDZ = 30720;            // dZ, 128 samples x 64 (K-major, K = layer width)
+constexpr uint32_t kBwdDZT = kBwdDZ + 16384;  // dZ^T, 128 rows (64 used, 64 zero) x 128 samples
+constexpr uint32_t kBwdHT0 = kBwdDZT + 32768; // H_0^T (layer 1's input), 128 x 128 samples
+constexpr uint32_t kBwdHT = kBwdHT0 + 32768;  // H^T of layers 2..5: 64 rows, a row of ones, 15 zero rows
+constexpr uint32_t kBwdB0 = kBwdHT + 20480;   // layer 1's bias gradient, 64 floats
+constexpr uint32_t kBwdBar = kBwdB0 + 256;
+constexpr uint32_t kBwdSmem = kBwdBar + 64;   // 133,440 bytes: one CTA per SM, which holds all 512 TMEM columns
+constexpr uint32_t kBwdHTRows = kHid + 16;    // rows of H^T for layers 2..5 (N of their dW MMA)
+// tensor-memory columns of the backward kernel: dH at 0, layer 1's dW at
+// 64 (128 columns), layer l = 1..4's dW (+ bias column 64) at 192 + 80 (l - 1)
+__host__ __device__ constexpr uint32_t bwd_dw_col(int l) { return l == 0 ? 64u : 192u + 80u * (uint32_t)(l - 1); }
 
 enum : int { MODE_RAW = 0, MODE_TRAIN = 1 };
 
@@ -159,22 +173,26 @@ __device__ __forceinline__ void block_sync_for_mma()
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kThreads, 1) k_guide_fwd(const float* __restrict__ params, Box box,
-                                                           const float* __restrict__ queries, uint32_t n,
-                                                           const uint32_t* __restrict__ d_n,
-                                                           float* __restrict__ raw_out,
-                                                           __nv_bfloat16* __restrict__ acts,
-                                                           uint32_t* __restrict__ status)
+__global__ void __launch_bounds__(kFwdThreads, 2) k_guide_fwd(const float* __restrict__ params, Box box,
+                                                              const float* __restrict__ queries, uint32_t n,
+                                                              const uint32_t* __restrict__ d_n,
+                                                              float* __restrict__ raw_out,
+                                                              __nv_bfloat16* __restrict__ acts,
+                                                              uint32_t* __restrict__ status)
 {
     if (d_n) n = *d_n;  // query count on the device (at most the n launched for)
     extern __shared__ __align__(1024) unsigned char smem[];
     float* sbias = reinterpret_cast<float*>(smem + kFwdBias);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kFwdBar);
     uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kFwdBar + 8);
-    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    // two threads per row of the tile: r = the row, half = which half of the
+    // row's features and columns this thread computes; a warp reads tensor
+    // memory lanes 32 (warp % 4) .. + 31, the rows of its threads
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, r = tid & (kTile - 1u), half = tid >> 7;
+    const uint32_t lane_base = (warp & 3u) * 32u;
 
     for (int l = 0; l < 5; l++) load_matrix(smem + fwd_w(l), params + w_off(l), layer_out(l), layer_in(l), false);
-    for (int i = tid; i < 4 * kHid + kOut; i += kThreads) {
+    for (int i = tid; i < 4 * kHid + kOut; i += kFwdThreads) {
         const int l = i / kHid < 4 ? i / kHid : 4, j = i - l * kHid;
         sbias[i] = params[b_off(l) + j];
     }
@@ -193,27 +211,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_fwd(const float* __restri
 
     const uint32_t ntiles = (n + kTile - 1) / kTile;
     for (uint32_t tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x) {
-        const uint32_t row = tile * kTile + tid;
-        // features of the row's query
+        const uint32_t row = tile * kTile + r;
+        // features of the row's query, eight at a time: groups half, half + 2, ...
         {
-            float f[kIn];
+            float x[3] = {0.0f, 0.0f, 0.0f}, nn[3] = {0.0f, 0.0f, 0.0f}, wo[3] = {0.0f, 0.0f, 0.0f};
             if (row < n) {
                 const float* q = queries + 9 * (size_t)row;
-                const float x[3] = {q[0], q[1], q[2]}, nn[3] = {q[3], q[4], q[5]}, wo[3] = {q[6], q[7], q[8]};
-                features(x, nn, wo, box.lo, box.inv_ext, f);
-            } else {
-                for (int k = 0; k < kIn; k++) f[k] = 0.0f;
+                for (int d = 0; d < 3; d++) {
+                    x[d] = q[d];
+                    nn[d] = q[3 + d];
+                    wo[d] = q[6 + d];
+                }
             }
-            for (int k = 0; k < kIn; k += 8) put8(smem + kFwdA, tid, k, kIn, f + k);
-            if (MODE == MODE_TRAIN && row < n) {
-                uint4* dst = reinterpret_cast<uint4*>(acts + (size_t)row * kActs);
-                for (int k = 0; k < kIn; k += 8)
-                    dst[k / 8] = make_uint4(pack2(f[k], f[k + 1]), pack2(f[k + 2], f[k + 3]), pack2(f[k + 4], f[k + 5]),
-                                            pack2(f[k + 6], f[k + 7]));
+#pragma unroll
+            for (int j8 = 0; j8 < kIn / 16; j8++) {
+                const int g8 = 2 * j8 + (int)half;
+                float f[8];
+                if (row < n) {
+                    features8(x, nn, wo, box.lo, box.inv_ext, g8, f);
+                } else {
+                    for (int j = 0; j < 8; j++) f[j] = 0.0f;
+                }
+                put8(smem + kFwdA, r, 8 * g8, kIn, f);
+                if (MODE == MODE_TRAIN && row < n)
+                    reinterpret_cast<uint4*>(acts + (size_t)row * kActs)[g8] =
+                        make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]), pack2(f[6], f[7]));
             }
         }
         block_sync_for_mma();
-        for (int l = 0; l < 5 && alive; l++) {
+#pragma unroll
+        for (int l = 0; l < 5; l++) {
+            if (!alive) break;
             // layer l reads buffer A (l even) or B (l odd)
             const uint32_t a_in = (l & 1) ? sB : sA;
             unsigned char* out_tile = smem + ((l & 1) ? kFwdA : kFwdB);
@@ -223,26 +251,34 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_fwd(const float* __restri
             if (!alive) break;
             const float* bias = sbias + l * kHid;
             if (l < 4) {
-                float h[kHid];
-                for (int c = 0; c < kHid; c += 16) tc::tmem_load16(tc::tmem_at(tmem, warp * 32, c), h + c);
+                // columns 32 half .. 32 half + 31 of the row
+                const uint32_t c0 = 32u * half;
+                float h[32];
+                tc::tmem_load16(tc::tmem_at(tmem, lane_base, c0), h);
+                tc::tmem_load16(tc::tmem_at(tmem, lane_base, c0 + 16u), h + 16);
                 tc::tmem_wait_ld();
-                for (int c = 0; c < kHid; c++) h[c] = fmaxf(h[c] + bias[c], 0.0f);
-                for (int c = 0; c < kHid; c += 8) put8(out_tile, tid, c, kHid, h + c);
+                for (int c = 0; c < 32; c++) h[c] = fmaxf(h[c] + bias[c0 + c], 0.0f);
+                for (int c = 0; c < 32; c += 8) put8(out_tile, r, c0 + c, kHid, h + c);
                 if (MODE == MODE_TRAIN && row < n) {
-                    uint4* dst = reinterpret_cast<uint4*>(acts + (size_t)row * kActs + kIn + l * kHid);
-                    for (int c = 0; c < kHid; c += 8)
+                    uint4* dst = reinterpret_cast<uint4*>(acts + (size_t)row * kActs + kIn + l * kHid + c0);
+                    for (int c = 0; c < 32; c += 8)
                         dst[c / 8] = make_uint4(pack2(h[c], h[c + 1]), pack2(h[c + 2], h[c + 3]),
                                                 pack2(h[c + 4], h[c + 5]), pack2(h[c + 6], h[c + 7]));
                 }
             } else {
-                float z[kOut];
-                for (int c = 0; c < kOut; c += 16) tc::tmem_load16(tc::tmem_at(tmem, warp * 32, c), z + c);
+                // raw outputs 0..31 (half 0) and 32..39 (half 1; columns 40..47 are padding)
+                float z[32];
+                tc::tmem_load16(tc::tmem_at(tmem, lane_base, 32u * half), z);
+                if (half == 0u) tc::tmem_load16(tc::tmem_at(tmem, lane_base, 16u), z + 16);
                 tc::tmem_wait_ld();
                 if (row < n) {
-                    float4* dst = reinterpret_cast<float4*>(raw_out + (size_t)row * kOutUsed);
-                    for (int c = 0; c < kOutUsed; c += 4)
-                        dst[c / 4] = make_float4(z[c] + bias[c], z[c + 1] + bias[c + 1], z[c + 2] + bias[c + 2],
-                                                 z[c + 3] + bias[c + 3]);
+                    const int c0 = 32 * (int)half, cn = half ? kOutUsed - 32 : 32;
+                    float4* dst = reinterpret_cast<float4*>(raw_out + (size_t)row * kOutUsed + c0);
+#pragma unroll
+                    for (int c = 0; c < 32; c += 4)
+                        if (c < cn)
+                            dst[c / 4] = make_float4(z[c] + bias[c0 + c], z[c + 1] + bias[c0 + c + 1],
+                                                     z[c + 2] + bias[c0 + c + 2], z[c + 3] + bias[c0 + c + 3]);
                 }
             }
             block_sync_for_mma();
@@ -251,27 +287,34 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_fwd(const float* __restri
     release_tmem(bar, phase, alive, tmem, 64);
 }
 
-// Adds the 32 lanes' values of v into *dst (one atomic per warp).
-__device__ __forceinline__ void warp_atomic_add(float* dst, float v)
-{
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31u) == 0u && v != 0.0f) atomicAdd(dst, v);
-}
-
 __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restrict__ params,
                                                            const float* __restrict__ raw,
                                                            const __nv_bfloat16* __restrict__ acts,
                                                            const float* __restrict__ dirs,
                                                            const float* __restrict__ weights, uint32_t n,
-                                                           float inv_batch, float* __restrict__ grad,
+                                                           float inv_batch, float* __restrict__ partials,
                                                            float* __restrict__ loss, uint32_t* __restrict__ status)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kBwdBar);
     uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kBwdBar + 8);
-    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    float* sb0 = reinterpret_cast<float*>(smem + kBwdB0);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    unsigned char* sDZ = smem + kBwdDZ;
+    unsigned char* sDZT = smem + kBwdDZT;
+    unsigned char* sHT0 = smem + kBwdHT0;
+    unsigned char* sHT = smem + kBwdHT;
     // W_l^T for l = 2..5 (tile rows = layer inputs, K = layer outputs)
     for (int l = 1; l < 5; l++) load_matrix(smem + bwd_wt(l), params + w_off(l), layer_out(l), layer_in(l), true);
+    // dZ^T rows 64..127 stay zero (M padding); H^T of layers 2..5: row 64
+    // ones (bias gradient), rows 65..79 zero
+    for (uint32_t i = tid; i < 32768u / 16u; i += kThreads)
+        reinterpret_cast<uint4*>(sDZT)[i] = make_uint4(0u, 0u, 0u, 0u);
+    for (uint32_t i = tid; i < (kBwdHTRows - (uint32_t)kHid) * (uint32_t)kTile; i += kThreads) {
+        const uint32_t r = (uint32_t)kHid + i / (uint32_t)kTile, k = i % (uint32_t)kTile;
+        put1(sHT, r, k, kTile, r == (uint32_t)kHid ? 1.0f : 0.0f);
+    }
+    if (tid < (uint32_t)kHid) sb0[tid] = 0.0f;
     if (tid == 0) {
         tc::mbar_init(bar, 1);
         tc::mbar_init_fence();
@@ -281,13 +324,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *s_tmem;
-    const uint32_t dh_col = 0, dw_col = 256;
-    unsigned char* sDZ = smem + kBwdDZ;
-    unsigned char* sDZT = smem + kBwdDZT;
-    unsigned char* sHT = smem + kBwdHT;
+    const uint32_t dh_col = 0;
     uint32_t phase = 0;
     bool alive = true;
-    const uint32_t half = tid >> 6, k_in_half = tid & 63u;
+    bool first = true;
+    float lsum = 0.0f;
 
     const uint32_t ntiles = (n + kTile - 1) / kTile;
     for (uint32_t tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x) {
@@ -296,39 +337,60 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
         // dL/dz of the output layer (rows 40..47 and invalid samples are zero)
         float dz[kHid];
         for (int c = 0; c < kHid; c++) dz[c] = 0.0f;
-        float lsum = 0.0f;
         if (valid) {
             float z[kOutUsed];
             for (int c = 0; c < kOutUsed; c++) z[c] = raw[(size_t)row * kOutUsed + c];
             Lobes L;
             lobes_from_raw(z, L);
             const float w3[3] = {dirs[3 * (size_t)row], dirs[3 * (size_t)row + 1], dirs[3 * (size_t)row + 2]};
-            lsum = loss_grad(L, w3, weights[row] * inv_batch, dz);
+            lsum += loss_grad(L, w3, weights[row] * inv_batch, dz);
         }
-        warp_atomic_add(loss, lsum);
-        // layers 5..1 (l = 4..0)
-        for (int l = 4; l >= 0 && alive; l--) {
+        // layers 5..1 (l = 4..0), unrolled so that every layer's widths are
+        // compile-time constants (register-resident dZ / dH rows)
+#pragma unroll
+        for (int l = 4; l >= 0; l--) {
+            if (!alive) break;
             const uint32_t Nl = layer_out(l), Kin = layer_in(l);
-            // dZ_l: bias gradient, K-major copy (A of dH) and the two-halves transpose (A' of dW)
-            for (uint32_t c = 0; c < Nl; c++) warp_atomic_add(grad + b_off(l) + c, dz[c]);
-            for (uint32_t c = 0; c < Nl; c += 8) put8(sDZ, tid, c, Nl, dz + c);
-            for (uint32_t c = 0; c < kHid; c++) put1(sDZT, c + 64u * half, k_in_half, 64, c < Nl ? dz[c] : 0.0f);
-            // H_{l-1}^T two-halves (B' of dW): the layer's input activations of this tile
+            // the layer's input activations H_{l-1} of this row (zeros for invalid rows)
+            uint4 hv[kIn / 8];
             {
-                const __nv_bfloat16* h = acts + (size_t)(valid ? row : 0) * kActs + (l == 0 ? 0 : kIn + (l - 1) * kHid);
-                for (uint32_t i = 0; i < Kin; i++) {
-                    const float v = valid ? __bfloat162float(h[i]) : 0.0f;
-                    put1(sHT, i + Kin * half, k_in_half, 64, v);
+                const uint4* src = reinterpret_cast<const uint4*>(acts + (size_t)(valid ? row : 0) * kActs +
+                                                                  (l == 0 ? 0 : kIn + (l - 1) * kHid));
+                for (uint32_t q = 0; q < Kin / 8; q++) hv[q] = valid ? src[q] : make_uint4(0u, 0u, 0u, 0u);
+            }
+            if (l == 0) {
+                // layer 1's bias gradient: per-warp sums into shared memory
+                for (int c = 0; c < kHid; c++) {
+                    float v = dz[c];
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    if (lane == 0u && v != 0.0f) atomicAdd(sb0 + c, v);
+                }
+            } else {
+                for (uint32_t c = 0; c < Nl; c += 8) put8(sDZ, tid, c, Nl, dz + c);
+            }
+            // dZ^T (rows = output features, K = samples) and H^T (rows = inputs)
+            for (uint32_t c = 0; c < (uint32_t)kHid; c++) put1(sDZT, c, tid, kTile, dz[c]);
+            {
+                unsigned char* ht = l == 0 ? sHT0 : sHT;
+                for (uint32_t q = 0; q < Kin / 8; q++) {
+                    const uint32_t w4[4] = {hv[q].x, hv[q].y, hv[q].z, hv[q].w};
+                    for (int e = 0; e < 4; e++) {
+                        const __nv_bfloat162 p = *reinterpret_cast<const __nv_bfloat162*>(&w4[e]);
+                        *reinterpret_cast<__nv_bfloat16*>(ht + tc::kmajor_offset(8 * q + 2 * e, tid, kTile)) = p.x;
+                        *reinterpret_cast<__nv_bfloat16*>(ht + tc::kmajor_offset(8 * q + 2 * e + 1, tid, kTile)) = p.y;
+                    }
                 }
             }
             block_sync_for_mma();
             if (tid == 0) {
-                // dW: [dZ_1^T ; dZ_2^T] (128 x 64) x [H_1^T ; H_2^T]^T -> 128 x 2 Kin
-                const uint32_t idesc_w = tc::idesc_bf16_f32(128, 2 * Kin);
-                const uint32_t a0 = tc::smem_addr(sDZT), b0 = tc::smem_addr(sHT);
-                for (uint32_t ks = 0; ks < 4; ks++)
-                    tc::mma_bf16(tmem + dw_col, tc::kmajor_desc(a0 + ks * 256u, 64), tc::kmajor_desc(b0 + ks * 256u, 64),
-                                 idesc_w, ks > 0 ? 1u : 0u);
+                // dW (+)= dZ^T (128 x 128 samples) x (H^T, N x 128 samples)^T,
+                // accumulated in tensor memory over the CTA's tiles
+                const uint32_t N = l == 0 ? (uint32_t)kIn : kBwdHTRows;
+                const uint32_t idesc_w = tc::idesc_bf16_f32(128, N);
+                const uint32_t a0 = tc::smem_addr(sDZT), b0 = tc::smem_addr(l == 0 ? sHT0 : sHT);
+                for (uint32_t ks = 0; ks < (uint32_t)kTile / 16u; ks++)
+                    tc::mma_bf16(tmem + bwd_dw_col(l), tc::kmajor_desc(a0 + ks * 256u, kTile),
+                                 tc::kmajor_desc(b0 + ks * 256u, kTile), idesc_w, (first && ks == 0) ? 0u : 1u);
                 // dH_{l-1} = dZ_l (128 x Nl) x (W_l^T, Kin x Nl)^T
                 if (l > 0) {
                     const uint32_t idesc_h = tc::idesc_bf16_f32(128, Kin);
@@ -341,34 +403,66 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
             }
             alive = wait_layer(bar, phase, status);
             if (!alive) break;
-            // dW block of this thread's row: output feature o of its half
-            {
-                const uint32_t o = tid & 63u;
-                const uint32_t col0 = dw_col + Kin * half;
-                float* gW = grad + w_off(l);
-                for (uint32_t c = 0; c < Kin; c += 16) {
-                    float v[16];
-                    tc::tmem_load16(tc::tmem_at(tmem, warp * 32, col0 + c), v);
-                    tc::tmem_wait_ld();
-                    if (o < (l == 4 ? (uint32_t)kOutUsed : Nl))
-                        for (int q = 0; q < 16; q++)
-                            if (v[q] != 0.0f) atomicAdd(gW + o * Kin + c + q, v[q]);
-                }
-            }
             if (l > 0) {
-                // dZ_{l-1} = dH_{l-1} * relu'(H_{l-1})
+                // dZ_{l-1} = dH_{l-1} * relu'(H_{l-1}); H_{l-1} is this layer's input
                 float dh[kHid];
                 for (int c = 0; c < kHid; c += 16) tc::tmem_load16(tc::tmem_at(tmem, warp * 32, dh_col + c), dh + c);
                 tc::tmem_wait_ld();
-                const __nv_bfloat16* h = acts + (size_t)(valid ? row : 0) * kActs + kIn + (l - 1) * kHid;
-                for (int c = 0; c < kHid; c++) dz[c] = (valid && __bfloat162float(h[c]) > 0.0f) ? dh[c] : 0.0f;
+                for (uint32_t q = 0; q < (uint32_t)kHid / 8; q++) {
+                    const uint32_t w4[4] = {hv[q].x, hv[q].y, hv[q].z, hv[q].w};
+                    for (int e = 0; e < 4; e++) {
+                        const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w4[e]));
+                        dz[8 * q + 2 * e] = f.x > 0.0f ? dh[8 * q + 2 * e] : 0.0f;
+                        dz[8 * q + 2 * e + 1] = f.y > 0.0f ? dh[8 * q + 2 * e + 1] : 0.0f;
+                    }
+                }
             }
             tc::fence_before_sync();
             __syncthreads();
             tc::fence_after_sync();
         }
+        first = false;
+    }
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if (lane == 0u && lsum != 0.0f) atomicAdd(loss, lsum);
+    // flush: this CTA's gradient (weights from tensor memory, lanes 0..63 =
+    // output features; layer 1's bias from shared memory) into its slice
+    float* part = partials + (size_t)blockIdx.x * kNumParams;
+    if (alive && !first) {
+        for (int l = 0; l < 5; l++) {
+            const uint32_t Kin = layer_in(l), cols = l == 0 ? (uint32_t)kIn : kBwdHTRows;
+            if (warp < 2) {
+                const uint32_t o = warp * 32 + lane;
+                for (uint32_t c = 0; c < cols; c += 16) {
+                    float v[16];
+                    tc::tmem_load16(tc::tmem_at(tmem, warp * 32, bwd_dw_col(l) + c), v);
+                    tc::tmem_wait_ld();
+                    if (o < (uint32_t)layer_out(l)) {
+                        for (int q = 0; q < 16; q++) {
+                            const uint32_t i = c + q;
+                            if (i < Kin) part[w_off(l) + o * Kin + i] = v[q];
+                            else if (i == Kin) part[b_off(l) + o] = v[q];
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (tid < (uint32_t)kHid) part[b_off(0) + tid] = sb0[tid];
+    } else {
+        for (int i = tid; i < kNumParams; i += kThreads) part[i] = 0.0f;
     }
     release_tmem(bar, phase, alive, tmem, 512);
+}
+
+// grad[i] += the CTAs' partial gradients of parameter i.
+__global__ void k_guide_reduce(const float* __restrict__ partials, int nparts, float* __restrict__ grad)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kNumParams) return;
+    float s = 0.0f;
+    for (int b = 0; b < nparts; b++) s += partials[(size_t)b * kNumParams + i];
+    grad[i] += s;
 }
 
 __global__ void k_guide_adam(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m,
@@ -406,7 +500,9 @@ struct lmgpu_guide {
     float* d_dir = nullptr;
     float* d_w = nullptr;
     __nv_bfloat16* d_acts = nullptr;
-    int grid = 0;
+    int grid = 0;         // backward: one CTA per SM
+    int fwd_grid = 0;     // forward: two CTAs per SM
+    float* partials = nullptr;  // [grid][kNumParams] per-CTA gradients of the backward
 };
 
 namespace lmgpu {
@@ -445,15 +541,17 @@ int guide_grid(lmgpu_guide* g)
                                             (int)kFwdSmem));
         LMGPU_CUDA_TRY(
             cudaFuncSetAttribute(k_guide_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
+        LMGPU_CUDA_TRY(cudaMalloc((void**)&g->partials, sizeof(float) * (size_t)sms * kNumParams));
         g->grid = sms;
+        g->fwd_grid = 2 * sms;
     }
     return LMGPU_OK;
 }
 
-unsigned tiles_grid(lmgpu_guide* g, uint64_t n)
+unsigned tiles_grid(uint64_t n, int cap)
 {
     const uint64_t tiles = (n + kTile - 1) / kTile;
-    return (unsigned)(tiles < (uint64_t)g->grid ? tiles : (uint64_t)g->grid);
+    return (unsigned)(tiles < (uint64_t)cap ? tiles : (uint64_t)cap);
 }
 
 int check_status(lmgpu_guide* g, cudaStream_t s, const char* name)
@@ -476,7 +574,7 @@ int guide_forward_device(lmgpu_guide* g, const float* d_queries, uint64_t n, flo
     if (n == 0) return LMGPU_OK;
     int rc = guide_grid(g);
     if (rc) return rc;
-    k_guide_fwd<MODE_RAW><<<tiles_grid(g, n), kThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
+    k_guide_fwd<MODE_RAW><<<tiles_grid(n, g->fwd_grid), kFwdThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
                                                                       nullptr, d_raw, nullptr, g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
     return LMGPU_OK;
@@ -490,7 +588,7 @@ int guide_forward_device_dn(lmgpu_guide* g, const float* d_queries, const uint32
     if (max_n == 0) return LMGPU_OK;
     int rc = guide_grid(g);
     if (rc) return rc;
-    k_guide_fwd<MODE_RAW><<<tiles_grid(g, max_n), kThreads, kFwdSmem, s>>>(g->params, g->box, d_queries,
+    k_guide_fwd<MODE_RAW><<<tiles_grid(max_n, g->fwd_grid), kFwdThreads, kFwdSmem, s>>>(g->params, g->box, d_queries,
                                                                           (uint32_t)max_n, d_n, d_raw, nullptr,
                                                                           g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
@@ -505,12 +603,14 @@ int guide_gradient_device(lmgpu_guide* g, const float* d_queries, const float* d
     if (n == 0) return LMGPU_OK;
     int rc = guide_grid(g);
     if (rc || (rc = ensure_scratch(g, n))) return rc;
-    k_guide_fwd<MODE_TRAIN><<<tiles_grid(g, n), kThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
+    k_guide_fwd<MODE_TRAIN><<<tiles_grid(n, g->fwd_grid), kFwdThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
                                                                         nullptr, g->d_raw, g->d_acts, g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
-    k_guide_bwd<<<tiles_grid(g, n), kThreads, kBwdSmem, s>>>(g->params, g->d_raw, g->d_acts, d_dirs, d_weights,
-                                                             (uint32_t)n, 1.0f / (float)n, g->grad, g->loss,
-                                                             g->status);
+    const unsigned bgrid = tiles_grid(n, g->grid);
+    k_guide_bwd<<<bgrid, kThreads, kBwdSmem, s>>>(g->params, g->d_raw, g->d_acts, d_dirs, d_weights, (uint32_t)n,
+                                                  1.0f / (float)n, g->partials, g->loss, g->status);
+    LMGPU_CUDA_TRY(cudaGetLastError());
+    k_guide_reduce<<<(kNumParams + 255) / 256, 256, 0, s>>>(g->partials, (int)bgrid, g->grad);
     LMGPU_CUDA_TRY(cudaGetLastError());
     return LMGPU_OK;
 }
@@ -617,7 +717,8 @@ void lmgpu_guide_destroy(lmgpu_guide* g)
 {
     if (!g) return;
     cudaDeviceSynchronize();
-    void* ptrs[] = {g->params, g->grad, g->m, g->v, g->loss, g->status, g->d_q, g->d_raw, g->d_dir, g->d_w, g->d_acts};
+    void* ptrs[] = {g->params, g->grad, g->m, g->v, g->loss, g->status, g->d_q, g->d_raw, g->d_dir, g->d_w, g->d_acts,
+                    g->partials};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete g;

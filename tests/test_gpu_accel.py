@@ -232,10 +232,15 @@ def test_benchmark_size_properties(gpu_lib, oracle_lib):
     assert np.array_equal(hc["prim"] >= 0, ha["prim"] >= 0)
     hit = hc["prim"] >= 0
     assert (hc["t"][hit] >= rays[hit, 3]).all()
-    # a seeded subsample against the oracle's binned-SAH BVH
-    sub = scenes.rng(2024, 1).choice(n, 1 << 15, replace=False)
-    ref = oracle_lib.OracleAccel(1, tris).trace(rays[sub], threads=16)
-    c = hitcheck.classify(tris, rays[sub], hc["prim"][sub], ref["id"])
-    print("classes", {k: v for k, v in c.items() if k != "unexplained"}, info)
-    assert len(c["unexplained"]) <= 1e-5 * len(sub) + 1, c
-    check_t(tris, rays[sub], hc[sub])
+    # every ray against the oracle's accel::qbvh (bit-identical to the
+    # reference's own qbvh): at most 1e-5 of the rays may disagree outside
+    # the documented classes, and those classes together stay under 1e-4
+    ref = oracle_lib.OracleAccel(oracle_lib.QBVH, tris).trace(rays, threads=os.cpu_count() or 16)
+    c = hitcheck.classify(tris, rays, hc["prim"], ref["id"])
+    excluded = c["tie"] + c["edge"] + c["range"] + c["grazing"] + c["degen"]
+    shares = {k: c[k] / n for k in ("mismatch", "tie", "edge", "range", "grazing", "degen")}
+    print("classes", {k: v for k, v in c.items() if k != "unexplained"}, "shares", shares,
+          "unexplained", len(c["unexplained"]), info)
+    assert len(c["unexplained"]) <= 1e-5 * n, c["unexplained"][:20]
+    assert excluded <= 1e-4 * n, shares
+    check_t(tris, rays, hc)

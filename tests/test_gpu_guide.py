@@ -64,6 +64,26 @@ def test_gradient_matches_fp64_oracle(gpu_lib):
     net.close()
 
 
+def test_gradient_over_many_tiles_per_cta(gpu_lib):
+    """Enough samples that every CTA of the backward accumulates several
+    128-sample tiles in tensor memory before its one flush (and a partial
+    last tile): the gradient still matches the FP64 oracle, and a second call
+    on other samples is not polluted by the first."""
+    net = gpu_lib.Guide(BOX, 4)
+    p = trained_like_params(31)
+    net.set_params(p)
+    for seed in (32, 33):
+        q, d, w = problem(3 * 160 * 128 + 77, seed)
+        loss, g = net.gradient(q, d, w)
+        ref_loss, ref = og.gradient(p, q, BOX, d, w)
+        cos = float(g @ ref / (np.linalg.norm(g) * np.linalg.norm(ref)))
+        rel = float(np.linalg.norm(g - ref) / np.linalg.norm(ref))
+        print("samples", q.shape[0], "loss", loss, ref_loss, "gradient cosine", cos, "relative L2", rel)
+        assert abs(loss - ref_loss) < 1e-2 * abs(ref_loss) + 1e-4
+        assert cos > 0.999 and rel < 5e-2, (cos, rel)
+    net.close()
+
+
 def test_training_fits_a_direction_field(gpu_lib):
     """Online Adam on samples of a position-dependent target (directions
     towards a point, kappa 30): the loss falls and the learned density at

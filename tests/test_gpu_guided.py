@@ -63,7 +63,9 @@ def test_trained_guide_lowers_error(gpu_lib):
     nonet, _, _ = sc.render_pt_guided(g0, 256, -1, 4, alpha=1.0, train=False, rr_mode=1)
     g = gpu_lib.Guide(scenes.scene_box(s), 3)
     untrained, _, _ = sc.render_pt_guided(g, 256, -1, 5, alpha=0.5, train=False, rr_mode=1)
-    sc.render_pt_guided(g, 2048, -1, 2, alpha=0.5, train=True, batch=1 << 16, rr_mode=1)  # training passes
+    # training passes: 32,768 spp of the 96 x 54 film (170M samples, ~650 Adam steps
+    # of 2^18); at 2,048 spp the network is still worse than BSDF sampling alone
+    sc.render_pt_guided(g, 32768, -1, 2, alpha=0.5, train=True, rr_mode=1)
     trained, _, _ = sc.render_pt_guided(g, 256, -1, 3, alpha=0.5, train=False, rr_mode=1)
     et, en, eu = (imgcheck.relmse(x, ref, trim=1e-3) for x in (trained, nonet, untrained))
     print("trimmed relMSE at 256 spp: trained", et, "no network", en, "untrained network", eu,
