@@ -2,17 +2,17 @@
 // forward, backward and Adam kernels for the MLP of guide_net.cuh, BF16
 // operands with FP32 accumulation in tensor memory.
 //
-// k_guide_fwd   one CTA (8 warps, two threads per query) per 128-query tile
-//               at a time, two CTAs per SM, persistent over tiles.  The five
-//               weight matrices stay in shared memory (BF16, K-major
-//               canonical layout); the tile's activations
-//               ping-pong between two shared-memory buffers; each layer is
-//               K/16 MMAs of M = 128 into a 64-column tensor-memory
-//               accumulator, issued by one thread and completed through an
-//               mbarrier; the feature encoding and the epilogue (bias, ReLU,
-//               BF16 pack) run on all 256 threads, two per row (half the
-//               features and half the columns each), reading the row's
-//               columns with tcgen05.ld.
+// k_guide_fwd   one CTA per SM, persistent over 128-query tiles, as two
+//               independent groups of 4 warps that work on alternate tiles
+//               (so one group's MMAs overlap the other's feature encoding
+//               and epilogues).  The five weight matrices stay in shared
+//               memory (BF16, K-major canonical layout); a group's tile
+//               activations ping-pong between its two shared-memory buffers;
+//               each layer is K/16 MMAs of M = 128 into the group's
+//               64-column tensor-memory accumulator, issued by one thread and
+//               completed through the group's mbarrier; the feature encoding
+//               and the epilogue (bias, ReLU, BF16 pack) run one row per
+//               thread, reading the row with tcgen05.ld.
 //               MODE_TRAIN also writes every layer's input (BF16) and the raw
 //               outputs to global memory for the backward pass.
 // k_guide_bwd   one CTA per SM, persistent over 128-sample tiles: the loss
@@ -51,29 +51,36 @@ constexpr uint32_t kStatusTimeout = 16;
 constexpr uint32_t kWaitLimit = 1u << 24;
 constexpr int kTile = 128;
 constexpr int kThreads = 128;      // backward: one thread per sample of a tile
-constexpr int kFwdThreads = 256;   // forward: two threads per query of a tile
+constexpr int kFwdThreads = 256;   // forward: two tile groups of 128 threads, one query each
 constexpr int kActs = kIn + 4 * kHid;  // stored activations per sample (bf16)
 
 // shared-memory plan of the forward kernel (bytes)
 // W1 (64x128) at 0, W2..W4 (64x64) at 16384 + 8192 (l - 1), W5 (48x64) at 40960
 __host__ __device__ constexpr uint32_t fwd_w(int l) { return l == 0 ? 0u : 16384u + 8192u * (uint32_t)(l - 1); }
-constexpr uint32_t kFwdA = 47104;                              // 128 x 128 activations
-constexpr uint32_t kFwdB = kFwdA + 32768;                      // 128 x 64 activations
-constexpr uint32_t kFwdBias = kFwdB + 16384;                   // 304 floats
-constexpr uint32_t kFwdBar = kFwdBias + 1280;
+// two tile groups, each with its own activation buffers
+__host__ __device__ constexpr uint32_t fwd_a(uint32_t g) { return 47104u + 49152u * g; }  // 128 x 128 activations
+__host__ __device__ constexpr uint32_t fwd_b(uint32_t g) { return fwd_a(g) + 32768u; }   // 128 x 64 activations
+constexpr uint32_t kFwdBias = fwd_a(2);                        // 304 floats
+constexpr uint32_t kFwdBar = kFwdBias + 1280;                  // one mbarrier per group, the TMEM address
 constexpr uint32_t kFwdSmem = kFwdBar + 64;
 
 // shared-memory plan of the backward kernel (bytes)
 // W_l^T for l = 1..4 (W2^T..W4^T 64x64, W5^T 64x48) at 8192 (l - 1)
 __host__ __device__ constexpr uint32_t bwd_wt(int l) { return 8192u * (uint32_t)(l - 1); }
-constexpr uint32_t kBwdDZ = 30720;            // dZ, 128 samples x 64 (K-major, K = layer width)
-constexpr uint32_t kBwdDZT = kBwdDZ + 16384;  // dZ^T, 128 rows (64 used, 64 zero) x 128 samples
-constexpr uint32_t kBwdHT0 = kBwdDZT + 32768; // H_0^T (layer 1's input), 128 x 128 samples
-constexpr uint32_t kBwdHT = kBwdHT0 + 32768;  // H^T of layers 2..5: 64 rows, a row of ones, 15 zero rows
-constexpr uint32_t kBwdB0 = kBwdHT + 20480;   // layer 1's bias gradient, 64 floats
+// dZ^T and H^T (MN = features, K = the tile's 128 samples) are MN-major
+// operand tiles: each thread stores its sample's features eight at a time
+// (16-byte stores of 8 consecutive features)
+constexpr uint32_t kBwdDZ = 30720;             // dZ, 128 samples x 64 (K-major, K = layer width)
+constexpr uint32_t kBwdDZT = kBwdDZ + 16384;   // dZ^T, 128 features (64 used, 64 zero) x 128 samples
+constexpr uint32_t kBwdHT0 = kBwdDZT + 32768;  // H_0^T (layer 1's input), 128 features x 128 samples
+constexpr uint32_t kBwdHT = kBwdHT0 + 32768;   // H^T of layers 2..5: 64 features, a feature of ones, 15 zero
+constexpr uint32_t kBwdB0 = kBwdHT + 20480;    // layer 1's bias gradient, 64 floats
 constexpr uint32_t kBwdBar = kBwdB0 + 256;
-constexpr uint32_t kBwdSmem = kBwdBar + 64;   // 133,440 bytes: one CTA per SM, which holds all 512 TMEM columns
-constexpr uint32_t kBwdHTRows = kHid + 16;    // rows of H^T for layers 2..5 (N of their dW MMA)
+// 16 KB of slack after the plan: descriptor address ranges of the MN-major
+// tiles stay inside the allocation even if their two strides were read the
+// other way round; 149,824 bytes, one CTA per SM holding all 512 TMEM columns
+constexpr uint32_t kBwdSmem = kBwdBar + 64 + 16384;
+constexpr uint32_t kBwdHTRows = kHid + 16;                 // rows of H^T for layers 2..5 (N of their dW MMA)
 // tensor-memory columns of the backward kernel: dH at 0, layer 1's dW at
 // 64 (128 columns), layer l = 1..4's dW (+ bias column 64) at 192 + 80 (l - 1)
 __host__ __device__ constexpr uint32_t bwd_dw_col(int l) { return l == 0 ? 64u : 192u + 80u * (uint32_t)(l - 1); }
@@ -101,9 +108,11 @@ __device__ __forceinline__ void put8(unsigned char* tile, uint32_t r, uint32_t k
     *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(r, k, K)) = q;
 }
 
-__device__ __forceinline__ void put1(unsigned char* tile, uint32_t r, uint32_t k, uint32_t K, float v)
+// Features m .. m + 7 (m a multiple of 8) of sample k into an MN-major tile
+// with MN feature rows.
+__device__ __forceinline__ void put8mn(unsigned char* tile, uint32_t m, uint32_t k, uint32_t MN, uint4 q)
 {
-    *reinterpret_cast<__nv_bfloat16*>(tile + tc::kmajor_offset(r, k, K)) = __float2bfloat16_rn(v);
+    *reinterpret_cast<uint4*>(tile + tc::mnmajor_offset(m, k, MN)) = q;
 }
 
 // W (rows x cols, fp32 row-major; transpose: stored as W^T) into a K-major tile.
@@ -172,8 +181,47 @@ __device__ __forceinline__ void block_sync_for_mma()
     tc::fence_after_sync();
 }
 
+// Named barrier over the 128 threads of tile group g (barrier 1 + g;
+// barrier 0 is __syncthreads).
+__device__ __forceinline__ void group_sync(uint32_t g)
+{
+    asm volatile("bar.sync %0, 128;" ::"r"(1u + g) : "memory");
+}
+
+// The same barrier, returning whether every thread of the group passed v.
+__device__ __forceinline__ bool group_sync_and(uint32_t g, bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(v ? 1u : 0u), "r"(1u + g)
+        : "memory");
+    return r != 0u;
+}
+
+__device__ __forceinline__ void group_sync_for_mma(uint32_t g)
+{
+    tc::fence_smem_async();
+    tc::fence_before_sync();
+    group_sync(g);
+    tc::fence_after_sync();
+}
+
+// wait_layer for one tile group.
+__device__ __forceinline__ bool group_wait_layer(uint32_t g, uint64_t* bar, uint32_t& phase, uint32_t* status)
+{
+    const bool mine = tc::mbar_wait(bar, phase, kWaitLimit);
+    phase ^= 1u;
+    const bool ok = group_sync_and(g, mine);
+    if (!ok && (threadIdx.x & 127u) == 0u) atomicOr(status, kStatusTimeout);
+    tc::fence_after_sync();
+    return ok;
+}
+
 template <int MODE>
-__global__ void __launch_bounds__(kFwdThreads, 2) k_guide_fwd(const float* __restrict__ params, Box box,
+__global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __restrict__ params, Box box,
                                                               const float* __restrict__ queries, uint32_t n,
                                                               const uint32_t* __restrict__ d_n,
                                                               float* __restrict__ raw_out,
@@ -183,12 +231,14 @@ __global__ void __launch_bounds__(kFwdThreads, 2) k_guide_fwd(const float* __res
     if (d_n) n = *d_n;  // query count on the device (at most the n launched for)
     extern __shared__ __align__(1024) unsigned char smem[];
     float* sbias = reinterpret_cast<float*>(smem + kFwdBias);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kFwdBar);
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kFwdBar + 8);
-    // two threads per row of the tile: r = the row, half = which half of the
-    // row's features and columns this thread computes; a warp reads tensor
-    // memory lanes 32 (warp % 4) .. + 31, the rows of its threads
-    const uint32_t tid = threadIdx.x, warp = tid >> 5, r = tid & (kTile - 1u), half = tid >> 7;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kFwdBar);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kFwdBar + 16);
+    // two independent tile groups of 128 threads, one row of a tile each;
+    // group g works on tiles 2 blockIdx.x + g, + 2 gridDim.x, ..., with its
+    // own activation buffers, mbarrier and 64 tensor-memory columns, so one
+    // group's MMAs run while the other computes features or an epilogue.  A
+    // warp reads tensor memory lanes 32 (warp % 4) .. + 31, its rows.
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, r = tid & (kTile - 1u);
     const uint32_t lane_base = (warp & 3u) * 32u;
 
     for (int l = 0; l < 5; l++) load_matrix(smem + fwd_w(l), params + w_off(l), layer_out(l), layer_in(l), false);
@@ -197,22 +247,26 @@ __global__ void __launch_bounds__(kFwdThreads, 2) k_guide_fwd(const float* __res
         sbias[i] = params[b_off(l) + j];
     }
     if (tid == 0) {
-        tc::mbar_init(bar, 1);
+        tc::mbar_init(bars, 1);
+        tc::mbar_init(bars + 1, 1);
         tc::mbar_init_fence();
     }
-    if (warp == 0) tc::tmem_alloc(s_tmem, 64);
+    if (warp == 0) tc::tmem_alloc(s_tmem, 128);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = *s_tmem;
-    const uint32_t sA = tc::smem_addr(smem + kFwdA), sB = tc::smem_addr(smem + kFwdB);
+    const uint32_t tmem = *s_tmem + 64u * g;
+    uint64_t* bar = bars + g;
+    unsigned char* bufA = smem + fwd_a(g);
+    unsigned char* bufB = smem + fwd_b(g);
+    const uint32_t sA = tc::smem_addr(bufA), sB = tc::smem_addr(bufB);
     uint32_t phase = 0;
     bool alive = true;
 
     const uint32_t ntiles = (n + kTile - 1) / kTile;
-    for (uint32_t tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x) {
+    for (uint32_t tile = 2u * blockIdx.x + g; tile < ntiles && alive; tile += 2u * gridDim.x) {
         const uint32_t row = tile * kTile + r;
-        // features of the row's query, eight at a time: groups half, half + 2, ...
+        // features of the row's query, eight at a time
         {
             float x[3] = {0.0f, 0.0f, 0.0f}, nn[3] = {0.0f, 0.0f, 0.0f}, wo[3] = {0.0f, 0.0f, 0.0f};
             if (row < n) {
@@ -224,67 +278,68 @@ __global__ void __launch_bounds__(kFwdThreads, 2) k_guide_fwd(const float* __res
                 }
             }
 #pragma unroll
-            for (int j8 = 0; j8 < kIn / 16; j8++) {
-                const int g8 = 2 * j8 + (int)half;
+            for (int g8 = 0; g8 < kIn / 8; g8++) {
                 float f[8];
                 if (row < n) {
                     features8(x, nn, wo, box.lo, box.inv_ext, g8, f);
                 } else {
                     for (int j = 0; j < 8; j++) f[j] = 0.0f;
                 }
-                put8(smem + kFwdA, r, 8 * g8, kIn, f);
+                put8(bufA, r, 8 * g8, kIn, f);
                 if (MODE == MODE_TRAIN && row < n)
                     reinterpret_cast<uint4*>(acts + (size_t)row * kActs)[g8] =
                         make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]), pack2(f[6], f[7]));
             }
         }
-        block_sync_for_mma();
+        group_sync_for_mma(g);
 #pragma unroll
         for (int l = 0; l < 5; l++) {
             if (!alive) break;
             // layer l reads buffer A (l even) or B (l odd)
             const uint32_t a_in = (l & 1) ? sB : sA;
-            unsigned char* out_tile = smem + ((l & 1) ? kFwdA : kFwdB);
+            unsigned char* out_tile = (l & 1) ? bufA : bufB;
             const uint32_t K = layer_in(l), N = layer_out(l);
-            if (tid == 0) issue_layer(tmem, a_in, K, tc::smem_addr(smem + fwd_w(l)), N, bar);
-            alive = wait_layer(bar, phase, status);
+            if (r == 0) issue_layer(tmem, a_in, K, tc::smem_addr(smem + fwd_w(l)), N, bar);
+            alive = group_wait_layer(g, bar, phase, status);
             if (!alive) break;
             const float* bias = sbias + l * kHid;
             if (l < 4) {
-                // columns 32 half .. 32 half + 31 of the row
-                const uint32_t c0 = 32u * half;
-                float h[32];
-                tc::tmem_load16(tc::tmem_at(tmem, lane_base, c0), h);
-                tc::tmem_load16(tc::tmem_at(tmem, lane_base, c0 + 16u), h + 16);
+                float h[kHid];
+#pragma unroll
+                for (int c = 0; c < kHid; c += 16) tc::tmem_load16(tc::tmem_at(tmem, lane_base, c), h + c);
                 tc::tmem_wait_ld();
-                for (int c = 0; c < 32; c++) h[c] = fmaxf(h[c] + bias[c0 + c], 0.0f);
-                for (int c = 0; c < 32; c += 8) put8(out_tile, r, c0 + c, kHid, h + c);
+                for (int c = 0; c < kHid; c++) h[c] = fmaxf(h[c] + bias[c], 0.0f);
+                for (int c = 0; c < kHid; c += 8) put8(out_tile, r, c, kHid, h + c);
                 if (MODE == MODE_TRAIN && row < n) {
-                    uint4* dst = reinterpret_cast<uint4*>(acts + (size_t)row * kActs + kIn + l * kHid + c0);
-                    for (int c = 0; c < 32; c += 8)
+                    uint4* dst = reinterpret_cast<uint4*>(acts + (size_t)row * kActs + kIn + l * kHid);
+                    for (int c = 0; c < kHid; c += 8)
                         dst[c / 8] = make_uint4(pack2(h[c], h[c + 1]), pack2(h[c + 2], h[c + 3]),
                                                 pack2(h[c + 4], h[c + 5]), pack2(h[c + 6], h[c + 7]));
                 }
             } else {
-                // raw outputs 0..31 (half 0) and 32..39 (half 1; columns 40..47 are padding)
-                float z[32];
-                tc::tmem_load16(tc::tmem_at(tmem, lane_base, 32u * half), z);
-                if (half == 0u) tc::tmem_load16(tc::tmem_at(tmem, lane_base, 16u), z + 16);
+                float z[kOut];
+#pragma unroll
+                for (int c = 0; c < kOut; c += 16) tc::tmem_load16(tc::tmem_at(tmem, lane_base, c), z + c);
                 tc::tmem_wait_ld();
                 if (row < n) {
-                    const int c0 = 32 * (int)half, cn = half ? kOutUsed - 32 : 32;
-                    float4* dst = reinterpret_cast<float4*>(raw_out + (size_t)row * kOutUsed + c0);
-#pragma unroll
-                    for (int c = 0; c < 32; c += 4)
-                        if (c < cn)
-                            dst[c / 4] = make_float4(z[c] + bias[c0 + c], z[c + 1] + bias[c0 + c + 1],
-                                                     z[c + 2] + bias[c0 + c + 2], z[c + 3] + bias[c0 + c + 3]);
+                    float4* dst = reinterpret_cast<float4*>(raw_out + (size_t)row * kOutUsed);
+                    for (int c = 0; c < kOutUsed; c += 4)
+                        dst[c / 4] = make_float4(z[c] + bias[c], z[c + 1] + bias[c + 1], z[c + 2] + bias[c + 2],
+                                                 z[c + 3] + bias[c + 3]);
                 }
             }
-            block_sync_for_mma();
+            group_sync_for_mma(g);
         }
     }
-    release_tmem(bar, phase, alive, tmem, 64);
+    // after a time-out, one more bounded wait for this group's MMAs in flight
+    if (!alive) tc::mbar_wait(bar, phase ^ 1u, kWaitLimit);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(*s_tmem, 128);
+        tc::tmem_relinquish();
+    }
 }
 
 __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restrict__ params,
@@ -310,9 +365,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
     // ones (bias gradient), rows 65..79 zero
     for (uint32_t i = tid; i < 32768u / 16u; i += kThreads)
         reinterpret_cast<uint4*>(sDZT)[i] = make_uint4(0u, 0u, 0u, 0u);
-    for (uint32_t i = tid; i < (kBwdHTRows - (uint32_t)kHid) * (uint32_t)kTile; i += kThreads) {
-        const uint32_t r = (uint32_t)kHid + i / (uint32_t)kTile, k = i % (uint32_t)kTile;
-        put1(sHT, r, k, kTile, r == (uint32_t)kHid ? 1.0f : 0.0f);
+    for (uint32_t k = tid; k < (uint32_t)kTile; k += kThreads) {
+        put8mn(sHT, kHid, k, kBwdHTRows, make_uint4(pack2(1.0f, 0.0f), 0u, 0u, 0u));
+        put8mn(sHT, kHid + 8, k, kBwdHTRows, make_uint4(0u, 0u, 0u, 0u));
     }
     if (tid < (uint32_t)kHid) sb0[tid] = 0.0f;
     if (tid == 0) {
@@ -368,29 +423,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
             } else {
                 for (uint32_t c = 0; c < Nl; c += 8) put8(sDZ, tid, c, Nl, dz + c);
             }
-            // dZ^T (rows = output features, K = samples) and H^T (rows = inputs)
-            for (uint32_t c = 0; c < (uint32_t)kHid; c++) put1(sDZT, c, tid, kTile, dz[c]);
-            {
-                unsigned char* ht = l == 0 ? sHT0 : sHT;
-                for (uint32_t q = 0; q < Kin / 8; q++) {
-                    const uint32_t w4[4] = {hv[q].x, hv[q].y, hv[q].z, hv[q].w};
-                    for (int e = 0; e < 4; e++) {
-                        const __nv_bfloat162 p = *reinterpret_cast<const __nv_bfloat162*>(&w4[e]);
-                        *reinterpret_cast<__nv_bfloat16*>(ht + tc::kmajor_offset(8 * q + 2 * e, tid, kTile)) = p.x;
-                        *reinterpret_cast<__nv_bfloat16*>(ht + tc::kmajor_offset(8 * q + 2 * e + 1, tid, kTile)) = p.y;
-                    }
-                }
-            }
+            // dZ^T (MN = output features, K = samples) and H^T (MN = inputs):
+            // this sample's column of each, eight features per store
+            for (uint32_t c = 0; c < (uint32_t)kHid; c += 8)
+                put8mn(sDZT, c, tid, kTile,
+                       make_uint4(pack2(dz[c], dz[c + 1]), pack2(dz[c + 2], dz[c + 3]), pack2(dz[c + 4], dz[c + 5]),
+                                  pack2(dz[c + 6], dz[c + 7])));
+            for (uint32_t q = 0; q < Kin / 8; q++)
+                put8mn(l == 0 ? sHT0 : sHT, 8 * q, tid, l == 0 ? (uint32_t)kIn : kBwdHTRows, hv[q]);
             block_sync_for_mma();
             if (tid == 0) {
                 // dW (+)= dZ^T (128 x 128 samples) x (H^T, N x 128 samples)^T,
                 // accumulated in tensor memory over the CTA's tiles
                 const uint32_t N = l == 0 ? (uint32_t)kIn : kBwdHTRows;
-                const uint32_t idesc_w = tc::idesc_bf16_f32(128, N);
+                const uint32_t idesc_w = tc::idesc_bf16_f32_mn(128, N);
                 const uint32_t a0 = tc::smem_addr(sDZT), b0 = tc::smem_addr(l == 0 ? sHT0 : sHT);
+                // one K step = 16 samples = two core matrices along K
                 for (uint32_t ks = 0; ks < (uint32_t)kTile / 16u; ks++)
-                    tc::mma_bf16(tmem + bwd_dw_col(l), tc::kmajor_desc(a0 + ks * 256u, kTile),
-                                 tc::kmajor_desc(b0 + ks * 256u, kTile), idesc_w, (first && ks == 0) ? 0u : 1u);
+                    tc::mma_bf16(tmem + bwd_dw_col(l), tc::mnmajor_desc(a0 + ks * 2u * (kTile * 16u), kTile),
+                                 tc::mnmajor_desc(b0 + ks * 2u * (N * 16u), N), idesc_w, (first && ks == 0) ? 0u : 1u);
                 // dH_{l-1} = dZ_l (128 x Nl) x (W_l^T, Kin x Nl)^T
                 if (l > 0) {
                     const uint32_t idesc_h = tc::idesc_bf16_f32(128, Kin);
@@ -501,7 +552,7 @@ struct lmgpu_guide {
     float* d_w = nullptr;
     __nv_bfloat16* d_acts = nullptr;
     int grid = 0;         // backward: one CTA per SM
-    int fwd_grid = 0;     // forward: two CTAs per SM
+    int fwd_grid = 0;     // forward: one CTA (two tile groups) per SM
     float* partials = nullptr;  // [grid][kNumParams] per-CTA gradients of the backward
 };
 
@@ -543,7 +594,7 @@ int guide_grid(lmgpu_guide* g)
             cudaFuncSetAttribute(k_guide_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
         LMGPU_CUDA_TRY(cudaMalloc((void**)&g->partials, sizeof(float) * (size_t)sms * kNumParams));
         g->grid = sms;
-        g->fwd_grid = 2 * sms;
+        g->fwd_grid = sms;
     }
     return LMGPU_OK;
 }
@@ -553,6 +604,9 @@ unsigned tiles_grid(uint64_t n, int cap)
     const uint64_t tiles = (n + kTile - 1) / kTile;
     return (unsigned)(tiles < (uint64_t)cap ? tiles : (uint64_t)cap);
 }
+
+// Forward CTAs: two tiles at a time each.
+unsigned fwd_grid_of(uint64_t n, int cap) { return tiles_grid((n + kTile - 1) / kTile * (kTile / 2), cap); }
 
 int check_status(lmgpu_guide* g, cudaStream_t s, const char* name)
 {
@@ -574,7 +628,7 @@ int guide_forward_device(lmgpu_guide* g, const float* d_queries, uint64_t n, flo
     if (n == 0) return LMGPU_OK;
     int rc = guide_grid(g);
     if (rc) return rc;
-    k_guide_fwd<MODE_RAW><<<tiles_grid(n, g->fwd_grid), kFwdThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
+    k_guide_fwd<MODE_RAW><<<fwd_grid_of(n, g->fwd_grid), kFwdThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
                                                                       nullptr, d_raw, nullptr, g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
     return LMGPU_OK;
@@ -588,7 +642,7 @@ int guide_forward_device_dn(lmgpu_guide* g, const float* d_queries, const uint32
     if (max_n == 0) return LMGPU_OK;
     int rc = guide_grid(g);
     if (rc) return rc;
-    k_guide_fwd<MODE_RAW><<<tiles_grid(max_n, g->fwd_grid), kFwdThreads, kFwdSmem, s>>>(g->params, g->box, d_queries,
+    k_guide_fwd<MODE_RAW><<<fwd_grid_of(max_n, g->fwd_grid), kFwdThreads, kFwdSmem, s>>>(g->params, g->box, d_queries,
                                                                           (uint32_t)max_n, d_n, d_raw, nullptr,
                                                                           g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
@@ -603,7 +657,7 @@ int guide_gradient_device(lmgpu_guide* g, const float* d_queries, const float* d
     if (n == 0) return LMGPU_OK;
     int rc = guide_grid(g);
     if (rc || (rc = ensure_scratch(g, n))) return rc;
-    k_guide_fwd<MODE_TRAIN><<<tiles_grid(n, g->fwd_grid), kFwdThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
+    k_guide_fwd<MODE_TRAIN><<<fwd_grid_of(n, g->fwd_grid), kFwdThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
                                                                         nullptr, g->d_raw, g->d_acts, g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
     const unsigned bgrid = tiles_grid(n, g->grid);

@@ -4,7 +4,8 @@
 // memory, its completion through an mbarrier (waited on with an iteration
 // limit), and tensor-memory loads for the epilogue.
 //
-// Operand layout used throughout: "K-major, no swizzle" canonical layout.
+// Operand layouts: "K-major, no swizzle" canonical layout, and its
+// MN-major counterpart for operands stored one K index at a time.
 // An R x K tile of bf16 is a grid of 8 x 8 core matrices; each core matrix
 // is 8 rows of 16 contiguous bytes (128 bytes).  Element (r, k) lives at
 //   (r / 8) * SBO + (k / 8) * LBO + (r % 8) * 16 + (k % 8) * 2
@@ -27,6 +28,17 @@ __host__ __device__ __forceinline__ uint32_t kmajor_offset(uint32_t r, uint32_t 
     return (r >> 3) * (K * 16u) + (k >> 3) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
 }
 
+// "MN-major, no swizzle" canonical layout of an MN x K tile: each core
+// matrix is 8 K-rows of 16 bytes (8 consecutive MN elements); core matrices
+// adjacent along MN are contiguous (SBO = 128) and those along K are
+// (MN / 8) * 128 bytes apart (LBO).  Element (m, k) lives at
+//   (m / 8) * 128 + (k / 8) * (MN / 8) * 128 + (k % 8) * 16 + (m % 8) * 2,
+// so eight consecutive MN elements of one K index are one 16-byte store.
+__host__ __device__ __forceinline__ uint32_t mnmajor_offset(uint32_t m, uint32_t k, uint32_t MN)
+{
+    return (m >> 3) * 128u + (k >> 3) * (MN * 16u) + (k & 7u) * 16u + (m & 7u) * 2u;
+}
+
 // Shared-memory matrix descriptor: start address, LBO, SBO (bytes, encoded
 // >> 4), descriptor version 1 (bits 46-48), base offset 0, no swizzle.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
@@ -42,11 +54,21 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 // Descriptor of a K-major canonical tile with K columns starting at saddr.
 __device__ __forceinline__ uint64_t kmajor_desc(uint32_t saddr, uint32_t K) { return smem_desc(saddr, 128u, K * 16u); }
 
+// Descriptor of an MN-major canonical tile with MN rows starting at saddr
+// (LBO = the stride between core matrices along K, SBO = along MN).
+__device__ __forceinline__ uint64_t mnmajor_desc(uint32_t saddr, uint32_t MN) { return smem_desc(saddr, MN * 16u, 128u); }
+
 // Instruction descriptor, kind::f16: D f32, A and B bf16, both K-major,
 // dense, M x N (M = 128: N multiple of 16 in [16, 256]).
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+// The same with A and B given MN-major (bits 15 and 16: transpose A, B).
+__host__ __device__ constexpr uint32_t idesc_bf16_f32_mn(uint32_t M, uint32_t N)
+{
+    return idesc_bf16_f32(M, N) | (1u << 15) | (1u << 16);
 }
 
 // Allocates ncols (power of two, 32..512) tensor-memory columns; the
