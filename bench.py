@@ -124,6 +124,16 @@ def traffic_per_launch() -> float | None:
     return None
 
 
+def l2_figures() -> dict | None:
+    """L2 throughput of the traversal from the committed ncu summary: the
+    level the node and triangle fetches actually hit."""
+    p = os.path.join(REPO, "profiles", "trace_closest_traffic.json")
+    try:
+        return dict(json.load(open(p))["l2"])
+    except Exception:
+        return None
+
+
 class CpuReference:
     """The reference's fastest native accel, accel::qbvh, on the host cores.
 
@@ -314,7 +324,8 @@ def run_gpu(args) -> None:
                              "nodes_per_ray": st["node_fetches"] / nr,
                              "tris_per_ray": st["triangle_fetches"] / nr,
                              "note": "algorithmic bytes = 32 B ray + 16 B hit + 80 B per node fetch + 48 B per "
-                                     "triangle test; node/triangle fetches are mostly L2 hits"},
+                                     "triangle test; node/triangle fetches are mostly L2 hits",
+                             "l2": l2_figures()},
                 "clocks": clk,
                 "accel": {"build_ms": info["build_ms"], "wide_nodes": info["num_wide_nodes"],
                           "binary_depth": info["binary_depth"], "wide_depth": info["wide_depth"],
