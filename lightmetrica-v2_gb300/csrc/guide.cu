@@ -15,17 +15,18 @@
 //               thread, reading the row with tcgen05.ld.
 //               MODE_TRAIN also writes every layer's input (BF16) and the raw
 //               outputs to global memory for the backward pass.
-// k_guide_bwd   one CTA per SM, persistent over 128-sample tiles: the loss
+// k_guide_bwd   one CTA per SM, persistent over 128-sample tiles, as two
+//               independent groups of 4 warps on alternate tiles: the loss
 //               gradient of the outputs, then for each layer, from the last,
-//               dH = dZ W (M = 128 MMA against W^T kept in shared memory) and
-//               dW += dZ^T H, an M = 128 MMA (dZ^T's 64 rows padded with
-//               zeros) over the tile's 128 samples as K, accumulated in tensor
-//               memory across every tile the CTA processes.  For layers 2..5
-//               H^T carries an extra row of ones, so the same MMA also sums
-//               the bias gradient (column 64 of the layer's accumulator);
-//               layer 1's bias gradient is summed in shared memory.  After
-//               its last tile each CTA writes its gradient once to its own
-//               slice of a partials buffer.
+//               dH = dZ W (M = 128 MMA against W^T kept in shared memory, into
+//               the group's own 64 tensor-memory columns) and dW += dZ^T H,
+//               an M = 128 MMA (dZ^T's 64 rows padded with zeros) over the
+//               tile's 128 samples as K, with dZ^T and H^T MN-major.  The dW
+//               accumulators (384 columns, zeroed at the start) are shared by
+//               both groups and summed across every tile the CTA processes;
+//               the bias gradients are summed from the dZ^T tiles in registers
+//               while the MMAs run.  After its last tile each CTA writes its
+//               gradient once to its own slice of a partials buffer.
 // k_guide_reduce  adds the CTAs' partial gradients into the FP32 gradient.
 // k_guide_adam  Adam on the FP32 master parameters (gradients zeroed).
 //
@@ -50,7 +51,7 @@ using namespace guide;
 constexpr uint32_t kStatusTimeout = 16;
 constexpr uint32_t kWaitLimit = 1u << 24;
 constexpr int kTile = 128;
-constexpr int kThreads = 128;      // backward: one thread per sample of a tile
+constexpr int kThreads = 256;      // backward: two tile groups of 128 threads, one sample each
 constexpr int kFwdThreads = 256;   // forward: two tile groups of 128 threads, one query each
 constexpr int kActs = kIn + 4 * kHid;  // stored activations per sample (bf16)
 
@@ -65,25 +66,19 @@ constexpr uint32_t kFwdBar = kFwdBias + 1280;                  // one mbarrier p
 constexpr uint32_t kFwdSmem = kFwdBar + 64;
 
 // shared-memory plan of the backward kernel (bytes)
-// W_l^T for l = 1..4 (W2^T..W4^T 64x64, W5^T 64x48) at 8192 (l - 1)
+// W_l^T for l = 1..4 (W2^T..W4^T 64x64, W5^T 64x48) at 8192 (l - 1), shared by both tile groups
 __host__ __device__ constexpr uint32_t bwd_wt(int l) { return 8192u * (uint32_t)(l - 1); }
-// dZ^T and H^T (MN = features, K = the tile's 128 samples) are MN-major
-// operand tiles: each thread stores its sample's features eight at a time
-// (16-byte stores of 8 consecutive features)
-constexpr uint32_t kBwdDZ = 30720;             // dZ, 128 samples x 64 (K-major, K = layer width)
-constexpr uint32_t kBwdDZT = kBwdDZ + 16384;   // dZ^T, 128 features (64 used, 64 zero) x 128 samples
-constexpr uint32_t kBwdHT0 = kBwdDZT + 32768;  // H_0^T (layer 1's input), 128 features x 128 samples
-constexpr uint32_t kBwdHT = kBwdHT0 + 32768;   // H^T of layers 2..5: 64 features, a feature of ones, 15 zero
-constexpr uint32_t kBwdB0 = kBwdHT + 20480;    // layer 1's bias gradient, 64 floats
-constexpr uint32_t kBwdBar = kBwdB0 + 256;
-// 16 KB of slack after the plan: descriptor address ranges of the MN-major
-// tiles stay inside the allocation even if their two strides were read the
-// other way round; 149,824 bytes, one CTA per SM holding all 512 TMEM columns
-constexpr uint32_t kBwdSmem = kBwdBar + 64 + 16384;
-constexpr uint32_t kBwdHTRows = kHid + 16;                 // rows of H^T for layers 2..5 (N of their dW MMA)
-// tensor-memory columns of the backward kernel: dH at 0, layer 1's dW at
-// 64 (128 columns), layer l = 1..4's dW (+ bias column 64) at 192 + 80 (l - 1)
-__host__ __device__ constexpr uint32_t bwd_dw_col(int l) { return l == 0 ? 64u : 192u + 80u * (uint32_t)(l - 1); }
+// per tile group g: dZ (128 samples x 64, K-major, K = layer width), dZ^T (MN-major,
+// 128 features of which 64 are used x 128 samples) and H^T (MN-major, up to 128
+// features x 128 samples): each thread stores its sample's features 8 at a time
+__host__ __device__ constexpr uint32_t bwd_dz(uint32_t g) { return 30720u + 81920u * g; }
+__host__ __device__ constexpr uint32_t bwd_dzt(uint32_t g) { return bwd_dz(g) + 16384u; }
+__host__ __device__ constexpr uint32_t bwd_ht(uint32_t g) { return bwd_dzt(g) + 32768u; }
+constexpr uint32_t kBwdBar = bwd_dz(2);        // one mbarrier per group, the TMEM address
+constexpr uint32_t kBwdSmem = kBwdBar + 64;    // 194,624 bytes: one CTA per SM, holding all 512 TMEM columns
+// tensor-memory columns of the backward kernel: group g's dH at 64 g, layer 1's
+// dW at 128 (128 columns), layer l = 1..4's dW at 256 + 64 (l - 1)
+__host__ __device__ constexpr uint32_t bwd_dw_col(int l) { return l == 0 ? 128u : 256u + 64u * (uint32_t)(l - 1); }
 
 enum : int { MODE_RAW = 0, MODE_TRAIN = 1 };
 
@@ -147,40 +142,6 @@ __device__ __forceinline__ void issue_layer(uint32_t d_tmem, uint32_t a_saddr, u
     tc::mma_commit(bar);
 }
 
-// All threads: wait for the committed MMAs (bounded), agree on the outcome,
-// then order tensor-memory reads after them.
-__device__ __forceinline__ bool wait_layer(uint64_t* bar, uint32_t& phase, uint32_t* status)
-{
-    const bool mine = tc::mbar_wait(bar, phase, kWaitLimit);
-    phase ^= 1u;
-    const bool ok = __syncthreads_and(mine ? 1 : 0) != 0;
-    if (!ok && threadIdx.x == 0) atomicOr(status, kStatusTimeout);
-    tc::fence_after_sync();
-    return ok;
-}
-
-// End of a kernel: after a time-out, one more bounded wait for the MMAs
-// still in flight; then the allocating warp frees its tensor memory.
-__device__ __forceinline__ void release_tmem(uint64_t* bar, uint32_t phase, bool alive, uint32_t tmem, uint32_t ncols)
-{
-    if (!alive) tc::mbar_wait(bar, phase ^ 1u, kWaitLimit);
-    tc::fence_before_sync();
-    __syncthreads();
-    if ((threadIdx.x >> 5) == 0) {
-        tc::fence_after_sync();
-        tc::tmem_dealloc(tmem, ncols);
-        tc::tmem_relinquish();
-    }
-}
-
-__device__ __forceinline__ void block_sync_for_mma()
-{
-    tc::fence_smem_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-}
-
 // Named barrier over the 128 threads of tile group g (barrier 1 + g;
 // barrier 0 is __syncthreads).
 __device__ __forceinline__ void group_sync(uint32_t g)
@@ -209,7 +170,8 @@ __device__ __forceinline__ void group_sync_for_mma(uint32_t g)
     tc::fence_after_sync();
 }
 
-// wait_layer for one tile group.
+// All threads of tile group g: wait for the group's committed MMAs (bounded),
+// agree on the outcome, then order tensor-memory reads after them.
 __device__ __forceinline__ bool group_wait_layer(uint32_t g, uint64_t* bar, uint32_t& phase, uint32_t* status)
 {
     const bool mine = tc::mbar_wait(bar, phase, kWaitLimit);
@@ -351,27 +313,27 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
                                                            float* __restrict__ loss, uint32_t* __restrict__ status)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kBwdBar);
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kBwdBar + 8);
-    float* sb0 = reinterpret_cast<float*>(smem + kBwdB0);
-    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-    unsigned char* sDZ = smem + kBwdDZ;
-    unsigned char* sDZT = smem + kBwdDZT;
-    unsigned char* sHT0 = smem + kBwdHT0;
-    unsigned char* sHT = smem + kBwdHT;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kBwdBar);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kBwdBar + 16);
+    // two independent tile groups of 128 threads (one sample each) on
+    // alternate tiles; they share the weights and the dW accumulators, and
+    // each has its own operand tiles, dH columns, mbarrier and named barrier
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u, g = tid >> 7, r = tid & (kTile - 1u);
+    const uint32_t lane_base = (warp & 3u) * 32u;
+    unsigned char* sDZ = smem + bwd_dz(g);
+    unsigned char* sDZT = smem + bwd_dzt(g);
+    unsigned char* sHT = smem + bwd_ht(g);
+    uint64_t* bar = bars + g;
     // W_l^T for l = 2..5 (tile rows = layer inputs, K = layer outputs)
     for (int l = 1; l < 5; l++) load_matrix(smem + bwd_wt(l), params + w_off(l), layer_out(l), layer_in(l), true);
-    // dZ^T rows 64..127 stay zero (M padding); H^T of layers 2..5: row 64
-    // ones (bias gradient), rows 65..79 zero
-    for (uint32_t i = tid; i < 32768u / 16u; i += kThreads)
-        reinterpret_cast<uint4*>(sDZT)[i] = make_uint4(0u, 0u, 0u, 0u);
-    for (uint32_t k = tid; k < (uint32_t)kTile; k += kThreads) {
-        put8mn(sHT, kHid, k, kBwdHTRows, make_uint4(pack2(1.0f, 0.0f), 0u, 0u, 0u));
-        put8mn(sHT, kHid + 8, k, kBwdHTRows, make_uint4(0u, 0u, 0u, 0u));
+    // dZ^T feature rows 64..127 stay zero (M padding)
+    for (uint32_t i = tid; i < 2u * 32768u / 16u; i += kThreads) {
+        const uint32_t gg = i / (32768u / 16u), j = i % (32768u / 16u);
+        reinterpret_cast<uint4*>(smem + bwd_dzt(gg))[j] = make_uint4(0u, 0u, 0u, 0u);
     }
-    if (tid < (uint32_t)kHid) sb0[tid] = 0.0f;
     if (tid == 0) {
-        tc::mbar_init(bar, 1);
+        tc::mbar_init(bars, 1);
+        tc::mbar_init(bars + 1, 1);
         tc::mbar_init_fence();
     }
     if (warp == 0) tc::tmem_alloc(s_tmem, 512);
@@ -379,15 +341,29 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *s_tmem;
-    const uint32_t dh_col = 0;
+    // zero the dW accumulators (columns 128..511): both groups then only add
+    {
+        const uint32_t c0 = 128u + 192u * g;
+        for (uint32_t c = 0; c < 192u; c += 16u) tc::tmem_store16_zero(tc::tmem_at(tmem, lane_base, c0 + c));
+        tc::tmem_wait_st();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t dh_col = 64u * g;
     uint32_t phase = 0;
     bool alive = true;
-    bool first = true;
     float lsum = 0.0f;
+    // bias-gradient partial sums: thread r adds features 8 q .. 8 q + 7 (q = r / 16)
+    // of samples r % 16 + 16 j, j = 0..7, of every tile, per layer
+    float bacc[5][8];
+    for (int l = 0; l < 5; l++)
+        for (int j = 0; j < 8; j++) bacc[l][j] = 0.0f;
+    const uint32_t bq = r >> 4, bk = r & 15u;
 
     const uint32_t ntiles = (n + kTile - 1) / kTile;
-    for (uint32_t tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x) {
-        const uint32_t row = tile * kTile + tid;
+    for (uint32_t tile = 2u * blockIdx.x + g; tile < ntiles && alive; tile += 2u * gridDim.x) {
+        const uint32_t row = tile * kTile + r;
         const bool valid = row < n;
         // dL/dz of the output layer (rows 40..47 and invalid samples are zero)
         float dz[kHid];
@@ -413,35 +389,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
                                                                   (l == 0 ? 0 : kIn + (l - 1) * kHid));
                 for (uint32_t q = 0; q < Kin / 8; q++) hv[q] = valid ? src[q] : make_uint4(0u, 0u, 0u, 0u);
             }
-            if (l == 0) {
-                // layer 1's bias gradient: per-warp sums into shared memory
-                for (int c = 0; c < kHid; c++) {
-                    float v = dz[c];
-                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                    if (lane == 0u && v != 0.0f) atomicAdd(sb0 + c, v);
-                }
-            } else {
-                for (uint32_t c = 0; c < Nl; c += 8) put8(sDZ, tid, c, Nl, dz + c);
-            }
+            if (l > 0)
+                for (uint32_t c = 0; c < Nl; c += 8) put8(sDZ, r, c, Nl, dz + c);
             // dZ^T (MN = output features, K = samples) and H^T (MN = inputs):
             // this sample's column of each, eight features per store
             for (uint32_t c = 0; c < (uint32_t)kHid; c += 8)
-                put8mn(sDZT, c, tid, kTile,
+                put8mn(sDZT, c, r, kTile,
                        make_uint4(pack2(dz[c], dz[c + 1]), pack2(dz[c + 2], dz[c + 3]), pack2(dz[c + 4], dz[c + 5]),
                                   pack2(dz[c + 6], dz[c + 7])));
-            for (uint32_t q = 0; q < Kin / 8; q++)
-                put8mn(l == 0 ? sHT0 : sHT, 8 * q, tid, l == 0 ? (uint32_t)kIn : kBwdHTRows, hv[q]);
-            block_sync_for_mma();
-            if (tid == 0) {
-                // dW (+)= dZ^T (128 x 128 samples) x (H^T, N x 128 samples)^T,
-                // accumulated in tensor memory over the CTA's tiles
-                const uint32_t N = l == 0 ? (uint32_t)kIn : kBwdHTRows;
-                const uint32_t idesc_w = tc::idesc_bf16_f32_mn(128, N);
-                const uint32_t a0 = tc::smem_addr(sDZT), b0 = tc::smem_addr(l == 0 ? sHT0 : sHT);
-                // one K step = 16 samples = two core matrices along K
+            for (uint32_t q = 0; q < Kin / 8; q++) put8mn(sHT, 8 * q, r, Kin, hv[q]);
+            group_sync_for_mma(g);
+            if (r == 0) {
+                // dW += dZ^T (128 x 128 samples) x (H^T, Kin x 128 samples)^T, in
+                // tensor memory across the CTA's tiles; one K step = 16 samples
+                const uint32_t idesc_w = tc::idesc_bf16_f32_mn(128, Kin);
+                const uint32_t a0 = tc::smem_addr(sDZT), b0 = tc::smem_addr(sHT);
                 for (uint32_t ks = 0; ks < (uint32_t)kTile / 16u; ks++)
                     tc::mma_bf16(tmem + bwd_dw_col(l), tc::mnmajor_desc(a0 + ks * 2u * (kTile * 16u), kTile),
-                                 tc::mnmajor_desc(b0 + ks * 2u * (N * 16u), N), idesc_w, (first && ks == 0) ? 0u : 1u);
+                                 tc::mnmajor_desc(b0 + ks * 2u * (Kin * 16u), Kin), idesc_w, 1u);
                 // dH_{l-1} = dZ_l (128 x Nl) x (W_l^T, Kin x Nl)^T
                 if (l > 0) {
                     const uint32_t idesc_h = tc::idesc_bf16_f32(128, Kin);
@@ -452,12 +417,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
                 }
                 tc::mma_commit(bar);
             }
-            alive = wait_layer(bar, phase, status);
+            // while the MMAs run: this thread's share of the bias gradient, the
+            // sums over samples of the dZ^T just stored (rows 0..63)
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const uint4 v = *reinterpret_cast<const uint4*>(sDZT + tc::mnmajor_offset(8u * bq, bk + 16u * j, kTile));
+                const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w4[e]));
+                    bacc[l][2 * e] += f.x;
+                    bacc[l][2 * e + 1] += f.y;
+                }
+            }
+            alive = group_wait_layer(g, bar, phase, status);
             if (!alive) break;
             if (l > 0) {
                 // dZ_{l-1} = dH_{l-1} * relu'(H_{l-1}); H_{l-1} is this layer's input
                 float dh[kHid];
-                for (int c = 0; c < kHid; c += 16) tc::tmem_load16(tc::tmem_at(tmem, warp * 32, dh_col + c), dh + c);
+                for (int c = 0; c < kHid; c += 16) tc::tmem_load16(tc::tmem_at(tmem, lane_base, dh_col + c), dh + c);
                 tc::tmem_wait_ld();
                 for (uint32_t q = 0; q < (uint32_t)kHid / 8; q++) {
                     const uint32_t w4[4] = {hv[q].x, hv[q].y, hv[q].z, hv[q].w};
@@ -469,41 +447,57 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
                 }
             }
             tc::fence_before_sync();
-            __syncthreads();
+            group_sync(g);
             tc::fence_after_sync();
         }
-        first = false;
     }
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
     if (lane == 0u && lsum != 0.0f) atomicAdd(loss, lsum);
-    // flush: this CTA's gradient (weights from tensor memory, lanes 0..63 =
-    // output features; layer 1's bias from shared memory) into its slice
+    // after a time-out, one more bounded wait for this group's MMAs in flight
+    if (!alive) tc::mbar_wait(bar, phase ^ 1u, kWaitLimit);
+    tc::fence_before_sync();
+    const bool all_alive = __syncthreads_and(alive ? 1 : 0) != 0;
+    tc::fence_after_sync();
+    // flush: this CTA's gradient into its slice of the partials.  Bias sums:
+    // the 16 threads of a feature group in each tile group, through shared
+    // memory (the operand tiles are free now)
     float* part = partials + (size_t)blockIdx.x * kNumParams;
-    if (alive && !first) {
+    float* sred = reinterpret_cast<float*>(smem + bwd_dz(0));  // [256 threads][40]
+    if (all_alive) {
+        for (int l = 0; l < 5; l++)
+            for (int j = 0; j < 8; j++) sred[tid * 40 + l * 8 + j] = bacc[l][j];
+        __syncthreads();
+        for (uint32_t i = tid; i < 5u * (uint32_t)kHid; i += kThreads) {
+            const uint32_t l = i / kHid, f = i % kHid, q = f >> 3, j = f & 7u;
+            float sum = 0.0f;
+            for (uint32_t gg = 0; gg < 2; gg++)
+                for (uint32_t k = 0; k < 16; k++) sum += sred[(128u * gg + 16u * q + k) * 40u + l * 8u + j];
+            if (f < (uint32_t)layer_out(l)) part[b_off(l) + f] = sum;
+        }
+        // weights: TMEM lanes 0..63 = output features (warps 0 and 1)
         for (int l = 0; l < 5; l++) {
-            const uint32_t Kin = layer_in(l), cols = l == 0 ? (uint32_t)kIn : kBwdHTRows;
+            const uint32_t Kin = layer_in(l);
             if (warp < 2) {
                 const uint32_t o = warp * 32 + lane;
-                for (uint32_t c = 0; c < cols; c += 16) {
+                for (uint32_t c = 0; c < Kin; c += 16) {
                     float v[16];
                     tc::tmem_load16(tc::tmem_at(tmem, warp * 32, bwd_dw_col(l) + c), v);
                     tc::tmem_wait_ld();
-                    if (o < (uint32_t)layer_out(l)) {
-                        for (int q = 0; q < 16; q++) {
-                            const uint32_t i = c + q;
-                            if (i < Kin) part[w_off(l) + o * Kin + i] = v[q];
-                            else if (i == Kin) part[b_off(l) + o] = v[q];
-                        }
-                    }
+                    if (o < (uint32_t)layer_out(l))
+                        for (int q = 0; q < 16; q++) part[w_off(l) + o * Kin + c + q] = v[q];
                 }
             }
         }
-        __syncthreads();
-        if (tid < (uint32_t)kHid) part[b_off(0) + tid] = sb0[tid];
     } else {
         for (int i = tid; i < kNumParams; i += kThreads) part[i] = 0.0f;
     }
-    release_tmem(bar, phase, alive, tmem, 512);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, 512);
+        tc::tmem_relinquish();
+    }
 }
 
 // grad[i] += the CTAs' partial gradients of parameter i.
@@ -660,7 +654,7 @@ int guide_gradient_device(lmgpu_guide* g, const float* d_queries, const float* d
     k_guide_fwd<MODE_TRAIN><<<fwd_grid_of(n, g->fwd_grid), kFwdThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
                                                                         nullptr, g->d_raw, g->d_acts, g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
-    const unsigned bgrid = tiles_grid(n, g->grid);
+    const unsigned bgrid = fwd_grid_of(n, g->grid);  // two tiles at a time per CTA, as the forward
     k_guide_bwd<<<bgrid, kThreads, kBwdSmem, s>>>(g->params, g->d_raw, g->d_acts, d_dirs, d_weights, (uint32_t)n,
                                                   1.0f / (float)n, g->partials, g->loss, g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());

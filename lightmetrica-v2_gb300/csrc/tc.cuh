@@ -172,6 +172,19 @@ __device__ __forceinline__ void tmem_load16(uint32_t taddr, float v[16])
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// Zeros 32 lanes x 16 columns of tensor memory (the warp's lanes from taddr.lane).
+__device__ __forceinline__ void tmem_store16_zero(uint32_t taddr)
+{
+    const uint32_t z = 0u;
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+        "%1};" ::"r"(taddr),
+        "r"(z)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 // Tensor-memory address of (lane, column).
 __device__ __forceinline__ uint32_t tmem_at(uint32_t base, uint32_t lane, uint32_t col)
 {
