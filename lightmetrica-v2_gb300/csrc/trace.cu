@@ -62,6 +62,11 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(cons
                                                          const uint32_t* __restrict__ d_n)
 {
     __shared__ unsigned long long s_next;
+    // inner-child hit masks permuted by octant (bit s -> bit s ^ o) for all 8
+    // octants and 256 masks: one shared-memory load per node instead of the
+    // three masked swaps (the ALU pipe is the busiest)
+    __shared__ uint8_t s_perm[8 * 256];
+    for (uint32_t i = threadIdx.x; i < 8u * 256u; i += blockDim.x) s_perm[i] = (uint8_t)permute_octant(i & 255u, i >> 8);
     if (d_n) n = *d_n;
     const uint64_t begin = (uint64_t)blockIdx.x * n / gridDim.x;
     const uint64_t end = (uint64_t)(blockIdx.x + 1) * n / gridDim.x;
@@ -152,7 +157,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(cons
                     uint32_t child_base, tri_base, imask, lmask;
                     const uint32_t h8 = intersect_node(lnodes, ni, R, best_t, child_base, tri_base, imask, lmask);
                     if (STATS) node_fetch++;
-                    ng = make_uint2(child_base, (permute_octant(h8 & imask, R.oct_inv) << 24) | imask);
+                    ng = make_uint2(child_base, ((uint32_t)s_perm[(R.oct_inv << 8) | (h8 & imask)] << 24) | imask);
                     tg = make_uint2(tri_base, (h8 & lmask) | (lmask << 8));
                 }
             } else if (sp > 0) {
