@@ -228,29 +228,36 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
     const uint32_t ntiles = (n + kTile - 1) / kTile;
     for (uint32_t tile = 2u * blockIdx.x + g; tile < ntiles && alive; tile += 2u * gridDim.x) {
         const uint32_t row = tile * kTile + r;
-        // features of the row's query, eight at a time
+        // features of the row's query (guide_net.cuh): per axis 16 frequencies
+        // (sin, cos), then the normal and the outgoing direction, then zeros;
+        // stored eight at a time
         {
-            float x[3] = {0.0f, 0.0f, 0.0f}, nn[3] = {0.0f, 0.0f, 0.0f}, wo[3] = {0.0f, 0.0f, 0.0f};
-            if (row < n) {
-                const float* q = queries + 9 * (size_t)row;
-                for (int d = 0; d < 3; d++) {
-                    x[d] = q[d];
-                    nn[d] = q[3 + d];
-                    wo[d] = q[6 + d];
+            float q9[9];
+            for (int j = 0; j < 9; j++) q9[j] = row < n ? queries[9 * (size_t)row + j] : 0.0f;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                float f[32];
+                axis_features((q9[d] - box.lo[d]) * box.inv_ext[d], f);
+                if (row >= n)
+                    for (int j = 0; j < 32; j++) f[j] = 0.0f;
+#pragma unroll
+                for (int g8 = 0; g8 < 4; g8++) {
+                    put8(bufA, r, 32 * d + 8 * g8, kIn, f + 8 * g8);
+                    if (MODE == MODE_TRAIN && row < n)
+                        reinterpret_cast<uint4*>(acts + (size_t)row * kActs)[4 * d + g8] = make_uint4(
+                            pack2(f[8 * g8], f[8 * g8 + 1]), pack2(f[8 * g8 + 2], f[8 * g8 + 3]),
+                            pack2(f[8 * g8 + 4], f[8 * g8 + 5]), pack2(f[8 * g8 + 6], f[8 * g8 + 7]));
                 }
             }
+            float f[8] = {q9[3], q9[4], q9[5], q9[6], q9[7], q9[8], 0.0f, 0.0f};
+            const float z8[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            put8(bufA, r, 96, kIn, f);
 #pragma unroll
-            for (int g8 = 0; g8 < kIn / 8; g8++) {
-                float f[8];
-                if (row < n) {
-                    features8(x, nn, wo, box.lo, box.inv_ext, g8, f);
-                } else {
-                    for (int j = 0; j < 8; j++) f[j] = 0.0f;
-                }
-                put8(bufA, r, 8 * g8, kIn, f);
-                if (MODE == MODE_TRAIN && row < n)
-                    reinterpret_cast<uint4*>(acts + (size_t)row * kActs)[g8] =
-                        make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]), pack2(f[6], f[7]));
+            for (int g8 = 13; g8 < 16; g8++) put8(bufA, r, 8 * g8, kIn, z8);
+            if (MODE == MODE_TRAIN && row < n) {
+                uint4* dst = reinterpret_cast<uint4*>(acts + (size_t)row * kActs);
+                dst[12] = make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]), pack2(f[6], f[7]));
+                for (int g8 = 13; g8 < 16; g8++) dst[g8] = make_uint4(0u, 0u, 0u, 0u);
             }
         }
         group_sync_for_mma(g);
@@ -462,16 +469,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
     // the 16 threads of a feature group in each tile group, through shared
     // memory (the operand tiles are free now)
     float* part = partials + (size_t)blockIdx.x * kNumParams;
-    float* sred = reinterpret_cast<float*>(smem + bwd_dz(0));  // [256 threads][40]
+    float* sred = reinterpret_cast<float*>(smem + bwd_dz(0));  // [256 threads][41] (41: no bank conflicts)
     if (all_alive) {
         for (int l = 0; l < 5; l++)
-            for (int j = 0; j < 8; j++) sred[tid * 40 + l * 8 + j] = bacc[l][j];
+            for (int j = 0; j < 8; j++) sred[tid * 41 + l * 8 + j] = bacc[l][j];
         __syncthreads();
         for (uint32_t i = tid; i < 5u * (uint32_t)kHid; i += kThreads) {
             const uint32_t l = i / kHid, f = i % kHid, q = f >> 3, j = f & 7u;
             float sum = 0.0f;
             for (uint32_t gg = 0; gg < 2; gg++)
-                for (uint32_t k = 0; k < 16; k++) sum += sred[(128u * gg + 16u * q + k) * 40u + l * 8u + j];
+                for (uint32_t k = 0; k < 16; k++) sum += sred[(128u * gg + 16u * q + k) * 41u + l * 8u + j];
             if (f < (uint32_t)layer_out(l)) part[b_off(l) + f] = sum;
         }
         // weights: TMEM lanes 0..63 = output features (warps 0 and 1)

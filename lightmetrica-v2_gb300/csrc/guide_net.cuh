@@ -61,32 +61,22 @@ __host__ __device__ constexpr int b_off(int l)
     return l == 0 ? kOffB1 : l == 1 ? kOffB2 : l == 2 ? kOffB3 : l == 3 ? kOffB4 : kOffB5;
 }
 
-// Input features 8 g .. 8 g + 7 (g = 0..15) of one query (x in world space,
-// its normal n and the outgoing direction wo; scene box [lo, lo + 1 /
-// inv_ext]): groups 0..11 are four frequencies (sin, cos of 2^(k/2) pi u, u
-// the box-normalised coordinate) of axis g / 4, group 12 the normal and the
-// outgoing direction, groups 13..15 zero padding.
-__device__ __forceinline__ void features8(const float x[3], const float n[3], const float wo[3], const float lo[3],
-                                          const float inv_ext[3], int g, float v[8])
+// Position features of one axis, u the box-normalised coordinate: the 32
+// values sin, cos of 2^(k/2) pi u, k = 0..15, in pairs (sin, cos) by k.
+// Two sincospif calls give k = 0 and k = 1; every further octave follows by
+// the double-angle identities sin 2a = 2 sin a cos a, cos 2a = 1 - 2 sin^2 a.
+// Seven doublings amplify an error of the first values by at most 2^7: a few
+// 1e-5 at most, below the rounding of the argument 2^7.5 pi u itself and far
+// below the BF16 rounding of the features.
+__device__ __forceinline__ void axis_features(float u, float f[32])
 {
-    if (g < 12) {
-        const int d = g >> 2;
-        // component d by selects (g may be a run-time value: no local-memory indexing)
-        const float xd = d == 0 ? x[0] : (d == 1 ? x[1] : x[2]);
-        const float lod = d == 0 ? lo[0] : (d == 1 ? lo[1] : lo[2]);
-        const float ied = d == 0 ? inv_ext[0] : (d == 1 ? inv_ext[1] : inv_ext[2]);
-        const float u = (xd - lod) * ied;
-        for (int j = 0; j < 4; j++) {
-            const int k = 4 * (g & 3) + j;
-            const float scale = (float)(1u << (k >> 1)) * ((k & 1) ? 1.41421356237309505f : 1.0f);
-            sincospif(u * scale, &v[2 * j], &v[2 * j + 1]);
-        }
-    } else if (g == 12) {
-        v[0] = n[0]; v[1] = n[1]; v[2] = n[2];
-        v[3] = wo[0]; v[4] = wo[1]; v[5] = wo[2];
-        v[6] = 0.0f; v[7] = 0.0f;
-    } else {
-        for (int j = 0; j < 8; j++) v[j] = 0.0f;
+    sincospif(u, &f[0], &f[1]);
+    sincospif(u * 1.41421356237309505f, &f[2], &f[3]);
+#pragma unroll
+    for (int k = 2; k < 16; k++) {
+        const float s = f[2 * (k - 2)], c = f[2 * (k - 2) + 1];
+        f[2 * k] = 2.0f * s * c;
+        f[2 * k + 1] = fmaf(-2.0f * s, s, 1.0f);
     }
 }
 
