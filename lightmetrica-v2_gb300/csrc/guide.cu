@@ -2,9 +2,9 @@
 // forward, backward and Adam kernels for the MLP of guide_net.cuh, BF16
 // operands with FP32 accumulation in tensor memory.
 //
-// k_guide_fwd   one CTA per SM, persistent over 128-query tiles, as two
+// k_guide_fwd   one CTA per SM, persistent over 128-query tiles, as three
 //               independent groups of 4 warps that work on alternate tiles
-//               (so one group's MMAs overlap the other's feature encoding
+//               (so one group's MMAs overlap the others' feature encoding
 //               and epilogues).  The five weight matrices stay in shared
 //               memory (BF16, K-major canonical layout); a group's tile
 //               activations ping-pong between its two shared-memory buffers;
@@ -52,16 +52,16 @@ constexpr uint32_t kStatusTimeout = 16;
 constexpr uint32_t kWaitLimit = 1u << 24;
 constexpr int kTile = 128;
 constexpr int kThreads = 256;      // backward: two tile groups of 128 threads, one sample each
-constexpr int kFwdThreads = 256;   // forward: two tile groups of 128 threads, one query each
+constexpr int kFwdThreads = 384;   // forward: three tile groups of 128 threads, one query each
 constexpr int kActs = kIn + 4 * kHid;  // stored activations per sample (bf16)
 
 // shared-memory plan of the forward kernel (bytes)
 // W1 (64x128) at 0, W2..W4 (64x64) at 16384 + 8192 (l - 1), W5 (48x64) at 40960
 __host__ __device__ constexpr uint32_t fwd_w(int l) { return l == 0 ? 0u : 16384u + 8192u * (uint32_t)(l - 1); }
-// two tile groups, each with its own activation buffers
+// three tile groups, each with its own activation buffers
 __host__ __device__ constexpr uint32_t fwd_a(uint32_t g) { return 47104u + 49152u * g; }  // 128 x 128 activations
 __host__ __device__ constexpr uint32_t fwd_b(uint32_t g) { return fwd_a(g) + 32768u; }   // 128 x 64 activations
-constexpr uint32_t kFwdBias = fwd_a(2);                        // 304 floats
+constexpr uint32_t kFwdBias = fwd_a(3);                        // 304 floats
 constexpr uint32_t kFwdBar = kFwdBias + 1280;                  // one mbarrier per group, the TMEM address
 constexpr uint32_t kFwdSmem = kFwdBar + 64;
 
@@ -194,11 +194,11 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
     extern __shared__ __align__(1024) unsigned char smem[];
     float* sbias = reinterpret_cast<float*>(smem + kFwdBias);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kFwdBar);
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kFwdBar + 16);
-    // two independent tile groups of 128 threads, one row of a tile each;
-    // group g works on tiles 2 blockIdx.x + g, + 2 gridDim.x, ..., with its
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kFwdBar + 32);
+    // three independent tile groups of 128 threads, one row of a tile each;
+    // group g works on tiles 3 blockIdx.x + g, + 3 gridDim.x, ..., with its
     // own activation buffers, mbarrier and 64 tensor-memory columns, so one
-    // group's MMAs run while the other computes features or an epilogue.  A
+    // group's MMAs run while the others compute features or epilogues.  A
     // warp reads tensor memory lanes 32 (warp % 4) .. + 31, its rows.
     const uint32_t tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, r = tid & (kTile - 1u);
     const uint32_t lane_base = (warp & 3u) * 32u;
@@ -211,9 +211,10 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
     if (tid == 0) {
         tc::mbar_init(bars, 1);
         tc::mbar_init(bars + 1, 1);
+        tc::mbar_init(bars + 2, 1);
         tc::mbar_init_fence();
     }
-    if (warp == 0) tc::tmem_alloc(s_tmem, 128);
+    if (warp == 0) tc::tmem_alloc(s_tmem, 256);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -226,7 +227,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
     bool alive = true;
 
     const uint32_t ntiles = (n + kTile - 1) / kTile;
-    for (uint32_t tile = 2u * blockIdx.x + g; tile < ntiles && alive; tile += 2u * gridDim.x) {
+    for (uint32_t tile = 3u * blockIdx.x + g; tile < ntiles && alive; tile += 3u * gridDim.x) {
         const uint32_t row = tile * kTile + r;
         // features of the row's query (guide_net.cuh): per axis 16 frequencies
         // (sin, cos), then the normal and the outgoing direction, then zeros;
@@ -306,7 +307,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
     __syncthreads();
     if (warp == 0) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(*s_tmem, 128);
+        tc::tmem_dealloc(*s_tmem, 256);
         tc::tmem_relinquish();
     }
 }
@@ -553,7 +554,7 @@ struct lmgpu_guide {
     float* d_w = nullptr;
     __nv_bfloat16* d_acts = nullptr;
     int grid = 0;         // backward: one CTA per SM
-    int fwd_grid = 0;     // forward: one CTA (two tile groups) per SM
+    int fwd_grid = 0;     // forward: one CTA (three tile groups) per SM
     float* partials = nullptr;  // [grid][kNumParams] per-CTA gradients of the backward
 };
 
@@ -606,8 +607,9 @@ unsigned tiles_grid(uint64_t n, int cap)
     return (unsigned)(tiles < (uint64_t)cap ? tiles : (uint64_t)cap);
 }
 
-// Forward CTAs: two tiles at a time each.
-unsigned fwd_grid_of(uint64_t n, int cap) { return tiles_grid((n + kTile - 1) / kTile * (kTile / 2), cap); }
+// Forward CTAs take three tiles at a time, backward CTAs two.
+unsigned fwd_grid_of(uint64_t n, int cap) { return tiles_grid((n + kTile - 1) / kTile * (kTile / 3 + 1), cap); }
+unsigned bwd_grid_of(uint64_t n, int cap) { return tiles_grid((n + kTile - 1) / kTile * (kTile / 2), cap); }
 
 int check_status(lmgpu_guide* g, cudaStream_t s, const char* name)
 {
@@ -661,7 +663,7 @@ int guide_gradient_device(lmgpu_guide* g, const float* d_queries, const float* d
     k_guide_fwd<MODE_TRAIN><<<fwd_grid_of(n, g->fwd_grid), kFwdThreads, kFwdSmem, s>>>(g->params, g->box, d_queries, (uint32_t)n,
                                                                         nullptr, g->d_raw, g->d_acts, g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
-    const unsigned bgrid = fwd_grid_of(n, g->grid);  // two tiles at a time per CTA, as the forward
+    const unsigned bgrid = bwd_grid_of(n, g->grid);
     k_guide_bwd<<<bgrid, kThreads, kBwdSmem, s>>>(g->params, g->d_raw, g->d_acts, d_dirs, d_weights, (uint32_t)n,
                                                   1.0f / (float)n, g->partials, g->loss, g->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
