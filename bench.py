@@ -307,7 +307,10 @@ def run_gpu(args) -> None:
         e2e_value = aggregate_rate(nr * e2e_steps, ws, e2e_s) / 1e6
         peak, peak_src = measured_peak()
         achieved = nr * bytes_per_ray / per_launch_s / 1e9
+        # the committed capture is of the closest-hit kernel; its DRAM bytes
+        # grow with the rays a launch processes
         traffic = traffic_per_launch()
+        traffic = None if (ah or traffic is None) else traffic * nr / N_RAYS
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
@@ -325,7 +328,7 @@ def run_gpu(args) -> None:
                              "tris_per_ray": st["triangle_fetches"] / nr,
                              "note": "algorithmic bytes = 32 B ray + 16 B hit + 80 B per node fetch + 48 B per "
                                      "triangle test; node/triangle fetches are mostly L2 hits",
-                             "l2": l2_figures()},
+                             "l2": None if ah else l2_figures()},
                 "clocks": clk,
                 "accel": {"build_ms": info["build_ms"], "wide_nodes": info["num_wide_nodes"],
                           "binary_depth": info["binary_depth"], "wide_depth": info["wide_depth"],

@@ -50,7 +50,8 @@ constexpr int kTraceBlocksPerSM = 8;
 // BVH tab[ray_scene[i]] (the batch renderer's views).  d_n, when not null,
 // holds the ray count on the device (launches captured in CUDA graphs).
 // SMALL: the same kernel as a separate function whose shared-memory
-// carveout is set to the largest L1, launched for BVHs that fit in L1.
+// carveout is the smallest that holds eight blocks (the largest L1 at full
+// occupancy), launched for BVHs that fit in L1.
 template <bool ANYHIT, bool STATS, bool MULTI, bool SMALL = false>
 __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(const WNode* __restrict__ nodes, const WTri* __restrict__ tris,
                                                          const float4* __restrict__ rays, lmgpu_hit* __restrict__ hits,
@@ -239,12 +240,32 @@ int grid_cap_of()
         int dev = 0, sms = 0, per_sm = 0;
         LMGPU_CUDA_TRY(cudaGetDevice(&dev));
         LMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        if (SMALL)
+        if (SMALL) {
+            // The smallest carveout that still holds kTraceBlocksPerSM blocks
+            // (static shared memory plus the per-block reservation): the
+            // carveout is honoured even where it costs occupancy, and the
+            // 2 KB mask table alone does not fit eight blocks in the
+            // minimum one.
+            cudaFuncAttributes fa{};
+            int smem_sm = 0, reserved = 0;
+            LMGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, k_trace<ANYHIT, STATS, MULTI, SMALL>));
+            LMGPU_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+            LMGPU_CUDA_TRY(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
+            const long need = (long)kTraceBlocksPerSM * ((long)fa.sharedSizeBytes + reserved);
+            const int pct = smem_sm > 0 ? (int)((need * 100 + smem_sm - 1) / smem_sm) : 100;
             LMGPU_CUDA_TRY(cudaFuncSetAttribute(k_trace<ANYHIT, STATS, MULTI, SMALL>,
-                                                cudaFuncAttributePreferredSharedMemoryCarveout,
-                                                (int)cudaSharedmemCarveoutMaxL1));
+                                                cudaFuncAttributePreferredSharedMemoryCarveout, pct < 100 ? pct : 100));
+        }
         LMGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<ANYHIT, STATS, MULTI, SMALL>,
                                                                      kTraceThreads, 0));
+        if (SMALL && per_sm < kTraceBlocksPerSM) {
+            // a carveout that cost occupancy after all: back to the default
+            LMGPU_CUDA_TRY(cudaFuncSetAttribute(k_trace<ANYHIT, STATS, MULTI, SMALL>,
+                                                cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                (int)cudaSharedmemCarveoutDefault));
+            LMGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<ANYHIT, STATS, MULTI, SMALL>,
+                                                                         kTraceThreads, 0));
+        }
         cap = sms * (per_sm > 0 ? per_sm : 1);
     }
     return cap;
@@ -289,8 +310,9 @@ int launch_trace_dn(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hit
 {
     if (max_n == 0) return LMGPU_OK;
     // closest hit in a BVH that fits in L1 (nodes and triangles within 96 KiB)
-    // runs the SMALL instantiation: largest-L1 carveout, measured +4 % on a
-    // 36-triangle scene and -6 % on the 1.5M-triangle ray-cast scene
+    // runs the SMALL instantiation: the smallest shared-memory carveout that
+    // holds eight blocks, i.e. the largest L1 (measured +4 % on a 36-triangle
+    // scene and -6 % on the 1.5M-triangle ray-cast scene)
     const bool small = !anyhit && (uint64_t)a->num_wide * sizeof(WNode) + a->ntri * sizeof(WTri) <= (96u << 10);
     const int grid_cap = small ? grid_cap_of<false, false, false, true>()
                                : (anyhit ? grid_cap_of<true, false, false>() : grid_cap_of<false, false, false>());
