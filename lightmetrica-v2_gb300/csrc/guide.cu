@@ -13,15 +13,19 @@
 //               completed through the group's mbarrier; the feature encoding
 //               and the epilogue (bias, ReLU, BF16 pack) run one row per
 //               thread, reading the row with tcgen05.ld.
-//               MODE_TRAIN also writes every layer's input (BF16) and the raw
-//               outputs to global memory for the backward pass.
+//               MODE_TRAIN also copies every layer's input tile, as the
+//               shared-memory image the MMAs read, to global memory with one
+//               bulk copy per layer, and writes the raw outputs, for the
+//               backward pass.
 // k_guide_bwd   one CTA per SM, persistent over 128-sample tiles, as two
 //               independent groups of 4 warps on alternate tiles: the loss
 //               gradient of the outputs, then for each layer, from the last,
 //               dH = dZ W (M = 128 MMA against W^T kept in shared memory, into
 //               the group's own 64 tensor-memory columns) and dW += dZ^T H,
 //               an M = 128 MMA (dZ^T's 64 rows padded with zeros) over the
-//               tile's 128 samples as K, with dZ^T and H^T MN-major.  The dW
+//               tile's 128 samples as K, with dZ^T and H^T MN-major; H^T is
+//               the forward's stored input tile, brought in by one bulk copy
+//               while the previous layer finishes.  The dW
 //               accumulators (384 columns, zeroed at the start) are shared by
 //               both groups and summed across every tile the CTA processes;
 //               the bias gradients are summed from the dZ^T tiles in registers
@@ -54,6 +58,17 @@ constexpr int kTile = 128;
 constexpr int kThreads = 256;      // backward: two tile groups of 128 threads, one sample each
 constexpr int kFwdThreads = 384;   // forward: three tile groups of 128 threads, one query each
 constexpr int kActs = kIn + 4 * kHid;  // stored activations per sample (bf16)
+// Stored activations of the training forward, tile by tile: the inputs of
+// layers 1..5 of a 128-sample tile as the K-major canonical images the
+// forward multiplies (features 32 KB, then four 16 KB hidden tiles).  The
+// same bytes are the MN-major H^T operands of the backward's weight
+// gradients, so both sides move them with one bulk copy per layer.
+constexpr uint32_t kActTileBytes = (uint32_t)kTile * kActs * 2u;  // 98,304
+__host__ __device__ constexpr uint32_t act_off(int l)
+{
+    return l == 0 ? 0u : (uint32_t)kTile * kIn * 2u + (uint32_t)kTile * kHid * 2u * (uint32_t)(l - 1);
+}
+__host__ __device__ constexpr uint32_t act_bytes(int l) { return (uint32_t)kTile * 2u * (uint32_t)layer_in(l); }
 
 // shared-memory plan of the forward kernel (bytes)
 // W1 (64x128) at 0, W2..W4 (64x64) at 16384 + 8192 (l - 1), W5 (48x64) at 40960
@@ -74,7 +89,7 @@ __host__ __device__ constexpr uint32_t bwd_wt(int l) { return 8192u * (uint32_t)
 __host__ __device__ constexpr uint32_t bwd_dz(uint32_t g) { return 30720u + 81920u * g; }
 __host__ __device__ constexpr uint32_t bwd_dzt(uint32_t g) { return bwd_dz(g) + 16384u; }
 __host__ __device__ constexpr uint32_t bwd_ht(uint32_t g) { return bwd_dzt(g) + 32768u; }
-constexpr uint32_t kBwdBar = bwd_dz(2);        // one mbarrier per group, the TMEM address
+constexpr uint32_t kBwdBar = bwd_dz(2);        // two mbarriers per group (MMAs, bulk loads), the TMEM address
 constexpr uint32_t kBwdSmem = kBwdBar + 64;    // 194,624 bytes: one CTA per SM, holding all 512 TMEM columns
 // tensor-memory columns of the backward kernel: group g's dH at 64 g, layer 1's
 // dW at 128 (128 columns), layer l = 1..4's dW at 256 + 64 (l - 1)
@@ -242,24 +257,13 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
                 if (row >= n)
                     for (int j = 0; j < 32; j++) f[j] = 0.0f;
 #pragma unroll
-                for (int g8 = 0; g8 < 4; g8++) {
-                    put8(bufA, r, 32 * d + 8 * g8, kIn, f + 8 * g8);
-                    if (MODE == MODE_TRAIN && row < n)
-                        reinterpret_cast<uint4*>(acts + (size_t)row * kActs)[4 * d + g8] = make_uint4(
-                            pack2(f[8 * g8], f[8 * g8 + 1]), pack2(f[8 * g8 + 2], f[8 * g8 + 3]),
-                            pack2(f[8 * g8 + 4], f[8 * g8 + 5]), pack2(f[8 * g8 + 6], f[8 * g8 + 7]));
-                }
+                for (int g8 = 0; g8 < 4; g8++) put8(bufA, r, 32 * d + 8 * g8, kIn, f + 8 * g8);
             }
-            float f[8] = {q9[3], q9[4], q9[5], q9[6], q9[7], q9[8], 0.0f, 0.0f};
+            const float f[8] = {q9[3], q9[4], q9[5], q9[6], q9[7], q9[8], 0.0f, 0.0f};
             const float z8[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
             put8(bufA, r, 96, kIn, f);
 #pragma unroll
             for (int g8 = 13; g8 < 16; g8++) put8(bufA, r, 8 * g8, kIn, z8);
-            if (MODE == MODE_TRAIN && row < n) {
-                uint4* dst = reinterpret_cast<uint4*>(acts + (size_t)row * kActs);
-                dst[12] = make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]), pack2(f[6], f[7]));
-                for (int g8 = 13; g8 < 16; g8++) dst[g8] = make_uint4(0u, 0u, 0u, 0u);
-            }
         }
         group_sync_for_mma(g);
 #pragma unroll
@@ -269,7 +273,18 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
             const uint32_t a_in = (l & 1) ? sB : sA;
             unsigned char* out_tile = (l & 1) ? bufA : bufB;
             const uint32_t K = layer_in(l), N = layer_out(l);
-            if (r == 0) issue_layer(tmem, a_in, K, tc::smem_addr(smem + fwd_w(l)), N, bar);
+            if (r == 0) {
+                issue_layer(tmem, a_in, K, tc::smem_addr(smem + fwd_w(l)), N, bar);
+                if (MODE == MODE_TRAIN) {
+                    // the layer's input tile, as it is, to the stored
+                    // activations; its buffer is rewritten only after the
+                    // copy has read it
+                    tc::bulk_store(reinterpret_cast<unsigned char*>(acts) + (size_t)tile * kActTileBytes + act_off(l),
+                                   a_in, act_bytes(l));
+                    tc::bulk_commit();
+                    tc::bulk_wait_read0();
+                }
+            }
             alive = group_wait_layer(g, bar, phase, status);
             if (!alive) break;
             const float* bias = sbias + l * kHid;
@@ -280,12 +295,6 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
                 tc::tmem_wait_ld();
                 for (int c = 0; c < kHid; c++) h[c] = fmaxf(h[c] + bias[c], 0.0f);
                 for (int c = 0; c < kHid; c += 8) put8(out_tile, r, c, kHid, h + c);
-                if (MODE == MODE_TRAIN && row < n) {
-                    uint4* dst = reinterpret_cast<uint4*>(acts + (size_t)row * kActs + kIn + l * kHid);
-                    for (int c = 0; c < kHid; c += 8)
-                        dst[c / 8] = make_uint4(pack2(h[c], h[c + 1]), pack2(h[c + 2], h[c + 3]),
-                                                pack2(h[c + 4], h[c + 5]), pack2(h[c + 6], h[c + 7]));
-                }
             } else {
                 float z[kOut];
 #pragma unroll
@@ -303,6 +312,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
     }
     // after a time-out, one more bounded wait for this group's MMAs in flight
     if (!alive) tc::mbar_wait(bar, phase ^ 1u, kWaitLimit);
+    if (MODE == MODE_TRAIN && r == 0) tc::bulk_wait0();
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
@@ -321,17 +331,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
                                                            float* __restrict__ loss, uint32_t* __restrict__ status)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kBwdBar);
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kBwdBar + 16);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kBwdBar);  // MMA barriers 0, 1; load barriers 2, 3
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kBwdBar + 32);
     // two independent tile groups of 128 threads (one sample each) on
     // alternate tiles; they share the weights and the dW accumulators, and
-    // each has its own operand tiles, dH columns, mbarrier and named barrier
+    // each has its own operand tiles, dH columns, mbarriers and named barrier
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u, g = tid >> 7, r = tid & (kTile - 1u);
     const uint32_t lane_base = (warp & 3u) * 32u;
     unsigned char* sDZ = smem + bwd_dz(g);
     unsigned char* sDZT = smem + bwd_dzt(g);
     unsigned char* sHT = smem + bwd_ht(g);
+    const uint32_t sHTa = tc::smem_addr(sHT);
     uint64_t* bar = bars + g;
+    uint64_t* lbar = bars + 2 + g;  // the bulk loads of H^T
     // W_l^T for l = 2..5 (tile rows = layer inputs, K = layer outputs)
     for (int l = 1; l < 5; l++) load_matrix(smem + bwd_wt(l), params + w_off(l), layer_out(l), layer_in(l), true);
     // dZ^T feature rows 64..127 stay zero (M padding)
@@ -340,8 +352,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
         reinterpret_cast<uint4*>(smem + bwd_dzt(gg))[j] = make_uint4(0u, 0u, 0u, 0u);
     }
     if (tid == 0) {
-        tc::mbar_init(bars, 1);
-        tc::mbar_init(bars + 1, 1);
+        for (int i = 0; i < 4; i++) tc::mbar_init(bars + i, 1);
         tc::mbar_init_fence();
     }
     if (warp == 0) tc::tmem_alloc(s_tmem, 512);
@@ -359,8 +370,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t dh_col = 64u * g;
-    uint32_t phase = 0;
-    bool alive = true;
+    uint32_t phase = 0, lphase = 0;
+    bool alive = true, load_pending = false;
     float lsum = 0.0f;
     // bias-gradient partial sums: thread r adds features 8 q .. 8 q + 7 (q = r / 16)
     // of samples r % 16 + 16 j, j = 0..7, of every tile, per layer
@@ -373,12 +384,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
     for (uint32_t tile = 2u * blockIdx.x + g; tile < ntiles && alive; tile += 2u * gridDim.x) {
         const uint32_t row = tile * kTile + r;
         const bool valid = row < n;
+        const unsigned char* tacts = reinterpret_cast<const unsigned char*>(acts) + (size_t)tile * kActTileBytes;
+        // the last layer's input tile (H_4^T) while the loss gradient is computed
+        if (r == 0) {
+            tc::mbar_arrive_expect_tx(lbar, act_bytes(4));
+            tc::bulk_load(sHTa, tacts + act_off(4), act_bytes(4), lbar);
+        }
+        load_pending = true;
         // dL/dz of the output layer (rows 40..47 and invalid samples are zero)
         float dz[kHid];
         for (int c = 0; c < kHid; c++) dz[c] = 0.0f;
         if (valid) {
             float z[kOutUsed];
-            for (int c = 0; c < kOutUsed; c++) z[c] = raw[(size_t)row * kOutUsed + c];
+            const float4* zr = reinterpret_cast<const float4*>(raw + (size_t)row * kOutUsed);
+            for (int c = 0; c < kOutUsed; c += 4) {
+                const float4 v = zr[c / 4];
+                z[c] = v.x;
+                z[c + 1] = v.y;
+                z[c + 2] = v.z;
+                z[c + 3] = v.w;
+            }
             Lobes L;
             lobes_from_raw(z, L);
             const float w3[3] = {dirs[3 * (size_t)row], dirs[3 * (size_t)row + 1], dirs[3 * (size_t)row + 2]};
@@ -390,31 +415,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
         for (int l = 4; l >= 0; l--) {
             if (!alive) break;
             const uint32_t Nl = layer_out(l), Kin = layer_in(l);
-            // the layer's input activations H_{l-1} of this row (zeros for invalid rows)
-            uint4 hv[kIn / 8];
-            {
-                const uint4* src = reinterpret_cast<const uint4*>(acts + (size_t)(valid ? row : 0) * kActs +
-                                                                  (l == 0 ? 0 : kIn + (l - 1) * kHid));
-                for (uint32_t q = 0; q < Kin / 8; q++) hv[q] = valid ? src[q] : make_uint4(0u, 0u, 0u, 0u);
-            }
             if (l > 0)
                 for (uint32_t c = 0; c < Nl; c += 8) put8(sDZ, r, c, Nl, dz + c);
-            // dZ^T (MN = output features, K = samples) and H^T (MN = inputs):
-            // this sample's column of each, eight features per store
+            // dZ^T (MN = output features, K = samples): this sample's column,
+            // eight features per store
             for (uint32_t c = 0; c < (uint32_t)kHid; c += 8)
                 put8mn(sDZT, c, r, kTile,
                        make_uint4(pack2(dz[c], dz[c + 1]), pack2(dz[c + 2], dz[c + 3]), pack2(dz[c + 4], dz[c + 5]),
                                   pack2(dz[c + 6], dz[c + 7])));
-            for (uint32_t q = 0; q < Kin / 8; q++) put8mn(sHT, 8 * q, r, Kin, hv[q]);
-            group_sync_for_mma(g);
+            // the layer's input H^T (MN = inputs, K = samples) has arrived
+            const bool loaded = tc::mbar_wait(lbar, lphase, kWaitLimit);
+            if (loaded) {
+                lphase ^= 1u;
+                load_pending = false;
+            }
+            tc::fence_smem_async();
+            tc::fence_before_sync();
+            const bool ok = group_sync_and(g, loaded);
+            tc::fence_after_sync();
+            if (!ok) {
+                if (r == 0) atomicOr(status, kStatusTimeout);
+                alive = false;
+                break;
+            }
             if (r == 0) {
                 // dW += dZ^T (128 x 128 samples) x (H^T, Kin x 128 samples)^T, in
                 // tensor memory across the CTA's tiles; one K step = 16 samples
                 const uint32_t idesc_w = tc::idesc_bf16_f32_mn(128, Kin);
-                const uint32_t a0 = tc::smem_addr(sDZT), b0 = tc::smem_addr(sHT);
+                const uint32_t a0 = tc::smem_addr(sDZT);
                 for (uint32_t ks = 0; ks < (uint32_t)kTile / 16u; ks++)
                     tc::mma_bf16(tmem + bwd_dw_col(l), tc::mnmajor_desc(a0 + ks * 2u * (kTile * 16u), kTile),
-                                 tc::mnmajor_desc(b0 + ks * 2u * (Kin * 16u), Kin), idesc_w, 1u);
+                                 tc::mnmajor_desc(sHTa + ks * 2u * (Kin * 16u), Kin), idesc_w, 1u);
                 // dH_{l-1} = dZ_l (128 x Nl) x (W_l^T, Kin x Nl)^T
                 if (l > 0) {
                     const uint32_t idesc_h = tc::idesc_bf16_f32(128, Kin);
@@ -426,7 +457,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
                 tc::mma_commit(bar);
             }
             // while the MMAs run: this thread's share of the bias gradient, the
-            // sums over samples of the dZ^T just stored (rows 0..63)
+            // sums over samples of the dZ^T just stored (rows 0..63), and the
+            // sample's own input row (the ReLU mask of dZ_{l-1})
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const uint4 v = *reinterpret_cast<const uint4*>(sDZT + tc::mnmajor_offset(8u * bq, bk + 16u * j, kTile));
@@ -438,9 +470,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
                     bacc[l][2 * e + 1] += f.y;
                 }
             }
+            uint4 hv[kHid / 8];
+            if (l > 0) {
+                for (uint32_t q = 0; q < (uint32_t)kHid / 8; q++)
+                    hv[q] = *reinterpret_cast<const uint4*>(sHT + tc::kmajor_offset(r, 8u * q, Kin));
+                // these reads come before the next bulk load rewrites H^T
+                tc::fence_smem_async();
+            }
             alive = group_wait_layer(g, bar, phase, status);
             if (!alive) break;
             if (l > 0) {
+                // the next layer's input tile, while dZ_{l-1} is formed
+                if (r == 0) {
+                    tc::mbar_arrive_expect_tx(lbar, act_bytes(l - 1));
+                    tc::bulk_load(sHTa, tacts + act_off(l - 1), act_bytes(l - 1), lbar);
+                }
+                load_pending = true;
                 // dZ_{l-1} = dH_{l-1} * relu'(H_{l-1}); H_{l-1} is this layer's input
                 float dh[kHid];
                 for (int c = 0; c < kHid; c += 16) tc::tmem_load16(tc::tmem_at(tmem, lane_base, dh_col + c), dh + c);
@@ -461,8 +506,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
     }
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
     if (lane == 0u && lsum != 0.0f) atomicAdd(loss, lsum);
-    // after a time-out, one more bounded wait for this group's MMAs in flight
-    if (!alive) tc::mbar_wait(bar, phase ^ 1u, kWaitLimit);
+    // after a time-out, one more bounded wait for this group's MMAs and its
+    // bulk load in flight
+    if (!alive) {
+        tc::mbar_wait(bar, phase ^ 1u, kWaitLimit);
+        if (load_pending) tc::mbar_wait(lbar, lphase, kWaitLimit);
+    }
     tc::fence_before_sync();
     const bool all_alive = __syncthreads_and(alive ? 1 : 0) != 0;
     tc::fence_after_sync();
@@ -574,7 +623,7 @@ int ensure_scratch(lmgpu_guide* g, uint64_t n)
         cudaMalloc(&g->d_raw, sizeof(float) * kOutUsed * n) != cudaSuccess ||
         cudaMalloc(&g->d_dir, sizeof(float) * 3 * n) != cudaSuccess ||
         cudaMalloc(&g->d_w, sizeof(float) * n) != cudaSuccess ||
-        cudaMalloc(&g->d_acts, sizeof(__nv_bfloat16) * kActs * n) != cudaSuccess) {
+        cudaMalloc(&g->d_acts, (size_t)kActTileBytes * ((n + kTile - 1) / kTile)) != cudaSuccess) {
         set_error("lmgpu_guide: scratch allocation failed");
         return LMGPU_ERR_CUDA;
     }

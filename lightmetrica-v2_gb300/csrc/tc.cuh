@@ -155,6 +155,36 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint3
     return false;
 }
 
+// Bulk (untiled TMA) copies.  Addresses 16-byte aligned, sizes multiples of
+// 16 bytes.
+// Shared -> global, tracked by bulk groups of the issuing thread.
+__device__ __forceinline__ void bulk_store(void* gdst, uint32_t ssrc, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(ssrc), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// Until this thread's committed bulk stores have read their shared sources.
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// Until they have completed.
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// One arrival on the mbarrier that also expects `bytes` of bulk-copy
+// transactions in the current phase.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bytes)
+                 : "memory");
+}
+
+// Global -> shared (this CTA), completing `bytes` of transactions on the mbarrier.
+__device__ __forceinline__ void bulk_load(uint32_t sdst, const void* gsrc, uint32_t bytes, uint64_t* mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(sdst),
+                 "l"(gsrc), "r"(bytes), "r"(smem_addr(mbar))
+                 : "memory");
+}
+
 // 32 lanes x 16 columns of fp32 from tensor memory: thread i of the warp gets
 // lane (taddr.lane + i), columns [taddr.col, taddr.col + 16).
 __device__ __forceinline__ void tmem_load16(uint32_t taddr, float v[16])
