@@ -473,6 +473,42 @@ RENDER_WORKLOADS = {
 }
 
 
+def render_trace_roofline(sc, render, step_ms: float, flush) -> dict:
+    """Roofline of a render's dominant kernel, its traversal launches: one
+    render (seed of the first timed step) with the counting traversal for
+    rays, node and triangle fetches, then the same render with CUDA events
+    around each production traversal launch (the library's trace profile),
+    L2 flushed before each.  achieved = algorithmic bytes of those launches
+    (32 B ray + 16 B hit + 80 B per node fetch + 48 B per triangle test) /
+    their summed device time."""
+    import lmgpu
+
+    sc.set_trace_profile(lmgpu.TRACE_PROFILE_COUNT)
+    flush.fill_(1.0)
+    render(1000)
+    cnt = sc.read_trace_profile()
+    sc.set_trace_profile(lmgpu.TRACE_PROFILE_TIME)
+    flush.fill_(2.0)
+    render(1000)
+    tim = sc.read_trace_profile()
+    sc.set_trace_profile(lmgpu.TRACE_PROFILE_OFF)
+    if cnt["rays"] == 0 or tim["timed_launches"] == 0 or tim["timed_launches"] != tim["launches"]:
+        return None
+    nbytes = (cnt["rays"] * (RAY_BYTES + HIT_BYTES) + cnt["node_fetches"] * NODE_BYTES
+              + cnt["triangle_fetches"] * TRI_BYTES)
+    achieved = nbytes / (tim["device_ms"] * 1e-3) / 1e9
+    peak, peak_src = measured_peak()
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "peak_source": peak_src, "kernel": "k_trace (the render's traversal launches)",
+            "launches_per_step": tim["launches"], "rays_per_step": cnt["rays"],
+            "bytes_per_ray": nbytes / cnt["rays"], "nodes_per_ray": cnt["node_fetches"] / cnt["rays"],
+            "tris_per_ray": cnt["triangle_fetches"] / cnt["rays"], "trace_ms_per_step": tim["device_ms"],
+            "share_of_step": tim["device_ms"] / step_ms,
+            "note": "algorithmic bytes = 32 B ray + 16 B hit + 80 B per node fetch + 48 B per triangle test over "
+                    "the summed device time of the render's traversal launches (CUDA events); a BVH that fits "
+                    "in L1 serves most node and triangle fetches from L1"}
+
+
 def run_render(args) -> None:
     """Rendering configurations (renderer::pt, renderer::bdpt, renderer::ltdirect).  Metric
     Msamples/s; value = film left on the device (lmgpu_render_*_device),
@@ -515,6 +551,10 @@ def run_render(args) -> None:
     clk = clocks.stop()
     launches = sc.launch_count() - l0
     ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    with torch.cuda.stream(stream):
+        roofline = render_trace_roofline(
+            sc, lambda seed: render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, seed, stream.cuda_stream), ms,
+            flush)
     t0 = time.perf_counter()
     for k in range(args.steps):
         render_host(spp, max_nv, 2000 + k)
@@ -529,7 +569,7 @@ def run_render(args) -> None:
                        "l2": "flushed before every timed step (256 MiB write, untimed)"},
             "e2e": {"value": samples / e2e_s / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": W * H * 3 * 4 * 2, "api": f"lmgpu_render_{cfg['renderer']} (host film)"},
-            "gpu_launches": launches, "clocks": clk}
+            "gpu_launches": launches, "clocks": clk, "roofline": roofline}
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import lmoracle

@@ -226,6 +226,31 @@ int lmgpu_scene_launch_count(const lmgpu_scene* scene, uint64_t* count);
 /* The scene's accel (owned by the scene), for ray queries on its triangles. */
 int lmgpu_scene_accel(const lmgpu_scene* scene, const lmgpu_accel** accel);
 
+/* Instrumentation of the traversal launches of this scene's renders, the
+ * dominant kernel of every renderer (a diagnostic; no counterpart in the
+ * reference).  Images are unchanged in every mode. */
+enum {
+    LMGPU_TRACE_PROFILE_OFF = 0,
+    LMGPU_TRACE_PROFILE_COUNT = 1, /* launch the counting traversal: rays, node and triangle fetches, hits */
+    LMGPU_TRACE_PROFILE_TIME = 2   /* the production traversal, device time of each launch (CUDA events) */
+};
+typedef struct {
+    uint64_t launches;         /* traversal launches since the last read */
+    uint64_t rays;             /* COUNT: rays traced */
+    uint64_t node_fetches;     /* COUNT: 80-byte node fetches */
+    uint64_t triangle_fetches; /* COUNT: 48-byte triangle tests */
+    uint64_t hits;             /* COUNT: rays that hit */
+    double device_ms;          /* TIME: summed device time of the timed launches */
+    uint64_t timed_launches;   /* TIME: launches inside device_ms (at most 4,096 between reads) */
+} lmgpu_trace_profile;
+
+/* Selects the mode and clears the record. */
+int lmgpu_scene_set_trace_profile(lmgpu_scene* scene, int mode);
+
+/* Waits for the device, returns the record since the last read or mode
+ * change and clears it. */
+int lmgpu_scene_read_trace_profile(lmgpu_scene* scene, lmgpu_trace_profile* out);
+
 /* Renders the scene with the wavefront path tracer and writes the film
  * (height x width x 3 floats, row = raster y from the bottom, as
  * film_hdr.cpp:218-223 indexes it) and, if variance is not NULL, the

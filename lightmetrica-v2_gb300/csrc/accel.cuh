@@ -6,6 +6,7 @@
 
 #include <atomic>
 #include <mutex>
+#include <vector>
 
 namespace lmgpu {
 // Tuning knobs of the traversal kernel (see trace.cu): lanes idle before a
@@ -75,10 +76,27 @@ int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t s
 int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, uint64_t n, bool anyhit,
                  bool stats, cudaStream_t stream);
 
+// Instrumentation of a renderer's traversal launches (the dominant kernel of
+// every wavefront renderer), off unless a scene asks for it.
+//   kProbeCount: launches take the counting instantiation, which adds rays,
+//                node fetches, triangle fetches and hits into d_counters;
+//   kProbeTime:  the production kernel, with a CUDA event pair recorded
+//                around each launch (up to kMaxEvents / 2 launches).
+struct TraceProbe {
+    static constexpr int kOff = 0, kProbeCount = 1, kProbeTime = 2;
+    static constexpr size_t kMaxEvents = 8192;
+    int mode = kOff;
+    unsigned long long* d_counters = nullptr;  // [4], device
+    std::vector<cudaEvent_t> events;
+    size_t used = 0;           // events recorded since the last read
+    uint64_t launches = 0;     // traversal launches since the last read
+    bool overflow = false;     // more launches than event pairs
+};
+
 // As launch_trace with the ray count read from d_n on the device (at most
-// max_n), so that launches need no host round trip.
+// max_n), so that launches need no host round trip.  probe: see TraceProbe.
 int launch_trace_dn(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, const uint32_t* d_n,
-                    uint64_t max_n, bool anyhit, cudaStream_t stream);
+                    uint64_t max_n, bool anyhit, cudaStream_t stream, TraceProbe* probe = nullptr);
 
 // Blocks of the persistent traversal grid (SMs x resident blocks); looked up
 // once per process.  Negative on a CUDA error.

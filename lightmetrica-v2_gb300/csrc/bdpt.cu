@@ -822,8 +822,9 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
         sc->launches++;
         int cur = 0;
         for (int k = 1; k < C.max_v; k++) {
-            if ((rc = launch_trace_dn(sc->accel, B.ext[cur], B.ext_hit, qn + cur, 2ull * w.n, false, stream)) ||
-                (rc = launch_trace_dn(sc->accel, B.sh, B.sh_hit, qn + cur, 2ull * w.n, true, stream)))
+            if ((rc = launch_trace_dn(sc->accel, B.ext[cur], B.ext_hit, qn + cur, 2ull * w.n, false, stream,
+                                      sc->probe)) ||
+                (rc = launch_trace_dn(sc->accel, B.sh, B.sh_hit, qn + cur, 2ull * w.n, true, stream, sc->probe)))
                 return rc;
             LMGPU_CUDA_TRY(cudaMemsetAsync(qn + (1 - cur), 0, sizeof(uint32_t), stream));
             k_bd_step<<<blocks(2ull * w.n, kBdptThreads), kBdptThreads, 0, stream>>>(

@@ -464,7 +464,8 @@ int render_pt_guided(lmgpu_scene* sc, lmgpu_guide* guide, const lmgpu_pt_params*
         sc->launches++;
         int cur = 0;
         for (int b = 0; b < maxb; b++) {
-            if ((rc = launch_trace_dn(sc->accel, sc->q_ray[cur], sc->q_hit, G.counts + cur, w.n, false, stream)))
+            if ((rc = launch_trace_dn(sc->accel, sc->q_ray[cur], sc->q_hit, G.counts + cur, w.n, false, stream,
+                                      sc->probe)))
                 return rc;
             LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts + (1 - cur), 0, sizeof(uint32_t), stream));
             LMGPU_CUDA_TRY(cudaMemsetAsync(G.counts + 2, 0, sizeof(uint32_t), stream));

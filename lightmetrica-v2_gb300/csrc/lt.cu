@@ -251,14 +251,14 @@ int render_ltdirect(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image,
         int cur = 0;
         for (int b = 0;; b++) {
             // the sensor connections of the previous kernel
-            rc = launch_trace_dn(sc->accel, sc->q_nray, sc->q_nhit, cnt + 2, n_wave, true, stream);
+            rc = launch_trace_dn(sc->accel, sc->q_nray, sc->q_nhit, cnt + 2, n_wave, true, stream, sc->probe);
             if (rc) return rc;
             k_lt_splat<<<gblocks, kLtThreads, 0, stream>>>(cnt + 2, sc->q_nrec, sc->q_nhit, sc->film_x,
                                                            sc->film_x_sq);
             LMGPU_CUDA_TRY(cudaGetLastError());
             sc->launches += 2;
             if (b >= maxb) break;
-            rc = launch_trace_dn(sc->accel, sc->q_ray[cur], sc->q_hit, cnt + cur, n_wave, false, stream);
+            rc = launch_trace_dn(sc->accel, sc->q_ray[cur], sc->q_hit, cnt + cur, n_wave, false, stream, sc->probe);
             if (rc) return rc;
             LMGPU_CUDA_TRY(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(uint32_t), stream));
             LMGPU_CUDA_TRY(cudaMemsetAsync(cnt + 2, 0, sizeof(uint32_t), stream));

@@ -368,7 +368,7 @@ int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float
         for (int b = 0;; b++) {
             if (nee) {
                 // the light samples of the previous kernel
-                rc = launch_trace_dn(sc->accel, sc->q_nray, sc->q_nhit, cnt + 2, n_wave, true, stream);
+                rc = launch_trace_dn(sc->accel, sc->q_nray, sc->q_nhit, cnt + 2, n_wave, true, stream, sc->probe);
                 if (rc) return rc;
                 k_pt_nee_splat<<<gblocks, kShadeThreads, 0, stream>>>(p0, np, cnt + 2, sc->q_nrec, sc->q_npath,
                                                                       sc->q_nhit, sc->q_own, sc->film_x,
@@ -377,7 +377,7 @@ int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float
                 sc->launches += 2;
             }
             if (b >= maxb) break;
-            rc = launch_trace_dn(sc->accel, sc->q_ray[cur], sc->q_hit, cnt + cur, n_wave, false, stream);
+            rc = launch_trace_dn(sc->accel, sc->q_ray[cur], sc->q_hit, cnt + cur, n_wave, false, stream, sc->probe);
             if (rc) return rc;
             LMGPU_CUDA_TRY(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(uint32_t), stream));
             LMGPU_CUDA_TRY(cudaMemsetAsync(cnt + 2, 0, sizeof(uint32_t), stream));

@@ -118,11 +118,14 @@ struct lmgpu_scene {
     int bdpt_mis = 0;  // MIS weight of the render in progress (LMGPU_MIS_*)      // buffers of the bidirectional renderer
     lmgpu::GuidedState* guided = nullptr;  // buffers of the guided renderer
     lmgpu::VcmState* vcm = nullptr;        // buffers of the VCM renderer
+    lmgpu::TraceProbe* probe = nullptr;    // traversal instrumentation (lmgpu_scene_set_trace_profile)
 };
 
 namespace lmgpu {
 
 int ensure_film(lmgpu_scene* sc, uint64_t npix);
+// Frees a traversal probe and its events (NULL is ignored).
+void free_probe(TraceProbe* p);
 int ensure_queues(lmgpu_scene* sc, uint64_t n);
 SceneGPU scene_view(const lmgpu_scene* sc);
 int clear_film(lmgpu_scene* sc, uint64_t npix, cudaStream_t stream);

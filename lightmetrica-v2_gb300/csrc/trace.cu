@@ -306,9 +306,27 @@ int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, 
 }
 
 int launch_trace_dn(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, const uint32_t* d_n,
-                    uint64_t max_n, bool anyhit, cudaStream_t stream)
+                    uint64_t max_n, bool anyhit, cudaStream_t stream, TraceProbe* probe)
 {
     if (max_n == 0) return LMGPU_OK;
+    if (probe && probe->mode != TraceProbe::kOff) probe->launches++;
+    if (probe && probe->mode == TraceProbe::kProbeCount) {
+        // the counting instantiation: the same hits, plus fetch counters
+        const int cap = anyhit ? grid_cap_of<true, true, false>() : grid_cap_of<false, true, false>();
+        if (cap <= 0) return LMGPU_ERR_CUDA;
+        const uint64_t by_rays = (max_n + 4 * kTraceThreads - 1) / (4 * kTraceThreads);
+        const unsigned grid = (unsigned)(by_rays < (uint64_t)cap ? by_rays : (uint64_t)cap);
+        auto k = anyhit ? k_trace<true, true, false> : k_trace<false, true, false>;
+        k<<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, max_n,
+                                              a->ntri > 0 ? (uint32_t)a->num_wide : 0u, (uint32_t)a->ntri,
+                                              a->tune.refill, a->tune.postpone, a->status, probe->d_counters,
+                                              nullptr, 0u, nullptr, d_n);
+        LMGPU_CUDA_TRY(cudaGetLastError());
+        return LMGPU_OK;
+    }
+    const bool timed = probe && probe->mode == TraceProbe::kProbeTime && probe->used + 2 <= probe->events.size();
+    if (probe && probe->mode == TraceProbe::kProbeTime && !timed) probe->overflow = true;
+    if (timed) LMGPU_CUDA_TRY(cudaEventRecord(probe->events[probe->used], stream));
     // closest hit in a BVH that fits in L1 (nodes and triangles within 96 KiB)
     // runs the SMALL instantiation: the smallest shared-memory carveout that
     // holds eight blocks, i.e. the largest L1 (measured +4 % on a 36-triangle
@@ -325,6 +343,10 @@ int launch_trace_dn(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hit
     k<<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, max_n, nn, nt, a->tune.refill,
                                           a->tune.postpone, a->status, nullptr, nullptr, 0u, nullptr, d_n);
     LMGPU_CUDA_TRY(cudaGetLastError());
+    if (timed) {
+        LMGPU_CUDA_TRY(cudaEventRecord(probe->events[probe->used + 1], stream));
+        probe->used += 2;
+    }
     return LMGPU_OK;
 }
 

@@ -978,7 +978,7 @@ int trace_subpaths(lmgpu_scene* sc, VcmState& V, const Ctx& C, const Pass& X, co
     sc->launches++;
     int cur = 0;
     for (int k = 1; k < C.max_v; k++) {
-        int rc = launch_trace_dn(sc->accel, V.rays[cur], V.hits, V.counter + cur, total, false, stream);
+        int rc = launch_trace_dn(sc->accel, V.rays[cur], V.hits, V.counter + cur, total, false, stream, sc->probe);
         if (rc) return rc;
         LMGPU_CUDA_TRY(cudaMemsetAsync(V.counter + (1 - cur), 0, sizeof(uint32_t), stream));
         k_vc_step<<<blocks(total, kVcThreads), kVcThreads, 0, stream>>>(
@@ -1124,7 +1124,8 @@ int render_vcm(lmgpu_scene* sc, const lmgpu_vcm_params* prm, float* d_image, flo
                 k_vc_connect<<<blocks(max_items, kVcThreads), kVcThreads, 0, stream>>>(C, X, eL, eE, V.items,
                                                                                        V.counter + 2, V.c_rays, V.c_rec);
                 LMGPU_CUDA_TRY(cudaGetLastError());
-                if ((rc = launch_trace_dn(sc->accel, V.c_rays, V.c_hit, V.counter + 2, max_items, true, stream)))
+                if ((rc = launch_trace_dn(sc->accel, V.c_rays, V.c_hit, V.counter + 2, max_items, true, stream,
+                                          sc->probe)))
                     return rc;
                 k_vc_csplat<<<blocks(max_items, 256), 256, 0, stream>>>(V.items, V.counter + 2, V.c_rec, V.c_hit,
                                                                         V.own_pix, V.own, sc->film_x, sc->film_x_sq);

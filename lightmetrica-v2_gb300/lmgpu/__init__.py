@@ -50,6 +50,25 @@ class AccelInfo(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class TraceProfile(ctypes.Structure):
+    """lmgpu_trace_profile: a scene's traversal launches since the last read."""
+    _fields_ = [
+        ("launches", ctypes.c_uint64),
+        ("rays", ctypes.c_uint64),
+        ("node_fetches", ctypes.c_uint64),
+        ("triangle_fetches", ctypes.c_uint64),
+        ("hits", ctypes.c_uint64),
+        ("device_ms", ctypes.c_double),
+        ("timed_launches", ctypes.c_uint64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+TRACE_PROFILE_OFF, TRACE_PROFILE_COUNT, TRACE_PROFILE_TIME = 0, 1, 2
+
+
 class TraceStats(ctypes.Structure):
     _fields_ = [
         ("rays", ctypes.c_uint64),
@@ -134,6 +153,8 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_render_ptdirect_device.argtypes = [vp, vp, vp, vp, vp]
     L.lmgpu_render_ptmis_device.argtypes = [vp, vp, vp, vp, vp]
     L.lmgpu_scene_launch_count.argtypes = [vp, ctypes.POINTER(u64)]
+    L.lmgpu_scene_set_trace_profile.argtypes = [vp, ctypes.c_int]
+    L.lmgpu_scene_read_trace_profile.argtypes = [vp, ctypes.POINTER(TraceProfile)]
     L.lmgpu_render_bdpt_device.argtypes = [vp, vp, vp, vp, vp]
     for name in ("lmgpu_accel_create", "lmgpu_accel_build", "lmgpu_accel_build_device", "lmgpu_accel_get_info",
                  "lmgpu_trace", "lmgpu_trace_device", "lmgpu_trace_stats_device", "lmgpu_accel_check",
@@ -151,7 +172,8 @@ def lib() -> ctypes.CDLL:
                  "lmgpu_flatten_meshes_device", "lmgpu_accel_build_meshes",
                  "lmgpu_render_vcm_device",
                  "lmgpu_accel_set_attributes", "lmgpu_surface", "lmgpu_surface_device",
-                 "lmgpu_scene_set_environment"):
+                 "lmgpu_scene_set_environment", "lmgpu_scene_set_trace_profile",
+                 "lmgpu_scene_read_trace_profile"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -455,6 +477,17 @@ class Scene:
         n = ctypes.c_uint64()
         _check(lib().lmgpu_scene_launch_count(self._h, ctypes.byref(n)))
         return n.value
+
+    def set_trace_profile(self, mode: int) -> None:
+        """Instruments the traversal launches of later renders: TRACE_PROFILE_COUNT
+        (fetch counters), TRACE_PROFILE_TIME (device time per launch) or _OFF."""
+        _check(lib().lmgpu_scene_set_trace_profile(self._h, mode))
+
+    def read_trace_profile(self) -> dict:
+        """The record since the last read or mode change (waits for the device)."""
+        r = TraceProfile()
+        _check(lib().lmgpu_scene_read_trace_profile(self._h, ctypes.byref(r)))
+        return r.as_dict()
 
     def render_bdpt(self, spp: int, max_num_vertices: int = -1, seed: int = 0,
                     mis: str = "powerheuristics", min_num_vertices: int = 0) -> tuple[np.ndarray, np.ndarray]:
