@@ -297,6 +297,7 @@ def run_gpu(args) -> None:
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     barrier()
+    single = single_ray_latency(acc, rays, ah) if rank == 0 else None
 
     # the slowest rank's times; the rate covers all ranks' rays
     ms, e2e_s = max_over_ranks([ms, e2e_s], device="cuda")
@@ -332,7 +333,8 @@ def run_gpu(args) -> None:
                 "clocks": clk,
                 "accel": {"build_ms": info["build_ms"], "wide_nodes": info["num_wide_nodes"],
                           "binary_depth": info["binary_depth"], "wide_depth": info["wide_depth"],
-                          "hit_fraction": st["hits"] / nr}}
+                          "hit_fraction": st["hits"] / nr},
+                "single_ray": single}
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
             cb = CpuReference(tris, threads).time_sample(rays, 15.0)
@@ -473,6 +475,26 @@ RENDER_WORKLOADS = {
 }
 
 
+def single_ray_latency(acc, rays, anyhit: bool, calls: int = 2000) -> dict:
+    """Latency of the single-ray path a stock CPU renderer takes through
+    accel::cuda's Accel3::Intersect: lmgpu_trace with n = 1 from pageable host
+    memory, a new ray per call (wall clock around each call from Python, so
+    about a microsecond of ctypes overhead is included)."""
+    warm = 50
+    r = np.ascontiguousarray(rays[:calls + warm])
+    hit = np.empty(4, np.float32)
+    for i in range(warm):
+        acc.trace_ptr(r[i].ctypes.data, hit.ctypes.data, 1, anyhit)
+    ts = np.empty(calls)
+    for i in range(calls):
+        t0 = time.perf_counter()
+        acc.trace_ptr(r[warm + i].ctypes.data, hit.ctypes.data, 1, anyhit)
+        ts[i] = time.perf_counter() - t0
+    return {"us_median": float(np.median(ts) * 1e6), "us_mean": float(ts.mean() * 1e6),
+            "Mrays_s_one_caller": float(1.0 / ts.mean() / 1e6), "calls": calls,
+            "api": "lmgpu_trace with n = 1, pageable host buffers (accel::cuda's Accel3::Intersect)"}
+
+
 def render_trace_roofline(sc, render, step_ms: float, flush) -> dict:
     """Roofline of a render's dominant kernel, its traversal launches: one
     render (seed of the first timed step) with the counting traversal for
@@ -513,11 +535,28 @@ def run_render(args) -> None:
     """Rendering configurations (renderer::pt, renderer::bdpt, renderer::ltdirect).  Metric
     Msamples/s; value = film left on the device (lmgpu_render_*_device),
     e2e = the host-pointer lmgpu_render_* (film and variance copied back
-    every step)."""
+    every step).  Under torchrun every rank renders its own sample set of the
+    view (seeds from rank_seed, weak scaling); the e2e step ends with the film
+    sum of all ranks (reduce_film), and the rate covers all ranks' samples
+    over the slowest rank's time."""
     import torch
 
     import lmgpu
     from lmgpu import scenes
+    from lmgpu.dist import rank_seed, reduce_film
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
 
     cfg = RENDER_WORKLOADS[args.workload]
     W, H, spp, max_nv = cfg["width"], cfg["height"], cfg["spp"], cfg["max_num_vertices"]
@@ -532,12 +571,13 @@ def run_render(args) -> None:
     dv = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
     samples = W * H * spp
     for k in range(args.warmup):
-        render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, k, stream.cuda_stream)
+        render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, rank_seed(k, rank), stream.cuda_stream)
     torch.cuda.synchronize()
     # each step timed alone with events on the render stream; L2 flushed
     # (a 256 MiB write, untimed) before every step
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
-    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks = ClockSampler(local)
+    barrier()
     clocks.start()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     l0 = sc.launch_count()
@@ -545,30 +585,45 @@ def run_render(args) -> None:
         for k in range(args.steps):
             flush.fill_(float(k))
             evs[k][0].record(stream)
-            render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, 1000 + k, stream.cuda_stream)
+            render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, rank_seed(1000 + k, rank), stream.cuda_stream)
             evs[k][1].record(stream)
     torch.cuda.synchronize()
+    barrier()
     clk = clocks.stop()
     launches = sc.launch_count() - l0
     ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
-    with torch.cuda.stream(stream):
-        roofline = render_trace_roofline(
-            sc, lambda seed: render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, seed, stream.cuda_stream), ms,
-            flush)
+    roofline = None
+    if rank == 0:
+        with torch.cuda.stream(stream):
+            roofline = render_trace_roofline(
+                sc, lambda seed: render_dev(di.data_ptr(), dv.data_ptr(), spp, max_nv, seed, stream.cuda_stream),
+                ms, flush)
+    barrier()
     t0 = time.perf_counter()
     for k in range(args.steps):
-        render_host(spp, max_nv, 2000 + k)
+        img, var = render_host(spp, max_nv, rank_seed(2000 + k, rank))
+        reduce_film(img, var, spp, device="cuda")
     e2e_s = (time.perf_counter() - t0) / args.steps
+    barrier()
+    ms, e2e_s = max_over_ranks([ms, e2e_s], device="cuda")
+    if rank != 0:
+        sc.close()
+        return
     ntri = int(sum(p["tris"].shape[0] for p in scene["prims"]))
-    line = {"metric": f"Msamples/s (renderer::{cfg['renderer']})", "value": samples / ms / 1e3,
-            "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+    line = {"metric": f"Msamples/s (renderer::{cfg['renderer']})",
+            "value": aggregate_rate(samples, ws, ms * 1e-3) / 1e6,
+            "unit": "Msamples/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": cfg["data"],
             "config": {"workload": cfg["workload"] if spp == cfg["spp"] else f"{cfg['workload']} at {spp} spp",
                        "width": W, "height": H, "spp": spp,
                        "max_num_vertices": max_nv, "triangles": ntri,
-                       "l2": "flushed before every timed step (256 MiB write, untimed)"},
-            "e2e": {"value": samples / e2e_s / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": W * H * 3 * 4 * 2, "api": f"lmgpu_render_{cfg['renderer']} (host film)"},
+                       "l2": "flushed before every timed step (256 MiB write, untimed)",
+                       "parallelism": f"replicated scene, samples sharded x{ws}, films summed" if ws > 1
+                       else "1 GPU"},
+            "e2e": {"value": aggregate_rate(samples, ws, e2e_s) / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": W * H * 3 * 4 * 2,
+                    "api": f"lmgpu_render_{cfg['renderer']} (host film)" + (", reduce_film over ranks" if ws > 1
+                                                                            else "")},
             "gpu_launches": launches, "clocks": clk, "roofline": roofline}
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
@@ -978,7 +1033,7 @@ def main() -> None:
                          "box; ptmis / ptdirect: next-event estimation on the Cornell box; bdpt: renderer::bdpt on the caustic room; ltdirect: light tracing on the Cornell "
                          "box; vcm: vertex connection and merging on the Cornell box; batch: 12 scenes in one "
                          "wavefront; "
-                         "guiding: learned path guiding vs plain PT at equal time; surface: surface geometry "
+                         "guiding: time to relMSE 1e-2 of guided, unguided and plain PT; surface: surface geometry "
                          "at the ray-cast hits")
     ap.add_argument("--mlp-only", action="store_true", help="guiding: time the MLP kernels only")
     ap.add_argument("--no-autotune", action="store_true", help="batch: keep the default tuning (profiling runs)")

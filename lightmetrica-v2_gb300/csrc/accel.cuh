@@ -64,6 +64,11 @@ struct lmgpu_accel {
     lmgpu_hit* stage_hits = nullptr;
     uint64_t stage_cap = 0;
     cudaStream_t stage_stream[2] = {nullptr, nullptr};
+    // Small queries (a single-ray Intersect): rays, hits and a copy of the
+    // status word in one pinned, device-mapped host buffer, so a call is one
+    // launch, one 4-byte copy and one synchronisation.
+    unsigned char* small_host = nullptr;
+    unsigned char* small_dev = nullptr;
 };
 
 namespace lmgpu {

@@ -30,11 +30,9 @@ int check_device()
     return LMGPU_OK;
 }
 
-int read_status(const lmgpu_accel* a, cudaStream_t stream)
+// The traversal status word as an error code and message.
+int status_error(uint32_t st)
 {
-    uint32_t st = 0;
-    LMGPU_CUDA_TRY(cudaMemcpyAsync(&st, a->status, sizeof(st), cudaMemcpyDeviceToHost, stream));
-    LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
     if (st & kStatusBadTree) {
         set_error("traversal met an out-of-range node or triangle index (malformed BVH)");
         return LMGPU_ERR_OVERFLOW;
@@ -46,9 +44,54 @@ int read_status(const lmgpu_accel* a, cudaStream_t stream)
     return LMGPU_OK;
 }
 
+int read_status(const lmgpu_accel* a, cudaStream_t stream)
+{
+    uint32_t st = 0;
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(&st, a->status, sizeof(st), cudaMemcpyDeviceToHost, stream));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    return status_error(st);
+}
+
 // Rays staged through device memory at once by the host-buffer entry point
 // (rays 32 B + hits 16 B per ray: 384 MiB for the two halves).
 constexpr uint64_t kHostBatch = 8ull << 20;
+
+// Queries of at most kSmallRays rays take the mapped-buffer path.
+constexpr uint64_t kSmallRays = 256;
+constexpr size_t kSmallHitsOff = kSmallRays * 32;
+constexpr size_t kSmallStatusOff = kSmallHitsOff + kSmallRays * sizeof(lmgpu_hit);
+constexpr size_t kSmallBytes = kSmallStatusOff + 16;
+
+// n <= kSmallRays rays from host memory: the kernel reads the rays from and
+// writes the hits to the pinned, mapped buffer directly.  Caller holds host_mu.
+int trace_small(lmgpu_accel* a, const float* rays, lmgpu_hit* hits, uint64_t n, int anyhit)
+{
+    if (!a->small_host) {
+        void* h = nullptr;
+        void* d = nullptr;
+        LMGPU_CUDA_TRY(cudaHostAlloc(&h, kSmallBytes, cudaHostAllocMapped));
+        if (cudaHostGetDevicePointer(&d, h, 0) != cudaSuccess) {
+            cudaFreeHost(h);
+            set_error("lmgpu_trace: mapped staging buffer unavailable");
+            return LMGPU_ERR_CUDA;
+        }
+        a->small_host = static_cast<unsigned char*>(h);
+        a->small_dev = static_cast<unsigned char*>(d);
+    }
+    if (!a->stage_stream[0]) LMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&a->stage_stream[0], cudaStreamNonBlocking));
+    cudaStream_t s = a->stage_stream[0];
+    std::memcpy(a->small_host, rays, n * 32);
+    int rc = launch_trace(a, reinterpret_cast<const float4*>(a->small_dev),
+                          reinterpret_cast<lmgpu_hit*>(a->small_dev + kSmallHitsOff), n, anyhit != 0, false, s);
+    if (rc) return rc;
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(a->small_host + kSmallStatusOff, a->status, sizeof(uint32_t),
+                                   cudaMemcpyDeviceToHost, s));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    std::memcpy(hits, a->small_host + kSmallHitsOff, n * sizeof(lmgpu_hit));
+    uint32_t st = 0;
+    std::memcpy(&st, a->small_host + kSmallStatusOff, sizeof(st));
+    return status_error(st);
+}
 
 }  // namespace
 
@@ -98,6 +141,7 @@ void lmgpu_accel_destroy(lmgpu_accel* a)
     if (a->stage_hits) cudaFree(a->stage_hits);
     for (int i = 0; i < 2; i++)
         if (a->stage_stream[i]) cudaStreamDestroy(a->stage_stream[i]);
+    if (a->small_host) cudaFreeHost(a->small_host);
     delete a;
 }
 
@@ -212,6 +256,7 @@ int lmgpu_trace(const lmgpu_accel* ca, const float* rays, lmgpu_hit* hits, uint6
     // The staging buffers are state of the accel object, not of the query.
     lmgpu_accel* a = const_cast<lmgpu_accel*>(ca);
     std::lock_guard<std::mutex> lock(a->host_mu);
+    if (n <= kSmallRays) return trace_small(a, rays, hits, n, anyhit);
     // Two staging halves; batch i is copied in on stream i%2 while the other
     // stream traces or copies out, so host<->device copies overlap traversal.
     const uint64_t half = kHostBatch / 2;

@@ -197,6 +197,35 @@ def test_device_entry_matches_host_entry(gpu_lib):
     assert st["node_fetches"] > 0
 
 
+@pytest.mark.parametrize("anyhit", [False, True])
+def test_small_host_queries_match_device_entry(gpu_lib, anyhit):
+    """Host queries of at most 256 rays (a single-ray Intersect, for one)
+    take the mapped-buffer path; their hits equal the device entry's, on
+    either side of the 256-ray boundary and for repeated calls."""
+    import torch
+    from lmgpu import scenes
+
+    tris = scenes.raycast_scene(20_000, 32, seed=8)
+    rays = scenes.raycast_rays(4096, seed=9)
+    acc = gpu_lib.Accel()
+    acc.build(tris)
+    dr = torch.from_numpy(rays).cuda()
+    dh = torch.empty((rays.shape[0], 4), dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    acc.trace_device(dr.data_ptr(), dh.data_ptr(), rays.shape[0], anyhit, s)
+    acc.check(s)
+    ref = dh.cpu().numpy().view(gpu_lib.HIT_DTYPE).reshape(-1)
+    off = 0
+    for n in (1, 1, 2, 255, 256, 257, 1000, 1):
+        h = acc.trace(rays[off:off + n], anyhit=anyhit)
+        assert np.array_equal(h["prim"], ref["prim"][off:off + n]), n
+        assert np.array_equal(h["t"], ref["t"][off:off + n]), n
+        if not anyhit:
+            assert np.array_equal(h["b1"], ref["b1"][off:off + n]), n
+        off += n
+    acc.close()
+
+
 def test_deterministic_across_builds(gpu_lib):
     from lmgpu import scenes
 
