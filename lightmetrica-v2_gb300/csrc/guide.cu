@@ -77,8 +77,12 @@ __host__ __device__ constexpr uint32_t fwd_w(int l) { return l == 0 ? 0u : 16384
 __host__ __device__ constexpr uint32_t fwd_a(uint32_t g) { return 47104u + 49152u * g; }  // 128 x 128 activations
 __host__ __device__ constexpr uint32_t fwd_b(uint32_t g) { return fwd_a(g) + 32768u; }   // 128 x 64 activations
 constexpr uint32_t kFwdBias = fwd_a(3);                        // 304 floats
-constexpr uint32_t kFwdBar = kFwdBias + 1280;                  // one mbarrier per group, the TMEM address
-constexpr uint32_t kFwdSmem = kFwdBar + 64;
+constexpr uint32_t kFwdBar = kFwdBias + 1280;                  // two mbarriers per group (MMAs, queries), the TMEM address
+// per group the next tile's 128 queries (9 floats each), brought in by one
+// bulk copy while the current tile runs
+constexpr uint32_t kTileQueryBytes = (uint32_t)kTile * 9u * 4u;  // 4,608
+__host__ __device__ constexpr uint32_t fwd_q(uint32_t g) { return kFwdBar + 64u + kTileQueryBytes * g; }
+constexpr uint32_t kFwdSmem = fwd_q(3);
 
 // shared-memory plan of the backward kernel (bytes)
 // W_l^T for l = 1..4 (W2^T..W4^T 64x64, W5^T 64x48) at 8192 (l - 1), shared by both tile groups
@@ -208,8 +212,8 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
     if (d_n) n = *d_n;  // query count on the device (at most the n launched for)
     extern __shared__ __align__(1024) unsigned char smem[];
     float* sbias = reinterpret_cast<float*>(smem + kFwdBias);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kFwdBar);
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kFwdBar + 32);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kFwdBar);  // MMA barriers 0..2, query barriers 3..5
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kFwdBar + 48);
     // three independent tile groups of 128 threads, one row of a tile each;
     // group g works on tiles 3 blockIdx.x + g, + 3 gridDim.x, ..., with its
     // own activation buffers, mbarrier and 64 tensor-memory columns, so one
@@ -224,9 +228,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
         sbias[i] = params[b_off(l) + j];
     }
     if (tid == 0) {
-        tc::mbar_init(bars, 1);
-        tc::mbar_init(bars + 1, 1);
-        tc::mbar_init(bars + 2, 1);
+        for (int i = 0; i < 6; i++) tc::mbar_init(bars + i, 1);
         tc::mbar_init_fence();
     }
     if (warp == 0) tc::tmem_alloc(s_tmem, 256);
@@ -235,13 +237,28 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
     tc::fence_after_sync();
     const uint32_t tmem = *s_tmem + 64u * g;
     uint64_t* bar = bars + g;
+    uint64_t* qbar = bars + 3 + g;
     unsigned char* bufA = smem + fwd_a(g);
     unsigned char* bufB = smem + fwd_b(g);
-    const uint32_t sA = tc::smem_addr(bufA), sB = tc::smem_addr(bufB);
-    uint32_t phase = 0;
-    bool alive = true;
+    const float* sq = reinterpret_cast<const float*>(smem + fwd_q(g));
+    const uint32_t sA = tc::smem_addr(bufA), sB = tc::smem_addr(bufB), sQ = tc::smem_addr(smem + fwd_q(g));
+    uint32_t phase = 0, qphase = 0;
+    bool alive = true, q_pending = false;
 
     const uint32_t ntiles = (n + kTile - 1) / kTile;
+    // full tiles of a 16-byte aligned query array come in by bulk copy, the
+    // next one while the current one runs; a partial last tile is read
+    // directly (a bulk copy would read past the array)
+    const bool q_bulk = ((uintptr_t)queries & 15u) == 0u;
+    auto full_tile = [&](uint32_t t) { return q_bulk && (uint64_t)(t + 1) * kTile <= (uint64_t)n; };
+    auto fetch_queries = [&](uint32_t t) {
+        if (r == 0) {
+            tc::mbar_arrive_expect_tx(qbar, kTileQueryBytes);
+            tc::bulk_load(sQ, queries + (size_t)t * kTile * 9u, kTileQueryBytes, qbar);
+        }
+        q_pending = true;
+    };
+    if (3u * blockIdx.x + g < ntiles && full_tile(3u * blockIdx.x + g)) fetch_queries(3u * blockIdx.x + g);
     for (uint32_t tile = 3u * blockIdx.x + g; tile < ntiles && alive; tile += 3u * gridDim.x) {
         const uint32_t row = tile * kTile + r;
         // features of the row's query (guide_net.cuh): per axis 16 frequencies
@@ -249,7 +266,21 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
         // stored eight at a time
         {
             float q9[9];
-            for (int j = 0; j < 9; j++) q9[j] = row < n ? queries[9 * (size_t)row + j] : 0.0f;
+            if (full_tile(tile)) {
+                const bool got = tc::mbar_wait(qbar, qphase, kWaitLimit);
+                if (got) {
+                    qphase ^= 1u;
+                    q_pending = false;
+                }
+                if (!group_sync_and(g, got)) {
+                    if (r == 0) atomicOr(status, kStatusTimeout);
+                    alive = false;
+                    break;
+                }
+                for (int j = 0; j < 9; j++) q9[j] = sq[9 * r + j];
+            } else {
+                for (int j = 0; j < 9; j++) q9[j] = row < n ? queries[9 * (size_t)row + j] : 0.0f;
+            }
 #pragma unroll
             for (int d = 0; d < 3; d++) {
                 float f[32];
@@ -266,6 +297,8 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
             for (int g8 = 13; g8 < 16; g8++) put8(bufA, r, 8 * g8, kIn, z8);
         }
         group_sync_for_mma(g);
+        // the query buffer is free (read before the barrier): the next tile's
+        if (tile + 3u * gridDim.x < ntiles && full_tile(tile + 3u * gridDim.x)) fetch_queries(tile + 3u * gridDim.x);
 #pragma unroll
         for (int l = 0; l < 5; l++) {
             if (!alive) break;
@@ -310,8 +343,10 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
             group_sync_for_mma(g);
         }
     }
-    // after a time-out, one more bounded wait for this group's MMAs in flight
+    // after a time-out, one more bounded wait for this group's MMAs and its
+    // query copy in flight
     if (!alive) tc::mbar_wait(bar, phase ^ 1u, kWaitLimit);
+    if (q_pending) tc::mbar_wait(qbar, qphase, kWaitLimit);
     if (MODE == MODE_TRAIN && r == 0) tc::bulk_wait0();
     tc::fence_before_sync();
     __syncthreads();
