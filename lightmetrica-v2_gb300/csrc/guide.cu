@@ -10,9 +10,12 @@
 //               activations ping-pong between its two shared-memory buffers;
 //               each layer is K/16 MMAs of M = 128 into the group's
 //               64-column tensor-memory accumulator, issued by one thread and
-//               completed through the group's mbarrier; the feature encoding
-//               and the epilogue (bias, ReLU, BF16 pack) run one row per
-//               thread, reading the row with tcgen05.ld.
+//               completed through the group's mbarrier.  The bias enters as
+//               one more K = 16 MMA (a ones tile against the bias split into
+//               two BF16 terms), so the epilogue is ReLU and BF16 rounding in
+//               one conversion per pair; the feature encoding and the
+//               epilogue run one row per thread, reading the row with
+//               tcgen05.ld.
 //               MODE_TRAIN also copies every layer's input tile, as the
 //               shared-memory image the MMAs read, to global memory with one
 //               bulk copy per layer, and writes the raw outputs, for the
@@ -76,13 +79,17 @@ __host__ __device__ constexpr uint32_t fwd_w(int l) { return l == 0 ? 0u : 16384
 // three tile groups, each with its own activation buffers
 __host__ __device__ constexpr uint32_t fwd_a(uint32_t g) { return 47104u + 49152u * g; }  // 128 x 128 activations
 __host__ __device__ constexpr uint32_t fwd_b(uint32_t g) { return fwd_a(g) + 32768u; }   // 128 x 64 activations
-constexpr uint32_t kFwdBias = fwd_a(3);                        // 304 floats
-constexpr uint32_t kFwdBar = kFwdBias + 1280;                  // two mbarriers per group (MMAs, queries), the TMEM address
+constexpr uint32_t kFwdBar = fwd_a(3);                         // two mbarriers per group (MMAs, queries), the TMEM address
 // per group the next tile's 128 queries (9 floats each), brought in by one
 // bulk copy while the current tile runs
 constexpr uint32_t kTileQueryBytes = (uint32_t)kTile * 9u * 4u;  // 4,608
 __host__ __device__ constexpr uint32_t fwd_q(uint32_t g) { return kFwdBar + 64u + kTileQueryBytes * g; }
-constexpr uint32_t kFwdSmem = fwd_q(3);
+// the bias as one more K = 16 MMA per layer: a constant 128 x 16 tile whose
+// columns 0 and 1 are ones, against a per-layer N x 16 tile holding the bias
+// split into two BF16 terms (hi + lo, about 16 significant bits)
+constexpr uint32_t kFwdOnes = fwd_q(3);                                      // 4 KB
+__host__ __device__ constexpr uint32_t fwd_bt(int l) { return kFwdOnes + 4096u + 2048u * (uint32_t)l; }  // 2 KB each
+constexpr uint32_t kFwdSmem = fwd_bt(5);
 
 // shared-memory plan of the backward kernel (bytes)
 // W_l^T for l = 1..4 (W2^T..W4^T 64x64, W5^T 64x48) at 8192 (l - 1), shared by both tile groups
@@ -150,15 +157,25 @@ __device__ void load_matrix(unsigned char* tile, const float* __restrict__ W, in
     }
 }
 
-// Issues the K / 16 MMAs of one M = 128 layer and commits them to the mbarrier.
+// Issues one M = 128 layer, the bias MMA (ones x bias tile) and then its
+// K / 16 MMAs, and commits them to the mbarrier.
 __device__ __forceinline__ void issue_layer(uint32_t d_tmem, uint32_t a_saddr, uint32_t K, uint32_t b_saddr,
-                                            uint32_t N, uint64_t* bar)
+                                            uint32_t N, uint32_t ones_saddr, uint32_t bias_saddr, uint64_t* bar)
 {
     const uint32_t idesc = tc::idesc_bf16_f32(128, N);
+    tc::mma_bf16(d_tmem, tc::kmajor_desc(ones_saddr, 16u), tc::kmajor_desc(bias_saddr, 16u), idesc, 0u);
     for (uint32_t ks = 0; ks < K / 16; ks++)
         tc::mma_bf16(d_tmem, tc::kmajor_desc(a_saddr + ks * 256u, K), tc::kmajor_desc(b_saddr + ks * 256u, K), idesc,
-                     ks > 0 ? 1u : 0u);
+                     1u);
     tc::mma_commit(bar);
+}
+
+// relu(a), relu(b) rounded to BF16 and packed (a in the low half).
+__device__ __forceinline__ uint32_t relu_pack2(float a, float b)
+{
+    uint32_t r;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+    return r;
 }
 
 // Named barrier over the 128 threads of tile group g (barrier 1 + g;
@@ -211,7 +228,6 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
 {
     if (d_n) n = *d_n;  // query count on the device (at most the n launched for)
     extern __shared__ __align__(1024) unsigned char smem[];
-    float* sbias = reinterpret_cast<float*>(smem + kFwdBias);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kFwdBar);  // MMA barriers 0..2, query barriers 3..5
     uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kFwdBar + 48);
     // three independent tile groups of 128 threads, one row of a tile each;
@@ -223,9 +239,23 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
     const uint32_t lane_base = (warp & 3u) * 32u;
 
     for (int l = 0; l < 5; l++) load_matrix(smem + fwd_w(l), params + w_off(l), layer_out(l), layer_in(l), false);
-    for (int i = tid; i < 4 * kHid + kOut; i += kFwdThreads) {
-        const int l = i / kHid < 4 ? i / kHid : 4, j = i - l * kHid;
-        sbias[i] = params[b_off(l) + j];
+    // the ones tile and the bias tiles (K-major, K = 16)
+    for (uint32_t i = tid; i < (uint32_t)kTile * 16u; i += kFwdThreads) {
+        const uint32_t rr = i >> 4, k = i & 15u;
+        *reinterpret_cast<__nv_bfloat16*>(smem + kFwdOnes + tc::kmajor_offset(rr, k, 16u)) =
+            __float2bfloat16_rn(k < 2u ? 1.0f : 0.0f);
+    }
+    for (uint32_t i = tid; i < 5u * 64u * 16u; i += kFwdThreads) {
+        const int l = (int)(i / 1024u);
+        const uint32_t nn = (i >> 4) & 63u, k = i & 15u;
+        float v = 0.0f;
+        if (nn < (uint32_t)layer_out(l) && k < 2u) {
+            const float b = params[b_off(l) + nn];
+            const float hi = __bfloat162float(__float2bfloat16_rn(b));
+            v = k == 0u ? hi : b - hi;
+        }
+        if (nn < (uint32_t)layer_out(l))
+            *reinterpret_cast<__nv_bfloat16*>(smem + fwd_bt(l) + tc::kmajor_offset(nn, k, 16u)) = __float2bfloat16_rn(v);
     }
     if (tid == 0) {
         for (int i = 0; i < 6; i++) tc::mbar_init(bars + i, 1);
@@ -307,7 +337,8 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
             unsigned char* out_tile = (l & 1) ? bufA : bufB;
             const uint32_t K = layer_in(l), N = layer_out(l);
             if (r == 0) {
-                issue_layer(tmem, a_in, K, tc::smem_addr(smem + fwd_w(l)), N, bar);
+                issue_layer(tmem, a_in, K, tc::smem_addr(smem + fwd_w(l)), N, tc::smem_addr(smem + kFwdOnes),
+                            tc::smem_addr(smem + fwd_bt(l)), bar);
                 if (MODE == MODE_TRAIN) {
                     // the layer's input tile, as it is, to the stored
                     // activations; its buffer is rewritten only after the
@@ -320,14 +351,17 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
             }
             alive = group_wait_layer(g, bar, phase, status);
             if (!alive) break;
-            const float* bias = sbias + l * kHid;
             if (l < 4) {
                 float h[kHid];
 #pragma unroll
                 for (int c = 0; c < kHid; c += 16) tc::tmem_load16(tc::tmem_at(tmem, lane_base, c), h + c);
                 tc::tmem_wait_ld();
-                for (int c = 0; c < kHid; c++) h[c] = fmaxf(h[c] + bias[c], 0.0f);
-                for (int c = 0; c < kHid; c += 8) put8(out_tile, r, c, kHid, h + c);
+                // the bias is in the accumulator: ReLU and BF16 rounding in one conversion
+#pragma unroll
+                for (int c = 0; c < kHid; c += 8)
+                    *reinterpret_cast<uint4*>(out_tile + tc::kmajor_offset(r, c, kHid)) =
+                        make_uint4(relu_pack2(h[c], h[c + 1]), relu_pack2(h[c + 2], h[c + 3]),
+                                   relu_pack2(h[c + 4], h[c + 5]), relu_pack2(h[c + 6], h[c + 7]));
             } else {
                 float z[kOut];
 #pragma unroll
@@ -336,8 +370,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
                 if (row < n) {
                     float4* dst = reinterpret_cast<float4*>(raw_out + (size_t)row * kOutUsed);
                     for (int c = 0; c < kOutUsed; c += 4)
-                        dst[c / 4] = make_float4(z[c] + bias[c], z[c + 1] + bias[c + 1], z[c + 2] + bias[c + 2],
-                                                 z[c + 3] + bias[c + 3]);
+                        dst[c / 4] = make_float4(z[c], z[c + 1], z[c + 2], z[c + 3]);
                 }
             }
             group_sync_for_mma(g);
