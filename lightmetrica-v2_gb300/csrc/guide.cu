@@ -2,12 +2,14 @@
 // forward, backward and Adam kernels for the MLP of guide_net.cuh, BF16
 // operands with FP32 accumulation in tensor memory.
 //
-// k_guide_fwd   one CTA per SM, persistent over 128-query tiles, as three
+// k_guide_fwd   one CTA per SM, persistent over 128-query tiles, as four
 //               independent groups of 4 warps that work on alternate tiles
 //               (so one group's MMAs overlap the others' feature encoding
 //               and epilogues).  The five weight matrices stay in shared
 //               memory (BF16, K-major canonical layout); a group's tile
-//               activations ping-pong between its two shared-memory buffers;
+//               activations ping-pong between its two 64-column
+//               shared-memory tiles, which together hold the 128 input
+//               features of the first layer;
 //               each layer is K/16 MMAs of M = 128 into the group's
 //               64-column tensor-memory accumulator, issued by one thread and
 //               completed through the group's mbarrier.  The bias enters as
@@ -26,9 +28,10 @@
 //               dH = dZ W (M = 128 MMA against W^T kept in shared memory, into
 //               the group's own 64 tensor-memory columns) and dW += dZ^T H,
 //               an M = 128 MMA (dZ^T's 64 rows padded with zeros) over the
-//               tile's 128 samples as K, with dZ^T and H^T MN-major; H^T is
-//               the forward's stored input tile, brought in by one bulk copy
-//               while the previous layer finishes.  The dW
+//               tile's 128 samples as K, with dZ^T and H^T MN-major (layer
+//               1's 128 inputs as two halves of 64, one N = 64 MMA each);
+//               H^T is the forward's stored input tile, brought in by one
+//               bulk copy while the previous layer finishes.  The dW
 //               accumulators (384 columns, zeroed at the start) are shared by
 //               both groups and summed across every tile the CTA processes;
 //               the bias gradients are summed from the dZ^T tiles in registers
@@ -59,13 +62,15 @@ constexpr uint32_t kStatusTimeout = 16;
 constexpr uint32_t kWaitLimit = 1u << 24;
 constexpr int kTile = 128;
 constexpr int kThreads = 256;      // backward: two tile groups of 128 threads, one sample each
-constexpr int kFwdThreads = 384;   // forward: three tile groups of 128 threads, one query each
+constexpr int kFwdGroups = 4;      // forward: tile groups of 128 threads, one query each
+constexpr int kFwdThreads = 128 * kFwdGroups;
 constexpr int kActs = kIn + 4 * kHid;  // stored activations per sample (bf16)
 // Stored activations of the training forward, tile by tile: the inputs of
 // layers 1..5 of a 128-sample tile as the K-major canonical images the
-// forward multiplies (features 32 KB, then four 16 KB hidden tiles).  The
-// same bytes are the MN-major H^T operands of the backward's weight
-// gradients, so both sides move them with one bulk copy per layer.
+// forward multiplies (the features as two 16 KB tiles of 64 columns, then
+// four 16 KB hidden tiles).  The same bytes are the MN-major H^T operands of
+// the backward's weight gradients (MN = 64 each), so both sides move them
+// with bulk copies.
 constexpr uint32_t kActTileBytes = (uint32_t)kTile * kActs * 2u;  // 98,304
 __host__ __device__ constexpr uint32_t act_off(int l)
 {
@@ -76,18 +81,20 @@ __host__ __device__ constexpr uint32_t act_bytes(int l) { return (uint32_t)kTile
 // shared-memory plan of the forward kernel (bytes)
 // W1 (64x128) at 0, W2..W4 (64x64) at 16384 + 8192 (l - 1), W5 (48x64) at 40960
 __host__ __device__ constexpr uint32_t fwd_w(int l) { return l == 0 ? 0u : 16384u + 8192u * (uint32_t)(l - 1); }
-// three tile groups, each with its own activation buffers
-__host__ __device__ constexpr uint32_t fwd_a(uint32_t g) { return 47104u + 49152u * g; }  // 128 x 128 activations
-__host__ __device__ constexpr uint32_t fwd_b(uint32_t g) { return fwd_a(g) + 32768u; }   // 128 x 64 activations
-constexpr uint32_t kFwdBar = fwd_a(3);                         // two mbarriers per group (MMAs, queries), the TMEM address
+// per tile group two 128 x 64 activation tiles X and Y (K-major, K = 64);
+// layer 1's 128 input features are X (0..63) and Y (64..127), and the
+// layers then alternate X -> Y -> X ...
+__host__ __device__ constexpr uint32_t fwd_x(uint32_t g) { return 47104u + 32768u * g; }
+__host__ __device__ constexpr uint32_t fwd_y(uint32_t g) { return fwd_x(g) + 16384u; }
+constexpr uint32_t kFwdBar = fwd_x(kFwdGroups);  // two mbarriers per group (MMAs, queries), the TMEM address
 // per group the next tile's 128 queries (9 floats each), brought in by one
 // bulk copy while the current tile runs
 constexpr uint32_t kTileQueryBytes = (uint32_t)kTile * 9u * 4u;  // 4,608
-__host__ __device__ constexpr uint32_t fwd_q(uint32_t g) { return kFwdBar + 64u + kTileQueryBytes * g; }
+__host__ __device__ constexpr uint32_t fwd_q(uint32_t g) { return kFwdBar + 128u + kTileQueryBytes * g; }
 // the bias as one more K = 16 MMA per layer: a constant 128 x 16 tile whose
 // columns 0 and 1 are ones, against a per-layer N x 16 tile holding the bias
 // split into two BF16 terms (hi + lo, about 16 significant bits)
-constexpr uint32_t kFwdOnes = fwd_q(3);                                      // 4 KB
+constexpr uint32_t kFwdOnes = fwd_q(kFwdGroups);                             // 4 KB
 __host__ __device__ constexpr uint32_t fwd_bt(int l) { return kFwdOnes + 4096u + 2048u * (uint32_t)l; }  // 2 KB each
 constexpr uint32_t kFwdSmem = fwd_bt(5);
 
@@ -158,15 +165,16 @@ __device__ void load_matrix(unsigned char* tile, const float* __restrict__ W, in
 }
 
 // Issues one M = 128 layer, the bias MMA (ones x bias tile) and then its
-// K / 16 MMAs, and commits them to the mbarrier.
-__device__ __forceinline__ void issue_layer(uint32_t d_tmem, uint32_t a_saddr, uint32_t K, uint32_t b_saddr,
+// K / 16 MMAs, and commits them to the mbarrier.  The A operand is K / 64
+// tiles of 64 columns (K-major, K = 64): a0 holds columns 0..63, a1 64..127.
+__device__ __forceinline__ void issue_layer(uint32_t d_tmem, uint32_t a0, uint32_t a1, uint32_t K, uint32_t b_saddr,
                                             uint32_t N, uint32_t ones_saddr, uint32_t bias_saddr, uint64_t* bar)
 {
     const uint32_t idesc = tc::idesc_bf16_f32(128, N);
     tc::mma_bf16(d_tmem, tc::kmajor_desc(ones_saddr, 16u), tc::kmajor_desc(bias_saddr, 16u), idesc, 0u);
     for (uint32_t ks = 0; ks < K / 16; ks++)
-        tc::mma_bf16(d_tmem, tc::kmajor_desc(a_saddr + ks * 256u, K), tc::kmajor_desc(b_saddr + ks * 256u, K), idesc,
-                     1u);
+        tc::mma_bf16(d_tmem, tc::kmajor_desc((ks < 4u ? a0 : a1) + (ks & 3u) * 256u, 64u),
+                     tc::kmajor_desc(b_saddr + ks * 256u, K), idesc, 1u);
     tc::mma_commit(bar);
 }
 
@@ -228,10 +236,10 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
 {
     if (d_n) n = *d_n;  // query count on the device (at most the n launched for)
     extern __shared__ __align__(1024) unsigned char smem[];
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kFwdBar);  // MMA barriers 0..2, query barriers 3..5
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kFwdBar + 48);
-    // three independent tile groups of 128 threads, one row of a tile each;
-    // group g works on tiles 3 blockIdx.x + g, + 3 gridDim.x, ..., with its
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kFwdBar);  // MMA barriers, then query barriers
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kFwdBar + 16u * kFwdGroups);
+    // four independent tile groups of 128 threads, one row of a tile each;
+    // group g works on tiles 4 blockIdx.x + g, + 4 gridDim.x, ..., with its
     // own activation buffers, mbarrier and 64 tensor-memory columns, so one
     // group's MMAs run while the others compute features or epilogues.  A
     // warp reads tensor memory lanes 32 (warp % 4) .. + 31, its rows.
@@ -258,7 +266,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
             *reinterpret_cast<__nv_bfloat16*>(smem + fwd_bt(l) + tc::kmajor_offset(nn, k, 16u)) = __float2bfloat16_rn(v);
     }
     if (tid == 0) {
-        for (int i = 0; i < 6; i++) tc::mbar_init(bars + i, 1);
+        for (int i = 0; i < 2 * kFwdGroups; i++) tc::mbar_init(bars + i, 1);
         tc::mbar_init_fence();
     }
     if (warp == 0) tc::tmem_alloc(s_tmem, 256);
@@ -267,11 +275,11 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
     tc::fence_after_sync();
     const uint32_t tmem = *s_tmem + 64u * g;
     uint64_t* bar = bars + g;
-    uint64_t* qbar = bars + 3 + g;
-    unsigned char* bufA = smem + fwd_a(g);
-    unsigned char* bufB = smem + fwd_b(g);
+    uint64_t* qbar = bars + kFwdGroups + g;
+    unsigned char* bufX = smem + fwd_x(g);
+    unsigned char* bufY = smem + fwd_y(g);
     const float* sq = reinterpret_cast<const float*>(smem + fwd_q(g));
-    const uint32_t sA = tc::smem_addr(bufA), sB = tc::smem_addr(bufB), sQ = tc::smem_addr(smem + fwd_q(g));
+    const uint32_t sX = tc::smem_addr(bufX), sY = tc::smem_addr(bufY), sQ = tc::smem_addr(smem + fwd_q(g));
     uint32_t phase = 0, qphase = 0;
     bool alive = true, q_pending = false;
 
@@ -288,8 +296,9 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
         }
         q_pending = true;
     };
-    if (3u * blockIdx.x + g < ntiles && full_tile(3u * blockIdx.x + g)) fetch_queries(3u * blockIdx.x + g);
-    for (uint32_t tile = 3u * blockIdx.x + g; tile < ntiles && alive; tile += 3u * gridDim.x) {
+    const uint32_t first = kFwdGroups * blockIdx.x + g, stride = kFwdGroups * gridDim.x;
+    if (first < ntiles && full_tile(first)) fetch_queries(first);
+    for (uint32_t tile = first; tile < ntiles && alive; tile += stride) {
         const uint32_t row = tile * kTile + r;
         // features of the row's query (guide_net.cuh): per axis 16 frequencies
         // (sin, cos), then the normal and the outgoing direction, then zeros;
@@ -311,6 +320,8 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
             } else {
                 for (int j = 0; j < 9; j++) q9[j] = row < n ? queries[9 * (size_t)row + j] : 0.0f;
             }
+            // features 0..63 (axes x, y) into X, 64..127 (axis z, normal,
+            // direction, zeros) into Y
 #pragma unroll
             for (int d = 0; d < 3; d++) {
                 float f[32];
@@ -318,33 +329,36 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
                 if (row >= n)
                     for (int j = 0; j < 32; j++) f[j] = 0.0f;
 #pragma unroll
-                for (int g8 = 0; g8 < 4; g8++) put8(bufA, r, 32 * d + 8 * g8, kIn, f + 8 * g8);
+                for (int g8 = 0; g8 < 4; g8++)
+                    put8(d < 2 ? bufX : bufY, r, (32 * d + 8 * g8) & 63, kHid, f + 8 * g8);
             }
             const float f[8] = {q9[3], q9[4], q9[5], q9[6], q9[7], q9[8], 0.0f, 0.0f};
             const float z8[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-            put8(bufA, r, 96, kIn, f);
+            put8(bufY, r, 32, kHid, f);
 #pragma unroll
-            for (int g8 = 13; g8 < 16; g8++) put8(bufA, r, 8 * g8, kIn, z8);
+            for (int g8 = 5; g8 < 8; g8++) put8(bufY, r, 8 * g8, kHid, z8);
         }
         group_sync_for_mma(g);
         // the query buffer is free (read before the barrier): the next tile's
-        if (tile + 3u * gridDim.x < ntiles && full_tile(tile + 3u * gridDim.x)) fetch_queries(tile + 3u * gridDim.x);
+        if (tile + stride < ntiles && full_tile(tile + stride)) fetch_queries(tile + stride);
 #pragma unroll
         for (int l = 0; l < 5; l++) {
             if (!alive) break;
-            // layer l reads buffer A (l even) or B (l odd)
-            const uint32_t a_in = (l & 1) ? sB : sA;
-            unsigned char* out_tile = (l & 1) ? bufA : bufB;
+            // layer 1 reads X and Y, then layers read X, Y, X, Y; outputs
+            // go to X, Y, X, Y
+            const uint32_t a_in = (l == 0 || (l & 1)) ? sX : sY;
+            unsigned char* out_tile = (l & 1) ? bufY : bufX;
             const uint32_t K = layer_in(l), N = layer_out(l);
             if (r == 0) {
-                issue_layer(tmem, a_in, K, tc::smem_addr(smem + fwd_w(l)), N, tc::smem_addr(smem + kFwdOnes),
+                issue_layer(tmem, a_in, sY, K, tc::smem_addr(smem + fwd_w(l)), N, tc::smem_addr(smem + kFwdOnes),
                             tc::smem_addr(smem + fwd_bt(l)), bar);
                 if (MODE == MODE_TRAIN) {
-                    // the layer's input tile, as it is, to the stored
-                    // activations; its buffer is rewritten only after the
-                    // copy has read it
-                    tc::bulk_store(reinterpret_cast<unsigned char*>(acts) + (size_t)tile * kActTileBytes + act_off(l),
-                                   a_in, act_bytes(l));
+                    // the layer's input tiles, as they are, to the stored
+                    // activations; their buffers are rewritten only after
+                    // the copies have read them
+                    unsigned char* dst = reinterpret_cast<unsigned char*>(acts) + (size_t)tile * kActTileBytes + act_off(l);
+                    tc::bulk_store(dst, a_in, 16384u);
+                    if (l == 0) tc::bulk_store(dst + 16384u, sY, 16384u);
                     tc::bulk_commit();
                     tc::bulk_wait_read0();
                 }
@@ -509,11 +523,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_guide_bwd(const float* __restri
             if (r == 0) {
                 // dW += dZ^T (128 x 128 samples) x (H^T, Kin x 128 samples)^T, in
                 // tensor memory across the CTA's tiles; one K step = 16 samples
-                const uint32_t idesc_w = tc::idesc_bf16_f32_mn(128, Kin);
+                // (layer 1's 128 inputs are two MN-major halves of 64, as the
+                // forward stored them: one N = 64 MMA per half)
+                const uint32_t idesc_w = tc::idesc_bf16_f32_mn(128, 64);
                 const uint32_t a0 = tc::smem_addr(sDZT);
-                for (uint32_t ks = 0; ks < (uint32_t)kTile / 16u; ks++)
-                    tc::mma_bf16(tmem + bwd_dw_col(l), tc::mnmajor_desc(a0 + ks * 2u * (kTile * 16u), kTile),
-                                 tc::mnmajor_desc(sHTa + ks * 2u * (Kin * 16u), Kin), idesc_w, 1u);
+                for (uint32_t h = 0; h < Kin / 64u; h++)
+                    for (uint32_t ks = 0; ks < (uint32_t)kTile / 16u; ks++)
+                        tc::mma_bf16(tmem + bwd_dw_col(l) + 64u * h,
+                                     tc::mnmajor_desc(a0 + ks * 2u * (kTile * 16u), kTile),
+                                     tc::mnmajor_desc(sHTa + 16384u * h + ks * 2u * (64u * 16u), 64u), idesc_w, 1u);
                 // dH_{l-1} = dZ_l (128 x Nl) x (W_l^T, Kin x Nl)^T
                 if (l > 0) {
                     const uint32_t idesc_h = tc::idesc_bf16_f32(128, Kin);
@@ -671,7 +689,7 @@ struct lmgpu_guide {
     float* d_w = nullptr;
     __nv_bfloat16* d_acts = nullptr;
     int grid = 0;         // backward: one CTA per SM
-    int fwd_grid = 0;     // forward: one CTA (three tile groups) per SM
+    int fwd_grid = 0;     // forward: one CTA (four tile groups) per SM
     float* partials = nullptr;  // [grid][kNumParams] per-CTA gradients of the backward
 };
 
@@ -724,8 +742,8 @@ unsigned tiles_grid(uint64_t n, int cap)
     return (unsigned)(tiles < (uint64_t)cap ? tiles : (uint64_t)cap);
 }
 
-// Forward CTAs take three tiles at a time, backward CTAs two.
-unsigned fwd_grid_of(uint64_t n, int cap) { return tiles_grid((n + kTile - 1) / kTile * (kTile / 3 + 1), cap); }
+// Forward CTAs take four tiles at a time, backward CTAs two.
+unsigned fwd_grid_of(uint64_t n, int cap) { return tiles_grid((n + kTile - 1) / kTile * (kTile / kFwdGroups), cap); }
 unsigned bwd_grid_of(uint64_t n, int cap) { return tiles_grid((n + kTile - 1) / kTile * (kTile / 2), cap); }
 
 int check_status(lmgpu_guide* g, cudaStream_t s, const char* name)
