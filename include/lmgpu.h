@@ -133,9 +133,12 @@ int lmgpu_accel_get_info(const lmgpu_accel* accel, lmgpu_accel_info* info);
  * full closest-hit query.  Ties at equal t resolve to the higher global
  * triangle id, the order accel::naive keeps (accel_naive.cpp:99-110).
  * Queries of at most 256 rays (a single-ray Intersect) go through a pinned,
- * device-mapped buffer: one launch and one synchronisation per call; larger
- * ones are staged through device memory in overlapped batches.  Calls on one
- * accel from several threads are serialised. */
+ * device-mapped buffer: one launch and one synchronisation per call.  Larger
+ * ones on page-locked buffers (cudaHostAlloc, cudaHostRegister) are traced in
+ * place, the kernel reading the rays and writing the hits across the host
+ * link; on pageable memory they are staged through device memory in
+ * overlapped batches.  Calls on one accel from several threads are
+ * serialised. */
 int lmgpu_trace(const lmgpu_accel* accel, const float* rays, lmgpu_hit* hits, uint64_t n, int anyhit);
 
 /* As lmgpu_trace on device buffers (rays 16-byte aligned), asynchronous on

@@ -62,6 +62,18 @@ constexpr size_t kSmallHitsOff = kSmallRays * 32;
 constexpr size_t kSmallStatusOff = kSmallHitsOff + kSmallRays * sizeof(lmgpu_hit);
 constexpr size_t kSmallBytes = kSmallStatusOff + 16;
 
+// The device address of a page-locked host buffer, or null for pageable
+// memory (or any other kind).
+const void* mapped_host(const void* p)
+{
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 // n <= kSmallRays rays from host memory: the kernel reads the rays from and
 // writes the hits to the pinned, mapped buffer directly.  Caller holds host_mu.
 int trace_small(lmgpu_accel* a, const float* rays, lmgpu_hit* hits, uint64_t n, int anyhit)
@@ -257,6 +269,19 @@ int lmgpu_trace(const lmgpu_accel* ca, const float* rays, lmgpu_hit* hits, uint6
     lmgpu_accel* a = const_cast<lmgpu_accel*>(ca);
     std::lock_guard<std::mutex> lock(a->host_mu);
     if (n <= kSmallRays) return trace_small(a, rays, hits, n, anyhit);
+    // Page-locked host buffers are mapped into the device's address space:
+    // the kernel reads the rays and writes the hits across the host link
+    // itself, with no staging copies and one launch.
+    const void* d_rays = mapped_host(rays);
+    void* d_hits = const_cast<void*>(mapped_host(hits));
+    if (d_rays && d_hits && !(((uintptr_t)d_rays | (uintptr_t)d_hits) & 15u)) {
+        if (!a->stage_stream[0])
+            LMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&a->stage_stream[0], cudaStreamNonBlocking));
+        const int rc = launch_trace(a, static_cast<const float4*>(d_rays), static_cast<lmgpu_hit*>(d_hits), n,
+                                    anyhit != 0, false, a->stage_stream[0]);
+        if (rc) return rc;
+        return read_status(a, a->stage_stream[0]);
+    }
     // Two staging halves; batch i is copied in on stream i%2 while the other
     // stream traces or copies out, so host<->device copies overlap traversal.
     const uint64_t half = kHostBatch / 2;

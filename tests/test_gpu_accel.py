@@ -226,6 +226,35 @@ def test_small_host_queries_match_device_entry(gpu_lib, anyhit):
     acc.close()
 
 
+@pytest.mark.parametrize("anyhit", [False, True])
+def test_pinned_host_buffers_match_device_entry(gpu_lib, anyhit):
+    """Page-locked host buffers are traced in place (the kernel reads the
+    rays and writes the hits across the host link); pageable ones are staged
+    through device memory.  Both give the device entry's hits."""
+    import torch
+    from lmgpu import scenes
+
+    tris = scenes.raycast_scene(50_000, 64, seed=13)
+    rays = scenes.raycast_rays(300_001, seed=14)
+    acc = gpu_lib.Accel()
+    acc.build(tris)
+    dr = torch.from_numpy(rays).cuda()
+    dh = torch.empty((rays.shape[0], 4), dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    acc.trace_device(dr.data_ptr(), dh.data_ptr(), rays.shape[0], anyhit, s)
+    acc.check(s)
+    ref = dh.cpu().numpy().view(gpu_lib.HIT_DTYPE).reshape(-1)
+    hr = torch.from_numpy(rays).pin_memory()
+    hh = torch.full((rays.shape[0], 4), -7.0, dtype=torch.float32).pin_memory()
+    acc.trace_ptr(hr.data_ptr(), hh.data_ptr(), rays.shape[0], anyhit)
+    pinned = hh.numpy().view(gpu_lib.HIT_DTYPE).reshape(-1)
+    pageable = acc.trace(rays, anyhit=anyhit)
+    for h in (pinned, pageable):
+        assert np.array_equal(h["prim"], ref["prim"])
+        assert np.array_equal(h["t"], ref["t"])
+    acc.close()
+
+
 def test_deterministic_across_builds(gpu_lib):
     from lmgpu import scenes
 
