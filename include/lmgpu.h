@@ -535,7 +535,9 @@ int lmgpu_accel_set_attributes(lmgpu_accel* accel, const float* normals, const f
  * The per-triangle records these queries read are packed by
  * lmgpu_accel_set_attributes, or else by the first query after a build,
  * which then waits for them (under the accel's lock, so concurrent queries
- * from several threads are safe). */
+ * from several threads are safe).  Page-locked buffers are read and written
+ * in place by the kernel; pageable ones go through a staging buffer the
+ * accel keeps, 2^20 hits at a time. */
 int lmgpu_surface(const lmgpu_accel* accel, const float* rays, const lmgpu_hit* hits, uint64_t n, float* surface);
 
 /* As lmgpu_surface on device buffers, asynchronous on `stream`, except the

@@ -69,6 +69,11 @@ struct lmgpu_accel {
     // launch, one 4-byte copy and one synchronisation.
     unsigned char* small_host = nullptr;
     unsigned char* small_dev = nullptr;
+    // Staging of the host-pointer surface entry point for pageable buffers
+    // (rays, hits and planes of one chunk), reused across calls under surf_mu.
+    std::mutex surf_mu;
+    unsigned char* surf_stage = nullptr;
+    uint64_t surf_stage_cap = 0;  // hits per chunk
 };
 
 namespace lmgpu {

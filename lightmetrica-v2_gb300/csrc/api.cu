@@ -154,6 +154,7 @@ void lmgpu_accel_destroy(lmgpu_accel* a)
     for (int i = 0; i < 2; i++)
         if (a->stage_stream[i]) cudaStreamDestroy(a->stage_stream[i]);
     if (a->small_host) cudaFreeHost(a->small_host);
+    if (a->surf_stage) cudaFree(a->surf_stage);
     delete a;
 }
 

@@ -183,6 +183,24 @@ int check_surface_args(const lmgpu_accel* a, const char* who)
     return LMGPU_OK;
 }
 
+// The records are derived state of the accel, packed on first use after a
+// build under the accel's host lock; the wait makes them visible to later
+// queries on any stream.  Once packed (surf_ntri published with release
+// order after the wait) queries take no lock, so they do not queue behind a
+// host trace that holds it.
+int ensure_packed(lmgpu_accel* a, cudaStream_t stream)
+{
+    if (a->ntri == 0 || a->surf_ntri.load(std::memory_order_acquire) == a->ntri) return LMGPU_OK;
+    std::lock_guard<std::mutex> lock(a->host_mu);
+    if (a->surf_ntri.load(std::memory_order_relaxed) != a->ntri) {
+        const int rc = pack_surface(a, stream);
+        if (rc) return rc;
+        LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+        a->surf_ntri.store(a->ntri, std::memory_order_release);
+    }
+    return LMGPU_OK;
+}
+
 int launch_surface(const lmgpu_accel* ca, const float* d_rays, const lmgpu_hit* d_hits, uint64_t n, float* d_out,
                    cudaStream_t stream)
 {
@@ -190,25 +208,38 @@ int launch_surface(const lmgpu_accel* ca, const float* d_rays, const lmgpu_hit* 
         if (n) LMGPU_CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(float) * LMGPU_SURFACE_PLANES * n, stream));
         return LMGPU_OK;
     }
-    // the records are derived state of the accel, packed on first use after a
-    // build under the accel's host lock; the wait makes them visible to later
-    // queries on any stream.  Once packed (surf_ntri published with release
-    // order after the wait) queries take no lock, so they do not queue behind
-    // a host trace that holds it.
     lmgpu_accel* a = const_cast<lmgpu_accel*>(ca);
-    if (a->surf_ntri.load(std::memory_order_acquire) != a->ntri) {
-        std::lock_guard<std::mutex> lock(a->host_mu);
-        if (a->surf_ntri.load(std::memory_order_relaxed) != a->ntri) {
-            const int rc = pack_surface(a, stream);
-            if (rc) return rc;
-            LMGPU_CUDA_TRY(cudaStreamSynchronize(stream));
-            a->surf_ntri.store(a->ntri, std::memory_order_release);
-        }
-    }
+    const int rc = ensure_packed(a, stream);
+    if (rc) return rc;
     const uint64_t blocks = (n + kSurfaceThreads - 1) / kSurfaceThreads;
     k_surface<<<(unsigned)blocks, kSurfaceThreads, 0, stream>>>(a->surf, a->ntri, reinterpret_cast<const float4*>(d_rays),
                                                                 d_hits, n, d_out, a->status);
     LMGPU_CUDA_TRY(cudaGetLastError());
+    return LMGPU_OK;
+}
+
+// The device address of a page-locked host buffer, or null for pageable
+// memory (or any other kind).
+const void* mapped_host(const void* p)
+{
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+// Waits for stream s and turns the accel's status word into an error.
+int surface_status(const lmgpu_accel* a, cudaStream_t s)
+{
+    uint32_t st = 0;
+    LMGPU_CUDA_TRY(cudaMemcpyAsync(&st, a->status, sizeof(st), cudaMemcpyDeviceToHost, s));
+    LMGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    if (st & kStatusBadTree) {
+        set_error("lmgpu_surface: the accel's triangle table is malformed");
+        return LMGPU_ERR_OVERFLOW;
+    }
     return LMGPU_OK;
 }
 
@@ -288,36 +319,44 @@ int lmgpu_surface(const lmgpu_accel* a, const float* rays, const lmgpu_hit* hits
     }
     int rc = check_surface_args(a, "lmgpu_surface");
     if (rc || n == 0) return rc;
-    float *d_rays = nullptr, *d_out = nullptr;
-    lmgpu_hit* d_hits = nullptr;
-    auto release = [&]() {
-        if (d_rays) cudaFree(d_rays);
-        if (d_hits) cudaFree(d_hits);
-        if (d_out) cudaFree(d_out);
-    };
-    cudaError_t e = cudaMalloc((void**)&d_rays, sizeof(float) * 8 * n);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&d_hits, sizeof(lmgpu_hit) * n);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&d_out, sizeof(float) * LMGPU_SURFACE_PLANES * n);
-    if (e == cudaSuccess) e = cudaMemcpy(d_rays, rays, sizeof(float) * 8 * n, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d_hits, hits, sizeof(lmgpu_hit) * n, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-        release();
-        set_error(std::string("lmgpu_surface: ") + cudaGetErrorString(e));
-        return LMGPU_ERR_CUDA;
+    lmgpu_accel* acc = const_cast<lmgpu_accel*>(a);
+    cudaStream_t s = 0;
+    if ((rc = ensure_packed(acc, s))) return rc;
+    // page-locked buffers: the kernel reads the rays and hits and writes the
+    // planes across the host link in place
+    const void* m_rays = mapped_host(rays);
+    const void* m_hits = mapped_host(hits);
+    const void* m_out = mapped_host(surface);
+    if (m_rays && m_hits && m_out && !(((uintptr_t)m_rays | (uintptr_t)m_hits) & 15u) && !((uintptr_t)m_out & 3u)) {
+        rc = launch_surface(a, static_cast<const float*>(m_rays), static_cast<const lmgpu_hit*>(m_hits), n,
+                            const_cast<float*>(static_cast<const float*>(m_out)), s);
+        if (rc) return rc;
+        return surface_status(a, s);
     }
-    rc = launch_surface(a, d_rays, d_hits, n, d_out, 0);
-    if (rc == LMGPU_OK) {
-        e = cudaMemcpy(surface, d_out, sizeof(float) * LMGPU_SURFACE_PLANES * n, cudaMemcpyDeviceToHost);
-        uint32_t st = 0;
-        if (e == cudaSuccess) e = cudaMemcpy(&st, a->status, sizeof(st), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) {
-            set_error(std::string("lmgpu_surface: ") + cudaGetErrorString(e));
-            rc = LMGPU_ERR_CUDA;
-        } else if (st & kStatusBadTree) {
-            set_error("lmgpu_surface: the accel's triangle table is malformed");
-            rc = LMGPU_ERR_OVERFLOW;
-        }
+    // pageable buffers: chunks through a staging buffer kept by the accel
+    constexpr uint64_t kChunkHits = 1ull << 20;
+    constexpr uint64_t kPerHit = 32 + sizeof(lmgpu_hit) + 4 * LMGPU_SURFACE_PLANES;
+    std::lock_guard<std::mutex> lock(acc->surf_mu);
+    const uint64_t want = n < kChunkHits ? n : kChunkHits;
+    if (acc->surf_stage_cap < want) {
+        if (acc->surf_stage) cudaFree(acc->surf_stage);
+        acc->surf_stage = nullptr;
+        acc->surf_stage_cap = 0;
+        LMGPU_CUDA_TRY(cudaMalloc((void**)&acc->surf_stage, want * kPerHit));
+        acc->surf_stage_cap = want;
     }
-    release();
-    return rc;
+    const uint64_t cap = acc->surf_stage_cap;
+    float* d_rays = reinterpret_cast<float*>(acc->surf_stage);
+    lmgpu_hit* d_hits = reinterpret_cast<lmgpu_hit*>(acc->surf_stage + cap * 32);
+    float* d_out = reinterpret_cast<float*>(acc->surf_stage + cap * (32 + sizeof(lmgpu_hit)));
+    for (uint64_t off = 0; off < n; off += cap) {
+        const uint64_t m = (n - off) < cap ? (n - off) : cap;
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(d_rays, rays + 8 * off, m * 32, cudaMemcpyHostToDevice, s));
+        LMGPU_CUDA_TRY(cudaMemcpyAsync(d_hits, hits + off, m * sizeof(lmgpu_hit), cudaMemcpyHostToDevice, s));
+        if ((rc = launch_surface(a, d_rays, d_hits, m, d_out, s))) return rc;
+        // plane k of the chunk -> surface[k n + off ...]
+        LMGPU_CUDA_TRY(cudaMemcpy2DAsync(surface + off, n * sizeof(float), d_out, m * sizeof(float),
+                                         m * sizeof(float), LMGPU_SURFACE_PLANES, cudaMemcpyDeviceToHost, s));
+    }
+    return surface_status(a, s);
 }

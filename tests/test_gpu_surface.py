@@ -89,6 +89,35 @@ def test_surface_of_traced_hits(gpu_lib, oracle_lib):
     acc.surface_device(d_rays.data_ptr(), d_hits.data_ptr(), rays.shape[0], d_out.data_ptr())
     acc.check()
     assert np.array_equal(d_out.cpu().numpy().T, out)
+    # page-locked host buffers are read and written in place
+    p_rays = torch.from_numpy(rays).pin_memory()
+    p_hits = torch.from_numpy(h.view(np.float32).reshape(-1, 4).copy()).pin_memory()
+    p_out = torch.full((23, rays.shape[0]), -3.0, dtype=torch.float32).pin_memory()
+    assert gpu_lib.lib().lmgpu_surface(acc.handle, p_rays.data_ptr(), p_hits.data_ptr(), rays.shape[0],
+                                       p_out.data_ptr()) == 0
+    assert np.array_equal(p_out.numpy().T, out)
+    acc.close()
+
+
+def test_surface_host_entry_in_chunks(gpu_lib):
+    """Pageable host buffers of more hits than one staging chunk (2^20):
+    the planes of every chunk land at their offsets in the caller's planes."""
+    import torch
+    from lmgpu import scenes
+
+    tris = scenes.random_soup(5000, 3)
+    rays = scenes.raycast_rays((1 << 20) + 4097, stream=5)
+    acc = gpu_lib.Accel()
+    acc.build(tris)
+    h = acc.trace(rays)
+    out = acc.surface(rays, h)
+    d_rays = torch.from_numpy(rays).cuda()
+    d_hits = torch.from_numpy(h.view(np.float32).reshape(-1, 4).copy()).cuda()
+    d_out = torch.empty((23, rays.shape[0]), dtype=torch.float32, device="cuda")
+    acc.surface_device(d_rays.data_ptr(), d_hits.data_ptr(), rays.shape[0], d_out.data_ptr())
+    acc.check()
+    assert (h["prim"] >= 0).sum() > 1000
+    assert np.array_equal(d_out.cpu().numpy().T, out)
     acc.close()
 
 
