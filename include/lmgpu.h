@@ -558,7 +558,7 @@ int lmgpu_surface_device(const lmgpu_accel* accel, const float* d_rays, const lm
  * allocate (a plugin inside a host that owns all device memory through its
  * own pool, or a query path that must not incur the device-wide
  * synchronisation of cudaMalloc/cudaFree).  All scratch, including the BVH,
- * is one fixed library-owned device array of about 5.2 MiB, reserved on
+ * is one fixed library-owned device array of about 5.4 MiB, reserved on
  * every device that loads the library until the process exits; scenes
  * above LMGPU_STATIC_MAX_TRIANGLES are rejected with LMGPU_ERR_INVALID.
  * The first call on a device looks up that array's address (set-up), so

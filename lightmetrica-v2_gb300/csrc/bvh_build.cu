@@ -8,12 +8,12 @@
 //
 //   1. large phase, one level per iteration: every task (node) with more than
 //      kSmallTask primitives is binned by all blocks covering its range
-//      (32 centroid bins on each of the three axes, shared-memory atomics,
+//      (64 centroid bins on each of the three axes, shared-memory atomics,
 //      then one global flush per block), the best SAH split over all axes is
 //      chosen by one warp per task, and the range is partitioned stably
 //      (chunk counts -> per-task scan -> scatter);
 //   2. small phase: one block per remaining task builds its whole subtree in
-//      shared memory (32 bins per axis, stable block partition); subtrees of
+//      shared memory (64 bins per axis, stable block partition); subtrees of
 //      at most kTinyTask triangles are finished by one thread;
 //   3. collapse: a top-down pass turns the binary tree into 8-wide nodes,
 //      expanding the child of largest surface area until 8 children exist,
@@ -38,8 +38,8 @@
 namespace lmgpu {
 namespace {
 
-constexpr int kBinsLarge = 32;
-constexpr int kBinsSmall = 32;
+constexpr int kBinsLarge = 64;
+constexpr int kBinsSmall = 64;
 constexpr int kBinWords = 13;  // count, aabb lo[3], aabb hi[3], centroid lo[3], centroid hi[3]
 constexpr int kChunk = 2048;   // primitives per block in the large phase
 constexpr int kLargeThreads = 256;
@@ -1424,7 +1424,7 @@ constexpr StaticLayout kSL = make_static_layout();
 }  // namespace
 }  // namespace lmgpu
 
-// The scratch itself (about 5.2 MiB for 16,384 triangles).  Host code must
+// The scratch itself (about 5.4 MiB for 16,384 triangles).  Host code must
 // not pass this name to a kernel: on the host it is only a stand-in symbol.
 static __device__ __align__(256) unsigned char g_static_scratch[lmgpu::kSL.total];
 
