@@ -82,9 +82,11 @@ namespace lmgpu {
 // accel's wide nodes.  d_tris: float[ntri*9] on the device.
 int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t stream);
 
-// Launches the traversal kernel over n rays.
+struct TraceProbe;
+
+// Launches the traversal kernel over n rays.  probe: see TraceProbe.
 int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, uint64_t n, bool anyhit,
-                 bool stats, cudaStream_t stream);
+                 bool stats, cudaStream_t stream, TraceProbe* probe = nullptr);
 
 // Instrumentation of a renderer's traversal launches (the dominant kernel of
 // every wavefront renderer), off unless a scene asks for it.

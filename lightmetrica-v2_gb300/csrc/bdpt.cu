@@ -852,7 +852,7 @@ int render_bdpt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, flo
             k_bd_connect<<<blocks(n_items, kBdptThreads), kBdptThreads, 0, stream>>>(C, w, B.items, n_items,
                                                                                    B.c_rays, B.c_rec);
             LMGPU_CUDA_TRY(cudaGetLastError());
-            if ((rc = launch_trace(sc->accel, B.c_rays, B.c_hit, n_items, true, false, stream))) return rc;
+            if ((rc = launch_trace(sc->accel, B.c_rays, B.c_hit, n_items, true, false, stream, sc->probe))) return rc;
             k_bd_splat<<<blocks(n_items, 256), 256, 0, stream>>>(w, B.items, n_items, B.c_rec, B.c_hit, sc->film_x,
                                                                   sc->film_x_sq);
             LMGPU_CUDA_TRY(cudaGetLastError());

@@ -26,14 +26,23 @@
 namespace lmgpu {
 namespace {
 
-constexpr int kTraceThreads = 128;
-// Resident blocks per SM the kernel is compiled for (64 registers a thread).
-constexpr int kTraceBlocksPerSM = 8;
+// One 1024-thread block per SM (64 registers a thread, the whole register
+// file): the SM's 32 warps share one ray counter, so they stay busy until the
+// SM's last rays (eight 128-thread blocks with fixed ranges left SMs idling
+// as their blocks ran dry: 1,540 against 1,667 Mrays/s on the ray-cast
+// benchmark).
+constexpr int kTraceThreads = 1024;
+// Resident blocks per SM the kernel is compiled for.
+constexpr int kTraceBlocksPerSM = 1;
 
-// Persistent traversal.  Each block owns the contiguous ray range
-// [blockIdx * n / grid, (blockIdx + 1) * n / grid) and its warps take rays
-// from it through a shared-memory counter, so no global state outlives a
-// launch and concurrent launches on other streams are independent.
+// Persistent traversal.  Each block owns the chunks blockIdx, blockIdx +
+// grid, ... of 256 consecutive rays and its warps take rays from them
+// through a shared-memory counter over the block's local index, so no global
+// state outlives a launch and concurrent launches on other streams are
+// independent.  The interleaving gives every block a mix of the whole range:
+// renderers queue rays in an order where cost varies along the queue (the
+// bidirectional tracer's connection rays are bucketed by strategy), and
+// contiguous ranges left some blocks with far more work than others.
 //
 // Per warp, every iteration of the main loop:
 //   1. refill: when at least `refill` lanes are idle, they take new rays
@@ -50,8 +59,8 @@ constexpr int kTraceBlocksPerSM = 8;
 // BVH tab[ray_scene[i]] (the batch renderer's views).  d_n, when not null,
 // holds the ray count on the device (launches captured in CUDA graphs).
 // SMALL: the same kernel as a separate function whose shared-memory
-// carveout is the smallest that holds eight blocks (the largest L1 at full
-// occupancy), launched for BVHs that fit in L1.
+// carveout is the smallest that holds its resident blocks (the largest L1 at
+// full occupancy), launched for BVHs that fit in L1.
 template <bool ANYHIT, bool STATS, bool MULTI, bool SMALL = false>
 __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(const WNode* __restrict__ nodes, const WTri* __restrict__ tris,
                                                          const float4* __restrict__ rays, lmgpu_hit* __restrict__ hits,
@@ -69,8 +78,13 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(cons
     __shared__ uint8_t s_perm[8 * 256];
     for (uint32_t i = threadIdx.x; i < 8u * 256u; i += blockDim.x) s_perm[i] = (uint8_t)permute_octant(i & 255u, i >> 8);
     if (d_n) n = *d_n;
-    const uint64_t begin = (uint64_t)blockIdx.x * n / gridDim.x;
-    const uint64_t end = (uint64_t)(blockIdx.x + 1) * n / gridDim.x;
+    // the block's rays: chunks blockIdx.x, + gridDim.x, ... of kChunkRays
+    // consecutive rays, counted by a local index (chunk k of the block, ray
+    // o of the chunk) so that every block sees a mix of the whole range
+    constexpr uint64_t kChunkRays = 256;
+    const uint64_t nchunks = (n + kChunkRays - 1) / kChunkRays;
+    const uint64_t my_chunks = blockIdx.x < nchunks ? (nchunks - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    const uint64_t begin = 0, end = my_chunks * kChunkRays;
     if (threadIdx.x == 0) s_next = begin;
     __syncthreads();
     const unsigned FULL = 0xffffffffu;
@@ -102,8 +116,9 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(cons
             base = __shfl_sync(FULL, base, leader);
             if (base + __popc(idle) >= end) exhausted = true;
             if (!active) {
-                const uint64_t id = base + __popc(idle & lt_mask);
-                if (id < end) {
+                const uint64_t li = base + __popc(idle & lt_mask);
+                const uint64_t id = ((li / kChunkRays) * gridDim.x + blockIdx.x) * kChunkRays + li % kChunkRays;
+                if (li < end && id < n) {
                     rid = id;
                     // rays and hits stream through once: cache-streaming
                     // accesses leave L1 / L2 to the BVH
@@ -243,9 +258,9 @@ int grid_cap_of()
         if (SMALL) {
             // The smallest carveout that still holds kTraceBlocksPerSM blocks
             // (static shared memory plus the per-block reservation): the
-            // carveout is honoured even where it costs occupancy, and the
-            // 2 KB mask table alone does not fit eight blocks in the
-            // minimum one.
+            // carveout is honoured even where it costs occupancy (with
+            // eight 128-thread blocks, the 2 KB mask table did not fit them
+            // in the minimum one).
             cudaFuncAttributes fa{};
             int smem_sm = 0, reserved = 0;
             LMGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, k_trace<ANYHIT, STATS, MULTI, SMALL>));
@@ -284,9 +299,19 @@ int trace_grid_cap()
 }
 
 int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, uint64_t n, bool anyhit, bool stats,
-                 cudaStream_t stream)
+                 cudaStream_t stream, TraceProbe* probe)
 {
     if (n == 0) return LMGPU_OK;
+    if (probe && probe->mode != TraceProbe::kOff) probe->launches++;
+    // a counting probe takes the counting instantiation with its counters
+    unsigned long long* cnt = a->counters;
+    if (probe && probe->mode == TraceProbe::kProbeCount) {
+        stats = true;
+        cnt = probe->d_counters;
+    }
+    const bool timed = probe && probe->mode == TraceProbe::kProbeTime && probe->used + 2 <= probe->events.size();
+    if (probe && probe->mode == TraceProbe::kProbeTime && !timed) probe->overflow = true;
+    if (timed) LMGPU_CUDA_TRY(cudaEventRecord(probe->events[probe->used], stream));
     const int grid_cap = anyhit ? (stats ? grid_cap_of<true, true, false>() : grid_cap_of<true, false, false>())
                                 : (stats ? grid_cap_of<false, true, false>() : grid_cap_of<false, false, false>());
     if (grid_cap <= 0) return LMGPU_ERR_CUDA;
@@ -296,12 +321,15 @@ int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, 
     const unsigned grid = (unsigned)(by_rays < (uint64_t)grid_cap ? by_rays : (uint64_t)grid_cap);
     const uint32_t nn = a->ntri > 0 ? (uint32_t)a->num_wide : 0u;
     const uint32_t nt = (uint32_t)a->ntri;
-    auto* cnt = a->counters;
     auto k = anyhit ? (stats ? k_trace<true, true, false> : k_trace<true, false, false>)
                     : (stats ? k_trace<false, true, false> : k_trace<false, false, false>);
     k<<<grid, kTraceThreads, 0, stream>>>(a->nodes, a->tris, d_rays, d_hits, n, nn, nt, cfg.refill, cfg.postpone,
                                           a->status, cnt, nullptr, 0u, nullptr, nullptr);
     LMGPU_CUDA_TRY(cudaGetLastError());
+    if (timed) {
+        LMGPU_CUDA_TRY(cudaEventRecord(probe->events[probe->used + 1], stream));
+        probe->used += 2;
+    }
     return LMGPU_OK;
 }
 
@@ -329,7 +357,7 @@ int launch_trace_dn(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hit
     if (timed) LMGPU_CUDA_TRY(cudaEventRecord(probe->events[probe->used], stream));
     // closest hit in a BVH that fits in L1 (nodes and triangles within 96 KiB)
     // runs the SMALL instantiation: the smallest shared-memory carveout that
-    // holds eight blocks, i.e. the largest L1 (measured +4 % on a 36-triangle
+    // holds its blocks, i.e. the largest L1 (measured +4 % on a 36-triangle
     // scene and -6 % on the 1.5M-triangle ray-cast scene)
     const bool small = !anyhit && (uint64_t)a->num_wide * sizeof(WNode) + a->ntri * sizeof(WTri) <= (96u << 10);
     const int grid_cap = small ? grid_cap_of<false, false, false, true>()
