@@ -124,6 +124,38 @@ def test_small_and_edge_sizes(gpu_lib, oracle_lib, ntri):
     assert c["unexplained"] == [], c
 
 
+@pytest.mark.parametrize("anyhit", [False, True])
+def test_every_ray_count_traces_every_ray_once(gpu_lib, anyhit):
+    """The persistent grid hands rays to blocks in interleaved 256-ray chunks:
+    for counts around the chunk and grid boundaries (fewer rays than blocks,
+    a partial last chunk, exactly one chunk per block ...) every ray's hit
+    equals its hit in one large launch, and hits past the count stay
+    untouched."""
+    import torch
+    from lmgpu import scenes
+
+    tris = scenes.raycast_scene(30_000, 32, seed=21)
+    nmax = 152 * 1024 * 2 + 777
+    rays = scenes.raycast_rays(nmax, seed=22)
+    acc = gpu_lib.Accel()
+    acc.build(tris)
+    s = torch.cuda.current_stream().cuda_stream
+    dr = torch.from_numpy(rays).cuda()
+    full = torch.empty((nmax, 4), dtype=torch.float32, device="cuda")
+    acc.trace_device(dr.data_ptr(), full.data_ptr(), nmax, anyhit, s)
+    acc.check(s)
+    ref = full.cpu().numpy().view(gpu_lib.HIT_DTYPE).reshape(-1)
+    for n in (1, 31, 255, 256, 257, 4095, 4097, 151 * 256, 152 * 256, 152 * 256 + 1, 152 * 1024, nmax - 1):
+        out = torch.full((nmax, 4), -5.0, dtype=torch.float32, device="cuda")
+        acc.trace_device(dr.data_ptr(), out.data_ptr(), n, anyhit, s)
+        acc.check(s)
+        h = out.cpu().numpy().view(gpu_lib.HIT_DTYPE).reshape(-1)
+        assert np.array_equal(h["prim"][:n], ref["prim"][:n]), n
+        assert np.array_equal(h["t"][:n], ref["t"][:n]), n
+        assert (out[n:].cpu().numpy() == -5.0).all(), n
+    acc.close()
+
+
 def test_medium_scene_vs_oracle(gpu_lib, oracle_lib):
     from lmgpu import scenes
 
