@@ -17,7 +17,9 @@
 //               two BF16 terms), so the epilogue is ReLU and BF16 rounding in
 //               one conversion per pair; the feature encoding and the
 //               epilogue run one row per thread, reading the row with
-//               tcgen05.ld.
+//               tcgen05.ld.  The raw outputs of a tile are staged in the
+//               group's activation tiles (free after the last layer) and
+//               leave with one bulk copy.
 //               MODE_TRAIN also copies every layer's input tile, as the
 //               shared-memory image the MMAs read, to global memory with one
 //               bulk copy per layer, and writes the raw outputs, for the
@@ -300,6 +302,9 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
     if (first < ntiles && full_tile(first)) fetch_queries(first);
     for (uint32_t tile = first; tile < ntiles && alive; tile += stride) {
         const uint32_t row = tile * kTile + r;
+        // the previous tile's output copy reads X and Y: done before they
+        // are rewritten (the barrier below orders the other threads)
+        if (r == 0) tc::bulk_wait_read0();
         // features of the row's query (guide_net.cuh): per axis 16 frequencies
         // (sin, cos), then the normal and the outgoing direction, then zeros;
         // stored eight at a time
@@ -318,6 +323,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
                 }
                 for (int j = 0; j < 9; j++) q9[j] = sq[9 * r + j];
             } else {
+                group_sync(g);
                 for (int j = 0; j < 9; j++) q9[j] = row < n ? queries[9 * (size_t)row + j] : 0.0f;
             }
             // features 0..63 (axes x, y) into X, 64..127 (axis z, normal,
@@ -381,20 +387,25 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_guide_fwd(const float* __res
 #pragma unroll
                 for (int c = 0; c < kOut; c += 16) tc::tmem_load16(tc::tmem_at(tmem, lane_base, c), z + c);
                 tc::tmem_wait_ld();
-                if (row < n) {
-                    float4* dst = reinterpret_cast<float4*>(raw_out + (size_t)row * kOutUsed);
-                    for (int c = 0; c < kOutUsed; c += 4)
-                        dst[c / 4] = make_float4(z[c], z[c + 1], z[c + 2], z[c + 3]);
-                }
+                // the row into the group's activation tiles, free now (160 B
+                // rows, as raw_out holds them), for one bulk copy of the tile
+                float4* srow = reinterpret_cast<float4*>(bufX + (size_t)r * kOutUsed * 4u);
+#pragma unroll
+                for (int c = 0; c < kOutUsed; c += 4) srow[c / 4] = make_float4(z[c], z[c + 1], z[c + 2], z[c + 3]);
             }
             group_sync_for_mma(g);
+            if (l == 4 && r == 0) {
+                const uint32_t rows = n - tile * kTile < (uint32_t)kTile ? n - tile * kTile : (uint32_t)kTile;
+                tc::bulk_store(raw_out + (size_t)tile * kTile * kOutUsed, sX, rows * kOutUsed * 4u);
+                tc::bulk_commit();
+            }
         }
     }
     // after a time-out, one more bounded wait for this group's MMAs and its
     // query copy in flight
     if (!alive) tc::mbar_wait(bar, phase ^ 1u, kWaitLimit);
     if (q_pending) tc::mbar_wait(qbar, qphase, kWaitLimit);
-    if (MODE == MODE_TRAIN && r == 0) tc::bulk_wait0();
+    if (r == 0) tc::bulk_wait0();
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
