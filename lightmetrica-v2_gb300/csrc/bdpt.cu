@@ -544,12 +544,11 @@ __global__ void k_bd_buckets(uint32_t* __restrict__ hist, uint32_t* __restrict__
 // a time: the s, t >= 1 connections as sample | s << 22 | t << 27, and the
 // s = 0 strategies (Path::Connect, :245-275; no visibility ray: the eye
 // subpath's own rays found the light) as sample | d << 21 | t << 27.
-__global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ offset, uint32_t* __restrict__ cursor,
-                           uint32_t* __restrict__ items)
+// The (s, t) buckets of one sample, in a fixed order; visit(b, m, lane-has,
+// item) for each, with m the warp's ballot of the samples that have it.
+template <typename F>
+__device__ __forceinline__ void for_each_bucket(const Ctx& C, int nL, int nE, uint32_t i, F visit)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned lane = threadIdx.x & 31u;
-    const int nL = i < w.n ? w.count[0][i] : 0, nE = i < w.n ? w.count[1][i] : 0;
     const int sw = __reduce_max_sync(0xffffffffu, nL);
     for (int s = 1; s <= sw; s++) {
         const int tm = s <= nL ? t_limit(s, nE, C.max_path) : 0;
@@ -557,13 +556,7 @@ __global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ offset, u
         for (int t = 1; t <= tw; t++) {
             const bool has = t <= tm;
             const unsigned m = __ballot_sync(0xffffffffu, has);
-            const int b = s * kStrideST + t;
-            uint32_t base = 0;
-            if (lane == (unsigned)(__ffs(m) - 1)) base = atomicAdd(&cursor[b], (uint32_t)__popc(m));
-            base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
-            if (has)
-                items[offset[b] + base + __popc(m & ((1u << lane) - 1u))] =
-                    i | ((uint32_t)s << kItemS) | ((uint32_t)t << kItemT);
+            visit(s * kStrideST + t, m, has, i | ((uint32_t)s << kItemS) | ((uint32_t)t << kItemT));
         }
     }
     // s = 0: i | d << 21 | t << 27
@@ -572,16 +565,38 @@ __global__ void k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ offset, u
     for (int t = 2; t <= t0w; t++) {
         const bool has = t <= t0;
         const unsigned m = __ballot_sync(0xffffffffu, has);
-        for (int d = 0; d < 2; d++) {
-            const int b = bucket_s0(t, d);
-            uint32_t base = 0;
-            if (lane == (unsigned)(__ffs(m) - 1)) base = atomicAdd(&cursor[b], (uint32_t)__popc(m));
-            base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
-            if (has)
-                items[offset[b] + base + __popc(m & ((1u << lane) - 1u))] =
-                    i | ((uint32_t)d << kItemD) | ((uint32_t)t << kItemT);
-        }
+        for (int d = 0; d < 2; d++)
+            visit(bucket_s0(t, d), m, has, i | ((uint32_t)d << kItemD) | ((uint32_t)t << kItemT));
     }
+}
+
+// Two passes over the same buckets: the block's count per bucket (shared
+// atomics, one per warp and bucket), one global reservation per bucket and
+// block, then each warp's positions inside the block's range.
+__global__ void __launch_bounds__(256) k_bd_items(Ctx C, Wave w, const uint32_t* __restrict__ offset,
+                                                  uint32_t* __restrict__ cursor, uint32_t* __restrict__ items)
+{
+    __shared__ uint32_t s_pos[kBuckets];
+    for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) s_pos[k] = 0u;
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned lane = threadIdx.x & 31u;
+    const int nL = i < w.n ? w.count[0][i] : 0, nE = i < w.n ? w.count[1][i] : 0;
+    for_each_bucket(C, nL, nE, i, [&](int b, unsigned m, bool, uint32_t) {
+        if (lane == (unsigned)(__ffs(m) - 1)) atomicAdd(&s_pos[b], (uint32_t)__popc(m));
+    });
+    __syncthreads();
+    for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) {
+        const uint32_t c = s_pos[k];
+        s_pos[k] = c ? offset[k] + atomicAdd(&cursor[k], c) : 0u;
+    }
+    __syncthreads();
+    for_each_bucket(C, nL, nE, i, [&](int b, unsigned m, bool has, uint32_t item) {
+        uint32_t base = 0;
+        if (lane == (unsigned)(__ffs(m) - 1)) base = atomicAdd(&s_pos[b], (uint32_t)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+        if (has) items[base + __popc(m & ((1u << lane) - 1u))] = item;
+    });
 }
 
 // One connection (Path::Connect, :298-330): the full path L[0..s-1] E[t-1..0],
