@@ -29,7 +29,7 @@
 //   per bounce      k_trace (closest hit, trace.cu) over the compacted queue,
 //                   its length read on the device (no host round trip);
 //                   k_pt_shade: emission (MIS-weighted for ptmis), roulette,
-//                   BSDF sampling, warp-aggregated append of surviving paths;
+//                   BSDF sampling, block-aggregated append of surviving paths;
 //                   ptmis: the new vertex's light sample as a shadow ray plus
 //                   a pending contribution, then k_trace (any hit) over the
 //                   shadow rays and k_pt_nee_splat
@@ -256,16 +256,26 @@ __global__ void __launch_bounds__(kShadeThreads, 4) k_pt_shade(Ctx C, const floa
         }
     }
     if (NEE) append_nee(has_nee, v, L, c, pixel, path, nrays, nrec, npath, ncount);
-    // warp-aggregated append to the next queue
+    // block-aggregated append to the next queue: one global atomic per block
+    // (one per warp serialised on the queue counter)
+    __shared__ uint32_t s_warp[kShadeThreads / 32];
+    __shared__ uint32_t s_base;
     const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (m == 0u) return;
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned leader = __ffs(m) - 1u;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(out_count, (uint32_t)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    if (lane == 0u) s_warp[warp] = (uint32_t)__popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (int k = 0; k < kShadeThreads / 32; k++) {
+            const uint32_t cw = s_warp[k];
+            s_warp[k] = tot;
+            tot += cw;
+        }
+        s_base = tot ? atomicAdd(out_count, tot) : 0u;
+    }
+    __syncthreads();
     if (keep) {
-        const uint32_t o = base + __popc(m & ((1u << lane) - 1u));
+        const uint32_t o = s_base + s_warp[warp] + __popc(m & ((1u << lane) - 1u));
         out_rays[2 * o] = nr0;
         out_rays[2 * o + 1] = nr1;
         out_state[o] = ns;
