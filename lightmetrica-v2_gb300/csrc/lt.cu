@@ -64,20 +64,14 @@ __device__ __forceinline__ bool sensor_connect(const Ctx& C, const PV& v, int ty
     return any;
 }
 
-// Warp-aggregated append of a path to the next queue; every lane calls it.
+// Append of a path to the next queue, one queue-counter atomic per block;
+// every thread of the block calls it (block_append_slot).
 __device__ __forceinline__ void append_path(bool keep, float4 r0, float4 r1, const PathState& s,
                                             float4* __restrict__ rays, PathState* __restrict__ state,
                                             uint32_t* __restrict__ count)
 {
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (m == 0u) return;
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned leader = __ffs(m) - 1u;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
+    const uint32_t o = block_append_slot<kLtThreads / 32>(keep, count);
     if (keep) {
-        const uint32_t o = base + __popc(m & ((1u << lane) - 1u));
         rays[2 * o] = r0;
         rays[2 * o + 1] = r1;
         state[o] = s;
