@@ -80,6 +80,19 @@ namespace lmgpu {
 
 // Builds the binned-SAH binary tree on the device and collapses it into the
 // accel's wide nodes.  d_tris: float[ntri*9] on the device.
+// The device address of a page-locked (cudaHostAlloc / cudaHostRegister)
+// host buffer, or null for pageable memory and any other kind: the host
+// entry points trace such buffers in place across the host link.
+inline const void* mapped_host(const void* p)
+{
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // an unknown pointer leaves a (non-sticky) error behind
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int build_bvh(lmgpu_accel* a, const float* d_tris, uint64_t ntri, cudaStream_t stream);
 
 struct TraceProbe;

@@ -62,18 +62,6 @@ constexpr size_t kSmallHitsOff = kSmallRays * 32;
 constexpr size_t kSmallStatusOff = kSmallHitsOff + kSmallRays * sizeof(lmgpu_hit);
 constexpr size_t kSmallBytes = kSmallStatusOff + 16;
 
-// The device address of a page-locked host buffer, or null for pageable
-// memory (or any other kind).
-const void* mapped_host(const void* p)
-{
-    cudaPointerAttributes at{};
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-        cudaGetLastError();  // clear the sticky-free error of an unknown pointer
-        return nullptr;
-    }
-    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
-}
-
 // n <= kSmallRays rays from host memory: the kernel reads the rays from and
 // writes the hits to the pinned, mapped buffer directly.  Caller holds host_mu.
 int trace_small(lmgpu_accel* a, const float* rays, lmgpu_hit* hits, uint64_t n, int anyhit)

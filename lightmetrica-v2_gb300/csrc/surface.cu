@@ -218,18 +218,6 @@ int launch_surface(const lmgpu_accel* ca, const float* d_rays, const lmgpu_hit* 
     return LMGPU_OK;
 }
 
-// The device address of a page-locked host buffer, or null for pageable
-// memory (or any other kind).
-const void* mapped_host(const void* p)
-{
-    cudaPointerAttributes at{};
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
-    }
-    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
-}
-
 // Waits for stream s and turns the accel's status word into an error.
 int surface_status(const lmgpu_accel* a, cudaStream_t s)
 {
