@@ -95,4 +95,38 @@ struct __align__(16) WTri {
     float4 v0, v1, v2;
 };
 
+// A queue slot for every thread of a kWarps-warp block with take set, with
+// one global atomic on *count per block (ordered by warp, then lane);
+// threads without take get an unused value.  Every thread of the block must
+// call it: it synchronises the block, so it is called only at the top level
+// of kernels without early returns; a second call in the same kernel needs a
+// __syncthreads() after the first one's slot has been taken.
+template <int kWarps>
+__device__ __forceinline__ uint32_t block_append_slot(bool take, uint32_t* __restrict__ count)
+{
+    static_assert(kWarps >= 1 && kWarps <= 32, "one scan warp covers the block");
+    __shared__ uint32_t s_off[kWarps];
+    const unsigned m = __ballot_sync(0xffffffffu, take);
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    if (lane == 0u) s_off[warp] = (uint32_t)__popc(m);
+    __syncthreads();
+    if (warp == 0u) {
+        // the warps' counts scanned by warp 0, one atomic for the block's total
+        const uint32_t c = lane < (unsigned)kWarps ? s_off[lane] : 0u;
+        uint32_t x = c;
+#pragma unroll
+        for (unsigned o = 1; o < 32u; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        const uint32_t tot = __shfl_sync(0xffffffffu, x, 31);
+        uint32_t base = 0u;
+        if (lane == 0u && tot) base = atomicAdd(count, tot);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (lane < (unsigned)kWarps) s_off[lane] = base + x - c;
+    }
+    __syncthreads();
+    return s_off[warp] + (uint32_t)__popc(m & ((1u << lane) - 1u));
+}
+
 }  // namespace lmgpu
