@@ -496,7 +496,8 @@ def single_ray_latency(acc, rays, anyhit: bool, calls: int = 2000) -> dict:
 
 
 def render_trace_roofline(sc, render, step_ms: float, flush) -> dict:
-    """Roofline of a render's dominant kernel, its traversal launches: one
+    """Roofline of a render's dominant kernel, its traversal launches (sc: the
+    Scene or Batch whose trace profile is read): one
     render (seed of the first timed step) with the counting traversal for
     rays, node and triangle fetches, then the same render with CUDA events
     around each production traversal launch (the library's trace profile),
@@ -773,6 +774,14 @@ def run_batch(args) -> None:
     clk = clocks.stop()
     launches = b.launch_count() - l0
     ms = sum(a.elapsed_time(c) for a, c in evs) / args.steps
+    # the traversal launches of the first timed step's render, counted and
+    # then timed (bounces launched one by one while the profile is on)
+    with torch.cuda.stream(stream):
+        roofline = render_trace_roofline(
+            b, lambda seed: b.render_pt_device(d_img.data_ptr(), d_var.data_ptr(), spp, max_nv, seed, rr_depth,
+                                               stream.cuda_stream), ms, flush)
+    if roofline is not None:
+        roofline["kernel"] = "k_trace<MULTI> (the batch's multi-scene traversal launches)"
     t1 = time.perf_counter()
     e2e_steps = max(1, min(args.steps, 3))
     for k in range(e2e_steps):
@@ -790,7 +799,7 @@ def run_batch(args) -> None:
                        "l2": "flushed before every timed step (256 MiB write, untimed)"},
             "e2e": {"value": samples / e2e_s / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": npix * 3 * 4 * 2, "api": "lmgpu_batch_render_pt (host films)"},
-            "gpu_launches": launches, "clocks": clk}
+            "gpu_launches": launches, "clocks": clk, "roofline": roofline}
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import lmoracle

@@ -233,9 +233,10 @@ int lmgpu_scene_launch_count(const lmgpu_scene* scene, uint64_t* count);
 /* The scene's accel (owned by the scene), for ray queries on its triangles. */
 int lmgpu_scene_accel(const lmgpu_scene* scene, const lmgpu_accel** accel);
 
-/* Instrumentation of the traversal launches of this scene's renders, the
- * dominant kernel of every renderer (a diagnostic; no counterpart in the
- * reference).  Images are unchanged in every mode. */
+/* Instrumentation of the traversal launches of a scene's renders (and of a
+ * batch's, lmgpu_batch_set_trace_profile), the dominant kernel of every
+ * renderer (a diagnostic; no counterpart in the reference).  Images are
+ * unchanged in every mode. */
 enum {
     LMGPU_TRACE_PROFILE_OFF = 0,
     LMGPU_TRACE_PROFILE_COUNT = 1, /* launch the counting traversal: rays, node and triangle fetches, hits */
@@ -434,6 +435,14 @@ int lmgpu_batch_get_tuning(const lmgpu_batch* batch, lmgpu_batch_tuning* tuning)
 
 /* Kernels the batch renderer has launched so far (a diagnostic). */
 int lmgpu_batch_launch_count(const lmgpu_batch* batch, uint64_t* count);
+
+/* The trace profile (lmgpu_scene_set_trace_profile) of the batch's
+ * multi-scene traversal launches.  While a mode other than OFF is set, the
+ * bounces are launched one by one instead of through the captured graphs,
+ * so that every traversal launch can be counted or timed; images are
+ * unchanged. */
+int lmgpu_batch_set_trace_profile(lmgpu_batch* batch, int mode);
+int lmgpu_batch_read_trace_profile(lmgpu_batch* batch, lmgpu_trace_profile* out);
 
 /* ---- Learned path guiding: the network ----------------------------------
  * A small MLP (input: position with a 16-frequency encoding, normal,

@@ -136,8 +136,9 @@ struct AccelView {
 
 // Traversal of rays from several scenes in one launch (ray i against
 // d_tab[d_ray_scene[i]]), the ray count read from d_n on the device.
+// probe: see TraceProbe (NULL inside a graph capture).
 int launch_trace_multi(const AccelView* d_tab, uint32_t ntab, const float4* d_rays, const uint8_t* d_ray_scene,
                        lmgpu_hit* d_hits, const uint32_t* d_n, uint64_t max_n, bool anyhit, TraceConfig cfg,
-                       uint32_t* d_status, cudaStream_t stream);
+                       uint32_t* d_status, cudaStream_t stream, TraceProbe* probe = nullptr);
 
 }  // namespace lmgpu

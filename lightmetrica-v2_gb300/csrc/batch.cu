@@ -257,6 +257,7 @@ struct lmgpu_batch {
     bool graphs_ok = false;
     cudaStream_t stream = nullptr;
     uint64_t launches = 0;
+    lmgpu::TraceProbe* probe = nullptr;  // traversal instrumentation (lmgpu_batch_set_trace_profile)
 };
 
 namespace lmgpu {
@@ -286,31 +287,44 @@ int ensure_batch_queues(lmgpu_batch* b, uint64_t cap)
     return LMGPU_OK;
 }
 
-// Captures one bounce per queue parity c: traversal of queue c, then shading
-// from queue c into queue 1 - c.
+// Blocks of the shading launch of one bounce.
+int shade_grid_of(const lmgpu_batch* b, unsigned* grid)
+{
+    int dev = 0, sms = 0;
+    LMGPU_CUDA_TRY(cudaGetDevice(&dev));
+    LMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const uint64_t by_n = (b->cap + kBtThreads - 1) / kBtThreads;
+    *grid = (unsigned)(by_n < (uint64_t)sms * 8 ? by_n : (uint64_t)sms * 8);
+    return LMGPU_OK;
+}
+
+// One bounce from queue parity c on stream s: traversal of queue c, then
+// shading from queue c into queue 1 - c.  probe: NULL inside a capture.
+int launch_bounce(lmgpu_batch* b, int c, unsigned shade_grid, cudaStream_t s, TraceProbe* probe)
+{
+    int rc = launch_trace_multi(b->d_tab, b->nviews, b->rays[c], b->ray_scene[c], b->hits, b->d_n + c, b->cap,
+                                false, b->tune, b->d_status, s, probe);
+    if (rc) return rc;
+    if (cudaMemsetAsync(b->d_n + (1 - c), 0, sizeof(uint32_t), s) != cudaSuccess) return LMGPU_ERR_CUDA;
+    k_bt_shade<<<shade_grid, kBtThreads, 0, s>>>(b->d_views, b->d_args, b->d_n + c, b->rays[c], b->state[c], b->hits,
+                                                 b->own, b->rays[1 - c], b->state[1 - c], b->ray_scene[1 - c],
+                                                 b->d_n + (1 - c));
+    return cudaGetLastError() == cudaSuccess ? LMGPU_OK : LMGPU_ERR_CUDA;
+}
+
+// Captures one bounce per queue parity c (launch_bounce).
 int capture_bounces(lmgpu_batch* b)
 {
     if (b->graphs_ok) return LMGPU_OK;
     drop_graphs(b);
     if (trace_grid_cap() <= 0) return LMGPU_ERR_CUDA;  // looked up outside the capture
-    int dev = 0, sms = 0;
-    LMGPU_CUDA_TRY(cudaGetDevice(&dev));
-    LMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const uint64_t by_n = (b->cap + kBtThreads - 1) / kBtThreads;
-    const unsigned shade_grid = (unsigned)(by_n < (uint64_t)sms * 8 ? by_n : (uint64_t)sms * 8);
+    unsigned shade_grid = 0;
+    int rc = shade_grid_of(b, &shade_grid);
+    if (rc) return rc;
     for (int c = 0; c < 2; c++) {
         cudaGraph_t g = nullptr;
         LMGPU_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = launch_trace_multi(b->d_tab, b->nviews, b->rays[c], b->ray_scene[c], b->hits, b->d_n + c, b->cap,
-                                    false, b->tune, b->d_status, b->stream);
-        if (rc == LMGPU_OK && cudaMemsetAsync(b->d_n + (1 - c), 0, sizeof(uint32_t), b->stream) != cudaSuccess)
-            rc = LMGPU_ERR_CUDA;
-        if (rc == LMGPU_OK) {
-            k_bt_shade<<<shade_grid, kBtThreads, 0, b->stream>>>(b->d_views, b->d_args, b->d_n + c, b->rays[c],
-                                                                b->state[c], b->hits, b->own, b->rays[1 - c],
-                                                                b->state[1 - c], b->ray_scene[1 - c], b->d_n + (1 - c));
-            if (cudaGetLastError() != cudaSuccess) rc = LMGPU_ERR_CUDA;
-        }
+        rc = launch_bounce(b, c, shade_grid, b->stream, nullptr);
         const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
         if (rc != LMGPU_OK || e != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -351,7 +365,16 @@ int batch_render(lmgpu_batch* b, const lmgpu_batch_params* prm, float* d_image, 
     const uint64_t wave = b->wave < total ? b->wave : total;
     int rc = ensure_batch_queues(b, wave);
     if (rc) return rc;
-    if ((rc = capture_bounces(b))) return rc;
+    // a trace profile launches the bounces one by one (the probe records
+    // events and picks the counting traversal per launch); otherwise the
+    // captured graphs run
+    TraceProbe* probe = b->probe && b->probe->mode != TraceProbe::kOff ? b->probe : nullptr;
+    unsigned shade_grid = 0;
+    if (probe) {
+        if ((rc = shade_grid_of(b, &shade_grid))) return rc;
+    } else if ((rc = capture_bounces(b))) {
+        return rc;
+    }
     // unbounded paths (max_num_vertices -1) stop after kMaxBounces segments;
     // with roulette the survivors are a 2^-(kMaxBounces - rr_depth) fraction
     const int max_bounces = prm->max_num_vertices < 0 ? kMaxBounces : prm->max_num_vertices - 1;
@@ -363,7 +386,11 @@ int batch_render(lmgpu_batch* b, const lmgpu_batch_params* prm, float* d_image, 
         b->launches++;
         int cur = 0;
         for (int k = 0; k < max_bounces; k++) {
-            LMGPU_CUDA_TRY(cudaGraphLaunch(b->bounce[cur], s));
+            if (probe) {
+                if ((rc = launch_bounce(b, cur, shade_grid, s, probe))) return rc;
+            } else {
+                LMGPU_CUDA_TRY(cudaGraphLaunch(b->bounce[cur], s));
+            }
             b->launches += 2;  // traversal + shading
             cur = 1 - cur;
             const bool last = k + 1 == max_bounces;
@@ -464,6 +491,7 @@ void lmgpu_batch_destroy(lmgpu_batch* b)
     if (!b) return;
     if (b->stream) cudaStreamSynchronize(b->stream);
     drop_graphs(b);
+    free_probe(b->probe);
     void* ptrs[] = {b->d_tab, b->d_views, b->d_args, b->d_status, b->film, b->film_sq, b->d_image, b->d_variance,
                     b->rays[0], b->rays[1], b->state[0], b->state[1], b->ray_scene[0], b->ray_scene[1], b->hits,
                     b->own, b->d_n};
@@ -621,6 +649,26 @@ int lmgpu_batch_launch_count(const lmgpu_batch* b, uint64_t* count)
     }
     *count = b->launches;
     return LMGPU_OK;
+}
+
+int lmgpu_batch_set_trace_profile(lmgpu_batch* b, int mode)
+{
+    clear_error();
+    if (!b) {
+        set_error("lmgpu_batch_set_trace_profile: NULL batch");
+        return LMGPU_ERR_INVALID;
+    }
+    return set_probe(&b->probe, mode, "lmgpu_batch_set_trace_profile");
+}
+
+int lmgpu_batch_read_trace_profile(lmgpu_batch* b, lmgpu_trace_profile* out)
+{
+    clear_error();
+    if (!b || !out) {
+        set_error("lmgpu_batch_read_trace_profile: NULL argument");
+        return LMGPU_ERR_INVALID;
+    }
+    return read_probe(b->probe, out);
 }
 
 }  // extern "C"

@@ -45,6 +45,68 @@ void free_probe(TraceProbe* p)
     delete p;
 }
 
+int set_probe(TraceProbe** slot, int mode, const char* fn)
+{
+    if (mode < TraceProbe::kOff || mode > TraceProbe::kProbeTime) {
+        set_error(std::string(fn) + ": unknown mode");
+        return LMGPU_ERR_INVALID;
+    }
+    if (mode == TraceProbe::kOff) {
+        if (*slot) LMGPU_CUDA_TRY(cudaDeviceSynchronize());
+        free_probe(*slot);
+        *slot = nullptr;
+        return LMGPU_OK;
+    }
+    if (!*slot) {
+        *slot = new TraceProbe;
+        if (cudaMalloc((void**)&(*slot)->d_counters, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+            free_probe(*slot);
+            *slot = nullptr;
+            set_error(std::string(fn) + ": counter allocation failed");
+            return LMGPU_ERR_CUDA;
+        }
+    }
+    TraceProbe* p = *slot;
+    if (mode == TraceProbe::kProbeTime && p->events.empty()) {
+        p->events.resize(TraceProbe::kMaxEvents, nullptr);
+        for (auto& e : p->events) LMGPU_CUDA_TRY(cudaEventCreate(&e));
+    }
+    LMGPU_CUDA_TRY(cudaDeviceSynchronize());
+    LMGPU_CUDA_TRY(cudaMemset(p->d_counters, 0, 4 * sizeof(unsigned long long)));
+    p->mode = mode;
+    p->used = 0;
+    p->launches = 0;
+    p->overflow = false;
+    return LMGPU_OK;
+}
+
+int read_probe(TraceProbe* p, lmgpu_trace_profile* out)
+{
+    *out = lmgpu_trace_profile{};
+    if (!p) return LMGPU_OK;
+    LMGPU_CUDA_TRY(cudaDeviceSynchronize());
+    unsigned long long c[4] = {0, 0, 0, 0};
+    LMGPU_CUDA_TRY(cudaMemcpy(c, p->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
+    out->launches = p->launches;
+    out->rays = c[0];
+    out->node_fetches = c[1];
+    out->triangle_fetches = c[2];
+    out->hits = c[3];
+    double ms = 0.0;
+    for (size_t i = 0; i + 1 < p->used; i += 2) {
+        float e = 0.0f;
+        LMGPU_CUDA_TRY(cudaEventElapsedTime(&e, p->events[i], p->events[i + 1]));
+        ms += e;
+    }
+    out->device_ms = ms;
+    out->timed_launches = p->used / 2;
+    LMGPU_CUDA_TRY(cudaMemset(p->d_counters, 0, sizeof(c)));
+    p->used = 0;
+    p->launches = 0;
+    p->overflow = false;
+    return LMGPU_OK;
+}
+
 int ensure_film(lmgpu_scene* sc, uint64_t npix)
 {
     if (sc->film_cap >= npix) return LMGPU_OK;
@@ -336,37 +398,11 @@ int lmgpu_scene_launch_count(const lmgpu_scene* sc, uint64_t* count)
 int lmgpu_scene_set_trace_profile(lmgpu_scene* sc, int mode)
 {
     clear_error();
-    if (!sc || mode < TraceProbe::kOff || mode > TraceProbe::kProbeTime) {
-        set_error("lmgpu_scene_set_trace_profile: NULL scene or unknown mode");
+    if (!sc) {
+        set_error("lmgpu_scene_set_trace_profile: NULL scene");
         return LMGPU_ERR_INVALID;
     }
-    if (mode == TraceProbe::kOff) {
-        if (sc->probe) LMGPU_CUDA_TRY(cudaDeviceSynchronize());
-        free_probe(sc->probe);
-        sc->probe = nullptr;
-        return LMGPU_OK;
-    }
-    if (!sc->probe) {
-        sc->probe = new TraceProbe;
-        if (cudaMalloc((void**)&sc->probe->d_counters, 4 * sizeof(unsigned long long)) != cudaSuccess) {
-            free_probe(sc->probe);
-            sc->probe = nullptr;
-            set_error("lmgpu_scene_set_trace_profile: counter allocation failed");
-            return LMGPU_ERR_CUDA;
-        }
-    }
-    TraceProbe* p = sc->probe;
-    if (mode == TraceProbe::kProbeTime && p->events.empty()) {
-        p->events.resize(TraceProbe::kMaxEvents, nullptr);
-        for (auto& e : p->events) LMGPU_CUDA_TRY(cudaEventCreate(&e));
-    }
-    LMGPU_CUDA_TRY(cudaDeviceSynchronize());
-    LMGPU_CUDA_TRY(cudaMemset(p->d_counters, 0, 4 * sizeof(unsigned long long)));
-    p->mode = mode;
-    p->used = 0;
-    p->launches = 0;
-    p->overflow = false;
-    return LMGPU_OK;
+    return set_probe(&sc->probe, mode, "lmgpu_scene_set_trace_profile");
 }
 
 int lmgpu_scene_read_trace_profile(lmgpu_scene* sc, lmgpu_trace_profile* out)
@@ -376,30 +412,7 @@ int lmgpu_scene_read_trace_profile(lmgpu_scene* sc, lmgpu_trace_profile* out)
         set_error("lmgpu_scene_read_trace_profile: NULL argument");
         return LMGPU_ERR_INVALID;
     }
-    *out = lmgpu_trace_profile{};
-    TraceProbe* p = sc->probe;
-    if (!p) return LMGPU_OK;
-    LMGPU_CUDA_TRY(cudaDeviceSynchronize());
-    unsigned long long c[4] = {0, 0, 0, 0};
-    LMGPU_CUDA_TRY(cudaMemcpy(c, p->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
-    out->launches = p->launches;
-    out->rays = c[0];
-    out->node_fetches = c[1];
-    out->triangle_fetches = c[2];
-    out->hits = c[3];
-    double ms = 0.0;
-    for (size_t i = 0; i + 1 < p->used; i += 2) {
-        float e = 0.0f;
-        LMGPU_CUDA_TRY(cudaEventElapsedTime(&e, p->events[i], p->events[i + 1]));
-        ms += e;
-    }
-    out->device_ms = ms;
-    out->timed_launches = p->used / 2;
-    LMGPU_CUDA_TRY(cudaMemset(p->d_counters, 0, sizeof(c)));
-    p->used = 0;
-    p->launches = 0;
-    p->overflow = false;
-    return LMGPU_OK;
+    return read_probe(sc->probe, out);
 }
 
 int lmgpu_scene_accel(const lmgpu_scene* sc, const lmgpu_accel** accel)

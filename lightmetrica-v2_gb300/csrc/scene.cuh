@@ -126,6 +126,12 @@ namespace lmgpu {
 int ensure_film(lmgpu_scene* sc, uint64_t npix);
 // Frees a traversal probe and its events (NULL is ignored).
 void free_probe(TraceProbe* p);
+// The trace-profile entry points of scenes and batches: set_probe selects the
+// mode of *slot (creating or freeing the probe) and clears its record;
+// read_probe waits for the device, returns the record and clears it (all
+// zero when p is NULL).  fn names the entry point in error messages.
+int set_probe(TraceProbe** slot, int mode, const char* fn);
+int read_probe(TraceProbe* p, lmgpu_trace_profile* out);
 int ensure_queues(lmgpu_scene* sc, uint64_t n);
 SceneGPU scene_view(const lmgpu_scene* sc);
 int clear_film(lmgpu_scene* sc, uint64_t npix, cudaStream_t stream);

@@ -380,18 +380,29 @@ int launch_trace_dn(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hit
 
 int launch_trace_multi(const AccelView* d_tab, uint32_t ntab, const float4* d_rays, const uint8_t* d_ray_scene,
                        lmgpu_hit* d_hits, const uint32_t* d_n, uint64_t max_n, bool anyhit, TraceConfig cfg,
-                       uint32_t* d_status, cudaStream_t stream)
+                       uint32_t* d_status, cudaStream_t stream, TraceProbe* probe)
 {
     if (max_n == 0) return LMGPU_OK;
-    const int grid_cap = anyhit ? grid_cap_of<true, false, true>() : grid_cap_of<false, false, true>();
+    if (probe && probe->mode != TraceProbe::kOff) probe->launches++;
+    const bool count = probe && probe->mode == TraceProbe::kProbeCount;
+    const bool timed = probe && probe->mode == TraceProbe::kProbeTime && probe->used + 2 <= probe->events.size();
+    if (probe && probe->mode == TraceProbe::kProbeTime && !timed) probe->overflow = true;
+    if (timed) LMGPU_CUDA_TRY(cudaEventRecord(probe->events[probe->used], stream));
+    const int grid_cap = count ? (anyhit ? grid_cap_of<true, true, true>() : grid_cap_of<false, true, true>())
+                               : (anyhit ? grid_cap_of<true, false, true>() : grid_cap_of<false, false, true>());
     if (grid_cap <= 0) return LMGPU_ERR_CUDA;
     // the ray count is read on the device: the full persistent grid, each
     // block taking its share of whatever count the launch finds
-    auto k = anyhit ? k_trace<true, false, true> : k_trace<false, false, true>;
+    auto k = count ? (anyhit ? k_trace<true, true, true> : k_trace<false, true, true>)
+                   : (anyhit ? k_trace<true, false, true> : k_trace<false, false, true>);
     k<<<(unsigned)grid_cap, kTraceThreads, 0, stream>>>(nullptr, nullptr, d_rays, d_hits, max_n, 0u, 0u, cfg.refill,
-                                                         cfg.postpone, d_status, nullptr, d_tab, ntab, d_ray_scene,
-                                                         d_n);
+                                                         cfg.postpone, d_status, count ? probe->d_counters : nullptr,
+                                                         d_tab, ntab, d_ray_scene, d_n);
     LMGPU_CUDA_TRY(cudaGetLastError());
+    if (timed) {
+        LMGPU_CUDA_TRY(cudaEventRecord(probe->events[probe->used + 1], stream));
+        probe->used += 2;
+    }
     return LMGPU_OK;
 }
 

@@ -155,6 +155,8 @@ def lib() -> ctypes.CDLL:
     L.lmgpu_scene_launch_count.argtypes = [vp, ctypes.POINTER(u64)]
     L.lmgpu_scene_set_trace_profile.argtypes = [vp, ctypes.c_int]
     L.lmgpu_scene_read_trace_profile.argtypes = [vp, ctypes.POINTER(TraceProfile)]
+    L.lmgpu_batch_set_trace_profile.argtypes = [vp, ctypes.c_int]
+    L.lmgpu_batch_read_trace_profile.argtypes = [vp, ctypes.POINTER(TraceProfile)]
     L.lmgpu_render_bdpt_device.argtypes = [vp, vp, vp, vp, vp]
     for name in ("lmgpu_accel_create", "lmgpu_accel_build", "lmgpu_accel_build_device", "lmgpu_accel_get_info",
                  "lmgpu_trace", "lmgpu_trace_device", "lmgpu_trace_stats_device", "lmgpu_accel_check",
@@ -173,7 +175,8 @@ def lib() -> ctypes.CDLL:
                  "lmgpu_render_vcm_device",
                  "lmgpu_accel_set_attributes", "lmgpu_surface", "lmgpu_surface_device",
                  "lmgpu_scene_set_environment", "lmgpu_scene_set_trace_profile",
-                 "lmgpu_scene_read_trace_profile"):
+                 "lmgpu_scene_read_trace_profile", "lmgpu_batch_set_trace_profile",
+                 "lmgpu_batch_read_trace_profile"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -605,6 +608,18 @@ class Batch:
         n = ctypes.c_uint64()
         _check(lib().lmgpu_batch_launch_count(self._h, ctypes.byref(n)))
         return n.value
+
+    def set_trace_profile(self, mode: int) -> None:
+        """Instruments the multi-scene traversal launches of later renders (as
+        Scene.set_trace_profile); while on, bounces are launched one by one
+        instead of through the captured graphs."""
+        _check(lib().lmgpu_batch_set_trace_profile(self._h, mode))
+
+    def read_trace_profile(self) -> dict:
+        """The record since the last read or mode change (waits for the device)."""
+        r = TraceProfile()
+        _check(lib().lmgpu_batch_read_trace_profile(self._h, ctypes.byref(r)))
+        return r.as_dict()
 
 
 class Guide:

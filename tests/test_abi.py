@@ -59,6 +59,8 @@ def test_null_arguments_rejected(gpu_lib):
     assert L.lmgpu_accel_get_info(None, None) == 1
     assert L.lmgpu_scene_set_trace_profile(None, 1) == 1
     assert L.lmgpu_scene_read_trace_profile(None, None) == 1
+    assert L.lmgpu_batch_set_trace_profile(None, 1) == 1
+    assert L.lmgpu_batch_read_trace_profile(None, None) == 1
     assert L.lmgpu_last_error()
 
 

@@ -1,5 +1,6 @@
-"""The traversal instrumentation of a scene's renders
-(lmgpu_scene_set_trace_profile / lmgpu_scene_read_trace_profile): the counting
+"""The traversal instrumentation of a scene's and a batch's renders
+(lmgpu_scene_set_trace_profile / lmgpu_scene_read_trace_profile and the
+lmgpu_batch_* pair): the counting
 mode runs the counting traversal, the timing mode the production one with
 events; neither changes the image, and the counts agree with the renders'
 own arithmetic."""
@@ -65,3 +66,43 @@ def test_trace_profile_rays_of_one_bounce(gpu_lib, golden_dir):
     sc.close()
     assert c["launches"] == 1
     assert c["rays"] == 32 * 32 * 8
+
+
+def test_batch_trace_profile(gpu_lib, golden_dir):
+    """The batch renderer's profile: bounces launched one by one instead of
+    through the captured graphs give the same films; with max_num_vertices 2
+    each sample traces exactly its camera ray, in one traversal launch."""
+    from lmgpu import scenes
+
+    cb, _ = ptscene.load_cornell(golden_dir)
+    cb["camera"].update(width=40, height=30)
+    grid = scenes.sphere_grid_scene(7, 0, 48, 27, grid=4)
+    scs = [gpu_lib.Scene(cb), gpu_lib.Scene(grid)]
+    b = gpu_lib.Batch(scs)
+    spp, seed = 8, 9
+    base = b.render_pt(spp, 9, seed, rr_depth=3)
+
+    b.set_trace_profile(gpu_lib.TRACE_PROFILE_COUNT)
+    counted = b.render_pt(spp, 9, seed, rr_depth=3)
+    c = b.read_trace_profile()
+    b.set_trace_profile(gpu_lib.TRACE_PROFILE_TIME)
+    timed = b.render_pt(spp, 9, seed, rr_depth=3)
+    t = b.read_trace_profile()
+    b.set_trace_profile(gpu_lib.TRACE_PROFILE_COUNT)
+    b.render_pt(spp, 2, seed, rr_depth=3)
+    one = b.read_trace_profile()
+    b.set_trace_profile(gpu_lib.TRACE_PROFILE_OFF)
+    after = b.render_pt(spp, 9, seed, rr_depth=3)
+    b.close()
+    for sc in scs:
+        sc.close()
+
+    for out in (counted, timed, after):
+        for (img, _), (ref, _) in zip(out, base):
+            _images_match(img, ref)
+    n = (40 * 30 + 48 * 27) * spp
+    assert c["rays"] >= n and 0 < c["hits"] <= c["rays"]
+    assert c["node_fetches"] >= c["rays"] and c["triangle_fetches"] >= c["hits"]
+    assert c["launches"] == t["launches"] == t["timed_launches"] > 0
+    assert t["device_ms"] > 0.0 and t["rays"] == 0
+    assert one["launches"] == 1 and one["rays"] == n
