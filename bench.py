@@ -916,6 +916,40 @@ def time_to_target(curve, target):
     return c / target, True
 
 
+def guided_trace_roofline(sc, guide, W: int, H: int, spp: int = 256) -> dict:
+    """Roofline of the guided renderer's traversal launches: renders of spp
+    samples per pixel with the trained network and no training, so that the
+    counted and the timed render trace the same rays.  The render's own
+    device time (CUDA events, L2 flushed) gives the traversal's share."""
+    import torch
+
+    d_img = torch.empty(H * W * 3, dtype=torch.float32, device="cuda")
+    d_var = torch.empty_like(d_img)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    st = torch.cuda.Stream()
+
+    def render(seed):
+        sc.render_pt_guided_device(guide, d_img.data_ptr(), d_var.data_ptr(), spp, -1, seed, train=False,
+                                   stream=st.cuda_stream)
+
+    with torch.cuda.stream(st):
+        for k in range(3):
+            render(500 + k)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.fill_(0.0)
+        e0.record(st)
+        render(1000)
+        e1.record(st)
+        torch.cuda.synchronize()
+        step_ms = e0.elapsed_time(e1)
+        roofline = render_trace_roofline(sc, render, step_ms, flush)
+    if roofline is not None:
+        roofline["kernel"] = "k_trace (the guided render's traversal launches)"
+        roofline["render"] = {"spp": spp, "ms": step_ms, "Msamples_per_s": W * H * spp / step_ms / 1e3,
+                              "training": False}
+    return roofline
+
+
 def run_guiding(args) -> None:
     """Learned path guiding vs plain PT on the narrow-gap room: the wall time
     each method needs to reach relMSE 1e-2 against a converged FP64 image.
@@ -994,6 +1028,7 @@ def run_guiding(args) -> None:
     launches = sc.launch_count() - l0
     clk = clocks.stop()
     mlp = mlp_timing(guide, box)
+    roofline = guided_trace_roofline(sc, guide, W, H)
 
     tg, tu, tp = guided["time_to_target_s"], unguided["time_to_target_s"], plain["time_to_target_s"]
     ratio = tg / tp
@@ -1017,7 +1052,7 @@ def run_guiding(args) -> None:
             "e2e": {"value": ratio, "unit": "x", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": W * H * 3 * 4 * 2,
                     "api": "lmgpu_render_pt / lmgpu_render_pt_guided (host films)"},
-            "gpu_launches": launches, "clocks": clk, "mlp": mlp}
+            "gpu_launches": launches, "clocks": clk, "mlp": mlp, "roofline": roofline}
     print(json.dumps(line), flush=True)
     for x in (guide, g0):
         x.close()
