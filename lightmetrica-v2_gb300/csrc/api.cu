@@ -120,7 +120,13 @@ int lmgpu_accel_create(lmgpu_accel** out)
         delete a;
         return LMGPU_ERR_CUDA;
     }
-    cudaMemset(a->status, 0, sizeof(uint32_t));
+    // the legacy stream's memset is not ordered with the library's
+    // non-blocking streams: finish it before the accel is used
+    if (cudaMemset(a->status, 0, sizeof(uint32_t)) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
+        set_error("lmgpu_accel_create: status initialisation failed");
+        lmgpu_accel_destroy(a);
+        return LMGPU_ERR_CUDA;
+    }
     *out = a;
     return LMGPU_OK;
 }

@@ -478,7 +478,8 @@ int lmgpu_batch_create(lmgpu_scene* const* scenes, uint32_t nviews, lmgpu_batch*
     if (cudaMallocHost((void**)&b->h_n, 2 * sizeof(uint32_t)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMemcpy(b->d_tab, tab.data(), sizeof(AccelView) * nviews, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(b->d_status, 0, sizeof(uint32_t)) != cudaSuccess) {
+        cudaMemset(b->d_status, 0, sizeof(uint32_t)) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess) {  // legacy-stream work done before the non-blocking stream runs
         set_error("lmgpu_batch_create: allocation or upload failed");
         return fail(LMGPU_ERR_CUDA);
     }

@@ -907,7 +907,8 @@ int lmgpu_guide_create(const float* box_lo_hi, uint32_t seed, lmgpu_guide** out)
         cudaMemcpy(g->params, p.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(g->grad, 0, bytes) != cudaSuccess || cudaMemset(g->m, 0, bytes) != cudaSuccess ||
         cudaMemset(g->v, 0, bytes) != cudaSuccess || cudaMemset(g->loss, 0, sizeof(float)) != cudaSuccess ||
-        cudaMemset(g->status, 0, sizeof(uint32_t)) != cudaSuccess) {
+        cudaMemset(g->status, 0, sizeof(uint32_t)) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess) {  // legacy-stream memsets done before use on other streams
         set_error("lmgpu_guide_create: allocation failed");
         lmgpu_guide_destroy(g);
         return LMGPU_ERR_CUDA;
@@ -946,6 +947,9 @@ int lmgpu_guide_set_params(lmgpu_guide* g, const float* in, uint64_t n)
         return LMGPU_ERR_INVALID;
     }
     LMGPU_CUDA_TRY(cudaMemcpy(g->params, in, sizeof(float) * n, cudaMemcpyHostToDevice));
+    // a pageable copy may return before its DMA ends; later steps may run on
+    // non-blocking streams
+    LMGPU_CUDA_TRY(cudaDeviceSynchronize());
     return LMGPU_OK;
 }
 
@@ -985,6 +989,8 @@ int lmgpu_guide_gradient(lmgpu_guide* g, const float* queries, const float* dirs
     LMGPU_CUDA_TRY(cudaMemcpy(grad, g->grad, sizeof(float) * kNumParams, cudaMemcpyDeviceToHost));
     if (loss) LMGPU_CUDA_TRY(cudaMemcpy(loss, g->loss, sizeof(float), cudaMemcpyDeviceToHost));
     LMGPU_CUDA_TRY(cudaMemset(g->grad, 0, sizeof(float) * kNumParams));
+    // finished before a later step on a non-blocking stream reads the gradient
+    LMGPU_CUDA_TRY(cudaDeviceSynchronize());
     return LMGPU_OK;
 }
 

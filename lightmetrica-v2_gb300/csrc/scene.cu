@@ -71,8 +71,11 @@ int set_probe(TraceProbe** slot, int mode, const char* fn)
         p->events.resize(TraceProbe::kMaxEvents, nullptr);
         for (auto& e : p->events) LMGPU_CUDA_TRY(cudaEventCreate(&e));
     }
+    // renders run on non-blocking streams, which the legacy stream's memset
+    // does not order: wait for it before any later counting launch
     LMGPU_CUDA_TRY(cudaDeviceSynchronize());
     LMGPU_CUDA_TRY(cudaMemset(p->d_counters, 0, 4 * sizeof(unsigned long long)));
+    LMGPU_CUDA_TRY(cudaDeviceSynchronize());
     p->mode = mode;
     p->used = 0;
     p->launches = 0;
@@ -101,6 +104,7 @@ int read_probe(TraceProbe* p, lmgpu_trace_profile* out)
     out->device_ms = ms;
     out->timed_launches = p->used / 2;
     LMGPU_CUDA_TRY(cudaMemset(p->d_counters, 0, sizeof(c)));
+    LMGPU_CUDA_TRY(cudaDeviceSynchronize());
     p->used = 0;
     p->launches = 0;
     p->overflow = false;
@@ -235,7 +239,8 @@ int build_lights(lmgpu_scene* sc, const float* tris, const int32_t* tri_prim, ui
                  o_off = put(tri_off.data(), 4 * tri_off.size()), o_tris = put(ltris.data(), 4 * ltris.size()),
                  o_cdf = put(cdf.data(), 4 * cdf.size()), o_ia = put(inv_area.data(), 4 * inv_area.size());
     if (cudaMalloc(&sc->light_buf, bytes) != cudaSuccess ||
-        cudaMemcpy(sc->light_buf, host.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaMemcpy(sc->light_buf, host.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess) {  // renders read it on non-blocking streams
         set_error("lmgpu_scene_create: light table upload failed");
         return LMGPU_ERR_CUDA;
     }
@@ -314,7 +319,10 @@ int lmgpu_scene_create(const float* tris, const int32_t* tri_prim, uint64_t ntri
     static_assert(sizeof(PrimGPU) == sizeof(lmgpu_prim), "primitive layout");
     if (cudaMemcpy(sc->tris, tris, sizeof(float) * 9 * ntri, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(sc->tri_prim, tri_prim, sizeof(int32_t) * ntri, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(sc->prims, prims, sizeof(PrimGPU) * nprims, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaMemcpy(sc->prims, prims, sizeof(PrimGPU) * nprims, cudaMemcpyHostToDevice) != cudaSuccess ||
+        // a copy from pageable memory may return before its DMA ends, and the
+        // build runs on the scene's non-blocking stream: wait for the copies
+        cudaDeviceSynchronize() != cudaSuccess) {
         set_error("lmgpu_scene_create: upload failed");
         return fail(LMGPU_ERR_CUDA);
     }
