@@ -651,6 +651,51 @@ VCM_WORKLOAD = {"workload": "vcm_cornell_256x256_4x4spp", "width": 256, "height"
                 "data": "synthetic (procedural Cornell box)"}
 
 
+# Algorithmic bytes of renderer::vcm's photon merges: a query's sort slot,
+# each eye-subpath vertex record it reads (32 B), each photon entry scanned in
+# its grid cells (16 B), and per photon within the radius the entry again and
+# its 80-byte prefix record.
+MERGE_QUERY_BYTES, EYE_VERTEX_BYTES, ENTRY_BYTES, MERGE_BYTES = 4, 32, 16, 96
+
+
+def vcm_merge_roofline(sc, render, step_ms: float, flush) -> dict:
+    """Roofline of renderer::vcm's dominant kernel, the photon merge: the
+    render of the first timed step's seed once with the counting merge
+    (queries, eye-vertex reads, scanned entries, merges) and once with CUDA
+    events around each production merge launch (the scene's trace
+    profile), L2 flushed before each."""
+    import lmgpu
+
+    sc.set_trace_profile(lmgpu.TRACE_PROFILE_COUNT)
+    flush.fill_(1.0)
+    render(1000)
+    cnt = sc.read_trace_profile()
+    sc.set_trace_profile(lmgpu.TRACE_PROFILE_TIME)
+    flush.fill_(2.0)
+    render(1000)
+    tim = sc.read_trace_profile()
+    sc.set_trace_profile(lmgpu.TRACE_PROFILE_OFF)
+    if (cnt["merge_queries"] == 0 or tim["merge_timed_launches"] == 0
+            or tim["merge_timed_launches"] != tim["merge_launches"]):
+        return None
+    nbytes = (cnt["merge_queries"] * MERGE_QUERY_BYTES + cnt["merge_eye_vertices"] * EYE_VERTEX_BYTES
+              + cnt["merge_entries"] * ENTRY_BYTES + cnt["merges"] * MERGE_BYTES)
+    achieved = nbytes / (tim["merge_ms"] * 1e-3) / 1e9
+    peak, peak_src = measured_peak()
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "peak_source": peak_src, "kernel": "k_vc_merge (the render's photon-merge launches)",
+            "launches_per_step": tim["merge_launches"], "queries_per_step": cnt["merge_queries"],
+            "eye_vertices_per_query": cnt["merge_eye_vertices"] / cnt["merge_queries"],
+            "entries_per_query": cnt["merge_entries"] / cnt["merge_queries"],
+            "merges_per_query": cnt["merges"] / cnt["merge_queries"], "bytes_per_query": nbytes / cnt["merge_queries"],
+            "merge_ms_per_step": tim["merge_ms"], "share_of_step": tim["merge_ms"] / step_ms,
+            "traversal_ms_per_step": tim["device_ms"],
+            "note": "algorithmic bytes = 4 B per query + 32 B per eye-vertex record + 16 B per scanned photon entry "
+                    "+ 96 B per photon within the radius (entry and prefix record), over the summed device time of "
+                    "the merge launches (CUDA events); the photon grid and records stay in L2, so the kernel is "
+                    "bound by latency, not by these bytes"}
+
+
 def run_vcm(args) -> None:
     """renderer::vcm (vertex connection and merging).  Metric Msamples/s: eye
     samples of all passes per second, photon subpaths and the grid build
@@ -691,6 +736,10 @@ def run_vcm(args) -> None:
     clk = clocks.stop()
     launches = sc.launch_count() - l0
     ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    with torch.cuda.stream(stream):
+        roofline = vcm_merge_roofline(
+            sc, lambda seed: sc.render_vcm_device(di.data_ptr(), dv.data_ptr(), stream.cuda_stream, seed=seed, **prm),
+            ms, flush)
     t0 = time.perf_counter()
     for k in range(args.steps):
         sc.render_vcm(seed=2000 + k, **prm)
@@ -704,7 +753,7 @@ def run_vcm(args) -> None:
                        "l2": "flushed before every timed step (256 MiB write, untimed)"},
             "e2e": {"value": samples / e2e_s / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": W * H * 3 * 4 * 2, "api": "lmgpu_render_vcm (host film)"},
-            "gpu_launches": launches, "clocks": clk}
+            "gpu_launches": launches, "clocks": clk, "roofline": roofline}
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import lmoracle

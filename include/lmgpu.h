@@ -250,6 +250,15 @@ typedef struct {
     uint64_t hits;             /* COUNT: rays that hit */
     double device_ms;          /* TIME: summed device time of the timed launches */
     uint64_t timed_launches;   /* TIME: launches inside device_ms (at most 4,096 between reads) */
+    /* The photon-merge launches of renderer::vcm (modes vcm and bdpm), that
+     * renderer's dominant kernel: */
+    uint64_t merge_launches;     /* merge launches since the last read */
+    uint64_t merge_queries;      /* COUNT: eye vertices that looked for photons */
+    uint64_t merge_eye_vertices; /* COUNT: eye-subpath vertex records those queries read */
+    uint64_t merge_entries;      /* COUNT: photon entries scanned in the queries' grid cells */
+    uint64_t merges;             /* COUNT: photons within the radius, evaluated */
+    double merge_ms;             /* TIME: summed device time of the merge launches */
+    uint64_t merge_timed_launches; /* TIME: launches inside merge_ms (at most 512 between reads) */
 } lmgpu_trace_profile;
 
 /* Selects the mode and clears the record. */

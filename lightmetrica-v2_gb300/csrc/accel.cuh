@@ -107,15 +107,24 @@ int launch_trace(const lmgpu_accel* a, const float4* d_rays, lmgpu_hit* d_hits, 
 //                node fetches, triangle fetches and hits into d_counters;
 //   kProbeTime:  the production kernel, with a CUDA event pair recorded
 //                around each launch (up to kMaxEvents / 2 launches).
+// The VCM renderer's photon-merge launches are instrumented the same way
+// (counters kMergeCounters.., their own event pairs).
 struct TraceProbe {
     static constexpr int kOff = 0, kProbeCount = 1, kProbeTime = 2;
     static constexpr size_t kMaxEvents = 8192;
+    static constexpr size_t kMaxMergeEvents = 1024;
+    // d_counters: [0, 4) traversal (rays, node fetches, triangle fetches,
+    // hits), [4, 8) merges (queries, eye-vertex reads, entries, merges)
+    static constexpr int kNumCounters = 8, kMergeCounters = 4;
     int mode = kOff;
-    unsigned long long* d_counters = nullptr;  // [4], device
+    unsigned long long* d_counters = nullptr;  // [kNumCounters], device
     std::vector<cudaEvent_t> events;
     size_t used = 0;           // events recorded since the last read
     uint64_t launches = 0;     // traversal launches since the last read
     bool overflow = false;     // more launches than event pairs
+    std::vector<cudaEvent_t> merge_events;
+    size_t merge_used = 0;
+    uint64_t merge_launches = 0;
 };
 
 // As launch_trace with the ray count read from d_n on the device (at most

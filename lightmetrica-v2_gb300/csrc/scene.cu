@@ -41,6 +41,8 @@ void free_probe(TraceProbe* p)
     if (!p) return;
     for (cudaEvent_t e : p->events)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : p->merge_events)
+        if (e) cudaEventDestroy(e);
     if (p->d_counters) cudaFree(p->d_counters);
     delete p;
 }
@@ -59,7 +61,8 @@ int set_probe(TraceProbe** slot, int mode, const char* fn)
     }
     if (!*slot) {
         *slot = new TraceProbe;
-        if (cudaMalloc((void**)&(*slot)->d_counters, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+        if (cudaMalloc((void**)&(*slot)->d_counters, TraceProbe::kNumCounters * sizeof(unsigned long long)) !=
+            cudaSuccess) {
             free_probe(*slot);
             *slot = nullptr;
             set_error(std::string(fn) + ": counter allocation failed");
@@ -70,16 +73,20 @@ int set_probe(TraceProbe** slot, int mode, const char* fn)
     if (mode == TraceProbe::kProbeTime && p->events.empty()) {
         p->events.resize(TraceProbe::kMaxEvents, nullptr);
         for (auto& e : p->events) LMGPU_CUDA_TRY(cudaEventCreate(&e));
+        p->merge_events.resize(TraceProbe::kMaxMergeEvents, nullptr);
+        for (auto& e : p->merge_events) LMGPU_CUDA_TRY(cudaEventCreate(&e));
     }
     // renders run on non-blocking streams, which the legacy stream's memset
     // does not order: wait for it before any later counting launch
     LMGPU_CUDA_TRY(cudaDeviceSynchronize());
-    LMGPU_CUDA_TRY(cudaMemset(p->d_counters, 0, 4 * sizeof(unsigned long long)));
+    LMGPU_CUDA_TRY(cudaMemset(p->d_counters, 0, TraceProbe::kNumCounters * sizeof(unsigned long long)));
     LMGPU_CUDA_TRY(cudaDeviceSynchronize());
     p->mode = mode;
     p->used = 0;
     p->launches = 0;
     p->overflow = false;
+    p->merge_used = 0;
+    p->merge_launches = 0;
     return LMGPU_OK;
 }
 
@@ -88,26 +95,40 @@ int read_probe(TraceProbe* p, lmgpu_trace_profile* out)
     *out = lmgpu_trace_profile{};
     if (!p) return LMGPU_OK;
     LMGPU_CUDA_TRY(cudaDeviceSynchronize());
-    unsigned long long c[4] = {0, 0, 0, 0};
+    unsigned long long c[TraceProbe::kNumCounters] = {};
     LMGPU_CUDA_TRY(cudaMemcpy(c, p->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
     out->launches = p->launches;
     out->rays = c[0];
     out->node_fetches = c[1];
     out->triangle_fetches = c[2];
     out->hits = c[3];
-    double ms = 0.0;
-    for (size_t i = 0; i + 1 < p->used; i += 2) {
-        float e = 0.0f;
-        LMGPU_CUDA_TRY(cudaEventElapsedTime(&e, p->events[i], p->events[i + 1]));
-        ms += e;
-    }
-    out->device_ms = ms;
+    const unsigned long long* m = c + TraceProbe::kMergeCounters;
+    out->merge_launches = p->merge_launches;
+    out->merge_queries = m[0];
+    out->merge_eye_vertices = m[1];
+    out->merge_entries = m[2];
+    out->merges = m[3];
+    auto summed = [](const std::vector<cudaEvent_t>& ev, size_t used, double* ms) -> cudaError_t {
+        *ms = 0.0;
+        for (size_t i = 0; i + 1 < used; i += 2) {
+            float e = 0.0f;
+            const cudaError_t rc = cudaEventElapsedTime(&e, ev[i], ev[i + 1]);
+            if (rc != cudaSuccess) return rc;
+            *ms += e;
+        }
+        return cudaSuccess;
+    };
+    LMGPU_CUDA_TRY(summed(p->events, p->used, &out->device_ms));
     out->timed_launches = p->used / 2;
+    LMGPU_CUDA_TRY(summed(p->merge_events, p->merge_used, &out->merge_ms));
+    out->merge_timed_launches = p->merge_used / 2;
     LMGPU_CUDA_TRY(cudaMemset(p->d_counters, 0, sizeof(c)));
     LMGPU_CUDA_TRY(cudaDeviceSynchronize());
     p->used = 0;
     p->launches = 0;
     p->overflow = false;
+    p->merge_used = 0;
+    p->merge_launches = 0;
     return LMGPU_OK;
 }
 

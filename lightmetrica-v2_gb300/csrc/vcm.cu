@@ -718,13 +718,18 @@ __device__ __forceinline__ bool merge_eval(const Ctx& C, const Pass& X, const Me
 constexpr int kMergeQueue = 64;
 // 8 blocks per SM (64 registers, a few spills): the scan phase waits on
 // memory, and twice the warps of the unbounded 96-register build hide more of it.
+// STATS: the counting instantiation of the trace profile, which also adds
+// queries, eye-vertex reads, scanned entries and evaluated merges into
+// stats[0..3].
+template <bool STATS>
 __global__ void __launch_bounds__(kVcThreads, 8) k_vc_merge(Ctx C, Pass X, Subs E, uint32_t n, uint32_t nq,
                                                          const uint32_t* __restrict__ order,
                                                          const uint32_t* __restrict__ start,
                                                          const float4* __restrict__ entries,
                                                          const float4* __restrict__ srec,
                                                          const uint32_t* __restrict__ own_pix, float* __restrict__ own,
-                                                         double* __restrict__ film_x, double* __restrict__ film_x_sq)
+                                                         double* __restrict__ film_x, double* __restrict__ film_x_sq,
+                                                         unsigned long long* __restrict__ stats)
 {
     __shared__ MergeQuery sq[kVcThreads];
     __shared__ float sacc[kVcThreads][3];
@@ -804,6 +809,7 @@ __global__ void __launch_bounds__(kVcThreads, 8) k_vc_merge(Ctx C, Pass X, Subs 
         }
     }
     const int ncell = valid ? ext[0] * ext[1] * ext[2] : 0;
+    uint32_t n_entries = 0, n_merges = 0;
     int cell = 0, cx = 0, cy = 0, cz = 0;
     uint32_t e = 0, e1 = 0;
     int qn = 0;  // queued entries (warp-uniform)
@@ -832,6 +838,10 @@ __global__ void __launch_bounds__(kVcThreads, 8) k_vc_merge(Ctx C, Pass X, Subs 
                       np <= C.max_path;
                 he = e;
                 e++;
+                if (STATS) {
+                    n_entries++;
+                    n_merges += has ? 1u : 0u;
+                }
             }
         }
         const bool more = valid && (e < e1 || cell < ncell);
@@ -862,6 +872,15 @@ __global__ void __launch_bounds__(kVcThreads, 8) k_vc_merge(Ctx C, Pass X, Subs 
         if (!any_more) break;
     }
     __syncwarp();
+    if (STATS) {
+        // every lane of the warp is here: one atomic per counter and warp
+        unsigned long long v[4] = {valid ? 1ull : 0ull, valid ? (unsigned long long)t : 0ull, n_entries, n_merges};
+        for (int k = 0; k < 4; k++) {
+            unsigned long long x = v[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) atomicAdd(&stats[k], x);
+        }
+    }
     if (!valid) return;
     const float acc[3] = {sacc[threadIdx.x][0], sacc[threadIdx.x][1], sacc[threadIdx.x][2]};
     if (acc[0] == 0.0f && acc[1] == 0.0f && acc[2] == 0.0f) return;
@@ -1010,7 +1029,8 @@ int render_vcm(lmgpu_scene* sc, const lmgpu_vcm_params* prm, float* d_image, flo
     // raise the stack limit once, up front
     {
         size_t need = 0;
-        const void* fns[] = {(const void*)k_vc_connect, (const void*)k_vc_merge, (const void*)k_vc_prep};
+        const void* fns[] = {(const void*)k_vc_connect, (const void*)k_vc_merge<false>, (const void*)k_vc_merge<true>,
+                             (const void*)k_vc_prep};
         for (const void* f : fns) {
             cudaFuncAttributes fa{};
             LMGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, f));
@@ -1141,10 +1161,22 @@ int render_vcm(lmgpu_scene* sc, const lmgpu_vcm_params* prm, float* d_image, flo
                 size_t sb = (size_t)V.sort_tmp_cap;
                 LMGPU_CUDA_TRY(cub::DeviceRadixSort::SortPairs(V.sort_tmp, sb, kin, kout, vin, vout, (int)nq, 0, 32,
                                                                stream));
-                k_vc_merge<<<blocks(nq, kVcThreads), kVcThreads, 0, stream>>>(C, X, eE, n, nq, vout, start, V.entries,
-                                                                             V.srec, V.own_pix, V.own, sc->film_x,
-                                                                             sc->film_x_sq);
+                // the trace profile: counting instantiation, or events around the launch
+                TraceProbe* pr = sc->probe && sc->probe->mode != TraceProbe::kOff ? sc->probe : nullptr;
+                const bool count = pr && pr->mode == TraceProbe::kProbeCount;
+                const bool timed = pr && pr->mode == TraceProbe::kProbeTime &&
+                                   pr->merge_used + 2 <= pr->merge_events.size();
+                if (pr) pr->merge_launches++;
+                if (timed) LMGPU_CUDA_TRY(cudaEventRecord(pr->merge_events[pr->merge_used], stream));
+                auto merge = count ? k_vc_merge<true> : k_vc_merge<false>;
+                merge<<<blocks(nq, kVcThreads), kVcThreads, 0, stream>>>(
+                    C, X, eE, n, nq, vout, start, V.entries, V.srec, V.own_pix, V.own, sc->film_x, sc->film_x_sq,
+                    count ? pr->d_counters + TraceProbe::kMergeCounters : nullptr);
                 LMGPU_CUDA_TRY(cudaGetLastError());
+                if (timed) {
+                    LMGPU_CUDA_TRY(cudaEventRecord(pr->merge_events[pr->merge_used + 1], stream));
+                    pr->merge_used += 2;
+                }
                 sc->launches += 2;
             }
             k_vc_flush<<<blocks(n, 256), 256, 0, stream>>>(n, V.own_pix, V.own, sc->film, sc->film_sq);

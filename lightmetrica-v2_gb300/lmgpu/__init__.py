@@ -51,7 +51,8 @@ class AccelInfo(ctypes.Structure):
 
 
 class TraceProfile(ctypes.Structure):
-    """lmgpu_trace_profile: a scene's traversal launches since the last read."""
+    """lmgpu_trace_profile: a scene's (or batch's) traversal launches since the
+    last read, and renderer::vcm's photon-merge launches."""
     _fields_ = [
         ("launches", ctypes.c_uint64),
         ("rays", ctypes.c_uint64),
@@ -60,6 +61,13 @@ class TraceProfile(ctypes.Structure):
         ("hits", ctypes.c_uint64),
         ("device_ms", ctypes.c_double),
         ("timed_launches", ctypes.c_uint64),
+        ("merge_launches", ctypes.c_uint64),
+        ("merge_queries", ctypes.c_uint64),
+        ("merge_eye_vertices", ctypes.c_uint64),
+        ("merge_entries", ctypes.c_uint64),
+        ("merges", ctypes.c_uint64),
+        ("merge_ms", ctypes.c_double),
+        ("merge_timed_launches", ctypes.c_uint64),
     ]
 
     def as_dict(self) -> dict:

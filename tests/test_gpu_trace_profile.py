@@ -106,3 +106,40 @@ def test_batch_trace_profile(gpu_lib, golden_dir):
     assert c["launches"] == t["launches"] == t["timed_launches"] > 0
     assert t["device_ms"] > 0.0 and t["rays"] == 0
     assert one["launches"] == 1 and one["rays"] == n
+
+
+@pytest.mark.parametrize("mode", ["vcm", "bdpt"])
+def test_vcm_merge_profile(gpu_lib, golden_dir, mode):
+    """renderer::vcm's photon merges in the profile: the counting merge and
+    the timed one leave the image as it was (up to the order of the float
+    sums of the merges), the counts hold together, and mode bdpt merges
+    nothing."""
+    scene, _ = ptscene.load_scene(golden_dir, "materials_ptmis")
+    scene["camera"].update(width=48, height=32)
+    kw = dict(max_num_vertices=7, num_iteration_pass=4, num_photon_trace_samples=4096,
+              num_eye_trace_samples=48 * 32 * 4, initial_radius=0.04, alpha=0.75, mode=mode, seed=5)
+    sc = gpu_lib.Scene(scene)
+    img0, _ = sc.render_vcm(**kw)
+    sc.set_trace_profile(gpu_lib.TRACE_PROFILE_COUNT)
+    img1, _ = sc.render_vcm(**kw)
+    c = sc.read_trace_profile()
+    sc.set_trace_profile(gpu_lib.TRACE_PROFILE_TIME)
+    img2, _ = sc.render_vcm(**kw)
+    t = sc.read_trace_profile()
+    sc.set_trace_profile(gpu_lib.TRACE_PROFILE_OFF)
+    sc.close()
+
+    for im in (img1, img2):
+        assert np.allclose(im, img0, rtol=1e-4, atol=1e-6)
+    assert c["launches"] == t["launches"] > 0 and c["rays"] > 0
+    if mode == "bdpt":
+        assert c["merge_launches"] == t["merge_launches"] == 0
+        assert c["merge_queries"] == 0 and t["merge_ms"] == 0.0
+        return
+    assert c["merge_launches"] == t["merge_launches"] == t["merge_timed_launches"] > 0
+    assert c["merge_queries"] > 0
+    # a query at eye vertex t reads the t vertices of its eye subpath, t >= 2
+    assert c["merge_eye_vertices"] >= 2 * c["merge_queries"]
+    assert 0 < c["merges"] <= c["merge_entries"]
+    assert c["merge_ms"] == 0.0 and c["merge_timed_launches"] == 0
+    assert t["merge_ms"] > 0.0 and t["merge_queries"] == 0
