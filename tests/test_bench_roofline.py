@@ -1,7 +1,8 @@
-"""The roofline arithmetic of bench.py's render lines, on the CPU with a fake
-scene whose trace profile returns fixed records: the counted render gives
-the algorithmic bytes, the timed render the device time, and a record that
-timed fewer launches than it ran gives no roofline."""
+"""bench.py's measurement arithmetic on the CPU.  The render lines' roofline,
+with a fake scene whose trace profile returns fixed records: the counted
+render gives the algorithmic bytes, the timed render the device time, and a
+record that timed fewer launches than it ran gives no roofline.  The guiding
+line's time to a relMSE target and its FP64 film accumulation."""
 import os
 import sys
 
@@ -73,3 +74,35 @@ def test_vcm_merge_roofline_formula():
     assert r["traversal_ms_per_step"] == pytest.approx(0.1)
     no_merges = FakeScene({}, {"merge_launches": 0})
     assert bench.vcm_merge_roofline(no_merges, no_merges.render, 1.0, FakeFlush()) is None
+
+
+def _curve(c, times):
+    # checkpoints (seconds, spp, raw relMSE, relMSE less the reference's noise) on relMSE = c / t
+    return [(t, int(100 * t), c / t + 0.001, c / t) for t in times]
+
+
+def test_time_to_target_interpolates_and_extrapolates():
+    """On relMSE = c / t (the Monte Carlo rate) both forms give c / target."""
+    c, target = 0.5, 1e-2
+    t, extrap = bench.time_to_target(_curve(c, [1, 2, 4, 8, 16, 32, 64, 128]), target)
+    assert not extrap and t == pytest.approx(c / target)
+    t, extrap = bench.time_to_target(_curve(c, [1, 2, 4, 8]), target)
+    assert extrap and t == pytest.approx(c / target)
+    t, extrap = bench.time_to_target(_curve(1e-3, [1, 2]), target)
+    assert not extrap and t == 1
+    assert bench.time_to_target([], target) == (None, True)
+
+
+def test_progressive_accumulation_is_sample_weighted():
+    """Films of 8 and 24 spp: the mean weights them by spp, and the variance
+    of the mean (each render's variance of its own mean v / spp) is v / 32."""
+    import numpy as np
+
+    acc = bench.Progressive((2, 2, 3))
+    v = 0.64
+    acc.add(np.full((2, 2, 3), 1.0, np.float32), np.full((2, 2, 3), v / 8, np.float32), 8, 0.5)
+    acc.add(np.full((2, 2, 3), 3.0, np.float32), np.full((2, 2, 3), v / 24, np.float32), 24, 1.5)
+    assert acc.spp == 32 and acc.seconds == 2.0
+    assert np.allclose(acc.mean(), (8 * 1.0 + 24 * 3.0) / 32)
+    assert np.allclose(acc.variance(), v / 32, rtol=1e-6)
+    assert bench.relmse_image(acc.mean(), acc.mean()) == 0.0
