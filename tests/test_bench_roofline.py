@@ -106,3 +106,12 @@ def test_progressive_accumulation_is_sample_weighted():
     assert np.allclose(acc.mean(), (8 * 1.0 + 24 * 3.0) / 32)
     assert np.allclose(acc.variance(), v / 32, rtol=1e-6)
     assert bench.relmse_image(acc.mean(), acc.mean()) == 0.0
+
+
+def test_committed_traffic_summary_is_read():
+    """The headline's roofline.traffic and L2 figures come from the committed
+    ncu summary of the closest-hit kernel (profiles/trace_closest_traffic.json)."""
+    t = bench.traffic_per_launch()
+    assert t is not None and 1e9 < t < 2e10
+    l2 = bench.l2_figures()
+    assert l2 is not None and l2
