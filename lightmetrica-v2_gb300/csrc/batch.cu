@@ -196,15 +196,16 @@ __global__ void k_bt_flush(const BatchView* __restrict__ views, uint32_t nviews,
     }
 }
 
+// inv_spp: 1 / spp from the host (FP64 multiplication instead of division).
 __global__ void k_bt_finalize(const double* __restrict__ film, const double* __restrict__ film_sq, uint64_t n3,
-                              double spp, float* __restrict__ image, float* __restrict__ variance)
+                              double inv_spp, float* __restrict__ image, float* __restrict__ variance)
 {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n3) return;
-    const double mean = film[i] / spp;
+    const double mean = film[i] * inv_spp;
     image[i] = (float)mean;
     if (variance) {
-        const double v = (film_sq[i] - film[i] * mean) / (spp * spp);
+        const double v = (film_sq[i] - film[i] * mean) * (inv_spp * inv_spp);
         variance[i] = (float)(v > 0.0 ? v : 0.0);
     }
 }
@@ -406,8 +407,8 @@ int batch_render(lmgpu_batch* b, const lmgpu_batch_params* prm, float* d_image, 
         b->launches++;
     }
     const uint64_t n3 = 3 * b->total_pix;
-    k_bt_finalize<<<(unsigned)((n3 + 255) / 256), 256, 0, s>>>(b->film, b->film_sq, n3, (double)prm->spp, d_image,
-                                                               d_variance);
+    k_bt_finalize<<<(unsigned)((n3 + 255) / 256), 256, 0, s>>>(b->film, b->film_sq, n3, 1.0 / (double)prm->spp,
+                                                               d_image, d_variance);
     LMGPU_CUDA_TRY(cudaGetLastError());
     b->launches++;
     uint32_t st = 0;

@@ -162,18 +162,21 @@ int ensure_queues(lmgpu_scene* sc, uint64_t n)
 // spp * (pixels - 1) i.i.d. samples of the other strata that splat there:
 // Var(I) = [spp Var(X_own) + n_x Var(X_x)] / spp^2, each Var(X) estimated as
 // sum(x^2) / n - (sum(x) / n)^2.
+// The divisors arrive as reciprocals computed once on the host: FP64
+// division is a long instruction sequence on this part, FP64 multiplication
+// one instruction (and exact for power-of-two sample counts).
 __global__ void k_film_finalize(const double* __restrict__ film, const double* __restrict__ film_sq,
                                 const double* __restrict__ film_x, const double* __restrict__ film_x_sq, uint32_t n3,
-                                double spp, double n_x, float* __restrict__ image, float* __restrict__ variance)
+                                double inv_spp, double inv_n_x, float* __restrict__ image, float* __restrict__ variance)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n3) return;
     const double so = film[i], sx = film_x[i];
-    image[i] = (float)((so + sx) / spp);
+    image[i] = (float)((so + sx) * inv_spp);
     if (variance) {
-        double v = film_sq[i] - so * so / spp;
-        if (n_x > 0.0) v += film_x_sq[i] - sx * sx / n_x;
-        v /= spp * spp;
+        double v = film_sq[i] - so * so * inv_spp;
+        if (inv_n_x > 0.0) v += film_x_sq[i] - sx * sx * inv_n_x;
+        v *= inv_spp * inv_spp;
         variance[i] = (float)(v > 0.0 ? v : 0.0);
     }
 }
@@ -195,7 +198,8 @@ int finalize_film_nx(lmgpu_scene* sc, double spp, double n_x, float* d_image, fl
     const uint64_t npix = (uint64_t)sc->cam.width * sc->cam.height;
     const uint32_t n3 = (uint32_t)(3 * npix);
     k_film_finalize<<<(n3 + 255) / 256, 256, 0, stream>>>(sc->film, sc->film_sq, sc->film_x, sc->film_x_sq, n3,
-                                                         spp, n_x, d_image, d_variance);
+                                                         1.0 / spp, n_x > 0.0 ? 1.0 / n_x : 0.0, d_image,
+                                                         d_variance);
     LMGPU_CUDA_TRY(cudaGetLastError());
     sc->launches++;
     return LMGPU_OK;
