@@ -716,13 +716,15 @@ __device__ __forceinline__ bool merge_eval(const Ctx& C, const Pass& X, const Me
 // its query's shared accumulator.  So the evaluation runs on full warps
 // however the candidates are spread over the lanes.
 constexpr int kMergeQueue = 64;
-// 8 blocks per SM (64 registers, a few spills): the scan phase waits on
-// memory, and twice the warps of the unbounded 96-register build hide more of it.
+// 6 blocks per SM (80 registers, some spills): the scan phase waits on
+// memory, so occupancy beats spill-free code.  Measured on the Cornell-box
+// workload: 8 blocks (64 registers) 23.45, 6 blocks 23.62, 4 blocks (106
+// registers, no spills) 21.6 M eye samples/s.
 // STATS: the counting instantiation of the trace profile, which also adds
 // queries, eye-vertex reads, scanned entries and evaluated merges into
 // stats[0..3].
 template <bool STATS>
-__global__ void __launch_bounds__(kVcThreads, 8) k_vc_merge(Ctx C, Pass X, Subs E, uint32_t n, uint32_t nq,
+__global__ void __launch_bounds__(kVcThreads, 6) k_vc_merge(Ctx C, Pass X, Subs E, uint32_t n, uint32_t nq,
                                                          const uint32_t* __restrict__ order,
                                                          const uint32_t* __restrict__ start,
                                                          const float4* __restrict__ entries,
