@@ -125,7 +125,9 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p
         s.thr = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pixel));
         // pinhole: pdf of the direction = importance, |cos| = 1 (degenerate end)
         s.id = make_uint4((uint32_t)p, (uint32_t)(p >> 32), 1u, __float_as_uint(NEE ? importance(cam, d) : 0.0f));
-        state[i] = s;
+        // renderer::pt passes no state array: its first shading launch
+        // rebuilds this state from the path index (first_state)
+        if (state) state[i] = s;
         own[3 * (size_t)i] = 0.0f;
         own[3 * (size_t)i + 1] = 0.0f;
         own[3 * (size_t)i + 2] = 0.0f;
@@ -145,6 +147,19 @@ __global__ void __launch_bounds__(kShadeThreads) k_pt_generate(Ctx C, uint64_t p
         }
     }
     if (NEE) append_nee(has_nee, v, L, c, nee_pix, i, nrays, nrec, npath, ncount);
+}
+
+// The state k_pt_generate gives path p0 + i of renderer::pt, whose first
+// shading launch reads no state array (its queue is still in path order):
+// saves writing and reading 32 bytes per path.
+__device__ __forceinline__ PathState first_state(const CameraGPU& cam, uint64_t p0, uint32_t i)
+{
+    const uint64_t p = p0 + i;
+    const uint32_t npix = (uint32_t)cam.width * (uint32_t)cam.height;
+    PathState s;
+    s.thr = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float((uint32_t)(p % npix)));
+    s.id = make_uint4((uint32_t)p, (uint32_t)(p >> 32), 1u, __float_as_uint(0.0f));
+    return s;
 }
 
 template <int MODE>
@@ -173,7 +188,8 @@ __global__ void __launch_bounds__(kShadeThreads, 4) k_pt_shade(Ctx C, const floa
     uint32_t pixel = 0, path = 0;
     if (i < n) {
         const lmgpu_hit h = hits[i];
-        const PathState s = state[i];
+        // state == NULL: renderer::pt's first bounce (first_state)
+        const PathState s = (NEE || state) ? state[i] : first_state(C.cam, p0, i);
         pixel = __float_as_uint(s.thr.w);
         const uint64_t p = (uint64_t)s.id.x | ((uint64_t)s.id.y << 32);
         path = (uint32_t)(p - p0);
@@ -370,7 +386,9 @@ int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float
         const uint32_t n_wave = (uint32_t)((total - p0) < kWave ? (total - p0) : kWave);
         const unsigned gblocks = (n_wave + kShadeThreads - 1) / kShadeThreads;
         LMGPU_CUDA_TRY(cudaMemsetAsync(cnt, 0, 4 * sizeof(uint32_t), stream));
-        gen<<<gblocks, kShadeThreads, 0, stream>>>(C, p0, n_wave, prm->seed, sc->q_ray[0], sc->q_state[0], cnt,
+        // renderer::pt's first bounce rebuilds its states (first_state)
+        PathState* const first = nee ? sc->q_state[0] : nullptr;
+        gen<<<gblocks, kShadeThreads, 0, stream>>>(C, p0, n_wave, prm->seed, sc->q_ray[0], first, cnt,
                                                    sc->q_own, sc->q_nray, sc->q_nrec, sc->q_npath, cnt + 2);
         LMGPU_CUDA_TRY(cudaGetLastError());
         sc->launches++;
@@ -391,10 +409,10 @@ int render_pt(lmgpu_scene* sc, const lmgpu_pt_params* prm, float* d_image, float
             if (rc) return rc;
             LMGPU_CUDA_TRY(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(uint32_t), stream));
             LMGPU_CUDA_TRY(cudaMemsetAsync(cnt + 2, 0, sizeof(uint32_t), stream));
-            shade<<<gblocks, kShadeThreads, 0, stream>>>(C, sc->q_ray[cur], sc->q_state[cur], sc->q_hit, cnt + cur,
-                                                         p0, prm->seed, sc->q_own, sc->q_ray[1 - cur],
-                                                         sc->q_state[1 - cur], cnt + (1 - cur), sc->q_nray,
-                                                         sc->q_nrec, sc->q_npath, cnt + 2);
+            shade<<<gblocks, kShadeThreads, 0, stream>>>(C, sc->q_ray[cur], b == 0 ? first : sc->q_state[cur],
+                                                         sc->q_hit, cnt + cur, p0, prm->seed, sc->q_own,
+                                                         sc->q_ray[1 - cur], sc->q_state[1 - cur], cnt + (1 - cur),
+                                                         sc->q_nray, sc->q_nrec, sc->q_npath, cnt + 2);
             LMGPU_CUDA_TRY(cudaGetLastError());
             sc->launches += 2;  // trace + shade
             cur = 1 - cur;
